@@ -1,0 +1,354 @@
+#!/usr/bin/env python3
+"""Frames/s of supereight2's per-frame dense-mapping path (track + integrate + raycast).
+
+Workload (config "tsdf640"): 640x480 pinhole (fx = fy = 525, cx = 319.5, cy = 239.5), a
+single-resolution TSDF map of 1024^3 voxels at 1 cm, a seeded synthetic room trajectory with
+random-walk velocity (0.02 m, 1 deg per frame). One step is one frame: 3-level ICP {10, 5, 4}
+against the previous raycast, integration at the tracked pose, raycast at that pose.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0). ``value``: frames/s with the depth images resident in HBM, the
+device time of the K steps measured with CUDA events on the launching stream and L2 flushed
+(256 MiB write) between steps outside the timed pairs. ``e2e``: the same through the public API
+with each frame's depth copied from pinned host memory and the pose read back, host clock.
+``--impl reference`` times the CPU oracle (the restatement of the reference's OpenMP code) on
+all host cores. Under torchrun every rank runs an independent replica (the path does not
+shard); the value is the sum of frames over the max time across ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MAP_DIM = 10.24
+MAP_RES = 0.01
+CONFIG = "tsdf640"
+METRIC = "frames/s 640x480 TSDF integrate+raycast+ICP"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_data(n_frames, device):
+    from supereight2_gb300 import synthetic as syn
+    return syn.dataset(CONFIG, n_frames, device=device)
+
+
+# ----------------------------------------------------------------------------- GPU arm --
+
+def run_ours(args, ws, rank, local):
+    import torch
+    import supereight2_gb300 as se
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n_frames = 1 + args.warmup + 2 * args.steps
+    t0 = time.perf_counter()
+    sensor_spec, scene, poses, frames = make_data(n_frames, dev)
+    gen_s = time.perf_counter() - t0
+    sensor = se.PinholeCamera.from_spec(sensor_spec)
+    W, H = sensor.width, sensor.height
+
+    m = se.Map(MAP_DIM, MAP_RES, max_blocks=args.max_blocks, storage=args.storage)
+    integ = se.MapIntegrator(m)
+    tracker = se.Tracker(m, sensor, se.TrackerConfig())
+    depth_dev = [torch.from_numpy(f).to(dev) for f in frames]
+    pts = torch.zeros((H, W, 3), dtype=torch.float32, device=dev)
+    nrm = torch.zeros_like(pts)
+    scale = torch.zeros((H, W), dtype=torch.int8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    T = poses[0].astype(np.float32).copy()
+    integ.integrateDepth(0, depth_dev[0], sensor, T)
+    se.raycast_volume(m, sensor, T, pts, nrm, scale)
+    m.check()
+
+    def step(i, depth):
+        nonlocal T
+        tracker.track(depth, T, pts, nrm)          # T updated in place (synchronous, as in se::)
+        integ.integrateDepth(i, depth, sensor, T)
+        se.raycast_volume(m, sensor, T, pts, nrm, scale)
+
+    for i in range(1, 1 + args.warmup):
+        step(i, depth_dev[i])
+    torch.cuda.synchronize()
+    m.check()
+
+    # ---- timed: device-resident inputs, CUDA events per step, L2 flushed between steps
+    L = se.library()
+    L.se_gpu_profiling_read(0, None, None, 1)
+    L.se_gpu_profiling_enable(1)
+    n_prof = L.se_gpu_profiling_count()
+    names = [L.se_gpu_profiling_name(i).decode() for i in range(n_prof)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    upd_stats = []
+    clocks = Clocks(local)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    wall0 = time.perf_counter()
+    first = 1 + args.warmup
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        step(first + k, depth_dev[first + k])
+        ev[k][1].record(stream)
+        upd_stats.append(m.integrate_stats())
+    torch.cuda.synchronize()
+    wall1 = time.perf_counter()
+    if ws > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    L.se_gpu_profiling_enable(0)
+    import ctypes as C
+    tot = (C.c_double * n_prof)()
+    cnt = (C.c_int64 * n_prof)()
+    L.se_gpu_profiling_read(n_prof, tot, cnt, 1)
+    kernel_ms = {names[i]: float(tot[i]) for i in range(n_prof)}
+    kernel_launches = {names[i]: int(cnt[i]) for i in range(n_prof)}
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_ms = float(sum(step_ms))
+    m.check()
+
+    # ---- e2e: pinned host depth copied in every step, pose read back, host clock
+    host_frames = [torch.from_numpy(f).pin_memory() for f in frames]
+    depth_buf = torch.empty((H, W), dtype=torch.float32, device=dev)
+    first_e2e = first + args.steps
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for k in range(args.steps):
+        depth_buf.copy_(host_frames[first_e2e + k], non_blocking=True)
+        step(first_e2e + k, depth_buf)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - e0
+    m.check()
+
+    # ---- max over ranks
+    times = torch.tensor([dev_ms, e2e_s, wall1 - wall0], dtype=torch.float64, device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    dev_ms_max, e2e_max, wall_max = [float(v) for v in times.cpu()]
+
+    # ---- roofline of the dominant kernel
+    hbm_peak, peak_kind = _peaks()
+    timed = {k: v for k, v in kernel_ms.items() if kernel_launches.get(k, 0)}
+    dom = max(timed, key=timed.get)
+    S_v = 8 if args.storage == "f32" else 4
+    algo = None
+    if dom == "update":
+        b = [s["n_updated_voxels"] * 2 * S_v + s["n_listed_blocks"] * 8 + W * H * 4 for s in upd_stats]
+        algo = float(np.mean(b))
+    elif dom == "icp_iter":
+        npx = sum((W >> l) * (H >> l) * it for l, it in enumerate((10, 5, 4)))
+        algo = npx * 48.0 / 19.0
+    elif dom == "raycast":
+        algo = W * H * 25.0
+    avg_launch_ms = kernel_ms[dom] / max(kernel_launches[dom], 1)
+    achieved = (algo / (avg_launch_ms * 1e-3) / 1e9) if algo else None
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": (achieved / hbm_peak) if achieved else None,
+                "traffic": None, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": algo, "avg_launch_us": avg_launch_ms * 1e3}
+
+    value = ws * args.steps / (dev_ms_max * 1e-3)
+    launches = int(sum(kernel_launches.values()))
+    upd_voxels = float(np.mean([s["n_updated_voxels"] for s in upd_stats]))
+    out = {
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded room: 6x5x3 m box, 12 spheres, 8 boxes; depth noise "
+                "N(0,(0.0015 z^2)^2), 2% dropout)",
+        "config": {"workload": "tsdf640: 640x480 pinhole, TSDF single-res 1024^3 @ 1 cm, "
+                               "ICP 3 levels {10,5,4}, integrate + raycast per frame",
+                   "map_res_m": MAP_RES, "map_voxels": 1024, "storage": args.storage,
+                   "parallelism": f"replicas x{ws}", "l2": "flushed (256 MiB write) between steps",
+                   "api": "synchronous track() per step, as se::Tracker::track"},
+        "roofline": roofline,
+        "e2e": {"value": ws * args.steps / e2e_max, "unit": "frames/s",
+                "h2d_bytes_per_step": W * H * 4, "d2h_bytes_per_step": 80},
+        "gpu_launches": launches,
+        "kernel_ms": kernel_ms, "kernel_launches": kernel_launches,
+        "voxels_per_s": upd_voxels * args.steps / (dev_ms_max * 1e-3) if dev_ms_max else None,
+        "updated_voxels_per_frame": upd_voxels,
+        "num_blocks": m.num_blocks(),
+        "wall_s_timed": wall_max, "gen_s": gen_s,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(frames, poses, sensor_spec, args.cpu_frames)
+    return out
+
+
+# --------------------------------------------------------------------- CPU oracle arm --
+
+def _oracle_pipeline(frames, poses, spec, n_steps, budget_s=None):
+    """Run the oracle (OpenMP) pipeline on frames 0..n_steps; return per-step seconds."""
+    from oracle import pyoracle as o
+    o.set_num_threads(os.cpu_count() or 1)
+    m = o.OracleMap(MAP_DIM, MAP_RES)
+    s = o.pinhole(spec.width, spec.height, spec.fx, spec.fy, spec.cx, spec.cy,
+                  spec.near_plane, spec.far_plane)
+    cfg = o.tracker_config()
+    T = poses[0].astype(np.float32)
+    m.integrate_depth(frames[0], s, T, 0)
+    pts, nrm, _ = m.raycast(s, T)
+    times = []
+    t_start = time.perf_counter()
+    for i in range(1, 1 + n_steps):
+        t0 = time.perf_counter()
+        _, T, _ = o.track(s, cfg, frames[i], T, pts, nrm)
+        m.integrate_depth(frames[i], s, T, i)
+        pts, nrm, _ = m.raycast(s, T)
+        times.append(time.perf_counter() - t0)
+        if budget_s is not None and time.perf_counter() - t_start > budget_s:
+            break
+    return times
+
+
+def cpu_baseline(frames, poses, spec, n):
+    times = _oracle_pipeline(frames, poses, spec, n)
+    return {"value": len(times) / sum(times), "unit": "frames/s", "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": f"frames 1..{len(times)} of the same trajectory (track+integrate+raycast), "
+                      f"after integrating frame 0; {sum(times):.1f} s of CPU work"}
+
+
+def run_reference(args, ws, rank, local):
+    if rank != 0:
+        return None
+    n_frames = 1 + args.warmup + args.steps
+    sensor_spec, scene, poses, frames = make_data(n_frames, "cpu")
+    from oracle import pyoracle as o
+    o.set_num_threads(os.cpu_count() or 1)
+    # warm-up frames are folded into the run (the map must grow the same way); the timed sample
+    # is bounded to ~120 s of CPU work
+    times = _oracle_pipeline(frames, poses, sensor_spec, args.warmup + args.steps,
+                             budget_s=args.reference_budget_s)
+    timed = times[args.warmup:] if len(times) > args.warmup else times
+    value = len(timed) / sum(timed)
+    return {
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws,
+        "steps": len(timed), "warmup": args.warmup, "ms_per_step": 1e3 * sum(timed) / len(timed),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded room)", "impl": "reference",
+        "config": {"workload": "tsdf640: 640x480 pinhole, TSDF single-res 1024^3 @ 1 cm, "
+                               "ICP 3 levels {10,5,4}, integrate + raycast per frame",
+                   "parallelism": "OpenMP, all host threads"},
+        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": os.cpu_count(),
+                         "kind": "port",
+                         "sample": f"{len(timed)} timed frames after {args.warmup} warm-up "
+                                   f"frames (bounded to {args.reference_budget_s:.0f} s)"},
+        "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--storage", choices=["f32", "f16"], default="f32")
+    ap.add_argument("--max-blocks", type=int, default=1 << 19)
+    ap.add_argument("--cpu-frames", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--reference-budget-s", type=float, default=120.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    ws, rank, local = _dist()
+    if args.impl == "reference":
+        # the CPU arm runs on rank 0 only; other ranks exit without work
+        out = run_reference(args, ws, rank, local)
+        if rank == 0 and out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    if ws > 1:
+        import torch
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, ws, rank, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,201 @@
+/*
+ * se_gpu.h — C ABI of the GB300 (sm_103a) implementation of supereight2's per-frame
+ * dense-mapping hot path: TSDF block allocation, voxel update, raycast and ICP tracking.
+ *
+ * Conventions
+ *   - Matrices are row-major float[16] (4x4 homogeneous transforms), e.g. T_WC maps camera
+ *     coordinates to world coordinates. Eigen's Isometry3f::matrix() is column-major: transpose
+ *     it (or map it with Eigen::RowMajor) when crossing this boundary.
+ *   - Images are device pointers, row-major, pixel (x, y) at index x + y * width, exactly the
+ *     memory layout of se::Image<T> (include/se/image/image.hpp:19-70). 3-vector images are
+ *     packed xyz float triplets (the layout of se::Image<Eigen::Vector3f>).
+ *   - Every call that takes a stream is stream-ordered and asynchronous unless stated. Calls on
+ *     one map are not re-entrant: issue them on one stream (the reference's calls on one map are
+ *     not re-entrant either).
+ *   - Errors: every function returns se_gpu_status. Device-side failures (block pool full, hash
+ *     probe limit) are latched in the map and reported by se_gpu_map_check(), which
+ *     synchronises the stream. The reference asserts or silently drops in these cases.
+ *
+ * Pinhole projection convention (the reference delegates it to the un-vendored srl_projection
+ * module): rz = 1/z, u = fx*(x*rz) + cx, v = fy*(y*rz) + cy; a projection is Successful iff
+ * z > 0 and (u, v) lies in [-0.5, w-0.5) x [-0.5, h-0.5); round_pixel is int(p + 0.5).
+ * backProject(u, v) = ((u - cx) * (1/fx), (v - cy) * (1/fy), 1).
+ */
+#ifndef SE_GPU_H
+#define SE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SE_GPU_API __attribute__((visibility("default")))
+#else
+#define SE_GPU_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SE_GPU_OK = 0,
+    SE_GPU_ERR_BAD_ARG = 1,        /* invalid argument (null pointer, size mismatch, ...) */
+    SE_GPU_ERR_CUDA = 2,           /* a CUDA runtime call failed; see se_gpu_last_error() */
+    SE_GPU_ERR_POOL_FULL = 3,      /* the block pool ran out; some blocks were not allocated */
+    SE_GPU_ERR_HASH_PROBE_LIMIT = 4, /* the block hash hit its probe limit */
+    SE_GPU_ERR_NOT_SUPPORTED = 5,  /* the map type does not support this call */
+    SE_GPU_ERR_NO_DEVICE = 6       /* no CUDA device of compute capability 10.3 */
+} se_gpu_status;
+
+typedef enum { SE_GPU_FIELD_TSDF = 0, SE_GPU_FIELD_OCCUPANCY = 1 } se_gpu_field;
+typedef enum { SE_GPU_RES_SINGLE = 0, SE_GPU_RES_MULTI = 1 } se_gpu_res;
+typedef enum {
+    SE_GPU_STORAGE_F32 = 0, /* float tsdf + float weight per voxel (the reference layout) */
+    SE_GPU_STORAGE_F16 = 1  /* half tsdf + uint16 weight per voxel; FP32 arithmetic */
+} se_gpu_storage;
+
+/* se::Map<Data<TSDF>, Res::Single, 8>::Config + FieldData<TSDF>::Config
+ * (include/se/map/map.hpp:41-57, include/se/map/data_field.hpp:76-84) plus pool sizing. */
+typedef struct {
+    float dim[3];      /* metres; the octree side is pow2ceil(max(dim)/res) voxels, >= 16 */
+    float res;         /* metres per voxel */
+    float T_MW[16];    /* world-to-map transform; set has_T_MW = 0 for translation(dim/2) */
+    int has_T_MW;
+    int field;         /* se_gpu_field; only SE_GPU_FIELD_TSDF in this library */
+    int res_type;      /* se_gpu_res; only SE_GPU_RES_SINGLE in this library */
+    int storage;       /* se_gpu_storage */
+    float truncation_boundary_factor; /* reference default 8 */
+    float max_weight;  /* reference default 100; must be an integer <= 65535 */
+    int64_t max_blocks; /* block pool capacity (8^3-voxel blocks) */
+} se_gpu_map_config;
+
+/* se::PinholeCamera::Config (include/se/sensor/sensor.hpp:29-57, pinhole_camera.hpp). */
+typedef struct {
+    int width;
+    int height;
+    float fx, fy, cx, cy;
+    float near_plane;
+    float far_plane;
+} se_gpu_pinhole;
+
+/* se::TrackerConfig (include/se/tracker/tracker.hpp:22-33). */
+typedef struct {
+    int num_levels;    /* at most 3 */
+    int iterations[3]; /* finest level first; reference default {10, 5, 4} */
+    float dist_threshold;   /* 0.1 */
+    float normal_threshold; /* 0.8 */
+    float track_threshold;  /* 0.15 */
+    float icp_threshold;    /* 1e-5 */
+} se_gpu_tracker_config;
+
+/* Per-call counters of the last integrate_depth (read with se_gpu_map_integrate_stats). */
+typedef struct {
+    int64_t n_new_blocks;      /* blocks allocated by the carver */
+    int64_t n_listed_blocks;   /* new + previously allocated blocks in the frustum */
+    int64_t n_updated_voxels;  /* voxels whose field update returned true */
+    int64_t n_valid_pixels;    /* pixels in [near, far + band/2] */
+} se_gpu_integrate_stats;
+
+typedef struct se_gpu_map se_gpu_map;
+typedef struct se_gpu_tracker se_gpu_tracker;
+
+/* Last error message of this thread (CUDA error string or argument check). */
+SE_GPU_API const char* se_gpu_last_error(void);
+SE_GPU_API const char* se_gpu_status_string(se_gpu_status status);
+/* ABI version, bumped on any incompatible change. */
+SE_GPU_API int se_gpu_abi_version(void);
+
+/* ------------------------------------------------------------------------------ maps -- */
+
+/* Replaces se::Map ctor (include/se/map/impl/map_impl.hpp:37-55) and the Octree ctor
+ * (include/se/map/octree/impl/octree_impl.hpp:14-19). Allocates the block pool and hash on the
+ * current CUDA device. */
+SE_GPU_API se_gpu_status se_gpu_map_create(const se_gpu_map_config* config, se_gpu_map** map);
+SE_GPU_API se_gpu_status se_gpu_map_destroy(se_gpu_map* map);
+/* Octree side in voxels (Octree::getSize()) and map side in metres (Map::getDim()). */
+SE_GPU_API se_gpu_status se_gpu_map_size(const se_gpu_map* map, int* size, float* dim_m);
+/* Synchronise the map's last stream and return any latched device-side error, then clear it. */
+SE_GPU_API se_gpu_status se_gpu_map_check(se_gpu_map* map);
+
+/* Replaces se::MapIntegrator<TSDFMap<Res::Single>>::integrateDepth(timestamp,
+ * Measurements{Measurement{depth, sensor, T_WC}}) (include/se/integrator/map_integrator.hpp:78-81,
+ * impl/map_integrator_impl.hpp:52-84): RaycastCarver allocation (allocator/impl/
+ * raycast_carver_impl.hpp:56-128) then the single-res TSDF update (updater/impl/
+ * singleres_tsdf_updater_impl.hpp:14-132). depth_dev: width*height floats on the device. */
+SE_GPU_API se_gpu_status se_gpu_integrate_depth(se_gpu_map* map, const float* depth_dev,
+                                     const se_gpu_pinhole* sensor, const float T_WC[16],
+                                     int timestamp, void* stream);
+/* Counters of the last integrate_depth; synchronises the stream. */
+SE_GPU_API se_gpu_status se_gpu_map_integrate_stats(se_gpu_map* map, se_gpu_integrate_stats* stats);
+
+/* Replaces se::raycaster::raycast_volume(map, sensor, T_WS, points_W, normals_W, scale)
+ * (include/se/map/raycaster.hpp:56-64, impl/raycaster_impl.hpp:456-627). Output device
+ * images: pts_W and nrm_W are width*height*3 floats, scale is width*height int8 (may be NULL). */
+SE_GPU_API se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinhole* sensor,
+                             const float T_WS[16], float* pts_W_dev, float* nrm_W_dev,
+                             int8_t* scale_dev, void* stream);
+
+/* Block download for checking and checkpointing. Writes up to capacity blocks:
+ * keys (Morton code << 5 | 3), coords (3 ints: the block's minimum voxel), tsdf and weight
+ * (512 floats per block, x + 8y + 64z), timestamps. Host pointers, any may be NULL.
+ * Synchronous. *count receives the number of allocated blocks. */
+SE_GPU_API se_gpu_status se_gpu_map_download_blocks(const se_gpu_map* map, int64_t capacity,
+                                         uint64_t* keys, int32_t* coords, float* tsdf,
+                                         float* weight, int32_t* timestamps, int64_t* count);
+/* Block upload (checkpoint restore, test set-up): allocates the blocks with the given keys
+ * (Morton code << 5 | 3, as written by se_gpu_map_download_blocks) if they are not allocated,
+ * then overwrites their 512 voxels from tsdf / weight (host, 512 floats per block; weights are
+ * rounded to integers). Synchronous. */
+SE_GPU_API se_gpu_status se_gpu_map_upload_blocks(se_gpu_map* map, int64_t n, const uint64_t* keys,
+                                       const float* tsdf, const float* weight);
+/* Replaces Map::getFieldInterp(point_W) and Map::getFieldGrad(point_W)
+ * (include/se/map/impl/map_impl.hpp:154-172,236-262) for a batch of n device points
+ * (3 floats each). valid_dev (n ints) receives 1 where the reference returns a value. */
+SE_GPU_API se_gpu_status se_gpu_map_field_interp(const se_gpu_map* map, int64_t n, const float* points_W_dev,
+                                      float* values_dev, int* valid_dev, void* stream);
+SE_GPU_API se_gpu_status se_gpu_map_field_grad(const se_gpu_map* map, int64_t n, const float* points_W_dev,
+                                    float* grads_dev, int* valid_dev, void* stream);
+/* Allocated-block AABB in voxels (Octree::aabb(), inclusive). Synchronous; returns
+ * SE_GPU_OK with *empty = 1 when no block is allocated. */
+SE_GPU_API se_gpu_status se_gpu_map_aabb(const se_gpu_map* map, int32_t mn[3], int32_t mx[3], int* empty);
+
+/* --------------------------------------------------------------------------- tracker -- */
+
+/* Replaces se::Tracker ctor (include/se/tracker/tracker.hpp:42-48): device buffers for the
+ * depth pyramid, per-level point clouds and normals and the ICP partial sums. */
+SE_GPU_API se_gpu_status se_gpu_tracker_create(const se_gpu_pinhole* sensor,
+                                    const se_gpu_tracker_config* config,
+                                    se_gpu_tracker** tracker);
+SE_GPU_API se_gpu_status se_gpu_tracker_destroy(se_gpu_tracker* tracker);
+
+/* Replaces se::Tracker::track(depth, T_WS, surface_point_cloud_W, surface_normals_W)
+ * (include/se/tracker/impl/tracker_impl.hpp:30-116): 3-level projective point-to-plane ICP
+ * against the raycast (ref_pts/ref_nrm, width*height*3 device floats) taken at the input T_WS.
+ * T_WS is read and written on the host; *accepted receives the checkPoseKernel result (a
+ * rejected track leaves T_WS unchanged, as in the reference). Synchronous. */
+SE_GPU_API se_gpu_status se_gpu_track(se_gpu_tracker* tracker, const float* depth_dev,
+                           const float* ref_pts_W_dev, const float* ref_nrm_W_dev,
+                           float T_WS[16], int* accepted, void* stream);
+/* Final 32-float reduction of the last track (icp.cpp:45-204 layout: [sum e^2, J^T e (6),
+ * upper J^T J (21), inliers, distance rejects, normal rejects, other]) and the iterations run
+ * per level. Synchronous. */
+SE_GPU_API se_gpu_status se_gpu_tracker_last_reduction(se_gpu_tracker* tracker, float reduction[32],
+                                            int iterations_run[3]);
+
+/* ------------------------------------------------------------------------- profiling -- */
+
+/* Per-kernel device time: when enabled, each public call records CUDA events on its stream
+ * around every kernel it launches. se_gpu_profiling_read synchronises on the recorded events
+ * and returns, for the first n kernels in se_gpu_profiling_name order, the accumulated
+ * milliseconds and launch counts (reset != 0 clears them). Off by default. */
+SE_GPU_API se_gpu_status se_gpu_profiling_enable(int enable);
+SE_GPU_API se_gpu_status se_gpu_profiling_read(int n, double* total_ms, int64_t* launches,
+                                               int reset);
+SE_GPU_API const char* se_gpu_profiling_name(int index);
+SE_GPU_API int se_gpu_profiling_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SE_GPU_H */

@@ -1,0 +1,230 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Only the tests, the smoke check and the benchmark's CPU-baseline leg import this module. It
+wraps ``libse_oracle.so`` (built by ``oracle/build.py``), the CPU restatement of the
+supereight2 hot path that the GPU product is checked against.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+class Pinhole(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("fx", C.c_float), ("fy", C.c_float),
+                ("cx", C.c_float), ("cy", C.c_float), ("near_plane", C.c_float),
+                ("far_plane", C.c_float)]
+
+
+class TrackerConfig(C.Structure):
+    _fields_ = [("num_levels", C.c_int), ("iterations", C.c_int * 3),
+                ("dist_threshold", C.c_float), ("normal_threshold", C.c_float),
+                ("track_threshold", C.c_float), ("icp_threshold", C.c_float)]
+
+
+class IntegrateStats(C.Structure):
+    _fields_ = [("n_valid_pixels", C.c_longlong), ("n_new_blocks", C.c_longlong),
+                ("n_frustum_blocks", C.c_longlong), ("n_updated_voxels", C.c_longlong)]
+
+
+class TrackStats(C.Structure):
+    _fields_ = [("converged_iterations", C.c_int * 3), ("accepted", C.c_int),
+                ("reduction", C.c_float * 32)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+        i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        i8p = np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS")
+        vp = C.c_void_p
+        sig = {
+            "so_set_num_threads": (None, [C.c_int]),
+            "so_get_num_threads": (C.c_int, []),
+            "so_map_create": (vp, [f32p, C.c_float, C.c_float, C.c_float, vp]),
+            "so_map_destroy": (None, [vp]),
+            "so_map_size": (C.c_int, [vp]),
+            "so_map_dim": (C.c_float, [vp]),
+            "so_integrate_depth": (None, [vp, f32p, C.POINTER(Pinhole), f32p, C.c_int,
+                                          C.POINTER(IntegrateStats)]),
+            "so_raycast_volume": (None, [vp, C.POINTER(Pinhole), f32p, f32p, f32p, i8p]),
+            "so_track": (C.c_int, [C.POINTER(Pinhole), C.POINTER(TrackerConfig), f32p, f32p,
+                                   f32p, f32p, C.POINTER(TrackStats)]),
+            "so_map_num_blocks": (C.c_longlong, [vp]),
+            "so_map_blocks": (None, [vp, vp, vp, vp, vp, vp]),
+            "so_map_aabb": (C.c_int, [vp, i32p, i32p]),
+            "so_map_set_block": (None, [vp, i32p, f32p, f32p]),
+            "so_map_get_data": (C.c_int, [vp, f32p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+            "so_map_get_field_interp": (C.c_int, [vp, f32p, C.POINTER(C.c_float)]),
+            "so_map_get_field_grad": (C.c_int, [vp, f32p, f32p]),
+            "so_first_block_tmin": (C.c_int, [vp, f32p, f32p, C.c_float, C.c_float,
+                                              C.POINTER(C.c_float)]),
+            "so_expand": (C.c_uint64, [C.c_uint64]),
+            "so_compact": (C.c_uint64, [C.c_uint64]),
+            "so_encode_code": (C.c_uint64, [C.c_int32, C.c_int32, C.c_int32]),
+            "so_decode_code": (None, [C.c_uint64, i32p]),
+            "so_encode_key": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
+                                        C.POINTER(C.c_uint64)]),
+            "so_decode_key": (None, [C.c_uint64, i32p, C.POINTER(C.c_uint64)]),
+            "so_code_to_child_idx": (C.c_uint64, [C.c_uint64, C.c_uint64]),
+            "so_parent_key": (C.c_uint64, [C.c_uint64]),
+            "so_key_at_scale": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)]),
+            "so_code_at_scale": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)]),
+            "so_block_key": (C.c_uint64, [C.c_uint64, C.c_uint64]),
+            "so_block_code": (C.c_uint64, [C.c_uint64, C.c_uint64]),
+            "so_is_child": (C.c_int, [C.c_uint64, C.c_uint64]),
+            "so_is_siblings": (C.c_int, [C.c_uint64, C.c_uint64]),
+            "so_unique_keys": (C.c_longlong, [u64p, C.c_longlong, u64p]),
+            "so_unique_codes": (C.c_longlong, [u64p, C.c_longlong, u64p]),
+            "so_unique_allocation": (C.c_longlong, [u64p, C.c_longlong, C.c_uint64, u64p]),
+            "so_unique_at_scale": (C.c_longlong, [u64p, C.c_longlong, C.c_uint64, u64p]),
+            "so_se3_exp": (None, [f32p, f32p]),
+            "so_half_sample_robust": (None, [f32p, C.c_int, C.c_int, C.c_float, C.c_int, f32p]),
+            "so_depth_to_point_cloud": (None, [f32p, C.POINTER(Pinhole), f32p]),
+            "so_point_cloud_to_normal": (None, [f32p, C.c_int, C.c_int, C.c_int, f32p]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def set_num_threads(n: int) -> None:
+    lib().so_set_num_threads(int(n))
+
+
+def num_threads() -> int:
+    return lib().so_get_num_threads()
+
+
+def pinhole(width, height, fx, fy, cx, cy, near_plane, far_plane) -> Pinhole:
+    return Pinhole(int(width), int(height), float(fx), float(fy), float(cx), float(cy),
+                   float(near_plane), float(far_plane))
+
+
+def _m16(T):
+    return np.ascontiguousarray(np.asarray(T, dtype=np.float32).reshape(16))
+
+
+class OracleMap:
+    """se::TSDFMap<Res::Single> restated on the CPU."""
+
+    def __init__(self, dim, res, truncation_boundary_factor=8.0, max_weight=100.0, T_MW=None):
+        d = np.ascontiguousarray(np.broadcast_to(np.asarray(dim, np.float32), (3,)))
+        self._tmw = None if T_MW is None else _m16(T_MW)
+        self.h = lib().so_map_create(d, float(res), float(truncation_boundary_factor),
+                                     float(max_weight),
+                                     None if self._tmw is None else self._tmw.ctypes.data)
+        self.res = float(res)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().so_map_destroy(self.h)
+            self.h = None
+
+    @property
+    def size(self) -> int:
+        return lib().so_map_size(self.h)
+
+    @property
+    def dim(self) -> float:
+        return lib().so_map_dim(self.h)
+
+    def integrate_depth(self, depth, sensor: Pinhole, T_WC, timestamp=0) -> IntegrateStats:
+        st = IntegrateStats()
+        depth = np.ascontiguousarray(depth, dtype=np.float32)
+        lib().so_integrate_depth(self.h, depth, C.byref(sensor), _m16(T_WC), int(timestamp),
+                                 C.byref(st))
+        return st
+
+    def raycast(self, sensor: Pinhole, T_WS):
+        n = sensor.width * sensor.height
+        pts = np.zeros((sensor.height, sensor.width, 3), np.float32)
+        nrm = np.zeros((sensor.height, sensor.width, 3), np.float32)
+        scale = np.zeros((sensor.height, sensor.width), np.int8)
+        lib().so_raycast_volume(self.h, C.byref(sensor), _m16(T_WS), pts.reshape(n * 3),
+                                nrm.reshape(n * 3), scale.reshape(n))
+        return pts, nrm, scale
+
+    def num_blocks(self) -> int:
+        return int(lib().so_map_num_blocks(self.h))
+
+    def blocks(self):
+        """Return (keys u64[N], coords i32[N,3], tsdf f32[N,512], weight f32[N,512], ts i32[N])."""
+        n = self.num_blocks()
+        keys = np.zeros(n, np.uint64)
+        coords = np.zeros((n, 3), np.int32)
+        tsdf = np.zeros((n, 512), np.float32)
+        weight = np.zeros((n, 512), np.float32)
+        ts = np.zeros(n, np.int32)
+        if n:
+            lib().so_map_blocks(self.h, keys.ctypes.data, coords.ctypes.data, tsdf.ctypes.data,
+                                weight.ctypes.data, ts.ctypes.data)
+        return keys, coords, tsdf, weight, ts
+
+    def aabb(self):
+        mn = np.zeros(3, np.int32)
+        mx = np.zeros(3, np.int32)
+        ok = lib().so_map_aabb(self.h, mn, mx)
+        return (mn, mx) if ok else None
+
+    def set_block(self, voxel_coord, tsdf512, weight512):
+        lib().so_map_set_block(self.h, np.asarray(voxel_coord, np.int32),
+                               np.ascontiguousarray(np.broadcast_to(np.float32(tsdf512), (512,))),
+                               np.ascontiguousarray(np.broadcast_to(np.float32(weight512), (512,))))
+
+    def get_data(self, p_W):
+        t, w = C.c_float(), C.c_float()
+        lib().so_map_get_data(self.h, np.asarray(p_W, np.float32), C.byref(t), C.byref(w))
+        return t.value, w.value
+
+    def field_interp(self, p_W):
+        v = C.c_float()
+        ok = lib().so_map_get_field_interp(self.h, np.asarray(p_W, np.float32), C.byref(v))
+        return v.value if ok else None
+
+    def field_grad(self, p_W):
+        g = np.zeros(3, np.float32)
+        ok = lib().so_map_get_field_grad(self.h, np.asarray(p_W, np.float32), g)
+        return g if ok else None
+
+    def first_block_tmin(self, origin, direction, t_near, t_far):
+        t = C.c_float()
+        found = lib().so_first_block_tmin(self.h, np.asarray(origin, np.float32),
+                                          np.asarray(direction, np.float32), float(t_near),
+                                          float(t_far), C.byref(t))
+        return bool(found), t.value
+
+
+def tracker_config(iterations=(10, 5, 4), dist_threshold=0.1, normal_threshold=0.8,
+                   track_threshold=0.15, icp_threshold=1e-5) -> TrackerConfig:
+    it = (C.c_int * 3)(*([int(i) for i in iterations] + [0] * (3 - len(iterations))))
+    return TrackerConfig(len(iterations), it, dist_threshold, normal_threshold,
+                         track_threshold, icp_threshold)
+
+
+def track(sensor: Pinhole, config: TrackerConfig, depth, T_WS, ref_pts, ref_nrm):
+    """Tracker::track(depth, T_WS, pts, nrm); returns (accepted, T_WS_new, stats)."""
+    T = _m16(T_WS).copy()
+    st = TrackStats()
+    acc = lib().so_track(C.byref(sensor), C.byref(config),
+                         np.ascontiguousarray(depth, np.float32).reshape(-1), T,
+                         np.ascontiguousarray(ref_pts, np.float32).reshape(-1),
+                         np.ascontiguousarray(ref_nrm, np.float32).reshape(-1), C.byref(st))
+    return bool(acc), T.reshape(4, 4), st
+
+
+def se3_exp(twist):
+    T = np.zeros(16, np.float32)
+    lib().so_se3_exp(np.asarray(twist, np.float32), T)
+    return T.reshape(4, 4)

@@ -1,0 +1,1698 @@
+/*
+ * se_oracle.cpp — CPU oracle for the supereight2 dense-mapping hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker the GPU product is compared against and the timed CPU
+ * baseline. It is never linked into or called by the product library.
+ *
+ * It restates the reference algorithms (cited per function, paths relative to the supereight2
+ * source tree) with the same loop structure and the same float arithmetic. Where the reference's
+ * float operation order is decided by Eigen expression templates (unavailable here), this file
+ * fixes one order and the GPU kernels use the same one:
+ *   dot3(a, b)      = (a0*b0 + a1*b1) + a2*b2
+ *   (M*v)_i         = (M_i0*v0 + M_i1*v1) + M_i2*v2
+ *   (T*p)_i         = ((R_i0*p0 + R_i1*p1) + R_i2*p2) + t_i
+ *   norm(v)         = sqrtf(dot3(v, v));  normalized(v) = v / norm(v) component-wise
+ *   compose(A, B)   = (R_A*R_B, R_A*t_B + t_A)
+ * Build with -ffp-contract=off so that no multiply-add is fused.
+ *
+ * Pinhole projection lives in the un-vendored srl_projection module. The convention used here
+ * (and in the GPU kernels) is the okvis-style pinhole model: rz = 1/z, u = fx*(x*rz) + cx,
+ * v = fy*(y*rz) + cy, Successful iff z > 0 and (u, v) in [-0.5, w-0.5) x [-0.5, h-0.5), so that
+ * round_pixel() always lands inside the image. backProject(u, v) = ((u-cx)*(1/fx),
+ * (v-cy)*(1/fy), 1).
+ */
+#include "se_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <set>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+/* ---------------------------------------------------------------- small float algebra -- */
+
+struct V3 {
+    float x, y, z;
+};
+static inline V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+static inline V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+static inline V3 operator*(float s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+static inline V3 operator/(V3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
+static inline float dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+static inline float norm(V3 a) { return std::sqrt(dot(a, a)); }
+static inline V3 normalized(V3 a)
+{
+    const float sq = dot(a, a);
+    if (sq > 0.0f) {
+        const float n = std::sqrt(sq);
+        return v3(a.x / n, a.y / n, a.z / n);
+    }
+    return a;
+}
+static inline V3 cross(V3 a, V3 b)
+{
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+static inline bool is_zero(V3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
+
+/* Rigid or affine transform, R row-major. */
+struct Tf {
+    float R[3][3];
+    float t[3];
+};
+
+static inline V3 rot(const Tf& T, V3 v)
+{
+    return v3((T.R[0][0] * v.x + T.R[0][1] * v.y) + T.R[0][2] * v.z,
+              (T.R[1][0] * v.x + T.R[1][1] * v.y) + T.R[1][2] * v.z,
+              (T.R[2][0] * v.x + T.R[2][1] * v.y) + T.R[2][2] * v.z);
+}
+static inline V3 apply(const Tf& T, V3 v)
+{
+    const V3 r = rot(T, v);
+    return v3(r.x + T.t[0], r.y + T.t[1], r.z + T.t[2]);
+}
+static inline Tf compose(const Tf& A, const Tf& B)
+{
+    Tf C;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) {
+            C.R[i][j] = (A.R[i][0] * B.R[0][j] + A.R[i][1] * B.R[1][j]) + A.R[i][2] * B.R[2][j];
+        }
+        C.t[i] = ((A.R[i][0] * B.t[0] + A.R[i][1] * B.t[1]) + A.R[i][2] * B.t[2]) + A.t[i];
+    }
+    return C;
+}
+/* Isometry inverse: (R^T, -(R^T t)). */
+static inline Tf inverse_iso(const Tf& A)
+{
+    Tf B;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            B.R[i][j] = A.R[j][i];
+    for (int i = 0; i < 3; ++i) {
+        B.t[i] = -((B.R[i][0] * A.t[0] + B.R[i][1] * A.t[1]) + B.R[i][2] * A.t[2]);
+    }
+    return B;
+}
+static inline Tf tf_from16(const float* m)
+{
+    Tf T;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            T.R[i][j] = m[4 * i + j];
+        T.t[i] = m[4 * i + 3];
+    }
+    return T;
+}
+static inline void tf_to16(const Tf& T, float* m)
+{
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            m[4 * i + j] = T.R[i][j];
+        m[4 * i + 3] = T.t[i];
+    }
+    m[12] = m[13] = m[14] = 0.0f;
+    m[15] = 1.0f;
+}
+static inline Tf tf_identity()
+{
+    Tf T;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            T.R[i][j] = (i == j) ? 1.0f : 0.0f;
+        T.t[i] = 0.0f;
+    }
+    return T;
+}
+
+/* ------------------------------------------------------------------------ Morton keys -- */
+/* include/se/map/utils/key_util.hpp:19-58, impl/key_util_impl.hpp:44-436 */
+
+constexpr uint64_t kCodeMask[] = {
+    0x1ffffffffffffffULL, 0x1fffffffffffff8ULL, 0x1ffffffffffffc0ULL, 0x1fffffffffffe00ULL,
+    0x1fffffffffff000ULL, 0x1ffffffffff8000ULL, 0x1fffffffffc0000ULL, 0x1ffffffffe00000ULL,
+    0x1ffffffff000000ULL, 0x1fffffff8000000ULL, 0x1ffffffc0000000ULL, 0x1fffffe00000000ULL,
+    0x1fffff000000000ULL, 0x1ffff8000000000ULL, 0x1fffc0000000000ULL, 0x1ffe00000000000ULL,
+    0x1ff000000000000ULL, 0x1f8000000000000ULL, 0x1c0000000000000ULL};
+constexpr uint64_t kScaleMask = 0x1f;
+constexpr int kScaleOffset = 5;
+
+/* Spread the low 19 bits of value so that bit i lands on bit 3i. */
+static inline uint64_t morton_expand(uint64_t v)
+{
+    uint64_t x = v & 0x7ffff;
+    x = (x | x << 32) & 0x1f00000000ffffULL;
+    x = (x | x << 16) & 0x1f0000ff0000ffULL;
+    x = (x | x << 8) & 0x100f00f00f00f00fULL;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ULL;
+    x = (x | x << 2) & 0x1249249249249249ULL;
+    return x;
+}
+/* Inverse of morton_expand. */
+static inline uint64_t morton_compact(uint64_t v)
+{
+    uint64_t x = v & 0x49249249249249ULL;
+    x = (x | x >> 2) & 0x10c30c30c30c30c3ULL;
+    x = (x | x >> 4) & 0x100f00f00f00f00fULL;
+    x = (x | x >> 8) & 0x1f0000ff0000ffULL;
+    x = (x | x >> 16) & 0x1f00000000ffffULL;
+    x = (x | x >> 32) & 0x1fffffULL;
+    return x;
+}
+static inline uint64_t encode_code(int x, int y, int z)
+{
+    return morton_expand((uint64_t) x) | (morton_expand((uint64_t) y) << 1)
+        | (morton_expand((uint64_t) z) << 2);
+}
+static inline uint64_t encode_key(int x, int y, int z, uint64_t scale)
+{
+    return ((encode_code(x, y, z) & kCodeMask[scale]) << kScaleOffset) | scale;
+}
+static inline uint64_t key_to_code(uint64_t key) { return key >> kScaleOffset; }
+static inline uint64_t key_to_scale(uint64_t key) { return key & kScaleMask; }
+static inline void decode_code(uint64_t code, int c[3])
+{
+    c[0] = (int) morton_compact(code);
+    c[1] = (int) morton_compact(code >> 1);
+    c[2] = (int) morton_compact(code >> 2);
+}
+static inline bool key_at_scale(uint64_t key, uint64_t scale, uint64_t& out)
+{
+    out = (key & (kCodeMask[scale] << kScaleOffset)) | scale;
+    return key_to_scale(key) <= scale;
+}
+static inline uint64_t block_key_of(uint64_t key, uint64_t max_block_scale)
+{
+    return key & ((kCodeMask[max_block_scale] << kScaleOffset) | kScaleMask);
+}
+static inline bool is_child_key(uint64_t parent, uint64_t child)
+{
+    const uint64_t ps = key_to_scale(parent), cs = key_to_scale(child);
+    if (cs >= ps)
+        return false;
+    return (key_to_code(parent) ^ (key_to_code(child) & kCodeMask[ps])) == 0;
+}
+
+/* ------------------------------------------------------------------------- the octree -- */
+/* Pointer octree like include/se/map/octree/octree.hpp: nodes own 8 child slots, blocks are
+ * 8^3 leaves with std::array<Data, 512>. Octants live in index-addressed vectors. */
+
+constexpr int kBlockSize = 8;
+constexpr int kBlockVoxels = 512;
+constexpr int kMaxBlockScale = 3;
+
+struct Octant {
+    int32_t child[8];
+    int32_t coord[3];
+    int32_t size;
+    int32_t block; /* index into blocks, -1 for nodes */
+    int32_t timestamp;
+};
+
+struct BlockData {
+    float tsdf[kBlockVoxels];
+    float weight[kBlockVoxels];
+};
+
+struct Octree {
+    int size = 0;
+    std::vector<Octant> octants; /* octants[0] is the root */
+    std::vector<BlockData> blocks;
+    std::vector<int32_t> block_octant;
+    bool aabb_empty = true;
+    int32_t aabb_min[3] = {0, 0, 0};
+    int32_t aabb_max[3] = {0, 0, 0};
+
+    void init(int sz)
+    {
+        size = sz;
+        octants.clear();
+        blocks.clear();
+        block_octant.clear();
+        Octant root{};
+        std::fill(root.child, root.child + 8, -1);
+        root.size = sz;
+        root.block = -1;
+        root.timestamp = -1;
+        octants.push_back(root);
+        aabb_empty = true;
+    }
+
+    void aabb_extend(const int32_t c[3], int sz)
+    {
+        for (int i = 0; i < 3; ++i) {
+            const int lo = c[i], hi = c[i] + sz - 1;
+            if (aabb_empty) {
+                aabb_min[i] = lo;
+                aabb_max[i] = hi;
+            }
+            else {
+                aabb_min[i] = std::min(aabb_min[i], lo);
+                aabb_max[i] = std::max(aabb_max[i], hi);
+            }
+        }
+        aabb_empty = false;
+    }
+
+    /* Octree::allocate, octree_impl.hpp:171-199 (new octants take the parent's default data). */
+    bool allocate(int parent, int child_idx, int& child)
+    {
+        child = octants[parent].child[child_idx];
+        if (child >= 0)
+            return false;
+        Octant o{};
+        std::fill(o.child, o.child + 8, -1);
+        const int psize = octants[parent].size;
+        const int csize = psize / 2;
+        for (int i = 0; i < 3; ++i)
+            o.coord[i] = octants[parent].coord[i] + csize * ((child_idx >> i) & 1);
+        o.size = csize;
+        o.timestamp = -1;
+        o.block = -1;
+        if (psize == 2 * kBlockSize) {
+            o.block = (int32_t) blocks.size();
+            blocks.emplace_back();
+            BlockData& b = blocks.back();
+            std::fill(b.tsdf, b.tsdf + kBlockVoxels, 1.0f);
+            std::fill(b.weight, b.weight + kBlockVoxels, 0.0f);
+        }
+        child = (int) octants.size();
+        octants.push_back(o);
+        if (o.block >= 0) {
+            block_octant.push_back(child);
+            aabb_extend(o.coord, csize);
+        }
+        octants[parent].child[child_idx] = child;
+        return true;
+    }
+
+    /* allocator::detail::allocate_key, allocator_impl.hpp:124-147 */
+    bool allocate_key(uint64_t key, int& out)
+    {
+        int parent = 0;
+        int child = -1;
+        int child_scale = (int) std::log2(octants[0].size) - 1;
+        const uint64_t code = key_to_code(key);
+        const int min_scale = std::max((int) key_to_scale(key), kMaxBlockScale);
+        bool did = false;
+        for (; child_scale >= min_scale; --child_scale) {
+            const int idx = (int) ((code >> (child_scale * 3)) & 7);
+            did = allocate(parent, idx, child);
+            parent = child;
+        }
+        out = child;
+        return did;
+    }
+
+    /* fetcher::block, fetcher_impl.hpp:107-126 */
+    int block_at(const int32_t c[3]) const
+    {
+        int parent = 0;
+        int child = -1;
+        for (int cs = size >> 1; cs >= kBlockSize; cs >>= 1) {
+            const int idx = ((c[0] & cs) > 0) + 2 * ((c[1] & cs) > 0) + 4 * ((c[2] & cs) > 0);
+            child = octants[parent].child[idx];
+            if (child < 0)
+                return -1;
+            parent = child;
+        }
+        return child;
+    }
+};
+
+/* ------------------------------------------------------------------------------ sensor -- */
+
+struct Pinhole {
+    int w, h;
+    float fx, fy, cx, cy;
+    float inv_fx, inv_fy;
+    float near_plane, far_plane;
+    bool left_hand;
+    float normals[6][4]; /* frustum planes: left, right, bottom, top, near, far */
+};
+
+static inline V3 back_project(const Pinhole& s, float u, float v)
+{
+    return v3((u - s.cx) * s.inv_fx, (v - s.cy) * s.inv_fy, 1.0f);
+}
+
+static inline bool project(const Pinhole& s, V3 p, float& u, float& v)
+{
+    if (std::fabs(p.z) < 1.0e-12f)
+        return false;
+    const float rz = 1.0f / p.z;
+    u = s.fx * (p.x * rz) + s.cx;
+    v = s.fy * (p.y * rz) + s.cy;
+    if (!(u >= -0.5f && u < (float) s.w - 0.5f && v >= -0.5f && v < (float) s.h - 0.5f))
+        return false;
+    return p.z > 0.0f;
+}
+
+/* se::math::plane_normal, math_util_impl.hpp:88-101 */
+static inline V3 plane_normal(V3 p1, V3 p2, V3 p3)
+{
+    return normalized(cross(p2 - p1, p3 - p2));
+}
+
+/* PinholeCamera ctor + computeFrustumVertices/Normals, pinhole_camera.cpp:63-84,246-310 */
+static Pinhole make_pinhole(int w, int h, float fx, float fy, float cx, float cy, float near_p,
+                            float far_p)
+{
+    Pinhole s;
+    s.w = w;
+    s.h = h;
+    s.fx = fx;
+    s.fy = fy;
+    s.cx = cx;
+    s.cy = cy;
+    s.inv_fx = 1.0f / fx;
+    s.inv_fy = 1.0f / fy;
+    s.near_plane = near_p;
+    s.far_plane = far_p;
+    s.left_hand = (fx < 0.0f) ^ (fy < 0.0f);
+    const V3 tl = back_project(s, 0.0f, 0.0f);
+    const V3 tr = back_project(s, (float) w, 0.0f);
+    const V3 br = back_project(s, (float) w, (float) h);
+    const V3 bl = back_project(s, 0.0f, (float) h);
+    const V3 tl_n = near_p * tl, tl_f = far_p * tl, tr_n = near_p * tr, tr_f = far_p * tr;
+    const V3 br_n = near_p * br, br_f = far_p * br, bl_n = near_p * bl, bl_f = far_p * bl;
+    const V3 n_left = plane_normal(tl_f, tl_n, bl_n);
+    const V3 n_right = plane_normal(tr_n, tr_f, br_f);
+    const V3 n_bottom = plane_normal(bl_f, bl_n, br_n);
+    const V3 n_top = plane_normal(tr_f, tr_n, tl_n);
+    const V3 ns[4] = {n_left, n_right, n_bottom, n_top};
+    float sign = fx * fy;
+    sign = sign / std::fabs(sign);
+    for (int i = 0; i < 4; ++i) {
+        s.normals[i][0] = ns[i].x * sign;
+        s.normals[i][1] = ns[i].y * sign;
+        s.normals[i][2] = ns[i].z * sign;
+        s.normals[i][3] = 0.0f;
+    }
+    s.normals[4][0] = 0.0f;
+    s.normals[4][1] = 0.0f;
+    s.normals[4][2] = 1.0f;
+    s.normals[4][3] = -near_p;
+    s.normals[5][0] = 0.0f;
+    s.normals[5][1] = 0.0f;
+    s.normals[5][2] = -1.0f;
+    s.normals[5][3] = far_p;
+    return s;
+}
+
+static Pinhole make_pinhole(const so_pinhole* p)
+{
+    return make_pinhole(
+        p->width, p->height, p->fx, p->fy, p->cx, p->cy, p->near_plane, p->far_plane);
+}
+
+/* PinholeCamera(const PinholeCamera&, dsf), pinhole_camera.cpp:95-111 */
+static Pinhole downsampled(const Pinhole& s, float dsf)
+{
+    return make_pinhole((int) ((float) s.w / dsf),
+                        (int) ((float) s.h / dsf),
+                        s.fx / dsf,
+                        s.fy / dsf,
+                        (s.cx + 0.5f) / dsf - 0.5f,
+                        (s.cy + 0.5f) / dsf - 0.5f,
+                        s.near_plane,
+                        s.far_plane);
+}
+
+/* sphereInFrustumImpl, pinhole_camera.cpp:189-204: distance = ((x*nx + y*ny) + z*nz) + nw */
+static inline bool sphere_in_frustum(const Pinhole& s, V3 c, float radius)
+{
+    for (int i = 0; i < 6; ++i) {
+        const float d =
+            ((c.x * s.normals[i][0] + c.y * s.normals[i][1]) + c.z * s.normals[i][2])
+            + s.normals[i][3];
+        if (d < -radius)
+            return false;
+    }
+    return true;
+}
+
+/* nearDistImpl / farDistImpl, pinhole_camera_impl.hpp:15-25 */
+static inline float near_dist(const Pinhole& s, V3 ray) { return s.near_plane / normalized(ray).z; }
+static inline float far_dist(const Pinhole& s, V3 ray) { return s.far_plane / normalized(ray).z; }
+
+static inline void round_pixel(float u, float v, int& x, int& y)
+{
+    x = (int) (u + 0.5f);
+    y = (int) (v + 0.5f);
+}
+
+} // namespace
+
+/* --------------------------------------------------------------------------------- map -- */
+
+struct so_map {
+    Octree octree;
+    float res;
+    float dim; /* octree size * res */
+    Tf T_MW;
+    Tf T_WM;
+    float trunc_factor;
+    float max_weight;
+
+    /* Map::contains + pointToVoxel<Safe::On>, map_impl.hpp:58-64,538-550 */
+    bool point_to_voxel(V3 p_W, int32_t v[3]) const
+    {
+        const V3 p_M = apply(T_MW, p_W);
+        if (!(p_M.x >= 0.0f && p_M.x < dim && p_M.y >= 0.0f && p_M.y < dim && p_M.z >= 0.0f
+              && p_M.z < dim)) {
+            v[0] = v[1] = v[2] = -1;
+            return false;
+        }
+        v[0] = (int) (p_M.x / res);
+        v[1] = (int) (p_M.y / res);
+        v[2] = (int) (p_M.z / res);
+        return true;
+    }
+    bool point_to_voxel_f(V3 p_W, V3& v) const
+    {
+        const V3 p_M = apply(T_MW, p_W);
+        if (!(p_M.x >= 0.0f && p_M.x < dim && p_M.y >= 0.0f && p_M.y < dim && p_M.z >= 0.0f
+              && p_M.z < dim)) {
+            v = v3(-1.0f, -1.0f, -1.0f);
+            return false;
+        }
+        v = p_M / res;
+        return true;
+    }
+    /* voxelToPoint(coord, stride), map_impl.hpp:503-509 */
+    V3 voxel_to_point(const int32_t c[3], int stride) const
+    {
+        const float off = (float) stride * 0.5f;
+        const V3 p_M =
+            v3(((float) c[0] + off) * res, ((float) c[1] + off) * res, ((float) c[2] + off) * res);
+        return apply(T_WM, p_M);
+    }
+};
+
+namespace {
+
+/* visitor::getData (single-res), visitor_impl.hpp:704-717: block voxel or the default data. */
+static inline bool get_voxel(const so_map& m, const int32_t c[3], float& tsdf, float& weight)
+{
+    const int o = m.octree.block_at(c);
+    if (o < 0) {
+        tsdf = 1.0f;
+        weight = 0.0f;
+        return false;
+    }
+    const Octant& oc = m.octree.octants[o];
+    const BlockData& b = m.octree.blocks[oc.block];
+    const int idx = (c[0] - oc.coord[0]) + 8 * (c[1] - oc.coord[1]) + 64 * (c[2] - oc.coord[2]);
+    tsdf = b.tsdf[idx];
+    weight = b.weight[idx];
+    return true;
+}
+
+/* visitor::getData(octree, block_ptr, coord), visitor_impl.hpp:718-735 */
+static inline void get_voxel_hint(const so_map& m, int hint_octant, const int32_t c[3],
+                                  float& tsdf, float& weight)
+{
+    const Octant& oc = m.octree.octants[hint_octant];
+    if (c[0] >= oc.coord[0] && c[0] <= oc.coord[0] + 7 && c[1] >= oc.coord[1]
+        && c[1] <= oc.coord[1] + 7 && c[2] >= oc.coord[2] && c[2] <= oc.coord[2] + 7) {
+        const BlockData& b = m.octree.blocks[oc.block];
+        const int idx =
+            (c[0] - oc.coord[0]) + 8 * (c[1] - oc.coord[1]) + 64 * (c[2] - oc.coord[2]);
+        tsdf = b.tsdf[idx];
+        weight = b.weight[idx];
+        return;
+    }
+    get_voxel(m, c, tsdf, weight);
+}
+
+/* visitor::getInterp single-res, visitor_impl.hpp:976-1024 (with get_neighbours :67-302: the
+ * neighbour gather fails if any of the up to 8 blocks touched is unallocated). */
+static bool field_interp_voxel(const so_map& m, V3 vf, float& out)
+{
+    const V3 bf = v3(vf.x - 0.5f, vf.y - 0.5f, vf.z - 0.5f);
+    const int32_t base[3] = {(int) bf.x, (int) bf.y, (int) bf.z};
+    const Octree& o = m.octree;
+    if (o.aabb_empty)
+        return false;
+    for (int i = 0; i < 3; ++i)
+        if (base[i] < o.aabb_min[i] || base[i] > o.aabb_max[i])
+            return false;
+    for (int i = 0; i < 3; ++i)
+        if (base[i] + 1 >= o.size || base[i] < 0)
+            return false;
+    /* every crossmask case of get_neighbours fetches the block of base first, then the other
+     * blocks touched; any unallocated block, then any invalid voxel, gives nullopt */
+    float f[8], wt[8];
+    for (int n = 0; n < 8; ++n) {
+        const int32_t c[3] = {base[0] + (n & 1), base[1] + ((n >> 1) & 1), base[2] + ((n >> 2) & 1)};
+        if (!get_voxel(m, c, f[n], wt[n]))
+            return false;
+    }
+    for (int n = 0; n < 8; ++n)
+        if (!(wt[n] != 0.0f))
+            return false;
+    const V3 t = v3(bf.x - std::floor(bf.x), bf.y - std::floor(bf.y), bf.z - std::floor(bf.z));
+    const V3 tc = v3(1.0f - t.x, 1.0f - t.y, 1.0f - t.z);
+    out = ((f[0] * tc.x + f[1] * t.x) * tc.y + (f[2] * tc.x + f[3] * t.x) * t.y) * tc.z
+        + ((f[4] * tc.x + f[5] * t.x) * tc.y + (f[6] * tc.x + f[7] * t.x) * t.y) * t.z;
+    return true;
+}
+
+/* visitor::getFieldGrad single-res, visitor_impl.hpp:1094-1251 */
+static bool field_grad_voxel(const so_map& m, V3 vf, V3& g)
+{
+    const V3 s = v3(vf.x - 0.5f, vf.y - 0.5f, vf.z - 0.5f);
+    const V3 fac = v3(s.x - std::floor(s.x), s.y - std::floor(s.y), s.z - std::floor(s.z));
+    const int32_t base[3] = {(int) s.x, (int) s.y, (int) s.z};
+    const int top = m.octree.size - 1;
+    int32_t ll[3], lu[3], ul[3], uu[3];
+    for (int i = 0; i < 3; ++i) {
+        ll[i] = std::max(base[i] - 1, 0);
+        lu[i] = std::max(base[i], 0);
+        ul[i] = std::min(base[i] + 1, top);
+        uu[i] = std::min(base[i] + 2, top);
+    }
+    const int hint = m.octree.block_at(base);
+    if (hint < 0)
+        return false;
+    /* the 32 sample coordinates, in the reference's order */
+    const int32_t* X[32] = {ll, ll, ll, ll, lu, lu, lu, lu, lu, lu, lu, lu, lu, lu, lu, lu,
+                            ul, ul, ul, ul, ul, ul, ul, ul, ul, ul, ul, ul, uu, uu, uu, uu};
+    const int32_t* Y[32] = {lu, ul, lu, ul, ll, ll, lu, lu, lu, lu, ul, ul, ul, ul, uu, uu,
+                            ll, ll, lu, lu, lu, lu, ul, ul, ul, ul, uu, uu, lu, ul, lu, ul};
+    const int32_t* Z[32] = {lu, lu, ul, ul, lu, ul, ll, lu, ul, uu, ll, lu, ul, uu, lu, ul,
+                            lu, ul, ll, lu, ul, uu, ll, lu, ul, uu, lu, ul, lu, lu, ul, ul};
+    float v[32];
+    for (int i = 0; i < 32; ++i) {
+        const int32_t c[3] = {X[i][0], Y[i][1], Z[i][2]};
+        float t, w;
+        get_voxel_hint(m, hint, c, t, w);
+        if (!(w != 0.0f))
+            return false;
+        v[i] = t;
+    }
+    const float rx = 1.0f - fac.x, ry = 1.0f - fac.y, rz = 1.0f - fac.z;
+    const float gx = (((v[19] - v[0]) * rx + (v[28] - v[7]) * fac.x) * ry
+                      + ((v[23] - v[1]) * rx + (v[29] - v[11]) * fac.x) * fac.y)
+            * rz
+        + (((v[20] - v[2]) * rx + (v[30] - v[8]) * fac.x) * ry
+           + ((v[24] - v[3]) * rx + (v[31] - v[12]) * fac.x) * fac.y)
+            * fac.z;
+    const float gy = (((v[11] - v[4]) * rx + (v[23] - v[16]) * fac.x) * ry
+                      + ((v[14] - v[7]) * rx + (v[26] - v[19]) * fac.x) * fac.y)
+            * rz
+        + (((v[12] - v[5]) * rx + (v[24] - v[17]) * fac.x) * ry
+           + ((v[15] - v[8]) * rx + (v[27] - v[20]) * fac.x) * fac.y)
+            * fac.z;
+    const float gz = (((v[8] - v[6]) * rx + (v[20] - v[18]) * fac.x) * ry
+                      + ((v[12] - v[10]) * rx + (v[24] - v[22]) * fac.x) * fac.y)
+            * rz
+        + (((v[9] - v[7]) * rx + (v[21] - v[19]) * fac.x) * ry
+           + ((v[13] - v[11]) * rx + (v[25] - v[23]) * fac.x) * fac.y)
+            * fac.z;
+    g = v3(0.5f * gx, 0.5f * gy, 0.5f * gz);
+    return true;
+}
+
+static bool map_field_interp(const so_map& m, V3 p_W, float& out)
+{
+    V3 vf;
+    if (!m.point_to_voxel_f(p_W, vf))
+        return false;
+    return field_interp_voxel(m, vf, out);
+}
+
+/* Map::getFieldGrad, map_impl.hpp:236-262 */
+static bool map_field_grad(const so_map& m, V3 p_W, V3& g)
+{
+    V3 vf;
+    if (!m.point_to_voxel_f(p_W, vf))
+        return false;
+    if (!field_grad_voxel(m, vf, g))
+        return false;
+    g = g / m.res;
+    return true;
+}
+
+/* Map::getData<Safe::On>, map_impl.hpp:68-86 */
+static inline void map_get_data(const so_map& m, V3 p_W, float& tsdf, float& weight)
+{
+    int32_t c[3];
+    if (!m.point_to_voxel(p_W, c)) {
+        tsdf = 1.0f;
+        weight = 0.0f;
+        return;
+    }
+    get_voxel(m, c, tsdf, weight);
+}
+
+/* ------------------------------------------------------- VoxelBlockRayIterator (ESVO) -- */
+/* voxel_block_ray_iterator_impl.hpp:19-249: Laine & Karras sparse-voxel-octree traversal in the
+ * [1, 2]^3 scaled frame, mirrored so that every direction component is negative. Returns the
+ * state after the first next(): whether a block was found, tcmin() and tmax(). */
+
+static inline int32_t f_as_i(float f)
+{
+    int32_t i;
+    std::memcpy(&i, &f, 4);
+    return i;
+}
+static inline float i_as_f(int32_t i)
+{
+    float f;
+    std::memcpy(&f, &i, 4);
+    return f;
+}
+
+struct RayBlockHit {
+    bool found;
+    float tcmin; /* metres */
+    float tmax;  /* metres */
+};
+
+static RayBlockHit first_block_on_ray(const so_map& m, V3 origin_W, V3 dir_W, float near_p,
+                                      float far_p)
+{
+    constexpr int kStackDepth = 23;
+    const Octree& oct = m.octree;
+    const float scaling = (float) oct.size * m.res;
+    const int min_scale = kStackDepth - (int) std::log2((double) (oct.size / kBlockSize));
+    const float eps = std::exp2((float) (-std::log2((double) oct.size)));
+
+    float d[3] = {dir_W.x, dir_W.y, dir_W.z};
+    for (int a = 0; a < 3; ++a)
+        if (std::fabs(d[a]) < eps)
+            d[a] = std::copysign(eps, d[a]);
+
+    /* pointToVoxel<Safe::Off> (float), then scale into [1, 2] */
+    const V3 o_M = apply(m.T_MW, origin_W);
+    const float o_v[3] = {o_M.x / m.res, o_M.y / m.res, o_M.z / m.res};
+    float o[3];
+    for (int a = 0; a < 3; ++a)
+        o[a] = o_v[a] / (float) oct.size + 1.0f;
+
+    float t_coef[3], t_bias[3];
+    for (int a = 0; a < 3; ++a) {
+        t_coef[a] = -1.0f * (1.0f / std::fabs(d[a]));
+        t_bias[a] = t_coef[a] * o[a];
+    }
+    int mirror_mask = 7;
+    for (int a = 0; a < 3; ++a) {
+        if (d[a] > 0.0f) {
+            mirror_mask ^= (1 << a);
+            t_bias[a] = 3.0f * t_coef[a] - t_bias[a];
+        }
+    }
+    float t_min = std::max(std::max(2.0f * t_coef[0] - t_bias[0], 2.0f * t_coef[1] - t_bias[1]),
+                           2.0f * t_coef[2] - t_bias[2]);
+    float t_max = std::min(std::min(t_coef[0] - t_bias[0], t_coef[1] - t_bias[1]),
+                           t_coef[2] - t_bias[2]);
+    float h = t_max;
+    t_min = std::max(t_min, near_p / scaling);
+    t_max = std::min(t_max, far_p / scaling);
+    const float t_max_init = t_max;
+
+    int idx = 0;
+    float pos[3] = {1.0f, 1.0f, 1.0f};
+    for (int a = 0; a < 3; ++a) {
+        if (1.5f * t_coef[a] - t_bias[a] > t_min) {
+            idx ^= (1 << a);
+            pos[a] = 1.5f;
+        }
+    }
+    int parent = 0;
+    int scale = kStackDepth - 1;
+    float scale_exp2 = 0.5f;
+    struct Entry {
+        int parent;
+        float t_max;
+    } stack[kStackDepth];
+    for (int i = 0; i < kStackDepth; ++i)
+        stack[i] = Entry{-1, 0.0f};
+
+    while (scale < kStackDepth) {
+        float tc[3];
+        for (int a = 0; a < 3; ++a)
+            tc[a] = pos[a] * t_coef[a] - t_bias[a];
+        const float tc_max = std::min(std::min(tc[0], tc[1]), tc[2]);
+        const int child = (parent >= 0) ? oct.octants[parent].child[idx ^ mirror_mask ^ 7] : -1;
+
+        if (scale == min_scale && child >= 0) {
+            return RayBlockHit{true, t_min * scaling, t_max_init * scaling};
+        }
+        if (child >= 0 && t_min <= t_max) {
+            /* descend */
+            const float tv_max = std::min(t_max, tc_max);
+            const float half = scale_exp2 * 0.5f;
+            float t_centre[3];
+            for (int a = 0; a < 3; ++a)
+                t_centre[a] = half * t_coef[a] + tc[a];
+            if (tc_max < h)
+                stack[scale] = Entry{parent, t_max};
+            h = tc_max;
+            parent = child;
+            idx = 0;
+            --scale;
+            scale_exp2 = half;
+            for (int a = 0; a < 3; ++a)
+                if (t_centre[a] > t_min)
+                    idx ^= (1 << a);
+            for (int a = 0; a < 3; ++a)
+                if (idx & (1 << a))
+                    pos[a] += scale_exp2;
+            t_max = tv_max;
+            continue;
+        }
+        /* advance */
+        int step_mask = 0;
+        for (int a = 0; a < 3; ++a)
+            if (tc[a] <= tc_max)
+                step_mask |= (1 << a);
+        for (int a = 0; a < 3; ++a)
+            if (step_mask & (1 << a))
+                pos[a] -= scale_exp2;
+        t_min = tc_max;
+        idx ^= step_mask;
+        if ((idx & step_mask) != 0) {
+            /* pop to the level where the position bits first differ */
+            uint32_t differing = 0;
+            for (int a = 0; a < 3; ++a)
+                if (step_mask & (1 << a))
+                    differing |= (uint32_t) (f_as_i(pos[a]) ^ f_as_i(pos[a] + scale_exp2));
+            scale = (f_as_i((float) differing) >> 23) - 127;
+            if (scale >= kStackDepth)
+                break;
+            scale_exp2 = i_as_f((scale - kStackDepth + 127) << 23);
+            parent = stack[scale].parent;
+            t_max = stack[scale].t_max;
+            int sh[3];
+            for (int a = 0; a < 3; ++a) {
+                sh[a] = f_as_i(pos[a]) >> scale;
+                pos[a] = i_as_f(sh[a] << scale);
+            }
+            idx = (sh[0] & 1) | ((sh[1] & 1) << 1) | ((sh[2] & 1) << 2);
+            h = 0.0f;
+        }
+    }
+    return RayBlockHit{false, t_min * scaling, t_max_init * scaling};
+}
+
+/* raycast<TSDF>, raycaster_impl.hpp:456-533. Returns true on a hit with point_W and scale. */
+static bool raycast_tsdf(const so_map& m, V3 origin_W, V3 dir_W, float t_near, float t_far,
+                         V3& hit_W)
+{
+    const RayBlockHit rb = first_block_on_ray(m, origin_W, dir_W, t_near, t_far);
+    const float step = m.res;
+    const float largestep = (float) kBlockSize * step;
+    const float t_min = rb.tcmin;
+    if (t_min <= 0.0f)
+        return false;
+    const float t_max = rb.tmax;
+    float t = t_min;
+    const float trunc = m.res * m.trunc_factor;
+    if (!(t_near < t_max))
+        return false;
+    float stepsize = largestep;
+    V3 p = origin_W + dir_W * t;
+    float f_t, w_t;
+    map_get_data(m, p, f_t, w_t);
+    float f_tt = 0.0f;
+    if (!(f_t >= 0.0f))
+        return false;
+    for (; t < t_far; t += stepsize) {
+        float f, w;
+        map_get_data(m, p, f, w);
+        if (!(w != 0.0f)) {
+            stepsize = largestep;
+            p = p + stepsize * dir_W;
+            continue;
+        }
+        f_tt = f;
+        /* the reference compares against the double literal 0.1 */
+        if ((double) f_tt <= 0.1 && f_tt >= -0.5f) {
+            float fi;
+            if (map_field_interp(m, p, fi))
+                f_tt = fi;
+        }
+        if (f_tt < 0.0f)
+            break;
+        stepsize = std::max(f_tt * trunc, step);
+        p = p + stepsize * dir_W;
+        f_t = f_tt;
+    }
+    if (f_tt < 0.0f) {
+        t = t - stepsize * (f_tt - 0.0f) / (f_tt - f_t);
+        hit_W = origin_W + dir_W * t;
+        return true;
+    }
+    return false;
+}
+
+/* ----------------------------------------------------------------- ICP helpers (float) -- */
+
+/* Eigen-style unblocked Cholesky (LLT) on the lower triangle, then forward/back substitution.
+ * Returns false on a non-positive pivot (icp.cpp:33-41 returns zero in that case). */
+static bool llt_solve6(const float C_in[6][6], const float b[6], float x[6])
+{
+    float L[6][6];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j)
+            L[i][j] = C_in[i][j];
+    for (int k = 0; k < 6; ++k) {
+        float sq = 0.0f;
+        for (int j = 0; j < k; ++j)
+            sq += L[k][j] * L[k][j];
+        float xk = L[k][k] - sq;
+        if (xk <= 0.0f)
+            return false;
+        xk = std::sqrt(xk);
+        L[k][k] = xk;
+        for (int i = k + 1; i < 6; ++i) {
+            float s = 0.0f;
+            for (int j = 0; j < k; ++j)
+                s += L[i][j] * L[k][j];
+            L[i][k] = (L[i][k] - s) / xk;
+        }
+    }
+    float y[6];
+    for (int i = 0; i < 6; ++i) {
+        float s = b[i];
+        for (int j = 0; j < i; ++j)
+            s -= L[i][j] * y[j];
+        y[i] = s / L[i][i];
+    }
+    for (int i = 5; i >= 0; --i) {
+        float s = y[i];
+        for (int j = i + 1; j < 6; ++j)
+            s -= L[j][i] * x[j];
+        x[i] = s / L[i][i];
+    }
+    return true;
+}
+
+/* math::exp_and_theta + math::exp, math_util_impl.hpp:117-174 */
+static Tf se3_exp(const float a[6])
+{
+    const V3 w = v3(a[3], a[4], a[5]);
+    const float theta_sq = dot(w, w);
+    const float theta = std::sqrt(theta_sq);
+    const float half_theta = 0.5f * theta;
+    float imag, real;
+    if ((double) theta < 1e-10) {
+        const float theta_po4 = theta_sq * theta_sq;
+        imag = 0.5f - 1.0f / 48.0f * theta_sq + 1.0f / 3840.0f * theta_po4;
+        real = 1.0f - 0.5f * theta_sq + 1.0f / 384.0f * theta_po4;
+    }
+    else {
+        imag = std::sin(half_theta) / theta;
+        real = std::cos(half_theta);
+    }
+    float qw = real, qx = imag * w.x, qy = imag * w.y, qz = imag * w.z;
+    /* Eigen stores (x, y, z, w); the norm sums in that order */
+    const float qn = std::sqrt(((qx * qx + qy * qy) + qz * qz) + qw * qw);
+    qw /= qn;
+    qx /= qn;
+    qy /= qn;
+    qz /= qn;
+    const float tx = 2.0f * qx, ty = 2.0f * qy, tz = 2.0f * qz;
+    const float twx = tx * qw, twy = ty * qw, twz = tz * qw;
+    const float txx = tx * qx, txy = ty * qx, txz = tz * qx;
+    const float tyy = ty * qy, tyz = tz * qy, tzz = tz * qz;
+    float R[3][3] = {{1.0f - (tyy + tzz), txy - twz, txz + twy},
+                     {txy + twz, 1.0f - (txx + tzz), tyz - twx},
+                     {txz - twy, tyz + twx, 1.0f - (txx + tyy)}};
+    const float O[3][3] = {{0.0f, -w.z, w.y}, {w.z, 0.0f, -w.x}, {-w.y, w.x, 0.0f}};
+    float O2[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            O2[i][j] = (O[i][0] * O[0][j] + O[i][1] * O[1][j]) + O[i][2] * O[2][j];
+    float V[3][3];
+    if ((double) theta < 1e-10) {
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                V[i][j] = R[i][j];
+    }
+    else {
+        const float tsq = theta * theta;
+        const float c1 = (1.0f - std::cos(theta)) / tsq;
+        const float c2 = (theta - std::sin(theta)) / (tsq * theta);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                V[i][j] = ((i == j ? 1.0f : 0.0f) + c1 * O[i][j]) + c2 * O2[i][j];
+    }
+    Tf T;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            T.R[i][j] = R[i][j];
+        T.t[i] = (V[i][0] * a[0] + V[i][1] * a[1]) + V[i][2] * a[2];
+    }
+    return T;
+}
+
+/* half_sample_robust_image, preprocessor.cpp:156-195 */
+static void half_sample_robust(const float* in, int in_w, int in_h, float e_d, int radius,
+                               float* out)
+{
+    const int ow = in_w / 2, oh = in_h / 2;
+#pragma omp parallel for
+    for (int y = 0; y < oh; y++) {
+        for (int x = 0; x < ow; x++) {
+            const int px = 2 * x, py = 2 * y;
+            float count = 0.0f, sum = 0.0f;
+            const float centre = in[px + py * in_w];
+            for (int i = -radius + 1; i <= radius; ++i) {
+                for (int j = -radius + 1; j <= radius; ++j) {
+                    int qx = px + j, qy = py + i;
+                    qx = std::min(std::max(qx, 0), 2 * ow - 1);
+                    qy = std::min(std::max(qy, 0), 2 * oh - 1);
+                    const float v = in[qx + qy * in_w];
+                    if (std::fabs(v - centre) < e_d) {
+                        count += 1.0f;
+                        sum += v;
+                    }
+                }
+            }
+            out[x + y * ow] = sum / count;
+        }
+    }
+}
+
+/* depth_to_point_cloud, preprocessor_impl.hpp:18-40 */
+static void depth_to_points(const float* depth, const Pinhole& s, V3* pts)
+{
+#pragma omp parallel for
+    for (int y = 0; y < s.h; y++) {
+        for (int x = 0; x < s.w; x++) {
+            const float d = depth[x + y * s.w];
+            if (d > 0.0f) {
+                pts[x + y * s.w] = d * back_project(s, (float) x, (float) y);
+            }
+            else {
+                pts[x + y * s.w] = v3(0.0f, 0.0f, 0.0f);
+            }
+        }
+    }
+}
+
+/* point_cloud_to_normal<NegY>, preprocessor.cpp:109-152 */
+static void points_to_normals(const V3* pts, int w, int h, bool neg_y, V3* nrm)
+{
+#pragma omp parallel for
+    for (int y = 0; y < h; y++) {
+        for (int x = 0; x < w; x++) {
+            const V3 p = pts[x + w * y];
+            if (p.z == 0.0f) {
+                nrm[x + y * w] = v3(0.0f, 0.0f, 0.0f);
+                continue;
+            }
+            const int lx = std::max(x - 1, 0), rx = std::min(x + 1, w - 1);
+            int uy, dy;
+            if (neg_y) {
+                uy = std::max(y - 1, 0);
+                dy = std::min(y + 1, h - 1);
+            }
+            else {
+                dy = std::max(y - 1, 0);
+                uy = std::min(y + 1, h - 1);
+            }
+            const V3 left = pts[lx + w * y], right = pts[rx + w * y];
+            const V3 up = pts[x + w * uy], down = pts[x + w * dy];
+            if (left.z == 0.0f || right.z == 0.0f || up.z == 0.0f || down.z == 0.0f) {
+                nrm[x + y * w] = v3(0.0f, 0.0f, 0.0f);
+                continue;
+            }
+            nrm[x + y * w] = normalized(cross(right - left, up - down));
+        }
+    }
+}
+
+enum { kSuccess = 1, kInvalidInputNormal = -1, kProjOutside = -2, kInvalidRefNormal = -3,
+       kDistThreshold = -4, kNormalThreshold = -5 };
+
+struct IcpRow {
+    int result;
+    float error;
+    float J[6];
+};
+
+} // namespace
+
+/* ===================================================================== C interface === */
+
+extern "C" {
+
+void so_set_num_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0)
+        omp_set_num_threads(n);
+#else
+    (void) n;
+#endif
+}
+
+int so_get_num_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* Map ctor, map_impl.hpp:37-55; Octree ctor, octree_impl.hpp:14-19 */
+so_map* so_map_create(const float dim[3], float res, float truncation_boundary_factor,
+                      float max_weight, const float* T_MW)
+{
+    so_map* m = new so_map();
+    const float dmax = std::max(std::max(dim[0], dim[1]), dim[2]);
+    const int requested = (int) std::ceil(dmax / res);
+    int sz = 1;
+    while (sz < std::max(requested, 2 * kBlockSize))
+        sz <<= 1;
+    m->octree.init(sz);
+    m->res = res;
+    m->dim = (float) sz * res;
+    if (T_MW) {
+        m->T_MW = tf_from16(T_MW);
+    }
+    else {
+        m->T_MW = tf_identity();
+        m->T_MW.t[0] = dim[0] / 2.0f;
+        m->T_MW.t[1] = dim[1] / 2.0f;
+        m->T_MW.t[2] = dim[2] / 2.0f;
+    }
+    m->T_WM = inverse_iso(m->T_MW);
+    m->trunc_factor = truncation_boundary_factor;
+    m->max_weight = max_weight;
+    return m;
+}
+
+void so_map_destroy(so_map* map) { delete map; }
+int so_map_size(const so_map* map) { return map->octree.size; }
+float so_map_dim(const so_map* map) { return map->dim; }
+
+void so_integrate_depth(so_map* map, const float* depth, const so_pinhole* sensor_c,
+                        const float T_WC_m[16], int timestamp, so_integrate_stats* stats)
+{
+    so_map& m = *map;
+    Octree& oct = m.octree;
+    const Pinhole s = make_pinhole(sensor_c);
+    const Tf T_WS = tf_from16(T_WC_m);
+    const float band = 2.0f * m.res * m.trunc_factor;
+
+    /* fetcher::frustum (raycast_carver_impl.hpp:17-32): FrustumIterator DFS over the octree; an
+     * octant whose bounding sphere misses the frustum is skipped with its subtree. The root is
+     * never tested (iterator_impl.hpp:88-118 pushes its children before testing it). */
+    const Tf T_SW = inverse_iso(T_WS);
+    std::vector<int> frustum_blocks;
+    {
+        std::vector<int> stack;
+        for (int c = 0; c < 8; ++c)
+            if (oct.octants[0].child[c] >= 0)
+                stack.push_back(oct.octants[0].child[c]);
+        while (!stack.empty()) {
+            const int o = stack.back();
+            stack.pop_back();
+            const Octant& oc = oct.octants[o];
+            const V3 centre_W = m.voxel_to_point(oc.coord, oc.size);
+            const V3 centre_S = apply(T_SW, centre_W);
+            const float radius = std::sqrt(3.0f) / 2.0f * m.res * (float) oc.size;
+            if (!sphere_in_frustum(s, centre_S, radius))
+                continue;
+            if (oc.block >= 0) {
+                frustum_blocks.push_back(o);
+                continue;
+            }
+            for (int c = 0; c < 8; ++c)
+                if (oc.child[c] >= 0)
+                    stack.push_back(oc.child[c]);
+        }
+    }
+
+    /* RaycastCarver::operator(), raycast_carver_impl.hpp:56-128 */
+    const int num_steps = (int) std::ceil(band / (2.0f * m.res));
+    const V3 t_WS = v3(T_WS.t[0], T_WS.t[1], T_WS.t[2]);
+    long long n_valid = 0;
+#pragma omp declare reduction(merge : std::set<uint64_t> : omp_out.insert(omp_in.begin(), omp_in.end()))
+    std::set<uint64_t> key_set;
+#pragma omp parallel for reduction(merge : key_set) reduction(+ : n_valid)
+    for (int x = 0; x < s.w; ++x) {
+        for (int y = 0; y < s.h; ++y) {
+            const float dv = depth[x + y * s.w];
+            if (dv < s.near_plane || dv > (s.far_plane + band * 0.5f))
+                continue;
+            ++n_valid;
+            const V3 ray_C = back_project(s, (float) x, (float) y);
+            const V3 point_W = apply(T_WS, dv * ray_C);
+            const V3 rev = normalized(t_WS - point_W);
+            const V3 origin = point_W - (band * 0.5f) * rev;
+            const V3 step = (rev * band) / (float) num_steps;
+            V3 pos = origin;
+            for (int i = 0; i < num_steps; i++) {
+                int32_t vc[3];
+                if (m.point_to_voxel(pos, vc)) {
+                    if (oct.block_at(vc) < 0) {
+                        key_set.insert(encode_key(vc[0], vc[1], vc[2], kMaxBlockScale));
+                    }
+                }
+                pos = pos + step;
+            }
+        }
+    }
+    const std::vector<uint64_t> keys(key_set.begin(), key_set.end());
+
+    /* allocator::blocks(keys, only_allocated = true), allocator_impl.hpp:68-116 (serial here:
+     * allocation order does not change the resulting tree) */
+    std::vector<int> list;
+    for (uint64_t k : keys) {
+        int o;
+        if (oct.allocate_key(k, o))
+            list.push_back(o);
+    }
+    const long long n_new = (long long) list.size();
+    list.insert(list.end(), frustum_blocks.begin(), frustum_blocks.end());
+
+    /* single-res TSDF Updater, singleres_tsdf_updater_impl.hpp:14-132 */
+    const float trunc = m.res * m.trunc_factor;
+    const Tf T_CW = inverse_iso(T_WS);
+    Tf T_CV = compose(T_CW, m.T_WM);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            T_CV.R[i][j] = T_CV.R[i][j] * m.res;
+    for (int i = 0; i < 3; ++i)
+        T_CV.t[i] = ((T_CV.R[i][0] * 0.5f + T_CV.R[i][1] * 0.5f) + T_CV.R[i][2] * 0.5f) + T_CV.t[i];
+    long long n_upd = 0;
+#pragma omp parallel for reduction(+ : n_upd)
+    for (long long i = 0; i < (long long) list.size(); i++) {
+        Octant& oc = oct.octants[list[i]];
+        oc.timestamp = timestamp;
+        BlockData& b = oct.blocks[oc.block];
+        for (int x = 0; x < kBlockSize; ++x) {
+            for (int y = 0; y < kBlockSize; ++y) {
+                for (int z = 0; z < kBlockSize; ++z) {
+                    const V3 vc = v3((float) (oc.coord[0] + x), (float) (oc.coord[1] + y),
+                                     (float) (oc.coord[2] + z));
+                    const V3 p_C = apply(T_CV, vc);
+                    const float pn = norm(p_C);
+                    if (pn > far_dist(s, p_C))
+                        continue;
+                    float u, v;
+                    if (!project(s, p_C, u, v))
+                        continue;
+                    int px, py;
+                    round_pixel(u, v, px, py);
+                    const float dv = depth[px + py * s.w];
+                    if (dv < s.near_plane)
+                        continue;
+                    const float mz = p_C.z;
+                    const float sdf = (dv - mz) / mz * pn;
+                    /* FieldData<TSDF>::update, data_field_impl.hpp:39-54 */
+                    if (sdf < -trunc)
+                        continue;
+                    const float upd = std::min(sdf / trunc, 1.0f);
+                    const int idx = x + 8 * y + 64 * z;
+                    float w = b.weight[idx];
+                    if (w < m.max_weight)
+                        w = w + 1.0f;
+                    b.tsdf[idx] = (b.tsdf[idx] * (w - 1.0f) + upd) / w;
+                    b.weight[idx] = w;
+                    ++n_upd;
+                }
+            }
+        }
+    }
+    if (stats) {
+        stats->n_valid_pixels = n_valid;
+        stats->n_new_blocks = n_new;
+        stats->n_frustum_blocks = (long long) frustum_blocks.size();
+        stats->n_updated_voxels = n_upd;
+    }
+}
+
+/* raycaster::raycast_volume, raycaster_impl.hpp:537-627 */
+void so_raycast_volume(const so_map* map, const so_pinhole* sensor_c, const float T_WS_m[16],
+                       float* pts_W, float* nrm_W, int8_t* scale)
+{
+    const so_map& m = *map;
+    const Pinhole s = make_pinhole(sensor_c);
+    const Tf T_WS = tf_from16(T_WS_m);
+    const V3 origin = v3(T_WS.t[0], T_WS.t[1], T_WS.t[2]);
+#pragma omp parallel for
+    for (int y = 0; y < s.h; y++) {
+        for (int x = 0; x < s.w; x++) {
+            const size_t idx = (size_t) x + (size_t) y * (size_t) s.w;
+            const V3 ray_S = back_project(s, (float) x, (float) y);
+            const V3 dir_W = rot(T_WS, normalized(ray_S));
+            V3 hit;
+            if (raycast_tsdf(m, origin, dir_W, near_dist(s, ray_S), far_dist(s, ray_S), hit)) {
+                scale[idx] = 0;
+                pts_W[3 * idx + 0] = hit.x;
+                pts_W[3 * idx + 1] = hit.y;
+                pts_W[3 * idx + 2] = hit.z;
+                V3 g;
+                if (map_field_grad(m, hit, g)) {
+                    const V3 n = normalized(g);
+                    nrm_W[3 * idx + 0] = n.x;
+                    nrm_W[3 * idx + 1] = n.y;
+                    nrm_W[3 * idx + 2] = n.z;
+                }
+                else {
+                    nrm_W[3 * idx + 0] = nrm_W[3 * idx + 1] = nrm_W[3 * idx + 2] = 0.0f;
+                }
+            }
+            else {
+                /* raycast_volume leaves the scale image untouched on a miss; it is set to 0 here */
+                scale[idx] = 0;
+                pts_W[3 * idx + 0] = pts_W[3 * idx + 1] = pts_W[3 * idx + 2] = 0.0f;
+                nrm_W[3 * idx + 0] = nrm_W[3 * idx + 1] = nrm_W[3 * idx + 2] = 0.0f;
+            }
+        }
+    }
+}
+
+/* Tracker::track(depth, T_WS, pts, nrm), tracker_impl.hpp:30-116 */
+int so_track(const so_pinhole* sensor_c, const so_tracker_config* cfg, const float* depth,
+             float T_WS_m[16], const float* ref_pts_W, const float* ref_nrm_W,
+             so_track_stats* stats)
+{
+    const Pinhole s = make_pinhole(sensor_c);
+    Tf T_WS = tf_from16(T_WS_m);
+    const Tf T_WS_ref = T_WS;
+    const int W = s.w, H = s.h;
+    const int L = std::min(std::max(cfg->num_levels, 1), 3);
+    std::vector<std::vector<float>> dimg(L);
+    std::vector<std::vector<V3>> pts(L), nrm(L);
+    std::vector<int> lw(L), lh(L);
+    for (int i = 0; i < L; ++i) {
+        lw[i] = W / (1 << i);
+        lh[i] = H / (1 << i);
+        dimg[i].assign((size_t) lw[i] * lh[i], 0.0f);
+        pts[i].assign((size_t) lw[i] * lh[i], v3(0, 0, 0));
+        nrm[i].assign((size_t) lw[i] * lh[i], v3(0, 0, 0));
+    }
+    std::memcpy(dimg[0].data(), depth, sizeof(float) * (size_t) W * H);
+    for (int i = 1; i < L; ++i)
+        half_sample_robust(dimg[i - 1].data(), lw[i - 1], lh[i - 1], 0.1f * 3.0f, 1, dimg[i].data());
+    for (int i = 0; i < L; ++i) {
+        const Pinhole si = downsampled(s, (float) (1 << i));
+        depth_to_points(dimg[i].data(), si, pts[i].data());
+        points_to_normals(pts[i].data(), si.w, si.h, s.left_hand, nrm[i].data());
+    }
+
+    std::vector<IcpRow> rows((size_t) W * H, IcpRow{0, 0.0f, {0, 0, 0, 0, 0, 0}});
+    float red[8][32];
+    std::memset(red, 0, sizeof(red));
+    const V3* rp = reinterpret_cast<const V3*>(ref_pts_W);
+    const V3* rn = reinterpret_cast<const V3*>(ref_nrm_W);
+    int iters_run[3] = {0, 0, 0};
+
+    for (int level = L - 1; level >= 0; --level) {
+        const int w = lw[level], h = lh[level];
+        for (int it = 0; it < cfg->iterations[level]; ++it) {
+            ++iters_run[level];
+            /* icp::trackKernel, icp_impl.hpp:16-102 */
+            const Tf T_ref_inv = inverse_iso(T_WS_ref);
+#pragma omp parallel for
+            for (int y = 0; y < h; y++) {
+                for (int x = 0; x < w; x++) {
+                    IcpRow& row = rows[(size_t) x + (size_t) y * W];
+                    const V3 n_in = nrm[level][x + y * w];
+                    if (is_zero(n_in)) {
+                        row.result = kInvalidInputNormal;
+                        continue;
+                    }
+                    const V3 p_W = apply(T_WS, pts[level][x + y * w]);
+                    const V3 p_ref = apply(T_ref_inv, p_W);
+                    float u, v;
+                    if (!project(s, p_ref, u, v)) {
+                        row.result = kProjOutside;
+                        continue;
+                    }
+                    int px, py;
+                    round_pixel(u, v, px, py);
+                    const size_t ri = (size_t) px + (size_t) py * W;
+                    const V3 n_ref = v3(-rn[ri].x, -rn[ri].y, -rn[ri].z);
+                    if (is_zero(n_ref)) {
+                        row.result = kInvalidRefNormal;
+                        continue;
+                    }
+                    const V3 diff = rp[ri] - p_W;
+                    const V3 n_W = rot(T_WS, n_in);
+                    if (norm(diff) > cfg->dist_threshold) {
+                        row.result = kDistThreshold;
+                        continue;
+                    }
+                    if (dot(n_W, n_ref) < cfg->normal_threshold) {
+                        row.result = kNormalThreshold;
+                        continue;
+                    }
+                    row.result = kSuccess;
+                    row.error = dot(n_ref, diff);
+                    row.J[0] = n_ref.x;
+                    row.J[1] = n_ref.y;
+                    row.J[2] = n_ref.z;
+                    const V3 c = cross(p_W, n_ref);
+                    row.J[3] = c.x;
+                    row.J[4] = c.y;
+                    row.J[5] = c.z;
+                }
+            }
+            /* icp::reduceKernel / newReduce, icp.cpp:45-204: 8 row-interleaved partials */
+            for (int b = 0; b < 8; ++b) {
+                float s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0, s8 = 0,
+                      s9 = 0, s10 = 0, s11 = 0, s12 = 0, s13 = 0, s14 = 0, s15 = 0, s16 = 0,
+                      s17 = 0, s18 = 0, s19 = 0, s20 = 0, s21 = 0, s22 = 0, s23 = 0, s24 = 0,
+                      s25 = 0, s26 = 0, s27 = 0, s28 = 0, s29 = 0, s30 = 0, s31 = 0;
+#pragma omp parallel for reduction(+ : s0, s1, s2, s3, s4, s5, s6, s7, s8, s9, s10, s11, s12, s13, s14, s15, s16, s17, s18, s19, s20, s21, s22, s23, s24, s25, s26, s27, s28, s29, s30, s31)
+                for (int y = b; y < h; y += 8) {
+                    for (int x = 0; x < w; x++) {
+                        const IcpRow& r = rows[(size_t) x + (size_t) y * W];
+                        if (r.result < kSuccess) {
+                            s29 += r.result == kDistThreshold ? 1 : 0;
+                            s30 += r.result == kNormalThreshold ? 1 : 0;
+                            s31 += r.result > kDistThreshold ? 1 : 0;
+                            continue;
+                        }
+                        const float e = r.error;
+                        const float* J = r.J;
+                        s0 += e * e;
+                        s1 += e * J[0];
+                        s2 += e * J[1];
+                        s3 += e * J[2];
+                        s4 += e * J[3];
+                        s5 += e * J[4];
+                        s6 += e * J[5];
+                        s7 += J[0] * J[0];
+                        s8 += J[0] * J[1];
+                        s9 += J[0] * J[2];
+                        s10 += J[0] * J[3];
+                        s11 += J[0] * J[4];
+                        s12 += J[0] * J[5];
+                        s13 += J[1] * J[1];
+                        s14 += J[1] * J[2];
+                        s15 += J[1] * J[3];
+                        s16 += J[1] * J[4];
+                        s17 += J[1] * J[5];
+                        s18 += J[2] * J[2];
+                        s19 += J[2] * J[3];
+                        s20 += J[2] * J[4];
+                        s21 += J[2] * J[5];
+                        s22 += J[3] * J[3];
+                        s23 += J[3] * J[4];
+                        s24 += J[3] * J[5];
+                        s25 += J[4] * J[4];
+                        s26 += J[4] * J[5];
+                        s27 += J[5] * J[5];
+                        s28 += 1;
+                    }
+                }
+                const float vals[32] = {s0,  s1,  s2,  s3,  s4,  s5,  s6,  s7,  s8,  s9,  s10,
+                                        s11, s12, s13, s14, s15, s16, s17, s18, s19, s20, s21,
+                                        s22, s23, s24, s25, s26, s27, s28, s29, s30, s31};
+                for (int k = 0; k < 32; ++k)
+                    red[b][k] = vals[k];
+            }
+            for (int j = 1; j < 8; ++j)
+                for (int k = 0; k < 32; ++k)
+                    red[0][k] += red[j][k];
+
+            /* icp::updatePoseKernel + solve/makeJTJ, icp.cpp:15-41,208-223 */
+            const float* v = &red[0][1];
+            float b6[6] = {v[0], v[1], v[2], v[3], v[4], v[5]};
+            float C[6][6];
+            int k = 6;
+            for (int r = 0; r < 6; ++r)
+                for (int c = r; c < 6; ++c)
+                    C[r][c] = v[k++];
+            for (int r = 1; r < 6; ++r)
+                for (int c = 0; c < r; ++c)
+                    C[r][c] = C[c][r];
+            float x6[6] = {0, 0, 0, 0, 0, 0};
+            if (!llt_solve6(C, b6, x6))
+                for (int q = 0; q < 6; ++q)
+                    x6[q] = 0.0f;
+            const Tf delta = se3_exp(x6);
+            T_WS = compose(delta, T_WS);
+            float xn2 = 0.0f;
+            for (int q = 0; q < 6; ++q)
+                xn2 += x6[q] * x6[q];
+            if (std::sqrt(xn2) < cfg->icp_threshold)
+                break;
+        }
+    }
+    /* icp::checkPoseKernel, icp.cpp:227-246 */
+    int accepted = 1;
+    if (((double) std::sqrt(red[0][0] / red[0][28]) > 2e-2)
+        || (red[0][28] / (float) (W * H) < cfg->track_threshold)) {
+        T_WS = T_WS_ref;
+        accepted = 0;
+    }
+    tf_to16(T_WS, T_WS_m);
+    if (stats) {
+        for (int l = 0; l < 3; ++l)
+            stats->converged_iterations[l] = iters_run[l];
+        stats->accepted = accepted;
+        for (int q = 0; q < 32; ++q)
+            stats->reduction[q] = red[0][q];
+    }
+    return accepted;
+}
+
+long long so_map_num_blocks(const so_map* map) { return (long long) map->octree.blocks.size(); }
+
+void so_map_blocks(const so_map* map, uint64_t* keys, int32_t* coords, float* tsdf,
+                   float* weight, int32_t* timestamps)
+{
+    const Octree& oct = map->octree;
+    for (size_t i = 0; i < oct.blocks.size(); ++i) {
+        const Octant& oc = oct.octants[oct.block_octant[i]];
+        if (keys)
+            keys[i] = encode_key(oc.coord[0], oc.coord[1], oc.coord[2], kMaxBlockScale);
+        if (coords) {
+            coords[3 * i + 0] = oc.coord[0];
+            coords[3 * i + 1] = oc.coord[1];
+            coords[3 * i + 2] = oc.coord[2];
+        }
+        if (tsdf)
+            std::memcpy(tsdf + i * kBlockVoxels, oct.blocks[oc.block].tsdf, sizeof(float) * kBlockVoxels);
+        if (weight)
+            std::memcpy(weight + i * kBlockVoxels, oct.blocks[oc.block].weight, sizeof(float) * kBlockVoxels);
+        if (timestamps)
+            timestamps[i] = oc.timestamp;
+    }
+}
+
+int so_map_aabb(const so_map* map, int32_t mn[3], int32_t mx[3])
+{
+    const Octree& oct = map->octree;
+    if (oct.aabb_empty)
+        return 0;
+    for (int i = 0; i < 3; ++i) {
+        mn[i] = oct.aabb_min[i];
+        mx[i] = oct.aabb_max[i];
+    }
+    return 1;
+}
+
+void so_map_set_block(so_map* map, const int32_t c[3], const float* tsdf512, const float* weight512)
+{
+    int o;
+    map->octree.allocate_key(encode_key(c[0], c[1], c[2], 0), o);
+    BlockData& b = map->octree.blocks[map->octree.octants[o].block];
+    if (tsdf512)
+        std::memcpy(b.tsdf, tsdf512, sizeof(float) * kBlockVoxels);
+    if (weight512)
+        std::memcpy(b.weight, weight512, sizeof(float) * kBlockVoxels);
+}
+
+int so_map_get_data(const so_map* map, const float p[3], float* tsdf, float* weight)
+{
+    float t, w;
+    map_get_data(*map, v3(p[0], p[1], p[2]), t, w);
+    *tsdf = t;
+    *weight = w;
+    return w != 0.0f;
+}
+
+int so_map_get_field_interp(const so_map* map, const float p[3], float* value)
+{
+    float v;
+    if (!map_field_interp(*map, v3(p[0], p[1], p[2]), v))
+        return 0;
+    *value = v;
+    return 1;
+}
+
+int so_map_get_field_grad(const so_map* map, const float p[3], float grad[3])
+{
+    V3 g;
+    if (!map_field_grad(*map, v3(p[0], p[1], p[2]), g))
+        return 0;
+    grad[0] = g.x;
+    grad[1] = g.y;
+    grad[2] = g.z;
+    return 1;
+}
+
+int so_first_block_tmin(const so_map* map, const float o[3], const float d[3], float t_near,
+                        float t_far, float* tcmin)
+{
+    const RayBlockHit r =
+        first_block_on_ray(*map, v3(o[0], o[1], o[2]), v3(d[0], d[1], d[2]), t_near, t_far);
+    *tcmin = r.tcmin;
+    return r.found ? 1 : 0;
+}
+
+uint64_t so_expand(uint64_t value) { return morton_expand(value); }
+uint64_t so_compact(uint64_t value) { return morton_compact(value); }
+uint64_t so_encode_code(int32_t x, int32_t y, int32_t z) { return encode_code(x, y, z); }
+void so_decode_code(uint64_t code, int32_t coord[3])
+{
+    int c[3];
+    decode_code(code, c);
+    coord[0] = c[0];
+    coord[1] = c[1];
+    coord[2] = c[2];
+}
+int so_encode_key(int32_t x, int32_t y, int32_t z, uint64_t scale, uint64_t* key)
+{
+    const uint64_t detailed = encode_code(x, y, z);
+    const uint64_t code = detailed & kCodeMask[scale];
+    *key = (code << kScaleOffset) | scale;
+    return detailed == code;
+}
+void so_decode_key(uint64_t key, int32_t coord[3], uint64_t* scale)
+{
+    *scale = key_to_scale(key);
+    so_decode_code(key_to_code(key), coord);
+}
+uint64_t so_code_to_child_idx(uint64_t code, uint64_t child_scale)
+{
+    return (code >> (child_scale * 3)) & 7;
+}
+uint64_t so_parent_key(uint64_t key)
+{
+    const uint64_t ps = key_to_scale(key) + 1;
+    return (key & (kCodeMask[ps] << kScaleOffset)) | ps;
+}
+int so_key_at_scale(uint64_t key, uint64_t scale, uint64_t* out)
+{
+    return key_at_scale(key, scale, *out) ? 1 : 0;
+}
+int so_code_at_scale(uint64_t key, uint64_t scale, uint64_t* out)
+{
+    *out = key_to_code(key) & kCodeMask[scale];
+    return key_to_scale(key) <= scale;
+}
+uint64_t so_block_key(uint64_t key, uint64_t max_block_scale)
+{
+    return block_key_of(key, max_block_scale);
+}
+uint64_t so_block_code(uint64_t key, uint64_t max_block_scale)
+{
+    return key_to_code(key) & kCodeMask[max_block_scale];
+}
+int so_is_child(uint64_t parent_key, uint64_t child_key)
+{
+    return is_child_key(parent_key, child_key) ? 1 : 0;
+}
+int so_is_siblings(uint64_t a, uint64_t b)
+{
+    const uint64_t sa = key_to_scale(a), sb = key_to_scale(b);
+    if (sa != sb)
+        return 0;
+    const uint64_t ps = sa + 1;
+    return ((key_to_code(a) & kCodeMask[ps]) ^ (key_to_code(b) & kCodeMask[ps])) == 0;
+}
+long long so_unique_keys(uint64_t* keys, long long n, uint64_t* out)
+{
+    if (n == 0)
+        return 0;
+    std::sort(keys, keys + n);
+    long long m = 0;
+    out[m++] = keys[0];
+    for (long long i = 0; i < n; ++i)
+        if (out[m - 1] != keys[i])
+            out[m++] = keys[i];
+    return m;
+}
+long long so_unique_codes(uint64_t* keys, long long n, uint64_t* out)
+{
+    if (n == 0)
+        return 0;
+    std::sort(keys, keys + n);
+    long long m = 0;
+    out[m++] = keys[0];
+    for (long long i = 0; i < n; ++i) {
+        if (key_to_code(out[m - 1]) != key_to_code(keys[i]))
+            out[m++] = keys[i];
+        else if (key_to_scale(out[m - 1]) > key_to_scale(keys[i]))
+            out[m - 1] = keys[i];
+    }
+    return m;
+}
+long long so_unique_allocation(uint64_t* keys, long long n, uint64_t max_block_scale, uint64_t* out)
+{
+    if (n == 0)
+        return 0;
+    std::sort(keys, keys + n);
+    long long m = 0;
+    out[m++] = block_key_of(keys[0], max_block_scale);
+    for (long long i = 0; i < n; ++i) {
+        const uint64_t bk = block_key_of(keys[i], max_block_scale);
+        if (is_child_key(out[m - 1], bk))
+            out[m - 1] = bk;
+        else if (out[m - 1] != bk)
+            out[m++] = bk;
+    }
+    return m;
+}
+long long so_unique_at_scale(uint64_t* keys, long long n, uint64_t scale, uint64_t* out)
+{
+    if (n == 0)
+        return 0;
+    std::sort(keys, keys + n);
+    long long m = 0;
+    long long restart = 1;
+    uint64_t k;
+    for (long long i = 0; i < n; ++i) {
+        if (key_at_scale(keys[i], scale, k)) {
+            out[m++] = k;
+            break;
+        }
+        ++restart;
+    }
+    for (long long i = restart; i < n; ++i) {
+        if (key_at_scale(keys[i], scale, k) && out[m - 1] != k)
+            out[m++] = k;
+    }
+    return m;
+}
+
+void so_se3_exp(const float twist[6], float T[16]) { tf_to16(se3_exp(twist), T); }
+
+void so_half_sample_robust(const float* in, int w, int h, float e_d, int radius, float* out)
+{
+    half_sample_robust(in, w, h, e_d, radius, out);
+}
+void so_depth_to_point_cloud(const float* depth, const so_pinhole* sensor, float* pts)
+{
+    depth_to_points(depth, make_pinhole(sensor), reinterpret_cast<V3*>(pts));
+}
+void so_point_cloud_to_normal(const float* pts, int w, int h, int neg_y, float* nrm)
+{
+    points_to_normals(reinterpret_cast<const V3*>(pts), w, h, neg_y != 0, reinterpret_cast<V3*>(nrm));
+}
+
+} /* extern "C" */

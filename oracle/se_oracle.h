@@ -1,0 +1,153 @@
+/*
+ * se_oracle.h — C interface of the CPU oracle for the supereight2 dense-mapping hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This library is the checker that the GPU product is compared
+ * against, and the timed CPU baseline. Only tests, the smoke check and the benchmark's CPU
+ * baseline leg may load it. The product library (libse_gpu) never links or calls it.
+ *
+ * It is a CPU restatement, in C++17 + OpenMP, of these reference paths (paths relative to the
+ * supereight2 source tree):
+ *   - Morton key operations        include/se/map/utils/impl/key_util_impl.hpp:44-436
+ *   - Map transforms / octree size include/se/map/impl/map_impl.hpp:37-55,494-590;
+ *                                  include/se/map/octree/impl/octree_impl.hpp:14-19
+ *   - RaycastCarver allocation     include/se/integrator/allocator/impl/raycast_carver_impl.hpp:17-128
+ *   - octree allocation            include/se/map/octree/impl/allocator_impl.hpp:68-147,
+ *                                  include/se/map/octree/impl/octree_impl.hpp:171-199
+ *   - FrustumIterator              include/se/map/octree/iterator.hpp:197-235,
+ *                                  include/se/map/octree/impl/iterator_impl.hpp:88-160
+ *   - single-res TSDF update       include/se/integrator/updater/impl/singleres_tsdf_updater_impl.hpp:14-132,
+ *                                  include/se/map/impl/data_field_impl.hpp:39-54
+ *   - raycast_volume (TSDF)        include/se/map/impl/raycaster_impl.hpp:456-627
+ *   - VoxelBlockRayIterator        include/se/map/octree/impl/voxel_block_ray_iterator_impl.hpp:19-249
+ *   - visitor interp / gradient    include/se/map/octree/impl/visitor_impl.hpp:67-302,704-717,976-1251
+ *   - Tracker / ICP                include/se/tracker/impl/tracker_impl.hpp:30-116,
+ *                                  include/se/tracker/impl/icp_impl.hpp:16-102, src/tracker/icp.cpp:15-246
+ *   - preprocessing                src/map/preprocessor.cpp:109-195,
+ *                                  include/se/map/impl/preprocessor_impl.hpp:18-40
+ *   - se(3) exponential            include/se/common/impl/math_util_impl.hpp:104-174
+ *   - PinholeCamera                src/sensor/pinhole_camera.cpp:29-39,95-111,189-310,
+ *                                  include/se/sensor/impl/pinhole_camera_impl.hpp:15-32
+ *
+ * All matrices cross this interface as row-major float[16] (4x4 homogeneous).
+ * Images are row-major, pixel (x, y) at index x + y * width; 3-vectors are packed xyz floats.
+ */
+#ifndef SE_ORACLE_H
+#define SE_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct so_map so_map;
+
+typedef struct {
+    int width;
+    int height;
+    float fx, fy, cx, cy;
+    float near_plane;
+    float far_plane;
+} so_pinhole;
+
+typedef struct {
+    int num_levels;     /* pyramid levels, at most 3 */
+    int iterations[3];  /* per level, finest first: reference default {10, 5, 4} */
+    float dist_threshold;
+    float normal_threshold;
+    float track_threshold;
+    float icp_threshold;
+} so_tracker_config;
+
+typedef struct {
+    long long n_valid_pixels;   /* pixels that passed the near/far test of the carver */
+    long long n_new_blocks;     /* blocks allocated by this call */
+    long long n_frustum_blocks; /* previously allocated blocks returned by the frustum fetch */
+    long long n_updated_voxels; /* voxels whose field update returned true */
+} so_integrate_stats;
+
+typedef struct {
+    int converged_iterations[3]; /* iterations actually run per level */
+    int accepted;                /* checkPoseKernel result */
+    float reduction[32];         /* final 32-float reduction (row 0 of the 8x32 buffer) */
+} so_track_stats;
+
+void so_set_num_threads(int n);
+int so_get_num_threads(void);
+
+/* Map<Data<TSDF>, Res::Single, 8>. T_MW may be NULL (reference default: translation dim/2). */
+so_map* so_map_create(const float dim[3], float res, float truncation_boundary_factor,
+                      float max_weight, const float* T_MW);
+void so_map_destroy(so_map* map);
+int so_map_size(const so_map* map);
+float so_map_dim(const so_map* map);
+
+/* se::MapIntegrator::integrateDepth for a TSDF single-res map and a pinhole camera. */
+void so_integrate_depth(so_map* map, const float* depth, const so_pinhole* sensor,
+                        const float T_WC[16], int timestamp, so_integrate_stats* stats);
+
+/* se::raycaster::raycast_volume. pts/nrm are width*height*3 floats, scale width*height. */
+void so_raycast_volume(const so_map* map, const so_pinhole* sensor, const float T_WS[16],
+                       float* pts_W, float* nrm_W, int8_t* scale);
+
+/* se::Tracker::track(depth, T_WS, pts, nrm). T_WS is updated in place; returns acceptance. */
+int so_track(const so_pinhole* sensor, const so_tracker_config* config, const float* depth,
+             float T_WS[16], const float* ref_pts_W, const float* ref_nrm_W,
+             so_track_stats* stats);
+
+/* Map inspection. */
+long long so_map_num_blocks(const so_map* map);
+/* keys: uint64 block keys (Morton code << 5 | scale 3); coords: 3 ints per block;
+ * tsdf / weight: 512 floats per block in x + 8y + 64z order. Any pointer may be NULL. */
+void so_map_blocks(const so_map* map, uint64_t* keys, int32_t* coords, float* tsdf,
+                   float* weight, int32_t* timestamps);
+/* Allocated-block AABB in voxel coordinates, inclusive; returns 0 when empty. */
+int so_map_aabb(const so_map* map, int32_t mn[3], int32_t mx[3]);
+/* Allocate the block containing voxel_coord (through the normal allocator) and overwrite its
+ * 512 voxels. */
+void so_map_set_block(so_map* map, const int32_t voxel_coord[3], const float* tsdf512,
+                      const float* weight512);
+int so_map_get_data(const so_map* map, const float point_W[3], float* tsdf, float* weight);
+int so_map_get_field_interp(const so_map* map, const float point_W[3], float* value);
+int so_map_get_field_grad(const so_map* map, const float point_W[3], float grad[3]);
+/* Distance (metres) to the first allocated block along a ray, as VoxelBlockRayIterator::tcmin()
+ * reports it after the first next(); returns 0 if next() returned no block. */
+int so_first_block_tmin(const so_map* map, const float origin_W[3], const float dir_W[3],
+                        float t_near, float t_far, float* tcmin);
+
+/* Morton key operations (key_util_impl.hpp). */
+uint64_t so_expand(uint64_t value);
+uint64_t so_compact(uint64_t value);
+uint64_t so_encode_code(int32_t x, int32_t y, int32_t z);
+void so_decode_code(uint64_t code, int32_t coord[3]);
+/* Returns 1 when no detail is lost at that scale (encode_key's bool). */
+int so_encode_key(int32_t x, int32_t y, int32_t z, uint64_t scale, uint64_t* key);
+void so_decode_key(uint64_t key, int32_t coord[3], uint64_t* scale);
+uint64_t so_code_to_child_idx(uint64_t code, uint64_t child_scale);
+uint64_t so_parent_key(uint64_t key);
+int so_key_at_scale(uint64_t key, uint64_t scale, uint64_t* key_at_scale);
+int so_code_at_scale(uint64_t key, uint64_t scale, uint64_t* code_at_scale);
+uint64_t so_block_key(uint64_t key, uint64_t max_block_scale);
+uint64_t so_block_code(uint64_t key, uint64_t max_block_scale);
+int so_is_child(uint64_t parent_key, uint64_t child_key);
+int so_is_siblings(uint64_t a, uint64_t b);
+/* The unique_* helpers sort keys in place; they return the number of unique keys written. */
+long long so_unique_keys(uint64_t* keys, long long n, uint64_t* out);
+long long so_unique_codes(uint64_t* keys, long long n, uint64_t* out);
+long long so_unique_allocation(uint64_t* keys, long long n, uint64_t max_block_scale,
+                               uint64_t* out);
+long long so_unique_at_scale(uint64_t* keys, long long n, uint64_t scale, uint64_t* out);
+
+/* se(3) exponential of a twist [rho; omega] as a row-major 4x4 (math_util_impl.hpp:117-174). */
+void so_se3_exp(const float twist[6], float T[16]);
+
+/* Preprocessing helpers exposed for tests. */
+void so_half_sample_robust(const float* in, int w, int h, float e_d, int radius, float* out);
+void so_depth_to_point_cloud(const float* depth, const so_pinhole* sensor, float* pts);
+void so_point_cloud_to_normal(const float* pts, int w, int h, int neg_y, float* nrm);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SE_ORACLE_H */

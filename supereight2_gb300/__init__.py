@@ -1,0 +1,362 @@
+"""supereight2_gb300 — GB300 (sm_103a) implementation of supereight2's per-frame mapping path.
+
+The compute lives in ``libse_gpu.so`` (hand-written CUDA kernels behind the C ABI of
+``include/se_gpu.h``). This module is the Python mirror of the reference's interface for that
+path, with the reference's names and argument meaning:
+
+    Map(dim, res, ...)                                  se::TSDFMap<se::Res::Single>
+    MapIntegrator(map).integrateDepth(ts, depth, sensor, T_WC)
+                                                        se::MapIntegrator::integrateDepth
+    raycast_volume(map, sensor, T_WS, pts, nrm, scale)  se::raycaster::raycast_volume
+    Tracker(map, sensor, config).track(depth, T_WS, pts, nrm) -> bool
+                                                        se::Tracker::track
+
+Device images are torch CUDA tensors (float32 depth [H, W], float32 points/normals [H, W, 3],
+int8 scale [H, W]); poses are 4x4 arrays (T_WC maps camera to world). There is no CPU
+fallback: without the built library or a GPU every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "raycast_volume",
+           "SeGpuError", "library", "library_path"]
+
+
+class SeGpuError(RuntimeError):
+    """A libse_gpu call returned a status other than SE_GPU_OK."""
+
+
+class _MapConfig(C.Structure):
+    _fields_ = [("dim", C.c_float * 3), ("res", C.c_float), ("T_MW", C.c_float * 16),
+                ("has_T_MW", C.c_int), ("field", C.c_int), ("res_type", C.c_int),
+                ("storage", C.c_int), ("truncation_boundary_factor", C.c_float),
+                ("max_weight", C.c_float), ("max_blocks", C.c_int64)]
+
+
+class _Pinhole(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("fx", C.c_float), ("fy", C.c_float),
+                ("cx", C.c_float), ("cy", C.c_float), ("near_plane", C.c_float),
+                ("far_plane", C.c_float)]
+
+
+class _TrackerConfig(C.Structure):
+    _fields_ = [("num_levels", C.c_int), ("iterations", C.c_int * 3),
+                ("dist_threshold", C.c_float), ("normal_threshold", C.c_float),
+                ("track_threshold", C.c_float), ("icp_threshold", C.c_float)]
+
+
+class _IntegrateStats(C.Structure):
+    _fields_ = [("n_new_blocks", C.c_int64), ("n_listed_blocks", C.c_int64),
+                ("n_updated_voxels", C.c_int64), ("n_valid_pixels", C.c_int64)]
+
+
+# Every symbol include/se_gpu.h declares, with its ctypes signature.
+_VP = C.c_void_p
+_F16 = C.POINTER(C.c_float)
+SIGNATURES = {
+    "se_gpu_last_error": (C.c_char_p, []),
+    "se_gpu_status_string": (C.c_char_p, [C.c_int]),
+    "se_gpu_abi_version": (C.c_int, []),
+    "se_gpu_map_create": (C.c_int, [C.POINTER(_MapConfig), C.POINTER(_VP)]),
+    "se_gpu_map_destroy": (C.c_int, [_VP]),
+    "se_gpu_map_size": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
+    "se_gpu_map_check": (C.c_int, [_VP]),
+    "se_gpu_integrate_depth": (C.c_int, [_VP, _VP, C.POINTER(_Pinhole), _F16, C.c_int, _VP]),
+    "se_gpu_map_integrate_stats": (C.c_int, [_VP, C.POINTER(_IntegrateStats)]),
+    "se_gpu_raycast": (C.c_int, [_VP, C.POINTER(_Pinhole), _F16, _VP, _VP, _VP, _VP]),
+    "se_gpu_map_download_blocks": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP,
+                                             C.POINTER(C.c_int64)]),
+    "se_gpu_map_upload_blocks": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP]),
+    "se_gpu_map_field_interp": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP]),
+    "se_gpu_map_field_grad": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP]),
+    "se_gpu_map_aabb": (C.c_int, [_VP, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_int)]),
+    "se_gpu_tracker_create": (C.c_int, [C.POINTER(_Pinhole), C.POINTER(_TrackerConfig),
+                                        C.POINTER(_VP)]),
+    "se_gpu_tracker_destroy": (C.c_int, [_VP]),
+    "se_gpu_track": (C.c_int, [_VP, _VP, _VP, _VP, _F16, C.POINTER(C.c_int), _VP]),
+    "se_gpu_tracker_last_reduction": (C.c_int, [_VP, _F16, C.POINTER(C.c_int)]),
+    "se_gpu_profiling_enable": (C.c_int, [C.c_int]),
+    "se_gpu_profiling_read": (C.c_int, [C.c_int, _VP, _VP, C.c_int]),
+    "se_gpu_profiling_name": (C.c_char_p, [C.c_int]),
+    "se_gpu_profiling_count": (C.c_int, []),
+}
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def library(build_if_missing: bool = True):
+    """Load libse_gpu.so (building it with nvcc if it is missing or stale)."""
+    global _lib
+    if _lib is None:
+        path = _build.build() if build_if_missing else _build.LIB_PATH
+        if not os.path.exists(path):
+            raise SeGpuError(f"libse_gpu.so not found at {path}: run supereight2_gb300/build.py")
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int, what: str):
+    if status != 0:
+        L = library()
+        raise SeGpuError(f"{what}: {L.se_gpu_status_string(status).decode()} "
+                         f"({L.se_gpu_last_error().decode()})")
+
+
+def _m16(T):
+    a = np.ascontiguousarray(np.asarray(T, dtype=np.float32).reshape(16))
+    return a, a.ctypes.data_as(_F16)
+
+
+def _stream(stream):
+    if stream is not None:
+        return C.c_void_p(int(stream))
+    import torch
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _dptr(t, dtype, shape=None, name="tensor"):
+    import torch
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise SeGpuError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype or not t.is_contiguous():
+        raise SeGpuError(f"{name} must be a contiguous {dtype} tensor")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise SeGpuError(f"{name} has shape {tuple(t.shape)}, expected {tuple(shape)}")
+    return C.c_void_p(t.data_ptr())
+
+
+class PinholeCamera:
+    """se::PinholeCamera::Config: width, height, fx, fy, cx, cy, near_plane, far_plane."""
+
+    def __init__(self, width, height, fx, fy, cx, cy, near_plane=0.01, far_plane=10.0):
+        self.width, self.height = int(width), int(height)
+        self.fx, self.fy, self.cx, self.cy = float(fx), float(fy), float(cx), float(cy)
+        self.near_plane, self.far_plane = float(near_plane), float(far_plane)
+
+    @classmethod
+    def from_spec(cls, s):
+        return cls(s.width, s.height, s.fx, s.fy, s.cx, s.cy, s.near_plane, s.far_plane)
+
+    def _c(self) -> _Pinhole:
+        return _Pinhole(self.width, self.height, self.fx, self.fy, self.cx, self.cy,
+                        self.near_plane, self.far_plane)
+
+
+class TrackerConfig:
+    """se::TrackerConfig (include/se/tracker/tracker.hpp:22-33) defaults."""
+
+    def __init__(self, iterations=(10, 5, 4), dist_threshold=0.1, normal_threshold=0.8,
+                 track_threshold=0.15, icp_threshold=1e-5):
+        self.iterations = tuple(int(i) for i in iterations)
+        self.dist_threshold = float(dist_threshold)
+        self.normal_threshold = float(normal_threshold)
+        self.track_threshold = float(track_threshold)
+        self.icp_threshold = float(icp_threshold)
+
+    def _c(self) -> _TrackerConfig:
+        it = list(self.iterations) + [0] * (3 - len(self.iterations))
+        return _TrackerConfig(len(self.iterations), (C.c_int * 3)(*it), self.dist_threshold,
+                              self.normal_threshold, self.track_threshold, self.icp_threshold)
+
+
+class Map:
+    """se::TSDFMap<se::Res::Single> on the GPU: block hash + block pool of 8^3 voxels."""
+
+    def __init__(self, dim, res, truncation_boundary_factor=8.0, max_weight=100.0,
+                 storage="f32", max_blocks=1 << 20, T_MW=None):
+        cfg = _MapConfig()
+        d = np.broadcast_to(np.asarray(dim, np.float32), (3,))
+        cfg.dim = (C.c_float * 3)(*[float(v) for v in d])
+        cfg.res = float(res)
+        if T_MW is not None:
+            cfg.T_MW = (C.c_float * 16)(*[float(v) for v in np.asarray(T_MW, np.float32).reshape(16)])
+            cfg.has_T_MW = 1
+        cfg.field = 0
+        cfg.res_type = 0
+        cfg.storage = {"f32": 0, "f16": 1}[storage]
+        cfg.truncation_boundary_factor = float(truncation_boundary_factor)
+        cfg.max_weight = float(max_weight)
+        cfg.max_blocks = int(max_blocks)
+        self._L = library()
+        h = C.c_void_p()
+        _check(self._L.se_gpu_map_create(C.byref(cfg), C.byref(h)), "se_gpu_map_create")
+        self.h = h
+        self.res = float(res)
+        self.storage = storage
+        self.max_blocks = int(max_blocks)
+        self.truncation_boundary_factor = float(truncation_boundary_factor)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self._L.se_gpu_map_destroy(h)
+            self.h = None
+
+    @property
+    def size(self) -> int:
+        s, d = C.c_int(), C.c_float()
+        _check(self._L.se_gpu_map_size(self.h, C.byref(s), C.byref(d)), "se_gpu_map_size")
+        return s.value
+
+    @property
+    def dim(self) -> float:
+        s, d = C.c_int(), C.c_float()
+        _check(self._L.se_gpu_map_size(self.h, C.byref(s), C.byref(d)), "se_gpu_map_size")
+        return d.value
+
+    def check(self):
+        """Synchronise and raise on a latched device-side error (pool full, probe limit)."""
+        _check(self._L.se_gpu_map_check(self.h), "se_gpu_map_check")
+
+    def integrate_stats(self) -> dict:
+        st = _IntegrateStats()
+        _check(self._L.se_gpu_map_integrate_stats(self.h, C.byref(st)), "integrate_stats")
+        return {"n_new_blocks": st.n_new_blocks, "n_listed_blocks": st.n_listed_blocks,
+                "n_updated_voxels": st.n_updated_voxels, "n_valid_pixels": st.n_valid_pixels}
+
+    def num_blocks(self) -> int:
+        n = C.c_int64()
+        _check(self._L.se_gpu_map_download_blocks(self.h, 0, None, None, None, None, None,
+                                                  C.byref(n)), "download_blocks")
+        return n.value
+
+    def download_blocks(self, voxels=True):
+        """(keys u64[N], coords i32[N,3], tsdf f32[N,512], weight f32[N,512], ts i32[N])."""
+        n = self.num_blocks()
+        keys = np.zeros(n, np.uint64)
+        coords = np.zeros((n, 3), np.int32)
+        ts = np.zeros(n, np.int32)
+        tsdf = np.zeros((n, 512), np.float32) if voxels else None
+        weight = np.zeros((n, 512), np.float32) if voxels else None
+        cnt = C.c_int64()
+        if n:
+            _check(self._L.se_gpu_map_download_blocks(
+                self.h, n, keys.ctypes.data, coords.ctypes.data,
+                tsdf.ctypes.data if voxels else None, weight.ctypes.data if voxels else None,
+                ts.ctypes.data, C.byref(cnt)), "download_blocks")
+        return keys, coords, tsdf, weight, ts
+
+    def upload_blocks(self, keys, tsdf, weight):
+        """Allocate the blocks with these keys (Morton code << 5 | 3) and overwrite their voxels."""
+        keys = np.ascontiguousarray(keys, np.uint64)
+        tsdf = np.ascontiguousarray(np.broadcast_to(np.asarray(tsdf, np.float32), (len(keys), 512)))
+        weight = np.ascontiguousarray(np.broadcast_to(np.asarray(weight, np.float32), (len(keys), 512)))
+        _check(self._L.se_gpu_map_upload_blocks(self.h, len(keys), keys.ctypes.data,
+                                                tsdf.ctypes.data, weight.ctypes.data),
+               "se_gpu_map_upload_blocks")
+
+    def getFieldInterp(self, points_W, stream=None):
+        """Map::getFieldInterp for a CUDA [N, 3] float32 tensor: (values [N], valid [N] bool)."""
+        return self._field_query(points_W, stream, grad=False)
+
+    def getFieldGrad(self, points_W, stream=None):
+        """Map::getFieldGrad for a CUDA [N, 3] float32 tensor: (grads [N, 3], valid [N] bool)."""
+        return self._field_query(points_W, stream, grad=True)
+
+    def _field_query(self, points_W, stream, grad):
+        import torch
+        n = points_W.shape[0]
+        p = _dptr(points_W, torch.float32, (n, 3), "points_W")
+        out = torch.zeros((n, 3) if grad else (n,), dtype=torch.float32, device=points_W.device)
+        valid = torch.zeros(n, dtype=torch.int32, device=points_W.device)
+        fn = self._L.se_gpu_map_field_grad if grad else self._L.se_gpu_map_field_interp
+        _check(fn(self.h, n, p, C.c_void_p(out.data_ptr()), C.c_void_p(valid.data_ptr()),
+                  _stream(stream)), "field query")
+        return out, valid.bool()
+
+    def aabb(self):
+        mn = (C.c_int32 * 3)()
+        mx = (C.c_int32 * 3)()
+        empty = C.c_int()
+        _check(self._L.se_gpu_map_aabb(self.h, mn, mx, C.byref(empty)), "se_gpu_map_aabb")
+        return None if empty.value else (np.array(mn[:], np.int32), np.array(mx[:], np.int32))
+
+
+class MapIntegrator:
+    """se::MapIntegrator<TSDFMap<Res::Single>>."""
+
+    def __init__(self, map: Map):
+        self.map = map
+
+    def integrateDepth(self, timestamp, depth, sensor: PinholeCamera, T_WC, stream=None):
+        import torch
+        ptr = _dptr(depth, torch.float32, (sensor.height, sensor.width), "depth")
+        s = sensor._c()
+        _, tp = _m16(T_WC)
+        L = self.map._L
+        _check(L.se_gpu_integrate_depth(self.map.h, ptr, C.byref(s), tp, int(timestamp),
+                                        _stream(stream)), "se_gpu_integrate_depth")
+
+
+def raycast_volume(map: Map, sensor: PinholeCamera, T_WS, surface_point_cloud_W,
+                   surface_normals_W, surface_scale=None, stream=None):
+    """se::raycaster::raycast_volume into preallocated device images."""
+    import torch
+    shp = (sensor.height, sensor.width, 3)
+    p = _dptr(surface_point_cloud_W, torch.float32, shp, "surface_point_cloud_W")
+    n = _dptr(surface_normals_W, torch.float32, shp, "surface_normals_W")
+    sc = None
+    if surface_scale is not None:
+        sc = _dptr(surface_scale, torch.int8, shp[:2], "surface_scale")
+    s = sensor._c()
+    _, tp = _m16(T_WS)
+    _check(map._L.se_gpu_raycast(map.h, C.byref(s), tp, p, n, sc, _stream(stream)),
+           "se_gpu_raycast")
+
+
+class Tracker:
+    """se::Tracker<MapT, PinholeCamera>: 3-level projective point-to-plane ICP."""
+
+    def __init__(self, map: Map, sensor: PinholeCamera, config: TrackerConfig = None):
+        self.map = map
+        self.sensor = sensor
+        self.config = config or TrackerConfig()
+        self._L = library()
+        h = C.c_void_p()
+        s = sensor._c()
+        c = self.config._c()
+        _check(self._L.se_gpu_tracker_create(C.byref(s), C.byref(c), C.byref(h)),
+               "se_gpu_tracker_create")
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self._L.se_gpu_tracker_destroy(h)
+            self.h = None
+
+    def track(self, depth, T_WS, surface_point_cloud_W, surface_normals_W, stream=None):
+        """Track depth against the raycast taken at T_WS. T_WS (a float32 4x4 numpy array) is
+        updated in place; returns whether the pose was accepted."""
+        import torch
+        s = self.sensor
+        d = _dptr(depth, torch.float32, (s.height, s.width), "depth")
+        p = _dptr(surface_point_cloud_W, torch.float32, (s.height, s.width, 3), "points")
+        n = _dptr(surface_normals_W, torch.float32, (s.height, s.width, 3), "normals")
+        if not (isinstance(T_WS, np.ndarray) and T_WS.dtype == np.float32 and T_WS.shape == (4, 4)
+                and T_WS.flags.c_contiguous):
+            raise SeGpuError("T_WS must be a C-contiguous float32 4x4 numpy array (updated in place)")
+        acc = C.c_int()
+        _check(self._L.se_gpu_track(self.h, d, p, n, T_WS.ctypes.data_as(_F16), C.byref(acc),
+                                    _stream(stream)), "se_gpu_track")
+        return bool(acc.value)
+
+    def last_reduction(self):
+        red = (C.c_float * 32)()
+        its = (C.c_int * 3)()
+        _check(self._L.se_gpu_tracker_last_reduction(self.h, red, its), "last_reduction")
+        return np.array(red[:], np.float32), list(its[:])

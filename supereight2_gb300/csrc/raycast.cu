@@ -1,0 +1,455 @@
+// raycast.cu — se::raycaster::raycast_volume for single-res TSDF maps.
+//
+// One thread per pixel (an 8 x 4 pixel tile per warp for coherent block lookups):
+//   1. first allocated block on the ray: the sparse-voxel-octree traversal of
+//      VoxelBlockRayIterator (voxel_block_ray_iterator_impl.hpp:19-249, Laine & Karras 2010)
+//      with the same float expressions, but node existence is a bit test in the occupancy
+//      pyramid instead of a child-pointer chase, and the traversal stack keeps only t_max;
+//   2. the TSDF march of raycast<TSDF> (raycaster_impl.hpp:456-533): voxel fetches through the
+//      block hash with a one-block cache, trilinear interpolation near the surface
+//      (visitor_impl.hpp:976-1024) and the linear zero-crossing estimate;
+//   3. the surface normal from the 32-sample central-difference gradient
+//      (visitor_impl.hpp:1094-1251, map_impl.hpp:236-262).
+#include "profile.cuh"
+#include "se_gpu_internal.cuh"
+
+namespace se_gpu {
+
+int device_sm_count();
+
+struct RaycastParams {
+    Tf T_WS;
+    float scaling; // octree size * res
+    float eps;     // 2^-log2(size)
+    int min_scale; // 23 - log2(size / 8)
+};
+
+__device__ __forceinline__ int f_as_i(float f) { return __float_as_int(f); }
+__device__ __forceinline__ float i_as_f(int i) { return __int_as_float(i); }
+__device__ __forceinline__ float fmax_std(float a, float b) { return (a < b) ? b : a; } // std::max
+__device__ __forceinline__ float fmin_std(float a, float b) { return (b < a) ? b : a; } // std::min
+
+// The state of VoxelBlockRayIterator after its first next(): found, tcmin(), tmax().
+__device__ bool first_block(const MapDevice& m, const RaycastParams& rp, F3 o_W, F3 d_W, float near_p,
+                            float far_p, float& tcmin, float& tmax)
+{
+    constexpr int kStackDepth = 23;
+    float d[3] = {d_W.x, d_W.y, d_W.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        if (fabsf(d[a]) < rp.eps)
+            d[a] = copysignf(rp.eps, d[a]);
+    const F3 o_M = apply(m.T_MW, o_W);
+    const float ov[3] = {o_M.x / m.res, o_M.y / m.res, o_M.z / m.res};
+    float t_coef[3], t_bias[3];
+    int mirror_mask = 7;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float o = ov[a] / (float) m.size + 1.0f;
+        t_coef[a] = -1.0f * (1.0f / fabsf(d[a]));
+        t_bias[a] = t_coef[a] * o;
+        if (d[a] > 0.0f) {
+            mirror_mask ^= (1 << a);
+            t_bias[a] = 3.0f * t_coef[a] - t_bias[a];
+        }
+    }
+    float t_min = fmax_std(fmax_std(2.0f * t_coef[0] - t_bias[0], 2.0f * t_coef[1] - t_bias[1]),
+                           2.0f * t_coef[2] - t_bias[2]);
+    float t_max = fmin_std(fmin_std(t_coef[0] - t_bias[0], t_coef[1] - t_bias[1]), t_coef[2] - t_bias[2]);
+    float h = t_max;
+    t_min = fmax_std(t_min, near_p / rp.scaling);
+    t_max = fmin_std(t_max, far_p / rp.scaling);
+    tmax = t_max * rp.scaling;
+
+    int idx = 0;
+    float pos[3] = {1.0f, 1.0f, 1.0f};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (1.5f * t_coef[a] - t_bias[a] > t_min) {
+            idx ^= (1 << a);
+            pos[a] = 1.5f;
+        }
+    }
+    int scale = kStackDepth - 1;
+    float scale_exp2 = 0.5f;
+    float stack_tmax[kStackDepth];
+#pragma unroll
+    for (int i = 0; i < kStackDepth; ++i)
+        stack_tmax[i] = 0.0f;
+
+    // Bounded: each iteration either descends (at most 23 levels between advances) or advances
+    // the ray past a cell boundary; the cap only guards against a malformed map.
+    for (int iter = 0; iter < (1 << 20) && scale < kStackDepth; ++iter) {
+        float tc[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            tc[a] = pos[a] * t_coef[a] - t_bias[a];
+        const float tc_max = fmin_std(fmin_std(tc[0], tc[1]), tc[2]);
+
+        // child at (pos, scale): mirrored cell index from the float bits, then real index
+        const int L = scale - rp.min_scale;
+        bool child = false;
+        if (L >= 0) {
+            const int lg = 23 - scale;
+            const uint32_t n = 1u << lg;
+            uint32_t c[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const uint32_t k = (uint32_t) (f_as_i(pos[a]) - 0x3f800000) >> scale;
+                c[a] = (mirror_mask & (1 << a)) ? k : (n - 1u - k);
+            }
+            // idx ^ mirror_mask ^ 7 picks the same cell as the mirrored position above
+            child = occ_test(m, L, c[0], c[1], c[2]);
+        }
+        if (scale == rp.min_scale && child) {
+            tcmin = t_min * rp.scaling;
+            return true;
+        }
+        if (child && t_min <= t_max) {
+            const float tv_max = fmin_std(t_max, tc_max);
+            const float half = scale_exp2 * 0.5f;
+            float t_centre[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                t_centre[a] = half * t_coef[a] + tc[a];
+            if (tc_max < h)
+                stack_tmax[scale] = t_max;
+            h = tc_max;
+            idx = 0;
+            --scale;
+            scale_exp2 = half;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                if (t_centre[a] > t_min)
+                    idx ^= (1 << a);
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                if (idx & (1 << a))
+                    pos[a] += scale_exp2;
+            t_max = tv_max;
+            continue;
+        }
+        int step_mask = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            if (tc[a] <= tc_max)
+                step_mask |= (1 << a);
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            if (step_mask & (1 << a))
+                pos[a] -= scale_exp2;
+        t_min = tc_max;
+        idx ^= step_mask;
+        if ((idx & step_mask) != 0) {
+            uint32_t differing = 0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                if (step_mask & (1 << a))
+                    differing |= (uint32_t) (f_as_i(pos[a]) ^ f_as_i(pos[a] + scale_exp2));
+            scale = (f_as_i((float) differing) >> 23) - 127;
+            if (scale >= kStackDepth)
+                break;
+            scale_exp2 = i_as_f((scale - kStackDepth + 127) << 23);
+            t_max = stack_tmax[scale];
+            int sh[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                sh[a] = f_as_i(pos[a]) >> scale;
+                pos[a] = i_as_f(sh[a] << scale);
+            }
+            idx = (sh[0] & 1) | ((sh[1] & 1) << 1) | ((sh[2] & 1) << 2);
+            h = 0.0f;
+        }
+    }
+    tcmin = t_min * rp.scaling;
+    return false;
+}
+
+// Block lookup with a one-entry cache of the last block touched by this thread.
+struct BlockCache {
+    int bx, by, bz;
+    int idx; // pool index or -1
+};
+
+__device__ __forceinline__ int lookup_block(const MapDevice& m, BlockCache& c, int vx, int vy, int vz)
+{
+    const int bx = vx >> 3, by = vy >> 3, bz = vz >> 3;
+    if (bx != c.bx || by != c.by || bz != c.bz) {
+        c.bx = bx;
+        c.by = by;
+        c.bz = bz;
+        c.idx = occ_test(m, 0, (uint32_t) bx, (uint32_t) by, (uint32_t) bz) ? hash_find(m, block_key(vx, vy, vz)) : -1;
+    }
+    return c.idx;
+}
+
+// visitor::getData single-res: block voxel or the default data (tsdf 1, weight 0).
+__device__ __forceinline__ bool fetch_voxel(const MapDevice& m, BlockCache& c, int vx, int vy, int vz, float& t,
+                                            float& w)
+{
+    const int b = lookup_block(m, c, vx, vy, vz);
+    if (b < 0) {
+        t = 1.0f;
+        w = 0.0f;
+        return false;
+    }
+    load_voxel(m, b, (vx & 7) + 8 * (vy & 7) + 64 * (vz & 7), t, w);
+    return true;
+}
+
+__device__ __forceinline__ void map_get_data(const MapDevice& m, BlockCache& c, F3 p, float& t, float& w)
+{
+    int vx, vy, vz;
+    if (!point_to_voxel(m, p, vx, vy, vz)) {
+        t = 1.0f;
+        w = 0.0f;
+        return;
+    }
+    fetch_voxel(m, c, vx, vy, vz, t, w);
+}
+
+__device__ bool field_interp(const MapDevice& m, BlockCache& c, F3 p_W, float& out)
+{
+    F3 vf;
+    if (!point_to_voxel_f(m, p_W, vf))
+        return false;
+    const F3 bf = f3(vf.x - 0.5f, vf.y - 0.5f, vf.z - 0.5f);
+    const int b0 = (int) bf.x, b1 = (int) bf.y, b2 = (int) bf.z;
+    if (b0 < 0 || b1 < 0 || b2 < 0 || b0 + 1 >= m.size || b1 + 1 >= m.size || b2 + 1 >= m.size)
+        return false;
+    float f[8], wt[8];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+        if (!fetch_voxel(m, c, b0 + (n & 1), b1 + ((n >> 1) & 1), b2 + ((n >> 2) & 1), f[n], wt[n]))
+            return false;
+    }
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+        if (!(wt[n] != 0.0f))
+            return false;
+    const F3 t = f3(bf.x - floorf(bf.x), bf.y - floorf(bf.y), bf.z - floorf(bf.z));
+    const F3 tc = f3(1.0f - t.x, 1.0f - t.y, 1.0f - t.z);
+    out = ((f[0] * tc.x + f[1] * t.x) * tc.y + (f[2] * tc.x + f[3] * t.x) * t.y) * tc.z
+        + ((f[4] * tc.x + f[5] * t.x) * tc.y + (f[6] * tc.x + f[7] * t.x) * t.y) * t.z;
+    return true;
+}
+
+// visitor::getFieldGrad single-res with Map::getFieldGrad's division by the resolution.
+__device__ bool field_grad(const MapDevice& m, BlockCache& c, F3 p_W, F3& g)
+{
+    F3 vf;
+    if (!point_to_voxel_f(m, p_W, vf))
+        return false;
+    const F3 s = f3(vf.x - 0.5f, vf.y - 0.5f, vf.z - 0.5f);
+    const F3 fac = f3(s.x - floorf(s.x), s.y - floorf(s.y), s.z - floorf(s.z));
+    const int base[3] = {(int) s.x, (int) s.y, (int) s.z};
+    const int top = m.size - 1;
+    int ll[3], lu[3], ul[3], uu[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        ll[i] = max(base[i] - 1, 0);
+        lu[i] = max(base[i], 0);
+        ul[i] = min(base[i] + 1, top);
+        uu[i] = min(base[i] + 2, top);
+    }
+    if (lookup_block(m, c, base[0], base[1], base[2]) < 0)
+        return false;
+    // 32 samples: selector per axis, 0 = ll, 1 = lu, 2 = ul, 3 = uu (reference order)
+    constexpr unsigned char SX[32] = {0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1,
+                                      2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 3, 3, 3, 3};
+    constexpr unsigned char SY[32] = {1, 2, 1, 2, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3,
+                                      0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 1, 2, 1, 2};
+    constexpr unsigned char SZ[32] = {1, 1, 2, 2, 1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 1, 2,
+                                      1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 1, 2, 1, 1, 2, 2};
+    float v[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+        const int sx = SX[i], sy = SY[i], sz = SZ[i];
+        const int cx = sx == 0 ? ll[0] : sx == 1 ? lu[0] : sx == 2 ? ul[0] : uu[0];
+        const int cy = sy == 0 ? ll[1] : sy == 1 ? lu[1] : sy == 2 ? ul[1] : uu[1];
+        const int cz = sz == 0 ? ll[2] : sz == 1 ? lu[2] : sz == 2 ? ul[2] : uu[2];
+        float t, w;
+        fetch_voxel(m, c, cx, cy, cz, t, w);
+        if (!(w != 0.0f))
+            return false;
+        v[i] = t;
+    }
+    const float rx = 1.0f - fac.x, ry = 1.0f - fac.y, rz = 1.0f - fac.z;
+    const float gx = (((v[19] - v[0]) * rx + (v[28] - v[7]) * fac.x) * ry
+                      + ((v[23] - v[1]) * rx + (v[29] - v[11]) * fac.x) * fac.y) * rz
+        + (((v[20] - v[2]) * rx + (v[30] - v[8]) * fac.x) * ry
+           + ((v[24] - v[3]) * rx + (v[31] - v[12]) * fac.x) * fac.y) * fac.z;
+    const float gy = (((v[11] - v[4]) * rx + (v[23] - v[16]) * fac.x) * ry
+                      + ((v[14] - v[7]) * rx + (v[26] - v[19]) * fac.x) * fac.y) * rz
+        + (((v[12] - v[5]) * rx + (v[24] - v[17]) * fac.x) * ry
+           + ((v[15] - v[8]) * rx + (v[27] - v[20]) * fac.x) * fac.y) * fac.z;
+    const float gz = (((v[8] - v[6]) * rx + (v[20] - v[18]) * fac.x) * ry
+                      + ((v[12] - v[10]) * rx + (v[24] - v[22]) * fac.x) * fac.y) * rz
+        + (((v[9] - v[7]) * rx + (v[21] - v[19]) * fac.x) * ry
+           + ((v[13] - v[11]) * rx + (v[25] - v[23]) * fac.x) * fac.y) * fac.z;
+    g = f3((0.5f * gx) / m.res, (0.5f * gy) / m.res, (0.5f * gz) / m.res);
+    return true;
+}
+
+__device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockCache& c, F3 o, F3 d, float t_near,
+                             float t_far, F3& hit)
+{
+    float t_min, t_max;
+    first_block(m, rp, o, d, t_near, t_far, t_min, t_max);
+    if (t_min <= 0.0f)
+        return false;
+    const float step = m.res;
+    const float largestep = (float) kBlockSize * step;
+    float t = t_min;
+    if (!(t_near < t_max))
+        return false;
+    float stepsize = largestep;
+    F3 p = add(o, mul(d, t));
+    float f_t, w_t;
+    map_get_data(m, c, p, f_t, w_t);
+    float f_tt = 0.0f;
+    if (!(f_t >= 0.0f))
+        return false;
+    // The march ends at t_far: every step is at least res, so it is bounded by (t_far - t)/res.
+    for (; t < t_far; t += stepsize) {
+        float f, w;
+        map_get_data(m, c, p, f, w);
+        if (!(w != 0.0f)) {
+            stepsize = largestep;
+            p = add(p, mul(stepsize, d));
+            continue;
+        }
+        f_tt = f;
+        if ((double) f_tt <= 0.1 && f_tt >= -0.5f) {
+            float fi;
+            if (field_interp(m, c, p, fi))
+                f_tt = fi;
+        }
+        if (f_tt < 0.0f)
+            break;
+        stepsize = fmax_std(f_tt * m.trunc, step);
+        p = add(p, mul(stepsize, d));
+        f_t = f_tt;
+    }
+    if (f_tt < 0.0f) {
+        t = t - stepsize * (f_tt - 0.0f) / (f_tt - f_t);
+        hit = add(o, mul(d, t));
+        return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(128) raycast_kernel(MapDevice m, Pinhole s, RaycastParams rp,
+                                                      float* __restrict__ pts, float* __restrict__ nrm,
+                                                      int8_t* __restrict__ scale)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+    const int y = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+    if (x >= s.w || y >= s.h)
+        return;
+    const size_t idx = (size_t) x + (size_t) y * s.w;
+    const F3 ray_S = back_project(s, (float) x, (float) y);
+    const F3 nS = normalized(ray_S);
+    const F3 dir_W = rot(rp.T_WS, nS);
+    const F3 origin = f3(rp.T_WS.t[0], rp.T_WS.t[1], rp.T_WS.t[2]);
+    const float t_near = s.near_plane / nS.z;
+    const float t_far = s.far_plane / nS.z;
+    BlockCache c{-1, -1, -1, -1};
+    F3 hit;
+    F3 n = f3(0.0f, 0.0f, 0.0f);
+    F3 p = f3(0.0f, 0.0f, 0.0f);
+    if (raycast_tsdf(m, rp, c, origin, dir_W, t_near, t_far, hit)) {
+        p = hit;
+        F3 g;
+        if (field_grad(m, c, hit, g))
+            n = normalized(g);
+    }
+    pts[3 * idx + 0] = p.x;
+    pts[3 * idx + 1] = p.y;
+    pts[3 * idx + 2] = p.z;
+    nrm[3 * idx + 0] = n.x;
+    nrm[3 * idx + 1] = n.y;
+    nrm[3 * idx + 2] = n.z;
+    if (scale)
+        scale[idx] = 0;
+}
+
+__global__ void field_query_kernel(MapDevice m, int n, const float* __restrict__ pts, float* __restrict__ out,
+                                   int* __restrict__ valid, int grad)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const F3 p = f3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+    BlockCache c{-1, -1, -1, -1};
+    bool ok;
+    if (grad) {
+        F3 g = f3(0.0f, 0.0f, 0.0f);
+        ok = field_grad(m, c, p, g);
+        out[3 * i] = ok ? g.x : 0.0f;
+        out[3 * i + 1] = ok ? g.y : 0.0f;
+        out[3 * i + 2] = ok ? g.z : 0.0f;
+    }
+    else {
+        float v = 0.0f;
+        ok = field_interp(m, c, p, v);
+        out[i] = ok ? v : 0.0f;
+    }
+    if (valid)
+        valid[i] = ok ? 1 : 0;
+}
+
+} // namespace se_gpu
+
+using namespace se_gpu;
+
+static se_gpu_status field_query(const se_gpu_map* map, int64_t n, const float* pts, float* out, int* valid,
+                                 void* stream_p, int grad)
+{
+    if (!map || n < 0 || n > (1ll << 31) - 1 || (n > 0 && (!pts || !out))) {
+        set_last_error("se_gpu_map_field_%s: invalid argument", grad ? "grad" : "interp");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    if (n == 0)
+        return SE_GPU_OK;
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    field_query_kernel<<<(unsigned) ((n + 127) / 128), 128, 0, stream>>>(map->dev, (int) n, pts, out, valid, grad);
+    SE_CUDA_TRY(cudaGetLastError());
+    return SE_GPU_OK;
+}
+
+extern "C" se_gpu_status se_gpu_map_field_interp(const se_gpu_map* map, int64_t n, const float* pts, float* values,
+                                                 int* valid, void* stream)
+{
+    return field_query(map, n, pts, values, valid, stream, 0);
+}
+
+extern "C" se_gpu_status se_gpu_map_field_grad(const se_gpu_map* map, int64_t n, const float* pts, float* grads,
+                                               int* valid, void* stream)
+{
+    return field_query(map, n, pts, grads, valid, stream, 1);
+}
+
+extern "C" se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinhole* sensor, const float T_WS[16],
+                                        float* pts_dev, float* nrm_dev, int8_t* scale_dev, void* stream_p)
+{
+    if (!map || !sensor || !T_WS || !pts_dev || !nrm_dev || sensor->width <= 0 || sensor->height <= 0) {
+        set_last_error("se_gpu_raycast: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    const_cast<se_gpu_map*>(map)->last_stream = stream;
+    const MapDevice& m = map->dev;
+    const Pinhole s = make_pinhole(*sensor);
+    RaycastParams rp;
+    rp.T_WS = tf_from16(T_WS);
+    rp.scaling = (float) m.size * m.res;
+    rp.eps = std::exp2((float) (-std::log2((double) m.size)));
+    rp.min_scale = 23 - m.log2_bps;
+    dim3 grid((s.w + 15) / 16, (s.h + 7) / 8);
+    ProfScope ps(kProfRaycast, stream);
+    raycast_kernel<<<grid, 128, 0, stream>>>(m, s, rp, pts_dev, nrm_dev, scale_dev);
+    SE_CUDA_TRY(cudaGetLastError());
+    return SE_GPU_OK;
+}

@@ -1,0 +1,318 @@
+// se_gpu_internal.cuh — device data structures and helpers shared by the kernels.
+//
+// Float arithmetic follows one fixed operation order (the CPU oracle uses the same):
+//   dot3 = (a0*b0 + a1*b1) + a2*b2;   (T*p)_i = ((R_i0 p0 + R_i1 p1) + R_i2 p2) + t_i
+//   norm = sqrtf(dot3(v, v));         normalized(v) = v / norm (component-wise division)
+// The library is compiled with --fmad=false and IEEE division / square root, so every
+// operation rounds separately and the allocation key set and integer weights are bit-exact
+// against the oracle.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/se_gpu.h"
+
+namespace se_gpu {
+
+constexpr int kBlockSize = 8;
+constexpr int kBlockVoxels = 512;
+constexpr int kMaxBlockScale = 3;
+constexpr unsigned long long kEmptyKey = 0xffffffffffffffffULL;
+constexpr int kMaxProbe = 256;
+
+// error bits latched in MapDevice::counters[kCntError]
+constexpr int kErrPoolFull = 1;
+constexpr int kErrProbeLimit = 2;
+
+// device counters
+enum {
+    kCntNumBlocks = 0,   // allocated blocks (may exceed capacity on overflow: clamp on read)
+    kCntError = 1,
+    kCntListed = 2,      // update list length of the current frame
+    kCntNumOld = 3,      // blocks allocated before the current frame
+    kCntValidPixels = 4,
+    kCntUpdated = 6,     // 64-bit (slots 6, 7)
+    kNumCounters = 16
+};
+
+struct F3 {
+    float x, y, z;
+};
+__host__ __device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__host__ __device__ __forceinline__ F3 add(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ F3 sub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ F3 mul(F3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__host__ __device__ __forceinline__ F3 mul(float s, F3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+__host__ __device__ __forceinline__ F3 divs(F3 a, float s) { return f3(a.x / s, a.y / s, a.z / s); }
+__host__ __device__ __forceinline__ float dot(F3 a, F3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__host__ __device__ __forceinline__ float norm(F3 a) { return sqrtf(dot(a, a)); }
+__host__ __device__ __forceinline__ F3 normalized(F3 a)
+{
+    const float sq = dot(a, a);
+    if (sq > 0.0f) {
+        const float n = sqrtf(sq);
+        return f3(a.x / n, a.y / n, a.z / n);
+    }
+    return a;
+}
+__host__ __device__ __forceinline__ F3 cross(F3 a, F3 b)
+{
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+// Rigid / affine transform with a row-major 3x3 part.
+struct Tf {
+    float R[9];
+    float t[3];
+};
+__host__ __device__ __forceinline__ F3 rot(const Tf& T, F3 v)
+{
+    return f3((T.R[0] * v.x + T.R[1] * v.y) + T.R[2] * v.z,
+              (T.R[3] * v.x + T.R[4] * v.y) + T.R[5] * v.z,
+              (T.R[6] * v.x + T.R[7] * v.y) + T.R[8] * v.z);
+}
+__host__ __device__ __forceinline__ F3 apply(const Tf& T, F3 v)
+{
+    const F3 r = rot(T, v);
+    return f3(r.x + T.t[0], r.y + T.t[1], r.z + T.t[2]);
+}
+__host__ __device__ inline Tf compose(const Tf& A, const Tf& B)
+{
+    Tf C;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            C.R[3 * i + j] = (A.R[3 * i] * B.R[j] + A.R[3 * i + 1] * B.R[3 + j]) + A.R[3 * i + 2] * B.R[6 + j];
+        C.t[i] = ((A.R[3 * i] * B.t[0] + A.R[3 * i + 1] * B.t[1]) + A.R[3 * i + 2] * B.t[2]) + A.t[i];
+    }
+    return C;
+}
+__host__ __device__ inline Tf inverse_iso(const Tf& A)
+{
+    Tf B;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            B.R[3 * i + j] = A.R[3 * j + i];
+    for (int i = 0; i < 3; ++i)
+        B.t[i] = -((B.R[3 * i] * A.t[0] + B.R[3 * i + 1] * A.t[1]) + B.R[3 * i + 2] * A.t[2]);
+    return B;
+}
+__host__ __device__ inline Tf tf_from16(const float* m)
+{
+    Tf T;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            T.R[3 * i + j] = m[4 * i + j];
+        T.t[i] = m[4 * i + 3];
+    }
+    return T;
+}
+__host__ __device__ inline void tf_to16(const Tf& T, float* m)
+{
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            m[4 * i + j] = T.R[3 * i + j];
+        m[4 * i + 3] = T.t[i];
+    }
+    m[12] = m[13] = m[14] = 0.0f;
+    m[15] = 1.0f;
+}
+
+// ---------------------------------------------------------------------- Morton keys --
+// include/se/map/utils/impl/key_util_impl.hpp:44-101: 19 bits per axis, x at bit 0.
+__host__ __device__ __forceinline__ uint64_t morton_expand(uint64_t v)
+{
+    uint64_t x = v & 0x7ffff;
+    x = (x | x << 32) & 0x1f00000000ffffULL;
+    x = (x | x << 16) & 0x1f0000ff0000ffULL;
+    x = (x | x << 8) & 0x100f00f00f00f00fULL;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ULL;
+    x = (x | x << 2) & 0x1249249249249249ULL;
+    return x;
+}
+__host__ __device__ __forceinline__ uint64_t morton_compact(uint64_t v)
+{
+    uint64_t x = v & 0x49249249249249ULL;
+    x = (x | x >> 2) & 0x10c30c30c30c30c3ULL;
+    x = (x | x >> 4) & 0x100f00f00f00f00fULL;
+    x = (x | x >> 8) & 0x1f0000ff0000ffULL;
+    x = (x | x >> 16) & 0x1f00000000ffffULL;
+    x = (x | x >> 32) & 0x1fffffULL;
+    return x;
+}
+// Key of the 8^3 block containing voxel (x, y, z): code masked at scale 3, << 5 | 3.
+__host__ __device__ __forceinline__ uint64_t block_key(int x, int y, int z)
+{
+    const uint64_t code = morton_expand((uint64_t) (x & ~7)) | (morton_expand((uint64_t) (y & ~7)) << 1)
+        | (morton_expand((uint64_t) (z & ~7)) << 2);
+    return (code << 5) | (uint64_t) kMaxBlockScale;
+}
+__host__ __device__ __forceinline__ uint32_t hash_slot(uint64_t key, uint32_t mask)
+{
+    // the low 9 code bits and the 5 scale bits of a block key are constant
+    const uint64_t h = (key >> 14) * 0x9E3779B97F4A7C15ULL;
+    return (uint32_t) (h >> 32) & mask;
+}
+
+// ------------------------------------------------------------------------ map state --
+struct MapDevice {
+    // geometry
+    int size;            // voxels per side
+    int log2_size;
+    int bps;             // blocks per side = size / 8
+    int log2_bps;
+    float res;
+    float dim;           // size * res
+    Tf T_MW;
+    Tf T_WM;
+    float trunc;         // res * truncation_boundary_factor
+    float max_weight;
+    int storage;         // se_gpu_storage
+    int capacity;        // block pool capacity
+    // block hash: Morton block key -> pool index (open addressing, linear probing). One
+    // 16-byte slot per entry: x = key (kEmptyKey when free), y = pool index (or -1).
+    ulonglong2* hash;
+    uint32_t hash_mask;
+    // block pool
+    int* block_coord;             // 3 ints per block
+    unsigned long long* block_keys;
+    int* block_ts;
+    void* voxels;                 // F32: float2 {tsdf, weight}; F16: {half tsdf, u16 weight}
+    // Occupancy pyramid for the raycast's first-block search: level 0 has one bit per block (bps^3 bits, x fastest), level L one bit
+    // per (2^L)^3 blocks. A bit is set iff an allocated block lies inside the cell, which is
+    // exactly when the reference's pointer octree holds the node.
+    uint32_t* occ[11];
+    int occ_levels;               // log2(bps) + 1
+    // scratch / counters
+    int* counters;                // kNumCounters ints
+    int* update_list;             // capacity ints
+};
+
+__device__ __forceinline__ int hash_find(const MapDevice& m, uint64_t key)
+{
+    uint32_t slot = hash_slot(key, m.hash_mask);
+    for (int p = 0; p < kMaxProbe; ++p) {
+        const ulonglong2 e = m.hash[slot];
+        if (e.x == key)
+            return (int) (long long) e.y;
+        if (e.x == kEmptyKey)
+            return -1;
+        slot = (slot + 1) & m.hash_mask;
+    }
+    return -1;
+}
+
+// Occupancy bit of the cell (cx, cy, cz) at pyramid level L.
+__device__ __forceinline__ bool occ_test(const MapDevice& m, int L, uint32_t cx, uint32_t cy, uint32_t cz)
+{
+    const int lg = m.log2_bps - L;
+    const uint32_t bit = (cz << (2 * lg)) | (cy << lg) | cx;
+    return (__ldg(&m.occ[L][bit >> 5]) >> (bit & 31)) & 1u;
+}
+
+// voxel data access (F32 and F16 layouts)
+__device__ __forceinline__ void load_voxel(const MapDevice& m, int blk, int vi, float& tsdf, float& w)
+{
+    if (m.storage == SE_GPU_STORAGE_F32) {
+        const float2 d = reinterpret_cast<const float2*>(m.voxels)[(size_t) blk * kBlockVoxels + vi];
+        tsdf = d.x;
+        w = d.y;
+    }
+    else {
+        const uint32_t d = reinterpret_cast<const uint32_t*>(m.voxels)[(size_t) blk * kBlockVoxels + vi];
+        tsdf = __half2float(__ushort_as_half((unsigned short) (d & 0xffffu)));
+        w = (float) (d >> 16);
+    }
+}
+__device__ __forceinline__ void store_voxel(const MapDevice& m, int blk, int vi, float tsdf, float w)
+{
+    if (m.storage == SE_GPU_STORAGE_F32) {
+        reinterpret_cast<float2*>(m.voxels)[(size_t) blk * kBlockVoxels + vi] = make_float2(tsdf, w);
+    }
+    else {
+        const uint32_t d = (uint32_t) __half_as_ushort(__float2half_rn(tsdf)) | ((uint32_t) w << 16);
+        reinterpret_cast<uint32_t*>(m.voxels)[(size_t) blk * kBlockVoxels + vi] = d;
+    }
+}
+
+// Map::contains + pointToVoxel<Safe::On> (include/se/map/impl/map_impl.hpp:58-64,538-550).
+__device__ __forceinline__ bool point_to_voxel(const MapDevice& m, F3 p_W, int& vx, int& vy, int& vz)
+{
+    const F3 p = apply(m.T_MW, p_W);
+    if (!(p.x >= 0.0f && p.x < m.dim && p.y >= 0.0f && p.y < m.dim && p.z >= 0.0f && p.z < m.dim))
+        return false;
+    vx = (int) (p.x / m.res);
+    vy = (int) (p.y / m.res);
+    vz = (int) (p.z / m.res);
+    return true;
+}
+__device__ __forceinline__ bool point_to_voxel_f(const MapDevice& m, F3 p_W, F3& v)
+{
+    const F3 p = apply(m.T_MW, p_W);
+    if (!(p.x >= 0.0f && p.x < m.dim && p.y >= 0.0f && p.y < m.dim && p.z >= 0.0f && p.z < m.dim))
+        return false;
+    v = f3(p.x / m.res, p.y / m.res, p.z / m.res);
+    return true;
+}
+
+// ---------------------------------------------------------------------------- sensor --
+struct Pinhole {
+    int w, h;
+    float fx, fy, cx, cy;
+    float inv_fx, inv_fy;
+    float near_plane, far_plane;
+    int left_hand;
+    float planes[6][4]; // left, right, bottom, top, near, far
+};
+
+__host__ __device__ __forceinline__ F3 back_project(const Pinhole& s, float u, float v)
+{
+    return f3((u - s.cx) * s.inv_fx, (v - s.cy) * s.inv_fy, 1.0f);
+}
+__host__ __device__ __forceinline__ bool project(const Pinhole& s, F3 p, float& u, float& v)
+{
+    if (fabsf(p.z) < 1.0e-12f)
+        return false;
+    const float rz = 1.0f / p.z;
+    u = s.fx * (p.x * rz) + s.cx;
+    v = s.fy * (p.y * rz) + s.cy;
+    if (!(u >= -0.5f && u < (float) s.w - 0.5f && v >= -0.5f && v < (float) s.h - 0.5f))
+        return false;
+    return p.z > 0.0f;
+}
+__host__ __device__ __forceinline__ bool sphere_in_frustum(const Pinhole& s, F3 c, float radius)
+{
+    for (int i = 0; i < 6; ++i) {
+        const float d = ((c.x * s.planes[i][0] + c.y * s.planes[i][1]) + c.z * s.planes[i][2]) + s.planes[i][3];
+        if (d < -radius)
+            return false;
+    }
+    return true;
+}
+
+// PinholeCamera ctor / downsampling ctor (src/sensor/pinhole_camera.cpp:63-111,246-310).
+Pinhole make_pinhole(int w, int h, float fx, float fy, float cx, float cy, float near_p, float far_p);
+Pinhole make_pinhole(const se_gpu_pinhole& p);
+Pinhole downsampled(const Pinhole& s, float dsf);
+
+// host-side error reporting
+void set_last_error(const char* fmt, ...);
+se_gpu_status cuda_status(cudaError_t e, const char* what);
+
+} // namespace se_gpu
+
+#define SE_CUDA_TRY(call)                                                                    \
+    do {                                                                                     \
+        cudaError_t _e = (call);                                                             \
+        if (_e != cudaSuccess)                                                               \
+            return ::se_gpu::cuda_status(_e, #call);                                         \
+    } while (0)
+
+struct se_gpu_map {
+    se_gpu::MapDevice dev;
+    se_gpu_map_config config;
+    int device;
+    cudaStream_t last_stream;
+    int host_num_blocks_hint;
+};

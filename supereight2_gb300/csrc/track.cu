@@ -1,0 +1,663 @@
+// track.cu — se::Tracker::track: projective point-to-plane ICP over a 3-level depth pyramid.
+//
+// Per frame: half_sample_robust_image x2, depth_to_point_cloud and point_cloud_to_normal for the
+// three levels, then one fused launch per ICP iteration (coarse to fine, {4, 5, 10} by default):
+//   - every thread evaluates trackKernel for a strided set of pixels (icp_impl.hpp:16-102) and
+//     accumulates the 32 reduction values of newReduce (icp.cpp:45-184) in FP32 with two-sum
+//     compensation (hi, lo pairs);
+//   - warp shuffles, then shared memory, give one compensated partial per CTA;
+//   - the last CTA to finish (atomic ticket, no waiting) adds the partials in FP64 in a fixed
+//     order, solves the 6x6 normal equations with an FP64 LDLT, applies the FP64 se(3)
+//     exponential and composes the pose in FP64 (icp.cpp:15-41,208-223,
+//     math_util_impl.hpp:117-174), and raises the level's convergence flag when |x| < threshold.
+// Later iterations of a converged level return at entry, so the launch sequence is fixed and
+// can be captured in a CUDA graph. checkPoseKernel (icp.cpp:227-246) runs in a final kernel.
+#include <cmath>
+#include <cstring>
+
+#include "profile.cuh"
+#include "se_gpu_internal.cuh"
+
+namespace se_gpu {
+
+int device_sm_count();
+
+constexpr int kTrackThreads = 256;
+constexpr int kMaxTrackCtas = 1024;
+
+enum {
+    kFlagDone0 = 0,  // level converged flags 0..2
+    kFlagIters0 = 3, // iterations run per level 3..5
+    kFlagAccepted = 6,
+    kNumFlags = 8
+};
+
+struct TrackState {
+    // the 80 bytes a synchronous track() reads back: pose_f then flags
+    float pose_f[12];    // FP32 copy of T_WS used by the per-pixel kernel
+    int flags[kNumFlags];
+    double pose[12];     // T_WS, row-major 3x4, FP64
+    float ref_inv[12];   // (T_WS_ref)^-1 in FP32
+    float ref_f[12];     // T_WS_ref
+    float last_red[32];  // final reduction of the last iteration run
+    unsigned int ticket;
+};
+constexpr size_t kTrackReadback = sizeof(float) * 12 + sizeof(int) * kNumFlags;
+
+struct LevelImages {
+    const float* depth[3];
+    float* pts[3];
+    float* nrm[3];
+    int w[3], h[3];
+    Pinhole s[3];
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+
+struct CSum {
+    float hi, lo;
+    __device__ __forceinline__ void add(float v)
+    {
+        float s, e;
+        two_sum(hi, v, s, e);
+        hi = s;
+        lo = lo + e;
+    }
+    __device__ __forceinline__ void merge(float h2, float l2)
+    {
+        float s, e;
+        two_sum(hi, h2, s, e);
+        hi = s;
+        lo = (lo + l2) + e;
+    }
+};
+
+// half_sample_robust_image (src/map/preprocessor.cpp:156-195)
+__global__ void half_sample_kernel(const float* __restrict__ in, int in_w, int in_h, float e_d, int radius,
+                                   float* __restrict__ out)
+{
+    const int ow = in_w / 2, oh = in_h / 2;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= ow || y >= oh)
+        return;
+    const int px = 2 * x, py = 2 * y;
+    float count = 0.0f, sum = 0.0f;
+    const float centre = in[px + py * in_w];
+    for (int i = -radius + 1; i <= radius; ++i) {
+        for (int j = -radius + 1; j <= radius; ++j) {
+            int qx = px + j, qy = py + i;
+            qx = min(max(qx, 0), 2 * ow - 1);
+            qy = min(max(qy, 0), 2 * oh - 1);
+            const float v = in[qx + qy * in_w];
+            if (fabsf(v - centre) < e_d) {
+                count += 1.0f;
+                sum += v;
+            }
+        }
+    }
+    out[x + y * ow] = sum / count;
+}
+
+// depth_to_point_cloud (include/se/map/impl/preprocessor_impl.hpp:18-40), all levels
+__global__ void points_kernel(LevelImages li, int levels)
+{
+    const int l = blockIdx.z;
+    if (l >= levels)
+        return;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int w = li.w[l], h = li.h[l];
+    if (x >= w || y >= h)
+        return;
+    const float d = li.depth[l][x + y * w];
+    F3 p = f3(0.0f, 0.0f, 0.0f);
+    if (d > 0.0f)
+        p = mul(d, back_project(li.s[l], (float) x, (float) y));
+    float* o = li.pts[l] + 3 * (size_t) (x + y * w);
+    o[0] = p.x;
+    o[1] = p.y;
+    o[2] = p.z;
+}
+
+__device__ __forceinline__ F3 ld3(const float* p, size_t i) { return f3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+
+// point_cloud_to_normal<NegY> (src/map/preprocessor.cpp:109-152), all levels
+__global__ void normals_kernel(LevelImages li, int levels, int neg_y)
+{
+    const int l = blockIdx.z;
+    if (l >= levels)
+        return;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int w = li.w[l], h = li.h[l];
+    if (x >= w || y >= h)
+        return;
+    const float* P = li.pts[l];
+    F3 n = f3(0.0f, 0.0f, 0.0f);
+    const F3 p = ld3(P, x + (size_t) w * y);
+    if (p.z != 0.0f) {
+        const int lx = max(x - 1, 0), rx = min(x + 1, w - 1);
+        int uy, dy;
+        if (neg_y) {
+            uy = max(y - 1, 0);
+            dy = min(y + 1, h - 1);
+        }
+        else {
+            dy = max(y - 1, 0);
+            uy = min(y + 1, h - 1);
+        }
+        const F3 left = ld3(P, lx + (size_t) w * y), right = ld3(P, rx + (size_t) w * y);
+        const F3 up = ld3(P, x + (size_t) w * uy), down = ld3(P, x + (size_t) w * dy);
+        if (!(left.z == 0.0f || right.z == 0.0f || up.z == 0.0f || down.z == 0.0f))
+            n = normalized(cross(sub(right, left), sub(up, down)));
+    }
+    float* o = li.nrm[l] + 3 * (size_t) (x + y * w);
+    o[0] = n.x;
+    o[1] = n.y;
+    o[2] = n.z;
+}
+
+struct TrackInit {
+    float T_WS[12];
+    float ref_inv[12];
+};
+
+__global__ void track_init_kernel(TrackState* st, TrackInit init)
+{
+    for (int i = 0; i < 12; ++i) {
+        st->pose[i] = (double) init.T_WS[i];
+        st->pose_f[i] = init.T_WS[i];
+        st->ref_f[i] = init.T_WS[i];
+        st->ref_inv[i] = init.ref_inv[i];
+    }
+    for (int i = 0; i < 32; ++i)
+        st->last_red[i] = 0.0f;
+    for (int i = 0; i < kNumFlags; ++i)
+        st->flags[i] = 0;
+    st->ticket = 0;
+}
+
+// ---------------------------------------------------------------------- FP64 solve --
+__device__ void se3_exp_d(const double a[6], double R[9], double t[3])
+{
+    const double wx = a[3], wy = a[4], wz = a[5];
+    const double theta_sq = (wx * wx + wy * wy) + wz * wz;
+    const double theta = sqrt(theta_sq);
+    const double half_theta = 0.5 * theta;
+    double imag, real;
+    if (theta < 1e-10) {
+        const double t4 = theta_sq * theta_sq;
+        imag = 0.5 - 1.0 / 48.0 * theta_sq + 1.0 / 3840.0 * t4;
+        real = 1.0 - 0.5 * theta_sq + 1.0 / 384.0 * t4;
+    }
+    else {
+        imag = sin(half_theta) / theta;
+        real = cos(half_theta);
+    }
+    double qw = real, qx = imag * wx, qy = imag * wy, qz = imag * wz;
+    const double qn = sqrt(((qx * qx + qy * qy) + qz * qz) + qw * qw);
+    qw /= qn;
+    qx /= qn;
+    qy /= qn;
+    qz /= qn;
+    const double tx = 2 * qx, ty = 2 * qy, tz = 2 * qz;
+    const double twx = tx * qw, twy = ty * qw, twz = tz * qw;
+    const double txx = tx * qx, txy = ty * qx, txz = tz * qx;
+    const double tyy = ty * qy, tyz = tz * qy, tzz = tz * qz;
+    R[0] = 1 - (tyy + tzz); R[1] = txy - twz;       R[2] = txz + twy;
+    R[3] = txy + twz;       R[4] = 1 - (txx + tzz); R[5] = tyz - twx;
+    R[6] = txz - twy;       R[7] = tyz + twx;       R[8] = 1 - (txx + tyy);
+    const double O[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
+    double V[9];
+    if (theta < 1e-10) {
+        for (int i = 0; i < 9; ++i)
+            V[i] = R[i];
+    }
+    else {
+        const double tsq = theta * theta;
+        const double c1 = (1.0 - cos(theta)) / tsq;
+        const double c2 = (theta - sin(theta)) / (tsq * theta);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                const double o2 = (O[3 * i] * O[j] + O[3 * i + 1] * O[3 + j]) + O[3 * i + 2] * O[6 + j];
+                V[3 * i + j] = ((i == j ? 1.0 : 0.0) + c1 * O[3 * i + j]) + c2 * o2;
+            }
+    }
+    for (int i = 0; i < 3; ++i)
+        t[i] = (V[3 * i] * a[0] + V[3 * i + 1] * a[1]) + V[3 * i + 2] * a[2];
+}
+
+// LDL^T of the symmetric 6x6 J^T J without pivoting; false on a non-positive pivot.
+__device__ bool ldlt_solve6(const double C[36], const double b[6], double x[6])
+{
+    double L[36], D[6];
+    for (int j = 0; j < 6; ++j) {
+        double dj = C[6 * j + j];
+        for (int k = 0; k < j; ++k)
+            dj -= L[6 * j + k] * L[6 * j + k] * D[k];
+        if (!(dj > 0.0))
+            return false;
+        D[j] = dj;
+        L[6 * j + j] = 1.0;
+        for (int i = j + 1; i < 6; ++i) {
+            double v = C[6 * i + j];
+            for (int k = 0; k < j; ++k)
+                v -= L[6 * i + k] * L[6 * j + k] * D[k];
+            L[6 * i + j] = v / dj;
+        }
+    }
+    double y[6];
+    for (int i = 0; i < 6; ++i) {
+        double s = b[i];
+        for (int k = 0; k < i; ++k)
+            s -= L[6 * i + k] * y[k];
+        y[i] = s;
+    }
+    for (int i = 0; i < 6; ++i)
+        y[i] /= D[i];
+    for (int i = 5; i >= 0; --i) {
+        double s = y[i];
+        for (int k = i + 1; k < 6; ++k)
+            s -= L[6 * k + i] * x[k];
+        x[i] = s;
+    }
+    return true;
+}
+
+struct IterParams {
+    const float* ref_pts;
+    const float* ref_nrm;
+    const float* pts;
+    const float* nrm;
+    int w, h;          // level size
+    int W;             // full-resolution width (row stride of the reference images)
+    int level;
+    float dist_threshold, normal_threshold, icp_threshold;
+};
+
+// One ICP iteration: trackKernel + newReduce/reduceKernel + updatePoseKernel.
+__global__ void __launch_bounds__(kTrackThreads) icp_iter_kernel(Pinhole s, IterParams ip, TrackState* st,
+                                                                float2* __restrict__ partials)
+{
+    __shared__ float2 sh_warp[kTrackThreads / 32][32];
+    __shared__ int sh_last;
+    if (st->flags[kFlagDone0 + ip.level])
+        return;
+
+    Tf T, Tri;
+    for (int i = 0; i < 9; ++i) {
+        T.R[i] = st->pose_f[(i / 3) * 4 + (i % 3)];
+        Tri.R[i] = st->ref_inv[(i / 3) * 4 + (i % 3)];
+    }
+    for (int i = 0; i < 3; ++i) {
+        T.t[i] = st->pose_f[4 * i + 3];
+        Tri.t[i] = st->ref_inv[4 * i + 3];
+    }
+
+    CSum acc[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k)
+        acc[k] = CSum{0.0f, 0.0f};
+
+    const int npix = ip.w * ip.h;
+    for (int i = blockIdx.x * kTrackThreads + threadIdx.x; i < npix; i += gridDim.x * kTrackThreads) {
+        const int x = i % ip.w, y = i / ip.w;
+        const F3 n_in = ld3(ip.nrm, (size_t) i);
+        int result;
+        float e = 0.0f;
+        float J[6];
+        if (n_in.x == 0.0f && n_in.y == 0.0f && n_in.z == 0.0f) {
+            result = -1;
+        }
+        else {
+            const F3 p_W = apply(T, ld3(ip.pts, (size_t) i));
+            const F3 p_ref = apply(Tri, p_W);
+            float u, v;
+            if (!project(s, p_ref, u, v)) {
+                result = -2;
+            }
+            else {
+                const int px = (int) (u + 0.5f), py = (int) (v + 0.5f);
+                const size_t ri = (size_t) px + (size_t) py * ip.W;
+                const F3 rn = ld3(ip.ref_nrm, ri);
+                const F3 n_ref = f3(-rn.x, -rn.y, -rn.z);
+                if (n_ref.x == 0.0f && n_ref.y == 0.0f && n_ref.z == 0.0f) {
+                    result = -3;
+                }
+                else {
+                    const F3 diff = sub(ld3(ip.ref_pts, ri), p_W);
+                    const F3 n_W = rot(T, n_in);
+                    if (norm(diff) > ip.dist_threshold) {
+                        result = -4;
+                    }
+                    else if (dot(n_W, n_ref) < ip.normal_threshold) {
+                        result = -5;
+                    }
+                    else {
+                        result = 1;
+                        e = dot(n_ref, diff);
+                        const F3 c = cross(p_W, n_ref);
+                        J[0] = n_ref.x;
+                        J[1] = n_ref.y;
+                        J[2] = n_ref.z;
+                        J[3] = c.x;
+                        J[4] = c.y;
+                        J[5] = c.z;
+                    }
+                }
+            }
+        }
+        (void) x;
+        (void) y;
+        if (result < 1) {
+            acc[29].add(result == -4 ? 1.0f : 0.0f);
+            acc[30].add(result == -5 ? 1.0f : 0.0f);
+            acc[31].add(result > -4 ? 1.0f : 0.0f);
+            continue;
+        }
+        acc[0].add(e * e);
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+            acc[1 + k].add(e * J[k]);
+        int q = 7;
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+#pragma unroll
+            for (int c = r; c < 6; ++c)
+                acc[q++].add(J[r] * J[c]);
+        acc[28].add(1.0f);
+    }
+
+    // warp reduction of the compensated pairs
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h2 = __shfl_down_sync(0xffffffffu, acc[k].hi, o);
+            const float l2 = __shfl_down_sync(0xffffffffu, acc[k].lo, o);
+            acc[k].merge(h2, l2);
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 32; ++k)
+            sh_warp[warp][k] = make_float2(acc[k].hi, acc[k].lo);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        CSum t{0.0f, 0.0f};
+        for (int wi = 0; wi < kTrackThreads / 32; ++wi)
+            t.merge(sh_warp[wi][threadIdx.x].x, sh_warp[wi][threadIdx.x].y);
+        partials[blockIdx.x * 32 + threadIdx.x] = make_float2(t.hi, t.lo);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0)
+        sh_last = (atomicAdd(&st->ticket, 1u) == gridDim.x - 1) ? 1 : 0;
+    __syncthreads();
+    if (!sh_last)
+        return;
+    __threadfence();
+
+    // ---- last CTA: fixed-order FP64 sum of the partials, solve, pose update
+    __shared__ double sh_chunk[8][32];
+    __shared__ double sh_val[32];
+    {
+        const int k = threadIdx.x & 31, chunk = threadIdx.x >> 5;
+        double acc_d = 0.0;
+        for (int b = chunk; b < (int) gridDim.x; b += 8) {
+            const float2 p = __ldcg(&partials[b * 32 + k]);
+            acc_d += (double) p.x + (double) p.y;
+        }
+        sh_chunk[chunk][k] = acc_d;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = 0.0;
+        for (int c = 0; c < 8; ++c)
+            v += sh_chunk[c][threadIdx.x];
+        sh_val[threadIdx.x] = v;
+        st->last_red[threadIdx.x] = (float) v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        st->ticket = 0;
+        st->flags[kFlagIters0 + ip.level] += 1;
+        double C[36], b[6], xs[6];
+        for (int i = 0; i < 6; ++i)
+            b[i] = sh_val[1 + i];
+        int q = 7;
+        for (int r = 0; r < 6; ++r)
+            for (int c = r; c < 6; ++c) {
+                C[6 * r + c] = sh_val[q];
+                C[6 * c + r] = sh_val[q];
+                ++q;
+            }
+        if (!ldlt_solve6(C, b, xs))
+            for (int i = 0; i < 6; ++i)
+                xs[i] = 0.0;
+        double dR[9], dt[3];
+        se3_exp_d(xs, dR, dt);
+        double P[12];
+        for (int i = 0; i < 3; ++i) {
+            for (int j = 0; j < 3; ++j)
+                P[4 * i + j] = (dR[3 * i] * st->pose[j] + dR[3 * i + 1] * st->pose[4 + j]) + dR[3 * i + 2] * st->pose[8 + j];
+            P[4 * i + 3] = ((dR[3 * i] * st->pose[3] + dR[3 * i + 1] * st->pose[7]) + dR[3 * i + 2] * st->pose[11]) + dt[i];
+        }
+        for (int i = 0; i < 12; ++i) {
+            st->pose[i] = P[i];
+            st->pose_f[i] = (float) P[i];
+        }
+        double xn = 0.0;
+        for (int i = 0; i < 6; ++i)
+            xn += xs[i] * xs[i];
+        if (sqrt(xn) < (double) ip.icp_threshold)
+            st->flags[kFlagDone0 + ip.level] = 1;
+    }
+}
+
+// checkPoseKernel (icp.cpp:227-246): revert to the reference pose on a poor final alignment.
+__global__ void icp_check_kernel(TrackState* st, int W, int H, float track_threshold)
+{
+    const float* v = st->last_red;
+    const bool reject = ((double) sqrtf(v[0] / v[28]) > 2e-2) || (v[28] / (float) (W * H) < track_threshold);
+    if (reject) {
+        for (int i = 0; i < 12; ++i) {
+            st->pose_f[i] = st->ref_f[i];
+            st->pose[i] = (double) st->ref_f[i];
+        }
+    }
+    st->flags[kFlagAccepted] = reject ? 0 : 1;
+}
+
+} // namespace se_gpu
+
+using namespace se_gpu;
+
+struct se_gpu_tracker {
+    se_gpu_pinhole sensor;
+    se_gpu_tracker_config config;
+    Pinhole s;
+    LevelImages li;
+    int levels;
+    float* pyr_depth[3]; // levels 1, 2 (index 0 unused: the input is level 0)
+    float* pts[3];
+    float* nrm[3];
+    float2* partials;
+    TrackState* state;
+    int nctas[3];
+};
+
+extern "C" {
+
+se_gpu_status se_gpu_tracker_create(const se_gpu_pinhole* sensor, const se_gpu_tracker_config* config,
+                                    se_gpu_tracker** out)
+{
+    if (!sensor || !config || !out || sensor->width <= 0 || sensor->height <= 0 || config->num_levels < 1
+        || config->num_levels > 3) {
+        set_last_error("se_gpu_tracker_create: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    se_gpu_tracker* t = new se_gpu_tracker();
+    std::memset(t, 0, sizeof(*t));
+    t->sensor = *sensor;
+    t->config = *config;
+    t->s = make_pinhole(*sensor);
+    t->levels = config->num_levels;
+    auto fail = [&](cudaError_t e, const char* what) {
+        se_gpu_status st = cuda_status(e, what);
+        se_gpu_tracker_destroy(t);
+        return st;
+    };
+    cudaError_t e;
+    for (int l = 0; l < t->levels; ++l) {
+        const int w = sensor->width / (1 << l), h = sensor->height / (1 << l);
+        t->li.w[l] = w;
+        t->li.h[l] = h;
+        t->li.s[l] = downsampled(t->s, (float) (1 << l));
+        if (l > 0 && (e = cudaMalloc(&t->pyr_depth[l], (size_t) w * h * sizeof(float))) != cudaSuccess)
+            return fail(e, "cudaMalloc(pyramid)");
+        if ((e = cudaMalloc(&t->pts[l], (size_t) w * h * 3 * sizeof(float))) != cudaSuccess)
+            return fail(e, "cudaMalloc(points)");
+        if ((e = cudaMalloc(&t->nrm[l], (size_t) w * h * 3 * sizeof(float))) != cudaSuccess)
+            return fail(e, "cudaMalloc(normals)");
+        t->li.pts[l] = t->pts[l];
+        t->li.nrm[l] = t->nrm[l];
+        t->li.depth[l] = t->pyr_depth[l];
+        const int ctas = (w * h + kTrackThreads * 4 - 1) / (kTrackThreads * 4);
+        t->nctas[l] = ctas < 2 * device_sm_count() ? (ctas > 0 ? ctas : 1) : 2 * device_sm_count();
+        if (t->nctas[l] > kMaxTrackCtas)
+            t->nctas[l] = kMaxTrackCtas;
+    }
+    if ((e = cudaMalloc(&t->partials, (size_t) kMaxTrackCtas * 32 * sizeof(float2))) != cudaSuccess)
+        return fail(e, "cudaMalloc(partials)");
+    if ((e = cudaMalloc(&t->state, sizeof(TrackState))) != cudaSuccess)
+        return fail(e, "cudaMalloc(state)");
+    if ((e = cudaMemset(t->state, 0, sizeof(TrackState))) != cudaSuccess)
+        return fail(e, "cudaMemset(state)");
+    *out = t;
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_tracker_destroy(se_gpu_tracker* t)
+{
+    if (!t)
+        return SE_GPU_OK;
+    for (int l = 0; l < 3; ++l) {
+        cudaFree(t->pyr_depth[l]);
+        cudaFree(t->pts[l]);
+        cudaFree(t->nrm[l]);
+    }
+    cudaFree(t->partials);
+    cudaFree(t->state);
+    delete t;
+    return SE_GPU_OK;
+}
+
+// Enqueue the whole track on `stream` from a host pose. Asynchronous.
+static se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const float* ref_pts,
+                                   const float* ref_nrm, const float T_WS[16], cudaStream_t stream)
+{
+    TrackInit init;
+    const Tf T = tf_from16(T_WS);
+    const Tf Ti = inverse_iso(T);
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) {
+            init.T_WS[4 * i + j] = T.R[3 * i + j];
+            init.ref_inv[4 * i + j] = Ti.R[3 * i + j];
+        }
+        init.T_WS[4 * i + 3] = T.t[i];
+        init.ref_inv[4 * i + 3] = Ti.t[i];
+    }
+    LevelImages li = t->li;
+    li.depth[0] = depth_dev;
+    {
+    ProfScope ps(kProfTrackPrep, stream);
+    track_init_kernel<<<1, 1, 0, stream>>>(t->state, init);
+    const float e_d = 0.1f * 3;
+    for (int l = 1; l < t->levels; ++l) {
+        dim3 b(32, 8), g((li.w[l] + 31) / 32, (li.h[l] + 7) / 8);
+        half_sample_kernel<<<g, b, 0, stream>>>(li.depth[l - 1], li.w[l - 1], li.h[l - 1], e_d, 1,
+                                                t->pyr_depth[l]);
+    }
+    {
+        dim3 b(32, 8), g((li.w[0] + 31) / 32, (li.h[0] + 7) / 8, t->levels);
+        points_kernel<<<g, b, 0, stream>>>(li, t->levels);
+        normals_kernel<<<g, b, 0, stream>>>(li, t->levels, t->s.left_hand);
+    }
+    }
+    for (int level = t->levels - 1; level >= 0; --level) {
+        IterParams ip;
+        ip.ref_pts = ref_pts;
+        ip.ref_nrm = ref_nrm;
+        ip.pts = t->pts[level];
+        ip.nrm = t->nrm[level];
+        ip.w = li.w[level];
+        ip.h = li.h[level];
+        ip.W = t->sensor.width;
+        ip.level = level;
+        ip.dist_threshold = t->config.dist_threshold;
+        ip.normal_threshold = t->config.normal_threshold;
+        ip.icp_threshold = t->config.icp_threshold;
+        for (int it = 0; it < t->config.iterations[level]; ++it) {
+            ProfScope ps(kProfIcpIter, stream);
+            icp_iter_kernel<<<t->nctas[level], kTrackThreads, 0, stream>>>(t->s, ip, t->state, t->partials);
+        }
+    }
+    {
+        ProfScope ps(kProfIcpCheck, stream);
+        icp_check_kernel<<<1, 1, 0, stream>>>(t->state, t->sensor.width, t->sensor.height,
+                                              t->config.track_threshold);
+    }
+    SE_CUDA_TRY(cudaGetLastError());
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_track(se_gpu_tracker* t, const float* depth_dev, const float* ref_pts, const float* ref_nrm,
+                           float T_WS[16], int* accepted, void* stream_p)
+{
+    if (!t || !depth_dev || !ref_pts || !ref_nrm || !T_WS) {
+        set_last_error("se_gpu_track: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    se_gpu_status st = enqueue_track(t, depth_dev, ref_pts, ref_nrm, T_WS, stream);
+    if (st != SE_GPU_OK)
+        return st;
+    TrackState hs;
+    SE_CUDA_TRY(cudaMemcpyAsync(&hs, t->state, kTrackReadback, cudaMemcpyDeviceToHost, stream));
+    SE_CUDA_TRY(cudaStreamSynchronize(stream));
+    for (int i = 0; i < 12; ++i)
+        T_WS[i] = hs.pose_f[i];
+    T_WS[12] = T_WS[13] = T_WS[14] = 0.0f;
+    T_WS[15] = 1.0f;
+    if (accepted)
+        *accepted = hs.flags[kFlagAccepted];
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_tracker_last_reduction(se_gpu_tracker* t, float reduction[32], int iterations_run[3])
+{
+    if (!t) {
+        set_last_error("se_gpu_tracker_last_reduction: null tracker");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    TrackState hs;
+    SE_CUDA_TRY(cudaMemcpy(&hs, t->state, sizeof(TrackState), cudaMemcpyDeviceToHost));
+    if (reduction)
+        for (int i = 0; i < 32; ++i)
+            reduction[i] = hs.last_red[i];
+    if (iterations_run)
+        for (int l = 0; l < 3; ++l)
+            iterations_run[l] = hs.flags[kFlagIters0 + l];
+    return SE_GPU_OK;
+}
+
+} // extern "C"

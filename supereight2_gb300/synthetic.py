@@ -1,0 +1,224 @@
+"""Seeded synthetic scenes and trajectories (input data for tests and the benchmark).
+
+The scene stands in for the datasets the reference reports on (they are not available here):
+an axis-aligned 6 x 5 x 3 m room seen from the inside, 12 random spheres (radius 0.1-0.6 m)
+and 8 randomly oriented boxes, ray traced analytically in float64 and stored as float32 depth
+(z, metres). Per-pixel noise N(0, (0.0015 z^2)^2) is added and 2 % of the pixels are zeroed.
+Pinhole camera frame: x right, y down, z forward. Poses are T_WC (camera to world), 4x4.
+
+Rendering runs with torch on any device; noise and dropout come from a numpy generator seeded
+per frame, so a frame's bytes do not depend on the device it was rendered on except for
+float64 rounding in the ray tracing.
+"""
+from dataclasses import dataclass, field
+import math
+
+import numpy as np
+import torch
+
+ROOM_HALF = (3.0, 2.5, 1.5)
+
+
+@dataclass
+class PinholeSpec:
+    width: int
+    height: int
+    fx: float
+    fy: float
+    cx: float
+    cy: float
+    near_plane: float = 0.4
+    far_plane: float = 6.0
+
+
+# The camera set-ups of the benchmark configurations.
+SENSOR_320 = PinholeSpec(320, 240, 262.5, 262.5, 159.5, 119.5, 0.4, 6.0)
+SENSOR_640 = PinholeSpec(640, 480, 525.0, 525.0, 319.5, 239.5, 0.4, 6.0)
+
+
+@dataclass
+class Scene:
+    sphere_c: np.ndarray  # [12, 3]
+    sphere_r: np.ndarray  # [12]
+    box_c: np.ndarray     # [8, 3]
+    box_R: np.ndarray     # [8, 3, 3] box-to-world rotation
+    box_h: np.ndarray     # [8, 3] half extents
+    seed: int = 0
+    room_half: tuple = field(default=ROOM_HALF)
+
+
+def _rot_zyx(yaw, pitch, roll):
+    cy, sy = math.cos(yaw), math.sin(yaw)
+    cp, sp = math.cos(pitch), math.sin(pitch)
+    cr, sr = math.cos(roll), math.sin(roll)
+    Rz = np.array([[cy, -sy, 0], [sy, cy, 0], [0, 0, 1]])
+    Ry = np.array([[cp, 0, sp], [0, 1, 0], [-sp, 0, cp]])
+    Rx = np.array([[1, 0, 0], [0, cr, -sr], [0, sr, cr]])
+    return Rz @ Ry @ Rx
+
+
+def make_scene(seed: int, keep_out_radius=(0.9, 2.1)) -> Scene:
+    """12 spheres and 8 oriented boxes, kept out of the annulus the cameras move in."""
+    rng = np.random.default_rng(seed)
+    hx, hy, hz = ROOM_HALF
+
+    def place(extent):
+        for _ in range(10000):
+            c = np.array([rng.uniform(-hx + extent, hx - extent),
+                          rng.uniform(-hy + extent, hy - extent),
+                          rng.uniform(-hz + extent, hz - extent)])
+            rxy = math.hypot(c[0], c[1])
+            if rxy + extent < keep_out_radius[0] or rxy - extent > keep_out_radius[1]:
+                return c
+        raise RuntimeError("could not place object")
+
+    sr = rng.uniform(0.1, 0.6, size=12)
+    sr = np.minimum(sr, 0.6)
+    sc = np.stack([place(r) for r in sr])
+    bh = rng.uniform(0.1, 0.4, size=(8, 3))
+    bR = np.stack([_rot_zyx(*rng.uniform(-math.pi, math.pi, size=3)) for _ in range(8)])
+    bc = np.stack([place(float(np.linalg.norm(h))) for h in bh])
+    return Scene(sc, sr, bc, bR, bh, seed)
+
+
+def look_at(eye, target, up=(0.0, 0.0, 1.0)) -> np.ndarray:
+    """T_WC of a z-forward, y-down camera at eye looking at target."""
+    eye = np.asarray(eye, np.float64)
+    z = np.asarray(target, np.float64) - eye
+    z /= np.linalg.norm(z)
+    x = np.cross(z, np.asarray(up, np.float64))
+    x /= np.linalg.norm(x)
+    y = np.cross(z, x)
+    T = np.eye(4)
+    T[:3, 0], T[:3, 1], T[:3, 2], T[:3, 3] = x, y, z, eye
+    return T
+
+
+def _axis_angle(axis, angle):
+    axis = np.asarray(axis, np.float64)
+    axis = axis / np.linalg.norm(axis)
+    K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+    return np.eye(3) + math.sin(angle) * K + (1 - math.cos(angle)) * K @ K
+
+
+def circle_trajectory(n_frames: int, radius=1.5, step_m=0.05, height=0.1) -> list:
+    """Frames on a horizontal circle, looking at the room centre, step_m apart."""
+    dtheta = step_m / radius
+    poses = []
+    for i in range(n_frames):
+        th = i * dtheta
+        eye = (radius * math.cos(th), radius * math.sin(th), height)
+        poses.append(look_at(eye, (0.0, 0.0, -0.2)))
+    return poses
+
+
+def random_walk_trajectory(n_frames: int, seed: int, sigma_m=0.02, sigma_deg=1.0,
+                           radius=1.5) -> list:
+    """Random-walk velocity around the circle: translation steps with std sigma_m and
+    orientation jitter of sigma_deg per frame about the inward-looking direction."""
+    rng = np.random.default_rng(seed)
+    th = 0.0
+    vel = np.zeros(3)
+    pos = np.array([radius, 0.0, 0.1])
+    yaw_off = pitch_off = 0.0
+    poses = []
+    for _ in range(n_frames):
+        base = look_at(pos, (0.0, 0.0, -0.2))
+        R = base[:3, :3] @ _axis_angle((0, 1, 0), yaw_off) @ _axis_angle((1, 0, 0), pitch_off)
+        T = np.eye(4)
+        T[:3, :3], T[:3, 3] = R, pos
+        poses.append(T)
+        # velocity: random walk plus a pull back onto the circle and along its tangent
+        th = math.atan2(pos[1], pos[0])
+        target = np.array([radius * math.cos(th + 0.015), radius * math.sin(th + 0.015), 0.1])
+        vel = 0.7 * vel + 0.3 * (target - pos) + rng.normal(0.0, sigma_m * 0.5, size=3)
+        n = np.linalg.norm(vel)
+        if n > 2.5 * sigma_m:
+            vel *= 2.5 * sigma_m / n
+        pos = pos + vel
+        yaw_off = float(np.clip(0.8 * yaw_off + math.radians(rng.normal(0, sigma_deg)), -0.15, 0.15))
+        pitch_off = float(np.clip(0.8 * pitch_off + math.radians(rng.normal(0, sigma_deg)), -0.1, 0.1))
+    return poses
+
+
+def render_depth(scene: Scene, sensor: PinholeSpec, T_WC, frame_seed: int, device="cpu",
+                 noise=True) -> np.ndarray:
+    """Ray trace one float32 depth image (metres of z) with noise and 2 % dropout."""
+    dt = torch.float64
+    dev = torch.device(device)
+    W, H = sensor.width, sensor.height
+    v, u = torch.meshgrid(torch.arange(H, dtype=dt, device=dev),
+                          torch.arange(W, dtype=dt, device=dev), indexing="ij")
+    d_C = torch.stack([(u - sensor.cx) / sensor.fx, (v - sensor.cy) / sensor.fy,
+                       torch.ones_like(u)], -1).reshape(-1, 3)
+    T = torch.as_tensor(np.asarray(T_WC, np.float64), dtype=dt, device=dev)
+    R, o = T[:3, :3], T[:3, 3]
+    d = d_C @ R.T  # world direction; the ray parameter equals the camera z-depth
+    inf = torch.full((d.shape[0],), float("inf"), dtype=dt, device=dev)
+
+    # room interior: exit distance of the box
+    half = torch.as_tensor(scene.room_half, dtype=dt, device=dev)
+    safe_d = torch.where(d.abs() < 1e-12, torch.full_like(d, 1e-12), d)
+    bound = torch.where(d > 0, half, -half)
+    t_room = ((bound - o) / safe_d).amin(-1)
+    best = torch.where(t_room > 0, t_room, inf)
+
+    for c, r in zip(scene.sphere_c, scene.sphere_r):
+        c = torch.as_tensor(c, dtype=dt, device=dev)
+        oc = o - c
+        a = (d * d).sum(-1)
+        b = (d * oc).sum(-1)
+        cc = (oc * oc).sum() - float(r) ** 2
+        disc = b * b - a * cc
+        sq = torch.sqrt(torch.clamp(disc, min=0.0))
+        t0 = (-b - sq) / a
+        t1 = (-b + sq) / a
+        t = torch.where(t0 > 1e-6, t0, t1)
+        hit = (disc >= 0) & (t > 1e-6)
+        best = torch.where(hit & (t < best), t, best)
+
+    for c, Rb, hb in zip(scene.box_c, scene.box_R, scene.box_h):
+        c = torch.as_tensor(c, dtype=dt, device=dev)
+        Rb = torch.as_tensor(Rb, dtype=dt, device=dev)
+        hb = torch.as_tensor(hb, dtype=dt, device=dev)
+        ol = (o - c) @ Rb
+        dl = d @ Rb
+        dl = torch.where(dl.abs() < 1e-12, torch.full_like(dl, 1e-12), dl)
+        ta = (-hb - ol) / dl
+        tb = (hb - ol) / dl
+        tn = torch.minimum(ta, tb).amax(-1)
+        tf = torch.maximum(ta, tb).amin(-1)
+        hit = (tn <= tf) & (tf > 1e-6)
+        t = torch.where(tn > 1e-6, tn, tf)
+        best = torch.where(hit & (t < best), t, best)
+
+    z = best.reshape(H, W).cpu().numpy()
+    z = np.where(np.isfinite(z), z, 0.0)
+    rng = np.random.default_rng(frame_seed)
+    if noise:
+        z = z + rng.standard_normal(z.shape) * (0.0015 * z * z)
+        drop = rng.random(z.shape) < 0.02
+        z = np.where(drop, 0.0, z)
+    return z.astype(np.float32)
+
+
+def dataset(config: str, n_frames: int, device="cpu", seed=None):
+    """(sensor, scene, poses, depth frames) for a named benchmark configuration.
+
+    config "tsdf320": 320x240, circle of 0.05 m / ~2 deg steps, ground-truth poses.
+    config "tsdf640": 640x480, random-walk velocity (0.02 m, 1 deg per frame).
+    """
+    if config == "tsdf320":
+        seed = 1001 if seed is None else seed
+        sensor = SENSOR_320
+        poses = circle_trajectory(n_frames, radius=1.5, step_m=0.05)
+    elif config == "tsdf640":
+        seed = 1002 if seed is None else seed
+        sensor = SENSOR_640
+        poses = random_walk_trajectory(n_frames, seed=seed * 31 + 7)
+    else:
+        raise ValueError(config)
+    scene = make_scene(seed)
+    frames = [render_depth(scene, sensor, T, seed * 7919 + i, device=device)
+              for i, T in enumerate(poses)]
+    return sensor, scene, poses, frames

@@ -1,0 +1,154 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle on seeded synthetic rooms.
+
+Bars: the allocated block-key set and the integer weights are bit-exact, TSDF values agree
+within 1e-5 * truncation, raycast depth within 1e-4 m on >= 99.9 % of the pixels that both
+hit, and ICP poses within 1e-5 m / 1e-5 rad.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TSDF_TOL = 1e-5        # in truncation units (the stored tsdf is sdf / truncation)
+DEPTH_TOL_M = 1e-4
+DEPTH_FRAC = 0.999
+POSE_TOL_M = 1e-5
+POSE_TOL_RAD = 1e-5
+
+
+def _rot_angle(R):
+    c = (np.trace(R) - 1.0) / 2.0
+    return float(np.arccos(np.clip(c, -1.0, 1.0)))
+
+
+@pytest.fixture(scope="module")
+def seq320(oracle, gpu):
+    """C1-shaped sequence: 320x240, 512^3 at 2 cm, 8 frames on a circle, ground-truth poses."""
+    import torch
+    from supereight2_gb300 import synthetic as syn
+    sensor, scene, poses, frames = syn.dataset("tsdf320", 8)
+    spec = dict(width=sensor.width, height=sensor.height, fx=sensor.fx, fy=sensor.fy,
+                cx=sensor.cx, cy=sensor.cy, near_plane=sensor.near_plane,
+                far_plane=sensor.far_plane)
+    om = oracle.OracleMap(10.24, 0.02)
+    os_ = oracle.pinhole(**spec)
+    gm = gpu.Map(10.24, 0.02, max_blocks=1 << 16)
+    gs = gpu.PinholeCamera(**spec)
+    integ = gpu.MapIntegrator(gm)
+    stats = []
+    for i, (T, d) in enumerate(zip(poses, frames)):
+        T32 = T.astype(np.float32)
+        ost = om.integrate_depth(d, os_, T32, i)
+        integ.integrateDepth(i, torch.from_numpy(d).cuda(), gs, T32)
+        gst = gm.integrate_stats()
+        stats.append((ost, gst))
+    gm.check()
+    return dict(om=om, gm=gm, os=os_, gs=gs, poses=poses, frames=frames, stats=stats,
+                spec=spec)
+
+
+def test_integration_counters_match(seq320):
+    for ost, gst in seq320["stats"]:
+        assert gst["n_valid_pixels"] == ost.n_valid_pixels
+        assert gst["n_new_blocks"] == ost.n_new_blocks
+        assert gst["n_listed_blocks"] == ost.n_new_blocks + ost.n_frustum_blocks
+        assert gst["n_updated_voxels"] == ost.n_updated_voxels
+
+
+def _by_key(keys, *arrays):
+    order = np.argsort(keys)
+    return (keys[order],) + tuple(a[order] for a in arrays)
+
+
+def test_block_keys_weights_tsdf_match(seq320):
+    ok, oc, ot, ow, ots = seq320["om"].blocks()
+    gk, gc, gt, gw, gts = seq320["gm"].download_blocks()
+    ok, oc, ot, ow, ots = _by_key(ok, oc, ot, ow, ots)
+    gk, gc, gt, gw, gts = _by_key(gk, gc, gt, gw, gts)
+    assert len(gk) == len(ok) > 0
+    assert np.array_equal(gk, ok)               # bit-exact key set
+    assert np.array_equal(gc, oc)
+    assert np.array_equal(gw, ow)               # bit-exact integer weights
+    assert np.array_equal(gts, ots)
+    assert np.max(np.abs(gt - ot)) <= TSDF_TOL  # tsdf is stored in truncation units
+
+
+def _cam_depth(pts, T_WS):
+    Tinv = np.linalg.inv(T_WS.astype(np.float64))
+    p = pts.reshape(-1, 3).astype(np.float64) @ Tinv[:3, :3].T + Tinv[:3, 3]
+    return p[:, 2].reshape(pts.shape[:2])
+
+
+def _gpu_raycast(gpu, gm, gs, T):
+    import torch
+    pts = torch.zeros((gs.height, gs.width, 3), dtype=torch.float32, device="cuda")
+    nrm = torch.zeros_like(pts)
+    sc = torch.zeros((gs.height, gs.width), dtype=torch.int8, device="cuda")
+    gpu.raycast_volume(gm, gs, T, pts, nrm, sc)
+    torch.cuda.synchronize()
+    return pts.cpu().numpy(), nrm.cpu().numpy(), sc.cpu().numpy()
+
+
+def test_raycast_matches(seq320, gpu):
+    for k in (3, len(seq320["poses"]) - 1):
+        T = seq320["poses"][k].astype(np.float32)
+        op, on, _ = seq320["om"].raycast(seq320["os"], T)
+        gp, gn, _ = _gpu_raycast(gpu, seq320["gm"], seq320["gs"], T)
+        ohit = (op != 0).any(-1)
+        ghit = (gp != 0).any(-1)
+        assert (ohit == ghit).mean() >= DEPTH_FRAC
+        both = ohit & ghit
+        assert both.mean() > 0.5
+        dz = np.abs(_cam_depth(gp, T) - _cam_depth(op, T))[both]
+        assert (dz <= DEPTH_TOL_M).mean() >= DEPTH_FRAC, np.quantile(dz, [0.5, 0.999, 1.0])
+        on_ok = (on != 0).any(-1) & both
+        cosang = np.sum(gn[on_ok] * on[on_ok], -1)
+        assert (cosang > 1 - 1e-6).mean() >= DEPTH_FRAC
+
+
+def test_track_matches(seq320, oracle, gpu):
+    import torch
+    from supereight2_gb300 import synthetic as syn
+    k = len(seq320["poses"]) - 2
+    T_ref = seq320["poses"][k].astype(np.float32)
+    # reference images from each implementation's own raycast (they agree, see above)
+    op, on, _ = seq320["om"].raycast(seq320["os"], T_ref)
+    gp, gn, _ = _gpu_raycast(gpu, seq320["gm"], seq320["gs"], T_ref)
+    depth = seq320["frames"][k + 1]
+    cfg_o = oracle.tracker_config()
+    acc_o, T_o, st_o = oracle.track(seq320["os"], cfg_o, depth, T_ref, op, on)
+    tracker = gpu.Tracker(seq320["gm"], seq320["gs"], gpu.TrackerConfig())
+    T_g = T_ref.copy()
+    acc_g = tracker.track(torch.from_numpy(depth).cuda(), T_g, torch.from_numpy(gp).cuda(),
+                          torch.from_numpy(gn).cuda())
+    assert acc_g == acc_o
+    assert np.max(np.abs(T_g[:3, 3] - T_o[:3, 3])) <= POSE_TOL_M
+    dR = T_g[:3, :3].astype(np.float64) @ T_o[:3, :3].astype(np.float64).T
+    assert _rot_angle(dR) <= POSE_TOL_RAD
+    red_g, its_g = tracker.last_reduction()
+    assert abs(red_g[28] - st_o.reduction[28]) <= 2  # inlier count
+    # the tracked pose is close to the ground truth of frame k + 1
+    T_gt = seq320["poses"][k + 1]
+    assert np.linalg.norm(T_g[:3, 3] - T_gt[:3, 3]) < 0.01
+
+
+def test_field_interp_and_grad_match_oracle(seq320, gpu):
+    import torch
+    rng = np.random.default_rng(5)
+    om, gm = seq320["om"], seq320["gm"]
+    T = seq320["poses"][-1].astype(np.float32)
+    op, _, _ = om.raycast(seq320["os"], T)
+    hits = op[(op != 0).any(-1)]
+    pts = (hits[rng.choice(len(hits), 2000)] + rng.normal(0, 0.02, (2000, 3))).astype(np.float32)
+    gv, gvalid = gm.getFieldInterp(torch.from_numpy(pts).cuda())
+    gg, ggvalid = gm.getFieldGrad(torch.from_numpy(pts).cuda())
+    gv, gvalid, gg, ggvalid = (a.cpu().numpy() for a in (gv, gvalid, gg, ggvalid))
+    for i in range(len(pts)):
+        v = om.field_interp(pts[i])
+        assert (v is not None) == bool(gvalid[i])
+        if v is not None:
+            assert gv[i] == np.float32(v)
+        g = om.field_grad(pts[i])
+        assert (g is not None) == bool(ggvalid[i])
+        if g is not None:
+            assert np.array_equal(gg[i], g)
