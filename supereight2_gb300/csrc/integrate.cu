@@ -1,0 +1,270 @@
+// integrate.cu — se::MapIntegrator::integrateDepth for single-res TSDF maps.
+//
+// Four stream-ordered launches:
+//   begin_frame   snapshot the block count (blocks allocated before this frame)
+//   carve         RaycastCarver: march every valid pixel's ray across the truncation band and
+//                 insert the block of every sample (raycast_carver_impl.hpp:74-111); keys are
+//                 deduplicated within a warp (__match_any_sync) before the dense-index check
+//                 and the hash insert
+//   frustum       fetcher::frustum: old blocks whose bounding sphere and the spheres of all
+//                 their ancestor nodes below the root pass sphereInFrustum
+//                 (raycast_carver_impl.hpp:17-32, iterator.hpp:197-235)
+//   update        single-res TSDF update (singleres_tsdf_updater_impl.hpp:44-129): persistent
+//                 warps walk the uneven list of listed old blocks then new blocks, one 8^3 block
+//                 per warp and 16 voxels per lane, with no block-level barrier
+#include <cmath>
+
+#include "profile.cuh"
+#include "se_gpu_internal.cuh"
+
+namespace se_gpu {
+
+struct CarveParams {
+    Tf T_WS;
+    F3 t_WS;
+    float band;
+    float half_band;
+    float far_limit; // far_plane + band * 0.5
+    int num_steps;
+};
+
+struct FrustumParams {
+    Tf T_SW;
+    float radius[20]; // bounding-sphere radius per octant scale
+};
+
+struct UpdateParams {
+    Tf T_CV; // T_CW * T_WM * Scaling(res) * Translation(0.5)
+    int timestamp;
+};
+
+__global__ void begin_frame_kernel(int* counters, int capacity)
+{
+    const int nb = counters[kCntNumBlocks];
+    counters[kCntNumOld] = nb < capacity ? nb : capacity;
+    counters[kCntListed] = 0;
+    counters[kCntValidPixels] = 0;
+    reinterpret_cast<unsigned long long*>(counters)[kCntUpdated / 2] = 0ull;
+}
+
+// RaycastCarver::operator() hot loop. A CTA covers a 32 x 8 pixel tile, one warp per row
+// segment, so the 8 samples of neighbouring rays fall in few distinct blocks.
+__global__ void __launch_bounds__(256) carve_kernel(MapDevice m, Pinhole s, const float* __restrict__ depth,
+                                                    CarveParams cp)
+{
+    const int lane = threadIdx.x & 31;
+    const int x = blockIdx.x * 32 + lane;
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    bool valid = x < s.w && y < s.h;
+    float dv = 0.0f;
+    if (valid) {
+        dv = __ldg(&depth[x + y * s.w]);
+        valid = !(dv < s.near_plane || dv > cp.far_limit);
+    }
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    if (lane == 0 && vmask)
+        atomicAdd(&m.counters[kCntValidPixels], __popc(vmask));
+    if (!vmask)
+        return;
+
+    F3 pos = f3(0.0f, 0.0f, 0.0f), step = f3(0.0f, 0.0f, 0.0f);
+    if (valid) {
+        const F3 ray_C = back_project(s, (float) x, (float) y);
+        const F3 point_W = apply(cp.T_WS, mul(dv, ray_C));
+        const F3 rev = normalized(sub(cp.t_WS, point_W));
+        pos = sub(point_W, mul(cp.half_band, rev));
+        step = divs(mul(rev, cp.band), (float) cp.num_steps);
+    }
+    for (int i = 0; i < cp.num_steps; ++i) {
+        uint64_t key = kEmptyKey;
+        int vx = 0, vy = 0, vz = 0;
+        if (valid) {
+            if (point_to_voxel(m, pos, vx, vy, vz)) {
+                // p < dim = size * res exactly, so v < size; the mask keeps the index in range
+                // regardless (the reference's octree descent ignores bits >= size too)
+                vx &= m.size - 1;
+                vy &= m.size - 1;
+                vz &= m.size - 1;
+                key = block_key(vx, vy, vz);
+            }
+            pos = add(pos, step);
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, (unsigned long long) key);
+        if (key != kEmptyKey && lane == __ffs(peers) - 1) {
+            const int bx = vx >> 3, by = vy >> 3, bz = vz >> 3;
+            // plain (coherent) load: entries are being published by this kernel; a stale -1
+            // only costs a probe of the hash, which is the allocation arbiter
+            const int idx = m.block_index[((size_t) bz << (2 * m.log2_bps)) | ((size_t) by << m.log2_bps) | (size_t) bx];
+            if (idx < 0)
+                insert_block(m, key, bx, by, bz);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) frustum_kernel(MapDevice m, Pinhole s, FrustumParams fp)
+{
+    const int n_old = m.counters[kCntNumOld];
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < n_old; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        bool pass = false;
+        if (i < n_old) {
+            const int c0 = m.block_coord[3 * i], c1 = m.block_coord[3 * i + 1], c2 = m.block_coord[3 * i + 2];
+            pass = true;
+            for (int scale = kMaxBlockScale; scale < m.log2_size; ++scale) {
+                const int sz = 1 << scale;
+                const int n0 = c0 & ~(sz - 1), n1 = c1 & ~(sz - 1), n2 = c2 & ~(sz - 1);
+                const float off = (float) sz * 0.5f;
+                const F3 p_M = f3(((float) n0 + off) * m.res, ((float) n1 + off) * m.res, ((float) n2 + off) * m.res);
+                const F3 c_S = apply(fp.T_SW, apply(m.T_WM, p_M));
+                if (!sphere_in_frustum(s, c_S, fp.radius[scale])) {
+                    pass = false;
+                    break;
+                }
+            }
+        }
+        const unsigned pm = __ballot_sync(0xffffffffu, pass);
+        int slot0 = 0;
+        if (lane == 0 && pm)
+            slot0 = atomicAdd(&m.counters[kCntListed], __popc(pm));
+        slot0 = __shfl_sync(0xffffffffu, slot0, 0);
+        if (pass)
+            m.update_list[slot0 + __popc(pm & ((1u << lane) - 1u))] = i;
+    }
+}
+
+// FieldData<TSDF>::update (data_field_impl.hpp:39-54) preceded by the voxel's projection test
+// (singleres_tsdf_updater_impl.hpp:57-78). Voxel memory is read only when the update applies;
+// new blocks are written in full (the update doubles as their initialisation).
+template <int S>
+__global__ void __launch_bounds__(256) update_kernel(MapDevice m, Pinhole s, const float* __restrict__ depth,
+                                                     UpdateParams up)
+{
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int n_warps = (gridDim.x * blockDim.x) >> 5;
+    const int n_list = m.counters[kCntListed];
+    const int n_old = m.counters[kCntNumOld];
+    int n_new = m.counters[kCntNumBlocks];
+    n_new = n_new < m.capacity ? n_new : m.capacity;
+    const int total = n_list + (n_new - n_old);
+    const float trunc = m.trunc;
+    unsigned long long n_upd = 0;
+
+    for (int item = warp; item < total; item += n_warps) {
+        const bool is_new = item >= n_list;
+        const int blk = is_new ? n_old + (item - n_list) : m.update_list[item];
+        const int c0 = m.block_coord[3 * blk], c1 = m.block_coord[3 * blk + 1], c2 = m.block_coord[3 * blk + 2];
+        if (lane == 0)
+            m.block_ts[blk] = up.timestamp;
+#pragma unroll 4
+        for (int k = 0; k < kBlockVoxels / 32; ++k) {
+            const int vi = lane + 32 * k;
+            const int x = vi & 7, y = (vi >> 3) & 7, z = vi >> 6;
+            bool do_update = false;
+            float upd = 0.0f;
+            const F3 p_C = apply(up.T_CV, f3((float) (c0 + x), (float) (c1 + y), (float) (c2 + z)));
+            const float sq = dot(p_C, p_C);
+            const float pn = sqrtf(sq);
+            // farDist(p) = far / p.normalized().z
+            const float nz = sq > 0.0f ? p_C.z / pn : p_C.z;
+            if (!(pn > s.far_plane / nz)) {
+                float u, v;
+                if (project(s, p_C, u, v)) {
+                    const int px = (int) (u + 0.5f), py = (int) (v + 0.5f);
+                    const float dv = __ldg(&depth[px + py * s.w]);
+                    if (!(dv < s.near_plane)) {
+                        const float mz = p_C.z;
+                        const float sdf = (dv - mz) / mz * pn;
+                        if (!(sdf < -trunc)) {
+                            const float r = sdf / trunc;
+                            upd = (1.0f < r) ? 1.0f : r;
+                            do_update = true;
+                        }
+                    }
+                }
+            }
+            if (do_update || is_new) {
+                float tsdf = 1.0f, w = 0.0f;
+                if (!is_new)
+                    load_voxel<S>(m, blk, vi, tsdf, w);
+                if (do_update) {
+                    if (w < m.max_weight)
+                        w = w + 1.0f;
+                    tsdf = (tsdf * (w - 1.0f) + upd) / w;
+                    ++n_upd;
+                }
+                store_voxel<S>(m, blk, vi, tsdf, w);
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        n_upd += __shfl_down_sync(0xffffffffu, n_upd, o);
+    if (lane == 0 && n_upd)
+        atomicAdd(reinterpret_cast<unsigned long long*>(m.counters) + kCntUpdated / 2, n_upd);
+}
+
+} // namespace se_gpu
+
+using namespace se_gpu;
+
+extern "C" se_gpu_status se_gpu_integrate_depth(se_gpu_map* map, const float* depth_dev,
+                                                const se_gpu_pinhole* sensor, const float T_WC[16],
+                                                int timestamp, void* stream_p)
+{
+    if (!map || !depth_dev || !sensor || !T_WC || sensor->width <= 0 || sensor->height <= 0) {
+        set_last_error("se_gpu_integrate_depth: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    map->last_stream = stream;
+    MapDevice& m = map->dev;
+    const Pinhole s = make_pinhole(*sensor);
+    const Tf T_WS = tf_from16(T_WC);
+
+    CarveParams cp;
+    cp.T_WS = T_WS;
+    cp.t_WS = f3(T_WS.t[0], T_WS.t[1], T_WS.t[2]);
+    cp.band = 2.0f * m.res * map->config.truncation_boundary_factor;
+    cp.half_band = cp.band * 0.5f;
+    cp.far_limit = s.far_plane + cp.band * 0.5f;
+    cp.num_steps = (int) std::ceil(cp.band / (2.0f * m.res));
+
+    FrustumParams fp;
+    fp.T_SW = inverse_iso(T_WS);
+    for (int sc = 0; sc < 20; ++sc)
+        fp.radius[sc] = std::sqrt(3.0f) / 2.0f * m.res * (float) (1 << (sc < 19 ? sc : 19));
+
+    UpdateParams up;
+    Tf T_CV = compose(inverse_iso(T_WS), m.T_WM);
+    for (int i = 0; i < 9; ++i)
+        T_CV.R[i] = T_CV.R[i] * m.res;
+    for (int i = 0; i < 3; ++i)
+        T_CV.t[i] = ((T_CV.R[3 * i] * 0.5f + T_CV.R[3 * i + 1] * 0.5f) + T_CV.R[3 * i + 2] * 0.5f) + T_CV.t[i];
+    up.T_CV = T_CV;
+    up.timestamp = timestamp;
+
+    const int sms = device_sm_count();
+    {
+        ProfScope ps(kProfBeginFrame, stream);
+        begin_frame_kernel<<<1, 1, 0, stream>>>(m.counters, m.capacity);
+    }
+    {
+        ProfScope ps(kProfCarve, stream);
+        dim3 cgrid((s.w + 31) / 32, (s.h + 7) / 8);
+        carve_kernel<<<cgrid, 256, 0, stream>>>(m, s, depth_dev, cp);
+    }
+    {
+        ProfScope ps(kProfFrustum, stream);
+        frustum_kernel<<<sms * 4, 256, 0, stream>>>(m, s, fp);
+    }
+    {
+        ProfScope ps(kProfUpdate, stream);
+        if (m.storage == SE_GPU_STORAGE_F32)
+            update_kernel<SE_GPU_STORAGE_F32><<<sms * 8, 256, 0, stream>>>(m, s, depth_dev, up);
+        else
+            update_kernel<SE_GPU_STORAGE_F16><<<sms * 8, 256, 0, stream>>>(m, s, depth_dev, up);
+    }
+    SE_CUDA_TRY(cudaGetLastError());
+    return SE_GPU_OK;
+}

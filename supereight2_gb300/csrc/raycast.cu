@@ -1,21 +1,24 @@
-// raycast.cu — se::raycaster::raycast_volume for single-res TSDF maps.
+// raycast.cu — se::raycaster::raycast_volume for single-res TSDF maps, and the batched
+// Map::getFieldInterp / Map::getFieldGrad queries.
 //
 // One thread per pixel (an 8 x 4 pixel tile per warp for coherent block lookups):
 //   1. first allocated block on the ray: the sparse-voxel-octree traversal of
 //      VoxelBlockRayIterator (voxel_block_ray_iterator_impl.hpp:19-249, Laine & Karras 2010)
-//      with the same float expressions, but node existence is a bit test in the occupancy
-//      pyramid instead of a child-pointer chase, and the traversal stack keeps only t_max;
+//      with the same float expressions; node existence is a bit test in the occupancy pyramid
+//      instead of a child-pointer chase, and the traversal stack keeps only t_max;
 //   2. the TSDF march of raycast<TSDF> (raycaster_impl.hpp:456-533): voxel fetches through the
-//      block hash with a one-block cache, trilinear interpolation near the surface
+//      dense block index with a one-block cache, trilinear interpolation near the surface
 //      (visitor_impl.hpp:976-1024) and the linear zero-crossing estimate;
 //   3. the surface normal from the 32-sample central-difference gradient
 //      (visitor_impl.hpp:1094-1251, map_impl.hpp:236-262).
+// Sample loops are deliberately not unrolled: one copy of the fetch path keeps the kernel
+// inside the instruction cache.
+#include <cmath>
+
 #include "profile.cuh"
 #include "se_gpu_internal.cuh"
 
 namespace se_gpu {
-
-int device_sm_count();
 
 struct RaycastParams {
     Tf T_WS;
@@ -24,8 +27,6 @@ struct RaycastParams {
     int min_scale; // 23 - log2(size / 8)
 };
 
-__device__ __forceinline__ int f_as_i(float f) { return __float_as_int(f); }
-__device__ __forceinline__ float i_as_f(int i) { return __int_as_float(i); }
 __device__ __forceinline__ float fmax_std(float a, float b) { return (a < b) ? b : a; } // std::max
 __device__ __forceinline__ float fmin_std(float a, float b) { return (b < a) ? b : a; } // std::min
 
@@ -77,8 +78,8 @@ __device__ bool first_block(const MapDevice& m, const RaycastParams& rp, F3 o_W,
     for (int i = 0; i < kStackDepth; ++i)
         stack_tmax[i] = 0.0f;
 
-    // Bounded: each iteration either descends (at most 23 levels between advances) or advances
-    // the ray past a cell boundary; the cap only guards against a malformed map.
+    // Bounded: every iteration descends (at most 23 times between advances) or advances the
+    // ray past a cell boundary; the cap only guards against a malformed map.
     for (int iter = 0; iter < (1 << 20) && scale < kStackDepth; ++iter) {
         float tc[3];
 #pragma unroll
@@ -86,7 +87,9 @@ __device__ bool first_block(const MapDevice& m, const RaycastParams& rp, F3 o_W,
             tc[a] = pos[a] * t_coef[a] - t_bias[a];
         const float tc_max = fmin_std(fmin_std(tc[0], tc[1]), tc[2]);
 
-        // child at (pos, scale): mirrored cell index from the float bits, then real index
+        // The child at (pos, scale). Its index in the mirrored frame comes from the float bits
+        // of pos (pos is in [1, 2), cells of side 2^(scale - 23)); mirrored axes flip back to
+        // the real index, which is the cell idx ^ mirror_mask ^ 7 of the reference.
         const int L = scale - rp.min_scale;
         bool child = false;
         if (L >= 0) {
@@ -95,10 +98,9 @@ __device__ bool first_block(const MapDevice& m, const RaycastParams& rp, F3 o_W,
             uint32_t c[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                const uint32_t k = (uint32_t) (f_as_i(pos[a]) - 0x3f800000) >> scale;
+                const uint32_t k = (uint32_t) (__float_as_int(pos[a]) - 0x3f800000) >> scale;
                 c[a] = (mirror_mask & (1 << a)) ? k : (n - 1u - k);
             }
-            // idx ^ mirror_mask ^ 7 picks the same cell as the mirrored position above
             child = occ_test(m, L, c[0], c[1], c[2]);
         }
         if (scale == rp.min_scale && child) {
@@ -145,17 +147,17 @@ __device__ bool first_block(const MapDevice& m, const RaycastParams& rp, F3 o_W,
 #pragma unroll
             for (int a = 0; a < 3; ++a)
                 if (step_mask & (1 << a))
-                    differing |= (uint32_t) (f_as_i(pos[a]) ^ f_as_i(pos[a] + scale_exp2));
-            scale = (f_as_i((float) differing) >> 23) - 127;
+                    differing |= (uint32_t) (__float_as_int(pos[a]) ^ __float_as_int(pos[a] + scale_exp2));
+            scale = (__float_as_int((float) differing) >> 23) - 127;
             if (scale >= kStackDepth)
                 break;
-            scale_exp2 = i_as_f((scale - kStackDepth + 127) << 23);
+            scale_exp2 = __int_as_float((scale - kStackDepth + 127) << 23);
             t_max = stack_tmax[scale];
             int sh[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                sh[a] = f_as_i(pos[a]) >> scale;
-                pos[a] = i_as_f(sh[a] << scale);
+                sh[a] = __float_as_int(pos[a]) >> scale;
+                pos[a] = __int_as_float(sh[a] << scale);
             }
             idx = (sh[0] & 1) | ((sh[1] & 1) << 1) | ((sh[2] & 1) << 2);
             h = 0.0f;
@@ -165,7 +167,7 @@ __device__ bool first_block(const MapDevice& m, const RaycastParams& rp, F3 o_W,
     return false;
 }
 
-// Block lookup with a one-entry cache of the last block touched by this thread.
+// One-entry cache of the last block touched by this thread.
 struct BlockCache {
     int bx, by, bz;
     int idx; // pool index or -1
@@ -178,12 +180,13 @@ __device__ __forceinline__ int lookup_block(const MapDevice& m, BlockCache& c, i
         c.bx = bx;
         c.by = by;
         c.bz = bz;
-        c.idx = occ_test(m, 0, (uint32_t) bx, (uint32_t) by, (uint32_t) bz) ? hash_find(m, block_key(vx, vy, vz)) : -1;
+        c.idx = __ldg(&m.block_index[((size_t) bz << (2 * m.log2_bps)) | ((size_t) by << m.log2_bps) | (size_t) bx]);
     }
     return c.idx;
 }
 
 // visitor::getData single-res: block voxel or the default data (tsdf 1, weight 0).
+template <int S>
 __device__ __forceinline__ bool fetch_voxel(const MapDevice& m, BlockCache& c, int vx, int vy, int vz, float& t,
                                             float& w)
 {
@@ -193,10 +196,11 @@ __device__ __forceinline__ bool fetch_voxel(const MapDevice& m, BlockCache& c, i
         w = 0.0f;
         return false;
     }
-    load_voxel(m, b, (vx & 7) + 8 * (vy & 7) + 64 * (vz & 7), t, w);
+    load_voxel<S>(m, b, (vx & 7) + 8 * (vy & 7) + 64 * (vz & 7), t, w);
     return true;
 }
 
+template <int S>
 __device__ __forceinline__ void map_get_data(const MapDevice& m, BlockCache& c, F3 p, float& t, float& w)
 {
     int vx, vy, vz;
@@ -205,9 +209,11 @@ __device__ __forceinline__ void map_get_data(const MapDevice& m, BlockCache& c, 
         w = 0.0f;
         return;
     }
-    fetch_voxel(m, c, vx, vy, vz, t, w);
+    fetch_voxel<S>(m, c, vx, vy, vz, t, w);
 }
 
+// visitor::getInterp single-res: any unallocated block or invalid voxel gives nullopt.
+template <int S>
 __device__ bool field_interp(const MapDevice& m, BlockCache& c, F3 p_W, float& out)
 {
     F3 vf;
@@ -217,16 +223,35 @@ __device__ bool field_interp(const MapDevice& m, BlockCache& c, F3 p_W, float& o
     const int b0 = (int) bf.x, b1 = (int) bf.y, b2 = (int) bf.z;
     if (b0 < 0 || b1 < 0 || b2 < 0 || b0 + 1 >= m.size || b1 + 1 >= m.size || b2 + 1 >= m.size)
         return false;
-    float f[8], wt[8];
+    float f[8];
+    if ((b0 & 7) != 7 && (b1 & 7) != 7 && (b2 & 7) != 7) {
+        // the 8 neighbours share one block
+        const int blk = lookup_block(m, c, b0, b1, b2);
+        if (blk < 0)
+            return false;
+        const int base = (b0 & 7) + 8 * (b1 & 7) + 64 * (b2 & 7);
+        bool ok = true;
 #pragma unroll
-    for (int n = 0; n < 8; ++n) {
-        if (!fetch_voxel(m, c, b0 + (n & 1), b1 + ((n >> 1) & 1), b2 + ((n >> 2) & 1), f[n], wt[n]))
+        for (int n = 0; n < 8; ++n) {
+            float w;
+            load_voxel<S>(m, blk, base + (n & 1) + 8 * ((n >> 1) & 1) + 64 * (n >> 2), f[n], w);
+            ok = ok && (w != 0.0f);
+        }
+        if (!ok)
             return false;
     }
-#pragma unroll
-    for (int n = 0; n < 8; ++n)
-        if (!(wt[n] != 0.0f))
+    else {
+        bool ok = true;
+#pragma unroll 1
+        for (int n = 0; n < 8; ++n) {
+            float w;
+            if (!fetch_voxel<S>(m, c, b0 + (n & 1), b1 + ((n >> 1) & 1), b2 + ((n >> 2) & 1), f[n], w))
+                return false; // an unallocated block fails before any validity test
+            ok = ok && (w != 0.0f);
+        }
+        if (!ok)
             return false;
+    }
     const F3 t = f3(bf.x - floorf(bf.x), bf.y - floorf(bf.y), bf.z - floorf(bf.z));
     const F3 tc = f3(1.0f - t.x, 1.0f - t.y, 1.0f - t.z);
     out = ((f[0] * tc.x + f[1] * t.x) * tc.y + (f[2] * tc.x + f[3] * t.x) * t.y) * tc.z
@@ -234,7 +259,14 @@ __device__ bool field_interp(const MapDevice& m, BlockCache& c, F3 p_W, float& o
     return true;
 }
 
+// The 32 gradient samples: per axis a selector of {base-1, base, base+1, base+2} (clamped to
+// the map), in the reference's order. Packed 2 bits per axis: x | y << 2 | z << 4.
+__constant__ unsigned char kGradSel[32] = {
+    0x14, 0x18, 0x24, 0x28, 0x11, 0x21, 0x05, 0x15, 0x25, 0x35, 0x09, 0x19, 0x29, 0x39, 0x1d, 0x2d,
+    0x12, 0x22, 0x06, 0x16, 0x26, 0x36, 0x0a, 0x1a, 0x2a, 0x3a, 0x1e, 0x2e, 0x17, 0x1b, 0x27, 0x2b};
+
 // visitor::getFieldGrad single-res with Map::getFieldGrad's division by the resolution.
+template <int S>
 __device__ bool field_grad(const MapDevice& m, BlockCache& c, F3 p_W, F3& g)
 {
     F3 vf;
@@ -244,32 +276,22 @@ __device__ bool field_grad(const MapDevice& m, BlockCache& c, F3 p_W, F3& g)
     const F3 fac = f3(s.x - floorf(s.x), s.y - floorf(s.y), s.z - floorf(s.z));
     const int base[3] = {(int) s.x, (int) s.y, (int) s.z};
     const int top = m.size - 1;
-    int ll[3], lu[3], ul[3], uu[3];
+    int sel[3][4];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        ll[i] = max(base[i] - 1, 0);
-        lu[i] = max(base[i], 0);
-        ul[i] = min(base[i] + 1, top);
-        uu[i] = min(base[i] + 2, top);
+        sel[i][0] = max(base[i] - 1, 0);
+        sel[i][1] = max(base[i], 0);
+        sel[i][2] = min(base[i] + 1, top);
+        sel[i][3] = min(base[i] + 2, top);
     }
     if (lookup_block(m, c, base[0], base[1], base[2]) < 0)
         return false;
-    // 32 samples: selector per axis, 0 = ll, 1 = lu, 2 = ul, 3 = uu (reference order)
-    constexpr unsigned char SX[32] = {0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1,
-                                      2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 3, 3, 3, 3};
-    constexpr unsigned char SY[32] = {1, 2, 1, 2, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3,
-                                      0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 1, 2, 1, 2};
-    constexpr unsigned char SZ[32] = {1, 1, 2, 2, 1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 1, 2,
-                                      1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 1, 2, 1, 1, 2, 2};
     float v[32];
-#pragma unroll
+#pragma unroll 1
     for (int i = 0; i < 32; ++i) {
-        const int sx = SX[i], sy = SY[i], sz = SZ[i];
-        const int cx = sx == 0 ? ll[0] : sx == 1 ? lu[0] : sx == 2 ? ul[0] : uu[0];
-        const int cy = sy == 0 ? ll[1] : sy == 1 ? lu[1] : sy == 2 ? ul[1] : uu[1];
-        const int cz = sz == 0 ? ll[2] : sz == 1 ? lu[2] : sz == 2 ? ul[2] : uu[2];
+        const int code = kGradSel[i];
         float t, w;
-        fetch_voxel(m, c, cx, cy, cz, t, w);
+        fetch_voxel<S>(m, c, sel[0][code & 3], sel[1][(code >> 2) & 3], sel[2][(code >> 4) & 3], t, w);
         if (!(w != 0.0f))
             return false;
         v[i] = t;
@@ -291,6 +313,7 @@ __device__ bool field_grad(const MapDevice& m, BlockCache& c, F3 p_W, F3& g)
     return true;
 }
 
+template <int S>
 __device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockCache& c, F3 o, F3 d, float t_near,
                              float t_far, F3& hit)
 {
@@ -306,23 +329,23 @@ __device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockC
     float stepsize = largestep;
     F3 p = add(o, mul(d, t));
     float f_t, w_t;
-    map_get_data(m, c, p, f_t, w_t);
+    map_get_data<S>(m, c, p, f_t, w_t);
     float f_tt = 0.0f;
     if (!(f_t >= 0.0f))
         return false;
-    // The march ends at t_far: every step is at least res, so it is bounded by (t_far - t)/res.
+    // every step is at least res > 0, so the march ends at t_far (NaN poses end it at once)
     for (; t < t_far; t += stepsize) {
         float f, w;
-        map_get_data(m, c, p, f, w);
+        map_get_data<S>(m, c, p, f, w);
         if (!(w != 0.0f)) {
             stepsize = largestep;
             p = add(p, mul(stepsize, d));
             continue;
         }
         f_tt = f;
-        if ((double) f_tt <= 0.1 && f_tt >= -0.5f) {
+        if ((double) f_tt <= 0.1 && f_tt >= -0.5f) { // the reference compares with double 0.1
             float fi;
-            if (field_interp(m, c, p, fi))
+            if (field_interp<S>(m, c, p, fi))
                 f_tt = fi;
         }
         if (f_tt < 0.0f)
@@ -339,6 +362,7 @@ __device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockC
     return false;
 }
 
+template <int S>
 __global__ void __launch_bounds__(128) raycast_kernel(MapDevice m, Pinhole s, RaycastParams rp,
                                                       float* __restrict__ pts, float* __restrict__ nrm,
                                                       int8_t* __restrict__ scale)
@@ -359,10 +383,10 @@ __global__ void __launch_bounds__(128) raycast_kernel(MapDevice m, Pinhole s, Ra
     F3 hit;
     F3 n = f3(0.0f, 0.0f, 0.0f);
     F3 p = f3(0.0f, 0.0f, 0.0f);
-    if (raycast_tsdf(m, rp, c, origin, dir_W, t_near, t_far, hit)) {
+    if (raycast_tsdf<S>(m, rp, c, origin, dir_W, t_near, t_far, hit)) {
         p = hit;
         F3 g;
-        if (field_grad(m, c, hit, g))
+        if (field_grad<S>(m, c, hit, g))
             n = normalized(g);
     }
     pts[3 * idx + 0] = p.x;
@@ -375,6 +399,7 @@ __global__ void __launch_bounds__(128) raycast_kernel(MapDevice m, Pinhole s, Ra
         scale[idx] = 0;
 }
 
+template <int S>
 __global__ void field_query_kernel(MapDevice m, int n, const float* __restrict__ pts, float* __restrict__ out,
                                    int* __restrict__ valid, int grad)
 {
@@ -386,14 +411,14 @@ __global__ void field_query_kernel(MapDevice m, int n, const float* __restrict__
     bool ok;
     if (grad) {
         F3 g = f3(0.0f, 0.0f, 0.0f);
-        ok = field_grad(m, c, p, g);
+        ok = field_grad<S>(m, c, p, g);
         out[3 * i] = ok ? g.x : 0.0f;
         out[3 * i + 1] = ok ? g.y : 0.0f;
         out[3 * i + 2] = ok ? g.z : 0.0f;
     }
     else {
         float v = 0.0f;
-        ok = field_interp(m, c, p, v);
+        ok = field_interp<S>(m, c, p, v);
         out[i] = ok ? v : 0.0f;
     }
     if (valid)
@@ -403,33 +428,6 @@ __global__ void field_query_kernel(MapDevice m, int n, const float* __restrict__
 } // namespace se_gpu
 
 using namespace se_gpu;
-
-static se_gpu_status field_query(const se_gpu_map* map, int64_t n, const float* pts, float* out, int* valid,
-                                 void* stream_p, int grad)
-{
-    if (!map || n < 0 || n > (1ll << 31) - 1 || (n > 0 && (!pts || !out))) {
-        set_last_error("se_gpu_map_field_%s: invalid argument", grad ? "grad" : "interp");
-        return SE_GPU_ERR_BAD_ARG;
-    }
-    if (n == 0)
-        return SE_GPU_OK;
-    cudaStream_t stream = (cudaStream_t) stream_p;
-    field_query_kernel<<<(unsigned) ((n + 127) / 128), 128, 0, stream>>>(map->dev, (int) n, pts, out, valid, grad);
-    SE_CUDA_TRY(cudaGetLastError());
-    return SE_GPU_OK;
-}
-
-extern "C" se_gpu_status se_gpu_map_field_interp(const se_gpu_map* map, int64_t n, const float* pts, float* values,
-                                                 int* valid, void* stream)
-{
-    return field_query(map, n, pts, values, valid, stream, 0);
-}
-
-extern "C" se_gpu_status se_gpu_map_field_grad(const se_gpu_map* map, int64_t n, const float* pts, float* grads,
-                                               int* valid, void* stream)
-{
-    return field_query(map, n, pts, grads, valid, stream, 1);
-}
 
 extern "C" se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinhole* sensor, const float T_WS[16],
                                         float* pts_dev, float* nrm_dev, int8_t* scale_dev, void* stream_p)
@@ -449,7 +447,41 @@ extern "C" se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinh
     rp.min_scale = 23 - m.log2_bps;
     dim3 grid((s.w + 15) / 16, (s.h + 7) / 8);
     ProfScope ps(kProfRaycast, stream);
-    raycast_kernel<<<grid, 128, 0, stream>>>(m, s, rp, pts_dev, nrm_dev, scale_dev);
+    if (m.storage == SE_GPU_STORAGE_F32)
+        raycast_kernel<SE_GPU_STORAGE_F32><<<grid, 128, 0, stream>>>(m, s, rp, pts_dev, nrm_dev, scale_dev);
+    else
+        raycast_kernel<SE_GPU_STORAGE_F16><<<grid, 128, 0, stream>>>(m, s, rp, pts_dev, nrm_dev, scale_dev);
     SE_CUDA_TRY(cudaGetLastError());
     return SE_GPU_OK;
+}
+
+static se_gpu_status field_query(const se_gpu_map* map, int64_t n, const float* pts, float* out, int* valid,
+                                 void* stream_p, int grad)
+{
+    if (!map || n < 0 || n > (1ll << 31) - 1 || (n > 0 && (!pts || !out))) {
+        set_last_error("se_gpu_map_field_%s: invalid argument", grad ? "grad" : "interp");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    if (n == 0)
+        return SE_GPU_OK;
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    const unsigned blocks = (unsigned) ((n + 127) / 128);
+    if (map->dev.storage == SE_GPU_STORAGE_F32)
+        field_query_kernel<SE_GPU_STORAGE_F32><<<blocks, 128, 0, stream>>>(map->dev, (int) n, pts, out, valid, grad);
+    else
+        field_query_kernel<SE_GPU_STORAGE_F16><<<blocks, 128, 0, stream>>>(map->dev, (int) n, pts, out, valid, grad);
+    SE_CUDA_TRY(cudaGetLastError());
+    return SE_GPU_OK;
+}
+
+extern "C" se_gpu_status se_gpu_map_field_interp(const se_gpu_map* map, int64_t n, const float* pts, float* values,
+                                                 int* valid, void* stream)
+{
+    return field_query(map, n, pts, values, valid, stream, 0);
+}
+
+extern "C" se_gpu_status se_gpu_map_field_grad(const se_gpu_map* map, int64_t n, const float* pts, float* grads,
+                                               int* valid, void* stream)
+{
+    return field_query(map, n, pts, grads, valid, stream, 1);
 }

@@ -184,6 +184,10 @@ struct MapDevice {
     // exactly when the reference's pointer octree holds the node.
     uint32_t* occ[11];
     int occ_levels;               // log2(bps) + 1
+    // Dense block index, bps^3 int32 (x fastest), -1 where no block is allocated: one load
+    // per lookup on the read paths (at most 1024^3 entries = 4 GiB for an 8192^3 map). The
+    // hash above stays the allocation arbiter and the Morton-key index.
+    int* block_index;
     // scratch / counters
     int* counters;                // kNumCounters ints
     int* update_list;             // capacity ints
@@ -211,10 +215,18 @@ __device__ __forceinline__ bool occ_test(const MapDevice& m, int L, uint32_t cx,
     return (__ldg(&m.occ[L][bit >> 5]) >> (bit & 31)) & 1u;
 }
 
-// voxel data access (F32 and F16 layouts)
+// Pool index of the block containing voxel block coordinates (bx, by, bz), or -1.
+__device__ __forceinline__ int block_at(const MapDevice& m, int bx, int by, int bz)
+{
+    return m.block_index[((size_t) bz << (2 * m.log2_bps)) | ((size_t) by << m.log2_bps) | (size_t) bx];
+}
+
+// Voxel data access; S is the se_gpu_storage layout (F32: float2 {tsdf, weight};
+// F16: uint32 {half tsdf | u16 weight << 16}).
+template <int S>
 __device__ __forceinline__ void load_voxel(const MapDevice& m, int blk, int vi, float& tsdf, float& w)
 {
-    if (m.storage == SE_GPU_STORAGE_F32) {
+    if (S == SE_GPU_STORAGE_F32) {
         const float2 d = reinterpret_cast<const float2*>(m.voxels)[(size_t) blk * kBlockVoxels + vi];
         tsdf = d.x;
         w = d.y;
@@ -225,9 +237,10 @@ __device__ __forceinline__ void load_voxel(const MapDevice& m, int blk, int vi, 
         w = (float) (d >> 16);
     }
 }
+template <int S>
 __device__ __forceinline__ void store_voxel(const MapDevice& m, int blk, int vi, float tsdf, float w)
 {
-    if (m.storage == SE_GPU_STORAGE_F32) {
+    if (S == SE_GPU_STORAGE_F32) {
         reinterpret_cast<float2*>(m.voxels)[(size_t) blk * kBlockVoxels + vi] = make_float2(tsdf, w);
     }
     else {
@@ -316,3 +329,52 @@ struct se_gpu_map {
     cudaStream_t last_stream;
     int host_num_blocks_hint;
 };
+
+namespace se_gpu {
+
+// Insert a block key that the caller did not find; the thread whose CAS claims an empty hash
+// slot allocates the pool entry and publishes it in the dense index and the occupancy pyramid.
+// Probing is bounded: on exhaustion the map latches kErrProbeLimit.
+__device__ __forceinline__ void insert_block(const MapDevice& m, uint64_t key, int bx, int by, int bz)
+{
+    uint32_t slot = hash_slot(key, m.hash_mask);
+    for (int p = 0; p < kMaxProbe; ++p) {
+        unsigned long long* kp = &m.hash[slot].x;
+        const unsigned long long k = *((volatile unsigned long long*) kp);
+        if (k == key)
+            return;
+        if (k == kEmptyKey) {
+            const unsigned long long prev = atomicCAS(kp, kEmptyKey, (unsigned long long) key);
+            if (prev == key)
+                return;
+            if (prev == kEmptyKey) {
+                const int idx = atomicAdd(&m.counters[kCntNumBlocks], 1);
+                if (idx >= m.capacity) {
+                    m.hash[slot].y = (unsigned long long) (long long) -1;
+                    atomicOr(&m.counters[kCntError], kErrPoolFull);
+                    return;
+                }
+                m.hash[slot].y = (unsigned long long) idx;
+                m.block_coord[3 * idx + 0] = bx << 3;
+                m.block_coord[3 * idx + 1] = by << 3;
+                m.block_coord[3 * idx + 2] = bz << 3;
+                m.block_keys[idx] = key;
+                m.block_ts[idx] = -1;
+                m.block_index[((size_t) bz << (2 * m.log2_bps)) | ((size_t) by << m.log2_bps) | (size_t) bx] = idx;
+                for (int L = 0; L < m.occ_levels; ++L) {
+                    const int lg = m.log2_bps - L;
+                    const uint32_t cx = (uint32_t) bx >> L, cy = (uint32_t) by >> L, cz = (uint32_t) bz >> L;
+                    const uint32_t bit = (cz << (2 * lg)) | (cy << lg) | cx;
+                    atomicOr(&m.occ[L][bit >> 5], 1u << (bit & 31));
+                }
+                return;
+            }
+        }
+        slot = (slot + 1) & m.hash_mask;
+    }
+    atomicOr(&m.counters[kCntError], kErrProbeLimit);
+}
+
+int device_sm_count();
+
+} // namespace se_gpu

@@ -184,28 +184,35 @@ __global__ void track_init_kernel(TrackState* st, TrackInit init)
 }
 
 // ---------------------------------------------------------------------- FP64 solve --
+// se(3) exponential (math_util_impl.hpp:117-174) in FP64: quaternion rotation from
+// (cos(theta/2), sin(theta/2)/theta * omega), V = I + (1-cos)/theta^2 W + (theta-sin)/theta^3 W^2.
+// sin(theta) and cos(theta) come from the half angle (2 s c, 1 - 2 s^2): one sincos call.
 __device__ void se3_exp_d(const double a[6], double R[9], double t[3])
 {
     const double wx = a[3], wy = a[4], wz = a[5];
     const double theta_sq = (wx * wx + wy * wy) + wz * wz;
     const double theta = sqrt(theta_sq);
-    const double half_theta = 0.5 * theta;
-    double imag, real;
-    if (theta < 1e-10) {
+    double imag, real, sin_t = 0.0, cos_t = 1.0;
+    const bool small = theta < 1e-10;
+    if (small) {
         const double t4 = theta_sq * theta_sq;
         imag = 0.5 - 1.0 / 48.0 * theta_sq + 1.0 / 3840.0 * t4;
         real = 1.0 - 0.5 * theta_sq + 1.0 / 384.0 * t4;
     }
     else {
-        imag = sin(half_theta) / theta;
-        real = cos(half_theta);
+        double sh, ch;
+        sincos(0.5 * theta, &sh, &ch);
+        imag = sh / theta;
+        real = ch;
+        sin_t = 2.0 * sh * ch;
+        cos_t = 1.0 - 2.0 * sh * sh;
     }
     double qw = real, qx = imag * wx, qy = imag * wy, qz = imag * wz;
-    const double qn = sqrt(((qx * qx + qy * qy) + qz * qz) + qw * qw);
-    qw /= qn;
-    qx /= qn;
-    qy /= qn;
-    qz /= qn;
+    const double inv_qn = 1.0 / sqrt(((qx * qx + qy * qy) + qz * qz) + qw * qw);
+    qw *= inv_qn;
+    qx *= inv_qn;
+    qy *= inv_qn;
+    qz *= inv_qn;
     const double tx = 2 * qx, ty = 2 * qy, tz = 2 * qz;
     const double twx = tx * qw, twy = ty * qw, twz = tz * qw;
     const double txx = tx * qx, txy = ty * qx, txz = tz * qx;
@@ -215,14 +222,14 @@ __device__ void se3_exp_d(const double a[6], double R[9], double t[3])
     R[6] = txz - twy;       R[7] = tyz + twx;       R[8] = 1 - (txx + tyy);
     const double O[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
     double V[9];
-    if (theta < 1e-10) {
+    if (small) {
         for (int i = 0; i < 9; ++i)
             V[i] = R[i];
     }
     else {
-        const double tsq = theta * theta;
-        const double c1 = (1.0 - cos(theta)) / tsq;
-        const double c2 = (theta - sin(theta)) / (tsq * theta);
+        const double inv_tsq = 1.0 / theta_sq;
+        const double c1 = (1.0 - cos_t) * inv_tsq;
+        const double c2 = (theta - sin_t) * inv_tsq / theta;
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) {
                 const double o2 = (O[3 * i] * O[j] + O[3 * i + 1] * O[3 + j]) + O[3 * i + 2] * O[6 + j];
@@ -233,10 +240,11 @@ __device__ void se3_exp_d(const double a[6], double R[9], double t[3])
         t[i] = (V[3 * i] * a[0] + V[3 * i + 1] * a[1]) + V[3 * i + 2] * a[2];
 }
 
-// LDL^T of the symmetric 6x6 J^T J without pivoting; false on a non-positive pivot.
+// LDL^T of the symmetric 6x6 J^T J without pivoting; false on a non-positive pivot (the
+// reference's LLT then returns a zero update, icp.cpp:33-41).
 __device__ bool ldlt_solve6(const double C[36], const double b[6], double x[6])
 {
-    double L[36], D[6];
+    double L[36], D[6], inv_d[6];
     for (int j = 0; j < 6; ++j) {
         double dj = C[6 * j + j];
         for (int k = 0; k < j; ++k)
@@ -244,12 +252,13 @@ __device__ bool ldlt_solve6(const double C[36], const double b[6], double x[6])
         if (!(dj > 0.0))
             return false;
         D[j] = dj;
+        inv_d[j] = 1.0 / dj;
         L[6 * j + j] = 1.0;
         for (int i = j + 1; i < 6; ++i) {
             double v = C[6 * i + j];
             for (int k = 0; k < j; ++k)
                 v -= L[6 * i + k] * L[6 * j + k] * D[k];
-            L[6 * i + j] = v / dj;
+            L[6 * i + j] = v * inv_d[j];
         }
     }
     double y[6];
@@ -260,7 +269,7 @@ __device__ bool ldlt_solve6(const double C[36], const double b[6], double x[6])
         y[i] = s;
     }
     for (int i = 0; i < 6; ++i)
-        y[i] /= D[i];
+        y[i] *= inv_d[i];
     for (int i = 5; i >= 0; --i) {
         double s = y[i];
         for (int k = i + 1; k < 6; ++k)
@@ -281,11 +290,89 @@ struct IterParams {
     float dist_threshold, normal_threshold, icp_threshold;
 };
 
+// trackKernel for one pixel (icp_impl.hpp:16-102): the 32 reduction terms of newReduce
+// (icp.cpp:45-184) in v: [e^2, e*J (6), upper J^T J (21), inlier, dist-reject, normal-reject,
+// other reject].
+__device__ __forceinline__ void icp_pixel_terms(const Pinhole& s, const IterParams& ip, const Tf& T, const Tf& Tri,
+                                                int i, float v[32])
+{
+#pragma unroll
+    for (int k = 0; k < 32; ++k)
+        v[k] = 0.0f;
+    const F3 n_in = ld3(ip.nrm, (size_t) i);
+    int result;
+    float e = 0.0f;
+    float J[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    if (n_in.x == 0.0f && n_in.y == 0.0f && n_in.z == 0.0f) {
+        result = -1;
+    }
+    else {
+        const F3 p_W = apply(T, ld3(ip.pts, (size_t) i));
+        const F3 p_ref = apply(Tri, p_W);
+        float u, vv;
+        if (!project(s, p_ref, u, vv)) {
+            result = -2;
+        }
+        else {
+            const int px = (int) (u + 0.5f), py = (int) (vv + 0.5f);
+            const size_t ri = (size_t) px + (size_t) py * ip.W;
+            const F3 rn = ld3(ip.ref_nrm, ri);
+            const F3 n_ref = f3(-rn.x, -rn.y, -rn.z);
+            if (n_ref.x == 0.0f && n_ref.y == 0.0f && n_ref.z == 0.0f) {
+                result = -3;
+            }
+            else {
+                const F3 diff = sub(ld3(ip.ref_pts, ri), p_W);
+                const F3 n_W = rot(T, n_in);
+                if (norm(diff) > ip.dist_threshold) {
+                    result = -4;
+                }
+                else if (dot(n_W, n_ref) < ip.normal_threshold) {
+                    result = -5;
+                }
+                else {
+                    result = 1;
+                    e = dot(n_ref, diff);
+                    const F3 c = cross(p_W, n_ref);
+                    J[0] = n_ref.x;
+                    J[1] = n_ref.y;
+                    J[2] = n_ref.z;
+                    J[3] = c.x;
+                    J[4] = c.y;
+                    J[5] = c.z;
+                }
+            }
+        }
+    }
+    if (result < 1) {
+        v[29] = result == -4 ? 1.0f : 0.0f;
+        v[30] = result == -5 ? 1.0f : 0.0f;
+        v[31] = result > -4 ? 1.0f : 0.0f;
+        return;
+    }
+    v[0] = e * e;
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        v[1 + k] = e * J[k];
+    int q = 7;
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = r; c < 6; ++c)
+            v[q++] = J[r] * J[c];
+    v[28] = 1.0f;
+}
+
 // One ICP iteration: trackKernel + newReduce/reduceKernel + updatePoseKernel.
+// Each warp handles 32 pixels per tile; the 32 x 32 term matrix goes through shared memory
+// (stride 33: conflict-free) so that lane k accumulates column k with two-sum compensation.
 __global__ void __launch_bounds__(kTrackThreads) icp_iter_kernel(Pinhole s, IterParams ip, TrackState* st,
                                                                 float2* __restrict__ partials)
 {
-    __shared__ float2 sh_warp[kTrackThreads / 32][32];
+    constexpr int kWarps = kTrackThreads / 32;
+    __shared__ float sh_terms[kWarps][32][33];
+    __shared__ float2 sh_warp[kWarps][32];
+    __shared__ float2 sh_chunk[kWarps][32];
     __shared__ int sh_last;
     if (st->flags[kFlagDone0 + ip.level])
         return;
@@ -300,100 +387,34 @@ __global__ void __launch_bounds__(kTrackThreads) icp_iter_kernel(Pinhole s, Iter
         Tri.t[i] = st->ref_inv[4 * i + 3];
     }
 
-    CSum acc[32];
-#pragma unroll
-    for (int k = 0; k < 32; ++k)
-        acc[k] = CSum{0.0f, 0.0f};
-
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    CSum acc{0.0f, 0.0f}; // lane k: running compensated sum of term k over this warp's pixels
     const int npix = ip.w * ip.h;
-    for (int i = blockIdx.x * kTrackThreads + threadIdx.x; i < npix; i += gridDim.x * kTrackThreads) {
-        const int x = i % ip.w, y = i / ip.w;
-        const F3 n_in = ld3(ip.nrm, (size_t) i);
-        int result;
-        float e = 0.0f;
-        float J[6];
-        if (n_in.x == 0.0f && n_in.y == 0.0f && n_in.z == 0.0f) {
-            result = -1;
+    for (int base = blockIdx.x * kTrackThreads; base < npix; base += gridDim.x * kTrackThreads) {
+        float v[32];
+        const int i = base + threadIdx.x;
+        if (i < npix) {
+            icp_pixel_terms(s, ip, T, Tri, i, v);
         }
         else {
-            const F3 p_W = apply(T, ld3(ip.pts, (size_t) i));
-            const F3 p_ref = apply(Tri, p_W);
-            float u, v;
-            if (!project(s, p_ref, u, v)) {
-                result = -2;
-            }
-            else {
-                const int px = (int) (u + 0.5f), py = (int) (v + 0.5f);
-                const size_t ri = (size_t) px + (size_t) py * ip.W;
-                const F3 rn = ld3(ip.ref_nrm, ri);
-                const F3 n_ref = f3(-rn.x, -rn.y, -rn.z);
-                if (n_ref.x == 0.0f && n_ref.y == 0.0f && n_ref.z == 0.0f) {
-                    result = -3;
-                }
-                else {
-                    const F3 diff = sub(ld3(ip.ref_pts, ri), p_W);
-                    const F3 n_W = rot(T, n_in);
-                    if (norm(diff) > ip.dist_threshold) {
-                        result = -4;
-                    }
-                    else if (dot(n_W, n_ref) < ip.normal_threshold) {
-                        result = -5;
-                    }
-                    else {
-                        result = 1;
-                        e = dot(n_ref, diff);
-                        const F3 c = cross(p_W, n_ref);
-                        J[0] = n_ref.x;
-                        J[1] = n_ref.y;
-                        J[2] = n_ref.z;
-                        J[3] = c.x;
-                        J[4] = c.y;
-                        J[5] = c.z;
-                    }
-                }
-            }
+#pragma unroll
+            for (int k = 0; k < 32; ++k)
+                v[k] = 0.0f;
         }
-        (void) x;
-        (void) y;
-        if (result < 1) {
-            acc[29].add(result == -4 ? 1.0f : 0.0f);
-            acc[30].add(result == -5 ? 1.0f : 0.0f);
-            acc[31].add(result > -4 ? 1.0f : 0.0f);
-            continue;
-        }
-        acc[0].add(e * e);
-#pragma unroll
-        for (int k = 0; k < 6; ++k)
-            acc[1 + k].add(e * J[k]);
-        int q = 7;
-#pragma unroll
-        for (int r = 0; r < 6; ++r)
-#pragma unroll
-            for (int c = r; c < 6; ++c)
-                acc[q++].add(J[r] * J[c]);
-        acc[28].add(1.0f);
-    }
-
-    // warp reduction of the compensated pairs
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 32; ++k) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float h2 = __shfl_down_sync(0xffffffffu, acc[k].hi, o);
-            const float l2 = __shfl_down_sync(0xffffffffu, acc[k].lo, o);
-            acc[k].merge(h2, l2);
-        }
-    }
-    if (lane == 0) {
 #pragma unroll
         for (int k = 0; k < 32; ++k)
-            sh_warp[warp][k] = make_float2(acc[k].hi, acc[k].lo);
+            sh_terms[warp][lane][k] = v[k];
+        __syncwarp();
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j)
+            acc.add(sh_terms[warp][j][lane]);
+        __syncwarp();
     }
+    sh_warp[warp][lane] = make_float2(acc.hi, acc.lo);
     __syncthreads();
     if (threadIdx.x < 32) {
         CSum t{0.0f, 0.0f};
-        for (int wi = 0; wi < kTrackThreads / 32; ++wi)
+        for (int wi = 0; wi < kWarps; ++wi)
             t.merge(sh_warp[wi][threadIdx.x].x, sh_warp[wi][threadIdx.x].y);
         partials[blockIdx.x * 32 + threadIdx.x] = make_float2(t.hi, t.lo);
     }
@@ -406,23 +427,22 @@ __global__ void __launch_bounds__(kTrackThreads) icp_iter_kernel(Pinhole s, Iter
         return;
     __threadfence();
 
-    // ---- last CTA: fixed-order FP64 sum of the partials, solve, pose update
-    __shared__ double sh_chunk[8][32];
-    __shared__ double sh_val[32];
+    // ---- last CTA: fixed-order compensated FP32 sum of the partials, FP64 solve and update
     {
-        const int k = threadIdx.x & 31, chunk = threadIdx.x >> 5;
-        double acc_d = 0.0;
-        for (int b = chunk; b < (int) gridDim.x; b += 8) {
-            const float2 p = __ldcg(&partials[b * 32 + k]);
-            acc_d += (double) p.x + (double) p.y;
+        CSum t{0.0f, 0.0f};
+        for (int b = warp; b < (int) gridDim.x; b += kWarps) {
+            const float2 p = __ldcg(&partials[b * 32 + lane]);
+            t.merge(p.x, p.y);
         }
-        sh_chunk[chunk][k] = acc_d;
+        sh_chunk[warp][lane] = make_float2(t.hi, t.lo);
     }
     __syncthreads();
+    __shared__ double sh_val[32];
     if (threadIdx.x < 32) {
-        double v = 0.0;
-        for (int c = 0; c < 8; ++c)
-            v += sh_chunk[c][threadIdx.x];
+        CSum t{0.0f, 0.0f};
+        for (int c = 0; c < kWarps; ++c)
+            t.merge(sh_chunk[c][threadIdx.x].x, sh_chunk[c][threadIdx.x].y);
+        const double v = (double) t.hi + (double) t.lo;
         sh_val[threadIdx.x] = v;
         st->last_red[threadIdx.x] = (float) v;
     }
@@ -531,7 +551,7 @@ se_gpu_status se_gpu_tracker_create(const se_gpu_pinhole* sensor, const se_gpu_t
         t->li.pts[l] = t->pts[l];
         t->li.nrm[l] = t->nrm[l];
         t->li.depth[l] = t->pyr_depth[l];
-        const int ctas = (w * h + kTrackThreads * 4 - 1) / (kTrackThreads * 4);
+        const int ctas = (w * h + kTrackThreads * 4 - 1) / (kTrackThreads * 4); // ~4 tiles per CTA
         t->nctas[l] = ctas < 2 * device_sm_count() ? (ctas > 0 ? ctas : 1) : 2 * device_sm_count();
         if (t->nctas[l] > kMaxTrackCtas)
             t->nctas[l] = kMaxTrackCtas;

@@ -81,9 +81,11 @@ def test_camera_outside_map_is_safe(gpu):
     gpu.raycast_volume(m, s, T, pts, nrm)
     torch.cuda.synchronize()
     hit = (pts != 0).any(-1)
-    assert hit.float().mean() > 0.9
+    # the wall at z = 0 is inside the map for |x| < 1.28 of +-1.92 and |y| < 1.28 of +-1.44
+    assert hit.float().mean() > 0.5
     z = pts[..., 2][hit]
-    assert torch.allclose(z, torch.zeros_like(z), atol=2e-3)
+    # an oblique ray crosses the along-ray TSDF of a 2 cm grid within a quarter voxel
+    assert torch.allclose(z, torch.zeros_like(z), atol=5e-3)
 
 
 def test_pool_full_is_reported(gpu):
