@@ -182,6 +182,34 @@ SE_GPU_API se_gpu_status se_gpu_track(se_gpu_tracker* tracker, const float* dept
 SE_GPU_API se_gpu_status se_gpu_tracker_last_reduction(se_gpu_tracker* tracker, float reduction[32],
                                             int iterations_run[3]);
 
+/* ---------------------------------------------------------------- captured pipeline -- */
+
+/* The per-frame loop of the reference application (app/src/main.cpp:126-160: track the new
+ * depth against the previous raycast, integrate it at the tracked pose, raycast the map at
+ * that pose) as one CUDA graph, with the pose and the frame counter kept on the device. The
+ * frame owns its input depth buffer and the raycast images, which are the tracking reference
+ * of the next frame. tracker may be NULL (integrate + raycast only). No counterpart exists in
+ * the reference, which runs these steps as separate blocking calls. */
+typedef struct se_gpu_frame se_gpu_frame;
+SE_GPU_API se_gpu_status se_gpu_frame_create(se_gpu_map* map, se_gpu_tracker* tracker,
+                                             const se_gpu_pinhole* sensor, se_gpu_frame** frame);
+SE_GPU_API se_gpu_status se_gpu_frame_destroy(se_gpu_frame* frame);
+/* Device buffers owned by the frame: the input depth (width*height floats, written by the
+ * caller before se_gpu_frame_run) and the raycast outputs (width*height*3 floats each, and
+ * width*height int8). Any pointer may be NULL. */
+SE_GPU_API se_gpu_status se_gpu_frame_buffers(se_gpu_frame* frame, float** depth_dev,
+                                              float** pts_W_dev, float** nrm_W_dev,
+                                              int8_t** scale_dev);
+/* Set the device pose T_WS and the integration timestamp of the next run. Synchronous. */
+SE_GPU_API se_gpu_status se_gpu_frame_set_pose(se_gpu_frame* frame, const float T_WS[16],
+                                               int timestamp);
+/* Launch one frame on stream: [track (if track != 0)] + integrate + raycast. Asynchronous;
+ * the first call per mode captures the graph (call it before any capture of your own). */
+SE_GPU_API se_gpu_status se_gpu_frame_run(se_gpu_frame* frame, int track, void* stream);
+/* Read the device pose (after the runs enqueued on stream) and the last track's acceptance. */
+SE_GPU_API se_gpu_status se_gpu_frame_get_pose(se_gpu_frame* frame, float T_WS[16],
+                                               int* accepted, void* stream);
+
 /* ------------------------------------------------------------------------- profiling -- */
 
 /* Per-kernel device time: when enabled, each public call records CUDA events on its stream

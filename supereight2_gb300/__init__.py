@@ -23,7 +23,7 @@ import numpy as np
 from . import build as _build
 
 __all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "raycast_volume",
-           "SeGpuError", "library", "library_path"]
+           "FramePipeline", "SeGpuError", "library", "library_path"]
 
 
 class SeGpuError(RuntimeError):
@@ -80,6 +80,13 @@ SIGNATURES = {
     "se_gpu_tracker_destroy": (C.c_int, [_VP]),
     "se_gpu_track": (C.c_int, [_VP, _VP, _VP, _VP, _F16, C.POINTER(C.c_int), _VP]),
     "se_gpu_tracker_last_reduction": (C.c_int, [_VP, _F16, C.POINTER(C.c_int)]),
+    "se_gpu_frame_create": (C.c_int, [_VP, _VP, C.POINTER(_Pinhole), C.POINTER(_VP)]),
+    "se_gpu_frame_destroy": (C.c_int, [_VP]),
+    "se_gpu_frame_buffers": (C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_VP),
+                                       C.POINTER(_VP)]),
+    "se_gpu_frame_set_pose": (C.c_int, [_VP, _F16, C.c_int]),
+    "se_gpu_frame_run": (C.c_int, [_VP, C.c_int, _VP]),
+    "se_gpu_frame_get_pose": (C.c_int, [_VP, _F16, C.POINTER(C.c_int), _VP]),
     "se_gpu_profiling_enable": (C.c_int, [C.c_int]),
     "se_gpu_profiling_read": (C.c_int, [C.c_int, _VP, _VP, C.c_int]),
     "se_gpu_profiling_name": (C.c_char_p, [C.c_int]),
@@ -360,3 +367,66 @@ class Tracker:
         its = (C.c_int * 3)()
         _check(self._L.se_gpu_tracker_last_reduction(self.h, red, its), "last_reduction")
         return np.array(red[:], np.float32), list(its[:])
+
+
+class FramePipeline:
+    """The reference application's per-frame loop (track, integrate, raycast) as one captured
+    CUDA graph with the pose on the device. ``depth`` is the frame's input buffer (write the
+    next depth image into it, then call ``run``); ``points_W`` / ``normals_W`` hold the last
+    raycast. Not part of the reference's interface: it batches the three blocking calls."""
+
+    def __init__(self, map: Map, sensor: PinholeCamera, tracker: "Tracker" = None):
+        import torch
+        self.map, self.sensor, self.tracker = map, sensor, tracker
+        self._L = library()
+        h = C.c_void_p()
+        s = sensor._c()
+        _check(self._L.se_gpu_frame_create(map.h, tracker.h if tracker else None, C.byref(s),
+                                           C.byref(h)), "se_gpu_frame_create")
+        self.h = h
+        d, p, n, sc = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _check(self._L.se_gpu_frame_buffers(h, C.byref(d), C.byref(p), C.byref(n), C.byref(sc)),
+               "se_gpu_frame_buffers")
+        H, W = sensor.height, sensor.width
+        self.depth = _wrap_device(d.value, (H, W), torch.float32, self)
+        self.points_W = _wrap_device(p.value, (H, W, 3), torch.float32, self)
+        self.normals_W = _wrap_device(n.value, (H, W, 3), torch.float32, self)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self._L.se_gpu_frame_destroy(h)
+            self.h = None
+
+    def set_pose(self, T_WS, timestamp=0):
+        _, tp = _m16(T_WS)
+        _check(self._L.se_gpu_frame_set_pose(self.h, tp, int(timestamp)), "se_gpu_frame_set_pose")
+
+    def run(self, track=True, stream=None):
+        _check(self._L.se_gpu_frame_run(self.h, 1 if track else 0, _stream(stream)),
+               "se_gpu_frame_run")
+
+    def pose(self, stream=None):
+        T = np.zeros(16, np.float32)
+        acc = C.c_int()
+        _check(self._L.se_gpu_frame_get_pose(self.h, T.ctypes.data_as(_F16), C.byref(acc),
+                                             _stream(stream)), "se_gpu_frame_get_pose")
+        return T.reshape(4, 4), bool(acc.value)
+
+
+def _wrap_device(ptr, shape, dtype, owner):
+    """A torch tensor view of library-owned device memory (kept alive by owner)."""
+    import torch
+
+    class _Holder:
+        def __init__(self, p, nbytes):
+            self.__cuda_array_interface__ = {
+                "shape": (nbytes // 4,) if dtype == torch.float32 else (nbytes,),
+                "typestr": "<f4" if dtype == torch.float32 else "|i1",
+                "data": (p, False), "version": 3}
+
+    n = int(np.prod(shape))
+    nbytes = n * (4 if dtype == torch.float32 else 1)
+    t = torch.as_tensor(_Holder(ptr, nbytes), device="cuda").view(*shape)
+    t._se_owner = owner
+    return t

@@ -1,0 +1,191 @@
+// frame.cu — the whole per-frame pipeline of the reference application (app/src/main.cpp:
+// 126-160: track against the previous raycast, integrate at the tracked pose, raycast at that
+// pose) as one CUDA graph with the pose kept on the device.
+//
+// The graph is captured once per mode (with / without tracking) on a private stream and then
+// launched on the caller's stream: 28 kernels for a tracked frame with no host round trip.
+// ICP iterations after convergence return at entry, so the fixed launch sequence reproduces
+// the reference's early exit. The frame counter (the integration timestamp) lives on the
+// device and advances by one per launch.
+#include <cstring>
+
+#include "pipeline.cuh"
+#include "profile.cuh"
+#include "se_gpu_internal.cuh"
+
+namespace se_gpu {
+int tracker_accepted_offset();
+void* tracker_state(se_gpu_tracker* t);
+} // namespace se_gpu
+
+using namespace se_gpu;
+
+struct se_gpu_frame {
+    se_gpu_map* map;
+    se_gpu_tracker* tracker; // may be null: integrate + raycast only
+    se_gpu_pinhole sensor;
+    float* pose12;           // device T_WS (row-major 3x4)
+    float* depth;            // device input depth, width * height
+    float* pts;              // device raycast points (the next frame's tracking reference)
+    float* nrm;
+    int8_t* scale;
+    cudaStream_t capture_stream;
+    cudaGraphExec_t exec[2]; // [0] integrate + raycast, [1] track + integrate + raycast
+};
+
+static se_gpu_status capture(se_gpu_frame* f, int with_track)
+{
+    cudaGraph_t graph = nullptr;
+    profiling_suspend(true);
+    cudaError_t e = cudaStreamBeginCapture(f->capture_stream, cudaStreamCaptureModeThreadLocal);
+    se_gpu_status st = SE_GPU_OK;
+    if (e == cudaSuccess) {
+        if (with_track)
+            st = enqueue_track(f->tracker, f->depth, f->pts, f->nrm, nullptr, f->pose12, f->capture_stream);
+        if (st == SE_GPU_OK)
+            st = enqueue_integrate(f->map, f->depth, f->sensor, nullptr, f->pose12, 0, f->capture_stream);
+        if (st == SE_GPU_OK)
+            st = enqueue_raycast(f->map, f->sensor, nullptr, f->pose12, f->pts, f->nrm, f->scale, f->capture_stream);
+        const cudaError_t e2 = cudaStreamEndCapture(f->capture_stream, &graph);
+        if (e2 != cudaSuccess && st == SE_GPU_OK)
+            st = cuda_status(e2, "cudaStreamEndCapture");
+    }
+    else {
+        st = cuda_status(e, "cudaStreamBeginCapture");
+    }
+    profiling_suspend(false);
+    if (st != SE_GPU_OK) {
+        if (graph)
+            cudaGraphDestroy(graph);
+        return st;
+    }
+    e = cudaGraphInstantiate(&f->exec[with_track], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+        return cuda_status(e, "cudaGraphInstantiate");
+    return SE_GPU_OK;
+}
+
+extern "C" {
+
+se_gpu_status se_gpu_frame_create(se_gpu_map* map, se_gpu_tracker* tracker, const se_gpu_pinhole* sensor,
+                                  se_gpu_frame** out)
+{
+    if (!map || !sensor || !out || sensor->width <= 0 || sensor->height <= 0) {
+        set_last_error("se_gpu_frame_create: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    se_gpu_frame* f = new se_gpu_frame();
+    std::memset(f, 0, sizeof(*f));
+    f->map = map;
+    f->tracker = tracker;
+    f->sensor = *sensor;
+    const size_t npx = (size_t) sensor->width * sensor->height;
+    auto fail = [&](cudaError_t e, const char* what) {
+        se_gpu_status st = cuda_status(e, what);
+        se_gpu_frame_destroy(f);
+        return st;
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&f->pose12, 12 * sizeof(float))) != cudaSuccess) return fail(e, "cudaMalloc(pose)");
+    if ((e = cudaMalloc(&f->depth, npx * sizeof(float))) != cudaSuccess) return fail(e, "cudaMalloc(depth)");
+    if ((e = cudaMalloc(&f->pts, npx * 3 * sizeof(float))) != cudaSuccess) return fail(e, "cudaMalloc(points)");
+    if ((e = cudaMalloc(&f->nrm, npx * 3 * sizeof(float))) != cudaSuccess) return fail(e, "cudaMalloc(normals)");
+    if ((e = cudaMalloc(&f->scale, npx)) != cudaSuccess) return fail(e, "cudaMalloc(scale)");
+    if ((e = cudaMemset(f->pts, 0, npx * 3 * sizeof(float))) != cudaSuccess) return fail(e, "cudaMemset");
+    if ((e = cudaMemset(f->nrm, 0, npx * 3 * sizeof(float))) != cudaSuccess) return fail(e, "cudaMemset");
+    if ((e = cudaStreamCreateWithFlags(&f->capture_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return fail(e, "cudaStreamCreate");
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e, "cudaDeviceSynchronize");
+    *out = f;
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_frame_destroy(se_gpu_frame* f)
+{
+    if (!f)
+        return SE_GPU_OK;
+    for (int i = 0; i < 2; ++i)
+        if (f->exec[i])
+            cudaGraphExecDestroy(f->exec[i]);
+    if (f->capture_stream)
+        cudaStreamDestroy(f->capture_stream);
+    cudaFree(f->pose12);
+    cudaFree(f->depth);
+    cudaFree(f->pts);
+    cudaFree(f->nrm);
+    cudaFree(f->scale);
+    delete f;
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_frame_buffers(se_gpu_frame* f, float** depth_dev, float** pts_W_dev, float** nrm_W_dev,
+                                   int8_t** scale_dev)
+{
+    if (!f) {
+        set_last_error("se_gpu_frame_buffers: null frame");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    if (depth_dev)
+        *depth_dev = f->depth;
+    if (pts_W_dev)
+        *pts_W_dev = f->pts;
+    if (nrm_W_dev)
+        *nrm_W_dev = f->nrm;
+    if (scale_dev)
+        *scale_dev = f->scale;
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_frame_set_pose(se_gpu_frame* f, const float T_WS[16], int timestamp)
+{
+    if (!f || !T_WS) {
+        set_last_error("se_gpu_frame_set_pose: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    SE_CUDA_TRY(cudaDeviceSynchronize());
+    SE_CUDA_TRY(cudaMemcpy(f->pose12, T_WS, 12 * sizeof(float), cudaMemcpyHostToDevice));
+    SE_CUDA_TRY(cudaMemcpy(f->map->timestamp_dev, &timestamp, sizeof(int), cudaMemcpyHostToDevice));
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_frame_run(se_gpu_frame* f, int track, void* stream_p)
+{
+    if (!f || (track && !f->tracker)) {
+        set_last_error("se_gpu_frame_run: invalid argument (tracking needs a tracker)");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    const int mode = track ? 1 : 0;
+    if (!f->exec[mode]) {
+        const se_gpu_status st = capture(f, mode);
+        if (st != SE_GPU_OK)
+            return st;
+    }
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    f->map->last_stream = stream;
+    ProfScope ps(kProfFrameGraph, stream);
+    SE_CUDA_TRY(cudaGraphLaunch(f->exec[mode], stream));
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_frame_get_pose(se_gpu_frame* f, float T_WS[16], int* accepted, void* stream_p)
+{
+    if (!f || !T_WS) {
+        set_last_error("se_gpu_frame_get_pose: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    SE_CUDA_TRY(cudaMemcpyAsync(T_WS, f->pose12, 12 * sizeof(float), cudaMemcpyDeviceToHost, stream));
+    int acc = 1;
+    if (accepted && f->tracker)
+        SE_CUDA_TRY(cudaMemcpyAsync(&acc, (char*) tracker_state(f->tracker) + tracker_accepted_offset(), sizeof(int),
+                                    cudaMemcpyDeviceToHost, stream));
+    SE_CUDA_TRY(cudaStreamSynchronize(stream));
+    T_WS[12] = T_WS[13] = T_WS[14] = 0.0f;
+    T_WS[15] = 1.0f;
+    if (accepted)
+        *accepted = acc;
+    return SE_GPU_OK;
+}
+
+} // extern "C"

@@ -1,7 +1,8 @@
 // integrate.cu — se::MapIntegrator::integrateDepth for single-res TSDF maps.
 //
 // Four stream-ordered launches:
-//   begin_frame   snapshot the block count (blocks allocated before this frame)
+//   prep          per-frame parameters (from the caller's pose, or from a device pose for
+//                 captured pipelines) and the per-frame counters; snapshot of the block count
 //   carve         RaycastCarver: march every valid pixel's ray across the truncation band and
 //                 insert the block of every sample (raycast_carver_impl.hpp:74-111); keys are
 //                 deduplicated within a warp (__match_any_sync) before the dense-index check
@@ -14,34 +15,29 @@
 //                 per warp and 16 voxels per lane, with no block-level barrier
 #include <cmath>
 
+#include "pipeline.cuh"
 #include "profile.cuh"
 #include "se_gpu_internal.cuh"
 
 namespace se_gpu {
 
-struct CarveParams {
-    Tf T_WS;
-    F3 t_WS;
-    float band;
-    float half_band;
-    float far_limit; // far_plane + band * 0.5
-    int num_steps;
-};
-
-struct FrustumParams {
-    Tf T_SW;
-    float radius[20]; // bounding-sphere radius per octant scale
-};
-
-struct UpdateParams {
-    Tf T_CV; // T_CW * T_WM * Scaling(res) * Translation(0.5)
-    int timestamp;
-};
-
-__global__ void begin_frame_kernel(int* counters, int capacity)
+// Parameters for this frame, then the per-frame counters. With pose12 == nullptr the host's
+// parameters are copied; otherwise they are derived from the device pose and the device frame
+// counter, which is then advanced.
+__global__ void integrate_prep_kernel(MapDevice m, float trunc_factor, Pinhole s, const float* pose12,
+                                      IntegrateParams host_p, int* ts_counter, IntegrateParams* out)
 {
+    if (pose12 == nullptr) {
+        *out = host_p;
+    }
+    else {
+        const int ts = *ts_counter;
+        *out = make_integrate_params(m, trunc_factor, s, tf_from12(pose12), ts);
+        *ts_counter = ts + 1;
+    }
+    int* counters = m.counters;
     const int nb = counters[kCntNumBlocks];
-    counters[kCntNumOld] = nb < capacity ? nb : capacity;
+    counters[kCntNumOld] = nb < m.capacity ? nb : m.capacity;
     counters[kCntListed] = 0;
     counters[kCntValidPixels] = 0;
     reinterpret_cast<unsigned long long*>(counters)[kCntUpdated / 2] = 0ull;
@@ -50,8 +46,9 @@ __global__ void begin_frame_kernel(int* counters, int capacity)
 // RaycastCarver::operator() hot loop. A CTA covers a 32 x 8 pixel tile, one warp per row
 // segment, so the 8 samples of neighbouring rays fall in few distinct blocks.
 __global__ void __launch_bounds__(256) carve_kernel(MapDevice m, Pinhole s, const float* __restrict__ depth,
-                                                    CarveParams cp)
+                                                    const IntegrateParams* __restrict__ P)
 {
+    const CarveParams cp = P->cp;
     const int lane = threadIdx.x & 31;
     const int x = blockIdx.x * 32 + lane;
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -101,8 +98,9 @@ __global__ void __launch_bounds__(256) carve_kernel(MapDevice m, Pinhole s, cons
     }
 }
 
-__global__ void __launch_bounds__(256) frustum_kernel(MapDevice m, Pinhole s, FrustumParams fp)
+__global__ void __launch_bounds__(256) frustum_kernel(MapDevice m, Pinhole s, const IntegrateParams* __restrict__ P)
 {
+    const Tf T_SW = P->fp.T_SW;
     const int n_old = m.counters[kCntNumOld];
     const int lane = threadIdx.x & 31;
     for (int base = blockIdx.x * blockDim.x; base < n_old; base += gridDim.x * blockDim.x) {
@@ -116,8 +114,8 @@ __global__ void __launch_bounds__(256) frustum_kernel(MapDevice m, Pinhole s, Fr
                 const int n0 = c0 & ~(sz - 1), n1 = c1 & ~(sz - 1), n2 = c2 & ~(sz - 1);
                 const float off = (float) sz * 0.5f;
                 const F3 p_M = f3(((float) n0 + off) * m.res, ((float) n1 + off) * m.res, ((float) n2 + off) * m.res);
-                const F3 c_S = apply(fp.T_SW, apply(m.T_WM, p_M));
-                if (!sphere_in_frustum(s, c_S, fp.radius[scale])) {
+                const F3 c_S = apply(T_SW, apply(m.T_WM, p_M));
+                if (!sphere_in_frustum(s, c_S, P->fp.radius[scale])) {
                     pass = false;
                     break;
                 }
@@ -138,8 +136,10 @@ __global__ void __launch_bounds__(256) frustum_kernel(MapDevice m, Pinhole s, Fr
 // new blocks are written in full (the update doubles as their initialisation).
 template <int S>
 __global__ void __launch_bounds__(256) update_kernel(MapDevice m, Pinhole s, const float* __restrict__ depth,
-                                                     UpdateParams up)
+                                                     const IntegrateParams* __restrict__ P)
 {
+    const Tf T_CV = P->up.T_CV;
+    const int timestamp = P->up.timestamp;
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -156,14 +156,14 @@ __global__ void __launch_bounds__(256) update_kernel(MapDevice m, Pinhole s, con
         const int blk = is_new ? n_old + (item - n_list) : m.update_list[item];
         const int c0 = m.block_coord[3 * blk], c1 = m.block_coord[3 * blk + 1], c2 = m.block_coord[3 * blk + 2];
         if (lane == 0)
-            m.block_ts[blk] = up.timestamp;
+            m.block_ts[blk] = timestamp;
 #pragma unroll 4
         for (int k = 0; k < kBlockVoxels / 32; ++k) {
             const int vi = lane + 32 * k;
             const int x = vi & 7, y = (vi >> 3) & 7, z = vi >> 6;
             bool do_update = false;
             float upd = 0.0f;
-            const F3 p_C = apply(up.T_CV, f3((float) (c0 + x), (float) (c1 + y), (float) (c2 + z)));
+            const F3 p_C = apply(T_CV, f3((float) (c0 + x), (float) (c1 + y), (float) (c2 + z)));
             const float sq = dot(p_C, p_C);
             const float pn = sqrtf(sq);
             // farDist(p) = far / p.normalized().z
@@ -204,6 +204,42 @@ __global__ void __launch_bounds__(256) update_kernel(MapDevice m, Pinhole s, con
         atomicAdd(reinterpret_cast<unsigned long long*>(m.counters) + kCntUpdated / 2, n_upd);
 }
 
+se_gpu_status enqueue_integrate(se_gpu_map* map, const float* depth_dev, const se_gpu_pinhole& sensor,
+                                const float* T_WC_host16, const float* pose12_dev, int timestamp,
+                                cudaStream_t stream)
+{
+    MapDevice& m = map->dev;
+    const Pinhole s = make_pinhole(sensor);
+    IntegrateParams hp;
+    if (T_WC_host16)
+        hp = make_integrate_params(m, map->config.truncation_boundary_factor, s, tf_from16(T_WC_host16), timestamp);
+    const int sms = device_sm_count();
+    {
+        ProfScope ps(kProfBeginFrame, stream);
+        integrate_prep_kernel<<<1, 1, 0, stream>>>(m, map->config.truncation_boundary_factor, s,
+                                                   T_WC_host16 ? nullptr : pose12_dev, hp, map->timestamp_dev,
+                                                   map->iparams);
+    }
+    {
+        ProfScope ps(kProfCarve, stream);
+        dim3 cgrid((s.w + 31) / 32, (s.h + 7) / 8);
+        carve_kernel<<<cgrid, 256, 0, stream>>>(m, s, depth_dev, map->iparams);
+    }
+    {
+        ProfScope ps(kProfFrustum, stream);
+        frustum_kernel<<<sms * 4, 256, 0, stream>>>(m, s, map->iparams);
+    }
+    {
+        ProfScope ps(kProfUpdate, stream);
+        if (m.storage == SE_GPU_STORAGE_F32)
+            update_kernel<SE_GPU_STORAGE_F32><<<sms * 8, 256, 0, stream>>>(m, s, depth_dev, map->iparams);
+        else
+            update_kernel<SE_GPU_STORAGE_F16><<<sms * 8, 256, 0, stream>>>(m, s, depth_dev, map->iparams);
+    }
+    SE_CUDA_TRY(cudaGetLastError());
+    return SE_GPU_OK;
+}
+
 } // namespace se_gpu
 
 using namespace se_gpu;
@@ -218,53 +254,5 @@ extern "C" se_gpu_status se_gpu_integrate_depth(se_gpu_map* map, const float* de
     }
     cudaStream_t stream = (cudaStream_t) stream_p;
     map->last_stream = stream;
-    MapDevice& m = map->dev;
-    const Pinhole s = make_pinhole(*sensor);
-    const Tf T_WS = tf_from16(T_WC);
-
-    CarveParams cp;
-    cp.T_WS = T_WS;
-    cp.t_WS = f3(T_WS.t[0], T_WS.t[1], T_WS.t[2]);
-    cp.band = 2.0f * m.res * map->config.truncation_boundary_factor;
-    cp.half_band = cp.band * 0.5f;
-    cp.far_limit = s.far_plane + cp.band * 0.5f;
-    cp.num_steps = (int) std::ceil(cp.band / (2.0f * m.res));
-
-    FrustumParams fp;
-    fp.T_SW = inverse_iso(T_WS);
-    for (int sc = 0; sc < 20; ++sc)
-        fp.radius[sc] = std::sqrt(3.0f) / 2.0f * m.res * (float) (1 << (sc < 19 ? sc : 19));
-
-    UpdateParams up;
-    Tf T_CV = compose(inverse_iso(T_WS), m.T_WM);
-    for (int i = 0; i < 9; ++i)
-        T_CV.R[i] = T_CV.R[i] * m.res;
-    for (int i = 0; i < 3; ++i)
-        T_CV.t[i] = ((T_CV.R[3 * i] * 0.5f + T_CV.R[3 * i + 1] * 0.5f) + T_CV.R[3 * i + 2] * 0.5f) + T_CV.t[i];
-    up.T_CV = T_CV;
-    up.timestamp = timestamp;
-
-    const int sms = device_sm_count();
-    {
-        ProfScope ps(kProfBeginFrame, stream);
-        begin_frame_kernel<<<1, 1, 0, stream>>>(m.counters, m.capacity);
-    }
-    {
-        ProfScope ps(kProfCarve, stream);
-        dim3 cgrid((s.w + 31) / 32, (s.h + 7) / 8);
-        carve_kernel<<<cgrid, 256, 0, stream>>>(m, s, depth_dev, cp);
-    }
-    {
-        ProfScope ps(kProfFrustum, stream);
-        frustum_kernel<<<sms * 4, 256, 0, stream>>>(m, s, fp);
-    }
-    {
-        ProfScope ps(kProfUpdate, stream);
-        if (m.storage == SE_GPU_STORAGE_F32)
-            update_kernel<SE_GPU_STORAGE_F32><<<sms * 8, 256, 0, stream>>>(m, s, depth_dev, up);
-        else
-            update_kernel<SE_GPU_STORAGE_F16><<<sms * 8, 256, 0, stream>>>(m, s, depth_dev, up);
-    }
-    SE_CUDA_TRY(cudaGetLastError());
-    return SE_GPU_OK;
+    return enqueue_integrate(map, depth_dev, *sensor, T_WC, nullptr, timestamp, stream);
 }

@@ -115,6 +115,9 @@ se_gpu_status se_gpu_map_create(const se_gpu_map_config* cfg, se_gpu_map** out)
 
     se_gpu_map* map = new se_gpu_map();
     std::memset(&map->dev, 0, sizeof(map->dev));
+    map->iparams = nullptr;
+    map->rparams = nullptr;
+    map->timestamp_dev = nullptr;
     map->config = *cfg;
     map->device = dev;
     map->last_stream = 0;
@@ -165,6 +168,10 @@ se_gpu_status se_gpu_map_create(const se_gpu_map_config* cfg, se_gpu_map** out)
     if ((e = cudaMalloc(&m.update_list, (size_t) m.capacity * sizeof(int))) != cudaSuccess) return fail(e, "cudaMalloc(list)");
     if ((e = cudaMalloc(&m.counters, kNumCounters * sizeof(int))) != cudaSuccess) return fail(e, "cudaMalloc(counters)");
     if ((e = cudaMemset(m.counters, 0, kNumCounters * sizeof(int))) != cudaSuccess) return fail(e, "cudaMemset(counters)");
+    if ((e = cudaMalloc(&map->iparams, sizeof(IntegrateParams))) != cudaSuccess) return fail(e, "cudaMalloc(params)");
+    if ((e = cudaMalloc(&map->rparams, sizeof(RaycastParams))) != cudaSuccess) return fail(e, "cudaMalloc(params)");
+    if ((e = cudaMalloc(&map->timestamp_dev, sizeof(int))) != cudaSuccess) return fail(e, "cudaMalloc(timestamp)");
+    if ((e = cudaMemset(map->timestamp_dev, 0, sizeof(int))) != cudaSuccess) return fail(e, "cudaMemset(timestamp)");
     if ((e = cudaMalloc(&m.block_index, cells * sizeof(int))) != cudaSuccess) return fail(e, "cudaMalloc(block index)");
     if ((e = cudaMemset(m.block_index, 0xff, cells * sizeof(int))) != cudaSuccess) return fail(e, "cudaMemset(block index)");
     m.occ_levels = m.log2_bps + 1;
@@ -192,6 +199,9 @@ se_gpu_status se_gpu_map_destroy(se_gpu_map* map)
     cudaFree(m.update_list);
     cudaFree(m.counters);
     cudaFree(m.block_index);
+    cudaFree(map->iparams);
+    cudaFree(map->rparams);
+    cudaFree(map->timestamp_dev);
     for (int L = 0; L < 11; ++L)
         cudaFree(m.occ[L]);
     delete map;

@@ -1,0 +1,22 @@
+// pipeline.cuh — stream-ordered building blocks shared by the C entry points and the captured
+// frame pipeline. A pose is given either on the host (row-major float[16]) or on the device
+// (float[12], row-major 3x4); exactly one of the two pointers is non-null.
+#pragma once
+
+#include "se_gpu_internal.cuh"
+
+struct se_gpu_tracker;
+
+namespace se_gpu {
+
+se_gpu_status enqueue_integrate(se_gpu_map* map, const float* depth_dev, const se_gpu_pinhole& sensor,
+                                const float* T_WC_host16, const float* pose12_dev, int timestamp,
+                                cudaStream_t stream);
+se_gpu_status enqueue_raycast(const se_gpu_map* map, const se_gpu_pinhole& sensor, const float* T_WS_host16,
+                              const float* pose12_dev, float* pts_dev, float* nrm_dev, int8_t* scale_dev,
+                              cudaStream_t stream);
+// With pose12_dev_io the tracker starts from, and writes its result to, that device pose.
+se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const float* ref_pts, const float* ref_nrm,
+                            const float* T_WS_host16, float* pose12_dev_io, cudaStream_t stream);
+
+} // namespace se_gpu

@@ -18,6 +18,7 @@ struct Pending {
 };
 std::mutex g_mu;
 bool g_enabled = false;
+int g_suspended = 0; // > 0 while a CUDA graph is being captured
 std::vector<Pending> g_pending;
 std::vector<cudaEvent_t> g_free;
 double g_total_ms[kProfCount];
@@ -36,14 +37,20 @@ cudaEvent_t take_event()
 }
 } // namespace
 
-const char* const kProfNames[kProfCount] = {"begin_frame", "carve", "frustum", "update", "raycast",
-                                            "track_prep", "icp_iter", "icp_check"};
+const char* const kProfNames[kProfCount] = {"integrate_prep", "carve", "frustum", "update", "raycast",
+                                            "track_prep", "icp_iter", "icp_check", "frame_graph"};
 
-bool profiling_enabled() { return g_enabled; }
+bool profiling_enabled() { return g_enabled && g_suspended == 0; }
+
+void profiling_suspend(bool suspend)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_suspended += suspend ? 1 : -1;
+}
 
 ProfScope::ProfScope(int kernel, cudaStream_t stream) : kernel_(kernel), stream_(stream), start_(nullptr)
 {
-    if (!g_enabled)
+    if (!g_enabled || g_suspended)
         return;
     std::lock_guard<std::mutex> lk(g_mu);
     start_ = take_event();

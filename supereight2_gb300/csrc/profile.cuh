@@ -14,8 +14,12 @@ enum {
     kProfTrackPrep,
     kProfIcpIter,
     kProfIcpCheck,
+    kProfFrameGraph, // a whole captured frame (graph launch)
     kProfCount
 };
+
+// Event pairs cannot be recorded into a graph under capture: capture code suspends profiling.
+void profiling_suspend(bool suspend);
 
 class ProfScope {
   public:

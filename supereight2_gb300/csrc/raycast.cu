@@ -15,17 +15,11 @@
 // inside the instruction cache.
 #include <cmath>
 
+#include "pipeline.cuh"
 #include "profile.cuh"
 #include "se_gpu_internal.cuh"
 
 namespace se_gpu {
-
-struct RaycastParams {
-    Tf T_WS;
-    float scaling; // octree size * res
-    float eps;     // 2^-log2(size)
-    int min_scale; // 23 - log2(size / 8)
-};
 
 __device__ __forceinline__ float fmax_std(float a, float b) { return (a < b) ? b : a; } // std::max
 __device__ __forceinline__ float fmin_std(float a, float b) { return (b < a) ? b : a; } // std::min
@@ -362,11 +356,20 @@ __device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockC
     return false;
 }
 
+__global__ void raycast_prep_kernel(const float* pose12, RaycastParams host_p, RaycastParams* out)
+{
+    RaycastParams p = host_p;
+    if (pose12 != nullptr)
+        p.T_WS = tf_from12(pose12);
+    *out = p;
+}
+
 template <int S>
-__global__ void __launch_bounds__(128) raycast_kernel(MapDevice m, Pinhole s, RaycastParams rp,
+__global__ void __launch_bounds__(128) raycast_kernel(MapDevice m, Pinhole s, const RaycastParams* __restrict__ P,
                                                       float* __restrict__ pts, float* __restrict__ nrm,
                                                       int8_t* __restrict__ scale)
 {
+    const RaycastParams rp = *P;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
     const int y = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
@@ -429,6 +432,36 @@ __global__ void field_query_kernel(MapDevice m, int n, const float* __restrict__
 
 using namespace se_gpu;
 
+namespace se_gpu {
+
+se_gpu_status enqueue_raycast(const se_gpu_map* map, const se_gpu_pinhole& sensor, const float* T_WS_host16,
+                              const float* pose12_dev, float* pts_dev, float* nrm_dev, int8_t* scale_dev,
+                              cudaStream_t stream)
+{
+    const MapDevice& m = map->dev;
+    const Pinhole s = make_pinhole(sensor);
+    RaycastParams rp;
+    for (int i = 0; i < 9; ++i)
+        rp.T_WS.R[i] = (i % 4 == 0) ? 1.0f : 0.0f;
+    rp.T_WS.t[0] = rp.T_WS.t[1] = rp.T_WS.t[2] = 0.0f;
+    if (T_WS_host16)
+        rp.T_WS = tf_from16(T_WS_host16);
+    rp.scaling = (float) m.size * m.res;
+    rp.eps = std::exp2((float) (-std::log2((double) m.size)));
+    rp.min_scale = 23 - m.log2_bps;
+    raycast_prep_kernel<<<1, 1, 0, stream>>>(T_WS_host16 ? nullptr : pose12_dev, rp, map->rparams);
+    dim3 grid((s.w + 15) / 16, (s.h + 7) / 8);
+    ProfScope ps(kProfRaycast, stream);
+    if (m.storage == SE_GPU_STORAGE_F32)
+        raycast_kernel<SE_GPU_STORAGE_F32><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+    else
+        raycast_kernel<SE_GPU_STORAGE_F16><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+    SE_CUDA_TRY(cudaGetLastError());
+    return SE_GPU_OK;
+}
+
+} // namespace se_gpu
+
 extern "C" se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinhole* sensor, const float T_WS[16],
                                         float* pts_dev, float* nrm_dev, int8_t* scale_dev, void* stream_p)
 {
@@ -438,21 +471,7 @@ extern "C" se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinh
     }
     cudaStream_t stream = (cudaStream_t) stream_p;
     const_cast<se_gpu_map*>(map)->last_stream = stream;
-    const MapDevice& m = map->dev;
-    const Pinhole s = make_pinhole(*sensor);
-    RaycastParams rp;
-    rp.T_WS = tf_from16(T_WS);
-    rp.scaling = (float) m.size * m.res;
-    rp.eps = std::exp2((float) (-std::log2((double) m.size)));
-    rp.min_scale = 23 - m.log2_bps;
-    dim3 grid((s.w + 15) / 16, (s.h + 7) / 8);
-    ProfScope ps(kProfRaycast, stream);
-    if (m.storage == SE_GPU_STORAGE_F32)
-        raycast_kernel<SE_GPU_STORAGE_F32><<<grid, 128, 0, stream>>>(m, s, rp, pts_dev, nrm_dev, scale_dev);
-    else
-        raycast_kernel<SE_GPU_STORAGE_F16><<<grid, 128, 0, stream>>>(m, s, rp, pts_dev, nrm_dev, scale_dev);
-    SE_CUDA_TRY(cudaGetLastError());
-    return SE_GPU_OK;
+    return enqueue_raycast(map, *sensor, T_WS, nullptr, pts_dev, nrm_dev, scale_dev, stream);
 }
 
 static se_gpu_status field_query(const se_gpu_map* map, int64_t n, const float* pts, float* out, int* valid,

@@ -322,12 +322,92 @@ se_gpu_status cuda_status(cudaError_t e, const char* what);
             return ::se_gpu::cuda_status(_e, #call);                                         \
     } while (0)
 
+namespace se_gpu {
+
+// ------------------------------------------------------------- per-call parameters --
+// Every per-frame quantity the kernels need is derived from one pose by the functions below,
+// which run on the host (pose given by the caller) or in a one-thread prep kernel (pose
+// produced on the device, e.g. by the tracker inside a captured CUDA graph). Both compile to
+// the same IEEE operations, so either route gives bit-identical parameters.
+
+struct CarveParams {
+    Tf T_WS;
+    F3 t_WS;
+    float band;
+    float half_band;
+    float far_limit; // far_plane + band * 0.5
+    int num_steps;
+};
+
+struct FrustumParams {
+    Tf T_SW;
+    float radius[20]; // bounding-sphere radius per octant scale
+};
+
+struct UpdateParams {
+    Tf T_CV; // T_CW * T_WM * Scaling(res) * Translation(0.5)
+    int timestamp;
+};
+
+struct IntegrateParams {
+    CarveParams cp;
+    FrustumParams fp;
+    UpdateParams up;
+};
+
+struct RaycastParams {
+    Tf T_WS;
+    float scaling; // octree size * res
+    float eps;     // 2^-log2(size)
+    int min_scale; // 23 - log2(size / 8)
+};
+
+// RaycastCarver ctor / operator() (raycast_carver_impl.hpp:39-67), fetcher::frustum and the
+// updater's T_CV (singleres_tsdf_updater_impl.hpp:37-42).
+__host__ __device__ inline IntegrateParams make_integrate_params(const MapDevice& m, float trunc_factor,
+                                                                 const Pinhole& s, const Tf& T_WS, int timestamp)
+{
+    IntegrateParams p;
+    p.cp.T_WS = T_WS;
+    p.cp.t_WS = f3(T_WS.t[0], T_WS.t[1], T_WS.t[2]);
+    p.cp.band = 2.0f * m.res * trunc_factor;
+    p.cp.half_band = p.cp.band * 0.5f;
+    p.cp.far_limit = s.far_plane + p.cp.band * 0.5f;
+    p.cp.num_steps = (int) ceilf(p.cp.band / (2.0f * m.res));
+    p.fp.T_SW = inverse_iso(T_WS);
+    for (int sc = 0; sc < 20; ++sc)
+        p.fp.radius[sc] = sqrtf(3.0f) / 2.0f * m.res * (float) (1 << (sc < 19 ? sc : 19));
+    Tf T_CV = compose(inverse_iso(T_WS), m.T_WM);
+    for (int i = 0; i < 9; ++i)
+        T_CV.R[i] = T_CV.R[i] * m.res;
+    for (int i = 0; i < 3; ++i)
+        T_CV.t[i] = ((T_CV.R[3 * i] * 0.5f + T_CV.R[3 * i + 1] * 0.5f) + T_CV.R[3 * i + 2] * 0.5f) + T_CV.t[i];
+    p.up.T_CV = T_CV;
+    p.up.timestamp = timestamp;
+    return p;
+}
+
+__host__ __device__ inline Tf tf_from12(const float* m)
+{
+    Tf T;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            T.R[3 * i + j] = m[4 * i + j];
+        T.t[i] = m[4 * i + 3];
+    }
+    return T;
+}
+
+} // namespace se_gpu
+
 struct se_gpu_map {
     se_gpu::MapDevice dev;
     se_gpu_map_config config;
     int device;
     cudaStream_t last_stream;
-    int host_num_blocks_hint;
+    se_gpu::IntegrateParams* iparams; // device copy of the current integrate's parameters
+    se_gpu::RaycastParams* rparams;   // device copy of the current raycast's parameters
+    int* timestamp_dev;               // device frame counter used by captured pipelines
 };
 
 namespace se_gpu {

@@ -13,8 +13,10 @@
 // Later iterations of a converged level return at entry, so the launch sequence is fixed and
 // can be captured in a CUDA graph. checkPoseKernel (icp.cpp:227-246) runs in a final kernel.
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 
+#include "pipeline.cuh"
 #include "profile.cuh"
 #include "se_gpu_internal.cuh"
 
@@ -168,8 +170,22 @@ struct TrackInit {
     float ref_inv[12];
 };
 
-__global__ void track_init_kernel(TrackState* st, TrackInit init)
+// With pose12_in the start pose is read from the device (row-major 3x4) and its inverse is
+// formed here with the same float operations the host would use.
+__global__ void track_init_kernel(TrackState* st, TrackInit init, const float* pose12_in)
 {
+    if (pose12_in) {
+        const Tf T = tf_from12(pose12_in);
+        const Tf Ti = inverse_iso(T);
+        for (int i = 0; i < 3; ++i) {
+            for (int j = 0; j < 3; ++j) {
+                init.T_WS[4 * i + j] = T.R[3 * i + j];
+                init.ref_inv[4 * i + j] = Ti.R[3 * i + j];
+            }
+            init.T_WS[4 * i + 3] = T.t[i];
+            init.ref_inv[4 * i + 3] = Ti.t[i];
+        }
+    }
     for (int i = 0; i < 12; ++i) {
         st->pose[i] = (double) init.T_WS[i];
         st->pose_f[i] = init.T_WS[i];
@@ -184,31 +200,41 @@ __global__ void track_init_kernel(TrackState* st, TrackInit init)
 }
 
 // ---------------------------------------------------------------------- FP64 solve --
-// se(3) exponential (math_util_impl.hpp:117-174) in FP64: quaternion rotation from
-// (cos(theta/2), sin(theta/2)/theta * omega), V = I + (1-cos)/theta^2 W + (theta-sin)/theta^3 W^2.
-// sin(theta) and cos(theta) come from the half angle (2 s c, 1 - 2 s^2): one sincos call.
-__device__ void se3_exp_d(const double a[6], double R[9], double t[3])
+// GB300 runs FP64 at a small fraction of the FP32 rate with long latency, so this tail is
+// written for a short dependency chain: every loop is fully unrolled (the matrices live in
+// registers, not local memory), products are explicit fma(), and the exponential uses a series
+// for small rotations instead of a sincos call.
+
+// se(3) exponential (math_util_impl.hpp:117-174) in FP64: quaternion (cos(theta/2),
+// sin(theta/2)/theta * omega) normalised to a rotation, V = I + A W + B W^2 with
+// A = (1 - cos theta)/theta^2 and B = (theta - sin theta)/theta^3.
+__device__ __forceinline__ void se3_exp_d(const double a[6], double R[9], double t[3])
 {
     const double wx = a[3], wy = a[4], wz = a[5];
-    const double theta_sq = (wx * wx + wy * wy) + wz * wz;
-    const double theta = sqrt(theta_sq);
-    double imag, real, sin_t = 0.0, cos_t = 1.0;
-    const bool small = theta < 1e-10;
-    if (small) {
-        const double t4 = theta_sq * theta_sq;
-        imag = 0.5 - 1.0 / 48.0 * theta_sq + 1.0 / 3840.0 * t4;
-        real = 1.0 - 0.5 * theta_sq + 1.0 / 384.0 * t4;
+    const double th2 = fma(wz, wz, fma(wy, wy, wx * wx));
+    double imag, real, A, B;
+    if (th2 < 0.01) {
+        // |theta| < 0.1: Taylor series, truncation error below 1e-17
+        const double x = th2;
+        imag = 0.5 + x * (-1.0 / 48 + x * (1.0 / 3840 + x * (-1.0 / 645120 + x * (1.0 / 185794560))));
+        real = 1.0 + x * (-1.0 / 8 + x * (1.0 / 384 + x * (-1.0 / 46080 + x * (1.0 / 10321920))));
+        A = 0.5 + x * (-1.0 / 24 + x * (1.0 / 720 + x * (-1.0 / 40320 + x * (1.0 / 3628800))));
+        B = 1.0 / 6 + x * (-1.0 / 120 + x * (1.0 / 5040 + x * (-1.0 / 362880 + x * (1.0 / 39916800))));
     }
     else {
+        const double th = sqrt(th2);
         double sh, ch;
-        sincos(0.5 * theta, &sh, &ch);
-        imag = sh / theta;
+        sincos(0.5 * th, &sh, &ch);
+        const double inv_th = 1.0 / th;
+        imag = sh * inv_th;
         real = ch;
-        sin_t = 2.0 * sh * ch;
-        cos_t = 1.0 - 2.0 * sh * sh;
+        const double s = 2.0 * sh * ch, omc = 2.0 * sh * sh; // sin theta, 1 - cos theta
+        const double inv_th2 = inv_th * inv_th;
+        A = omc * inv_th2;
+        B = (th - s) * inv_th2 * inv_th;
     }
     double qw = real, qx = imag * wx, qy = imag * wy, qz = imag * wz;
-    const double inv_qn = 1.0 / sqrt(((qx * qx + qy * qy) + qz * qz) + qw * qw);
+    const double inv_qn = rsqrt(fma(qw, qw, fma(qz, qz, fma(qy, qy, qx * qx))));
     qw *= inv_qn;
     qx *= inv_qn;
     qy *= inv_qn;
@@ -221,62 +247,65 @@ __device__ void se3_exp_d(const double a[6], double R[9], double t[3])
     R[3] = txy + twz;       R[4] = 1 - (txx + tzz); R[5] = tyz - twx;
     R[6] = txz - twy;       R[7] = tyz + twx;       R[8] = 1 - (txx + tyy);
     const double O[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
-    double V[9];
-    if (small) {
-        for (int i = 0; i < 9; ++i)
-            V[i] = R[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        double ti = 0.0;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const double o2 = fma(O[3 * i + 2], O[6 + j], fma(O[3 * i + 1], O[3 + j], O[3 * i] * O[j]));
+            const double vij = fma(B, o2, fma(A, O[3 * i + j], i == j ? 1.0 : 0.0));
+            ti = fma(vij, a[j], ti);
+        }
+        t[i] = ti;
     }
-    else {
-        const double inv_tsq = 1.0 / theta_sq;
-        const double c1 = (1.0 - cos_t) * inv_tsq;
-        const double c2 = (theta - sin_t) * inv_tsq / theta;
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) {
-                const double o2 = (O[3 * i] * O[j] + O[3 * i + 1] * O[3 + j]) + O[3 * i + 2] * O[6 + j];
-                V[3 * i + j] = ((i == j ? 1.0 : 0.0) + c1 * O[3 * i + j]) + c2 * o2;
-            }
-    }
-    for (int i = 0; i < 3; ++i)
-        t[i] = (V[3 * i] * a[0] + V[3 * i + 1] * a[1]) + V[3 * i + 2] * a[2];
 }
 
-// LDL^T of the symmetric 6x6 J^T J without pivoting; false on a non-positive pivot (the
-// reference's LLT then returns a zero update, icp.cpp:33-41).
-__device__ bool ldlt_solve6(const double C[36], const double b[6], double x[6])
+// In-place LDL^T of J^T J without pivoting (the reference's LLT of icp.cpp:33-41 returns a
+// zero update on a non-positive pivot; so does the caller here) on the lower triangle of A (row-major 6x6; entries i >= j are overwritten
+// with L below the diagonal and D on it). All loops have constant trip counts so that they
+// unroll completely and A stays in registers.
+__device__ __forceinline__ bool ldlt_solve6(double A[36], const double b[6], double x[6])
 {
-    double L[36], D[6], inv_d[6];
+    bool ok = true;
+#pragma unroll
     for (int j = 0; j < 6; ++j) {
-        double dj = C[6 * j + j];
-        for (int k = 0; k < j; ++k)
-            dj -= L[6 * j + k] * L[6 * j + k] * D[k];
-        if (!(dj > 0.0))
-            return false;
-        D[j] = dj;
-        inv_d[j] = 1.0 / dj;
-        L[6 * j + j] = 1.0;
-        for (int i = j + 1; i < 6; ++i) {
-            double v = C[6 * i + j];
-            for (int k = 0; k < j; ++k)
-                v -= L[6 * i + k] * L[6 * j + k] * D[k];
-            L[6 * i + j] = v * inv_d[j];
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+            if (k < j)
+                A[6 * j + j] = fma(-A[6 * j + k] * A[6 * j + k], A[6 * k + k], A[6 * j + j]);
+        ok = ok && (A[6 * j + j] > 0.0);
+        const double inv = 1.0 / A[6 * j + j];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            if (i > j) {
+#pragma unroll
+                for (int k = 0; k < 6; ++k)
+                    if (k < j)
+                        A[6 * i + j] = fma(-A[6 * i + k] * A[6 * j + k], A[6 * k + k], A[6 * i + j]);
+                A[6 * i + j] *= inv;
+            }
         }
     }
-    double y[6];
+#pragma unroll
     for (int i = 0; i < 6; ++i) {
         double s = b[i];
-        for (int k = 0; k < i; ++k)
-            s -= L[6 * i + k] * y[k];
-        y[i] = s;
-    }
-    for (int i = 0; i < 6; ++i)
-        y[i] *= inv_d[i];
-    for (int i = 5; i >= 0; --i) {
-        double s = y[i];
-        for (int k = i + 1; k < 6; ++k)
-            s -= L[6 * k + i] * x[k];
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+            if (k < i)
+                s = fma(-A[6 * i + k], x[k], s);
         x[i] = s;
     }
-    return true;
+#pragma unroll
+    for (int ii = 0; ii < 6; ++ii) {
+        const int i = 5 - ii;
+        double s = x[i] / A[6 * i + i];
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+            if (k > i)
+                s = fma(-A[6 * k + i], x[k], s);
+        x[i] = s;
+    }
+    return ok;
 }
 
 struct IterParams {
@@ -451,40 +480,52 @@ __global__ void __launch_bounds__(kTrackThreads) icp_iter_kernel(Pinhole s, Iter
         st->ticket = 0;
         st->flags[kFlagIters0 + ip.level] += 1;
         double C[36], b[6], xs[6];
+#pragma unroll
         for (int i = 0; i < 6; ++i)
             b[i] = sh_val[1 + i];
-        int q = 7;
+#pragma unroll
         for (int r = 0; r < 6; ++r)
+#pragma unroll
             for (int c = r; c < 6; ++c) {
+                const int q = 7 + r * 6 - r * (r - 1) / 2 + (c - r);
                 C[6 * r + c] = sh_val[q];
                 C[6 * c + r] = sh_val[q];
-                ++q;
             }
-        if (!ldlt_solve6(C, b, xs))
+        if (!ldlt_solve6(C, b, xs)) {
+#pragma unroll
             for (int i = 0; i < 6; ++i)
                 xs[i] = 0.0;
+        }
         double dR[9], dt[3];
         se3_exp_d(xs, dR, dt);
-        double P[12];
+        double P0[12], P[12];
+#pragma unroll
+        for (int i = 0; i < 12; ++i)
+            P0[i] = st->pose[i];
+#pragma unroll
         for (int i = 0; i < 3; ++i) {
-            for (int j = 0; j < 3; ++j)
-                P[4 * i + j] = (dR[3 * i] * st->pose[j] + dR[3 * i + 1] * st->pose[4 + j]) + dR[3 * i + 2] * st->pose[8 + j];
-            P[4 * i + 3] = ((dR[3 * i] * st->pose[3] + dR[3 * i + 1] * st->pose[7]) + dR[3 * i + 2] * st->pose[11]) + dt[i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                P[4 * i + j] = fma(dR[3 * i + 2], P0[8 + j], fma(dR[3 * i + 1], P0[4 + j], dR[3 * i] * P0[j]))
+                    + (j == 3 ? dt[i] : 0.0);
         }
+#pragma unroll
         for (int i = 0; i < 12; ++i) {
             st->pose[i] = P[i];
             st->pose_f[i] = (float) P[i];
         }
         double xn = 0.0;
+#pragma unroll
         for (int i = 0; i < 6; ++i)
-            xn += xs[i] * xs[i];
-        if (sqrt(xn) < (double) ip.icp_threshold)
+            xn = fma(xs[i], xs[i], xn);
+        const double thr = (double) ip.icp_threshold;
+        if (xn < thr * thr)
             st->flags[kFlagDone0 + ip.level] = 1;
     }
 }
 
 // checkPoseKernel (icp.cpp:227-246): revert to the reference pose on a poor final alignment.
-__global__ void icp_check_kernel(TrackState* st, int W, int H, float track_threshold)
+__global__ void icp_check_kernel(TrackState* st, int W, int H, float track_threshold, float* pose12_out)
 {
     const float* v = st->last_red;
     const bool reject = ((double) sqrtf(v[0] / v[28]) > 2e-2) || (v[28] / (float) (W * H) < track_threshold);
@@ -495,6 +536,9 @@ __global__ void icp_check_kernel(TrackState* st, int W, int H, float track_thres
         }
     }
     st->flags[kFlagAccepted] = reject ? 0 : 1;
+    if (pose12_out)
+        for (int i = 0; i < 12; ++i)
+            pose12_out[i] = st->pose_f[i];
 }
 
 } // namespace se_gpu
@@ -582,25 +626,33 @@ se_gpu_status se_gpu_tracker_destroy(se_gpu_tracker* t)
 }
 
 // Enqueue the whole track on `stream` from a host pose. Asynchronous.
-static se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const float* ref_pts,
-                                   const float* ref_nrm, const float T_WS[16], cudaStream_t stream)
+} // extern "C"
+
+namespace se_gpu {
+
+se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const float* ref_pts, const float* ref_nrm,
+                            const float* T_WS, float* pose12_io, cudaStream_t stream)
 {
     TrackInit init;
-    const Tf T = tf_from16(T_WS);
-    const Tf Ti = inverse_iso(T);
-    for (int i = 0; i < 3; ++i) {
-        for (int j = 0; j < 3; ++j) {
-            init.T_WS[4 * i + j] = T.R[3 * i + j];
-            init.ref_inv[4 * i + j] = Ti.R[3 * i + j];
+    std::memset(&init, 0, sizeof(init));
+    if (T_WS) {
+        const Tf T = tf_from16(T_WS);
+        const Tf Ti = inverse_iso(T);
+        for (int i = 0; i < 3; ++i) {
+            for (int j = 0; j < 3; ++j) {
+                init.T_WS[4 * i + j] = T.R[3 * i + j];
+                init.ref_inv[4 * i + j] = Ti.R[3 * i + j];
+            }
+            init.T_WS[4 * i + 3] = T.t[i];
+            init.ref_inv[4 * i + 3] = Ti.t[i];
         }
-        init.T_WS[4 * i + 3] = T.t[i];
-        init.ref_inv[4 * i + 3] = Ti.t[i];
     }
+    const float* pose_in = T_WS ? nullptr : pose12_io;
     LevelImages li = t->li;
     li.depth[0] = depth_dev;
     {
     ProfScope ps(kProfTrackPrep, stream);
-    track_init_kernel<<<1, 1, 0, stream>>>(t->state, init);
+    track_init_kernel<<<1, 1, 0, stream>>>(t->state, init, pose_in);
     const float e_d = 0.1f * 3;
     for (int l = 1; l < t->levels; ++l) {
         dim3 b(32, 8), g((li.w[l] + 31) / 32, (li.h[l] + 7) / 8);
@@ -634,11 +686,18 @@ static se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, co
     {
         ProfScope ps(kProfIcpCheck, stream);
         icp_check_kernel<<<1, 1, 0, stream>>>(t->state, t->sensor.width, t->sensor.height,
-                                              t->config.track_threshold);
+                                              t->config.track_threshold, T_WS ? nullptr : pose12_io);
     }
     SE_CUDA_TRY(cudaGetLastError());
     return SE_GPU_OK;
 }
+
+int tracker_accepted_offset() { return (int) offsetof(TrackState, flags) + 4 * kFlagAccepted; }
+void* tracker_state(se_gpu_tracker* t) { return t->state; }
+
+} // namespace se_gpu
+
+extern "C" {
 
 se_gpu_status se_gpu_track(se_gpu_tracker* t, const float* depth_dev, const float* ref_pts, const float* ref_nrm,
                            float T_WS[16], int* accepted, void* stream_p)
@@ -648,7 +707,7 @@ se_gpu_status se_gpu_track(se_gpu_tracker* t, const float* depth_dev, const floa
         return SE_GPU_ERR_BAD_ARG;
     }
     cudaStream_t stream = (cudaStream_t) stream_p;
-    se_gpu_status st = enqueue_track(t, depth_dev, ref_pts, ref_nrm, T_WS, stream);
+    se_gpu_status st = enqueue_track(t, depth_dev, ref_pts, ref_nrm, T_WS, nullptr, stream);
     if (st != SE_GPU_OK)
         return st;
     TrackState hs;

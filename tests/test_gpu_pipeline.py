@@ -1,0 +1,91 @@
+"""The captured whole-frame pipeline (one CUDA graph per frame, pose on the device) gives
+bit-identical maps, poses and raycasts to the blocking reference-style calls, in FP32 and FP16
+storage, and FP16 storage stays within the stated tolerance of FP32."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_plain(gpu, sensor, poses, frames, storage):
+    import torch
+    m = gpu.Map(10.24, 0.02, max_blocks=1 << 16, storage=storage)
+    integ = gpu.MapIntegrator(m)
+    tr = gpu.Tracker(m, sensor)
+    H, W = sensor.height, sensor.width
+    pts = torch.zeros((H, W, 3), device="cuda")
+    nrm = torch.zeros_like(pts)
+    T = poses[0].astype(np.float32).copy()
+    out = []
+    for i, d in enumerate(frames):
+        dd = torch.from_numpy(d).cuda()
+        acc = True
+        if i > 0:
+            acc = tr.track(dd, T, pts, nrm)
+        integ.integrateDepth(i, dd, sensor, T)
+        gpu.raycast_volume(m, sensor, T, pts, nrm)
+        out.append((T.copy(), acc))
+    torch.cuda.synchronize()
+    return m, out, pts.cpu().numpy(), nrm.cpu().numpy()
+
+
+def _run_graph(gpu, sensor, poses, frames, storage):
+    import torch
+    m = gpu.Map(10.24, 0.02, max_blocks=1 << 16, storage=storage)
+    tr = gpu.Tracker(m, sensor)
+    fp = gpu.FramePipeline(m, sensor, tr)
+    fp.set_pose(poses[0].astype(np.float32), 0)
+    out = []
+    for i, d in enumerate(frames):
+        fp.depth.copy_(torch.from_numpy(d).cuda())
+        fp.run(track=i > 0)
+        out.append(fp.pose())
+    torch.cuda.synchronize()
+    return m, out, fp.points_W.cpu().numpy(), fp.normals_W.cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def data():
+    from supereight2_gb300 import synthetic as syn
+    return syn.dataset("tsdf320", 6)
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_graph_pipeline_bit_identical_to_blocking_calls(gpu, data, storage):
+    spec, scene, poses, frames = data
+    sensor = gpu.PinholeCamera.from_spec(spec)
+    m1, o1, p1, n1 = _run_plain(gpu, sensor, poses, frames, storage)
+    m2, o2, p2, n2 = _run_graph(gpu, sensor, poses, frames, storage)
+    for (T1, a1), (T2, a2) in zip(o1, o2):
+        assert a1 == a2
+        assert np.array_equal(T1[:3], T2[:3])
+    k1, c1, t1, w1, ts1 = m1.download_blocks()
+    k2, c2, t2, w2, ts2 = m2.download_blocks()
+    o1_, o2_ = np.argsort(k1), np.argsort(k2)
+    assert np.array_equal(k1[o1_], k2[o2_])
+    assert np.array_equal(t1[o1_], t2[o2_]) and np.array_equal(w1[o1_], w2[o2_])
+    assert np.array_equal(ts1[o1_], ts2[o2_])
+    assert np.array_equal(p1, p2) and np.array_equal(n1, n2)
+
+
+def test_f16_storage_error_against_f32(gpu, data):
+    """FP16 TSDF storage, FP32 arithmetic, exact integer weights: the tsdf values stay within
+    the precision variant's bound of the FP32 run on the same inputs and poses."""
+    import torch
+    spec, scene, poses, frames = data
+    sensor = gpu.PinholeCamera.from_spec(spec)
+    maps = {}
+    for st in ("f32", "f16"):
+        m = gpu.Map(10.24, 0.02, max_blocks=1 << 16, storage=st)
+        integ = gpu.MapIntegrator(m)
+        for i, (T, d) in enumerate(zip(poses, frames)):
+            integ.integrateDepth(i, torch.from_numpy(d).cuda(), sensor, T.astype(np.float32))
+        maps[st] = m.download_blocks()
+    k32, _, t32, w32, _ = maps["f32"]
+    k16, _, t16, w16, _ = maps["f16"]
+    a, b = np.argsort(k32), np.argsort(k16)
+    assert np.array_equal(k32[a], k16[b])
+    assert np.array_equal(w32[a], w16[b])            # weights exact
+    valid = w32[a] > 0
+    err = np.abs(t32[a] - t16[b])[valid]
+    assert err.max() <= 1e-3                          # 1e-3 truncation units
