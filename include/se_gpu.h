@@ -206,7 +206,8 @@ SE_GPU_API se_gpu_status se_gpu_frame_set_pose(se_gpu_frame* frame, const float 
 /* Launch one frame on stream: [track (if track != 0)] + integrate + raycast. Asynchronous;
  * the first call per mode captures the graph (call it before any capture of your own). */
 SE_GPU_API se_gpu_status se_gpu_frame_run(se_gpu_frame* frame, int track, void* stream);
-/* Read the device pose (after the runs enqueued on stream) and the last track's acceptance. */
+/* Read the device pose (after the runs enqueued on stream) and the last run's acceptance (the
+ * checkPoseKernel result; 1 when the last run did not track). Synchronous. */
 SE_GPU_API se_gpu_status se_gpu_frame_get_pose(se_gpu_frame* frame, float T_WS[16],
                                                int* accepted, void* stream);
 

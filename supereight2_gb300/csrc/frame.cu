@@ -31,6 +31,7 @@ struct se_gpu_frame {
     int8_t* scale;
     cudaStream_t capture_stream;
     cudaGraphExec_t exec[2]; // [0] integrate + raycast, [1] track + integrate + raycast
+    int last_tracked;        // whether the last run tracked (acceptance is 1 otherwise)
 };
 
 static se_gpu_status capture(se_gpu_frame* f, int with_track)
@@ -163,6 +164,7 @@ se_gpu_status se_gpu_frame_run(se_gpu_frame* f, int track, void* stream_p)
     }
     cudaStream_t stream = (cudaStream_t) stream_p;
     f->map->last_stream = stream;
+    f->last_tracked = mode;
     ProfScope ps(kProfFrameGraph, stream);
     SE_CUDA_TRY(cudaGraphLaunch(f->exec[mode], stream));
     return SE_GPU_OK;
@@ -177,7 +179,7 @@ se_gpu_status se_gpu_frame_get_pose(se_gpu_frame* f, float T_WS[16], int* accept
     cudaStream_t stream = (cudaStream_t) stream_p;
     SE_CUDA_TRY(cudaMemcpyAsync(T_WS, f->pose12, 12 * sizeof(float), cudaMemcpyDeviceToHost, stream));
     int acc = 1;
-    if (accepted && f->tracker)
+    if (accepted && f->tracker && f->last_tracked)
         SE_CUDA_TRY(cudaMemcpyAsync(&acc, (char*) tracker_state(f->tracker) + tracker_accepted_offset(), sizeof(int),
                                     cudaMemcpyDeviceToHost, stream));
     SE_CUDA_TRY(cudaStreamSynchronize(stream));

@@ -164,11 +164,13 @@ __global__ void __launch_bounds__(256) update_kernel(MapDevice m, Pinhole s, con
             bool do_update = false;
             float upd = 0.0f;
             const F3 p_C = apply(T_CV, f3((float) (c0 + x), (float) (c1 + y), (float) (c2 + z)));
-            const float sq = dot(p_C, p_C);
+            // A voxel with z <= 0 never updates: z < 0 fails the far test (far / nz < 0) and
+            // z == 0 fails the projection; skipping it early changes no result.
+            const float sq = p_C.z > 0.0f ? dot(p_C, p_C) : 0.0f;
             const float pn = sqrtf(sq);
             // farDist(p) = far / p.normalized().z
-            const float nz = sq > 0.0f ? p_C.z / pn : p_C.z;
-            if (!(pn > s.far_plane / nz)) {
+            const float nz = p_C.z / pn;
+            if (p_C.z > 0.0f && !(pn > s.far_plane / nz)) {
                 float u, v;
                 if (project(s, p_C, u, v)) {
                     const int px = (int) (u + 0.5f), py = (int) (v + 0.5f);

@@ -337,7 +337,9 @@ __device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockC
             continue;
         }
         f_tt = f;
-        if ((double) f_tt <= 0.1 && f_tt >= -0.5f) { // the reference compares with double 0.1
+        // The reference compares with the double literal 0.1; no float lies in (0.1, 0.1f), so
+        // (double) f <= 0.1 is exactly f < 0.1f, with no FP64 instruction.
+        if (f_tt < 0.1f && f_tt >= -0.5f) {
             float fi;
             if (field_interp<S>(m, c, p, fi))
                 f_tt = fi;

@@ -458,10 +458,20 @@ __global__ void __launch_bounds__(kTrackThreads) icp_iter_kernel(Pinhole s, Iter
 
     // ---- last CTA: fixed-order compensated FP32 sum of the partials, FP64 solve and update
     {
+        // warp w merges rows w, w + 8, ...; loads are issued 16 at a time so that the L2
+        // latency is paid once per batch, not once per row
         CSum t{0.0f, 0.0f};
-        for (int b = warp; b < (int) gridDim.x; b += kWarps) {
-            const float2 p = __ldcg(&partials[b * 32 + lane]);
-            t.merge(p.x, p.y);
+        const int nb = (int) gridDim.x;
+        for (int b0 = warp; b0 < nb; b0 += 16 * kWarps) {
+            float2 p[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                const int b = b0 + u * kWarps;
+                p[u] = b < nb ? __ldcg(&partials[b * 32 + lane]) : make_float2(0.0f, 0.0f);
+            }
+#pragma unroll
+            for (int u = 0; u < 16; ++u)
+                t.merge(p[u].x, p[u].y);
         }
         sh_chunk[warp][lane] = make_float2(t.hi, t.lo);
     }
