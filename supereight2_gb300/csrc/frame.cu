@@ -3,7 +3,7 @@
 // pose) as one CUDA graph with the pose kept on the device.
 //
 // The graph is captured once per mode (with / without tracking) on a private stream and then
-// launched on the caller's stream: 28 kernels for a tracked frame with no host round trip.
+// launched on the caller's stream: 31 kernels for a tracked frame with no host round trip.
 // ICP iterations after convergence return at entry, so the fixed launch sequence reproduces
 // the reference's early exit. The frame counter (the integration timestamp) lives on the
 // device and advances by one per launch.

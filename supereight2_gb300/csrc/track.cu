@@ -200,6 +200,17 @@ __global__ void track_init_kernel(TrackState* st, TrackInit init, const float* p
 }
 
 // ---------------------------------------------------------------------- FP64 solve --
+// Measured on GB300: a dependent FP64 FMA takes 64 cycles and an IEEE FP64 division 650, so
+// the reciprocal is an FP32 seed refined by two FP64 Newton steps (relative error ~1e-30
+// before the final rounding, i.e. a double within an ulp of 1/x) for ~6 dependent FMAs.
+__device__ __forceinline__ double drcp(double x)
+{
+    double r = (double) (1.0f / (float) x);
+    r = fma(r, fma(-x, r, 1.0), r);
+    r = fma(r, fma(-x, r, 1.0), r);
+    return r;
+}
+
 // GB300 runs FP64 at a small fraction of the FP32 rate with long latency, so this tail is
 // written for a short dependency chain: every loop is fully unrolled (the matrices live in
 // registers, not local memory), products are explicit fma(), and the exponential uses a series
@@ -225,7 +236,7 @@ __device__ __forceinline__ void se3_exp_d(const double a[6], double R[9], double
         const double th = sqrt(th2);
         double sh, ch;
         sincos(0.5 * th, &sh, &ch);
-        const double inv_th = 1.0 / th;
+        const double inv_th = drcp(th);
         imag = sh * inv_th;
         real = ch;
         const double s = 2.0 * sh * ch, omc = 2.0 * sh * sh; // sin theta, 1 - cos theta
@@ -234,11 +245,15 @@ __device__ __forceinline__ void se3_exp_d(const double a[6], double R[9], double
         B = (th - s) * inv_th2 * inv_th;
     }
     double qw = real, qx = imag * wx, qy = imag * wy, qz = imag * wz;
-    const double inv_qn = rsqrt(fma(qw, qw, fma(qz, qz, fma(qy, qy, qx * qx))));
-    qw *= inv_qn;
-    qx *= inv_qn;
-    qy *= inv_qn;
-    qz *= inv_qn;
+    if (!(th2 < 0.01)) {
+        // the series path is unit to ~1e-17 already; renormalise the sincos path as the
+        // reference does
+        const double inv_qn = rsqrt(fma(qw, qw, fma(qz, qz, fma(qy, qy, qx * qx))));
+        qw *= inv_qn;
+        qx *= inv_qn;
+        qy *= inv_qn;
+        qz *= inv_qn;
+    }
     const double tx = 2 * qx, ty = 2 * qy, tz = 2 * qz;
     const double twx = tx * qw, twy = ty * qw, twz = tz * qw;
     const double txx = tx * qx, txy = ty * qx, txz = tz * qx;
@@ -267,6 +282,7 @@ __device__ __forceinline__ void se3_exp_d(const double a[6], double R[9], double
 __device__ __forceinline__ bool ldlt_solve6(double A[36], const double b[6], double x[6])
 {
     bool ok = true;
+    double inv_d[6];
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
 #pragma unroll
@@ -274,7 +290,8 @@ __device__ __forceinline__ bool ldlt_solve6(double A[36], const double b[6], dou
             if (k < j)
                 A[6 * j + j] = fma(-A[6 * j + k] * A[6 * j + k], A[6 * k + k], A[6 * j + j]);
         ok = ok && (A[6 * j + j] > 0.0);
-        const double inv = 1.0 / A[6 * j + j];
+        inv_d[j] = drcp(A[6 * j + j]);
+        const double inv = inv_d[j];
 #pragma unroll
         for (int i = 0; i < 6; ++i) {
             if (i > j) {
@@ -298,7 +315,7 @@ __device__ __forceinline__ bool ldlt_solve6(double A[36], const double b[6], dou
 #pragma unroll
     for (int ii = 0; ii < 6; ++ii) {
         const int i = 5 - ii;
-        double s = x[i] / A[6 * i + i];
+        double s = x[i] * inv_d[i];
 #pragma unroll
         for (int k = 0; k < 6; ++k)
             if (k > i)
@@ -395,7 +412,7 @@ __device__ __forceinline__ void icp_pixel_terms(const Pinhole& s, const IterPara
 // One ICP iteration: trackKernel + newReduce/reduceKernel + updatePoseKernel.
 // Each warp handles 32 pixels per tile; the 32 x 32 term matrix goes through shared memory
 // (stride 33: conflict-free) so that lane k accumulates column k with two-sum compensation.
-__global__ void __launch_bounds__(kTrackThreads) icp_iter_kernel(Pinhole s, IterParams ip, TrackState* st,
+__global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, IterParams ip, TrackState* st,
                                                                 float2* __restrict__ partials)
 {
     constexpr int kWarps = kTrackThreads / 32;
