@@ -200,129 +200,119 @@ __global__ void track_init_kernel(TrackState* st, TrackInit init, const float* p
 }
 
 // ---------------------------------------------------------------------- FP64 solve --
-// Measured on GB300: a dependent FP64 FMA takes 64 cycles and an IEEE FP64 division 650, so
-// the reciprocal is an FP32 seed refined by two FP64 Newton steps (relative error ~1e-30
-// before the final rounding, i.e. a double within an ulp of 1/x) for ~6 dependent FMAs.
+// Measured on GB300: a dependent FP64 FMA takes 64 cycles and an IEEE FP64 division 650. The
+// solve below is arranged for short dependency chains: a right-looking LDL^T (each pivot
+// needs one reciprocal and one trailing update), reciprocals from an FP32 seed and one FP64
+// Newton step (relative error ~1e-14), a Rodrigues-form exponential, and the pose composition
+// spread over 12 threads.
+
 __device__ __forceinline__ double drcp(double x)
 {
-    double r = (double) (1.0f / (float) x);
-    r = fma(r, fma(-x, r, 1.0), r);
-    r = fma(r, fma(-x, r, 1.0), r);
-    return r;
+    const float xf = (float) x;
+    if (!(fabsf(xf) > 1e-30f && fabsf(xf) < 1e30f))
+        return 1.0 / x;
+    const double r = (double) (1.0f / xf);
+    return fma(r, fma(-x, r, 1.0), r);
 }
 
-// GB300 runs FP64 at a small fraction of the FP32 rate with long latency, so this tail is
-// written for a short dependency chain: every loop is fully unrolled (the matrices live in
-// registers, not local memory), products are explicit fma(), and the exponential uses a series
-// for small rotations instead of a sincos call.
+// Solves C x = b for the symmetric 6x6 C given as its packed upper triangle in the order of
+// newReduce (row-major, icp.cpp:15-31). Returns false on a non-positive pivot, where the
+// reference's LLT fails and its update is zero (icp.cpp:33-41).
+__device__ __forceinline__ bool ldlt_solve6(const double* upper21, const double* b_in, double x[6])
+{
+    double A[6][6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c)
+            if (c >= r) {
+                A[r][c] = upper21[r * 6 - r * (r - 1) / 2 + (c - r)];
+                A[c][r] = A[r][c];
+            }
+    double inv_d[6];
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        const double dj = A[j][j];
+        ok = ok && (dj > 0.0);
+        inv_d[j] = drcp(dj);
+        // column j of L, then the trailing update A_ik -= L_ij * D_j * L_kj = A_ij * L_kj
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+            if (i > j)
+                A[i][j] = A[i][j] * inv_d[j];
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+                if (i > j && k > j && k <= i)
+                    A[i][k] = fma(-A[i][j], A[k][j] * dj, A[i][k]);
+    }
+    double y[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        y[i] = b_in[i];
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+            if (i > k)
+                y[i] = fma(-A[i][k], y[k], y[i]);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        y[i] *= inv_d[i];
+#pragma unroll
+    for (int kk = 0; kk < 6; ++kk) {
+        const int k = 5 - kk;
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+            if (i < k)
+                y[i] = fma(-A[k][i], y[k], y[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        x[i] = y[i];
+    return ok;
+}
 
-// se(3) exponential (math_util_impl.hpp:117-174) in FP64: quaternion (cos(theta/2),
-// sin(theta/2)/theta * omega) normalised to a rotation, V = I + A W + B W^2 with
-// A = (1 - cos theta)/theta^2 and B = (theta - sin theta)/theta^3.
-__device__ __forceinline__ void se3_exp_d(const double a[6], double R[9], double t[3])
+// se(3) exponential of [rho; omega] (math_util_impl.hpp:117-174) in FP64, Rodrigues form:
+// R = I + A W + B W^2 and V = I + B W + C W^2 with W = hat(omega), A = sin(t)/t,
+// B = (1 - cos t)/t^2, C = (t - sin t)/t^3 (series below |t| = 0.1), translation V rho.
+__device__ __forceinline__ void se3_exp_d(const double a[6], double R[9], double tr[3])
 {
     const double wx = a[3], wy = a[4], wz = a[5];
-    const double th2 = fma(wz, wz, fma(wy, wy, wx * wx));
-    double imag, real, A, B;
-    if (th2 < 0.01) {
-        // |theta| < 0.1: Taylor series, truncation error below 1e-17
-        const double x = th2;
-        imag = 0.5 + x * (-1.0 / 48 + x * (1.0 / 3840 + x * (-1.0 / 645120 + x * (1.0 / 185794560))));
-        real = 1.0 + x * (-1.0 / 8 + x * (1.0 / 384 + x * (-1.0 / 46080 + x * (1.0 / 10321920))));
-        A = 0.5 + x * (-1.0 / 24 + x * (1.0 / 720 + x * (-1.0 / 40320 + x * (1.0 / 3628800))));
-        B = 1.0 / 6 + x * (-1.0 / 120 + x * (1.0 / 5040 + x * (-1.0 / 362880 + x * (1.0 / 39916800))));
+    const double x = fma(wz, wz, fma(wy, wy, wx * wx));
+    double A, B, Cc;
+    if (x < 0.01) {
+        A = 1.0 + x * (-1.0 / 6 + x * (1.0 / 120 + x * (-1.0 / 5040 + x * (1.0 / 362880))));
+        B = 0.5 + x * (-1.0 / 24 + x * (1.0 / 720 + x * (-1.0 / 40320 + x * (1.0 / 3628800))));
+        Cc = 1.0 / 6 + x * (-1.0 / 120 + x * (1.0 / 5040 + x * (-1.0 / 362880 + x * (1.0 / 39916800))));
     }
     else {
-        const double th = sqrt(th2);
-        double sh, ch;
-        sincos(0.5 * th, &sh, &ch);
-        const double inv_th = drcp(th);
-        imag = sh * inv_th;
-        real = ch;
-        const double s = 2.0 * sh * ch, omc = 2.0 * sh * sh; // sin theta, 1 - cos theta
-        const double inv_th2 = inv_th * inv_th;
-        A = omc * inv_th2;
-        B = (th - s) * inv_th2 * inv_th;
+        const double t = sqrt(x);
+        double sn, cs;
+        sincos(t, &sn, &cs);
+        const double it = drcp(t);
+        const double it2 = it * it;
+        A = sn * it;
+        B = (1.0 - cs) * it2;
+        Cc = (t - sn) * it2 * it;
     }
-    double qw = real, qx = imag * wx, qy = imag * wy, qz = imag * wz;
-    if (!(th2 < 0.01)) {
-        // the series path is unit to ~1e-17 already; renormalise the sincos path as the
-        // reference does
-        const double inv_qn = rsqrt(fma(qw, qw, fma(qz, qz, fma(qy, qy, qx * qx))));
-        qw *= inv_qn;
-        qx *= inv_qn;
-        qy *= inv_qn;
-        qz *= inv_qn;
-    }
-    const double tx = 2 * qx, ty = 2 * qy, tz = 2 * qz;
-    const double twx = tx * qw, twy = ty * qw, twz = tz * qw;
-    const double txx = tx * qx, txy = ty * qx, txz = tz * qx;
-    const double tyy = ty * qy, tyz = tz * qy, tzz = tz * qz;
-    R[0] = 1 - (tyy + tzz); R[1] = txy - twz;       R[2] = txz + twy;
-    R[3] = txy + twz;       R[4] = 1 - (txx + tzz); R[5] = tyz - twx;
-    R[6] = txz - twy;       R[7] = tyz + twx;       R[8] = 1 - (txx + tyy);
-    const double O[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
+    const double w[3] = {wx, wy, wz};
+    const double W[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         double ti = 0.0;
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const double o2 = fma(O[3 * i + 2], O[6 + j], fma(O[3 * i + 1], O[3 + j], O[3 * i] * O[j]));
-            const double vij = fma(B, o2, fma(A, O[3 * i + j], i == j ? 1.0 : 0.0));
-            ti = fma(vij, a[j], ti);
+            const double w2 = w[i] * w[j] - (i == j ? x : 0.0); // (W^2)_ij = w_i w_j - |w|^2 d_ij
+            const double id = i == j ? 1.0 : 0.0;
+            R[3 * i + j] = fma(B, w2, fma(A, W[3 * i + j], id));
+            const double v = fma(Cc, w2, fma(B, W[3 * i + j], id));
+            ti = fma(v, a[j], ti);
         }
-        t[i] = ti;
+        tr[i] = ti;
     }
-}
-
-// In-place LDL^T of J^T J without pivoting (the reference's LLT of icp.cpp:33-41 returns a
-// zero update on a non-positive pivot; so does the caller here) on the lower triangle of A (row-major 6x6; entries i >= j are overwritten
-// with L below the diagonal and D on it). All loops have constant trip counts so that they
-// unroll completely and A stays in registers.
-__device__ __forceinline__ bool ldlt_solve6(double A[36], const double b[6], double x[6])
-{
-    bool ok = true;
-    double inv_d[6];
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k)
-            if (k < j)
-                A[6 * j + j] = fma(-A[6 * j + k] * A[6 * j + k], A[6 * k + k], A[6 * j + j]);
-        ok = ok && (A[6 * j + j] > 0.0);
-        inv_d[j] = drcp(A[6 * j + j]);
-        const double inv = inv_d[j];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) {
-            if (i > j) {
-#pragma unroll
-                for (int k = 0; k < 6; ++k)
-                    if (k < j)
-                        A[6 * i + j] = fma(-A[6 * i + k] * A[6 * j + k], A[6 * k + k], A[6 * i + j]);
-                A[6 * i + j] *= inv;
-            }
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        double s = b[i];
-#pragma unroll
-        for (int k = 0; k < 6; ++k)
-            if (k < i)
-                s = fma(-A[6 * i + k], x[k], s);
-        x[i] = s;
-    }
-#pragma unroll
-    for (int ii = 0; ii < 6; ++ii) {
-        const int i = 5 - ii;
-        double s = x[i] * inv_d[i];
-#pragma unroll
-        for (int k = 0; k < 6; ++k)
-            if (k > i)
-                s = fma(-A[6 * k + i], x[k], s);
-        x[i] = s;
-    }
-    return ok;
 }
 
 struct IterParams {
@@ -336,16 +326,17 @@ struct IterParams {
     float dist_threshold, normal_threshold, icp_threshold;
 };
 
-// trackKernel for one pixel (icp_impl.hpp:16-102): the 32 reduction terms of newReduce
-// (icp.cpp:45-184) in v: [e^2, e*J (6), upper J^T J (21), inlier, dist-reject, normal-reject,
-// other reject].
+// trackKernel for one pixel (icp_impl.hpp:16-102) given its input normal and point: the 32
+// reduction terms of newReduce (icp.cpp:45-184) in v: [e^2, e*J (6), upper J^T J (21),
+// inlier, dist-reject, normal-reject, other reject].
 __device__ __forceinline__ void icp_pixel_terms(const Pinhole& s, const IterParams& ip, const Tf& T, const Tf& Tri,
-                                                int i, float v[32])
+                                                bool in_range, F3 n_in, F3 p_S, float v[32])
 {
 #pragma unroll
     for (int k = 0; k < 32; ++k)
         v[k] = 0.0f;
-    const F3 n_in = ld3(ip.nrm, (size_t) i);
+    if (!in_range)
+        return;
     int result;
     float e = 0.0f;
     float J[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -353,7 +344,7 @@ __device__ __forceinline__ void icp_pixel_terms(const Pinhole& s, const IterPara
         result = -1;
     }
     else {
-        const F3 p_W = apply(T, ld3(ip.pts, (size_t) i));
+        const F3 p_W = apply(T, p_S);
         const F3 p_ref = apply(Tri, p_W);
         float u, vv;
         if (!project(s, p_ref, u, vv)) {
@@ -363,12 +354,13 @@ __device__ __forceinline__ void icp_pixel_terms(const Pinhole& s, const IterPara
             const int px = (int) (u + 0.5f), py = (int) (vv + 0.5f);
             const size_t ri = (size_t) px + (size_t) py * ip.W;
             const F3 rn = ld3(ip.ref_nrm, ri);
+            const F3 rp = ld3(ip.ref_pts, ri);
             const F3 n_ref = f3(-rn.x, -rn.y, -rn.z);
             if (n_ref.x == 0.0f && n_ref.y == 0.0f && n_ref.z == 0.0f) {
                 result = -3;
             }
             else {
-                const F3 diff = sub(ld3(ip.ref_pts, ri), p_W);
+                const F3 diff = sub(rp, p_W);
                 const F3 n_W = rot(T, n_in);
                 if (norm(diff) > ip.dist_threshold) {
                     result = -4;
@@ -410,53 +402,67 @@ __device__ __forceinline__ void icp_pixel_terms(const Pinhole& s, const IterPara
 }
 
 // One ICP iteration: trackKernel + newReduce/reduceKernel + updatePoseKernel.
-// Each warp handles 32 pixels per tile; the 32 x 32 term matrix goes through shared memory
-// (stride 33: conflict-free) so that lane k accumulates column k with two-sum compensation.
+// Main phase: each warp takes 32 pixels per tile (the next tile's input normal and point are
+// loaded before the current one is processed); the 32 x 32 term matrix goes through shared
+// memory (stride 33: conflict-free) so that lane k accumulates term k, with two-sum
+// compensation in 4 independent accumulators. Tail (last CTA to finish, found with an atomic
+// ticket, no waiting): fixed-order compensated FP32 sum of the CTA partials, then the FP64
+// solve, exponential and pose composition.
 __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, IterParams ip, TrackState* st,
-                                                                float2* __restrict__ partials)
+                                                                   float2* __restrict__ partials)
 {
     constexpr int kWarps = kTrackThreads / 32;
     __shared__ float sh_terms[kWarps][32][33];
     __shared__ float2 sh_warp[kWarps][32];
-    __shared__ float2 sh_chunk[kWarps][32];
     __shared__ int sh_last;
+    __shared__ Tf T, Tri; // the poses live in shared memory: fewer live registers per thread
     if (st->flags[kFlagDone0 + ip.level])
         return;
-
-    Tf T, Tri;
-    for (int i = 0; i < 9; ++i) {
-        T.R[i] = st->pose_f[(i / 3) * 4 + (i % 3)];
-        Tri.R[i] = st->ref_inv[(i / 3) * 4 + (i % 3)];
-    }
-    for (int i = 0; i < 3; ++i) {
-        T.t[i] = st->pose_f[4 * i + 3];
-        Tri.t[i] = st->ref_inv[4 * i + 3];
-    }
-
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    CSum acc{0.0f, 0.0f}; // lane k: running compensated sum of term k over this warp's pixels
-    const int npix = ip.w * ip.h;
-    for (int base = blockIdx.x * kTrackThreads; base < npix; base += gridDim.x * kTrackThreads) {
-        float v[32];
-        const int i = base + threadIdx.x;
-        if (i < npix) {
-            icp_pixel_terms(s, ip, T, Tri, i, v);
+    if (threadIdx.x < 12) {
+        const int i = threadIdx.x, r = i >> 2, c = i & 3;
+        if (c < 3) {
+            T.R[3 * r + c] = st->pose_f[i];
+            Tri.R[3 * r + c] = st->ref_inv[i];
         }
         else {
-#pragma unroll
-            for (int k = 0; k < 32; ++k)
-                v[k] = 0.0f;
+            T.t[r] = st->pose_f[i];
+            Tri.t[r] = st->ref_inv[i];
         }
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    CSum acc[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+    const int npix = ip.w * ip.h;
+    const int stride = gridDim.x * kTrackThreads;
+    int i = blockIdx.x * kTrackThreads + threadIdx.x;
+    bool in_range = i < npix;
+    F3 n_cur = in_range ? ld3(ip.nrm, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
+    F3 p_cur = in_range ? ld3(ip.pts, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
+    for (int base = blockIdx.x * kTrackThreads; base < npix; base += stride) {
+        const int i_next = i + stride;
+        const bool next_in = i_next < npix;
+        const F3 n_next = next_in ? ld3(ip.nrm, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
+        const F3 p_next = next_in ? ld3(ip.pts, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
+        float v[32];
+        icp_pixel_terms(s, ip, T, Tri, in_range, n_cur, p_cur, v);
 #pragma unroll
         for (int k = 0; k < 32; ++k)
             sh_terms[warp][lane][k] = v[k];
         __syncwarp();
-#pragma unroll 8
+#pragma unroll
         for (int j = 0; j < 32; ++j)
-            acc.add(sh_terms[warp][j][lane]);
+            acc[j & 3].add(sh_terms[warp][j][lane]);
         __syncwarp();
+        i = i_next;
+        in_range = next_in;
+        n_cur = n_next;
+        p_cur = p_next;
     }
-    sh_warp[warp][lane] = make_float2(acc.hi, acc.lo);
+    acc[0].merge(acc[1].hi, acc[1].lo);
+    acc[2].merge(acc[3].hi, acc[3].lo);
+    acc[0].merge(acc[2].hi, acc[2].lo);
+    sh_warp[warp][lane] = make_float2(acc[0].hi, acc[0].lo);
     __syncthreads();
     if (threadIdx.x < 32) {
         CSum t{0.0f, 0.0f};
@@ -473,31 +479,36 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
         return;
     __threadfence();
 
-    // ---- last CTA: fixed-order compensated FP32 sum of the partials, FP64 solve and update
+    // ---- last CTA
+    __shared__ double sh_pose[12];
+    __shared__ double sh_val[32];
+    __shared__ double sh_dR[9], sh_dt[3];
+    __shared__ int sh_conv;
+    if (threadIdx.x < 12)
+        sh_pose[threadIdx.x] = __ldcg(&st->pose[threadIdx.x]); // overlaps the merge below
     {
         // warp w merges rows w, w + 8, ...; loads are issued 16 at a time so that the L2
         // latency is paid once per batch, not once per row
         CSum t{0.0f, 0.0f};
         const int nb = (int) gridDim.x;
         for (int b0 = warp; b0 < nb; b0 += 16 * kWarps) {
-            float2 p[16];
+            float2 pr[16];
 #pragma unroll
             for (int u = 0; u < 16; ++u) {
                 const int b = b0 + u * kWarps;
-                p[u] = b < nb ? __ldcg(&partials[b * 32 + lane]) : make_float2(0.0f, 0.0f);
+                pr[u] = b < nb ? __ldcg(&partials[b * 32 + lane]) : make_float2(0.0f, 0.0f);
             }
 #pragma unroll
             for (int u = 0; u < 16; ++u)
-                t.merge(p[u].x, p[u].y);
+                t.merge(pr[u].x, pr[u].y);
         }
-        sh_chunk[warp][lane] = make_float2(t.hi, t.lo);
+        sh_warp[warp][lane] = make_float2(t.hi, t.lo);
     }
     __syncthreads();
-    __shared__ double sh_val[32];
     if (threadIdx.x < 32) {
         CSum t{0.0f, 0.0f};
         for (int c = 0; c < kWarps; ++c)
-            t.merge(sh_chunk[c][threadIdx.x].x, sh_chunk[c][threadIdx.x].y);
+            t.merge(sh_warp[c][threadIdx.x].x, sh_warp[c][threadIdx.x].y);
         const double v = (double) t.hi + (double) t.lo;
         sh_val[threadIdx.x] = v;
         st->last_red[threadIdx.x] = (float) v;
@@ -506,49 +517,40 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
     if (threadIdx.x == 0) {
         st->ticket = 0;
         st->flags[kFlagIters0 + ip.level] += 1;
-        double C[36], b[6], xs[6];
+        double xs[6];
+        if (!ldlt_solve6(&sh_val[7], &sh_val[1], xs)) {
 #pragma unroll
-        for (int i = 0; i < 6; ++i)
-            b[i] = sh_val[1 + i];
-#pragma unroll
-        for (int r = 0; r < 6; ++r)
-#pragma unroll
-            for (int c = r; c < 6; ++c) {
-                const int q = 7 + r * 6 - r * (r - 1) / 2 + (c - r);
-                C[6 * r + c] = sh_val[q];
-                C[6 * c + r] = sh_val[q];
-            }
-        if (!ldlt_solve6(C, b, xs)) {
-#pragma unroll
-            for (int i = 0; i < 6; ++i)
-                xs[i] = 0.0;
+            for (int k = 0; k < 6; ++k)
+                xs[k] = 0.0;
         }
         double dR[9], dt[3];
         se3_exp_d(xs, dR, dt);
-        double P0[12], P[12];
 #pragma unroll
-        for (int i = 0; i < 12; ++i)
-            P0[i] = st->pose[i];
+        for (int k = 0; k < 9; ++k)
+            sh_dR[k] = dR[k];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                P[4 * i + j] = fma(dR[3 * i + 2], P0[8 + j], fma(dR[3 * i + 1], P0[4 + j], dR[3 * i] * P0[j]))
-                    + (j == 3 ? dt[i] : 0.0);
-        }
-#pragma unroll
-        for (int i = 0; i < 12; ++i) {
-            st->pose[i] = P[i];
-            st->pose_f[i] = (float) P[i];
-        }
+        for (int k = 0; k < 3; ++k)
+            sh_dt[k] = dt[k];
         double xn = 0.0;
 #pragma unroll
-        for (int i = 0; i < 6; ++i)
-            xn = fma(xs[i], xs[i], xn);
+        for (int k = 0; k < 6; ++k)
+            xn = fma(xs[k], xs[k], xn);
         const double thr = (double) ip.icp_threshold;
-        if (xn < thr * thr)
-            st->flags[kFlagDone0 + ip.level] = 1;
+        sh_conv = xn < thr * thr;
     }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        // T_WS <- exp(x) * T_WS, one entry per thread
+        const int r = threadIdx.x >> 2, c = threadIdx.x & 3;
+        double v = fma(sh_dR[3 * r + 2], sh_pose[8 + c],
+                       fma(sh_dR[3 * r + 1], sh_pose[4 + c], sh_dR[3 * r] * sh_pose[c]));
+        if (c == 3)
+            v += sh_dt[r];
+        st->pose[threadIdx.x] = v;
+        st->pose_f[threadIdx.x] = (float) v;
+    }
+    if (threadIdx.x == 0 && sh_conv)
+        st->flags[kFlagDone0 + ip.level] = 1;
 }
 
 // checkPoseKernel (icp.cpp:227-246): revert to the reference pose on a poor final alignment.
@@ -622,7 +624,8 @@ se_gpu_status se_gpu_tracker_create(const se_gpu_pinhole* sensor, const se_gpu_t
         t->li.pts[l] = t->pts[l];
         t->li.nrm[l] = t->nrm[l];
         t->li.depth[l] = t->pyr_depth[l];
-        const int ctas = (w * h + kTrackThreads * 4 - 1) / (kTrackThreads * 4); // ~4 tiles per CTA
+        const int tiles = (w * h + kTrackThreads - 1) / kTrackThreads; // one tile = 256 pixels
+        const int ctas = tiles < 300 ? tiles : 300;
         t->nctas[l] = ctas < 2 * device_sm_count() ? (ctas > 0 ? ctas : 1) : 2 * device_sm_count();
         if (t->nctas[l] > kMaxTrackCtas)
             t->nctas[l] = kMaxTrackCtas;
