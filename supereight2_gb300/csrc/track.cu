@@ -315,6 +315,123 @@ __device__ __forceinline__ void se3_exp_d(const double a[6], double R[9], double
     }
 }
 
+// ------------------------------------------------ warp-parallel FP64 solve and update --
+// One warp solves J^T J x = J^T e, forms exp(x) and composes the pose. Every dependent step
+// is a single FP64 instruction issued for all lanes, which on GB300 costs the same as one
+// issued for a single lane.
+//
+// Lane l < 21 holds entry (i, k), k <= i, of the symmetric matrix (l = i(i+1)/2 + k); lane
+// 21 + i holds b_i (column 6 of the augmented system). The elimination is division-free:
+// step j replaces every trailing entry by D_j A_ik - A_ij A_kj (rows scaled by the positive
+// pivot D_j instead of divided by it), so the six pivot reciprocals are formed together at
+// the end instead of one per step. Pivots <= 0 fail like the reference's LLT (icp.cpp:33-41).
+__constant__ signed char kTriRow[32] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 4, 5, 5, 5, 5, 5, 5,
+                                        0, 1, 2, 3, 4, 5, -1, -1, -1, -1, -1};
+__constant__ signed char kTriCol[32] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 4, 0, 1, 2, 3, 4, 5,
+                                        6, 6, 6, 6, 6, 6, -1, -1, -1, -1, -1};
+
+__device__ __forceinline__ int tri_lane(int i, int k) { return (i * (i + 1)) / 2 + k; }
+
+// sh_val: the 32 reduction values in shared memory (newReduce layout). Returns x in every lane.
+__device__ __forceinline__ bool warp_solve6(const double* sh_val, double x[6])
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int li = kTriRow[lane], lk = kTriCol[lane];
+    double a = 0.0;
+    if (lane < 21)
+        a = sh_val[7 + lk * 6 - lk * (lk - 1) / 2 + (li - lk)]; // upper-triangle entry (k, i)
+    else if (lane < 27)
+        a = sh_val[1 + li];
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        const double d = __shfl_sync(full, a, tri_lane(j, j));
+        ok = ok && (d > 0.0);
+        const bool trailing = li > j && lk > j;
+        const int src_ij = trailing ? tri_lane(li, j) : 0;
+        const int src_kj = trailing ? (lk == 6 ? 21 + j : tri_lane(lk, j)) : 0;
+        const double a_ij = __shfl_sync(full, a, src_ij);
+        const double a_kj = __shfl_sync(full, a, src_kj);
+        if (trailing)
+            a = fma(d, a, -(a_ij * a_kj));
+    }
+    // reciprocal of pivot i in lane 21 + i
+    const double piv = __shfl_sync(full, a, lane < 27 && lane >= 21 ? tri_lane(li, li) : 0);
+    const double r = (lane >= 21 && lane < 27) ? drcp(piv) : 0.0;
+    // back substitution on the upper-triangular rows: x_k = b_k / D_k, then b_j -= A_kj x_k
+#pragma unroll
+    for (int kk = 0; kk < 6; ++kk) {
+        const int k = 5 - kk;
+        const double xk = __shfl_sync(full, a * r, 21 + k);
+        x[k] = xk;
+        const bool upd = lk == 6 && li < k;
+        const double akj = __shfl_sync(full, a, upd ? tri_lane(k, li) : 0);
+        if (upd)
+            a = fma(-akj, xk, a);
+    }
+    return ok;
+}
+
+// Series coefficients (Horner, highest first) of A = sin t / t, B = (1 - cos t) / t^2 and
+// C = (t - sin t) / t^3 in x = t^2, for lanes 0, 1, 2.
+__constant__ double kExpSeries[3][5] = {{1.0 / 362880, -1.0 / 5040, 1.0 / 120, -1.0 / 6, 1.0},
+                                        {1.0 / 3628800, -1.0 / 40320, 1.0 / 720, -1.0 / 24, 0.5},
+                                        {1.0 / 39916800, -1.0 / 362880, 1.0 / 5040, -1.0 / 120, 1.0 / 6}};
+
+// T <- exp(x) * T in FP64 (math_util_impl.hpp:117-174 in Rodrigues form: R = I + A W + B W^2,
+// V = I + B W + C W^2, W = hat(omega), translation V rho). pose (shared memory, row-major
+// 3x4) is read by lanes 0..11, which then write the new pose to st.
+__device__ __forceinline__ void warp_exp_compose(const double x[6], const double* sh_pose, double* pose_out,
+                                                 float* pose_f_out)
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const double wx = x[3], wy = x[4], wz = x[5];
+    const double xx = fma(wz, wz, fma(wy, wy, wx * wx));
+    double coef;
+    if (xx < 0.01) {
+        const int c = lane % 3;
+        coef = kExpSeries[c][0];
+#pragma unroll
+        for (int u = 1; u < 5; ++u)
+            coef = fma(coef, xx, kExpSeries[c][u]);
+    }
+    else {
+        const double t = sqrt(xx);
+        double sn, cs;
+        sincos(t, &sn, &cs);
+        const double it = drcp(t), it2 = it * it;
+        const int c = lane % 3;
+        coef = c == 0 ? sn * it : (c == 1 ? (1.0 - cs) * it2 : (t - sn) * it2 * it);
+    }
+    const double cA = __shfl_sync(full, coef, 0), cB = __shfl_sync(full, coef, 1), cC = __shfl_sync(full, coef, 2);
+    // lanes 0..8: R_ij; lanes 9..17: V_ij (e = lane mod 9, i = e / 3, j = e mod 3)
+    const int e = lane % 9, i = e / 3, j = e % 3;
+    const double wi = i == 0 ? wx : (i == 1 ? wy : wz);
+    const double wj = j == 0 ? wx : (j == 1 ? wy : wz);
+    const double w_hat = (i == j) ? 0.0 : ((j == (i + 1) % 3) ? -(3 - i - j == 0 ? wx : (3 - i - j == 1 ? wy : wz))
+                                                              : (3 - i - j == 0 ? wx : (3 - i - j == 1 ? wy : wz)));
+    const double w2 = fma(wi, wj, i == j ? -xx : 0.0);
+    const double c1 = lane < 9 ? cA : cB, c2 = lane < 9 ? cB : cC;
+    const double val = fma(c2, w2, fma(c1, w_hat, i == j ? 1.0 : 0.0));
+    // translation t_i = sum_j V_ij rho_j at lanes 9 + 3i
+    const double rho_j = j == 0 ? x[0] : (j == 1 ? x[1] : x[2]);
+    const double vr = (lane >= 9 && lane < 18) ? val * rho_j : 0.0;
+    const double t_i = vr + __shfl_down_sync(full, vr, 1) + __shfl_down_sync(full, vr, 2);
+    // compose: lane 4r + c (r < 3, c < 4) forms P_rc = sum_k R_rk P_kc (+ t_r for c = 3)
+    const int pr = (lane >> 2) % 3, pc = lane & 3;
+    const double r0 = __shfl_sync(full, val, 3 * pr), r1 = __shfl_sync(full, val, 3 * pr + 1);
+    const double r2 = __shfl_sync(full, val, 3 * pr + 2), tr = __shfl_sync(full, t_i, 9 + 3 * pr);
+    if (lane < 12) {
+        double v = fma(r2, sh_pose[8 + pc], fma(r1, sh_pose[4 + pc], r0 * sh_pose[pc]));
+        if (pc == 3)
+            v += tr;
+        pose_out[lane] = v;
+        pose_f_out[lane] = (float) v;
+    }
+}
+
 struct IterParams {
     const float* ref_pts;
     const float* ref_nrm;
@@ -482,7 +599,6 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
     // ---- last CTA
     __shared__ double sh_pose[12];
     __shared__ double sh_val[32];
-    __shared__ double sh_dR[9], sh_dt[3];
     __shared__ int sh_conv;
     if (threadIdx.x < 12)
         sh_pose[threadIdx.x] = __ldcg(&st->pose[threadIdx.x]); // overlaps the merge below
@@ -514,41 +630,26 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
         st->last_red[threadIdx.x] = (float) v;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        st->ticket = 0;
-        st->flags[kFlagIters0 + ip.level] += 1;
+    if (threadIdx.x < 32) {
         double xs[6];
-        if (!ldlt_solve6(&sh_val[7], &sh_val[1], xs)) {
+        if (!warp_solve6(sh_val, xs)) {
 #pragma unroll
             for (int k = 0; k < 6; ++k)
                 xs[k] = 0.0;
         }
-        double dR[9], dt[3];
-        se3_exp_d(xs, dR, dt);
+        warp_exp_compose(xs, sh_pose, st->pose, st->pose_f);
+        if (threadIdx.x == 0) {
+            st->ticket = 0;
+            st->flags[kFlagIters0 + ip.level] += 1;
+            double xn = 0.0;
 #pragma unroll
-        for (int k = 0; k < 9; ++k)
-            sh_dR[k] = dR[k];
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-            sh_dt[k] = dt[k];
-        double xn = 0.0;
-#pragma unroll
-        for (int k = 0; k < 6; ++k)
-            xn = fma(xs[k], xs[k], xn);
-        const double thr = (double) ip.icp_threshold;
-        sh_conv = xn < thr * thr;
+            for (int k = 0; k < 6; ++k)
+                xn = fma(xs[k], xs[k], xn);
+            const double thr = (double) ip.icp_threshold;
+            sh_conv = xn < thr * thr;
+        }
     }
     __syncthreads();
-    if (threadIdx.x < 12) {
-        // T_WS <- exp(x) * T_WS, one entry per thread
-        const int r = threadIdx.x >> 2, c = threadIdx.x & 3;
-        double v = fma(sh_dR[3 * r + 2], sh_pose[8 + c],
-                       fma(sh_dR[3 * r + 1], sh_pose[4 + c], sh_dR[3 * r] * sh_pose[c]));
-        if (c == 3)
-            v += sh_dt[r];
-        st->pose[threadIdx.x] = v;
-        st->pose_f[threadIdx.x] = (float) v;
-    }
     if (threadIdx.x == 0 && sh_conv)
         st->flags[kFlagDone0 + ip.level] = 1;
 }
