@@ -333,7 +333,9 @@ __constant__ signed char kTriCol[32] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 0, 1, 2, 3
 __device__ __forceinline__ int tri_lane(int i, int k) { return (i * (i + 1)) / 2 + k; }
 
 // sh_val: the 32 reduction values in shared memory (newReduce layout). Returns x in every lane.
-__device__ __forceinline__ bool warp_solve6(const double* sh_val, double x[6])
+// The loops are deliberately rolled: the tail runs once per launch on whichever SM finishes
+// last, so its instruction stream is cold and code size costs more than loop overhead.
+__device__ __noinline__ bool warp_solve6(const double* sh_val, double x[6])
 {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -344,7 +346,7 @@ __device__ __forceinline__ bool warp_solve6(const double* sh_val, double x[6])
     else if (lane < 27)
         a = sh_val[1 + li];
     bool ok = true;
-#pragma unroll
+#pragma unroll 1
     for (int j = 0; j < 6; ++j) {
         const double d = __shfl_sync(full, a, tri_lane(j, j));
         ok = ok && (d > 0.0);
@@ -360,16 +362,20 @@ __device__ __forceinline__ bool warp_solve6(const double* sh_val, double x[6])
     const double piv = __shfl_sync(full, a, lane < 27 && lane >= 21 ? tri_lane(li, li) : 0);
     const double r = (lane >= 21 && lane < 27) ? drcp(piv) : 0.0;
     // back substitution on the upper-triangular rows: x_k = b_k / D_k, then b_j -= A_kj x_k
-#pragma unroll
-    for (int kk = 0; kk < 6; ++kk) {
-        const int k = 5 - kk;
+    double xv = 0.0; // lane 21 + k ends up holding x_k
+#pragma unroll 1
+    for (int k = 5; k >= 0; --k) {
         const double xk = __shfl_sync(full, a * r, 21 + k);
-        x[k] = xk;
+        if (lane == 21 + k)
+            xv = xk;
         const bool upd = lk == 6 && li < k;
         const double akj = __shfl_sync(full, a, upd ? tri_lane(k, li) : 0);
         if (upd)
             a = fma(-akj, xk, a);
     }
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        x[k] = __shfl_sync(full, xv, 21 + k);
     return ok;
 }
 
@@ -382,8 +388,8 @@ __constant__ double kExpSeries[3][5] = {{1.0 / 362880, -1.0 / 5040, 1.0 / 120, -
 // T <- exp(x) * T in FP64 (math_util_impl.hpp:117-174 in Rodrigues form: R = I + A W + B W^2,
 // V = I + B W + C W^2, W = hat(omega), translation V rho). pose (shared memory, row-major
 // 3x4) is read by lanes 0..11, which then write the new pose to st.
-__device__ __forceinline__ void warp_exp_compose(const double x[6], const double* sh_pose, double* pose_out,
-                                                 float* pose_f_out)
+__device__ __noinline__ void warp_exp_compose(const double x[6], const double* sh_pose, double* pose_out,
+                                              float* pose_f_out)
 {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -393,7 +399,7 @@ __device__ __forceinline__ void warp_exp_compose(const double x[6], const double
     if (xx < 0.01) {
         const int c = lane % 3;
         coef = kExpSeries[c][0];
-#pragma unroll
+#pragma unroll 1
         for (int u = 1; u < 5; ++u)
             coef = fma(coef, xx, kExpSeries[c][u]);
     }
@@ -567,7 +573,7 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
         for (int k = 0; k < 32; ++k)
             sh_terms[warp][lane][k] = v[k];
         __syncwarp();
-#pragma unroll
+#pragma unroll 4
         for (int j = 0; j < 32; ++j)
             acc[j & 3].add(sh_terms[warp][j][lane]);
         __syncwarp();
