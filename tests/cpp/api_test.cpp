@@ -1,0 +1,88 @@
+// Exercises the C++ mirror of the reference API (include/se_gpu.hpp) the way the reference's
+// own tests and application use se::MapIntegrator / se::raycaster / se::Tracker: the wall of
+// test/map/map/map_aabb_unittest.cpp integrated, raycast and tracked. Exit code 0 on success.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "se_gpu.hpp"
+
+#define REQUIRE(cond)                                                                              \
+    do {                                                                                           \
+        if (!(cond)) {                                                                             \
+            std::printf("FAILED: %s (line %d)\n", #cond, __LINE__);                                \
+            return 1;                                                                              \
+        }                                                                                          \
+    } while (0)
+
+int main()
+{
+    const int W = 100, H = 100;
+    se::gpu::PinholeCamera sensor(W, H, 100.0f, 100.0f, W / 2 - 0.5f, H / 2 - 0.5f, 0.1f, 10.0f);
+    // T_BS = AngleAxis(pi/2, Y) * AngleAxis(-pi/2, Z): z-forward camera looking along world +x
+    se::gpu::Pose T_WC = {0, 0, 1, 0, -1, 0, 0, 0, 0, -1, 0, 0, 0, 0, 0, 1};
+
+    se::gpu::TSDFMap::Config cfg;
+    cfg.dim = {12.8f, 12.8f, 12.8f};
+    cfg.res = 0.1f;
+    cfg.max_blocks = 1 << 14;
+    se::gpu::TSDFMap map(cfg);
+    REQUIRE(map.size() == 128);
+
+    float *depth = nullptr, *pts = nullptr, *nrm = nullptr;
+    int8_t* scale = nullptr;
+    REQUIRE(cudaMalloc(&depth, W * H * sizeof(float)) == cudaSuccess);
+    REQUIRE(cudaMalloc(&pts, W * H * 3 * sizeof(float)) == cudaSuccess);
+    REQUIRE(cudaMalloc(&nrm, W * H * 3 * sizeof(float)) == cudaSuccess);
+    REQUIRE(cudaMalloc(&scale, W * H) == cudaSuccess);
+    std::vector<float> wall(W * H, 4.0f);
+    REQUIRE(cudaMemcpy(depth, wall.data(), W * H * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess);
+
+    se::gpu::MapIntegrator integrator(map);
+    for (int frame = 0; frame < 3; ++frame)
+        integrator.integrateDepth(frame, se::gpu::Measurement{{depth, W, H}, sensor, T_WC});
+    map.check_errors();
+    REQUIRE(map.num_blocks() > 0);
+
+    int32_t mn[3], mx[3];
+    int empty = 1;
+    se::gpu::check(se_gpu_map_aabb(map.handle(), mn, mx, &empty), "aabb");
+    REQUIRE(!empty);
+    // the band [4 - 0.8, 4 + 0.8] m in x, map origin at 6.4 m: voxels 96..111
+    REQUIRE(mn[0] == 96 && mx[0] == 111);
+
+    se::gpu::raycaster::raycast_volume(map, sensor, T_WC, {pts, W, H}, {nrm, W, H}, {scale, W, H});
+    std::vector<float> hp(W * H * 3), hn(W * H * 3);
+    REQUIRE(cudaMemcpy(hp.data(), pts, hp.size() * 4, cudaMemcpyDeviceToHost) == cudaSuccess);
+    REQUIRE(cudaMemcpy(hn.data(), nrm, hn.size() * 4, cudaMemcpyDeviceToHost) == cudaSuccess);
+    int hits = 0;
+    for (int i = 0; i < W * H; ++i) {
+        if (hp[3 * i] != 0.0f) {
+            ++hits;
+            REQUIRE(std::fabs(hp[3 * i] - 4.0f) < 2e-3f); // the wall is the plane x = 4
+            REQUIRE(hn[3 * i] < -0.99f);                  // normal towards the camera
+        }
+    }
+    REQUIRE(hits > W * H / 2);
+
+    se::gpu::Tracker tracker(map, sensor);
+    se::gpu::Pose T = T_WC;
+    const bool ok = tracker.track({depth, W, H}, T, {pts, W, H}, {nrm, W, H});
+    // A fronto-parallel wall constrains only the x translation and two rotations, so the
+    // normal equations may be singular (then the update is zero, as in the reference). Either
+    // way the pose stays finite and, when accepted, does not move along x: the wall is at the
+    // integrated depth.
+    for (int i = 0; i < 16; ++i)
+        REQUIRE(std::isfinite(T[i]));
+    if (ok)
+        REQUIRE(std::fabs(T[3] - T_WC[3]) < 1e-2f);
+
+    cudaFree(depth);
+    cudaFree(pts);
+    cudaFree(nrm);
+    cudaFree(scale);
+    std::printf("cpp api ok: %d hits, %lld blocks\n", hits, (long long) map.num_blocks());
+    return 0;
+}
