@@ -182,6 +182,23 @@ SE_GPU_API se_gpu_status se_gpu_track(se_gpu_tracker* tracker, const float* dept
 SE_GPU_API se_gpu_status se_gpu_tracker_last_reduction(se_gpu_tracker* tracker, float reduction[32],
                                             int iterations_run[3]);
 
+/* Allocation-free tracking. No counterpart in the reference. For callers that cannot
+ * allocate device memory while they track (a host whose pool allocator owns the free device
+ * memory, a loop with a memory budget fixed at start-up, or code that must not let
+ * cudaMalloc's implicit device synchronisation stall its other streams): one full-resolution
+ * ICP level (config->num_levels must be 1, config->iterations[0] iterations), with the
+ * tracker's scratch in a static device array of about 77 KiB that the library holds on every
+ * GPU that loads it. Depth images larger than 4096 x 4096 pixels are rejected. The first call
+ * on a device looks up the array's device address; make that first call before any stream
+ * capture. Calls share the array: calls that overlap on the GPU race. T_WS is read and
+ * written on the host; accepted and reduction (32 floats, se_gpu_tracker_last_reduction's
+ * layout) may be NULL. Synchronous. */
+SE_GPU_API se_gpu_status se_gpu_track_noalloc(const se_gpu_pinhole* sensor,
+                                              const se_gpu_tracker_config* config,
+                                              const float* depth_dev, const float* ref_pts_W_dev,
+                                              const float* ref_nrm_W_dev, float T_WS[16],
+                                              int* accepted, float reduction[32], void* stream);
+
 /* ---------------------------------------------------------------- captured pipeline -- */
 
 /* The per-frame loop of the reference application (app/src/main.cpp:126-160: track the new

@@ -23,6 +23,7 @@ import numpy as np
 from . import build as _build
 
 __all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "raycast_volume",
+           "track_noalloc",
            "FramePipeline", "SeGpuError", "library", "library_path"]
 
 
@@ -80,6 +81,8 @@ SIGNATURES = {
     "se_gpu_tracker_destroy": (C.c_int, [_VP]),
     "se_gpu_track": (C.c_int, [_VP, _VP, _VP, _VP, _F16, C.POINTER(C.c_int), _VP]),
     "se_gpu_tracker_last_reduction": (C.c_int, [_VP, _F16, C.POINTER(C.c_int)]),
+    "se_gpu_track_noalloc": (C.c_int, [C.POINTER(_Pinhole), C.POINTER(_TrackerConfig), _VP, _VP,
+                                       _VP, _F16, C.POINTER(C.c_int), _F16, _VP]),
     "se_gpu_frame_create": (C.c_int, [_VP, _VP, C.POINTER(_Pinhole), C.POINTER(_VP)]),
     "se_gpu_frame_destroy": (C.c_int, [_VP]),
     "se_gpu_frame_buffers": (C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_VP),
@@ -367,6 +370,31 @@ class Tracker:
         its = (C.c_int * 3)()
         _check(self._L.se_gpu_tracker_last_reduction(self.h, red, its), "last_reduction")
         return np.array(red[:], np.float32), list(its[:])
+
+
+def track_noalloc(sensor: PinholeCamera, config: TrackerConfig, depth, T_WS,
+                  surface_point_cloud_W, surface_normals_W, stream=None):
+    """One-level ICP that allocates no device memory (no counterpart in the reference).
+
+    For callers that cannot allocate while they track; the scratch is a static device array
+    inside the library, shared by all calls, so calls must not overlap on the GPU. ``config``
+    must have exactly one level. T_WS (float32 4x4 numpy, C-contiguous) is updated in place.
+    Returns (accepted, reduction[32])."""
+    import torch
+    L = library()
+    d = _dptr(depth, torch.float32, (sensor.height, sensor.width), "depth")
+    p = _dptr(surface_point_cloud_W, torch.float32, (sensor.height, sensor.width, 3), "points")
+    n = _dptr(surface_normals_W, torch.float32, (sensor.height, sensor.width, 3), "normals")
+    if not (isinstance(T_WS, np.ndarray) and T_WS.dtype == np.float32 and T_WS.shape == (4, 4)
+            and T_WS.flags.c_contiguous):
+        raise SeGpuError("T_WS must be a C-contiguous float32 4x4 numpy array (updated in place)")
+    s = sensor._c()
+    c = config._c()
+    acc = C.c_int()
+    red = (C.c_float * 32)()
+    _check(L.se_gpu_track_noalloc(C.byref(s), C.byref(c), d, p, n, T_WS.ctypes.data_as(_F16),
+                                  C.byref(acc), red, _stream(stream)), "se_gpu_track_noalloc")
+    return bool(acc.value), np.array(red[:], np.float32)
 
 
 class FramePipeline:

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstring>
+#include <mutex>
 
 #include "pipeline.cuh"
 #include "profile.cuh"
@@ -877,3 +878,313 @@ se_gpu_status se_gpu_tracker_last_reduction(se_gpu_tracker* t, float reduction[3
 }
 
 } // extern "C"
+
+namespace se_gpu {
+
+// ================================================== allocation-free single-level tracking ==
+//
+// Some callers cannot allocate device memory when they track: a host that has handed all
+// free device memory to its own pool allocator, a real-time or certified loop whose memory
+// budget is fixed at start-up, or a process that must not let cudaMalloc's implicit device
+// synchronisation stall its other streams. se_gpu_track_noalloc serves them: the caller passes
+// only its depth image, the reference raycast and the pose, and the ICP's scratch (the
+// iteration state and the per-CTA partial sums) lives in the file-scope array below, which
+// every GPU that loads this library keeps for the life of the process.
+//
+// It tracks at full resolution only (config->num_levels == 1): the input point cloud and
+// normals are formed on the fly from the depth image, with the arithmetic of
+// depth_to_point_cloud and point_cloud_to_normal, so no pyramid images are needed.
+
+constexpr int kNoAllocMaxCtas = 300;                  // the tracker's largest ICP grid
+constexpr long long kNoAllocMaxPixels = 4096LL * 4096LL; // largest depth image accepted
+
+struct NoAllocScratch {
+    TrackState state;
+    float2 partials[kNoAllocMaxCtas * 32];
+};
+
+// 256-byte aligned scratch of sizeof(NoAllocScratch) bytes (about 77 KiB) per device. All
+// calls share it and it keeps the last call's contents: each call clears what must start at
+// zero (flags, ticket, reduction) in track_init_kernel, and calls that overlap on the GPU
+// (two streams, or two host threads) race on it.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+// depth_to_point_cloud for pixel i of the full-resolution image
+__device__ __forceinline__ F3 depth_point(const float* __restrict__ depth, const Pinhole& s, int w, int i)
+{
+    const float d = depth[i];
+    if (d > 0.0f)
+        return mul(d, back_project(s, (float) (i % w), (float) (i / w)));
+    return f3(0.0f, 0.0f, 0.0f);
+}
+
+// point_cloud_to_normal<NegY> for pixel i, reading the neighbours' points from the depth image
+__device__ __forceinline__ F3 depth_normal(const float* __restrict__ depth, const Pinhole& s, int w, int h, int i,
+                                           int neg_y)
+{
+    const int x = i % w, y = i / w;
+    const F3 p = depth_point(depth, s, w, i);
+    if (p.z == 0.0f)
+        return f3(0.0f, 0.0f, 0.0f);
+    const int lx = max(x - 1, 0), rx = min(x + 1, w - 1);
+    int uy, dy;
+    if (neg_y) {
+        uy = max(y - 1, 0);
+        dy = min(y + 1, h - 1);
+    }
+    else {
+        dy = max(y - 1, 0);
+        uy = min(y + 1, h - 1);
+    }
+    const F3 left = depth_point(depth, s, w, lx + w * y), right = depth_point(depth, s, w, rx + w * y);
+    const F3 up = depth_point(depth, s, w, x + w * uy), down = depth_point(depth, s, w, x + w * dy);
+    if (left.z == 0.0f || right.z == 0.0f || up.z == 0.0f || down.z == 0.0f)
+        return f3(0.0f, 0.0f, 0.0f);
+    return normalized(cross(sub(right, left), sub(up, down)));
+}
+
+// icp_iter_kernel with its inputs formed from the depth image and its scratch in the static
+// array (same per-pixel terms, reduction order and FP64 tail).
+__global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_noalloc_kernel(Pinhole s, IterParams ip, const float* __restrict__ depth,
+                                                                          int neg_y, NoAllocScratch* scratch)
+{
+    constexpr int kWarps = kTrackThreads / 32;
+    TrackState* st = &scratch->state;
+    float2* __restrict__ partials = scratch->partials;
+    __shared__ float sh_terms[kWarps][32][33];
+    __shared__ float2 sh_warp[kWarps][32];
+    __shared__ int sh_last;
+    __shared__ Tf T, Tri; // the poses live in shared memory: fewer live registers per thread
+    if (st->flags[kFlagDone0 + ip.level])
+        return;
+    if (threadIdx.x < 12) {
+        const int i = threadIdx.x, r = i >> 2, c = i & 3;
+        if (c < 3) {
+            T.R[3 * r + c] = st->pose_f[i];
+            Tri.R[3 * r + c] = st->ref_inv[i];
+        }
+        else {
+            T.t[r] = st->pose_f[i];
+            Tri.t[r] = st->ref_inv[i];
+        }
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    CSum acc[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+    const int npix = ip.w * ip.h;
+    const int stride = gridDim.x * kTrackThreads;
+    int i = blockIdx.x * kTrackThreads + threadIdx.x;
+    bool in_range = i < npix;
+    F3 n_cur = in_range ? depth_normal(depth, s, ip.w, ip.h, i, neg_y) : f3(0.0f, 0.0f, 0.0f);
+    F3 p_cur = in_range ? depth_point(depth, s, ip.w, i) : f3(0.0f, 0.0f, 0.0f);
+    for (int base = blockIdx.x * kTrackThreads; base < npix; base += stride) {
+        const int i_next = i + stride;
+        const bool next_in = i_next < npix;
+        const F3 n_next = next_in ? depth_normal(depth, s, ip.w, ip.h, i_next, neg_y) : f3(0.0f, 0.0f, 0.0f);
+        const F3 p_next = next_in ? depth_point(depth, s, ip.w, i_next) : f3(0.0f, 0.0f, 0.0f);
+        float v[32];
+        icp_pixel_terms(s, ip, T, Tri, in_range, n_cur, p_cur, v);
+#pragma unroll
+        for (int k = 0; k < 32; ++k)
+            sh_terms[warp][lane][k] = v[k];
+        __syncwarp();
+#pragma unroll 4
+        for (int j = 0; j < 32; ++j)
+            acc[j & 3].add(sh_terms[warp][j][lane]);
+        __syncwarp();
+        i = i_next;
+        in_range = next_in;
+        n_cur = n_next;
+        p_cur = p_next;
+    }
+    acc[0].merge(acc[1].hi, acc[1].lo);
+    acc[2].merge(acc[3].hi, acc[3].lo);
+    acc[0].merge(acc[2].hi, acc[2].lo);
+    sh_warp[warp][lane] = make_float2(acc[0].hi, acc[0].lo);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        CSum t{0.0f, 0.0f};
+        for (int wi = 0; wi < kWarps; ++wi)
+            t.merge(sh_warp[wi][threadIdx.x].x, sh_warp[wi][threadIdx.x].y);
+        partials[blockIdx.x * 32 + threadIdx.x] = make_float2(t.hi, t.lo);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0)
+        sh_last = (atomicAdd(&st->ticket, 1u) == gridDim.x - 1) ? 1 : 0;
+    __syncthreads();
+    if (!sh_last)
+        return;
+    __threadfence();
+
+    // ---- last CTA
+    __shared__ double sh_pose[12];
+    __shared__ double sh_val[32];
+    __shared__ int sh_conv;
+    if (threadIdx.x < 12)
+        sh_pose[threadIdx.x] = __ldcg(&st->pose[threadIdx.x]); // overlaps the merge below
+    {
+        // warp w merges rows w, w + 8, ...; loads are issued 16 at a time so that the L2
+        // latency is paid once per batch, not once per row
+        CSum t{0.0f, 0.0f};
+        const int nb = (int) gridDim.x;
+        for (int b0 = warp; b0 < nb; b0 += 16 * kWarps) {
+            float2 pr[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                const int b = b0 + u * kWarps;
+                pr[u] = b < nb ? __ldcg(&partials[b * 32 + lane]) : make_float2(0.0f, 0.0f);
+            }
+#pragma unroll
+            for (int u = 0; u < 16; ++u)
+                t.merge(pr[u].x, pr[u].y);
+        }
+        sh_warp[warp][lane] = make_float2(t.hi, t.lo);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        CSum t{0.0f, 0.0f};
+        for (int c = 0; c < kWarps; ++c)
+            t.merge(sh_warp[c][threadIdx.x].x, sh_warp[c][threadIdx.x].y);
+        const double v = (double) t.hi + (double) t.lo;
+        sh_val[threadIdx.x] = v;
+        st->last_red[threadIdx.x] = (float) v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double xs[6];
+        if (!warp_solve6(sh_val, xs)) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+                xs[k] = 0.0;
+        }
+        warp_exp_compose(xs, sh_pose, st->pose, st->pose_f);
+        if (threadIdx.x == 0) {
+            st->ticket = 0;
+            st->flags[kFlagIters0 + ip.level] += 1;
+            double xn = 0.0;
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+                xn = fma(xs[k], xs[k], xn);
+            const double thr = (double) ip.icp_threshold;
+            sh_conv = xn < thr * thr;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && sh_conv)
+        st->flags[kFlagDone0 + ip.level] = 1;
+}
+
+
+} // namespace se_gpu
+
+// Device address of the static scratch, looked up once per device (cudaGetSymbolAddress with
+// that device current) by the first call made on the device.
+static void* g_noalloc_addr[64];
+static std::mutex g_noalloc_mu;
+
+static se_gpu_status noalloc_scratch(NoAllocScratch** out)
+{
+    int dev = 0;
+    SE_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_last_error("se_gpu_track_noalloc: device ordinal %d out of range", dev);
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr)
+            return cuda_status(e != cudaSuccess ? e : cudaErrorInvalidSymbol, "cudaGetSymbolAddress(scratch)");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = (NoAllocScratch*) g_noalloc_addr[dev];
+    return SE_GPU_OK;
+}
+
+extern "C" se_gpu_status se_gpu_track_noalloc(const se_gpu_pinhole* sensor, const se_gpu_tracker_config* config,
+                                              const float* depth_dev, const float* ref_pts, const float* ref_nrm,
+                                              float T_WS[16], int* accepted, float reduction[32],
+                                              void* stream_p)
+{
+    if (!sensor || !config || !depth_dev || !ref_pts || !ref_nrm || !T_WS || sensor->width <= 0
+        || sensor->height <= 0) {
+        set_last_error("se_gpu_track_noalloc: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    if (config->num_levels != 1) {
+        set_last_error("se_gpu_track_noalloc: tracks one full-resolution level only (num_levels = %d; a pyramid "
+                       "would need scratch images)", config->num_levels);
+        return SE_GPU_ERR_NOT_SUPPORTED;
+    }
+    const long long npix = (long long) sensor->width * sensor->height;
+    if (npix > kNoAllocMaxPixels) {
+        set_last_error("se_gpu_track_noalloc: a %dx%d image exceeds the allocation-free limit of %lld pixels",
+                       sensor->width, sensor->height, kNoAllocMaxPixels);
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    if (config->iterations[0] < 0 || config->iterations[0] > 1000) {
+        set_last_error("se_gpu_track_noalloc: iterations[0] = %d out of range", config->iterations[0]);
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    NoAllocScratch* scratch = nullptr;
+    se_gpu_status st = noalloc_scratch(&scratch);
+    if (st != SE_GPU_OK)
+        return st;
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    const Pinhole s = make_pinhole(*sensor);
+
+    TrackInit init;
+    std::memset(&init, 0, sizeof(init));
+    const Tf T = tf_from16(T_WS);
+    const Tf Ti = inverse_iso(T);
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) {
+            init.T_WS[4 * i + j] = T.R[3 * i + j];
+            init.ref_inv[4 * i + j] = Ti.R[3 * i + j];
+        }
+        init.T_WS[4 * i + 3] = T.t[i];
+        init.ref_inv[4 * i + 3] = Ti.t[i];
+    }
+    track_init_kernel<<<1, 1, 0, stream>>>(&scratch->state, init, nullptr);
+    IterParams ip;
+    ip.ref_pts = ref_pts;
+    ip.ref_nrm = ref_nrm;
+    ip.pts = nullptr;
+    ip.nrm = nullptr;
+    ip.w = sensor->width;
+    ip.h = sensor->height;
+    ip.W = sensor->width;
+    ip.level = 0;
+    ip.dist_threshold = config->dist_threshold;
+    ip.normal_threshold = config->normal_threshold;
+    ip.icp_threshold = config->icp_threshold;
+    const long long tiles = (npix + kTrackThreads - 1) / kTrackThreads;
+    int ctas = (int) (tiles < kNoAllocMaxCtas ? tiles : kNoAllocMaxCtas);
+    if (ctas > 2 * device_sm_count())
+        ctas = 2 * device_sm_count();
+    for (int it = 0; it < config->iterations[0]; ++it)
+        icp_iter_noalloc_kernel<<<ctas, kTrackThreads, 0, stream>>>(s, ip, depth_dev, s.left_hand, scratch);
+    icp_check_kernel<<<1, 1, 0, stream>>>(&scratch->state, sensor->width, sensor->height, config->track_threshold,
+                                          nullptr);
+    SE_CUDA_TRY(cudaGetLastError());
+    float head[12 + kNumFlags];
+    float red[32];
+    SE_CUDA_TRY(cudaMemcpyAsync(head, &scratch->state, kTrackReadback, cudaMemcpyDeviceToHost, stream));
+    SE_CUDA_TRY(cudaMemcpyAsync(red, scratch->state.last_red, sizeof(red), cudaMemcpyDeviceToHost, stream));
+    SE_CUDA_TRY(cudaStreamSynchronize(stream));
+    for (int i = 0; i < 12; ++i)
+        T_WS[i] = head[i];
+    T_WS[12] = T_WS[13] = T_WS[14] = 0.0f;
+    T_WS[15] = 1.0f;
+    if (accepted) {
+        int flags[kNumFlags];
+        std::memcpy(flags, &head[12], sizeof(flags));
+        *accepted = flags[kFlagAccepted];
+    }
+    if (reduction)
+        std::memcpy(reduction, red, sizeof(red));
+    return SE_GPU_OK;
+}
