@@ -43,6 +43,26 @@ def _peaks():
     return 6800.0, "fallback"
 
 
+# Bench kernel names -> the kernel names of the committed DRAM-traffic capture of this workload
+_TRAFFIC_NAMES = {"icp_iter": "icp_iter_kernel", "update": "update_kernel<0>", "raycast": "raycast_kernel<0>",
+                  "carve": "carve_kernel", "frustum": "frustum_kernel"}
+
+
+def _traffic(kernel):
+    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu capture of this
+    workload (profiles/dram_traffic_tsdf640_bench.txt), or None."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic_tsdf640_bench.txt")
+    name = _TRAFFIC_NAMES.get(kernel)
+    if not name or not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            parts = line.split()
+            if parts and not line.startswith("#") and parts[0] == name:
+                return float(parts[4])
+    return None
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -258,7 +278,8 @@ def run_ours(args, ws, rank, local):
     ub = [st["n_updated_voxels"] * 2 * S_v + st["n_listed_blocks"] * 8 + W * H * 4 for st in plain["stats"]]
     upd_ms = kms.get("update", 0.0) / max(kl.get("update", 1), 1)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
+                "frac": (achieved / hbm_peak) if achieved else None, "traffic": _traffic(dom),
+                "traffic_source": "profiles/dram_traffic_tsdf640_bench.txt (ncu, --cache-control none)",
                 "peak_kind": peak_kind, "algorithmic_bytes_per_launch": algo,
                 "avg_launch_us": avg_launch_ms * 1e3,
                 "integration": {"kernel": "update", "avg_launch_us": upd_ms * 1e3,
