@@ -62,7 +62,7 @@ typedef struct {
     float T_MW[16];    /* world-to-map transform; set has_T_MW = 0 for translation(dim/2) */
     int has_T_MW;
     int field;         /* se_gpu_field; only SE_GPU_FIELD_TSDF in this library */
-    int res_type;      /* se_gpu_res; only SE_GPU_RES_SINGLE in this library */
+    int res_type;      /* se_gpu_res: single-res (Map<.., Res::Single>) or multi-res TSDF */
     int storage;       /* se_gpu_storage */
     float truncation_boundary_factor; /* reference default 8 */
     float max_weight;  /* reference default 100; must be an integer <= 65535 */
@@ -117,11 +117,12 @@ SE_GPU_API se_gpu_status se_gpu_map_size(const se_gpu_map* map, int* size, float
 /* Synchronise the map's last stream and return any latched device-side error, then clear it. */
 SE_GPU_API se_gpu_status se_gpu_map_check(se_gpu_map* map);
 
-/* Replaces se::MapIntegrator<TSDFMap<Res::Single>>::integrateDepth(timestamp,
+/* Replaces se::MapIntegrator<TSDFMap<Res::Single | Res::Multi>>::integrateDepth(timestamp,
  * Measurements{Measurement{depth, sensor, T_WC}}) (include/se/integrator/map_integrator.hpp:78-81,
  * impl/map_integrator_impl.hpp:52-84): RaycastCarver allocation (allocator/impl/
  * raycast_carver_impl.hpp:56-128) then the single-res TSDF update (updater/impl/
- * singleres_tsdf_updater_impl.hpp:14-132). depth_dev: width*height floats on the device. */
+ * singleres_tsdf_updater_impl.hpp:14-132) or the multi-res one (updater/impl/
+ * multires_tsdf_updater_impl.hpp:14-250). depth_dev: width*height floats on the device. */
 SE_GPU_API se_gpu_status se_gpu_integrate_depth(se_gpu_map* map, const float* depth_dev,
                                      const se_gpu_pinhole* sensor, const float T_WC[16],
                                      int timestamp, void* stream);
@@ -142,7 +143,17 @@ SE_GPU_API se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinh
 SE_GPU_API se_gpu_status se_gpu_map_download_blocks(const se_gpu_map* map, int64_t capacity,
                                          uint64_t* keys, int32_t* coords, float* tsdf,
                                          float* weight, int32_t* timestamps, int64_t* count);
-/* Block upload (checkpoint restore, test set-up): allocates the blocks with the given keys
+/* Multi-resolution maps: per block the 585-entry voxel pyramid of BlockMultiRes
+ * (include/se/map/octant/block.hpp:66-166; scale 0: 512 entries x + 8y + 64z at offset 0,
+ * scale 1: 64 at 512, scale 2: 8 at 576, scale 3: 1 at 584) of data (tsdf, weight) and past
+ * data (past_tsdf, past_weight), and scales (2 ints per block: current_scale, min_scale; -1
+ * before the first update). se_gpu_map_download_blocks returns a multi-res map's scale-0
+ * level. Host pointers, any may be NULL; synchronous. */
+SE_GPU_API se_gpu_status se_gpu_map_download_multires(const se_gpu_map* map, int64_t capacity,
+                                           uint64_t* keys, int32_t* coords, float* tsdf,
+                                           float* weight, float* past_tsdf, float* past_weight,
+                                           int32_t* scales, int64_t* count);
+/* Block upload (checkpoint restore, test set-up, single-res maps only): allocates the blocks with the given keys
  * (Morton code << 5 | 3, as written by se_gpu_map_download_blocks) if they are not allocated,
  * then overwrites their 512 voxels from tsdf / weight (host, 512 floats per block; weights are
  * rounded to integers). Synchronous. */

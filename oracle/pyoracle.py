@@ -50,6 +50,9 @@ def lib():
             "so_set_num_threads": (None, [C.c_int]),
             "so_get_num_threads": (C.c_int, []),
             "so_map_create": (vp, [f32p, C.c_float, C.c_float, C.c_float, vp]),
+            "so_map_create_multires": (vp, [f32p, C.c_float, C.c_float, C.c_float, vp]),
+            "so_map_is_multires": (C.c_int, [vp]),
+            "so_map_mr_blocks": (None, [vp, vp, vp, vp, vp, vp, vp, vp]),
             "so_map_destroy": (None, [vp]),
             "so_map_size": (C.c_int, [vp]),
             "so_map_dim": (C.c_float, [vp]),
@@ -117,15 +120,18 @@ def _m16(T):
 
 
 class OracleMap:
-    """se::TSDFMap<Res::Single> restated on the CPU."""
+    """se::TSDFMap<Res::Single> (or, with multires=True, se::TSDFMap<Res::Multi>) restated on
+    the CPU."""
 
-    def __init__(self, dim, res, truncation_boundary_factor=8.0, max_weight=100.0, T_MW=None):
+    def __init__(self, dim, res, truncation_boundary_factor=8.0, max_weight=100.0, T_MW=None,
+                 multires=False):
         d = np.ascontiguousarray(np.broadcast_to(np.asarray(dim, np.float32), (3,)))
         self._tmw = None if T_MW is None else _m16(T_MW)
-        self.h = lib().so_map_create(d, float(res), float(truncation_boundary_factor),
-                                     float(max_weight),
-                                     None if self._tmw is None else self._tmw.ctypes.data)
+        create = lib().so_map_create_multires if multires else lib().so_map_create
+        self.h = create(d, float(res), float(truncation_boundary_factor), float(max_weight),
+                        None if self._tmw is None else self._tmw.ctypes.data)
         self.res = float(res)
+        self.multires = bool(multires)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -171,6 +177,19 @@ class OracleMap:
             lib().so_map_blocks(self.h, keys.ctypes.data, coords.ctypes.data, tsdf.ctypes.data,
                                 weight.ctypes.data, ts.ctypes.data)
         return keys, coords, tsdf, weight, ts
+
+    def mr_blocks(self):
+        """Multi-res blocks: (keys u64[N], coords i32[N,3], tsdf f32[N,585], weight f32[N,585],
+        past_tsdf f32[N,585], past_weight f32[N,585], scales i32[N,2] = (current, min))."""
+        n = self.num_blocks()
+        keys = np.zeros(n, np.uint64)
+        coords = np.zeros((n, 3), np.int32)
+        arrs = [np.zeros((n, 585), np.float32) for _ in range(4)]
+        scales = np.zeros((n, 2), np.int32)
+        if n:
+            lib().so_map_mr_blocks(self.h, keys.ctypes.data, coords.ctypes.data,
+                                   *[a.ctypes.data for a in arrs], scales.ctypes.data)
+        return (keys, coords, *arrs, scales)
 
     def aabb(self):
         mn = np.zeros(3, np.int32)

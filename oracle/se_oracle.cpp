@@ -223,10 +223,26 @@ struct BlockData {
     float weight[kBlockVoxels];
 };
 
+/* BlockMultiRes<Data<TSDF>> (block.hpp:66-166, block_impl.hpp:80-202): the 8^3 + 4^3 + 2^3 + 1
+ * voxel pyramid of data and of past data (delta down-propagation), the current integration
+ * scale and the finest scale ever integrated (-1 before the first update). */
+constexpr int kMrVoxels = 585;
+constexpr int kMrScaleOffset[4] = {0, 512, 576, 584};
+struct MRBlock {
+    float tsdf[kMrVoxels];
+    float weight[kMrVoxels];
+    float past_tsdf[kMrVoxels];
+    float past_weight[kMrVoxels];
+    int current_scale;
+    int min_scale;
+};
+
 struct Octree {
     int size = 0;
     std::vector<Octant> octants; /* octants[0] is the root */
     std::vector<BlockData> blocks;
+    bool multires = false;
+    std::vector<MRBlock> mr; /* multi-res blocks (Octant::block indexes this when multires) */
     std::vector<int32_t> block_octant;
     bool aabb_empty = true;
     int32_t aabb_min[3] = {0, 0, 0};
@@ -237,6 +253,7 @@ struct Octree {
         size = sz;
         octants.clear();
         blocks.clear();
+        mr.clear();
         block_octant.clear();
         Octant root{};
         std::fill(root.child, root.child + 8, -1);
@@ -278,7 +295,18 @@ struct Octree {
         o.size = csize;
         o.timestamp = -1;
         o.block = -1;
-        if (psize == 2 * kBlockSize) {
+        if (psize == 2 * kBlockSize && multires) {
+            o.block = (int32_t) mr.size();
+            mr.emplace_back();
+            MRBlock& b = mr.back();
+            std::fill(b.tsdf, b.tsdf + kMrVoxels, 1.0f);
+            std::fill(b.weight, b.weight + kMrVoxels, 0.0f);
+            std::fill(b.past_tsdf, b.past_tsdf + kMrVoxels, 1.0f);
+            std::fill(b.past_weight, b.past_weight + kMrVoxels, 0.0f);
+            b.current_scale = -1;
+            b.min_scale = -1;
+        }
+        else if (psize == 2 * kBlockSize) {
             o.block = (int32_t) blocks.size();
             blocks.emplace_back();
             BlockData& b = blocks.back();
@@ -656,6 +684,233 @@ static inline void map_get_data(const so_map& m, V3 p_W, float& tsdf, float& wei
     get_voxel(m, c, tsdf, weight);
 }
 
+/* ---------------------------------------------------------- multi-res TSDF access -- */
+
+/* BlockMultiRes::getVoxelIdx, block_impl.hpp:80-91 */
+static inline int mr_index(const Octant& oc, const int32_t c[3], int scale)
+{
+    const int n = kBlockSize >> scale;
+    return kMrScaleOffset[scale] + ((c[0] - oc.coord[0]) >> scale) + n * ((c[1] - oc.coord[1]) >> scale)
+        + n * n * ((c[2] - oc.coord[2]) >> scale);
+}
+
+/* The current scale of a block as a data index. A block is updated in the frame that allocates
+ * it, so -1 (never integrated) is only seen by queries between allocation and update, for
+ * which the reference's index is undefined; scale 0 is used. */
+static inline int mr_cur(const MRBlock& b) { return b.current_scale < 0 ? 0 : b.current_scale; }
+
+static inline V3 fracf(V3 v) { return v3(v.x - std::floor(v.x), v.y - std::floor(v.y), v.z - std::floor(v.z)); }
+
+/* visitor::getData multi-res: the block's data at its current scale (visitor_impl.hpp:704-717,
+ * block_impl.hpp:117-133). */
+static inline bool mr_get_voxel(const so_map& m, const int32_t c[3], float& tsdf, float& weight)
+{
+    const int o = m.octree.block_at(c);
+    if (o < 0) {
+        tsdf = 1.0f;
+        weight = 0.0f;
+        return false;
+    }
+    const Octant& oc = m.octree.octants[o];
+    const MRBlock& b = m.octree.mr[oc.block];
+    const int i = mr_index(oc, c, mr_cur(b));
+    tsdf = b.tsdf[i];
+    weight = b.weight[i];
+    return true;
+}
+
+/* visitor::getData(octree, block_ptr, coord, scale_desired, scale_returned) multi-res
+ * (visitor_impl.hpp:740-790): data at max(scale_desired, current_scale) of the block holding
+ * the voxel (the hint block first); returns false when no block holds it. */
+static inline bool mr_get_voxel_at(const so_map& m, int hint_octant, const int32_t c[3], int scale_desired,
+                                   float& tsdf, float& weight, int& scale_returned)
+{
+    int o = hint_octant;
+    const Octant* oc = &m.octree.octants[o];
+    if (!(c[0] >= oc->coord[0] && c[0] <= oc->coord[0] + 7 && c[1] >= oc->coord[1] && c[1] <= oc->coord[1] + 7
+          && c[2] >= oc->coord[2] && c[2] <= oc->coord[2] + 7)) {
+        o = m.octree.block_at(c);
+        if (o < 0) {
+            tsdf = 1.0f;
+            weight = 0.0f;
+            return false;
+        }
+        oc = &m.octree.octants[o];
+    }
+    const MRBlock& b = m.octree.mr[oc->block];
+    scale_returned = std::max(scale_desired, b.current_scale);
+    const int i = mr_index(*oc, c, scale_returned < 0 ? 0 : scale_returned);
+    tsdf = b.tsdf[i];
+    weight = b.weight[i];
+    return true;
+}
+
+/* visitor::getInterp multi-res (visitor_impl.hpp:906-972) with detail::get_neighbours
+ * (:398-697). Starting at max(current scale of the query's block, desired scale), a scale is
+ * skipped when one of the up to 8 blocks its neighbourhood touches is unallocated or integrates
+ * at a coarser scale; an invalid neighbour ends the query. */
+static bool mr_interp_voxel(const so_map& m, V3 vf, int desired_scale, float& out, int* returned_scale)
+{
+    const Octree& o = m.octree;
+    const int32_t c0[3] = {(int) vf.x, (int) vf.y, (int) vf.z};
+    const int oq = o.block_at(c0);
+    if (oq < 0)
+        return false;
+    const int init = std::max(o.mr[o.octants[oq].block].current_scale, desired_scale);
+    for (int scale = init; scale <= kMaxBlockScale; ++scale) {
+        const int stride = 1 << scale;
+        const float inv = 1.0f / (float) stride;
+        const V3 bf = v3(inv * vf.x - 0.5f, inv * vf.y - 0.5f, inv * vf.z - 0.5f);
+        const int32_t base[3] = {stride * (int) bf.x, stride * (int) bf.y, stride * (int) bf.z};
+        if (o.aabb_empty)
+            return false;
+        for (int i = 0; i < 3; ++i)
+            if (base[i] < o.aabb_min[i] || base[i] > o.aabb_max[i])
+                return false;
+        bool ok = true;
+        for (int i = 0; i < 3; ++i)
+            if (base[i] + stride >= o.size || base[i] < 0)
+                ok = false;
+        float f[8], w[8];
+        for (int n = 0; ok && n < 8; ++n) {
+            const int32_t c[3] = {base[0] + stride * (n & 1), base[1] + stride * ((n >> 1) & 1),
+                                  base[2] + stride * ((n >> 2) & 1)};
+            const int ob = o.block_at(c);
+            if (ob < 0) {
+                ok = false;
+                break;
+            }
+            const Octant& oc = o.octants[ob];
+            const MRBlock& b = o.mr[oc.block];
+            if (b.current_scale > scale) {
+                ok = false;
+                break;
+            }
+            const int i = mr_index(oc, c, scale);
+            f[n] = b.tsdf[i];
+            w[n] = b.weight[i];
+        }
+        if (!ok)
+            continue;
+        for (int n = 0; n < 8; ++n)
+            if (!(w[n] != 0.0f))
+                return false;
+        if (returned_scale)
+            *returned_scale = scale;
+        const V3 t = fracf(bf);
+        const V3 tc = v3(1.0f - t.x, 1.0f - t.y, 1.0f - t.z);
+        out = ((f[0] * tc.x + f[1] * t.x) * tc.y + (f[2] * tc.x + f[3] * t.x) * t.y) * tc.z
+            + ((f[4] * tc.x + f[5] * t.x) * tc.y + (f[6] * tc.x + f[7] * t.x) * t.y) * t.z;
+        return true;
+    }
+    return false;
+}
+
+/* visitor::getFieldGrad multi-res (visitor_impl.hpp:1257-1497), desired scale 0: the 32-sample
+ * central-difference gradient at the first scale (from the block's current one up) whose 32
+ * samples are all valid and stored at exactly that scale. */
+static bool mr_grad_voxel(const so_map& m, V3 vf, V3& g, int& scale_returned)
+{
+    const Octree& o = m.octree;
+    const int32_t c0[3] = {(int) vf.x, (int) vf.y, (int) vf.z};
+    const int oq = o.block_at(c0);
+    if (oq < 0)
+        return false;
+    const int init = std::max(0, o.mr[o.octants[oq].block].current_scale);
+    const int top = o.size - 1;
+    for (int scale = init; scale <= kMaxBlockScale; ++scale) {
+        scale_returned = scale;
+        const int stride = 1 << scale;
+        const float inv = 1.0f / (float) stride;
+        const V3 sv = v3(inv * vf.x - 0.5f, inv * vf.y - 0.5f, inv * vf.z - 0.5f);
+        const V3 fac = fracf(sv);
+        const int32_t base[3] = {stride * (int) sv.x, stride * (int) sv.y, stride * (int) sv.z};
+        int32_t ll[3], lu[3], ul[3], uu[3];
+        for (int i = 0; i < 3; ++i) {
+            ll[i] = std::max(base[i] - stride, 0);
+            lu[i] = std::max(base[i], 0);
+            ul[i] = std::min(base[i] + stride, top);
+            uu[i] = std::min(base[i] + 2 * stride, top);
+        }
+        /* finest_octant(base, scale): a TSDF node holds no data, so only a block continues */
+        const int hint = o.block_at(base);
+        if (hint < 0)
+            continue;
+        const int32_t* X[32] = {ll, ll, ll, ll, lu, lu, lu, lu, lu, lu, lu, lu, lu, lu, lu, lu,
+                                ul, ul, ul, ul, ul, ul, ul, ul, ul, ul, ul, ul, uu, uu, uu, uu};
+        const int32_t* Y[32] = {lu, ul, lu, ul, ll, ll, lu, lu, lu, lu, ul, ul, ul, ul, uu, uu,
+                                ll, ll, lu, lu, lu, lu, ul, ul, ul, ul, uu, uu, lu, ul, lu, ul};
+        const int32_t* Z[32] = {lu, lu, ul, ul, lu, ul, ll, lu, ul, uu, ll, lu, ul, uu, lu, ul,
+                                lu, ul, ll, lu, ul, uu, ll, lu, ul, uu, lu, ul, lu, lu, ul, ul};
+        float v[32];
+        bool ok = true;
+        for (int i = 0; i < 32 && ok; ++i) {
+            const int32_t c[3] = {X[i][0], Y[i][1], Z[i][2]};
+            float t, w;
+            int rs = -1;
+            if (!mr_get_voxel_at(m, hint, c, scale, t, w, rs) || !(w != 0.0f) || rs != scale)
+                ok = false;
+            v[i] = t;
+        }
+        if (!ok)
+            continue;
+        const float rx = 1.0f - fac.x, ry = 1.0f - fac.y, rz = 1.0f - fac.z;
+        const float gx = (((v[19] - v[0]) * rx + (v[28] - v[7]) * fac.x) * ry
+                          + ((v[23] - v[1]) * rx + (v[29] - v[11]) * fac.x) * fac.y)
+                * rz
+            + (((v[20] - v[2]) * rx + (v[30] - v[8]) * fac.x) * ry
+               + ((v[24] - v[3]) * rx + (v[31] - v[12]) * fac.x) * fac.y)
+                * fac.z;
+        const float gy = (((v[11] - v[4]) * rx + (v[23] - v[16]) * fac.x) * ry
+                          + ((v[14] - v[7]) * rx + (v[26] - v[19]) * fac.x) * fac.y)
+                * rz
+            + (((v[12] - v[5]) * rx + (v[24] - v[17]) * fac.x) * ry
+               + ((v[15] - v[8]) * rx + (v[27] - v[20]) * fac.x) * fac.y)
+                * fac.z;
+        const float gz = (((v[8] - v[6]) * rx + (v[20] - v[18]) * fac.x) * ry
+                          + ((v[12] - v[10]) * rx + (v[24] - v[22]) * fac.x) * fac.y)
+                * rz
+            + (((v[9] - v[7]) * rx + (v[21] - v[19]) * fac.x) * ry
+               + ((v[13] - v[11]) * rx + (v[25] - v[23]) * fac.x) * fac.y)
+                * fac.z;
+        const float sf = (float) stride;
+        g = v3((0.5f * gx) / sf, (0.5f * gy) / sf, (0.5f * gz) / sf);
+        return true;
+    }
+    return false;
+}
+
+static bool map_field_interp_mr(const so_map& m, V3 p_W, float& out, int* returned_scale)
+{
+    V3 vf;
+    if (!m.point_to_voxel_f(p_W, vf))
+        return false;
+    return mr_interp_voxel(m, vf, 0, out, returned_scale);
+}
+
+static bool map_field_grad_mr(const so_map& m, V3 p_W, V3& g)
+{
+    V3 vf;
+    if (!m.point_to_voxel_f(p_W, vf))
+        return false;
+    int sr;
+    if (!mr_grad_voxel(m, vf, g, sr))
+        return false;
+    g = g / m.res;
+    return true;
+}
+
+static inline void map_get_data_mr(const so_map& m, V3 p_W, float& tsdf, float& weight)
+{
+    int32_t c[3];
+    if (!m.point_to_voxel(p_W, c)) {
+        tsdf = 1.0f;
+        weight = 0.0f;
+        return;
+    }
+    mr_get_voxel(m, c, tsdf, weight);
+}
+
 /* ------------------------------------------------------- VoxelBlockRayIterator (ESVO) -- */
 /* voxel_block_ray_iterator_impl.hpp:19-249: Laine & Karras sparse-voxel-octree traversal in the
  * [1, 2]^3 scaled frame, mirrored so that every direction component is negative. Returns the
@@ -809,8 +1064,10 @@ static RayBlockHit first_block_on_ray(const so_map& m, V3 origin_W, V3 dir_W, fl
 
 /* raycast<TSDF>, raycaster_impl.hpp:456-533. Returns true on a hit with point_W and scale. */
 static bool raycast_tsdf(const so_map& m, V3 origin_W, V3 dir_W, float t_near, float t_far,
-                         V3& hit_W)
+                         V3& hit_W, int& scale_out)
 {
+    const bool mres = m.octree.multires;
+    int scale_tt = 0;
     const RayBlockHit rb = first_block_on_ray(m, origin_W, dir_W, t_near, t_far);
     const float step = m.res;
     const float largestep = (float) kBlockSize * step;
@@ -825,13 +1082,19 @@ static bool raycast_tsdf(const so_map& m, V3 origin_W, V3 dir_W, float t_near, f
     float stepsize = largestep;
     V3 p = origin_W + dir_W * t;
     float f_t, w_t;
-    map_get_data(m, p, f_t, w_t);
+    if (mres)
+        map_get_data_mr(m, p, f_t, w_t);
+    else
+        map_get_data(m, p, f_t, w_t);
     float f_tt = 0.0f;
     if (!(f_t >= 0.0f))
         return false;
     for (; t < t_far; t += stepsize) {
         float f, w;
-        map_get_data(m, p, f, w);
+        if (mres)
+            map_get_data_mr(m, p, f, w);
+        else
+            map_get_data(m, p, f, w);
         if (!(w != 0.0f)) {
             stepsize = largestep;
             p = p + stepsize * dir_W;
@@ -841,7 +1104,7 @@ static bool raycast_tsdf(const so_map& m, V3 origin_W, V3 dir_W, float t_near, f
         /* the reference compares against the double literal 0.1 */
         if ((double) f_tt <= 0.1 && f_tt >= -0.5f) {
             float fi;
-            if (map_field_interp(m, p, fi))
+            if (mres ? map_field_interp_mr(m, p, fi, &scale_tt) : map_field_interp(m, p, fi))
                 f_tt = fi;
         }
         if (f_tt < 0.0f)
@@ -853,6 +1116,7 @@ static bool raycast_tsdf(const so_map& m, V3 origin_W, V3 dir_W, float t_near, f
     if (f_tt < 0.0f) {
         t = t - stepsize * (f_tt - 0.0f) / (f_tt - f_t);
         hit_W = origin_W + dir_W * t;
+        scale_out = scale_tt;
         return true;
     }
     return false;
@@ -1039,6 +1303,204 @@ static void points_to_normals(const V3* pts, int w, int h, bool neg_y, V3* nrm)
 enum { kSuccess = 1, kInvalidInputNormal = -1, kProjOutside = -2, kInvalidRefNormal = -3,
        kDistThreshold = -4, kNormalThreshold = -5 };
 
+/* --------------------------------------------------------- multi-res TSDF updater -- */
+
+/* PinholeCamera::computeIntegrationScaleImpl, pinhole_camera.cpp:115-152, with the default
+ * pixel_voxel_ratio_per_scale {1.5, 3, 6} (sensor.hpp:56) and scaled_pixel = 1/fx. */
+static int integration_scale(const Pinhole& s, V3 c_S, float res, int last_scale, int min_scale, int max_scale)
+{
+    static const float kRatio[3] = {1.5f, 3.0f, 6.0f};
+    const float dist = c_S.z;
+    const float pixel_dim = dist * s.inv_fx;
+    const float pv_ratio = pixel_dim / res;
+    int scale = 0;
+    for (float r : kRatio) {
+        if (pv_ratio < r)
+            break;
+        scale++;
+    }
+    scale = std::min(scale, max_scale);
+    if (scale > last_scale && min_scale != -1) {
+        c_S.z -= 0.25f;
+        return integration_scale(s, c_S, res, last_scale, -1, max_scale);
+    }
+    if (scale < last_scale && min_scale != -1) {
+        c_S.z += 0.25f;
+        return integration_scale(s, c_S, res, last_scale, -1, max_scale);
+    }
+    return scale;
+}
+
+/* propagator::propagateBlockDown (propagator_impl.hpp:71-117) by one scale, with the multi-res
+ * TSDF updater's child / parent functions (multires_tsdf_updater_impl.hpp:70-146): observed
+ * children take the parent's change since its last down-propagation, unobserved children are
+ * initialised by interpolation at their scale. */
+static void mr_propagate_down(const so_map& m, const Octant& oc, MRBlock& b, int parent_scale)
+{
+    const int ps = parent_scale, cs = ps - 1;
+    const int pstride = 1 << ps, cstride = pstride >> 1;
+    for (int z = 0; z < kBlockSize; z += pstride) {
+        for (int y = 0; y < kBlockSize; y += pstride) {
+            for (int x = 0; x < kBlockSize; x += pstride) {
+                const int32_t pc[3] = {oc.coord[0] + x, oc.coord[1] + y, oc.coord[2] + z};
+                const int pi = mr_index(oc, pc, ps);
+                for (int k = 0; k < pstride; k += cstride) {
+                    for (int j = 0; j < pstride; j += cstride) {
+                        for (int i = 0; i < pstride; i += cstride) {
+                            const int32_t cc[3] = {pc[0] + i, pc[1] + j, pc[2] + k};
+                            const int ci = mr_index(oc, cc, cs);
+                            if (b.weight[ci] != 0.0f) {
+                                const float delta = b.tsdf[pi] - b.past_tsdf[pi];
+                                b.tsdf[ci] = std::max(b.tsdf[ci] + delta, -1.0f);
+                                b.weight[ci] = fminf(b.weight[ci] + b.past_weight[pi], m.max_weight);
+                                b.past_weight[ci] = b.past_weight[pi];
+                            }
+                            else {
+                                const float half = 0.5f * (float) cstride;
+                                const V3 cf = v3((float) cc[0] + half, (float) cc[1] + half, (float) cc[2] + half);
+                                float iv;
+                                if (mr_interp_voxel(m, cf, cs, iv, nullptr)) {
+                                    b.tsdf[ci] = iv;
+                                    b.weight[ci] = b.weight[pi];
+                                    b.past_tsdf[ci] = iv;
+                                    b.past_weight[ci] = 0.0f;
+                                }
+                            }
+                        }
+                    }
+                }
+                b.past_tsdf[pi] = b.tsdf[pi];
+                b.past_weight[pi] = 0.0f;
+            }
+        }
+    }
+}
+
+/* propagator::propagateBlockUp (propagator_impl.hpp:17-67) with data::up_prop_mean
+ * (data_impl.hpp:13-50) and the updater's aggregate function (multires_tsdf_updater_impl.hpp:
+ * 234-246). */
+static void mr_propagate_up(const Octant& oc, MRBlock& b, int init_scale)
+{
+    for (int cs = init_scale; cs < kMaxBlockScale; ++cs) {
+        const int cstride = 1 << cs, pstride = cstride << 1;
+        for (int z = 0; z < kBlockSize; z += pstride) {
+            for (int y = 0; y < kBlockSize; y += pstride) {
+                for (int x = 0; x < kBlockSize; x += pstride) {
+                    const int32_t pc[3] = {oc.coord[0] + x, oc.coord[1] + y, oc.coord[2] + z};
+                    float tsdf_sum = 0.0f, weight_sum = 0.0f;
+                    int n_valid = 0;
+                    for (int k = 0; k < pstride; k += cstride) {
+                        for (int j = 0; j < pstride; j += cstride) {
+                            for (int i = 0; i < pstride; i += cstride) {
+                                const int32_t cc[3] = {pc[0] + i, pc[1] + j, pc[2] + k};
+                                const int ci = mr_index(oc, cc, cs);
+                                if (b.weight[ci] != 0.0f) {
+                                    ++n_valid;
+                                    tsdf_sum += b.tsdf[ci];
+                                    weight_sum += b.weight[ci];
+                                }
+                            }
+                        }
+                    }
+                    const int pi = mr_index(oc, pc, cs + 1);
+                    if (n_valid > 0) {
+                        b.tsdf[pi] = tsdf_sum / (float) n_valid;
+                        b.weight[pi] = std::ceil(weight_sum / (float) n_valid);
+                        b.past_tsdf[pi] = b.tsdf[pi];
+                        b.past_weight[pi] = 0.0f;
+                    }
+                    else {
+                        b.past_tsdf[pi] = 1.0f;
+                        b.past_weight[pi] = 0.0f;
+                    }
+                }
+            }
+        }
+    }
+}
+
+/* Multi-res TSDF Updater, multires_tsdf_updater_impl.hpp:14-250.
+ *
+ * The reference runs the per-block body in one OpenMP loop, so a block's down-propagation
+ * (which interpolates across neighbouring blocks) reads neighbours that other threads may be
+ * updating at the same time. This restatement fixes one schedule of that loop: every block's
+ * scale selection and down-propagation first (reading the map as it was before the update),
+ * then every block's voxel update and up-propagation. A block's down-propagation writes only
+ * scales finer than its previous scale, and the interpolation reads each block only at its
+ * previous scale or coarser, so the first phase is free of races. */
+static long long mr_update(so_map& m, const Pinhole& s, const Tf& T_WS, const float* depth,
+                           const std::vector<int>& list, int timestamp)
+{
+    Octree& oct = m.octree;
+    const float trunc = m.res * m.trunc_factor;
+    const Tf T_CW = inverse_iso(T_WS);
+    Tf T_CV = compose(T_CW, m.T_WM);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            T_CV.R[i][j] = T_CV.R[i][j] * m.res;
+    for (int i = 0; i < 3; ++i)
+        T_CV.t[i] = ((T_CV.R[i][0] * 0.5f + T_CV.R[i][1] * 0.5f) + T_CV.R[i][2] * 0.5f) + T_CV.t[i];
+    const long long n = (long long) list.size();
+    std::vector<int> new_scale((size_t) n);
+#pragma omp parallel for
+    for (long long i = 0; i < n; i++) {
+        const Octant& oc = oct.octants[list[i]];
+        MRBlock& b = oct.mr[oc.block];
+        const V3 centre_C = apply(T_CW, m.voxel_to_point(oc.coord, kBlockSize));
+        const int last = b.current_scale;
+        const int curr = std::max(integration_scale(s, centre_C, m.res, last, b.min_scale, kMaxBlockScale), last - 1);
+        b.min_scale = b.min_scale < 0 ? curr : std::min(b.min_scale, curr);
+        new_scale[(size_t) i] = curr;
+        if (curr < last)
+            mr_propagate_down(m, oc, b, last);
+    }
+    long long n_upd = 0;
+#pragma omp parallel for reduction(+ : n_upd)
+    for (long long i = 0; i < n; i++) {
+        Octant& oc = oct.octants[list[i]];
+        MRBlock& b = oct.mr[oc.block];
+        oc.timestamp = timestamp;
+        const int curr = new_scale[(size_t) i];
+        b.current_scale = curr;
+        const int stride = 1 << curr;
+        for (int x = 0; x < kBlockSize; x += stride) {
+            for (int y = 0; y < kBlockSize; y += stride) {
+                for (int z = 0; z < kBlockSize; z += stride) {
+                    const int32_t c[3] = {oc.coord[0] + x, oc.coord[1] + y, oc.coord[2] + z};
+                    const V3 vc = v3((float) c[0], (float) c[1], (float) c[2]);
+                    const V3 p_C = apply(T_CV, vc);
+                    const float pn = norm(p_C);
+                    if (pn > far_dist(s, p_C))
+                        continue;
+                    float u, v;
+                    if (!project(s, p_C, u, v))
+                        continue;
+                    int px, py;
+                    round_pixel(u, v, px, py);
+                    const float dv = depth[px + py * s.w];
+                    if (dv < s.near_plane)
+                        continue;
+                    const float mz = p_C.z;
+                    const float sdf = (dv - mz) / mz * pn;
+                    const int idx = mr_index(oc, c, curr);
+                    if (!(sdf < -trunc)) {
+                        const float upd = std::min(sdf / trunc, 1.0f);
+                        float w = b.weight[idx];
+                        if (w < m.max_weight)
+                            w = w + 1.0f;
+                        b.tsdf[idx] = (b.tsdf[idx] * (w - 1.0f) + upd) / w;
+                        b.weight[idx] = w;
+                        ++n_upd;
+                    }
+                    b.past_weight[idx] = b.past_weight[idx] + 1.0f;
+                }
+            }
+        }
+        mr_propagate_up(oc, b, curr);
+    }
+    return n_upd;
+}
+
 struct IcpRow {
     int result;
     float error;
@@ -1096,6 +1558,45 @@ so_map* so_map_create(const float dim[3], float res, float truncation_boundary_f
     m->trunc_factor = truncation_boundary_factor;
     m->max_weight = max_weight;
     return m;
+}
+
+so_map* so_map_create_multires(const float dim[3], float res, float truncation_boundary_factor,
+                               float max_weight, const float* T_MW)
+{
+    so_map* m = so_map_create(dim, res, truncation_boundary_factor, max_weight, T_MW);
+    m->octree.multires = true;
+    return m;
+}
+
+int so_map_is_multires(const so_map* map) { return map->octree.multires ? 1 : 0; }
+
+void so_map_mr_blocks(const so_map* map, uint64_t* keys, int32_t* coords, float* tsdf, float* weight,
+                      float* past_tsdf, float* past_weight, int32_t* scales)
+{
+    const Octree& o = map->octree;
+    if (!o.multires)
+        return;
+    for (size_t i = 0; i < o.block_octant.size(); ++i) {
+        const Octant& oc = o.octants[o.block_octant[i]];
+        const MRBlock& b = o.mr[oc.block];
+        if (keys)
+            keys[i] = encode_key(oc.coord[0], oc.coord[1], oc.coord[2], kMaxBlockScale);
+        if (coords)
+            for (int k = 0; k < 3; ++k)
+                coords[3 * i + k] = oc.coord[k];
+        if (tsdf)
+            std::memcpy(tsdf + i * kMrVoxels, b.tsdf, sizeof(b.tsdf));
+        if (weight)
+            std::memcpy(weight + i * kMrVoxels, b.weight, sizeof(b.weight));
+        if (past_tsdf)
+            std::memcpy(past_tsdf + i * kMrVoxels, b.past_tsdf, sizeof(b.past_tsdf));
+        if (past_weight)
+            std::memcpy(past_weight + i * kMrVoxels, b.past_weight, sizeof(b.past_weight));
+        if (scales) {
+            scales[2 * i] = b.current_scale;
+            scales[2 * i + 1] = b.min_scale;
+        }
+    }
 }
 
 void so_map_destroy(so_map* map) { delete map; }
@@ -1183,6 +1684,17 @@ void so_integrate_depth(so_map* map, const float* depth, const so_pinhole* senso
     const long long n_new = (long long) list.size();
     list.insert(list.end(), frustum_blocks.begin(), frustum_blocks.end());
 
+    if (oct.multires) {
+        const long long n_upd = mr_update(m, s, T_WS, depth, list, timestamp);
+        if (stats) {
+            stats->n_valid_pixels = n_valid;
+            stats->n_new_blocks = n_new;
+            stats->n_frustum_blocks = (long long) frustum_blocks.size();
+            stats->n_updated_voxels = n_upd;
+        }
+        return;
+    }
+
     /* single-res TSDF Updater, singleres_tsdf_updater_impl.hpp:14-132 */
     const float trunc = m.res * m.trunc_factor;
     const Tf T_CW = inverse_iso(T_WS);
@@ -1255,13 +1767,14 @@ void so_raycast_volume(const so_map* map, const so_pinhole* sensor_c, const floa
             const V3 ray_S = back_project(s, (float) x, (float) y);
             const V3 dir_W = rot(T_WS, normalized(ray_S));
             V3 hit;
-            if (raycast_tsdf(m, origin, dir_W, near_dist(s, ray_S), far_dist(s, ray_S), hit)) {
-                scale[idx] = 0;
+            int hit_scale = 0;
+            if (raycast_tsdf(m, origin, dir_W, near_dist(s, ray_S), far_dist(s, ray_S), hit, hit_scale)) {
+                scale[idx] = (int8_t) hit_scale;
                 pts_W[3 * idx + 0] = hit.x;
                 pts_W[3 * idx + 1] = hit.y;
                 pts_W[3 * idx + 2] = hit.z;
                 V3 g;
-                if (map_field_grad(m, hit, g)) {
+                if (m.octree.multires ? map_field_grad_mr(m, hit, g) : map_field_grad(m, hit, g)) {
                     const V3 n = normalized(g);
                     nrm_W[3 * idx + 0] = n.x;
                     nrm_W[3 * idx + 1] = n.y;
@@ -1469,13 +1982,13 @@ int so_track(const so_pinhole* sensor_c, const so_tracker_config* cfg, const flo
     return accepted;
 }
 
-long long so_map_num_blocks(const so_map* map) { return (long long) map->octree.blocks.size(); }
+long long so_map_num_blocks(const so_map* map) { return (long long) map->octree.block_octant.size(); }
 
 void so_map_blocks(const so_map* map, uint64_t* keys, int32_t* coords, float* tsdf,
                    float* weight, int32_t* timestamps)
 {
     const Octree& oct = map->octree;
-    for (size_t i = 0; i < oct.blocks.size(); ++i) {
+    for (size_t i = 0; i < oct.block_octant.size(); ++i) {
         const Octant& oc = oct.octants[oct.block_octant[i]];
         if (keys)
             keys[i] = encode_key(oc.coord[0], oc.coord[1], oc.coord[2], kMaxBlockScale);
@@ -1484,10 +1997,13 @@ void so_map_blocks(const so_map* map, uint64_t* keys, int32_t* coords, float* ts
             coords[3 * i + 1] = oc.coord[1];
             coords[3 * i + 2] = oc.coord[2];
         }
+        /* multi-res maps report their finest (scale 0) level here */
+        const float* bt = oct.multires ? oct.mr[oc.block].tsdf : oct.blocks[oc.block].tsdf;
+        const float* bw = oct.multires ? oct.mr[oc.block].weight : oct.blocks[oc.block].weight;
         if (tsdf)
-            std::memcpy(tsdf + i * kBlockVoxels, oct.blocks[oc.block].tsdf, sizeof(float) * kBlockVoxels);
+            std::memcpy(tsdf + i * kBlockVoxels, bt, sizeof(float) * kBlockVoxels);
         if (weight)
-            std::memcpy(weight + i * kBlockVoxels, oct.blocks[oc.block].weight, sizeof(float) * kBlockVoxels);
+            std::memcpy(weight + i * kBlockVoxels, bw, sizeof(float) * kBlockVoxels);
         if (timestamps)
             timestamps[i] = oc.timestamp;
     }
@@ -1507,6 +2023,8 @@ int so_map_aabb(const so_map* map, int32_t mn[3], int32_t mx[3])
 
 void so_map_set_block(so_map* map, const int32_t c[3], const float* tsdf512, const float* weight512)
 {
+    if (map->octree.multires)
+        return;
     int o;
     map->octree.allocate_key(encode_key(c[0], c[1], c[2], 0), o);
     BlockData& b = map->octree.blocks[map->octree.octants[o].block];
@@ -1519,7 +2037,10 @@ void so_map_set_block(so_map* map, const int32_t c[3], const float* tsdf512, con
 int so_map_get_data(const so_map* map, const float p[3], float* tsdf, float* weight)
 {
     float t, w;
-    map_get_data(*map, v3(p[0], p[1], p[2]), t, w);
+    if (map->octree.multires)
+        map_get_data_mr(*map, v3(p[0], p[1], p[2]), t, w);
+    else
+        map_get_data(*map, v3(p[0], p[1], p[2]), t, w);
     *tsdf = t;
     *weight = w;
     return w != 0.0f;
@@ -1528,7 +2049,8 @@ int so_map_get_data(const so_map* map, const float p[3], float* tsdf, float* wei
 int so_map_get_field_interp(const so_map* map, const float p[3], float* value)
 {
     float v;
-    if (!map_field_interp(*map, v3(p[0], p[1], p[2]), v))
+    const V3 q = v3(p[0], p[1], p[2]);
+    if (!(map->octree.multires ? map_field_interp_mr(*map, q, v, nullptr) : map_field_interp(*map, q, v)))
         return 0;
     *value = v;
     return 1;
@@ -1537,7 +2059,8 @@ int so_map_get_field_interp(const so_map* map, const float p[3], float* value)
 int so_map_get_field_grad(const so_map* map, const float p[3], float grad[3])
 {
     V3 g;
-    if (!map_field_grad(*map, v3(p[0], p[1], p[2]), g))
+    const V3 q = v3(p[0], p[1], p[2]);
+    if (!(map->octree.multires ? map_field_grad_mr(*map, q, g) : map_field_grad(*map, q, g)))
         return 0;
     grad[0] = g.x;
     grad[1] = g.y;

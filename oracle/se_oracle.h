@@ -17,9 +17,15 @@
  *                                  include/se/map/octree/impl/iterator_impl.hpp:88-160
  *   - single-res TSDF update       include/se/integrator/updater/impl/singleres_tsdf_updater_impl.hpp:14-132,
  *                                  include/se/map/impl/data_field_impl.hpp:39-54
+ *   - multi-res TSDF update        include/se/integrator/updater/impl/multires_tsdf_updater_impl.hpp:14-250,
+ *                                  src/sensor/pinhole_camera.cpp:115-152,
+ *                                  include/se/map/octree/impl/propagator_impl.hpp:17-117,
+ *                                  include/se/map/impl/data_impl.hpp:13-50,
+ *                                  include/se/map/octant/impl/block_impl.hpp:80-202
  *   - raycast_volume (TSDF)        include/se/map/impl/raycaster_impl.hpp:456-627
  *   - VoxelBlockRayIterator        include/se/map/octree/impl/voxel_block_ray_iterator_impl.hpp:19-249
  *   - visitor interp / gradient    include/se/map/octree/impl/visitor_impl.hpp:67-302,704-717,976-1251
+ *                                  (multi-res: :398-697,740-790,906-972,1257-1497)
  *   - Tracker / ICP                include/se/tracker/impl/tracker_impl.hpp:30-116,
  *                                  include/se/tracker/impl/icp_impl.hpp:16-102, src/tracker/icp.cpp:15-246
  *   - preprocessing                src/map/preprocessor.cpp:109-195,
@@ -78,6 +84,10 @@ int so_get_num_threads(void);
 /* Map<Data<TSDF>, Res::Single, 8>. T_MW may be NULL (reference default: translation dim/2). */
 so_map* so_map_create(const float dim[3], float res, float truncation_boundary_factor,
                       float max_weight, const float* T_MW);
+/* Map<Data<TSDF>, Res::Multi, 8> (multires_tsdf_updater_impl.hpp:14-250). */
+so_map* so_map_create_multires(const float dim[3], float res, float truncation_boundary_factor,
+                               float max_weight, const float* T_MW);
+int so_map_is_multires(const so_map* map);
 void so_map_destroy(so_map* map);
 int so_map_size(const so_map* map);
 float so_map_dim(const so_map* map);
@@ -101,6 +111,11 @@ long long so_map_num_blocks(const so_map* map);
  * tsdf / weight: 512 floats per block in x + 8y + 64z order. Any pointer may be NULL. */
 void so_map_blocks(const so_map* map, uint64_t* keys, int32_t* coords, float* tsdf,
                    float* weight, int32_t* timestamps);
+/* Multi-res blocks: 585 values per block (scale 0: 512 in x + 8y + 64z order, scale 1: 64,
+ * scale 2: 8, scale 3: 1) of data and past data; scales: (current_scale, min_scale) per block.
+ * so_map_blocks reports a multi-res map's scale-0 level. */
+void so_map_mr_blocks(const so_map* map, uint64_t* keys, int32_t* coords, float* tsdf, float* weight,
+                      float* past_tsdf, float* past_weight, int32_t* scales);
 /* Allocated-block AABB in voxel coordinates, inclusive; returns 0 when empty. */
 int so_map_aabb(const so_map* map, int32_t mn[3], int32_t mx[3]);
 /* Allocate the block containing voxel_coord (through the normal allocator) and overwrite its

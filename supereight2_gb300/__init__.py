@@ -72,6 +72,8 @@ SIGNATURES = {
     "se_gpu_map_download_blocks": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP,
                                              C.POINTER(C.c_int64)]),
     "se_gpu_map_upload_blocks": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP]),
+    "se_gpu_map_download_multires": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                                               C.POINTER(C.c_int64)]),
     "se_gpu_map_field_interp": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP]),
     "se_gpu_map_field_grad": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP]),
     "se_gpu_map_aabb": (C.c_int, [_VP, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
@@ -184,10 +186,11 @@ class TrackerConfig:
 
 
 class Map:
-    """se::TSDFMap<se::Res::Single> on the GPU: block hash + block pool of 8^3 voxels."""
+    """se::TSDFMap<se::Res::Single> (or, with res="multi", se::TSDFMap<se::Res::Multi>) on the
+    GPU: block hash + block pool of 8^3 voxels (585-entry voxel pyramids for multi-res)."""
 
     def __init__(self, dim, res, truncation_boundary_factor=8.0, max_weight=100.0,
-                 storage="f32", max_blocks=1 << 20, T_MW=None):
+                 storage="f32", max_blocks=1 << 20, T_MW=None, res_type="single"):
         cfg = _MapConfig()
         d = np.broadcast_to(np.asarray(dim, np.float32), (3,))
         cfg.dim = (C.c_float * 3)(*[float(v) for v in d])
@@ -196,7 +199,7 @@ class Map:
             cfg.T_MW = (C.c_float * 16)(*[float(v) for v in np.asarray(T_MW, np.float32).reshape(16)])
             cfg.has_T_MW = 1
         cfg.field = 0
-        cfg.res_type = 0
+        cfg.res_type = {"single": 0, "multi": 1}[res_type]
         cfg.storage = {"f32": 0, "f16": 1}[storage]
         cfg.truncation_boundary_factor = float(truncation_boundary_factor)
         cfg.max_weight = float(max_weight)
@@ -207,6 +210,7 @@ class Map:
         self.h = h
         self.res = float(res)
         self.storage = storage
+        self.res_type = res_type
         self.max_blocks = int(max_blocks)
         self.truncation_boundary_factor = float(truncation_boundary_factor)
 
@@ -259,6 +263,21 @@ class Map:
                 tsdf.ctypes.data if voxels else None, weight.ctypes.data if voxels else None,
                 ts.ctypes.data, C.byref(cnt)), "download_blocks")
         return keys, coords, tsdf, weight, ts
+
+    def download_multires(self):
+        """Multi-res maps: (keys u64[N], coords i32[N,3], tsdf, weight, past_tsdf, past_weight
+        f32[N,585], scales i32[N,2] = (current, min))."""
+        n = self.num_blocks()
+        keys = np.zeros(n, np.uint64)
+        coords = np.zeros((n, 3), np.int32)
+        arrs = [np.zeros((n, 585), np.float32) for _ in range(4)]
+        scales = np.zeros((n, 2), np.int32)
+        cnt = C.c_int64()
+        if n:
+            _check(self._L.se_gpu_map_download_multires(
+                self.h, n, keys.ctypes.data, coords.ctypes.data, *[a.ctypes.data for a in arrs],
+                scales.ctypes.data, C.byref(cnt)), "download_multires")
+        return (keys, coords, *arrs, scales)
 
     def upload_blocks(self, keys, tsdf, weight):
         """Allocate the blocks with these keys (Morton code << 5 | 3) and overwrite their voxels."""

@@ -231,7 +231,10 @@ se_gpu_status enqueue_integrate(se_gpu_map* map, const float* depth_dev, const s
         ProfScope ps(kProfFrustum, stream);
         frustum_kernel<<<sms * 4, 256, 0, stream>>>(m, s, map->iparams);
     }
-    {
+    if (m.res_type == SE_GPU_RES_MULTI) {
+        enqueue_update_multires(m, s, depth_dev, map->iparams, stream);
+    }
+    else {
         ProfScope ps(kProfUpdate, stream);
         if (m.storage == SE_GPU_STORAGE_F32)
             update_kernel<SE_GPU_STORAGE_F32><<<sms * 8, 256, 0, stream>>>(m, s, depth_dev, map->iparams);

@@ -1,8 +1,11 @@
 // map.cu — device map lifecycle: block hash + block pool + dense block index + occupancy
 // pyramid, error latching, block download / upload and the allocated-block AABB.
 #include <cmath>
+#include <climits>
 #include <cstring>
+#include <vector>
 
+#include "multires.cuh"
 #include "se_gpu_internal.cuh"
 
 namespace se_gpu {
@@ -55,6 +58,26 @@ __global__ void download_voxels_kernel(MapDevice m, int n, float* tsdf, float* w
     }
 }
 
+// Multi-res blocks: the scale-0 level as tsdf / weight (se_gpu_map_download_blocks), or all
+// 585 entries with past data and scales (se_gpu_map_download_multires).
+template <int S>
+__global__ void download_mr_kernel(MapDevice m, int n, int per_block, float* tsdf, float* weight, float* past_tsdf,
+                                   float* past_weight)
+{
+    const size_t total = (size_t) n * per_block;
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < total; i += (size_t) gridDim.x * blockDim.x) {
+        const MrVoxel v = mr_load<S>(m, (int) (i / per_block), (int) (i % per_block));
+        if (tsdf)
+            tsdf[i] = v.tsdf;
+        if (weight)
+            weight[i] = v.weight;
+        if (past_tsdf)
+            past_tsdf[i] = v.past_tsdf;
+        if (past_weight)
+            past_weight[i] = v.past_weight;
+    }
+}
+
 __global__ void aabb_kernel(MapDevice m, int* out)
 {
     int n = m.counters[kCntNumBlocks];
@@ -81,8 +104,8 @@ se_gpu_status se_gpu_map_create(const se_gpu_map_config* cfg, se_gpu_map** out)
         return SE_GPU_ERR_BAD_ARG;
     }
     *out = nullptr;
-    if (cfg->field != SE_GPU_FIELD_TSDF || cfg->res_type != SE_GPU_RES_SINGLE) {
-        set_last_error("se_gpu_map_create: only single-resolution TSDF maps are supported");
+    if (cfg->field != SE_GPU_FIELD_TSDF || (cfg->res_type != SE_GPU_RES_SINGLE && cfg->res_type != SE_GPU_RES_MULTI)) {
+        set_last_error("se_gpu_map_create: only TSDF maps (single- or multi-resolution) are supported");
         return SE_GPU_ERR_NOT_SUPPORTED;
     }
     if (!(cfg->res > 0.0f) || cfg->max_blocks <= 0 || cfg->max_blocks > (1ll << 30) || !(cfg->max_weight >= 1.0f)
@@ -145,12 +168,16 @@ se_gpu_status se_gpu_map_create(const se_gpu_map_config* cfg, se_gpu_map** out)
     m.max_weight = cfg->max_weight;
     m.storage = cfg->storage;
     m.capacity = (int) cfg->max_blocks;
+    m.res_type = cfg->res_type;
+    const bool mr = m.res_type == SE_GPU_RES_MULTI;
 
     uint64_t hslots = 1024;
     while (hslots < 2ull * (uint64_t) m.capacity)
         hslots <<= 1;
     m.hash_mask = (uint32_t) (hslots - 1);
-    const size_t vox_bytes = (size_t) m.capacity * kBlockVoxels * (m.storage == SE_GPU_STORAGE_F32 ? 8 : 4);
+    // single-res: 512 x {tsdf, weight}; multi-res: 585 x {data, past data} per block
+    const size_t vox_bytes = mr ? (size_t) m.capacity * kMrVoxels * (m.storage == SE_GPU_STORAGE_F32 ? 16 : 8)
+                                : (size_t) m.capacity * kBlockVoxels * (m.storage == SE_GPU_STORAGE_F32 ? 8 : 4);
     const size_t cells = (size_t) m.bps * m.bps * m.bps;
 
     auto fail = [&](cudaError_t e, const char* what) {
@@ -172,6 +199,16 @@ se_gpu_status se_gpu_map_create(const se_gpu_map_config* cfg, se_gpu_map** out)
     if ((e = cudaMalloc(&map->rparams, sizeof(RaycastParams))) != cudaSuccess) return fail(e, "cudaMalloc(params)");
     if ((e = cudaMalloc(&map->timestamp_dev, sizeof(int))) != cudaSuccess) return fail(e, "cudaMalloc(timestamp)");
     if ((e = cudaMemset(map->timestamp_dev, 0, sizeof(int))) != cudaSuccess) return fail(e, "cudaMemset(timestamp)");
+    if ((e = cudaMalloc(&m.aabb, 6 * sizeof(int))) != cudaSuccess) return fail(e, "cudaMalloc(aabb)");
+    {
+        const int init[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
+        if ((e = cudaMemcpy(m.aabb, init, sizeof(init), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e, "cudaMemcpy(aabb)");
+    }
+    if (mr) {
+        if ((e = cudaMalloc(&m.block_scale, (size_t) m.capacity * 2)) != cudaSuccess) return fail(e, "cudaMalloc(scales)");
+        if ((e = cudaMemset(m.block_scale, 0xff, (size_t) m.capacity * 2)) != cudaSuccess) return fail(e, "cudaMemset(scales)");
+        if ((e = cudaMalloc(&m.block_nscale, (size_t) m.capacity)) != cudaSuccess) return fail(e, "cudaMalloc(scales)");
+    }
     if ((e = cudaMalloc(&m.block_index, cells * sizeof(int))) != cudaSuccess) return fail(e, "cudaMalloc(block index)");
     if ((e = cudaMemset(m.block_index, 0xff, cells * sizeof(int))) != cudaSuccess) return fail(e, "cudaMemset(block index)");
     m.occ_levels = m.log2_bps + 1;
@@ -199,6 +236,9 @@ se_gpu_status se_gpu_map_destroy(se_gpu_map* map)
     cudaFree(m.update_list);
     cudaFree(m.counters);
     cudaFree(m.block_index);
+    cudaFree(m.aabb);
+    cudaFree(m.block_scale);
+    cudaFree(m.block_nscale);
     cudaFree(map->iparams);
     cudaFree(map->rparams);
     cudaFree(map->timestamp_dev);
@@ -291,7 +331,13 @@ se_gpu_status se_gpu_map_download_blocks(const se_gpu_map* map, int64_t capacity
             SE_CUDA_TRY(cudaMalloc(&dt, bytes));
         if (weight)
             SE_CUDA_TRY(cudaMalloc(&dw, bytes));
-        if (m.storage == SE_GPU_STORAGE_F32)
+        if (m.res_type == SE_GPU_RES_MULTI && m.storage == SE_GPU_STORAGE_F32)
+            download_mr_kernel<SE_GPU_STORAGE_F32><<<device_sm_count() * 4, 256>>>(m, n, kBlockVoxels, dt, dw, nullptr,
+                                                                                  nullptr);
+        else if (m.res_type == SE_GPU_RES_MULTI)
+            download_mr_kernel<SE_GPU_STORAGE_F16><<<device_sm_count() * 4, 256>>>(m, n, kBlockVoxels, dt, dw, nullptr,
+                                                                                  nullptr);
+        else if (m.storage == SE_GPU_STORAGE_F32)
             download_voxels_kernel<SE_GPU_STORAGE_F32><<<device_sm_count() * 4, 256>>>(m, n, dt, dw);
         else
             download_voxels_kernel<SE_GPU_STORAGE_F16><<<device_sm_count() * 4, 256>>>(m, n, dt, dw);
@@ -314,6 +360,10 @@ se_gpu_status se_gpu_map_upload_blocks(se_gpu_map* map, int64_t n, const uint64_
     if (!map || n < 0 || n > (1ll << 30) || (n > 0 && (!keys || !tsdf || !weight))) {
         set_last_error("se_gpu_map_upload_blocks: invalid argument");
         return SE_GPU_ERR_BAD_ARG;
+    }
+    if (map->dev.res_type != SE_GPU_RES_SINGLE) {
+        set_last_error("se_gpu_map_upload_blocks: single-resolution maps only");
+        return SE_GPU_ERR_NOT_SUPPORTED;
     }
     if (n == 0)
         return SE_GPU_OK;
@@ -347,6 +397,64 @@ se_gpu_status se_gpu_map_upload_blocks(se_gpu_map* map, int64_t n, const uint64_
         return cuda_status(e, "se_gpu_map_upload_blocks");
     map->last_stream = 0;
     return se_gpu_map_check(map);
+}
+
+se_gpu_status se_gpu_map_download_multires(const se_gpu_map* map, int64_t capacity, uint64_t* keys, int32_t* coords,
+                                           float* tsdf, float* weight, float* past_tsdf, float* past_weight,
+                                           int32_t* scales, int64_t* count)
+{
+    if (!map || capacity < 0) {
+        set_last_error("se_gpu_map_download_multires: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    const MapDevice& m = map->dev;
+    if (m.res_type != SE_GPU_RES_MULTI) {
+        set_last_error("se_gpu_map_download_multires: not a multi-resolution map");
+        return SE_GPU_ERR_NOT_SUPPORTED;
+    }
+    SE_CUDA_TRY(cudaStreamSynchronize(map->last_stream));
+    int nb = 0;
+    SE_CUDA_TRY(cudaMemcpy(&nb, m.counters + kCntNumBlocks, sizeof(int), cudaMemcpyDeviceToHost));
+    nb = nb < m.capacity ? nb : m.capacity;
+    if (count)
+        *count = nb;
+    const int n = (int) (capacity < nb ? capacity : nb);
+    if (n == 0)
+        return SE_GPU_OK;
+    if (keys)
+        SE_CUDA_TRY(cudaMemcpy(keys, m.block_keys, (size_t) n * 8, cudaMemcpyDeviceToHost));
+    if (coords)
+        SE_CUDA_TRY(cudaMemcpy(coords, m.block_coord, (size_t) n * 12, cudaMemcpyDeviceToHost));
+    if (scales) {
+        std::vector<signed char> sc((size_t) n * 2);
+        SE_CUDA_TRY(cudaMemcpy(sc.data(), m.block_scale, sc.size(), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < sc.size(); ++i)
+            scales[i] = sc[i];
+    }
+    float* host[4] = {tsdf, weight, past_tsdf, past_weight};
+    float* dev[4] = {nullptr, nullptr, nullptr, nullptr};
+    const size_t bytes = (size_t) n * kMrVoxels * sizeof(float);
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+        if (host[k])
+            e = cudaMalloc(&dev[k], bytes);
+    if (e == cudaSuccess) {
+        if (m.storage == SE_GPU_STORAGE_F32)
+            download_mr_kernel<SE_GPU_STORAGE_F32><<<device_sm_count() * 4, 256>>>(m, n, kMrVoxels, dev[0], dev[1],
+                                                                                  dev[2], dev[3]);
+        else
+            download_mr_kernel<SE_GPU_STORAGE_F16><<<device_sm_count() * 4, 256>>>(m, n, kMrVoxels, dev[0], dev[1],
+                                                                                  dev[2], dev[3]);
+        e = cudaDeviceSynchronize();
+    }
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+        if (host[k])
+            e = cudaMemcpy(host[k], dev[k], bytes, cudaMemcpyDeviceToHost);
+    for (int k = 0; k < 4; ++k)
+        cudaFree(dev[k]);
+    if (e != cudaSuccess)
+        return cuda_status(e, "se_gpu_map_download_multires");
+    return SE_GPU_OK;
 }
 
 se_gpu_status se_gpu_map_aabb(const se_gpu_map* map, int32_t mn[3], int32_t mx[3], int* empty)

@@ -15,6 +15,9 @@ se_gpu_status enqueue_integrate(se_gpu_map* map, const float* depth_dev, const s
 se_gpu_status enqueue_raycast(const se_gpu_map* map, const se_gpu_pinhole& sensor, const float* T_WS_host16,
                               const float* pose12_dev, float* pts_dev, float* nrm_dev, int8_t* scale_dev,
                               cudaStream_t stream);
+// Multi-res TSDF update over the frame's block list (after carve and frustum).
+void enqueue_update_multires(const MapDevice& m, const Pinhole& s, const float* depth_dev,
+                             const IntegrateParams* params, cudaStream_t stream);
 // With pose12_dev_io the tracker starts from, and writes its result to, that device pose.
 se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const float* ref_pts, const float* ref_nrm,
                             const float* T_WS_host16, float* pose12_dev_io, cudaStream_t stream);

@@ -17,6 +17,7 @@
 
 #include "pipeline.cuh"
 #include "profile.cuh"
+#include "multires.cuh"
 #include "se_gpu_internal.cuh"
 
 namespace se_gpu {
@@ -307,10 +308,50 @@ __device__ bool field_grad(const MapDevice& m, BlockCache& c, F3 p_W, F3& g)
     return true;
 }
 
+// Map::getData<Safe::On> on a multi-res map: the data at the block's current scale.
 template <int S>
-__device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockCache& c, F3 o, F3 d, float t_near,
-                             float t_far, F3& hit)
+__device__ __forceinline__ void mr_map_get_data(const MapDevice& m, F3 p, float& t, float& w)
 {
+    int vx, vy, vz;
+    if (!point_to_voxel(m, p, vx, vy, vz)) {
+        t = 1.0f;
+        w = 0.0f;
+        return;
+    }
+    mr_get_data<S>(m, vx, vy, vz, t, w);
+}
+
+// Map::getFieldInterp(point, returned_scale) on a multi-res map (map_impl.hpp:176-196).
+template <int S>
+__device__ __forceinline__ bool mr_field_interp(const MapDevice& m, F3 p_W, float& out, int* returned_scale)
+{
+    F3 vf;
+    if (!point_to_voxel_f(m, p_W, vf))
+        return false;
+    return mr_interp<S>(m, vf, 0, out, returned_scale);
+}
+
+// Map::getFieldGrad on a multi-res map (map_impl.hpp:236-262).
+template <int S>
+__device__ __forceinline__ bool mr_field_grad(const MapDevice& m, F3 p_W, F3& g)
+{
+    F3 vf;
+    if (!point_to_voxel_f(m, p_W, vf))
+        return false;
+    F3 gv;
+    if (!mr_grad<S>(m, vf, gv))
+        return false;
+    g = f3(gv.x / m.res, gv.y / m.res, gv.z / m.res);
+    return true;
+}
+
+// raycast<TSDF> (raycaster_impl.hpp:456-533). MR selects the multi-res data access; the
+// returned scale is the one of the last successful interpolation (0 for single-res maps).
+template <int S, bool MR>
+__device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockCache& c, F3 o, F3 d, float t_near,
+                             float t_far, F3& hit, int& scale_out)
+{
+    int scale_tt = 0;
     float t_min, t_max;
     first_block(m, rp, o, d, t_near, t_far, t_min, t_max);
     if (t_min <= 0.0f)
@@ -323,14 +364,20 @@ __device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockC
     float stepsize = largestep;
     F3 p = add(o, mul(d, t));
     float f_t, w_t;
-    map_get_data<S>(m, c, p, f_t, w_t);
+    if constexpr (MR)
+        mr_map_get_data<S>(m, p, f_t, w_t);
+    else
+        map_get_data<S>(m, c, p, f_t, w_t);
     float f_tt = 0.0f;
     if (!(f_t >= 0.0f))
         return false;
     // every step is at least res > 0, so the march ends at t_far (NaN poses end it at once)
     for (; t < t_far; t += stepsize) {
         float f, w;
-        map_get_data<S>(m, c, p, f, w);
+        if constexpr (MR)
+            mr_map_get_data<S>(m, p, f, w);
+        else
+            map_get_data<S>(m, c, p, f, w);
         if (!(w != 0.0f)) {
             stepsize = largestep;
             p = add(p, mul(stepsize, d));
@@ -341,7 +388,12 @@ __device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockC
         // (double) f <= 0.1 is exactly f < 0.1f, with no FP64 instruction.
         if (f_tt < 0.1f && f_tt >= -0.5f) {
             float fi;
-            if (field_interp<S>(m, c, p, fi))
+            bool ok;
+            if constexpr (MR)
+                ok = mr_field_interp<S>(m, p, fi, &scale_tt);
+            else
+                ok = field_interp<S>(m, c, p, fi);
+            if (ok)
                 f_tt = fi;
         }
         if (f_tt < 0.0f)
@@ -353,6 +405,7 @@ __device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockC
     if (f_tt < 0.0f) {
         t = t - stepsize * (f_tt - 0.0f) / (f_tt - f_t);
         hit = add(o, mul(d, t));
+        scale_out = scale_tt;
         return true;
     }
     return false;
@@ -366,7 +419,7 @@ __global__ void raycast_prep_kernel(const float* pose12, RaycastParams host_p, R
     *out = p;
 }
 
-template <int S>
+template <int S, bool MR>
 __global__ void __launch_bounds__(128) raycast_kernel(MapDevice m, Pinhole s, const RaycastParams* __restrict__ P,
                                                       float* __restrict__ pts, float* __restrict__ nrm,
                                                       int8_t* __restrict__ scale)
@@ -388,10 +441,16 @@ __global__ void __launch_bounds__(128) raycast_kernel(MapDevice m, Pinhole s, co
     F3 hit;
     F3 n = f3(0.0f, 0.0f, 0.0f);
     F3 p = f3(0.0f, 0.0f, 0.0f);
-    if (raycast_tsdf<S>(m, rp, c, origin, dir_W, t_near, t_far, hit)) {
+    int hit_scale = 0;
+    if (raycast_tsdf<S, MR>(m, rp, c, origin, dir_W, t_near, t_far, hit, hit_scale)) {
         p = hit;
         F3 g;
-        if (field_grad<S>(m, c, hit, g))
+        bool ok;
+        if constexpr (MR)
+            ok = mr_field_grad<S>(m, hit, g);
+        else
+            ok = field_grad<S>(m, c, hit, g);
+        if (ok)
             n = normalized(g);
     }
     pts[3 * idx + 0] = p.x;
@@ -401,10 +460,10 @@ __global__ void __launch_bounds__(128) raycast_kernel(MapDevice m, Pinhole s, co
     nrm[3 * idx + 1] = n.y;
     nrm[3 * idx + 2] = n.z;
     if (scale)
-        scale[idx] = 0;
+        scale[idx] = (int8_t) hit_scale;
 }
 
-template <int S>
+template <int S, bool MR>
 __global__ void field_query_kernel(MapDevice m, int n, const float* __restrict__ pts, float* __restrict__ out,
                                    int* __restrict__ valid, int grad)
 {
@@ -416,14 +475,20 @@ __global__ void field_query_kernel(MapDevice m, int n, const float* __restrict__
     bool ok;
     if (grad) {
         F3 g = f3(0.0f, 0.0f, 0.0f);
-        ok = field_grad<S>(m, c, p, g);
+        if constexpr (MR)
+            ok = mr_field_grad<S>(m, p, g);
+        else
+            ok = field_grad<S>(m, c, p, g);
         out[3 * i] = ok ? g.x : 0.0f;
         out[3 * i + 1] = ok ? g.y : 0.0f;
         out[3 * i + 2] = ok ? g.z : 0.0f;
     }
     else {
         float v = 0.0f;
-        ok = field_interp<S>(m, c, p, v);
+        if constexpr (MR)
+            ok = mr_field_interp<S>(m, p, v, nullptr);
+        else
+            ok = field_interp<S>(m, c, p, v);
         out[i] = ok ? v : 0.0f;
     }
     if (valid)
@@ -454,10 +519,15 @@ se_gpu_status enqueue_raycast(const se_gpu_map* map, const se_gpu_pinhole& senso
     raycast_prep_kernel<<<1, 1, 0, stream>>>(T_WS_host16 ? nullptr : pose12_dev, rp, map->rparams);
     dim3 grid((s.w + 15) / 16, (s.h + 7) / 8);
     ProfScope ps(kProfRaycast, stream);
-    if (m.storage == SE_GPU_STORAGE_F32)
-        raycast_kernel<SE_GPU_STORAGE_F32><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+    const bool mr = m.res_type == SE_GPU_RES_MULTI;
+    if (m.storage == SE_GPU_STORAGE_F32 && !mr)
+        raycast_kernel<SE_GPU_STORAGE_F32, false><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+    else if (!mr)
+        raycast_kernel<SE_GPU_STORAGE_F16, false><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+    else if (m.storage == SE_GPU_STORAGE_F32)
+        raycast_kernel<SE_GPU_STORAGE_F32, true><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
     else
-        raycast_kernel<SE_GPU_STORAGE_F16><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+        raycast_kernel<SE_GPU_STORAGE_F16, true><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
     SE_CUDA_TRY(cudaGetLastError());
     return SE_GPU_OK;
 }
@@ -487,10 +557,15 @@ static se_gpu_status field_query(const se_gpu_map* map, int64_t n, const float* 
         return SE_GPU_OK;
     cudaStream_t stream = (cudaStream_t) stream_p;
     const unsigned blocks = (unsigned) ((n + 127) / 128);
-    if (map->dev.storage == SE_GPU_STORAGE_F32)
-        field_query_kernel<SE_GPU_STORAGE_F32><<<blocks, 128, 0, stream>>>(map->dev, (int) n, pts, out, valid, grad);
+    const bool mr = map->dev.res_type == SE_GPU_RES_MULTI;
+    if (map->dev.storage == SE_GPU_STORAGE_F32 && !mr)
+        field_query_kernel<SE_GPU_STORAGE_F32, false><<<blocks, 128, 0, stream>>>(map->dev, (int) n, pts, out, valid, grad);
+    else if (!mr)
+        field_query_kernel<SE_GPU_STORAGE_F16, false><<<blocks, 128, 0, stream>>>(map->dev, (int) n, pts, out, valid, grad);
+    else if (map->dev.storage == SE_GPU_STORAGE_F32)
+        field_query_kernel<SE_GPU_STORAGE_F32, true><<<blocks, 128, 0, stream>>>(map->dev, (int) n, pts, out, valid, grad);
     else
-        field_query_kernel<SE_GPU_STORAGE_F16><<<blocks, 128, 0, stream>>>(map->dev, (int) n, pts, out, valid, grad);
+        field_query_kernel<SE_GPU_STORAGE_F16, true><<<blocks, 128, 0, stream>>>(map->dev, (int) n, pts, out, valid, grad);
     SE_CUDA_TRY(cudaGetLastError());
     return SE_GPU_OK;
 }

@@ -19,6 +19,7 @@ namespace se_gpu {
 constexpr int kBlockSize = 8;
 constexpr int kBlockVoxels = 512;
 constexpr int kMaxBlockScale = 3;
+constexpr int kMrVoxels = 585; // 8^3 + 4^3 + 2^3 + 1 (BlockMultiRes, block.hpp:126-157)
 constexpr unsigned long long kEmptyKey = 0xffffffffffffffffULL;
 constexpr int kMaxProbe = 256;
 
@@ -191,6 +192,15 @@ struct MapDevice {
     // scratch / counters
     int* counters;                // kNumCounters ints
     int* update_list;             // capacity ints
+    // Allocated-block AABB in voxels (min xyz, max xyz, inclusive), extended on every insert
+    // like Octree::aabbExtend; INT_MAX / INT_MIN while the map is empty.
+    int* aabb;
+    // Multi-resolution TSDF (res_type SE_GPU_RES_MULTI): `voxels` holds kMrVoxels entries per
+    // block, each {data, past data}; block_scale holds (current_scale, min_scale) per block
+    // (-1 before the first update) and block_nscale this frame's integration scale.
+    int res_type;
+    signed char* block_scale;
+    signed char* block_nscale;
 };
 
 __device__ __forceinline__ int hash_find(const MapDevice& m, uint64_t key)
@@ -440,6 +450,16 @@ __device__ __forceinline__ void insert_block(const MapDevice& m, uint64_t key, i
                 m.block_coord[3 * idx + 2] = bz << 3;
                 m.block_keys[idx] = key;
                 m.block_ts[idx] = -1;
+                if (m.block_scale) {
+                    m.block_scale[2 * idx] = -1;
+                    m.block_scale[2 * idx + 1] = -1;
+                }
+                atomicMin(&m.aabb[0], bx << 3);
+                atomicMin(&m.aabb[1], by << 3);
+                atomicMin(&m.aabb[2], bz << 3);
+                atomicMax(&m.aabb[3], (bx << 3) + kBlockSize - 1);
+                atomicMax(&m.aabb[4], (by << 3) + kBlockSize - 1);
+                atomicMax(&m.aabb[5], (bz << 3) + kBlockSize - 1);
                 m.block_index[((size_t) bz << (2 * m.log2_bps)) | ((size_t) by << m.log2_bps) | (size_t) bx] = idx;
                 for (int L = 0; L < m.occ_levels; ++L) {
                     const int lg = m.log2_bps - L;

@@ -34,6 +34,9 @@ class PinholeSpec:
 # The camera set-ups of the benchmark configurations.
 SENSOR_320 = PinholeSpec(320, 240, 262.5, 262.5, 159.5, 119.5, 0.4, 6.0)
 SENSOR_640 = PinholeSpec(640, 480, 525.0, 525.0, 319.5, 239.5, 0.4, 6.0)
+# A wide, coarse camera for multi-resolution tests: at 2 cm voxels a pixel covers z / 1.6
+# voxels, so the reference's pixel/voxel ratios {1.5, 3, 6} select scales 0-2 within the room.
+SENSOR_160W = PinholeSpec(160, 120, 80.0, 80.0, 79.5, 59.5, 0.4, 6.0)
 
 
 @dataclass
@@ -141,6 +144,22 @@ def random_walk_trajectory(n_frames: int, seed: int, sigma_m=0.02, sigma_deg=1.0
     return poses
 
 
+def dolly_trajectory(n_frames: int, x_far=-2.0, x_near=1.8) -> list:
+    """Frames looking along +x at the room's end wall: the first 70 % move from x_far to
+    x_near (5 m to 1.2 m from the wall), the rest move back, with a small sideways wobble."""
+    n_in = max(2, int(math.ceil(0.7 * n_frames)))
+    poses = []
+    for i in range(n_frames):
+        if i < n_in:
+            x = x_far + (x_near - x_far) * i / (n_in - 1)
+        else:
+            x = x_near - (x_near - x_far) * 0.6 * (i - n_in + 1) / max(1, n_frames - n_in)
+        eye = np.array([x, 0.3 * math.sin(0.4 * i), 0.1])
+        target = eye + np.array([1.0, 0.1 * math.cos(0.3 * i), -0.05])
+        poses.append(look_at(eye, target))
+    return poses
+
+
 def render_depth(scene: Scene, sensor: PinholeSpec, T_WC, frame_seed: int, device="cpu",
                  noise=True) -> np.ndarray:
     """Ray trace one float32 depth image (metres of z) with noise and 2 % dropout."""
@@ -207,6 +226,8 @@ def dataset(config: str, n_frames: int, device="cpu", seed=None):
 
     config "tsdf320": 320x240, circle of 0.05 m / ~2 deg steps, ground-truth poses.
     config "tsdf640": 640x480, random-walk velocity (0.02 m, 1 deg per frame).
+    config "mr160": 160x120 wide camera dollying towards and away from the end wall (multi-res
+    integration scales 0-2 at 2 cm voxels); objects kept out of the central 2.2 m.
     """
     if config == "tsdf320":
         seed = 1001 if seed is None else seed
@@ -216,9 +237,15 @@ def dataset(config: str, n_frames: int, device="cpu", seed=None):
         seed = 1002 if seed is None else seed
         sensor = SENSOR_640
         poses = random_walk_trajectory(n_frames, seed=seed * 31 + 7)
+    elif config == "mr160":
+        seed = 1003 if seed is None else seed
+        sensor = SENSOR_160W
+        poses = dolly_trajectory(n_frames)
+        scene = make_scene(seed, keep_out_radius=(0.0, 2.2))
     else:
         raise ValueError(config)
-    scene = make_scene(seed)
+    if config != "mr160":
+        scene = make_scene(seed)
     frames = [render_depth(scene, sensor, T, seed * 7919 + i, device=device)
               for i, T in enumerate(poses)]
     return sensor, scene, poses, frames
