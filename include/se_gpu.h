@@ -170,6 +170,28 @@ SE_GPU_API se_gpu_status se_gpu_map_field_grad(const se_gpu_map* map, int64_t n,
  * SE_GPU_OK with *empty = 1 when no block is allocated. */
 SE_GPU_API se_gpu_status se_gpu_map_aabb(const se_gpu_map* map, int32_t mn[3], int32_t mx[3], int* empty);
 
+/* ---------------------------------------------------------- differentiable raycast -- */
+
+/* Differentiable depth render of a single-res map. No counterpart in the reference. Per
+ * pixel, the march of raycast_volume (include/se/map/impl/raycaster_impl.hpp:456-533) up to
+ * the first sample below the surface, then regula falsi on the trilinear TSDF inside that
+ * last step: depth_dev[x + y*width] = z (camera frame) of the root, 0 where the march finds
+ * no crossing or the interpolation is undefined at the bracket. */
+SE_GPU_API se_gpu_status se_gpu_render_depth(const se_gpu_map* map, const se_gpu_pinhole* sensor,
+                                             const float T_WS[16], float* depth_dev, void* stream);
+/* Adjoint of se_gpu_render_depth, recomputing each ray's march. No counterpart in the
+ * reference. With the pose perturbed on the left, T = exp(xi) T_WS, xi = [rho; omega] (the
+ * reference's se(3) update, src/tracker/icp.cpp:208-223):
+ *   twist_grad_dev[6] += sum_i grad_depth_dev[i] * d depth_i / d xi     (device doubles)
+ *   voxel_grad_dev[b*512 + v] += sum_i grad_depth_dev[i] * d depth_i / d tsdf(b, v)
+ *       (b the pool index, the block order of se_gpu_map_download_blocks; may be NULL)
+ *   jac_dev[6*i + j] = d depth_i / d xi_j  (width*height*6 floats; may be NULL)
+ * grad_depth_dev (width*height floats) may be NULL when jac_dev is given. Asynchronous. */
+SE_GPU_API se_gpu_status se_gpu_raycast_adjoint(const se_gpu_map* map, const se_gpu_pinhole* sensor,
+                                                const float T_WS[16], const float* grad_depth_dev,
+                                                double* twist_grad_dev, float* voxel_grad_dev,
+                                                float* jac_dev, void* stream);
+
 /* --------------------------------------------------------------------------- tracker -- */
 
 /* Replaces se::Tracker ctor (include/se/tracker/tracker.hpp:42-48): device buffers for the

@@ -45,6 +45,7 @@ def lib():
         u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
         i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
         i8p = np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS")
+        f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
         vp = C.c_void_p
         sig = {
             "so_set_num_threads": (None, [C.c_int]),
@@ -54,6 +55,9 @@ def lib():
             "so_map_is_multires": (C.c_int, [vp]),
             "so_map_mr_blocks": (None, [vp, vp, vp, vp, vp, vp, vp, vp]),
             "so_map_destroy": (None, [vp]),
+            "so_render_depth_f64": (None, [vp, C.POINTER(Pinhole), f64p, f64p]),
+            "so_raycast_adjoint_f64": (None, [vp, C.POINTER(Pinhole), f64p, vp, f64p, vp, vp]),
+            "so_map_set_voxel": (None, [vp, i32p, C.c_float, C.c_float]),
             "so_map_size": (C.c_int, [vp]),
             "so_map_dim": (C.c_float, [vp]),
             "so_integrate_depth": (None, [vp, f32p, C.POINTER(Pinhole), f32p, C.c_int,
@@ -177,6 +181,29 @@ class OracleMap:
             lib().so_map_blocks(self.h, keys.ctypes.data, coords.ctypes.data, tsdf.ctypes.data,
                                 weight.ctypes.data, ts.ctypes.data)
         return keys, coords, tsdf, weight, ts
+
+    def render_depth_f64(self, sensor: Pinhole, T_WS):
+        """Differentiable depth render in FP64: z of the trilinear root per pixel, 0 if none."""
+        d = np.zeros((sensor.height, sensor.width), np.float64)
+        T = np.ascontiguousarray(np.asarray(T_WS, np.float64).reshape(16))
+        lib().so_render_depth_f64(self.h, C.byref(sensor), T, d.reshape(-1))
+        return d
+
+    def adjoint_f64(self, sensor: Pinhole, T_WS, grad_depth=None, voxel_grad=False, jac=False):
+        """(twist_grad[6], voxel_grad[N, 512] or None, jac[H, W, 6] or None) in FP64."""
+        T = np.ascontiguousarray(np.asarray(T_WS, np.float64).reshape(16))
+        g = None if grad_depth is None else np.ascontiguousarray(grad_depth, np.float64)
+        tw = np.zeros(6, np.float64)
+        vg = np.zeros((self.num_blocks(), 512), np.float64) if voxel_grad else None
+        jc = np.zeros((sensor.height, sensor.width, 6), np.float64) if jac else None
+        lib().so_raycast_adjoint_f64(self.h, C.byref(sensor), T, None if g is None else g.ctypes.data,
+                                     tw, None if vg is None else vg.ctypes.data,
+                                     None if jc is None else jc.ctypes.data)
+        return tw, vg, jc
+
+    def set_voxel(self, voxel_coord, tsdf, weight):
+        lib().so_map_set_voxel(self.h, np.ascontiguousarray(voxel_coord, np.int32), float(tsdf),
+                               float(weight))
 
     def mr_blocks(self):
         """Multi-res blocks: (keys u64[N], coords i32[N,3], tsdf f32[N,585], weight f32[N,585],

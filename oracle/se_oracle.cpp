@@ -1122,6 +1122,194 @@ static bool raycast_tsdf(const so_map& m, V3 origin_W, V3 dir_W, float t_near, f
     return false;
 }
 
+/* ------------------------------------- differentiable depth render, FP64 (no reference) -- */
+/* The CPU check of the GPU's differentiable render and its adjoint: the same algorithm (march
+ * of raycast<TSDF> to the first sample below the surface, then regula falsi on the trilinear
+ * field inside the last step) evaluated in double precision on the map's float voxels, with
+ * the root found to 1e-13. The gradients follow from the implicit function theorem at the
+ * root with the pose perturbed on the left, T = exp(xi) T_WS, xi = [rho; omega]. */
+
+struct D3 {
+    double x, y, z;
+};
+static inline D3 d3(double x, double y, double z) { return D3{x, y, z}; }
+static inline D3 dadd(D3 a, D3 b) { return d3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline D3 dmul(D3 a, double s) { return d3(a.x * s, a.y * s, a.z * s); }
+static inline double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline D3 dcross(D3 a, D3 b) { return d3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+
+struct TriD {
+    int oct[8];
+    int vi[8];
+    double f[8];
+    D3 t;
+};
+
+static inline D3 to_map_voxels(const so_map& m, D3 p)
+{
+    const Tf& T = m.T_MW;
+    const D3 q = d3((double) T.R[0][0] * p.x + (double) T.R[0][1] * p.y + (double) T.R[0][2] * p.z + (double) T.t[0],
+                    (double) T.R[1][0] * p.x + (double) T.R[1][1] * p.y + (double) T.R[1][2] * p.z + (double) T.t[1],
+                    (double) T.R[2][0] * p.x + (double) T.R[2][1] * p.y + (double) T.R[2][2] * p.z + (double) T.t[2]);
+    return q;
+}
+
+static inline bool in_map(const so_map& m, D3 q)
+{
+    const double dim = (double) m.dim;
+    return q.x >= 0.0 && q.x < dim && q.y >= 0.0 && q.y < dim && q.z >= 0.0 && q.z < dim;
+}
+
+static bool tri_sample_d(const so_map& m, D3 p, TriD& q, double& value)
+{
+    const D3 pm = to_map_voxels(m, p);
+    if (!in_map(m, pm))
+        return false;
+    const double r = (double) m.res;
+    const D3 bf = d3(pm.x / r - 0.5, pm.y / r - 0.5, pm.z / r - 0.5);
+    const int b[3] = {(int) bf.x, (int) bf.y, (int) bf.z};
+    for (int i = 0; i < 3; ++i)
+        if (b[i] < 0 || b[i] + 1 >= m.octree.size)
+            return false;
+    for (int n = 0; n < 8; ++n) {
+        const int32_t c[3] = {b[0] + (n & 1), b[1] + ((n >> 1) & 1), b[2] + (n >> 2)};
+        const int o = m.octree.block_at(c);
+        if (o < 0)
+            return false;
+        const Octant& oc = m.octree.octants[o];
+        const BlockData& bd = m.octree.blocks[oc.block];
+        const int vi = (c[0] - oc.coord[0]) + 8 * (c[1] - oc.coord[1]) + 64 * (c[2] - oc.coord[2]);
+        if (!(bd.weight[vi] != 0.0f))
+            return false;
+        q.f[n] = (double) bd.tsdf[vi];
+        q.oct[n] = o;
+        q.vi[n] = vi;
+    }
+    q.t = d3(bf.x - std::floor(bf.x), bf.y - std::floor(bf.y), bf.z - std::floor(bf.z));
+    const D3 t = q.t, tc = d3(1.0 - t.x, 1.0 - t.y, 1.0 - t.z);
+    const double* f = q.f;
+    value = ((f[0] * tc.x + f[1] * t.x) * tc.y + (f[2] * tc.x + f[3] * t.x) * t.y) * tc.z
+        + ((f[4] * tc.x + f[5] * t.x) * tc.y + (f[6] * tc.x + f[7] * t.x) * t.y) * t.z;
+    return true;
+}
+
+static inline void get_data_d(const so_map& m, D3 p, double& f, double& w)
+{
+    const D3 pm = to_map_voxels(m, p);
+    f = 1.0;
+    w = 0.0;
+    if (!in_map(m, pm))
+        return;
+    const double r = (double) m.res;
+    const int32_t c[3] = {(int) (pm.x / r), (int) (pm.y / r), (int) (pm.z / r)};
+    float tf, wf;
+    if (get_voxel(m, c, tf, wf)) {
+        f = tf;
+        w = wf;
+    }
+}
+
+static bool diff_hit_d(const so_map& m, D3 o, D3 d, double t_near, double t_far, double& t_star, TriD& q)
+{
+    const RayBlockHit rb = first_block_on_ray(m, v3((float) o.x, (float) o.y, (float) o.z),
+                                              v3((float) d.x, (float) d.y, (float) d.z), (float) t_near,
+                                              (float) t_far);
+    const double t_min = rb.tcmin, t_max = rb.tmax;
+    if (t_min <= 0.0 || !(t_near < t_max))
+        return false;
+    const double step = m.res, largestep = kBlockSize * step, trunc = (double) m.res * m.trunc_factor;
+    double t = t_min, stepsize = largestep, f_t, w_t, f_tt = 0.0;
+    get_data_d(m, dadd(o, dmul(d, t)), f_t, w_t);
+    if (!(f_t >= 0.0))
+        return false;
+    for (; t < t_far; t += stepsize) {
+        double f, w;
+        get_data_d(m, dadd(o, dmul(d, t)), f, w);
+        if (!(w != 0.0)) {
+            stepsize = largestep;
+            continue;
+        }
+        f_tt = f;
+        if (f_tt < 0.1 && f_tt >= -0.5) {
+            double fi;
+            TriD tq;
+            if (tri_sample_d(m, dadd(o, dmul(d, t)), tq, fi))
+                f_tt = fi;
+        }
+        if (f_tt < 0.0)
+            break;
+        stepsize = std::max(f_tt * trunc, step);
+    }
+    if (!(f_tt < 0.0))
+        return false;
+    double ta = t - stepsize, tb = t, fa, fb;
+    if (!tri_sample_d(m, dadd(o, dmul(d, ta)), q, fa) || !tri_sample_d(m, dadd(o, dmul(d, tb)), q, fb))
+        return false;
+    if (!(fa >= 0.0 && fb < 0.0))
+        return false;
+    double tm = tb;
+    int side = 0;
+    for (int it = 0; it < 200; ++it) {
+        tm = (ta * fb - tb * fa) / (fb - fa);
+        double fm;
+        if (!tri_sample_d(m, dadd(o, dmul(d, tm)), q, fm))
+            return false;
+        if (std::fabs(fm) < 1.0e-13)
+            break;
+        if (fm < 0.0) {
+            tb = tm;
+            fb = fm;
+            if (side == -1)
+                fa *= 0.5;
+            side = -1;
+        }
+        else {
+            ta = tm;
+            fa = fm;
+            if (side == 1)
+                fb *= 0.5;
+            side = 1;
+        }
+        if (!(tb - ta > 1.0e-15 * tb))
+            break;
+    }
+    t_star = tm;
+    return true;
+}
+
+struct RayD {
+    D3 o, d;
+    double nz, t_near, t_far;
+};
+
+static RayD ray_d(const so_pinhole& sp, const double T[16], int x, int y)
+{
+    const double rx = (x - (double) sp.cx) / (double) sp.fx, ry = (y - (double) sp.cy) / (double) sp.fy;
+    const double nrm = std::sqrt(rx * rx + ry * ry + 1.0);
+    const D3 n = d3(rx / nrm, ry / nrm, 1.0 / nrm);
+    RayD r;
+    r.d = d3(T[0] * n.x + T[1] * n.y + T[2] * n.z, T[4] * n.x + T[5] * n.y + T[6] * n.z,
+             T[8] * n.x + T[9] * n.y + T[10] * n.z);
+    r.o = d3(T[3], T[7], T[11]);
+    r.nz = n.z;
+    r.t_near = sp.near_plane / n.z;
+    r.t_far = sp.far_plane / n.z;
+    return r;
+}
+
+static D3 tri_grad_world_d(const so_map& m, const TriD& q)
+{
+    const double* f = q.f;
+    const D3 t = q.t, tc = d3(1.0 - t.x, 1.0 - t.y, 1.0 - t.z);
+    const double gx = ((f[1] - f[0]) * tc.y + (f[3] - f[2]) * t.y) * tc.z + ((f[5] - f[4]) * tc.y + (f[7] - f[6]) * t.y) * t.z;
+    const double gy = ((f[2] - f[0]) * tc.x + (f[3] - f[1]) * t.x) * tc.z + ((f[6] - f[4]) * tc.x + (f[7] - f[5]) * t.x) * t.z;
+    const double gz = ((f[4] - f[0]) * tc.x + (f[5] - f[1]) * t.x) * tc.y + ((f[6] - f[2]) * tc.x + (f[7] - f[3]) * t.x) * t.y;
+    const Tf& T = m.T_MW;
+    const double r = m.res;
+    return d3((T.R[0][0] * gx + T.R[1][0] * gy + T.R[2][0] * gz) / r, (T.R[0][1] * gx + T.R[1][1] * gy + T.R[2][1] * gz) / r,
+              (T.R[0][2] * gx + T.R[1][2] * gy + T.R[2][2] * gz) / r);
+}
+
 /* ----------------------------------------------------------------- ICP helpers (float) -- */
 
 /* Eigen-style unblocked Cholesky (LLT) on the lower triangle, then forward/back substitution.
@@ -2075,6 +2263,89 @@ int so_first_block_tmin(const so_map* map, const float o[3], const float d[3], f
         first_block_on_ray(*map, v3(o[0], o[1], o[2]), v3(d[0], d[1], d[2]), t_near, t_far);
     *tcmin = r.tcmin;
     return r.found ? 1 : 0;
+}
+
+void so_render_depth_f64(const so_map* map, const so_pinhole* sensor, const double T_WS[16], double* depth)
+{
+    const int W = sensor->width, H = sensor->height;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            const RayD r = ray_d(*sensor, T_WS, x, y);
+            double t;
+            TriD q;
+            depth[(size_t) x + (size_t) y * W] =
+                diff_hit_d(*map, r.o, r.d, r.t_near, r.t_far, t, q) ? t * r.nz : 0.0;
+        }
+    }
+}
+
+void so_raycast_adjoint_f64(const so_map* map, const so_pinhole* sensor, const double T_WS[16],
+                            const double* grad_depth, double twist_grad[6], double* voxel_grad, double* jac)
+{
+    const so_map& m = *map;
+    const int W = sensor->width, H = sensor->height;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    std::vector<int> block_of_octant;
+    if (voxel_grad) {
+        block_of_octant.assign(m.octree.octants.size(), -1);
+        for (size_t i = 0; i < m.octree.block_octant.size(); ++i)
+            block_of_octant[m.octree.block_octant[i]] = (int) i;
+    }
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            const size_t i = (size_t) x + (size_t) y * W;
+            double row[6] = {0, 0, 0, 0, 0, 0};
+            const double gd = grad_depth ? grad_depth[i] : 0.0;
+            if (gd != 0.0 || jac) {
+                const RayD r = ray_d(*sensor, T_WS, x, y);
+                double t;
+                TriD q;
+                if (diff_hit_d(m, r.o, r.d, r.t_near, r.t_far, t, q)) {
+                    const D3 g = tri_grad_world_d(m, q);
+                    const double den = ddot(g, r.d);
+                    if (std::fabs(den) > 1e-12) {
+                        const D3 p = dadd(r.o, dmul(r.d, t));
+                        const D3 pg = dcross(p, g);
+                        const double k = -r.nz / den;
+                        row[0] = k * g.x;
+                        row[1] = k * g.y;
+                        row[2] = k * g.z;
+                        row[3] = k * pg.x;
+                        row[4] = k * pg.y;
+                        row[5] = k * pg.z;
+                        for (int j = 0; j < 6; ++j)
+                            acc[j] += gd * row[j];
+                        if (voxel_grad && gd != 0.0) {
+                            const D3 tt = q.t, tc = d3(1.0 - tt.x, 1.0 - tt.y, 1.0 - tt.z);
+                            for (int n = 0; n < 8; ++n) {
+                                const double w = ((n & 1) ? tt.x : tc.x) * (((n >> 1) & 1) ? tt.y : tc.y)
+                                    * ((n >> 2) ? tt.z : tc.z);
+                                voxel_grad[(size_t) block_of_octant[q.oct[n]] * kBlockVoxels + q.vi[n]] += gd * k * w;
+                            }
+                        }
+                    }
+                }
+            }
+            if (jac)
+                for (int j = 0; j < 6; ++j)
+                    jac[6 * i + j] = row[j];
+        }
+    }
+    for (int j = 0; j < 6; ++j)
+        twist_grad[j] = acc[j];
+}
+
+void so_map_set_voxel(so_map* map, const int32_t c[3], float tsdf, float weight)
+{
+    const int o = map->octree.block_at(c);
+    if (o < 0 || map->octree.multires)
+        return;
+    const Octant& oc = map->octree.octants[o];
+    BlockData& b = map->octree.blocks[oc.block];
+    const int vi = (c[0] - oc.coord[0]) + 8 * (c[1] - oc.coord[1]) + 64 * (c[2] - oc.coord[2]);
+    b.tsdf[vi] = tsdf;
+    b.weight[vi] = weight;
 }
 
 uint64_t so_expand(uint64_t value) { return morton_expand(value); }

@@ -130,6 +130,18 @@ int so_map_get_field_grad(const so_map* map, const float point_W[3], float grad[
 int so_first_block_tmin(const so_map* map, const float origin_W[3], const float dir_W[3],
                         float t_near, float t_far, float* tcmin);
 
+/* Differentiable depth render of a single-res map in FP64 (no reference counterpart; the
+ * checker of se_gpu_render_depth / se_gpu_raycast_adjoint): depth = z of the root of the
+ * trilinear TSDF on each pixel's ray after the raycast march (0 where there is none).
+ * The adjoint accumulates sum_i grad_depth[i] * d depth_i / d xi for the left perturbation
+ * T = exp(xi) T_WS, xi = [rho; omega]; voxel_grad (num_blocks * 512, in so_map_blocks order)
+ * and jac (width * height * 6: d depth_i / d xi) may be NULL. */
+void so_render_depth_f64(const so_map* map, const so_pinhole* sensor, const double T_WS[16], double* depth);
+void so_raycast_adjoint_f64(const so_map* map, const so_pinhole* sensor, const double T_WS[16],
+                            const double* grad_depth, double twist_grad[6], double* voxel_grad, double* jac);
+/* Overwrite one voxel of an allocated single-res block (no-op elsewhere). */
+void so_map_set_voxel(so_map* map, const int32_t voxel_coord[3], float tsdf, float weight);
+
 /* Morton key operations (key_util_impl.hpp). */
 uint64_t so_expand(uint64_t value);
 uint64_t so_compact(uint64_t value);

@@ -23,7 +23,7 @@ import numpy as np
 from . import build as _build
 
 __all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "raycast_volume",
-           "track_noalloc",
+           "render_depth", "raycast_adjoint", "track_noalloc",
            "FramePipeline", "SeGpuError", "library", "library_path"]
 
 
@@ -78,6 +78,8 @@ SIGNATURES = {
     "se_gpu_map_field_grad": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP]),
     "se_gpu_map_aabb": (C.c_int, [_VP, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                   C.POINTER(C.c_int)]),
+    "se_gpu_render_depth": (C.c_int, [_VP, C.POINTER(_Pinhole), _F16, _VP, _VP]),
+    "se_gpu_raycast_adjoint": (C.c_int, [_VP, C.POINTER(_Pinhole), _F16, _VP, _VP, _VP, _VP, _VP]),
     "se_gpu_tracker_create": (C.c_int, [C.POINTER(_Pinhole), C.POINTER(_TrackerConfig),
                                         C.POINTER(_VP)]),
     "se_gpu_tracker_destroy": (C.c_int, [_VP]),
@@ -389,6 +391,41 @@ class Tracker:
         its = (C.c_int * 3)()
         _check(self._L.se_gpu_tracker_last_reduction(self.h, red, its), "last_reduction")
         return np.array(red[:], np.float32), list(its[:])
+
+
+def render_depth(map: Map, sensor: PinholeCamera, T_WS, out=None, stream=None):
+    """Differentiable depth render (no counterpart in the reference): z of the root of the
+    trilinear TSDF on each pixel's ray, 0 where there is none. Returns a CUDA [H, W] tensor."""
+    import torch
+    L = library()
+    if out is None:
+        out = torch.zeros((sensor.height, sensor.width), dtype=torch.float32, device="cuda")
+    d = _dptr(out, torch.float32, (sensor.height, sensor.width), "depth")
+    s = sensor._c()
+    _, tp = _m16(T_WS)
+    _check(L.se_gpu_render_depth(map.h, C.byref(s), tp, d, _stream(stream)), "se_gpu_render_depth")
+    return out
+
+
+def raycast_adjoint(map: Map, sensor: PinholeCamera, T_WS, grad_depth=None, twist_grad=None,
+                    voxel_grad=None, jac=None, stream=None):
+    """Adjoint of render_depth: accumulates sum_i grad_depth[i] * d depth_i / d xi into
+    twist_grad (CUDA float64 [6]; allocated and returned if None) for T = exp(xi) T_WS,
+    xi = [rho; omega]; voxel_grad (CUDA float32 [max_blocks, 512], pool order) receives
+    d L / d tsdf; jac (CUDA float32 [H, W, 6]) receives d depth_i / d xi."""
+    import torch
+    L = library()
+    if twist_grad is None:
+        twist_grad = torch.zeros(6, dtype=torch.float64, device="cuda")
+    g = _dptr(grad_depth, torch.float32, (sensor.height, sensor.width), "grad_depth") if grad_depth is not None else None
+    tw = _dptr(twist_grad, torch.float64, (6,), "twist_grad")
+    vg = _dptr(voxel_grad, torch.float32, (map.max_blocks, 512), "voxel_grad") if voxel_grad is not None else None
+    jc = _dptr(jac, torch.float32, (sensor.height, sensor.width, 6), "jac") if jac is not None else None
+    s = sensor._c()
+    _, tp = _m16(T_WS)
+    _check(L.se_gpu_raycast_adjoint(map.h, C.byref(s), tp, g, tw, vg, jc, _stream(stream)),
+           "se_gpu_raycast_adjoint")
+    return twist_grad
 
 
 def track_noalloc(sensor: PinholeCamera, config: TrackerConfig, depth, T_WS,
