@@ -127,14 +127,14 @@ def make_data(n_frames, device):
 # ----------------------------------------------------------------------------- GPU arm --
 
 def _variant(se, torch, dev, sensor, poses, depth_dev, first, steps, warmup, path, storage, max_blocks,
-             flush, profile=False, clocks=None):
+             flush, profile=False, clocks=None, res_type="single"):
     """Run frame 0 untimed, `warmup` untimed frames, then time `steps` frames (CUDA events per
     step on the launching stream, L2 flushed between steps outside the timed pairs).
     path "plain": the blocking reference-style calls (track with host pose readback, integrate,
     raycast); path "graph": the captured whole-frame pipeline with the pose on the device."""
     import ctypes as C
     W, H = sensor.width, sensor.height
-    m = se.Map(MAP_DIM, MAP_RES, max_blocks=max_blocks, storage=storage)
+    m = se.Map(MAP_DIM, MAP_RES, max_blocks=max_blocks, storage=storage, res_type=res_type)
     tracker = se.Tracker(m, sensor, se.TrackerConfig())
     stream = torch.cuda.current_stream(dev)
     T0 = poses[0].astype(np.float32).copy()
@@ -211,7 +211,7 @@ def run_ours(args, ws, rank, local):
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    n_frames = 1 + args.warmup + 2 * args.steps
+    n_frames = 1 + args.warmup + 2 * args.steps + 1  # the last frame is held out (adjoint)
     t0 = time.perf_counter()
     sensor_spec, scene, poses, frames = make_data(n_frames, dev)
     gen_s = time.perf_counter() - t0
@@ -251,6 +251,19 @@ def run_ours(args, ws, rank, local):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - e0
     g32["map"].check()
+
+    # differentiable render + adjoint on the map after all integrated frames, against the
+    # held-out frame
+    adjoint = _adjoint_bench(se, torch, g32["map"], sensor, poses[-1], depth_dev[-1], flush)
+
+    # multi-resolution TSDF map (the reference's MultiresTSDF), FP32 and FP16 storage, same
+    # frames through the captured pipeline
+    mr = {}
+    for st in ("f32", "f16"):
+        v = _variant(se, torch, dev, sensor, poses, depth_dev, first, K, args.warmup, "graph", st,
+                     args.max_blocks, flush, res_type="multi")
+        mr[st] = {"value": K / (v["dev_ms"] * 1e-3), "ms_per_step": v["dev_ms"] / K}
+        del v["map"], v["tracker"], v["fp"]
 
     times = torch.tensor([g32["dev_ms"], e2e_s, plain["dev_ms"], g16["dev_ms"]], dtype=torch.float64,
                          device=dev)
@@ -316,12 +329,123 @@ def run_ours(args, ws, rank, local):
         "voxels_per_s": float(np.mean(upd)) * K / (g32_ms * 1e-3),
         "updated_voxels_per_frame": float(np.mean(upd)),
         "num_blocks": g32["num_blocks"],
+        "multires": {"workload": "the same frames into a MultiresTSDF map (1024^3 at 1 cm, 8^3 blocks "
+                                 "with the 585-entry voxel pyramid), captured graph per frame",
+                     "graph_f32": mr["f32"], "graph_f16": mr["f16"]},
+        "adjoint": adjoint,
         "gen_s": gen_s,
         "clocks": g32["clocks"],
     }
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(frames, poses, sensor_spec, args.warmup, 2 * K, args.cpu_budget_s)
     return out
+
+
+def _se3_exp(xi):
+    xi = np.asarray(xi, np.float64)
+    rho, w = xi[:3], xi[3:]
+    th = float(np.linalg.norm(w))
+    K = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]])
+    if th < 1e-12:
+        R, V = np.eye(3) + K, np.eye(3) + 0.5 * K
+    else:
+        R = np.eye(3) + np.sin(th) / th * K + (1 - np.cos(th)) / th ** 2 * K @ K
+        V = np.eye(3) + (1 - np.cos(th)) / th ** 2 * K + (th - np.sin(th)) / th ** 3 * K @ K
+    T = np.eye(4)
+    T[:3, :3], T[:3, 3] = R, V @ rho
+    return T
+
+
+def _adjoint_bench(se, torch, m, sensor, T_gt, obs, flush, reps=20, gn_steps=50, delta=0.02):
+    """Differentiable render + adjoint against a held-out frame whose pose is perturbed by a
+    seeded 0.05 m / 3 deg twist: the forward + backward time (render, Huber gradient, adjoint
+    into the twist and every TSDF voxel), a central-difference check of the twist gradient with
+    the FP32 render (h = 1e-4, pixels where the render is smooth), and the pose error after
+    Gauss-Newton refinement with the adjoint's Jacobian rows."""
+    rng = np.random.default_rng(1005)
+    a, w = rng.normal(size=3), rng.normal(size=3)
+    xi0 = np.concatenate([0.05 * a / np.linalg.norm(a), np.deg2rad(3.0) * w / np.linalg.norm(w)])
+    T = _se3_exp(xi0) @ T_gt
+    H, W = sensor.height, sensor.width
+    obs64 = obs.to(torch.float64)
+    vg = torch.zeros((m.max_blocks, 512), dtype=torch.float32, device="cuda")
+    tw = torch.zeros(6, dtype=torch.float64, device="cuda")
+    depth = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def fwd_bwd(Tp):
+        se.render_depth(m, sensor, Tp, out=depth)
+        r = torch.where((depth > 0) & (obs > 0), depth - obs, torch.zeros_like(depth))
+        g = torch.clamp(r, -delta, delta).contiguous()
+        tw.zero_()
+        vg.zero_()
+        se.raycast_adjoint(m, sensor, Tp, g, twist_grad=tw, voxel_grad=vg)
+
+    for _ in range(3):
+        fwd_bwd(T)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for e0, e1 in ev:
+        flush.zero_()
+        e0.record(stream)
+        fwd_bwd(T)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
+
+    def loss_of(d):
+        r = torch.where(mask, d.to(torch.float64) - obs64, torch.zeros_like(obs64))
+        a_ = r.abs()
+        return float(torch.where(a_ <= delta, 0.5 * r * r, delta * (a_ - 0.5 * delta)).sum())
+
+    # central differences over the twist with the FP32 render
+    h = 1e-4
+    base = se.render_depth(m, sensor, T).clone()
+    ds = []
+    for j in range(6):
+        e = np.zeros(6)
+        e[j] = h
+        ds.append((se.render_depth(m, sensor, _se3_exp(e) @ T).clone(),
+                   se.render_depth(m, sensor, _se3_exp(-e) @ T).clone()))
+    mask = (base > 0) & (obs > 0)
+    for dp, dm in ds:
+        mask &= (dp > 0) & (dm > 0) & ((dp.double() - 2 * base.double() + dm.double()).abs() < 2e-5)
+    fd = np.array([(loss_of(dp) - loss_of(dm)) / (2 * h) for dp, dm in ds])
+    g = torch.where(mask, torch.clamp(base - obs, -delta, delta), torch.zeros_like(base)).contiguous()
+    tw.zero_()
+    se.raycast_adjoint(m, sensor, T, g, twist_grad=tw)
+    adj = tw.cpu().numpy()
+    fd_rel = float(np.linalg.norm(adj - fd) / max(np.linalg.norm(fd), 1e-30))
+
+    # Gauss-Newton refinement (Huber IRLS weights) with the adjoint's per-pixel rows
+    jac = torch.zeros((H, W, 6), dtype=torch.float32, device="cuda")
+    Tk = T.copy()
+    for _ in range(gn_steps):
+        d = se.render_depth(m, sensor, Tk)
+        valid = ((d > 0) & (obs > 0)).reshape(-1)
+        r = (d.double() - obs64).reshape(-1)[valid]
+        jac.zero_()
+        se.raycast_adjoint(m, sensor, Tk, None, twist_grad=tw, jac=jac)
+        J = jac.reshape(-1, 6).double()[valid]
+        wgt = torch.clamp(delta / r.abs().clamp_min(1e-12), max=1.0)
+        Hm = (J * wgt[:, None]).T @ J
+        Hm = Hm + 1e-6 * torch.trace(Hm) * torch.eye(6, dtype=torch.float64, device="cuda")
+        b = J.T @ torch.clamp(r, -delta, delta)
+        Tk = _se3_exp((-torch.linalg.solve(Hm, b)).cpu().numpy()) @ Tk
+
+    def pose_err(Ta):
+        dT = np.linalg.inv(T_gt) @ Ta
+        return (float(np.linalg.norm(dT[:3, 3])),
+                float(np.degrees(np.arccos(np.clip((np.trace(dT[:3, :3]) - 1) / 2, -1, 1)))))
+
+    t0, r0 = pose_err(T)
+    t1, r1 = pose_err(Tk)
+    return {"workload": "640x480 differentiable depth render of the headline map after all its frames, "
+                        "Huber (0.02 m) loss against the next (held-out) frame, start pose perturbed by "
+                        "0.05 m / 3 deg",
+            "fwd_bwd_ms": ms, "fwd_bwd_per_s": 1e3 / ms,
+            "fd_rel_err": fd_rel, "fd_h": h, "fd_pixels": int(mask.sum()),
+            "gn_steps": gn_steps, "pose_err_start": {"m": t0, "deg": r0},
+            "pose_err_final": {"m": t1, "deg": r1}}
 
 
 # --------------------------------------------------------------------- CPU oracle arm --
