@@ -1,6 +1,6 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles ``se_oracle.cpp`` into ``oracle/_build/libse_oracle.so`` with OpenMP and
+Compiles ``se_oracle.cpp`` (TSDF maps, ICP) and ``se_oracle_occ.cpp`` (occupancy maps) into ``oracle/_build/libse_oracle.so`` with OpenMP and
 ``-ffp-contract=off`` (no fused multiply-add, on x86-64 and aarch64 alike) so that its float
 arithmetic follows the operation order written in the source.
 """
@@ -11,8 +11,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libse_oracle.so")
-SOURCES = [os.path.join(HERE, "se_oracle.cpp")]
-HEADERS = [os.path.join(HERE, "se_oracle.h")]
+SOURCES = [os.path.join(HERE, f) for f in ("se_oracle.cpp", "se_oracle_occ.cpp")]
+HEADERS = [os.path.join(HERE, f) for f in ("se_oracle.h", "oracle_common.hpp")]
 
 
 def _stale() -> bool:
@@ -30,7 +30,7 @@ def build(force: bool = False) -> str:
     tmp = LIB_PATH + ".tmp"
     cmd = [
         "g++", "-std=c++17", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
-        "-fPIC", "-shared", "-Wall", "-Wno-unknown-pragmas",
+        "-fPIC", "-shared", "-Wall", "-Wno-unknown-pragmas", "-Wno-unused-function",
         *SOURCES, "-o", tmp,
     ]
     subprocess.run(cmd, check=True)

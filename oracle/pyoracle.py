@@ -55,6 +55,21 @@ def lib():
             "so_map_is_multires": (C.c_int, [vp]),
             "so_map_mr_blocks": (None, [vp, vp, vp, vp, vp, vp, vp, vp]),
             "so_map_destroy": (None, [vp]),
+            "so_occ_map_create": (vp, [f32p, C.c_float, vp]),
+            "so_occ_map_destroy": (None, [vp]),
+            "so_occ_map_create_cfg": (vp, [f32p, C.c_float, vp, vp]),
+            "so_occ_get_data": (None, [vp, f32p, f32p]),
+            "so_occ_get_field_interp": (C.c_int, [vp, f32p, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
+            "so_occ_map_size": (C.c_int, [vp]),
+            "so_occ_integrate_depth": (None, [vp, f32p, C.POINTER(Pinhole), f32p, C.c_int,
+                                              C.POINTER(OccStats)]),
+            "so_occ_num_blocks": (C.c_longlong, [vp]),
+            "so_occ_num_nodes": (C.c_longlong, [vp]),
+            "so_occ_blocks": (None, [vp, vp, vp, vp, vp, vp, vp]),
+            "so_occ_nodes": (C.c_longlong, [vp, vp, vp, vp, vp]),
+            "so_occ_aabb": (C.c_int, [vp, i32p, i32p]),
+            "so_occ_depth_sigma": (None, [f32p, C.c_int, C.c_float, f32p]),
+            "so_occ_pooling_image": (C.c_int, [f32p, C.c_int, C.c_int, vp, C.POINTER(C.c_float)]),
             "so_render_depth_f64": (None, [vp, C.POINTER(Pinhole), f64p, f64p]),
             "so_raycast_adjoint_f64": (None, [vp, C.POINTER(Pinhole), f64p, vp, f64p, vp, vp]),
             "so_map_set_voxel": (None, [vp, i32p, C.c_float, C.c_float]),
@@ -121,6 +136,105 @@ def pinhole(width, height, fx, fy, cx, cy, near_plane, far_plane) -> Pinhole:
 
 def _m16(T):
     return np.ascontiguousarray(np.asarray(T, dtype=np.float32).reshape(16))
+
+
+class OccStats(C.Structure):
+    _fields_ = [("n_blocks_listed", C.c_longlong), ("n_nodes_listed", C.c_longlong),
+                ("n_blocks_freed", C.c_longlong), ("n_nodes_pruned", C.c_longlong)]
+
+
+class OracleOccMap:
+    """se::OccupancyMap<Res::Multi> restated on the CPU (pinhole integration)."""
+
+    # the field configuration of a YAML "data" node, in so_occ_map_create_cfg's order
+    CFG_KEYS = ("k_sigma", "sigma_min_factor", "sigma_max_factor", "k_tau", "tau_min_factor",
+                "tau_max_factor", "log_odd_min", "log_odd_max", "fs_integr_scale")
+
+    def __init__(self, dim, res, T_MW=None, **cfg):
+        d = np.ascontiguousarray(np.broadcast_to(np.asarray(dim, np.float32), (3,)))
+        self._tmw = None if T_MW is None else _m16(T_MW)
+        tmw = None if self._tmw is None else self._tmw.ctypes.data
+        if cfg:
+            defaults = dict(k_sigma=0.052, sigma_min_factor=1.5, sigma_max_factor=6.0, k_tau=0.026,
+                            tau_min_factor=6.0, tau_max_factor=16.0, log_odd_min=-5.015,
+                            log_odd_max=5.015, fs_integr_scale=1)
+            defaults.update(cfg)
+            self._cfg = np.array([defaults[k] for k in self.CFG_KEYS], np.float32)
+            self.h = lib().so_occ_map_create_cfg(d, float(res), tmw, self._cfg.ctypes.data)
+        else:
+            self.h = lib().so_occ_map_create(d, float(res), tmw)
+        self.res = float(res)
+
+    def get_data(self, p):
+        out = np.zeros(3, np.float32)
+        lib().so_occ_get_data(self.h, np.ascontiguousarray(p, np.float32), out)
+        return out
+
+    def get_field_interp(self, p):
+        v, sc = C.c_float(), C.c_int()
+        ok = lib().so_occ_get_field_interp(self.h, np.ascontiguousarray(p, np.float32), C.byref(v), C.byref(sc))
+        return (v.value, sc.value) if ok else None
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().so_occ_map_destroy(self.h)
+            self.h = None
+
+    @property
+    def size(self):
+        return lib().so_occ_map_size(self.h)
+
+    def integrate_depth(self, depth, sensor, T_WC, timestamp=0):
+        st = OccStats()
+        depth = np.ascontiguousarray(depth, dtype=np.float32)
+        lib().so_occ_integrate_depth(self.h, depth, C.byref(sensor), _m16(T_WC), int(timestamp), C.byref(st))
+        return st
+
+    def blocks(self):
+        """(coords i32[N,3], scales i32[N,3] (current, min, buffer), counts i64[N,4],
+        mean / min / max f32[N,585,3] (occupancy, weight, observed))."""
+        n = int(lib().so_occ_num_blocks(self.h))
+        coords = np.zeros((n, 3), np.int32)
+        scales = np.zeros((n, 3), np.int32)
+        counts = np.zeros((n, 4), np.int64)
+        arrs = [np.zeros((n, 585, 3), np.float32) for _ in range(3)]
+        if n:
+            lib().so_occ_blocks(self.h, coords.ctypes.data, scales.ctypes.data, counts.ctypes.data,
+                                *[a.ctypes.data for a in arrs])
+        return (coords, scales, counts, *arrs)
+
+    def nodes(self):
+        """(coords+size i32[N,4], min f32[N,3], max f32[N,3], leaf i32[N]) depth first."""
+        n = int(lib().so_occ_nodes(self.h, None, None, None, None))
+        c = np.zeros((n, 4), np.int32)
+        mn = np.zeros((n, 3), np.float32)
+        mx = np.zeros((n, 3), np.float32)
+        lf = np.zeros(n, np.int32)
+        lib().so_occ_nodes(self.h, c.ctypes.data, mn.ctypes.data, mx.ctypes.data, lf.ctypes.data)
+        return c, mn, mx, lf
+
+    def aabb(self):
+        mn = np.zeros(3, np.int32)
+        mx = np.zeros(3, np.int32)
+        return (mn, mx) if lib().so_occ_aabb(self.h, mn, mx) else None
+
+
+def occ_depth_sigma(depth, res):
+    depth = np.ascontiguousarray(depth, np.float32)
+    out = np.zeros_like(depth)
+    lib().so_occ_depth_sigma(depth.reshape(-1), depth.size, float(res), out.reshape(-1))
+    return out
+
+
+def pooling_image(depth):
+    """(levels f32[L+1, h, w, 4] of (min, max, crossing, known), max_value)."""
+    depth = np.ascontiguousarray(depth, np.float32)
+    h, w = depth.shape
+    mv = C.c_float()
+    L = lib().so_occ_pooling_image(depth.reshape(-1), w, h, None, C.byref(mv))
+    out = np.zeros((L + 1, h, w, 4), np.float32)
+    lib().so_occ_pooling_image(depth.reshape(-1), w, h, out.ctypes.data, C.byref(mv))
+    return out, mv.value
 
 
 class OracleMap:

@@ -142,6 +142,48 @@ void so_raycast_adjoint_f64(const so_map* map, const so_pinhole* sensor, const d
 /* Overwrite one voxel of an allocated single-res block (no-op elsewhere). */
 void so_map_set_voxel(so_map* map, const int32_t voxel_coord[3], float tsdf, float weight);
 
+/* --------------------------------------------------------- multi-res occupancy maps -- */
+/* Map<Data<Occupancy>, Res::Multi, 8> with the reference's default field configuration
+ * (data_field.hpp:52-71). T_MW may be NULL (translation dim/2). */
+typedef struct so_occ_map so_occ_map;
+typedef struct {
+    long long n_blocks_listed; /* blocks the VolumeCarver returned for update */
+    long long n_nodes_listed;  /* free-space nodes the VolumeCarver returned */
+    long long n_blocks_freed;  /* blocks freed below those nodes */
+    long long n_nodes_pruned;  /* nodes whose children were deleted by the propagation */
+} so_occ_stats;
+so_occ_map* so_occ_map_create(const float dim[3], float res, const float* T_MW);
+/* The same with the field configuration of a YAML "data" node: cfg = {k_sigma,
+ * sigma_min_factor, sigma_max_factor, k_tau, tau_min_factor, tau_max_factor, log_odd_min,
+ * log_odd_max, fs_integr_scale}. */
+so_occ_map* so_occ_map_create_cfg(const float dim[3], float res, const float* T_MW, const float cfg[9]);
+void so_occ_map_destroy(so_occ_map* map);
+/* Map::getData / Map::getFieldInterp for occupancy maps; data as (occupancy, weight,
+ * observed); the interpolation returns 0 for nullopt. */
+void so_occ_get_data(const so_occ_map* map, const float point_W[3], float out[3]);
+int so_occ_get_field_interp(const so_occ_map* map, const float point_W[3], float* value, int* scale);
+int so_occ_map_size(const so_occ_map* map);
+/* MapIntegrator<OccupancyMap<Res::Multi>>::integrateDepth for a pinhole camera. */
+void so_occ_integrate_depth(so_occ_map* map, const float* depth, const so_pinhole* sensor,
+                            const float T_WC[16], int timestamp, so_occ_stats* stats);
+long long so_occ_num_blocks(const so_occ_map* map);
+long long so_occ_num_nodes(const so_occ_map* map);
+/* Live blocks in allocation order; every pointer may be NULL. coords: 3 ints; scales:
+ * (current, min, buffer); counts: (curr_integr, curr_observed, buffer_integr,
+ * buffer_observed); mean / min / max: 585 entries of (occupancy, weight, observed). */
+void so_occ_blocks(const so_occ_map* map, int32_t* coords, int32_t* scales, int64_t* counts,
+                   float* mean, float* min_data, float* max_data);
+/* Nodes reachable from the root (depth first): coords (x, y, z, size), min / max data as
+ * (occupancy, weight, observed), leaf flag. Returns the count (pass NULLs to count). */
+long long so_occ_nodes(const so_occ_map* map, int32_t* coords, float* min_data, float* max_data,
+                       int32_t* leaf);
+int so_occ_aabb(const so_occ_map* map, int32_t mn[3], int32_t mx[3]);
+/* uncert::depth_sigma with the default linear model. */
+void so_occ_depth_sigma(const float* depth, int n, float res, float* sigma);
+/* DensePoolingImage<PinholeCamera>: (max_level + 1) * w * h pixels of (min, max, crossing,
+ * known) into out (may be NULL); returns max_level. */
+int so_occ_pooling_image(const float* depth, int w, int h, float* out, float* max_value);
+
 /* Morton key operations (key_util_impl.hpp). */
 uint64_t so_expand(uint64_t value);
 uint64_t so_compact(uint64_t value);
