@@ -61,13 +61,27 @@ typedef struct {
     float res;         /* metres per voxel */
     float T_MW[16];    /* world-to-map transform; set has_T_MW = 0 for translation(dim/2) */
     int has_T_MW;
-    int field;         /* se_gpu_field; only SE_GPU_FIELD_TSDF in this library */
+    int field;         /* se_gpu_field: TSDF, or occupancy (multi-res only) */
     int res_type;      /* se_gpu_res: single-res (Map<.., Res::Single>) or multi-res TSDF */
     int storage;       /* se_gpu_storage */
     float truncation_boundary_factor; /* reference default 8 */
     float max_weight;  /* reference default 100; must be an integer <= 65535 */
     int64_t max_blocks; /* block pool capacity (8^3-voxel blocks) */
 } se_gpu_map_config;
+
+/* se::FieldData<Occupancy>::Config (include/se/map/data_field.hpp:52-71): the parameters a YAML
+ * "data" node sets. max_weight keeps the reference's default floor(|-100 / (0.97 * -5.015)|). */
+typedef struct {
+    float k_sigma;          /* 0.052 */
+    float sigma_min_factor; /* 1.5 */
+    float sigma_max_factor; /* 6 */
+    float k_tau;            /* 0.026 */
+    float tau_min_factor;   /* 6 */
+    float tau_max_factor;   /* 16 */
+    float log_odd_min;      /* -5.015 */
+    float log_odd_max;      /* 5.015 */
+    int fs_integr_scale;    /* 1 */
+} se_gpu_occupancy_config;
 
 /* se::PinholeCamera::Config (include/se/sensor/sensor.hpp:29-57, pinhole_camera.hpp). */
 typedef struct {
@@ -111,6 +125,12 @@ SE_GPU_API int se_gpu_abi_version(void);
  * (include/se/map/octree/impl/octree_impl.hpp:14-19). Allocates the block pool and hash on the
  * current CUDA device. */
 SE_GPU_API se_gpu_status se_gpu_map_create(const se_gpu_map_config* config, se_gpu_map** map);
+/* The same for an occupancy map (field SE_GPU_FIELD_OCCUPANCY, res_type SE_GPU_RES_MULTI) with
+ * its field configuration (NULL: the reference's defaults); se_gpu_map_create uses the defaults.
+ * max_blocks bounds the block pool; the node pool holds max_blocks / 2 + 4096 nodes. */
+SE_GPU_API se_gpu_status se_gpu_map_create_occupancy(const se_gpu_map_config* config,
+                                                     const se_gpu_occupancy_config* occupancy,
+                                                     se_gpu_map** map);
 SE_GPU_API se_gpu_status se_gpu_map_destroy(se_gpu_map* map);
 /* Octree side in voxels (Octree::getSize()) and map side in metres (Map::getDim()). */
 SE_GPU_API se_gpu_status se_gpu_map_size(const se_gpu_map* map, int* size, float* dim_m);
@@ -153,6 +173,24 @@ SE_GPU_API se_gpu_status se_gpu_map_download_multires(const se_gpu_map* map, int
                                            uint64_t* keys, int32_t* coords, float* tsdf,
                                            float* weight, float* past_tsdf, float* past_weight,
                                            int32_t* scales, int64_t* count);
+/* Occupancy maps. Counters of the last integrate_depth: {blocks the VolumeCarver listed,
+ * free-space nodes it listed, blocks freed below those nodes, nodes pruned}; synchronises. */
+SE_GPU_API se_gpu_status se_gpu_map_occupancy_stats(se_gpu_map* map, int64_t stats[4]);
+/* Live blocks (pool order), up to capacity: coords (3 ints), scales (current, min, buffer),
+ * counts (current integrations, current observed, buffer integrations, buffer observed), and
+ * the 585-entry mean / min / max pyramids (offsets as for multi-res TSDF) of (occupancy,
+ * weight, observed) with min / max at the finest scale equal to the mean data and the block's
+ * init data below it (BlockMultiRes<Occupancy>, include/se/map/octant/impl/block_impl.hpp:
+ * 206-855). Host pointers, any may be NULL; synchronous; *count receives the live blocks. */
+SE_GPU_API se_gpu_status se_gpu_map_download_occupancy(const se_gpu_map* map, int64_t capacity,
+                                                       int32_t* coords, int32_t* scales,
+                                                       int64_t* counts, float* mean, float* min_data,
+                                                       float* max_data, int64_t* count);
+/* Nodes reachable from the root, depth first in child order: (x, y, z, size), min / max data
+ * as (occupancy, weight, observed), leaf flag. Synchronous; *count receives the number. */
+SE_GPU_API se_gpu_status se_gpu_map_download_nodes(const se_gpu_map* map, int64_t capacity,
+                                                   int32_t* coords, float* min_data, float* max_data,
+                                                   int32_t* leaf, int64_t* count);
 /* Block upload (checkpoint restore, test set-up, single-res maps only): allocates the blocks with the given keys
  * (Morton code << 5 | 3, as written by se_gpu_map_download_blocks) if they are not allocated,
  * then overwrites their 512 voxels from tsdf / weight (host, 512 floats per block; weights are

@@ -38,6 +38,17 @@ class _MapConfig(C.Structure):
                 ("max_weight", C.c_float), ("max_blocks", C.c_int64)]
 
 
+class _OccupancyConfig(C.Structure):
+    _fields_ = [("k_sigma", C.c_float), ("sigma_min_factor", C.c_float), ("sigma_max_factor", C.c_float),
+                ("k_tau", C.c_float), ("tau_min_factor", C.c_float), ("tau_max_factor", C.c_float),
+                ("log_odd_min", C.c_float), ("log_odd_max", C.c_float), ("fs_integr_scale", C.c_int)]
+
+
+OCCUPANCY_DEFAULTS = dict(k_sigma=0.052, sigma_min_factor=1.5, sigma_max_factor=6.0, k_tau=0.026,
+                          tau_min_factor=6.0, tau_max_factor=16.0, log_odd_min=-5.015,
+                          log_odd_max=5.015, fs_integr_scale=1)
+
+
 class _Pinhole(C.Structure):
     _fields_ = [("width", C.c_int), ("height", C.c_int), ("fx", C.c_float), ("fy", C.c_float),
                 ("cx", C.c_float), ("cy", C.c_float), ("near_plane", C.c_float),
@@ -64,6 +75,12 @@ SIGNATURES = {
     "se_gpu_abi_version": (C.c_int, []),
     "se_gpu_map_create": (C.c_int, [C.POINTER(_MapConfig), C.POINTER(_VP)]),
     "se_gpu_map_destroy": (C.c_int, [_VP]),
+    "se_gpu_map_create_occupancy": (C.c_int, [C.POINTER(_MapConfig), C.POINTER(_OccupancyConfig),
+                                              C.POINTER(_VP)]),
+    "se_gpu_map_occupancy_stats": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
+    "se_gpu_map_download_occupancy": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP,
+                                                C.POINTER(C.c_int64)]),
+    "se_gpu_map_download_nodes": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, C.POINTER(C.c_int64)]),
     "se_gpu_map_size": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "se_gpu_map_check": (C.c_int, [_VP]),
     "se_gpu_integrate_depth": (C.c_int, [_VP, _VP, C.POINTER(_Pinhole), _F16, C.c_int, _VP]),
@@ -192,7 +209,8 @@ class Map:
     GPU: block hash + block pool of 8^3 voxels (585-entry voxel pyramids for multi-res)."""
 
     def __init__(self, dim, res, truncation_boundary_factor=8.0, max_weight=100.0,
-                 storage="f32", max_blocks=1 << 20, T_MW=None, res_type="single"):
+                 storage="f32", max_blocks=1 << 20, T_MW=None, res_type="single", field="tsdf",
+                 occupancy=None):
         cfg = _MapConfig()
         d = np.broadcast_to(np.asarray(dim, np.float32), (3,))
         cfg.dim = (C.c_float * 3)(*[float(v) for v in d])
@@ -200,7 +218,7 @@ class Map:
         if T_MW is not None:
             cfg.T_MW = (C.c_float * 16)(*[float(v) for v in np.asarray(T_MW, np.float32).reshape(16)])
             cfg.has_T_MW = 1
-        cfg.field = 0
+        cfg.field = {"tsdf": 0, "occupancy": 1}[field]
         cfg.res_type = {"single": 0, "multi": 1}[res_type]
         cfg.storage = {"f32": 0, "f16": 1}[storage]
         cfg.truncation_boundary_factor = float(truncation_boundary_factor)
@@ -208,7 +226,15 @@ class Map:
         cfg.max_blocks = int(max_blocks)
         self._L = library()
         h = C.c_void_p()
-        _check(self._L.se_gpu_map_create(C.byref(cfg), C.byref(h)), "se_gpu_map_create")
+        self.field = field
+        if field == "occupancy":
+            oc = dict(OCCUPANCY_DEFAULTS)
+            oc.update(occupancy or {})
+            occ = _OccupancyConfig(*[oc[k] for k, _ in _OccupancyConfig._fields_])
+            _check(self._L.se_gpu_map_create_occupancy(C.byref(cfg), C.byref(occ), C.byref(h)),
+                   "se_gpu_map_create_occupancy")
+        else:
+            _check(self._L.se_gpu_map_create(C.byref(cfg), C.byref(h)), "se_gpu_map_create")
         self.h = h
         self.res = float(res)
         self.storage = storage
@@ -265,6 +291,45 @@ class Map:
                 tsdf.ctypes.data if voxels else None, weight.ctypes.data if voxels else None,
                 ts.ctypes.data, C.byref(cnt)), "download_blocks")
         return keys, coords, tsdf, weight, ts
+
+    def occupancy_stats(self):
+        """(blocks listed, free-space nodes listed, blocks freed, nodes pruned) of the last frame."""
+        st = (C.c_int64 * 4)()
+        _check(self._L.se_gpu_map_occupancy_stats(self.h, st), "occupancy_stats")
+        return tuple(int(v) for v in st)
+
+    def download_occupancy(self):
+        """Live blocks: (coords i32[N,3], scales i32[N,3], counts i64[N,4], mean / min / max
+        f32[N,585,3] of (occupancy, weight, observed))."""
+        n = C.c_int64()
+        _check(self._L.se_gpu_map_download_occupancy(self.h, 0, None, None, None, None, None, None,
+                                                     C.byref(n)), "download_occupancy")
+        k = n.value
+        coords = np.zeros((k, 3), np.int32)
+        scales = np.zeros((k, 3), np.int32)
+        counts = np.zeros((k, 4), np.int64)
+        arrs = [np.zeros((k, 585, 3), np.float32) for _ in range(3)]
+        if k:
+            _check(self._L.se_gpu_map_download_occupancy(
+                self.h, k, coords.ctypes.data, scales.ctypes.data, counts.ctypes.data,
+                *[a.ctypes.data for a in arrs], C.byref(n)), "download_occupancy")
+        return (coords, scales, counts, *arrs)
+
+    def download_nodes(self):
+        """Nodes reachable from the root, depth first: (coords+size i32[N,4], min f32[N,3],
+        max f32[N,3], leaf i32[N])."""
+        n = C.c_int64()
+        _check(self._L.se_gpu_map_download_nodes(self.h, 0, None, None, None, None, C.byref(n)),
+               "download_nodes")
+        k = n.value
+        c = np.zeros((k, 4), np.int32)
+        mn = np.zeros((k, 3), np.float32)
+        mx = np.zeros((k, 3), np.float32)
+        lf = np.zeros(k, np.int32)
+        _check(self._L.se_gpu_map_download_nodes(self.h, k, c.ctypes.data, mn.ctypes.data,
+                                                 mx.ctypes.data, lf.ctypes.data, C.byref(n)),
+               "download_nodes")
+        return c, mn, mx, lf
 
     def download_multires(self):
         """Multi-res maps: (keys u64[N], coords i32[N,3], tsdf, weight, past_tsdf, past_weight

@@ -76,6 +76,10 @@ se_gpu_status se_gpu_frame_create(se_gpu_map* map, se_gpu_tracker* tracker, cons
         set_last_error("se_gpu_frame_create: invalid argument");
         return SE_GPU_ERR_BAD_ARG;
     }
+    if (map->occ) {
+        set_last_error("se_gpu_frame_create: TSDF maps only");
+        return SE_GPU_ERR_NOT_SUPPORTED;
+    }
     se_gpu_frame* f = new se_gpu_frame();
     std::memset(f, 0, sizeof(*f));
     f->map = map;

@@ -259,5 +259,7 @@ extern "C" se_gpu_status se_gpu_integrate_depth(se_gpu_map* map, const float* de
     }
     cudaStream_t stream = (cudaStream_t) stream_p;
     map->last_stream = stream;
+    if (map->occ)
+        return occ_integrate(map->occ, depth_dev, *sensor, T_WC, timestamp, stream);
     return enqueue_integrate(map, depth_dev, *sensor, T_WC, nullptr, timestamp, stream);
 }

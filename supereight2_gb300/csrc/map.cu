@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "multires.cuh"
+#include "pipeline.cuh"
 #include "se_gpu_internal.cuh"
 
 namespace se_gpu {
@@ -104,6 +105,8 @@ se_gpu_status se_gpu_map_create(const se_gpu_map_config* cfg, se_gpu_map** out)
         return SE_GPU_ERR_BAD_ARG;
     }
     *out = nullptr;
+    if (cfg->field == SE_GPU_FIELD_OCCUPANCY)
+        return se_gpu_map_create_occupancy(cfg, nullptr, out);
     if (cfg->field != SE_GPU_FIELD_TSDF || (cfg->res_type != SE_GPU_RES_SINGLE && cfg->res_type != SE_GPU_RES_MULTI)) {
         set_last_error("se_gpu_map_create: only TSDF maps (single- or multi-resolution) are supported");
         return SE_GPU_ERR_NOT_SUPPORTED;
@@ -138,6 +141,7 @@ se_gpu_status se_gpu_map_create(const se_gpu_map_config* cfg, se_gpu_map** out)
 
     se_gpu_map* map = new se_gpu_map();
     std::memset(&map->dev, 0, sizeof(map->dev));
+    map->occ = nullptr;
     map->iparams = nullptr;
     map->rparams = nullptr;
     map->timestamp_dev = nullptr;
@@ -223,10 +227,72 @@ se_gpu_status se_gpu_map_create(const se_gpu_map_config* cfg, se_gpu_map** out)
     return SE_GPU_OK;
 }
 
+se_gpu_status se_gpu_map_create_occupancy(const se_gpu_map_config* cfg, const se_gpu_occupancy_config* occ,
+                                          se_gpu_map** out)
+{
+    if (!cfg || !out) {
+        set_last_error("se_gpu_map_create_occupancy: null argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    *out = nullptr;
+    if (cfg->res_type != SE_GPU_RES_MULTI) {
+        set_last_error("se_gpu_map_create_occupancy: occupancy maps are multi-resolution (res_type SE_GPU_RES_MULTI)");
+        return SE_GPU_ERR_NOT_SUPPORTED;
+    }
+    if (!(cfg->res > 0.0f) || cfg->max_blocks <= 0 || cfg->max_blocks > (1ll << 26)) {
+        set_last_error("se_gpu_map_create_occupancy: invalid configuration");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    int dev = 0;
+    SE_CUDA_TRY(cudaGetDevice(&dev));
+    int major = 0, minor = 0;
+    SE_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    SE_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+    if (major != 10 || minor != 3) {
+        set_last_error("se_gpu: device %d has compute capability %d.%d; this build targets sm_103a", dev, major,
+                       minor);
+        return SE_GPU_ERR_NO_DEVICE;
+    }
+    const float dmax = std::fmax(std::fmax(cfg->dim[0], cfg->dim[1]), cfg->dim[2]);
+    const int requested = (int) std::ceil(dmax / cfg->res);
+    int size = 1;
+    while (size < (requested > 2 * kBlockSize ? requested : 2 * kBlockSize))
+        size <<= 1;
+    if (size > 8192) {
+        set_last_error("se_gpu_map_create_occupancy: octree side %d voxels exceeds the supported 8192", size);
+        return SE_GPU_ERR_NOT_SUPPORTED;
+    }
+    se_gpu_map* map = new se_gpu_map();
+    std::memset(&map->dev, 0, sizeof(map->dev));
+    map->config = *cfg;
+    map->device = dev;
+    map->last_stream = 0;
+    map->iparams = nullptr;
+    map->rparams = nullptr;
+    map->timestamp_dev = nullptr;
+    map->occ = nullptr;
+    map->dev.size = size;
+    map->dev.res = cfg->res;
+    map->dev.dim = (float) size * cfg->res;
+    map->dev.res_type = -1; // not a TSDF map
+    const se_gpu_status st = occ_map_create(cfg, occ, size, &map->occ);
+    if (st != SE_GPU_OK) {
+        delete map;
+        return st;
+    }
+    *out = map;
+    return SE_GPU_OK;
+}
+
 se_gpu_status se_gpu_map_destroy(se_gpu_map* map)
 {
     if (!map)
         return SE_GPU_OK;
+    if (map->occ) {
+        occ_map_destroy(map->occ);
+        delete map;
+        return SE_GPU_OK;
+    }
     MapDevice& m = map->dev;
     cudaFree(m.hash);
     cudaFree(m.block_coord);
@@ -268,6 +334,8 @@ se_gpu_status se_gpu_map_check(se_gpu_map* map)
         return SE_GPU_ERR_BAD_ARG;
     }
     SE_CUDA_TRY(cudaStreamSynchronize(map->last_stream));
+    if (map->occ)
+        return occ_check(map->occ);
     int err = 0;
     SE_CUDA_TRY(cudaMemcpy(&err, map->dev.counters + kCntError, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) {
@@ -288,6 +356,10 @@ se_gpu_status se_gpu_map_integrate_stats(se_gpu_map* map, se_gpu_integrate_stats
         set_last_error("se_gpu_map_integrate_stats: null argument");
         return SE_GPU_ERR_BAD_ARG;
     }
+    if (map->occ) {
+        set_last_error("se_gpu_map_integrate_stats: occupancy maps report se_gpu_map_occupancy_stats");
+        return SE_GPU_ERR_NOT_SUPPORTED;
+    }
     int c[kNumCounters];
     SE_CUDA_TRY(cudaStreamSynchronize(map->last_stream));
     SE_CUDA_TRY(cudaMemcpy(c, map->dev.counters, sizeof(c), cudaMemcpyDeviceToHost));
@@ -307,6 +379,10 @@ se_gpu_status se_gpu_map_download_blocks(const se_gpu_map* map, int64_t capacity
     if (!map || capacity < 0) {
         set_last_error("se_gpu_map_download_blocks: invalid argument");
         return SE_GPU_ERR_BAD_ARG;
+    }
+    if (map->occ) {
+        set_last_error("se_gpu_map_download_blocks: occupancy maps use se_gpu_map_download_occupancy");
+        return SE_GPU_ERR_NOT_SUPPORTED;
     }
     const MapDevice& m = map->dev;
     SE_CUDA_TRY(cudaStreamSynchronize(map->last_stream));
@@ -361,7 +437,7 @@ se_gpu_status se_gpu_map_upload_blocks(se_gpu_map* map, int64_t n, const uint64_
         set_last_error("se_gpu_map_upload_blocks: invalid argument");
         return SE_GPU_ERR_BAD_ARG;
     }
-    if (map->dev.res_type != SE_GPU_RES_SINGLE) {
+    if (map->occ || map->dev.res_type != SE_GPU_RES_SINGLE) {
         set_last_error("se_gpu_map_upload_blocks: single-resolution maps only");
         return SE_GPU_ERR_NOT_SUPPORTED;
     }
@@ -459,6 +535,10 @@ se_gpu_status se_gpu_map_download_multires(const se_gpu_map* map, int64_t capaci
 
 se_gpu_status se_gpu_map_aabb(const se_gpu_map* map, int32_t mn[3], int32_t mx[3], int* empty)
 {
+    if (map && map->occ && mn && mx && empty) {
+        SE_CUDA_TRY(cudaStreamSynchronize(map->last_stream));
+        return occ_aabb(map->occ, mn, mx, empty);
+    }
     if (!map || !mn || !mx || !empty) {
         set_last_error("se_gpu_map_aabb: null argument");
         return SE_GPU_ERR_BAD_ARG;

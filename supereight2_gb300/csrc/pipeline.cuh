@@ -18,6 +18,14 @@ se_gpu_status enqueue_raycast(const se_gpu_map* map, const se_gpu_pinhole& senso
 // Multi-res TSDF update over the frame's block list (after carve and frustum).
 void enqueue_update_multires(const MapDevice& m, const Pinhole& s, const float* depth_dev,
                              const IntegrateParams* params, cudaStream_t stream);
+// Occupancy maps (occupancy.cu).
+se_gpu_status occ_map_create(const se_gpu_map_config* cfg, const se_gpu_occupancy_config* occ, int size,
+                             se_gpu_occ_map** out);
+void occ_map_destroy(se_gpu_occ_map* om);
+se_gpu_status occ_check(se_gpu_occ_map* om);
+se_gpu_status occ_aabb(const se_gpu_occ_map* om, int32_t mn[3], int32_t mx[3], int* empty);
+se_gpu_status occ_integrate(se_gpu_occ_map* om, const float* depth_dev, const se_gpu_pinhole& sensor,
+                            const float* T_WC16, int timestamp, cudaStream_t stream);
 // With pose12_dev_io the tracker starts from, and writes its result to, that device pose.
 se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const float* ref_pts, const float* ref_nrm,
                             const float* T_WS_host16, float* pose12_dev_io, cudaStream_t stream);

@@ -153,6 +153,10 @@ extern "C" se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinh
     }
     cudaStream_t stream = (cudaStream_t) stream_p;
     const_cast<se_gpu_map*>(map)->last_stream = stream;
+    if (map->occ) {
+        set_last_error("se_gpu_raycast: occupancy maps are not supported by this build's raycast");
+        return SE_GPU_ERR_NOT_SUPPORTED;
+    }
     return enqueue_raycast(map, *sensor, T_WS, nullptr, pts_dev, nrm_dev, scale_dev, stream);
 }
 
@@ -162,6 +166,10 @@ static se_gpu_status field_query(const se_gpu_map* map, int64_t n, const float* 
     if (!map || n < 0 || n > (1ll << 31) - 1 || (n > 0 && (!pts || !out))) {
         set_last_error("se_gpu_map_field_%s: invalid argument", grad ? "grad" : "interp");
         return SE_GPU_ERR_BAD_ARG;
+    }
+    if (map->occ) {
+        set_last_error("se_gpu_map_field_%s: TSDF maps only", grad ? "grad" : "interp");
+        return SE_GPU_ERR_NOT_SUPPORTED;
     }
     if (n == 0)
         return SE_GPU_OK;

@@ -410,8 +410,11 @@ __host__ __device__ inline Tf tf_from12(const float* m)
 
 } // namespace se_gpu
 
+struct se_gpu_occ_map;
+
 struct se_gpu_map {
     se_gpu::MapDevice dev;
+    se_gpu_occ_map* occ;              // occupancy maps only (dev holds the geometry)
     se_gpu_map_config config;
     int device;
     cudaStream_t last_stream;
