@@ -150,7 +150,8 @@ SE_GPU_API se_gpu_status se_gpu_integrate_depth(se_gpu_map* map, const float* de
 SE_GPU_API se_gpu_status se_gpu_map_integrate_stats(se_gpu_map* map, se_gpu_integrate_stats* stats);
 
 /* Replaces se::raycaster::raycast_volume(map, sensor, T_WS, points_W, normals_W, scale)
- * (include/se/map/raycaster.hpp:56-64, impl/raycaster_impl.hpp:456-627). Output device
+ * (include/se/map/raycaster.hpp:56-64, impl/raycaster_impl.hpp:456-627; occupancy maps:
+ * impl/raycaster_impl.hpp:32-452 with normals against the field gradient). Output device
  * images: pts_W and nrm_W are width*height*3 floats, scale is width*height int8 (may be NULL). */
 SE_GPU_API se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinhole* sensor,
                              const float T_WS[16], float* pts_W_dev, float* nrm_W_dev,

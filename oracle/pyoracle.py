@@ -68,6 +68,7 @@ def lib():
             "so_occ_blocks": (None, [vp, vp, vp, vp, vp, vp, vp]),
             "so_occ_nodes": (C.c_longlong, [vp, vp, vp, vp, vp]),
             "so_occ_aabb": (C.c_int, [vp, i32p, i32p]),
+            "so_occ_raycast_volume": (None, [vp, C.POINTER(Pinhole), f32p, f32p, f32p, i8p]),
             "so_occ_depth_sigma": (None, [f32p, C.c_int, C.c_float, f32p]),
             "so_occ_pooling_image": (C.c_int, [f32p, C.c_int, C.c_int, vp, C.POINTER(C.c_float)]),
             "so_render_depth_f64": (None, [vp, C.POINTER(Pinhole), f64p, f64p]),
@@ -164,6 +165,15 @@ class OracleOccMap:
         else:
             self.h = lib().so_occ_map_create(d, float(res), tmw)
         self.res = float(res)
+
+    def raycast(self, sensor, T_WS):
+        n = sensor.width * sensor.height
+        pts = np.zeros((sensor.height, sensor.width, 3), np.float32)
+        nrm = np.zeros((sensor.height, sensor.width, 3), np.float32)
+        scale = np.zeros((sensor.height, sensor.width), np.int8)
+        lib().so_occ_raycast_volume(self.h, C.byref(sensor), _m16(T_WS), pts.reshape(n * 3),
+                                    nrm.reshape(n * 3), scale.reshape(n))
+        return pts, nrm, scale
 
     def get_data(self, p):
         out = np.zeros(3, np.float32)

@@ -178,6 +178,9 @@ void so_occ_blocks(const so_occ_map* map, int32_t* coords, int32_t* scales, int6
 long long so_occ_nodes(const so_occ_map* map, int32_t* coords, float* min_data, float* max_data,
                        int32_t* leaf);
 int so_occ_aabb(const so_occ_map* map, int32_t mn[3], int32_t mx[3]);
+/* raycaster::raycast_volume for an occupancy map (raycaster_impl.hpp:32-452,537-627). */
+void so_occ_raycast_volume(const so_occ_map* map, const so_pinhole* sensor, const float T_WS[16],
+                           float* pts_W, float* nrm_W, int8_t* scale);
 /* uncert::depth_sigma with the default linear model. */
 void so_occ_depth_sigma(const float* depth, int n, float res, float* sigma);
 /* DensePoolingImage<PinholeCamera>: (max_level + 1) * w * h pixels of (min, max, crossing,

@@ -1257,6 +1257,371 @@ static bool occ_interp(const so_occ_map& m, V3 vf, int desired_scale, float& out
     return false;
 }
 
+/* fetcher::finest_octant (fetcher_impl.hpp:69-94) as a slot: the octant of size
+ * max(2^scale, 8) on the voxel's path, the deepest node when that node has no children, or -1. */
+static int occ_finest_octant(const OccOctree& o, const int32_t c[3], int scale_desired)
+{
+    const int size_desired = std::max(1 << scale_desired, 8);
+    int n = 0, child = -1;
+    for (int cs = o.size >> 1; cs >= size_desired; cs >>= 1) {
+        const int idx = ((c[0] & cs) > 0) + 2 * ((c[1] & cs) > 0) + 4 * ((c[2] & cs) > 0);
+        child = o.nodes[n].child[idx];
+        if (child == -1)
+            return o.nodes[n].is_leaf() ? n : -1;
+        if (slot_is_block(child))
+            return child;
+        n = child;
+    }
+    return child;
+}
+
+/* visitor::getMaxData (visitor_impl.hpp:815-835) */
+static OccData occ_max_data(const so_occ_map& m, const int32_t c[3], int scale_desired)
+{
+    const int slot = occ_finest_octant(m.octree, c, scale_desired);
+    if (slot == -1)
+        return OccData();
+    if (slot_is_block(slot)) {
+        OccBlock& b = const_cast<OccBlock&>(m.octree.blocks[slot_block(slot)]);
+        const int so = std::max(scale_desired, b.current_scale);
+        return b.max_at(so)[b.voxel_idx(c, so)];
+    }
+    return m.octree.nodes[slot].max_data;
+}
+
+/* visitor::getData(octree, block_ptr, voxel, scale_desired, scale_returned) for occupancy maps;
+ * false for no octant (the default data). */
+static bool occ_data_at(const so_occ_map& m, int hint_block, const int32_t c[3], int scale_desired, OccData& d,
+                        int& scale_returned)
+{
+    const OccBlock* hb = &m.octree.blocks[hint_block];
+    int slot = -2 - hint_block;
+    if (!(c[0] >= hb->coord[0] && c[0] <= hb->coord[0] + 7 && c[1] >= hb->coord[1] && c[1] <= hb->coord[1] + 7
+          && c[2] >= hb->coord[2] && c[2] <= hb->coord[2] + 7))
+        slot = m.octree.leaf(c);
+    if (slot == -1) {
+        d = OccData();
+        return false;
+    }
+    if (slot_is_block(slot)) {
+        OccBlock& b = const_cast<OccBlock&>(m.octree.blocks[slot_block(slot)]);
+        scale_returned = std::max(scale_desired, b.current_scale);
+        d = b.mean_at(scale_returned)[b.voxel_idx(c, scale_returned)];
+        return true;
+    }
+    scale_returned = scale_desired;
+    d = m.octree.nodes[slot].data();
+    return true;
+}
+
+/* visitor::getFieldGrad multi-res, desired scale 0 (visitor_impl.hpp:1257-1497), occupancy */
+static bool occ_grad(const so_occ_map& m, V3 vf, V3& g)
+{
+    const OccOctree& o = m.octree;
+    const int32_t c0[3] = {(int) vf.x, (int) vf.y, (int) vf.z};
+    const int q = occ_finest_octant(o, c0, 0);
+    if (q == -1)
+        return false;
+    if (!slot_is_block(q)) {
+        if (occ_valid(o.nodes[q].data())) {
+            g = v3(0.0f, 0.0f, 0.0f);
+            return true;
+        }
+        return false;
+    }
+    const int init = std::max(0, o.blocks[slot_block(q)].current_scale);
+    const int top = o.size - 1;
+    for (int scale = init; scale <= kOccMaxScale; ++scale) {
+        const int stride = 1 << scale;
+        const float inv = 1.0f / (float) stride;
+        const V3 sv = v3(inv * vf.x - 0.5f, inv * vf.y - 0.5f, inv * vf.z - 0.5f);
+        const V3 fac = v3(sv.x - std::floor(sv.x), sv.y - std::floor(sv.y), sv.z - std::floor(sv.z));
+        const int32_t base[3] = {stride * (int) sv.x, stride * (int) sv.y, stride * (int) sv.z};
+        int32_t ll[3], lu[3], ul[3], uu[3];
+        for (int i = 0; i < 3; ++i) {
+            ll[i] = std::max(base[i] - stride, 0);
+            lu[i] = std::max(base[i], 0);
+            ul[i] = std::min(base[i] + stride, top);
+            uu[i] = std::min(base[i] + 2 * stride, top);
+        }
+        const int oct = occ_finest_octant(o, base, scale);
+        if (oct == -1)
+            continue;
+        if (!slot_is_block(oct)) {
+            if (o.nodes[oct].is_leaf() && occ_valid(o.nodes[oct].data())) {
+                g = v3(0.0f, 0.0f, 0.0f);
+                return true;
+            }
+            continue;
+        }
+        const int32_t* X[32] = {ll, ll, ll, ll, lu, lu, lu, lu, lu, lu, lu, lu, lu, lu, lu, lu,
+                                ul, ul, ul, ul, ul, ul, ul, ul, ul, ul, ul, ul, uu, uu, uu, uu};
+        const int32_t* Y[32] = {lu, ul, lu, ul, ll, ll, lu, lu, lu, lu, ul, ul, ul, ul, uu, uu,
+                                ll, ll, lu, lu, lu, lu, ul, ul, ul, ul, uu, uu, lu, ul, lu, ul};
+        const int32_t* Z[32] = {lu, lu, ul, ul, lu, ul, ll, lu, ul, uu, ll, lu, ul, uu, lu, ul,
+                                lu, ul, ll, lu, ul, uu, ll, lu, ul, uu, lu, ul, lu, lu, ul, ul};
+        float v[32];
+        bool ok = true;
+        for (int i = 0; i < 32 && ok; ++i) {
+            const int32_t c[3] = {X[i][0], Y[i][1], Z[i][2]};
+            OccData d;
+            int rs = -1;
+            if (!occ_data_at(m, slot_block(oct), c, scale, d, rs) || !occ_valid(d) || rs != scale)
+                ok = false;
+            else
+                v[i] = occ_field(d);
+        }
+        if (!ok)
+            continue;
+        const float rx = 1.0f - fac.x, ry = 1.0f - fac.y, rz = 1.0f - fac.z;
+        const float gx = (((v[19] - v[0]) * rx + (v[28] - v[7]) * fac.x) * ry
+                          + ((v[23] - v[1]) * rx + (v[29] - v[11]) * fac.x) * fac.y) * rz
+            + (((v[20] - v[2]) * rx + (v[30] - v[8]) * fac.x) * ry
+               + ((v[24] - v[3]) * rx + (v[31] - v[12]) * fac.x) * fac.y) * fac.z;
+        const float gy = (((v[11] - v[4]) * rx + (v[23] - v[16]) * fac.x) * ry
+                          + ((v[14] - v[7]) * rx + (v[26] - v[19]) * fac.x) * fac.y) * rz
+            + (((v[12] - v[5]) * rx + (v[24] - v[17]) * fac.x) * ry
+               + ((v[15] - v[8]) * rx + (v[27] - v[20]) * fac.x) * fac.y) * fac.z;
+        const float gz = (((v[8] - v[6]) * rx + (v[20] - v[18]) * fac.x) * ry
+                          + ((v[12] - v[10]) * rx + (v[24] - v[22]) * fac.x) * fac.y) * rz
+            + (((v[9] - v[7]) * rx + (v[21] - v[19]) * fac.x) * ry
+               + ((v[13] - v[11]) * rx + (v[25] - v[23]) * fac.x) * fac.y) * fac.z;
+        const float sf = (float) stride;
+        g = v3((0.5f * gx) / sf, (0.5f * gy) / sf, (0.5f * gz) / sf);
+        return true;
+    }
+    return false;
+}
+
+static inline bool occ_contains(const so_occ_map& m, V3 p_W)
+{
+    const V3 p = apply(m.T_MW, p_W);
+    return p.x >= 0.0f && p.x < m.dim && p.y >= 0.0f && p.y < m.dim && p.z >= 0.0f && p.z < m.dim;
+}
+
+static inline bool occ_interp_W(const so_occ_map& m, V3 p_W, float& out, int* scale)
+{
+    return occ_interp(m, apply(m.T_MW, p_W) / m.res, 0, out, scale);
+}
+
+/* find_valid_point (raycaster_impl.hpp:32-70) */
+static bool find_valid_point(const so_occ_map& m, V3 o, V3 d, float step, float t_max, float& t, V3& point_W,
+                             float& value)
+{
+    bool has = false;
+    V3 p = o + t * d;
+    if (occ_contains(m, p) && occ_valid(occ_get_data(m, p)))
+        has = occ_interp_W(m, p, value, nullptr);
+    while (!has) {
+        t += step;
+        if (t > t_max)
+            return false;
+        p = o + t * d;
+        if (occ_contains(m, p) && occ_valid(occ_get_data(m, p)))
+            has = occ_interp_W(m, p, value, nullptr);
+    }
+    point_W = p;
+    return true;
+}
+
+/* compute_map_intersection (raycaster_impl.hpp:85-173) */
+static float compute_map_intersection(const so_occ_map& m, V3 pos_W, V3 dir_W, float t_far, bool& valid)
+{
+    const V3 p = apply(m.T_MW, pos_W), dr = rot(m.T_MW, dir_W);
+    const float pm[3] = {p.x, p.y, p.z}, dm[3] = {dr.x, dr.y, dr.z};
+    const float mx = m.dim;
+    bool inside = true;
+    int quadrant[3];
+    float cand[3] = {0.0f, 0.0f, 0.0f}, maxT[3];
+    for (int i = 0; i < 3; ++i) {
+        if (pm[i] < 0.0f) {
+            quadrant[i] = 1;
+            cand[i] = 0.0f;
+            inside = false;
+        }
+        else if (pm[i] > mx) {
+            quadrant[i] = 0;
+            cand[i] = mx;
+            inside = false;
+        }
+        else {
+            quadrant[i] = 2;
+        }
+    }
+    if (inside)
+        return 0.0f;
+    for (int i = 0; i < 3; ++i)
+        maxT[i] = (quadrant[i] != 2 && (double) dm[i] != 0.) ? (cand[i] - pm[i]) / dm[i] : -1.0f;
+    int which = 0;
+    for (int i = 1; i < 3; ++i)
+        if (maxT[which] < maxT[i])
+            which = i;
+    if (maxT[which] < 0.0f) {
+        valid = false;
+        return 0.0f;
+    }
+    float hit[3];
+    for (int i = 0; i < 3; ++i) {
+        if (which != i) {
+            hit[i] = pm[i] + maxT[which] * dm[i];
+            if (hit[i] < 0.0f || hit[i] > mx) {
+                valid = false;
+                return 0.0f;
+            }
+        }
+        else {
+            hit[i] = cand[i];
+        }
+    }
+    const float t = norm(v3(hit[0] - pm[0], hit[1] - pm[1], hit[2] - pm[2]));
+    if (t_far < t) {
+        valid = false;
+        return 0.0f;
+    }
+    return t;
+}
+
+/* advance_ray (raycaster_impl.hpp:189-338) */
+static void advance_ray(const so_occ_map& m, V3 o, V3 d, float& t, float& t_far, int max_scale, bool& valid)
+{
+    const float voxel_dim = m.res;
+    int scale = max_scale;
+    float v_add = 0.0f;
+    const float v = 1.0f / voxel_dim * t;
+    float v_far = 1.0f / voxel_dim * t_far;
+    V3 oc = v3(-1.0f, -1.0f, -1.0f);
+    if (occ_contains(m, o))
+        oc = apply(m.T_MW, o) / m.res;
+    const float sz = (float) m.octree.size;
+    const float dv[3] = {d.x, d.y, d.z};
+    const float ocv[3] = {oc.x, oc.y, oc.z};
+    float vmap[3];
+    for (int i = 0; i < 3; ++i) {
+        const float dvm = sz / std::fabs(dv[i]);
+        const float frac = ocv[i] / sz;
+        vmap[i] = dv[i] < 0 ? frac * dvm : (1 - frac) * dvm;
+    }
+    v_far = std::min(std::min(std::min(vmap[0], vmap[1]), vmap[2]) + v, v_far);
+    t_far = voxel_dim * v_far;
+    auto max_field = [&](V3 c, int s) {
+        const int32_t ci[3] = {(int) c.x, (int) c.y, (int) c.z};
+        return occ_field(occ_max_data(m, ci, s));
+    };
+    float f = max_field(oc, scale);
+    while (f > -0.2f && scale > 2) {
+        scale -= 1;
+        f = max_field(oc, scale);
+    }
+    V3 rc = oc;
+    while ((v + v_add) < v_far) {
+        if (scale <= 2) {
+            t = voxel_dim * (v + v_add - 4);
+            return;
+        }
+        const int node_size = 1 << scale;
+        const float rcv[3] = {rc.x, rc.y, rc.z};
+        float Vmax[3];
+        for (int i = 0; i < 3; ++i) {
+            const int curr = node_size * (int) (std::floor(rcv[i]) / (float) node_size);
+            const float frac = (rcv[i] - (float) curr) / (float) node_size;
+            const float dV = (float) node_size / std::fabs(dv[i]);
+            Vmax[i] = dv[i] < 0 ? frac * dV : (1 - frac) * dV;
+            if (std::fabs(dv[i]) < 1.0e-6f)
+                Vmax[i] = std::numeric_limits<float>::infinity();
+        }
+        const float Vmin = std::min(std::min(Vmax[0], Vmax[1]), Vmax[2]);
+        v_add = (float) ((double) v_add + ((double) Vmin + 0.01));
+        rc = (v + v_add) * d + oc;
+        f = max_field(rc, scale);
+        if (f > -0.2f) {
+            while (f > -0.2f && scale > 2) {
+                scale -= 1;
+                f = max_field(rc, scale);
+            }
+        }
+        else {
+            for (int s = scale + 1; s <= max_scale; s++) {
+                f = max_field(rc, s);
+                if (f > -0.2f)
+                    break;
+                scale += 1;
+            }
+        }
+    }
+    valid = false;
+}
+
+/* raycast<Occupancy> (raycaster_impl.hpp:352-452). Returns 0 no hit, 1 hit; *zero_hit is set
+ * when the reference returns its all-zero intersection (a hit at the origin with scale 0). */
+static int raycast_occ(const so_occ_map& m, V3 o, V3 d, float t_far, V3& hit, int& scale_out)
+{
+    bool valid = true;
+    float t = compute_map_intersection(m, o, d, t_far, valid);
+    if (!valid)
+        return 0;
+    const int max_scale = std::min(7, (int) std::lround(std::log2((double) m.octree.size)) - 1);
+    advance_ray(m, o, d, t, t_far, max_scale, valid);
+    if (!valid)
+        return 0;
+    const float step = m.res / 2;
+    float value_t = 0.0f, value_tt = 0.0f;
+    bool has_tt = false;
+    V3 pt = v3(0.0f, 0.0f, 0.0f), ptt = v3(0.0f, 0.0f, 0.0f);
+    int scale_tt = 0;
+    if (!find_valid_point(m, o, d, step, t_far, t, pt, value_t))
+        return 0;
+    t += step;
+    if (value_t <= 0.0f) {
+        for (; t < t_far; t += step) {
+            const V3 p = o + d * t;
+            const OccData data = occ_get_data(m, p);
+            if (!occ_valid(data)) {
+                t += step;
+                if (!find_valid_point(m, o, d, step, t_far, t, pt, value_t)) {
+                    hit = v3(0.0f, 0.0f, 0.0f);
+                    scale_out = 0;
+                    return 1;
+                }
+                if (value_t > 0.0f)
+                    break;
+                continue;
+            }
+            value_tt = occ_field(data);
+            has_tt = true;
+            ptt = p;
+            if (value_tt > -0.2f) {
+                float vi;
+                int sc = scale_tt;
+                if (occ_interp_W(m, p, vi, &sc)) {
+                    value_tt = vi;
+                    scale_tt = sc;
+                }
+                else {
+                    has_tt = false;
+                    t += step;
+                    if (!find_valid_point(m, o, d, step, t_far, t, pt, value_t))
+                        return 0;
+                    if (value_t > 0.0f)
+                        break;
+                    continue;
+                }
+            }
+            if (value_tt > 0.0f)
+                break;
+            value_t = value_tt;
+            pt = ptt;
+        }
+        /* an empty value_tt (no sample assigned it) gives no hit */
+        if (has_tt && value_tt > 0.0f && value_t < 0.0f) {
+            t = t - norm(ptt - pt) * (value_tt - 0.0f) / (value_tt - value_t);
+            hit = o + d * t;
+            scale_out = scale_tt;
+            return 1;
+        }
+    }
+    return 0;
+}
+
 } // namespace
 
 /* ------------------------------------------------------------------------ C API -- */
@@ -1515,6 +1880,50 @@ long long so_occ_nodes(const so_occ_map* mp, int32_t* coords, float* min_data, f
 }
 
 int so_occ_map_size(const so_occ_map* m) { return m->octree.size; }
+
+/* raycaster::raycast_volume for occupancy maps (raycaster_impl.hpp:537-627): normals are the
+ * negated normalised field gradient (normals_along_gradient is false for occupancy). */
+void so_occ_raycast_volume(const so_occ_map* mp, const so_pinhole* sensor_c, const float T_WS_m[16], float* pts_W,
+                           float* nrm_W, int8_t* scale)
+{
+    const so_occ_map& m = *mp;
+    const Pinhole s = make_pinhole(sensor_c);
+    const Tf T_WS = tf_from16(T_WS_m);
+    const V3 origin = v3(T_WS.t[0], T_WS.t[1], T_WS.t[2]);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int y = 0; y < s.h; y++) {
+        for (int x = 0; x < s.w; x++) {
+            const size_t idx = (size_t) x + (size_t) y * (size_t) s.w;
+            const V3 ray_S = back_project(s, (float) x, (float) y);
+            const V3 dir_W = rot(T_WS, normalized(ray_S));
+            V3 hit;
+            int sc = 0;
+            V3 p = v3(0.0f, 0.0f, 0.0f), n = v3(0.0f, 0.0f, 0.0f);
+            if (raycast_occ(m, origin, dir_W, far_dist(s, ray_S), hit, sc)) {
+                p = hit;
+                V3 g;
+                if (occ_grad(m, apply(m.T_MW, hit) / m.res, g)) {
+                    g = g / m.res;
+                    const float nn = norm(g);
+                    if (nn > 0.0f)
+                        n = v3(-(g.x / nn), -(g.y / nn), -(g.z / nn));
+                    else
+                        n = v3(-g.x, -g.y, -g.z);
+                }
+            }
+            else {
+                sc = 0;
+            }
+            scale[idx] = (int8_t) sc;
+            pts_W[3 * idx + 0] = p.x;
+            pts_W[3 * idx + 1] = p.y;
+            pts_W[3 * idx + 2] = p.z;
+            nrm_W[3 * idx + 0] = n.x;
+            nrm_W[3 * idx + 1] = n.y;
+            nrm_W[3 * idx + 2] = n.z;
+        }
+    }
+}
 
 int so_occ_aabb(const so_occ_map* m, int32_t mn[3], int32_t mx[3])
 {

@@ -24,6 +24,8 @@ se_gpu_status occ_map_create(const se_gpu_map_config* cfg, const se_gpu_occupanc
 void occ_map_destroy(se_gpu_occ_map* om);
 se_gpu_status occ_check(se_gpu_occ_map* om);
 se_gpu_status occ_aabb(const se_gpu_occ_map* om, int32_t mn[3], int32_t mx[3], int* empty);
+se_gpu_status occ_raycast_volume(const se_gpu_occ_map* om, const se_gpu_pinhole& sensor, const float* T_WS16,
+                                 float* pts, float* nrm, int8_t* scale, cudaStream_t stream);
 se_gpu_status occ_integrate(se_gpu_occ_map* om, const float* depth_dev, const se_gpu_pinhole& sensor,
                             const float* T_WC16, int timestamp, cudaStream_t stream);
 // With pose12_dev_io the tracker starts from, and writes its result to, that device pose.

@@ -153,10 +153,8 @@ extern "C" se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinh
     }
     cudaStream_t stream = (cudaStream_t) stream_p;
     const_cast<se_gpu_map*>(map)->last_stream = stream;
-    if (map->occ) {
-        set_last_error("se_gpu_raycast: occupancy maps are not supported by this build's raycast");
-        return SE_GPU_ERR_NOT_SUPPORTED;
-    }
+    if (map->occ)
+        return occ_raycast_volume(map->occ, *sensor, T_WS, pts_dev, nrm_dev, scale_dev, stream);
     return enqueue_raycast(map, *sensor, T_WS, nullptr, pts_dev, nrm_dev, scale_dev, stream);
 }
 

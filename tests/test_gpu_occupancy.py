@@ -100,3 +100,44 @@ def test_room_dolly_default_config(oracle, gpu):
     _compare(om, gm)
     scales = om.blocks()[1]
     assert len(np.unique(scales[:, 0])) >= 2
+
+
+def _gpu_raycast(gpu, gm, spec, T):
+    import torch
+    gs = gpu.PinholeCamera(**spec)
+    pts = torch.zeros((gs.height, gs.width, 3), dtype=torch.float32, device="cuda")
+    nrm = torch.zeros_like(pts)
+    sc = torch.zeros((gs.height, gs.width), dtype=torch.int8, device="cuda")
+    gpu.raycast_volume(gm, gs, T, pts, nrm, sc)
+    torch.cuda.synchronize()
+    return pts.cpu().numpy(), nrm.cpu().numpy(), sc.cpu().numpy()
+
+
+def _compare_raycast(om, gm, gpu, oracle, spec, T):
+    op, on, osc = om.raycast(oracle.pinhole(**spec), T)
+    gp, gn, gsc = _gpu_raycast(gpu, gm, spec, T)
+    ohit, ghit = (op != 0).any(-1), (gp != 0).any(-1)
+    assert (ohit == ghit).mean() >= 0.999
+    both = ohit & ghit
+    assert both.mean() > 0.5
+    assert (np.abs(op - gp)[both].max(-1) <= 1e-4).mean() >= 0.999
+    assert (osc[both] == gsc[both]).mean() >= 0.999
+    on_ok = (on != 0).any(-1) & both
+    assert (np.sum(on[on_ok] * gn[on_ok], -1) > 1 - 1e-5).mean() >= 0.999
+
+
+def test_raycast_room_dolly(oracle, gpu):
+    from supereight2_gb300 import synthetic as syn
+    sensor, _, poses, frames = syn.dataset("mr160", 8)
+    spec = dict(width=sensor.width, height=sensor.height, fx=sensor.fx, fy=sensor.fy, cx=sensor.cx,
+                cy=sensor.cy, near_plane=sensor.near_plane, far_plane=sensor.far_plane)
+    om, gm, _ = _run(oracle, gpu, frames, spec, [T.astype(np.float32) for T in poses], None,
+                     res=0.02, max_blocks=1 << 18)
+    for k in (3, 7):
+        _compare_raycast(om, gm, gpu, oracle, spec, poses[k].astype(np.float32))
+
+
+def test_raycast_system_test_wall(oracle, gpu):
+    wall = np.full((240, 320), 4.0, np.float32)
+    om, gm, _ = _run(oracle, gpu, [wall] * 3, _pinhole_spec(), [np.eye(4, dtype=np.float32)] * 3, CFG)
+    _compare_raycast(om, gm, gpu, oracle, _pinhole_spec(), np.eye(4, dtype=np.float32))

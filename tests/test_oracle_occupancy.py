@@ -84,3 +84,18 @@ def test_delete_children_run_prunes_and_keeps_invariants(oracle):
             assert np.isfinite(f_mean).all()
     nc, nmin, nmax, leaf = m.nodes()
     assert (nmin[:, 1] >= 0).all() and leaf.sum() > 0
+
+
+def test_raycast_finds_the_wall(oracle):
+    m = oracle.OracleOccMap(10.24, 0.01, **CFG)
+    wall = np.full((240, 320), 4.0, np.float32)
+    for f in range(3):
+        m.integrate_depth(wall, _sensor(oracle), np.eye(4, dtype=np.float32), f)
+    pts, nrm, sc = m.raycast(_sensor(oracle), np.eye(4, dtype=np.float32))
+    hit = (pts != 0).any(-1)
+    assert hit.mean() > 0.9
+    # the occupancy zero crossing lies within the surface thickness in front of the wall
+    assert np.median(np.abs(pts[hit][:, 2] - 4.0)) < 0.05
+    n_ok = (nrm != 0).any(-1) & hit
+    assert n_ok.mean() > 0.5
+    assert np.median(nrm[n_ok][:, 2]) < -0.9   # normals face the camera (-z)
