@@ -92,6 +92,25 @@ typedef struct {
     float far_plane;
 } se_gpu_pinhole;
 
+/* se::OusterLidar::Config (include/se/sensor/ouster_lidar.hpp:25-60) for an equiangular spinning
+ * LiDAR. The reference delegates the projection to the un-vendored srl_projection module; this
+ * ABI fixes it: column u sweeps 360 degrees of azimuth clockwise from +x, u = (pi - atan2(y, x))
+ * * width / 2pi - 0.5 wrapped into [-0.5, width - 0.5); row v = (el_max - el) * (height - 1) /
+ * (el_max - el_min) with el = atan2(z, |xy|), row 0 the highest beam, Successful iff v lies in
+ * [-0.5, height - 0.5). Angles use an arctangent of documented accuracy (1e-5 rad,
+ * Abramowitz-Stegun 4.4.49) so that every platform rounds alike. Range images hold the range
+ * (metres, <= 0: no return); measurementFromPoint is the point's norm. The beam elevations are
+ * linear from elevation_max_deg (row 0) to elevation_min_deg; min_ray_angle = min(beam spacing,
+ * 360 / width) (src/sensor/ouster_lidar.cpp:59-85). */
+typedef struct {
+    int width;                  /* columns (azimuth steps) */
+    int height;                 /* beams */
+    float elevation_min_deg;
+    float elevation_max_deg;
+    float near_plane;
+    float far_plane;
+} se_gpu_lidar;
+
 /* se::TrackerConfig (include/se/tracker/tracker.hpp:22-33). */
 typedef struct {
     int num_levels;    /* at most 3 */
@@ -146,6 +165,37 @@ SE_GPU_API se_gpu_status se_gpu_map_check(se_gpu_map* map);
 SE_GPU_API se_gpu_status se_gpu_integrate_depth(se_gpu_map* map, const float* depth_dev,
                                      const se_gpu_pinhole* sensor, const float T_WC[16],
                                      int timestamp, void* stream);
+/* Replaces se::MapIntegrator<OccupancyMap<Res::Multi>>::integrateDepth(timestamp,
+ * Measurements{Measurement{range, OusterLidar, T_WS}}) (impl/map_integrator_impl.hpp:90-130)
+ * with the Ouster variants of the pooling image (allocator/impl/dense_pooling_image_impl.hpp:
+ * 395-784), of the VolumeCarver (allocator/impl/volume_carver_impl.hpp:339-537) and of the
+ * integration scale (src/sensor/ouster_lidar.cpp:107-146). Occupancy maps only. range_dev:
+ * width*height floats on the device. */
+SE_GPU_API se_gpu_status se_gpu_integrate_range(se_gpu_map* map, const float* range_dev,
+                                                const se_gpu_lidar* sensor, const float T_WS[16],
+                                                int timestamp, void* stream);
+
+/* Batched occupancy integration; no counterpart in the reference, which integrates one map per
+ * call. n (<= 16) occupancy maps with one sensor (a pinhole camera or a LiDAR: exactly one of
+ * the two pointers non-NULL) integrate one frame each per call, every stage of the pipeline in
+ * one launch over all maps' work (uneven block and node counts share the grid). With use_graph
+ * the launches of a call are captured once into a CUDA graph (on the first call) and each call
+ * replays it with that call's poses and images. The maps stay owned by the caller and must
+ * outlive the batch; calls on a batch are not re-entrant and none of its maps may be used by
+ * another call in flight. */
+typedef struct se_gpu_occ_batch se_gpu_occ_batch;
+SE_GPU_API se_gpu_status se_gpu_occ_batch_create(se_gpu_map* const* maps, int n,
+                                                 const se_gpu_pinhole* pinhole,
+                                                 const se_gpu_lidar* lidar, int use_graph,
+                                                 se_gpu_occ_batch** batch);
+/* images_dev[i]: map i's depth / range image on the device; T_WS: n row-major 4x4 poses
+ * (host); timestamps: n frame numbers (host). Stream-ordered. */
+SE_GPU_API se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* batch,
+                                                    const float* const* images_dev,
+                                                    const float* T_WS, const int* timestamps,
+                                                    void* stream);
+SE_GPU_API se_gpu_status se_gpu_occ_batch_destroy(se_gpu_occ_batch* batch);
+
 /* Counters of the last integrate_depth; synchronises the stream. */
 SE_GPU_API se_gpu_status se_gpu_map_integrate_stats(se_gpu_map* map, se_gpu_integrate_stats* stats);
 

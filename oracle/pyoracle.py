@@ -20,6 +20,11 @@ class Pinhole(C.Structure):
                 ("far_plane", C.c_float)]
 
 
+class Lidar(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("elevation_min_deg", C.c_float),
+                ("elevation_max_deg", C.c_float), ("near_plane", C.c_float), ("far_plane", C.c_float)]
+
+
 class TrackerConfig(C.Structure):
     _fields_ = [("num_levels", C.c_int), ("iterations", C.c_int * 3),
                 ("dist_threshold", C.c_float), ("normal_threshold", C.c_float),
@@ -71,6 +76,12 @@ def lib():
             "so_occ_raycast_volume": (None, [vp, C.POINTER(Pinhole), f32p, f32p, f32p, i8p]),
             "so_occ_depth_sigma": (None, [f32p, C.c_int, C.c_float, f32p]),
             "so_occ_pooling_image": (C.c_int, [f32p, C.c_int, C.c_int, vp, C.POINTER(C.c_float)]),
+            "so_occ_pooling_image_lidar": (C.c_int, [f32p, C.c_int, C.c_int, vp, C.POINTER(C.c_float)]),
+            "so_occ_integrate_lidar": (None, [vp, f32p, C.POINTER(Lidar), f32p, C.c_int, vp]),
+            "so_lidar_project": (C.c_int, [C.POINTER(Lidar), f32p, f32p]),
+            "so_atan2": (C.c_float, [C.c_float, C.c_float]),
+            "so_lidar_tan_half_min_angle": (C.c_float, [C.POINTER(Lidar)]),
+            "so_occ_lidar_integration_scale": (C.c_int, [C.POINTER(Lidar), f32p, C.c_float, C.c_int, C.c_int]),
             "so_render_depth_f64": (None, [vp, C.POINTER(Pinhole), f64p, f64p]),
             "so_raycast_adjoint_f64": (None, [vp, C.POINTER(Pinhole), f64p, vp, f64p, vp, vp]),
             "so_map_set_voxel": (None, [vp, i32p, C.c_float, C.c_float]),
@@ -200,6 +211,12 @@ class OracleOccMap:
         lib().so_occ_integrate_depth(self.h, depth, C.byref(sensor), _m16(T_WC), int(timestamp), C.byref(st))
         return st
 
+    def integrate_lidar(self, rng, sensor, T_WS, timestamp=0):
+        rng = np.ascontiguousarray(rng, np.float32).reshape(-1)
+        st = OccStats()
+        lib().so_occ_integrate_lidar(self.h, rng, C.byref(sensor), _m16(T_WS), int(timestamp), C.byref(st))
+        return st
+
     def blocks(self):
         """(coords i32[N,3], scales i32[N,3] (current, min, buffer), counts i64[N,4],
         mean / min / max f32[N,585,3] (occupancy, weight, observed))."""
@@ -234,6 +251,36 @@ def occ_depth_sigma(depth, res):
     out = np.zeros_like(depth)
     lib().so_occ_depth_sigma(depth.reshape(-1), depth.size, float(res), out.reshape(-1))
     return out
+
+
+def lidar(width, height, elevation_min_deg, elevation_max_deg, near_plane, far_plane) -> Lidar:
+    return Lidar(int(width), int(height), float(elevation_min_deg), float(elevation_max_deg),
+                 float(near_plane), float(far_plane))
+
+
+def lidar_project(sensor, p_S):
+    uv = np.zeros(2, np.float32)
+    ok = lib().so_lidar_project(C.byref(sensor), np.ascontiguousarray(p_S, np.float32), uv)
+    return bool(ok), uv
+
+
+def atan2(y, x):
+    return np.float32(lib().so_atan2(float(y), float(x)))
+
+
+def lidar_integration_scale(sensor, c_S, res, last_scale, min_scale):
+    return int(lib().so_occ_lidar_integration_scale(C.byref(sensor), np.ascontiguousarray(c_S, np.float32),
+                                                    float(res), int(last_scale), int(min_scale)))
+
+
+def pooling_image_lidar(depth):
+    depth = np.ascontiguousarray(depth, np.float32)
+    h, w = depth.shape
+    mv = C.c_float()
+    L = lib().so_occ_pooling_image_lidar(depth.reshape(-1), w, h, None, C.byref(mv))
+    out = np.zeros((L + 1, h, w, 4), np.float32)
+    lib().so_occ_pooling_image_lidar(depth.reshape(-1), w, h, out.ctypes.data, C.byref(mv))
+    return out, float(mv.value)
 
 
 def pooling_image(depth):

@@ -181,6 +181,23 @@ int so_occ_aabb(const so_occ_map* map, int32_t mn[3], int32_t mx[3]);
 /* raycaster::raycast_volume for an occupancy map (raycaster_impl.hpp:32-452,537-627). */
 void so_occ_raycast_volume(const so_occ_map* map, const so_pinhole* sensor, const float T_WS[16],
                            float* pts_W, float* nrm_W, int8_t* scale);
+/* A spinning LiDAR (the reference's OusterLidar): equiangular columns over 360 degrees of azimuth
+ * (clockwise from +x), rows linear in elevation from elevation_max_deg (row 0) down to
+ * elevation_min_deg; the range image holds ranges in metres (<= 0: no return). */
+typedef struct {
+    int width, height;
+    float elevation_min_deg, elevation_max_deg;
+    float near_plane, far_plane;
+} so_lidar;
+/* MapIntegrator<OccupancyMap<Res::Multi>>::integrateDepth for an OusterLidar range image. */
+void so_occ_integrate_lidar(so_occ_map* map, const float* range, const so_lidar* sensor,
+                            const float T_WS[16], int timestamp, so_occ_stats* stats);
+int so_lidar_project(const so_lidar* sensor, const float p_S[3], float uv[2]);
+float so_atan2(float y, float x);
+float so_lidar_tan_half_min_angle(const so_lidar* sensor);
+int so_occ_lidar_integration_scale(const so_lidar* sensor, const float c_S[3], float res, int last_scale,
+                                   int min_scale);
+int so_occ_pooling_image_lidar(const float* depth, int w, int h, float* out, float* max_value);
 /* uncert::depth_sigma with the default linear model. */
 void so_occ_depth_sigma(const float* depth, int n, float res, float* sigma);
 /* DensePoolingImage<PinholeCamera>: (max_level + 1) * w * h pixels of (min, max, crossing,

@@ -434,13 +434,15 @@ static inline PPixel outside_pixel_batch() { return pix(0.0f, 0.0f, 2, 2); }
 /* DensePoolingImage<PinholeCamera>, dense_pooling_image_impl.hpp:56-347 */
 struct PoolingImage {
     int w = 0, h = 0, max_level = 0;
+    bool wrap = false; /* DensePoolingImage<OusterLidar>: columns wrap around (360 degrees) */
     float max_value = 0.0f;
     std::vector<std::vector<PPixel>> img;
 
-    void build(const float* depth, int w_, int h_)
+    void build(const float* depth, int w_, int h_, bool wrap_ = false)
     {
         w = w_;
         h = h_;
+        wrap = wrap_;
         const int image_max_dim = std::min(w, h);
         max_level = (int) (std::log2((double) ((image_max_dim - 1) / 2)) + 2) - 1;
         img.assign(max_level + 1, std::vector<PPixel>((size_t) w * h));
@@ -463,10 +465,12 @@ struct PoolingImage {
             for (int y = 0; y < h; ++y)
                 for (int x = 0; x < w; ++x) {
                     PPixel& p = img[1][x + w * y];
-                    if (y >= 1 && y < h - 1 && x >= 1 && x < w - 1)
+                    if (wrap ? (y >= 1 && y < h - 1) : (y >= 1 && y < h - 1 && x >= 1 && x < w - 1))
                         p.crossing = 0;
                     const int top = y > 0 ? y - 1 : 0, bottom = y < h - 1 ? y + 1 : h - 1;
-                    const int left = x > 0 ? x - 1 : 0, right = x < w - 1 ? x + 1 : w - 1;
+                    /* dense_pooling_image_impl.hpp:436-437: the Ouster image wraps in x */
+                    const int left = x > 0 ? x - 1 : (wrap ? w - 1 : 0);
+                    const int right = x < w - 1 ? x + 1 : (wrap ? 0 : w - 1);
                     auto at = [&](int xx, int yy) -> const PPixel& { return L0[xx + yy * w]; };
                     p.min = std::min(at(x, y).min,
                                      std::min(std::min(std::min(at(left, top).min, at(x, top).min),
@@ -496,14 +500,16 @@ struct PoolingImage {
                     PPixel& p = img[l][x + y * w];
                     int left, right, top, bottom;
                     if (x - s_half < 0) {
-                        left = 0;
-                        p.crossing = 1;
+                        left = wrap ? w + (x - s_half) : 0;
+                        if (!wrap)
+                            p.crossing = 1;
                     }
                     else
                         left = x - s_half;
                     if (x + s_half >= w) {
-                        right = w - 1;
-                        p.crossing = 1;
+                        right = wrap ? (x + s_half) - w : w - 1;
+                        if (!wrap)
+                            p.crossing = 1;
                     }
                     else
                         right = x + s_half;
@@ -569,7 +575,14 @@ struct PoolingImage {
             for (int u = u_min + s; true; u += step) {
                 if (u > u_max - s)
                     u = u_max - s;
-                const PPixel& p = img[level][u + w * v];
+                int uf = u;
+                if (wrap && (u_min < 0 || u_max > w - 1)) {
+                    if (u < 0)
+                        uf += w;
+                    else if (u > w - 1)
+                        uf -= w;
+                }
+                const PPixel& p = img[level][uf + w * v];
                 if (batch.max < p.max)
                     batch.max = p.max;
                 if (batch.min > p.min)
@@ -592,6 +605,31 @@ struct PoolingImage {
         else if (n_part > 0)
             batch.known = 1;
         return batch;
+    }
+
+    /* DensePoolingImage<OusterLidar>::conservativeQuery, dense_pooling_image_impl.hpp:743-781 */
+    PPixel conservative_query_lidar(int u_min, int v_min, int u_max, int v_max) const
+    {
+        bool v_in = true, v_out = false;
+        if ((float) v_min < 0.0f) {
+            v_in = false;
+            v_min = 0;
+            if ((float) v_max < 0.0f)
+                v_out = true;
+        }
+        else if ((float) v_min > (float) (unsigned) (h - 1)) {
+            v_out = true;
+        }
+        if ((float) v_max > (float) (unsigned) (h - 1)) {
+            v_in = false;
+            v_max = h - 1;
+        }
+        if (v_out || u_min == u_max || v_min == v_max)
+            return outside_pixel_batch();
+        PPixel p = pool_bounding_box(u_min, u_max, v_min, v_max);
+        if (!v_in)
+            p.crossing = 1;
+        return p;
     }
 
     PPixel conservative_query(int u_min, int v_min, int u_max, int v_max) const
@@ -631,6 +669,83 @@ struct PoolingImage {
         return p;
     }
 };
+
+/* ----------------------------------------------------------------- LiDAR model -- */
+/* The Ouster projection lives in the un-vendored srl_projection module; this is a
+ * project-defined equiangular model (parity unpinned), the same in the oracle and the GPU:
+ * columns sweep the azimuth clockwise from +x (u = (pi - az) * w / (2 pi) - 0.5, wrapped into
+ * [-0.5, w - 0.5)), rows sweep the elevation linearly from el_max (row 0) to el_min (row h-1),
+ * projection succeeds for rows in [-0.5, h - 0.5). Angles use atan2 built on the
+ * Abramowitz-Stegun 4.4.49 polynomial for atan on [0, 1] (|error| <= 1e-5 rad), in plain float
+ * operations, so every platform rounds the same way. */
+static inline float atan01_as(float x)
+{
+    const float x2 = x * x;
+    return x * (0.9998660f + x2 * (-0.3302995f + x2 * (0.1801410f + x2 * (-0.0851330f + x2 * 0.0208351f))));
+}
+
+static inline float atan2_as(float y, float x)
+{
+    const float ax = std::fabs(x), ay = std::fabs(y);
+    if (ax == 0.0f && ay == 0.0f)
+        return 0.0f;
+    float a = ay <= ax ? atan01_as(ay / ax) : 1.57079637f - atan01_as(ax / ay);
+    if (x < 0.0f)
+        a = 3.14159274f - a;
+    return y < 0.0f ? -a : a;
+}
+
+struct Lidar {
+    int w, h;
+    float el_min_rad, el_max_rad;
+    float near_plane, far_plane;
+    float u_scale, v_scale;   /* w / (2 pi), (h - 1) / (el_max - el_min) */
+    float tan_half_min_angle; /* tan(min_ray_angle / 2 in radians) */
+};
+
+static Lidar make_lidar(const so_lidar* c)
+{
+    Lidar L;
+    L.w = c->width;
+    L.h = c->height;
+    L.near_plane = c->near_plane;
+    L.far_plane = c->far_plane;
+    constexpr float deg_to_rad = (float) M_PI / 180.0f;
+    /* the beam elevation angles of the model, then OusterLidar's constructor (ouster_lidar.cpp:59-85) */
+    std::vector<float> el((size_t) c->height);
+    const float step = (c->elevation_max_deg - c->elevation_min_deg) / (float) (c->height - 1);
+    for (int i = 0; i < c->height; ++i)
+        el[(size_t) i] = c->elevation_max_deg - (float) i * step;
+    float min_el = std::fabs(el[1] - el[0]);
+    for (int i = 2; i < c->height; ++i)
+        min_el = std::min(min_el, std::fabs(el[(size_t) i - 1] - el[(size_t) i]));
+    const float az = 360.0f / (float) c->width;
+    const float min_ray_angle = std::min(min_el, az);
+    L.tan_half_min_angle = std::tan(min_ray_angle / 2.0f * deg_to_rad);
+    L.el_min_rad = *std::min_element(el.begin(), el.end()) * deg_to_rad;
+    L.el_max_rad = *std::max_element(el.begin(), el.end()) * deg_to_rad;
+    L.u_scale = (float) c->width / (2.0f * 3.14159274f);
+    L.v_scale = (float) (c->height - 1) / (L.el_max_rad - L.el_min_rad);
+    return L;
+}
+
+static inline bool lidar_project(const Lidar& L, V3 p, float& u, float& v)
+{
+    const float rxy = std::sqrt(p.x * p.x + p.y * p.y);
+    if (rxy == 0.0f && p.z == 0.0f) {
+        u = v = 0.0f;
+        return false;
+    }
+    const float az = atan2_as(p.y, p.x);
+    const float el = atan2_as(p.z, rxy);
+    u = (3.14159274f - az) * L.u_scale - 0.5f;
+    if (u < -0.5f)
+        u += (float) L.w;
+    if (u >= (float) L.w - 0.5f)
+        u -= (float) L.w;
+    v = (L.el_max_rad - el) * L.v_scale;
+    return v >= -0.5f && v < (float) L.h - 0.5f;
+}
 
 } // namespace
 
@@ -705,10 +820,35 @@ static bool free_voxel(OccData& d, const OccConfig& c)
     return newly;
 }
 
+/* OusterLidar::computeIntegrationScaleImpl, ouster_lidar.cpp:107-146 */
+static int lidar_integration_scale(const Lidar& L, V3 c, float res, int last_scale, int min_scale, int max_scale)
+{
+    static const float kRatio[3] = {1.5f, 3.0f, 6.0f};
+    const float dist = norm(c);
+    const float pixel_dim = 2.0f * dist * L.tan_half_min_angle;
+    const float pv = (float) ((double) pixel_dim / (std::sqrt(3.0) * (double) res));
+    int scale = 0;
+    for (float r : kRatio) {
+        if (pv < r)
+            break;
+        scale++;
+    }
+    scale = std::min(scale, max_scale);
+    if ((scale > last_scale || scale < last_scale) && min_scale != -1) {
+        const V3 n = normalized(c);
+        const V3 h = scale > last_scale ? c - 0.25f * n : c + 0.25f * n;
+        return lidar_integration_scale(L, h, res, last_scale, -1, max_scale);
+    }
+    return scale;
+}
+
 enum class VarState { Constant, Gradient, Undefined };
 
 struct Frame {
     const so_occ_map* m;
+    bool lidar = false;
+    Lidar L;
+    int w, h; /* image size */
     Pinhole s;
     Tf T_WS, T_SW;
     const float* depth;
@@ -738,6 +878,10 @@ static VarState compute_variance(const Frame& f, float d_min, float d_max, float
         return VarState::Constant;
     return VarState::Gradient;
 }
+
+static void carve_emit(so_occ_map& mm, Frame& f, int depth, int slot, bool should_split, VarState var,
+                       bool projects_inside, Allocation& out);
+static bool camera_in_node(const so_occ_map& mm, const Frame& f, const int32_t coord[3], int size);
 
 /* VolumeCarver<.., PinholeCamera>::operator()(coord, size, depth, octant), volume_carver_impl.hpp:132-310.
  * `slot` is the octant: a node index or a block slot code. */
@@ -785,17 +929,7 @@ static void carve(so_occ_map& mm, Frame& f, const int32_t coord[3], int size, in
     const bool is_block = slot_is_block(slot);
     if (depth < oct.block_depth() + 1) {
         if (n_front < 8) {
-            /* cameraInNode: pointToVoxel<Safe::On>(camera position) */
-            V3 cam_v = v3(-1.0f, -1.0f, -1.0f);
-            {
-                const V3 t = v3(f.T_WS.t[0], f.T_WS.t[1], f.T_WS.t[2]);
-                const V3 p_M = apply(mm.T_MW, t);
-                if (p_M.x >= 0.0f && p_M.x < mm.dim && p_M.y >= 0.0f && p_M.y < mm.dim && p_M.z >= 0.0f && p_M.z < mm.dim)
-                    cam_v = p_M / mm.res;
-            }
-            const bool cam_in = cam_v.x >= (float) coord[0] && cam_v.x <= (float) (coord[0] + size)
-                && cam_v.y >= (float) coord[1] && cam_v.y <= (float) (coord[1] + size) && cam_v.z >= (float) coord[2]
-                && cam_v.z <= (float) (coord[2] + size);
+            const bool cam_in = camera_in_node(mm, f, coord, size);
             bool crosses = false;
             for (int k = 0; k < 8; ++k)
                 crosses = crosses || ok[k];
@@ -857,6 +991,101 @@ static void carve(so_occ_map& mm, Frame& f, const int32_t coord[3], int size, in
             projects_inside = pp.known == 0;
         }
     }
+    carve_emit(mm, f, depth, slot, should_split, var, projects_inside, out);
+}
+
+/* cameraInNode, volume_carver_impl.hpp:83-98 */
+static bool camera_in_node(const so_occ_map& mm, const Frame& f, const int32_t coord[3], int size)
+{
+    V3 cam_v = v3(-1.0f, -1.0f, -1.0f);
+    const V3 t = v3(f.T_WS.t[0], f.T_WS.t[1], f.T_WS.t[2]);
+    const V3 p_M = apply(mm.T_MW, t);
+    if (p_M.x >= 0.0f && p_M.x < mm.dim && p_M.y >= 0.0f && p_M.y < mm.dim && p_M.z >= 0.0f && p_M.z < mm.dim)
+        cam_v = p_M / mm.res;
+    return cam_v.x >= (float) coord[0] && cam_v.x <= (float) (coord[0] + size) && cam_v.y >= (float) coord[1]
+        && cam_v.y <= (float) (coord[1] + size) && cam_v.z >= (float) coord[2] && cam_v.z <= (float) (coord[2] + size);
+}
+
+/* VolumeCarver<.., OusterLidar>::operator()(coord, size, depth, octant), volume_carver_impl.hpp:339-537:
+ * range-based depth bounds, the camera-in-node test first, and corner columns unwrapped around
+ * the centre's column before the bounding box goes to the wrap-around pooling image. */
+static void carve_lidar(so_occ_map& mm, Frame& f, const int32_t coord[3], int size, int depth, int slot, Allocation& out)
+{
+    OccOctree& oct = mm.octree;
+    const float size_to_radius = std::sqrt(3.0f) / 2.0f;
+    const V3 centre_W = occ_voxel_to_point(mm, coord, size);
+    const V3 centre_S = apply(f.T_SW, centre_W);
+    const float rad = (float) size * size_to_radius * mm.res;
+    const float range = norm(centre_S);
+    const float approx_max = range + rad;
+    const float approx_min = range - rad;
+    if (approx_min > f.max_depth_value)
+        return;
+    bool should_split = false, projects_inside = false;
+    VarState var = VarState::Gradient;
+    const bool is_block = slot_is_block(slot);
+    if (depth < oct.block_depth() + 1) {
+        if (camera_in_node(mm, f, coord, size))
+            should_split = true;
+        else {
+            float pu[8], pv[8];
+            for (int k = 0; k < 8; ++k) {
+                const float rx = (float) (k & 1), ry = (float) ((k >> 1) & 1), rz = (float) (k >> 2);
+                const V3 p_M = v3(((float) size * rx + (float) coord[0]) * mm.res,
+                                  ((float) size * ry + (float) coord[1]) * mm.res,
+                                  ((float) size * rz + (float) coord[2]) * mm.res);
+                lidar_project(f.L, apply(f.T_SW, apply(mm.T_WM, p_M)), pu[k], pv[k]);
+            }
+            float cu, cv;
+            lidar_project(f.L, centre_S, cu, cv);
+            const float W = (float) f.L.w;
+            float cu_comp = cu + (float) (f.L.w / 2);
+            if (cu_comp > W - 0.5f)
+                cu_comp = cu_comp - W;
+            for (int k = 0; k < 8; ++k) {
+                if (cu < cu_comp && pu[k] > cu && pu[k] > cu_comp)
+                    pu[k] = pu[k] - W;
+                else if (cu > cu_comp && pu[k] < cu && pu[k] < cu_comp)
+                    pu[k] = pu[k] + W;
+            }
+            float umin = pu[0], umax = pu[0], vmin = pv[0], vmax = pv[0];
+            for (int k = 1; k < 8; ++k) {
+                umin = std::min(umin, pu[k]);
+                umax = std::max(umax, pu[k]);
+                vmin = std::min(vmin, pv[k]);
+                vmax = std::max(vmax, pv[k]);
+            }
+            const int bb_min[2] = {(int) umin, (int) vmin}, bb_max[2] = {(int) umax, (int) vmax};
+            const PPixel pp = f.depth_pool.conservative_query_lidar(bb_min[0], bb_min[1], bb_max[0], bb_max[1]);
+            if (pp.known == 2)
+                return;
+            if (approx_min > pp.max + f.tau_max)
+                return;
+            const PPixel sp = f.sigma_pool.conservative_query_lidar(bb_min[0], bb_min[1], bb_max[0], bb_max[1]);
+            var = compute_variance(f, pp.min, pp.max, approx_min, approx_max, sp.max);
+            if (var != VarState::Gradient) {
+                OccData cd = is_block ? oct.blocks[slot_block(slot)].max_data() : oct.nodes[slot].data();
+                if (cd.observed && (double) occ_field(cd) <= 0.95 * (double) kMinOccupancy)
+                    return;
+            }
+            if (pp.crossing == 1)
+                should_split = true;
+            else if (pp.known == 1)
+                should_split = true;
+            else if (var == VarState::Gradient)
+                should_split = true;
+            projects_inside = pp.known == 0;
+        }
+    }
+    carve_emit(mm, f, depth, slot, should_split, var, projects_inside, out);
+}
+
+/* the common tail of both carvers: split (allocate the children and recurse) or list the octant */
+static void carve_emit(so_occ_map& mm, Frame& f, int depth, int slot, bool should_split, VarState var,
+                       bool projects_inside, Allocation& out)
+{
+    OccOctree& oct = mm.octree;
+    const bool is_block = slot_is_block(slot);
     if (should_split) {
         if (is_block) {
             out.block_list.push_back(slot_block(slot));
@@ -870,7 +1099,11 @@ static void carve(so_occ_map& mm, Frame& f, const int32_t coord[3], int size, in
                 int32_t cc[3];
                 for (int a = 0; a < 3; ++a)
                     cc[a] = oct.nodes[slot].coord[a] + csize * ((i >> a) & 1);
-                carve(mm, f, cc, csize, depth + 1, oct.nodes[slot].child[i], out);
+                const int child = oct.nodes[slot].child[i];
+                if (f.lidar)
+                    carve_lidar(mm, f, cc, csize, depth + 1, child, out);
+                else
+                    carve(mm, f, cc, csize, depth + 1, child, out);
             }
         }
     }
@@ -891,7 +1124,8 @@ static void carve(so_occ_map& mm, Frame& f, const int32_t coord[3], int size, in
 static int recommended_scale(const so_occ_map& m, const Frame& f, OccBlock& b, V3 centre_C, bool free_min, int& last_scale)
 {
     last_scale = (b.min_scale == -1) ? 0 : b.current_scale;
-    const int computed = occ_integration_scale(f.s, centre_C, m.res, last_scale, b.min_scale, kOccMaxScale);
+    const int computed = f.lidar ? lidar_integration_scale(f.L, centre_C, m.res, last_scale, b.min_scale, kOccMaxScale)
+                                 : occ_integration_scale(f.s, centre_C, m.res, last_scale, b.min_scale, kOccMaxScale);
     const int min_integr = (free_min && (b.min_scale == -1 || (double) b.max_data().occ < 0.95 * (double) m.cfg.log_odd_min))
         ? m.cfg.fs_integr_scale
         : std::max(0, last_scale - 1);
@@ -938,8 +1172,10 @@ static void update_block_data(const so_occ_map& m, const Frame& f, OccBlock& b, 
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
             D[i][j] = f.T_SW.R[i][j] * rs;
-    const float tau = compute_tau(centre_C.z, f.tau_min, f.tau_max, m.cfg);
+    const float tau = compute_tau(f.lidar ? norm(centre_C) : centre_C.z, f.tau_min, f.tau_max, m.cfg);
     OccData* data = to_buffer ? b.buffer_data() : b.curr_data();
+    const float near_p = f.lidar ? f.L.near_plane : f.s.near_plane;
+    const float far_p = f.lidar ? f.L.far_plane : f.s.far_plane;
     for (int z = 0; z < n; z++)
         for (int y = 0; y < n; y++)
             for (int x = 0; x < n; x++) {
@@ -948,25 +1184,25 @@ static void update_block_data(const so_occ_map& m, const Frame& f, OccBlock& b, 
                                   (D[2][0] * fx + D[2][1] * fy) + D[2][2] * fz);
                 const V3 p = base_C + dlt;
                 float u, v;
-                if (!project(f.s, p, u, v))
+                if (!(f.lidar ? lidar_project(f.L, p, u, v) : project(f.s, p, u, v)))
                     continue;
                 int px, py;
                 round_pixel(u, v, px, py);
-                const float dv = f.depth[px + py * f.s.w];
-                if (dv < f.s.near_plane)
+                const float dv = f.depth[px + py * f.w];
+                if (dv < near_p)
                     continue;
-                const float three_sigma = 3.0f * f.sigma[px + py * f.s.w];
+                const float three_sigma = 3.0f * f.sigma[px + py * f.w];
                 OccData& d = data[x + y * n + z * n2];
                 bool newly;
                 if (low_var) {
                     newly = free_voxel(d, m.cfg);
                 }
                 else {
-                    const float pm = p.z;
+                    const float pm = f.lidar ? norm(p) : p.z;
                     const float range = norm(p);
                     const float range_diff = (pm - dv) * (range / pm);
                     newly = update_voxel(d, range_diff, tau, three_sigma, m.cfg);
-                    if (dv > f.s.far_plane)
+                    if (dv > far_p)
                         continue;
                 }
                 if (to_buffer) {
@@ -1695,27 +1931,26 @@ int so_occ_get_field_interp(const so_occ_map* mp, const float p[3], float* value
     return 1;
 }
 
-void so_occ_integrate_depth(so_occ_map* mp, const float* depth, const so_pinhole* sensor, const float T_WC[16],
-                            int timestamp, so_occ_stats* stats)
+/* MapIntegrator<OccupancyMap<Res::Multi>>::integrateDepth after the sensor-specific frame set-up:
+ * sigma image, pooling images, VolumeCarver, Updater (map_integrator_impl.hpp:96-125). */
+static void occ_integrate_frame(so_occ_map& m, Frame& f, const float* depth, const float T_WC[16], float far_plane,
+                                int timestamp, so_occ_stats* stats)
 {
-    so_occ_map& m = *mp;
     OccOctree& oct = m.octree;
-    Frame f;
-    f.m = mp;
-    f.s = make_pinhole(sensor);
+    f.m = &m;
     f.T_WS = tf_from16(T_WC);
     f.T_SW = inverse_iso(f.T_WS);
     f.depth = depth;
-    const int npx = sensor->width * sensor->height;
+    const int npx = f.w * f.h;
     f.sigma.resize((size_t) npx);
     depth_sigma(depth, npx, m.res, m.cfg, f.sigma.data());
     f.sigma_min = m.cfg.sigma_min_factor * m.res;
     f.sigma_max = m.cfg.sigma_max_factor * m.res;
     f.tau_min = m.cfg.tau_min_factor * m.res;
     f.tau_max = m.cfg.tau_max_factor * m.res;
-    f.depth_pool.build(depth, sensor->width, sensor->height);
-    f.sigma_pool.build(f.sigma.data(), sensor->width, sensor->height);
-    f.max_depth_value = std::min(f.s.far_plane, f.depth_pool.max_value + f.tau_max);
+    f.depth_pool.build(depth, f.w, f.h, f.lidar);
+    f.sigma_pool.build(f.sigma.data(), f.w, f.h, f.lidar);
+    f.max_depth_value = std::min(far_plane, f.depth_pool.max_value + f.tau_max);
 
     /* VolumeCarver::operator()(), volume_carver_impl.hpp:46-70 */
     Allocation alloc;
@@ -1725,7 +1960,10 @@ void so_occ_integrate_depth(so_occ_map* mp, const float* depth, const so_pinhole
         int32_t cc[3];
         for (int a = 0; a < 3; ++a)
             cc[a] = csize * ((i >> a) & 1);
-        carve(m, f, cc, csize, 1, oct.nodes[0].child[i], alloc);
+        if (f.lidar)
+            carve_lidar(m, f, cc, csize, 1, oct.nodes[0].child[i], alloc);
+        else
+            carve(m, f, cc, csize, 1, oct.nodes[0].child[i], alloc);
     }
     for (int n : alloc.node_list)
         if (oct.nodes[n].is_leaf())
@@ -1776,6 +2014,64 @@ void so_occ_integrate_depth(so_occ_map* mp, const float* depth, const so_pinhole
         stats->n_blocks_freed = (long long) st.freed_blocks.size();
         stats->n_nodes_pruned = n_pruned;
     }
+}
+
+void so_occ_integrate_depth(so_occ_map* mp, const float* depth, const so_pinhole* sensor, const float T_WC[16],
+                            int timestamp, so_occ_stats* stats)
+{
+    Frame f;
+    f.s = make_pinhole(sensor);
+    f.w = sensor->width;
+    f.h = sensor->height;
+    occ_integrate_frame(*mp, f, depth, T_WC, f.s.far_plane, timestamp, stats);
+}
+
+void so_occ_integrate_lidar(so_occ_map* mp, const float* range, const so_lidar* sensor, const float T_WS[16],
+                            int timestamp, so_occ_stats* stats)
+{
+    Frame f;
+    f.lidar = true;
+    f.L = make_lidar(sensor);
+    f.w = sensor->width;
+    f.h = sensor->height;
+    occ_integrate_frame(*mp, f, range, T_WS, f.L.far_plane, timestamp, stats);
+}
+
+int so_lidar_project(const so_lidar* sensor, const float p_S[3], float uv[2])
+{
+    const Lidar L = make_lidar(sensor);
+    return lidar_project(L, v3(p_S[0], p_S[1], p_S[2]), uv[0], uv[1]) ? 1 : 0;
+}
+
+float so_atan2(float y, float x) { return atan2_as(y, x); }
+
+float so_lidar_tan_half_min_angle(const so_lidar* sensor) { return make_lidar(sensor).tan_half_min_angle; }
+
+int so_occ_lidar_integration_scale(const so_lidar* sensor, const float c_S[3], float res, int last_scale,
+                                   int min_scale)
+{
+    const Lidar L = make_lidar(sensor);
+    return lidar_integration_scale(L, v3(c_S[0], c_S[1], c_S[2]), res, last_scale, min_scale, kOccMaxScale);
+}
+
+/* DensePoolingImage<OusterLidar>: the same layout as so_occ_pooling_image */
+int so_occ_pooling_image_lidar(const float* depth, int w, int h, float* out, float* max_value)
+{
+    PoolingImage P;
+    P.build(depth, w, h, true);
+    if (out)
+        for (int l = 0; l <= P.max_level; ++l)
+            for (int i = 0; i < w * h; ++i) {
+                const PPixel& p = P.img[(size_t) l][(size_t) i];
+                float* o = out + 4 * ((size_t) l * w * h + i);
+                o[0] = p.min;
+                o[1] = p.max;
+                o[2] = (float) p.crossing;
+                o[3] = (float) p.known;
+            }
+    if (max_value)
+        *max_value = P.max_value;
+    return P.max_level;
 }
 
 long long so_occ_num_blocks(const so_occ_map* m)

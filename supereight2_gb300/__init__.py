@@ -22,7 +22,8 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "raycast_volume",
+__all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "OusterLidar",
+           "OccupancyBatch", "raycast_volume",
            "render_depth", "raycast_adjoint", "track_noalloc",
            "FramePipeline", "SeGpuError", "library", "library_path"]
 
@@ -55,6 +56,12 @@ class _Pinhole(C.Structure):
                 ("far_plane", C.c_float)]
 
 
+class _Lidar(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("elevation_min_deg", C.c_float),
+                ("elevation_max_deg", C.c_float), ("near_plane", C.c_float),
+                ("far_plane", C.c_float)]
+
+
 class _TrackerConfig(C.Structure):
     _fields_ = [("num_levels", C.c_int), ("iterations", C.c_int * 3),
                 ("dist_threshold", C.c_float), ("normal_threshold", C.c_float),
@@ -84,6 +91,11 @@ SIGNATURES = {
     "se_gpu_map_size": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "se_gpu_map_check": (C.c_int, [_VP]),
     "se_gpu_integrate_depth": (C.c_int, [_VP, _VP, C.POINTER(_Pinhole), _F16, C.c_int, _VP]),
+    "se_gpu_integrate_range": (C.c_int, [_VP, _VP, C.POINTER(_Lidar), _F16, C.c_int, _VP]),
+    "se_gpu_occ_batch_create": (C.c_int, [_VP, C.c_int, C.POINTER(_Pinhole), C.POINTER(_Lidar),
+                                          C.c_int, C.POINTER(_VP)]),
+    "se_gpu_occ_batch_integrate": (C.c_int, [_VP, _VP, _F16, _VP, _VP]),
+    "se_gpu_occ_batch_destroy": (C.c_int, [_VP]),
     "se_gpu_map_integrate_stats": (C.c_int, [_VP, C.POINTER(_IntegrateStats)]),
     "se_gpu_raycast": (C.c_int, [_VP, C.POINTER(_Pinhole), _F16, _VP, _VP, _VP, _VP]),
     "se_gpu_map_download_blocks": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP,
@@ -185,6 +197,27 @@ class PinholeCamera:
     def _c(self) -> _Pinhole:
         return _Pinhole(self.width, self.height, self.fx, self.fy, self.cx, self.cy,
                         self.near_plane, self.far_plane)
+
+
+class OusterLidar:
+    """se::OusterLidar::Config of an equiangular spinning LiDAR: width columns over 360 degrees,
+    height beams linear in elevation from elevation_max_deg (row 0) to elevation_min_deg.
+    Range images hold metres (<= 0: no return)."""
+
+    def __init__(self, width, height, elevation_min_deg, elevation_max_deg, near_plane=0.5,
+                 far_plane=60.0):
+        self.width, self.height = int(width), int(height)
+        self.elevation_min_deg, self.elevation_max_deg = float(elevation_min_deg), float(elevation_max_deg)
+        self.near_plane, self.far_plane = float(near_plane), float(far_plane)
+
+    @classmethod
+    def from_spec(cls, s):
+        return cls(s.width, s.height, s.elevation_min_deg, s.elevation_max_deg, s.near_plane,
+                   s.far_plane)
+
+    def _c(self) -> _Lidar:
+        return _Lidar(self.width, self.height, self.elevation_min_deg, self.elevation_max_deg,
+                      self.near_plane, self.far_plane)
 
 
 class TrackerConfig:
@@ -388,14 +421,65 @@ class MapIntegrator:
     def __init__(self, map: Map):
         self.map = map
 
-    def integrateDepth(self, timestamp, depth, sensor: PinholeCamera, T_WC, stream=None):
+    def integrateDepth(self, timestamp, depth, sensor, T_WC, stream=None):
+        """sensor: PinholeCamera (depth in metres of z) or OusterLidar (occupancy maps; range in
+        metres)."""
         import torch
         ptr = _dptr(depth, torch.float32, (sensor.height, sensor.width), "depth")
         s = sensor._c()
         _, tp = _m16(T_WC)
         L = self.map._L
+        if isinstance(sensor, OusterLidar):
+            _check(L.se_gpu_integrate_range(self.map.h, ptr, C.byref(s), tp, int(timestamp),
+                                            _stream(stream)), "se_gpu_integrate_range")
+            return
         _check(L.se_gpu_integrate_depth(self.map.h, ptr, C.byref(s), tp, int(timestamp),
                                         _stream(stream)), "se_gpu_integrate_depth")
+
+
+class OccupancyBatch:
+    """Several occupancy maps integrated together, one frame each per call, every pipeline stage
+    in one launch over all maps (no counterpart in the reference). graph=True captures the
+    launches of a call into a CUDA graph on the first call and replays it afterwards."""
+
+    def __init__(self, maps, sensor, graph=True):
+        self.maps = list(maps)
+        self.sensor = sensor
+        self._L = library()
+        arr = (_VP * len(self.maps))(*[m.h for m in self.maps])
+        s = sensor._c()
+        pin = C.byref(s) if isinstance(sensor, PinholeCamera) else None
+        lid = C.byref(s) if isinstance(sensor, OusterLidar) else None
+        h = _VP()
+        _check(self._L.se_gpu_occ_batch_create(arr, len(self.maps), pin, lid, int(bool(graph)),
+                                               C.byref(h)), "se_gpu_occ_batch_create")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.se_gpu_occ_batch_destroy(self.h)
+            self.h = None
+
+    def integrate(self, images, T_WS, timestamps, stream=None):
+        """images: per map a [height, width] float32 CUDA tensor (or one [n, height, width]
+        tensor); T_WS: n 4x4 poses; timestamps: n ints (or one int for all maps)."""
+        import torch
+        n = len(self.maps)
+        if isinstance(images, torch.Tensor) and images.dim() == 3:
+            _dptr(images, torch.float32, (n, self.sensor.height, self.sensor.width), "images")
+            ptrs = [images.data_ptr() + i * images.stride(0) * 4 for i in range(n)]
+        else:
+            if len(images) != n:
+                raise SeGpuError(f"{len(images)} images for {n} maps")
+            ptrs = [_dptr(im, torch.float32, (self.sensor.height, self.sensor.width), "image").value
+                    for im in images]
+        arr = (_VP * n)(*ptrs)
+        T = np.ascontiguousarray(np.asarray(T_WS, np.float32).reshape(n, 16))
+        if np.isscalar(timestamps):
+            timestamps = [int(timestamps)] * n
+        ts = (C.c_int * n)(*[int(t) for t in timestamps])
+        _check(self._L.se_gpu_occ_batch_integrate(self.h, arr, T.ctypes.data_as(_F16), ts,
+                                                  _stream(stream)), "se_gpu_occ_batch_integrate")
 
 
 def raycast_volume(map: Map, sensor: PinholeCamera, T_WS, surface_point_cloud_W,

@@ -1,20 +1,6 @@
-// occupancy.cu — se::MapIntegrator::integrateDepth for multi-resolution occupancy maps and a
-// pinhole camera (map_integrator_impl.hpp:90-130), as stream-ordered launches:
-//   sigma          uncert::depth_sigma (uncertainty.cpp:12-34)
-//   pooling        DensePoolingImage<PinholeCamera> of the depth and sigma images
-//                  (dense_pooling_image_impl.hpp:56-213): one launch per level
-//   carve          VolumeCarver (volume_carver_impl.hpp:46-310) breadth first: one launch per
-//                  octree depth over that depth's octants; a split node allocates its 8 children
-//                  (Octree::allocateChildren) and queues them for the next depth
-//   free nodes     Updater::freeNodeRecurse (multires_ofusion_updater_impl.hpp:550-600) breadth
-//                  first over the free-space nodes' subtrees, then freeBlock on the blocks below
-//   update         Updater::updateBlock (:296-409) on the carver's blocks, one warp per block
-//   propagate      propagate_block_to_coarsest_scale on updated and freed blocks, then
-//                  propagateToRoot (:129-164) one depth per launch from the blocks' parents up,
-//                  with pruning, and the root
-// The reference's recursion and OpenMP loops visit independent octants; the breadth-first
-// launches visit the same octants with the same per-octant computation, so the allocated
-// octree, the block lists (as sets) and every voxel agree with a serial run.
+// occupancy.cu — multi-resolution occupancy maps (Map<Data<Occupancy>, Res::Multi, 8>): the
+// map's pools (creation, destruction, checks, downloads) and the raycast over the octree
+// (raycaster_impl.hpp:32-452). Integration lives in occ_integrate.cu.
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -26,1173 +12,6 @@
 #include "profile.cuh"
 
 namespace se_gpu {
-
-struct OccFrame {
-    Pinhole s;
-    Tf T_WS, T_SW;
-    int w, h, levels;
-    float tau_min, tau_max, sigma_min, sigma_max;
-    int frame_id;
-};
-
-struct OccScratch {
-    int w = 0, h = 0, levels = 0;
-    float* sigma = nullptr;
-    float4* pool_depth = nullptr; // levels * w * h of (min, max, crossing, known)
-    float4* pool_sigma = nullptr;
-    float* max_value = nullptr;   // [0] max pooled depth, [1] max_depth_value
-    int* frontier[2] = {nullptr, nullptr};
-    int* block_list = nullptr;    // slot block index
-    int* block_var = nullptr;     // 0 Constant, 1 Gradient, 2 Undefined
-    int* block_inside = nullptr;
-    int* node_list = nullptr;
-    int* freed = nullptr;
-    int2* work[2] = {nullptr, nullptr}; // (node, depth)
-    int* sets = nullptr;          // per depth, node_capacity entries each
-    int set_depths = 0;
-};
-
-} // namespace se_gpu
-
-struct se_gpu_occ_map {
-    se_gpu::OccDevice dev;
-    se_gpu::OccScratch scratch;
-    int frame_id;
-};
-
-namespace se_gpu {
-
-// ------------------------------------------------------------------ per-pixel inputs --
-
-__global__ void occ_sigma_kernel(const float* __restrict__ depth, int n, float smin, float smax, float k_sigma,
-                                 float* __restrict__ sigma)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n)
-        return;
-    const float d = depth[i];
-    if (d <= 0.0f || isnan(d)) {
-        sigma[i] = 0.0f;
-        return;
-    }
-    const float v = k_sigma * d;
-    sigma[i] = v < smin ? smin : (smax < v ? smax : v); // std::clamp
-}
-
-// Pixel::knownPixel / unknownPixel: min = FLT_MAX, max = FLT_MIN (the smallest normal float)
-__global__ void pool_l0_kernel(const float* __restrict__ img, int w, int h, float4* __restrict__ L0)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w * h)
-        return;
-    const float d = img[i];
-    L0[i] = d <= 0.0f ? make_float4(FLT_MAX, FLT_MIN, 0.0f, 2.0f) : make_float4(d, d, 0.0f, 0.0f);
-}
-
-__global__ void pool_l1_kernel(const float4* __restrict__ L0, int w, int h, float4* __restrict__ L1)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w * h)
-        return;
-    const int x = i % w, y = i / w;
-    float4 p = make_float4(FLT_MAX, FLT_MIN, 1.0f, 0.0f); // crossingKnownPixel
-    if (y >= 1 && y < h - 1 && x >= 1 && x < w - 1)
-        p.z = 0.0f;
-    const int top = y > 0 ? y - 1 : 0, bottom = y < h - 1 ? y + 1 : h - 1;
-    const int left = x > 0 ? x - 1 : 0, right = x < w - 1 ? x + 1 : w - 1;
-    const int xs[9] = {x, left, x, right, right, right, x, left, left};
-    const int ys[9] = {y, top, top, top, y, bottom, bottom, bottom, y};
-    float mn = FLT_MAX, mx = -FLT_MAX;
-    int uf = 0;
-    for (int k = 0; k < 9; ++k) {
-        const float4 q = L0[xs[k] + ys[k] * w];
-        mn = fminf(mn, q.x);
-        mx = fmaxf(mx, q.y);
-        uf += (int) q.w;
-    }
-    p.x = mn;
-    p.y = mx;
-    if (uf == 18)
-        p.w = 2.0f;
-    else if (uf > 0)
-        p.w = 1.0f;
-    L1[i] = p;
-}
-
-__global__ void pool_lk_kernel(const float4* __restrict__ P, int w, int h, int s, float4* __restrict__ L)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w * h)
-        return;
-    const int x = i % w, y = i / w;
-    float4 p = make_float4(FLT_MAX, FLT_MIN, 1.0f, 0.0f);
-    const int s_half = s / 2;
-    int left, right, top, bottom;
-    if (x - s_half < 0) {
-        left = 0;
-        p.z = 1.0f;
-    }
-    else
-        left = x - s_half;
-    if (x + s_half >= w) {
-        right = w - 1;
-        p.z = 1.0f;
-    }
-    else
-        right = x + s_half;
-    if (y - s_half < 0) {
-        top = 0;
-        p.z = 1.0f;
-    }
-    else
-        top = y - s_half;
-    if (y + s_half >= h) {
-        bottom = h - 1;
-        p.z = 1.0f;
-    }
-    else
-        bottom = y + s_half;
-    const float4 a = P[left + top * w], b = P[right + top * w], c = P[left + bottom * w], d = P[right + bottom * w];
-    p.x = fminf(fminf(a.x, b.x), fminf(c.x, d.x));
-    p.y = fmaxf(fmaxf(a.y, b.y), fmaxf(c.y, d.y));
-    const int uf = (int) a.w + (int) b.w + (int) c.w + (int) d.w;
-    if (uf == 8)
-        p.w = 2.0f;
-    else if (uf > 0)
-        p.w = 1.0f;
-    if (y >= s && y < h - s && x >= s && x < w - s)
-        p.z = 0.0f;
-    L[i] = p;
-}
-
-// DensePoolingImage::maxValue over the coarsest level, then VolumeCarver's max_depth_value
-__global__ void pool_max_kernel(const float4* __restrict__ Lmax, int w, int h, int max_level, float far_plane,
-                                float tau_max, float* out)
-{
-    const int s = 1 << (max_level - 1);
-    float mv = 0.0f;
-    for (int v = s; true; v += 2 * s) {
-        if (v > h - s - 1)
-            v = h - s - 1;
-        for (int u = s; true; u += 2 * s) {
-            if (u > w - s - 1)
-                u = w - s - 1;
-            const float m = Lmax[u + w * v].y;
-            if (mv < m)
-                mv = m;
-            if (u == w - s - 1)
-                break;
-        }
-        if (v == h - s - 1)
-            break;
-    }
-    out[0] = mv;
-    const float t = mv + tau_max;
-    out[1] = far_plane < t ? far_plane : t;
-}
-
-struct PoolQuery {
-    float min, max;
-    int crossing, known;
-};
-
-// DensePoolingImage<PinholeCamera>::poolBoundingBox (dense_pooling_image_impl.hpp:218-290)
-__device__ PoolQuery pool_bounding_box(const float4* __restrict__ pool, int w, int h, int max_level, int u_min,
-                                       int u_max, int v_min, int v_max)
-{
-    const int min_side = min(u_max - u_min, v_max - v_min);
-    const int half = min_side / 2;
-    // log2(0) = -inf: the reference's clamps turn it into level 0
-    int lc = INT_MIN;
-    if (half > 0)
-        lc = (int) ceil(log2((double) half));
-    const int level = max(0, min(max_level, lc));
-    const int s = level > 0 ? 1 << max(level - 1, 0) : 0;
-    PoolQuery b{FLT_MAX, FLT_MIN, 0, 0};
-    unsigned long long n = 0, n_unknown = 0, n_part = 0;
-    const int step = 2 * s + 1;
-    const float4* L = pool + (size_t) level * w * h;
-    for (int v = v_min + s; true; v += step) {
-        if (v > v_max - s)
-            v = v_max - s;
-        for (int u = u_min + s; true; u += step) {
-            if (u > u_max - s)
-                u = u_max - s;
-            const float4 p = L[u + w * v];
-            if (b.max < p.y)
-                b.max = p.y;
-            if (b.min > p.x)
-                b.min = p.x;
-            if (p.w == 2.0f) {
-                ++n_unknown;
-                ++n_part;
-            }
-            else if (p.w == 1.0f) {
-                ++n_part;
-            }
-            ++n;
-            if (u == u_max - s)
-                break;
-        }
-        if (v == v_max - s)
-            break;
-    }
-    if (n == n_unknown)
-        b.known = 2;
-    else if (n_part > 0)
-        b.known = 1;
-    return b;
-}
-
-// DensePoolingImage<PinholeCamera>::conservativeQuery (dense_pooling_image_impl.hpp:295-347)
-__device__ PoolQuery conservative_query(const float4* __restrict__ pool, int w, int h, int max_level, int u_min,
-                                        int v_min, int u_max, int v_max)
-{
-    bool u_in = true, u_out = false, v_in = true, v_out = false;
-    const float wl = (float) (unsigned) (w - 1), hl = (float) (unsigned) (h - 1);
-    if ((float) u_min < 0.0f) {
-        u_in = false;
-        u_min = 0;
-        if ((float) u_max < 0.0f)
-            u_out = true;
-    }
-    else if ((float) u_min > wl) {
-        u_out = true;
-    }
-    if ((float) u_max > wl) {
-        u_in = false;
-        u_max = w - 1;
-    }
-    if ((float) v_min < 0.0f) {
-        v_in = false;
-        v_min = 0;
-        if ((float) v_max < 0.0f)
-            v_out = true;
-    }
-    else if ((float) v_min > hl) {
-        v_out = true;
-    }
-    if ((float) v_max > hl) {
-        v_in = false;
-        v_max = h - 1;
-    }
-    if (u_out || v_out || u_min == u_max || v_min == v_max)
-        return PoolQuery{0.0f, 0.0f, 2, 2};
-    PoolQuery p = pool_bounding_box(pool, w, h, max_level, u_min, u_max, v_min, v_max);
-    if (!u_in || !v_in)
-        p.crossing = 1;
-    return p;
-}
-
-// ---------------------------------------------------------------------- allocation --
-
-__device__ __forceinline__ void occ_aabb_extend(const OccDevice& m, int x, int y, int z, int sz)
-{
-    atomicMin(&m.aabb[0], x);
-    atomicMin(&m.aabb[1], y);
-    atomicMin(&m.aabb[2], z);
-    atomicMax(&m.aabb[3], x + sz - 1);
-    atomicMax(&m.aabb[4], y + sz - 1);
-    atomicMax(&m.aabb[5], z + sz - 1);
-    m.aabb[6] = 0;
-}
-
-// Octree::allocateChildren (octree_impl.hpp:200-233); only the thread that owns node n calls it
-__device__ void occ_allocate_children(const OccDevice& m, int n)
-{
-    const OccD init = node_data(m, n);
-    const int4 nc = m.node_coord[n];
-    const int csize = nc.w / 2;
-    const bool blocks_below = nc.w == 16;
-    int* child = m.node_child + 8 * (size_t) n;
-    for (int i = 0; i < 8; ++i) {
-        if (child[i] != -1)
-            continue;
-        const int cx = nc.x + csize * (i & 1), cy = nc.y + csize * ((i >> 1) & 1), cz = nc.z + csize * (i >> 2);
-        if (blocks_below) {
-            const int b = atomicAdd(&m.counters[kOccBlocks], 1);
-            if (b >= m.block_capacity) {
-                atomicOr(&m.counters[kOccError], kOccErrBlockPool);
-                continue;
-            }
-            m.block_coord[3 * b] = cx;
-            m.block_coord[3 * b + 1] = cy;
-            m.block_coord[3 * b + 2] = cz;
-            OccBlockState st;
-            st.init_data = init;
-            st.min_scale = -1;
-            st.current_scale = kOccMaxScale;
-            st.finest = kOccMaxScale;
-            st.buffer_scale = -1;
-            st.curr_integr = st.curr_obs = st.buf_integr = st.buf_obs = 0ull;
-            st.parent = n;
-            st.live = 1;
-            m.block_state[b] = st;
-            blk_mean(m, b, kOccMaxScale)[0] = init;
-            child[i] = -2 - b;
-        }
-        else {
-            const int c = atomicAdd(&m.counters[kOccNodes], 1);
-            if (c >= m.node_capacity) {
-                atomicOr(&m.counters[kOccError], kOccErrNodePool);
-                continue;
-            }
-            m.node_coord[c] = make_int4(cx, cy, cz, csize);
-            m.node_parent[c] = n;
-            for (int k = 0; k < 8; ++k)
-                m.node_child[8 * (size_t) c + k] = -1;
-            m.node_min[c] = init;
-            m.node_max[c] = init;
-            m.node_mark[c] = -1;
-            m.node_ts[c] = -1;
-            child[i] = c;
-        }
-    }
-    if (blocks_below)
-        occ_aabb_extend(m, nc.x, nc.y, nc.z, nc.w);
-}
-
-__global__ void occ_carve_root_kernel(OccDevice m, int* frontier, int* frontier_n)
-{
-    occ_allocate_children(m, 0);
-    int n = 0;
-    for (int i = 0; i < 8; ++i)
-        if (m.node_child[i] != -1)
-            frontier[n++] = m.node_child[i];
-    *frontier_n = n;
-}
-
-__device__ __forceinline__ int push(int* list, int* count, int cap, int v, int* err)
-{
-    const int k = atomicAdd(count, 1);
-    if (k < cap)
-        list[k] = v;
-    else
-        atomicOr(err, kOccErrList);
-    return k;
-}
-
-// VolumeCarver<.., PinholeCamera>::operator()(octant) (volume_carver_impl.hpp:132-310)
-__global__ void __launch_bounds__(128) occ_carve_kernel(OccDevice m, OccFrame f, const float4* __restrict__ pool_d,
-                                                        const float4* __restrict__ pool_s,
-                                                        const float* __restrict__ maxv, const int* __restrict__ in,
-                                                        const int* __restrict__ in_n, int* out, int* out_n,
-                                                        int* block_list, int* block_var, int* block_inside,
-                                                        int* node_list, int depth)
-{
-    const int n_in = *in_n < (m.node_capacity + m.block_capacity) ? *in_n : (m.node_capacity + m.block_capacity);
-    const float max_depth_value = maxv[1];
-    int* err = &m.counters[kOccError];
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_in; idx += gridDim.x * blockDim.x) {
-        const int slot = in[idx];
-        const bool is_block = slot_is_block(slot);
-        int cx, cy, cz, size;
-        if (is_block) {
-            const int b = slot_block(slot);
-            cx = m.block_coord[3 * b];
-            cy = m.block_coord[3 * b + 1];
-            cz = m.block_coord[3 * b + 2];
-            size = 8;
-        }
-        else {
-            const int4 nc = m.node_coord[slot];
-            cx = nc.x;
-            cy = nc.y;
-            cz = nc.z;
-            size = nc.w;
-        }
-        const float size_to_radius = sqrtf(3.0f) / 2.0f;
-        const float zero_depth_band = 1.0e-6f;
-        const float off = (float) size * 0.5f;
-        const F3 centre_W =
-            apply(m.T_WM, f3(((float) cx + off) * m.res, ((float) cy + off) * m.res, ((float) cz + off) * m.res));
-        const F3 centre_S = apply(f.T_SW, centre_W);
-        const float rad = (float) size * size_to_radius * m.res;
-        if (centre_S.z - rad > max_depth_value || centre_S.z + rad < zero_depth_band)
-            continue;
-        F3 cS[8];
-        int n_front = 0;
-        for (int k = 0; k < 8; ++k) {
-            const F3 p_M = f3(((float) size * (float) (k & 1) + (float) cx) * m.res,
-                              ((float) size * (float) ((k >> 1) & 1) + (float) cy) * m.res,
-                              ((float) size * (float) (k >> 2) + (float) cz) * m.res);
-            cS[k] = apply(f.T_SW, apply(m.T_WM, p_M));
-            if (!(cS[k].z < zero_depth_band))
-                ++n_front;
-        }
-        if (n_front == 0)
-            continue;
-        float pu[8], pv[8];
-        bool ok[8];
-        for (int k = 0; k < 8; ++k) {
-            const F3 p = cS[k];
-            if (fabsf(p.z) < 1.0e-12f) {
-                pu[k] = pv[k] = 0.0f;
-                ok[k] = false;
-                continue;
-            }
-            const float rz = 1.0f / p.z;
-            pu[k] = f.s.fx * (p.x * rz) + f.s.cx;
-            pv[k] = f.s.fy * (p.y * rz) + f.s.cy;
-            ok[k] = p.z > 0.0f && pu[k] >= -0.5f && pu[k] < (float) f.s.w - 0.5f && pv[k] >= -0.5f
-                && pv[k] < (float) f.s.h - 0.5f;
-        }
-        bool should_split = false, projects_inside = false;
-        int var = 1; // Gradient
-        if (n_front < 8) {
-            // cameraInNode with pointToVoxel<Safe::On>
-            float vx = -1.0f, vy = -1.0f, vz = -1.0f;
-            const F3 p_M = apply(m.T_MW, f3(f.T_WS.t[0], f.T_WS.t[1], f.T_WS.t[2]));
-            if (p_M.x >= 0.0f && p_M.x < m.dim && p_M.y >= 0.0f && p_M.y < m.dim && p_M.z >= 0.0f && p_M.z < m.dim) {
-                vx = p_M.x / m.res;
-                vy = p_M.y / m.res;
-                vz = p_M.z / m.res;
-            }
-            const bool cam_in = vx >= (float) cx && vx <= (float) (cx + size) && vy >= (float) cy
-                && vy <= (float) (cy + size) && vz >= (float) cz && vz <= (float) (cz + size);
-            bool crosses = false;
-            for (int k = 0; k < 8; ++k)
-                crosses = crosses || ok[k];
-            if (cam_in || crosses) {
-                should_split = true;
-            }
-            else {
-                bool in_f = true;
-                for (int i = 0; i < 5; ++i) {
-                    const float d = ((centre_S.x * f.s.planes[i][0] + centre_S.y * f.s.planes[i][1])
-                                     + centre_S.z * f.s.planes[i][2])
-                        + f.s.planes[i][3];
-                    if (d < -rad)
-                        in_f = false;
-                }
-                if (!in_f)
-                    continue;
-                should_split = true;
-            }
-        }
-        else {
-            float umin = 0.0f, umax = 0.0f, vmin = 0.0f, vmax = 0.0f, zmin = 0.0f, zmax = 0.0f;
-            for (int k = 0; k < 8; ++k) {
-                float u = pu[k] > 1e7f ? 1e7f : pu[k];
-                float v = pv[k] > 1e7f ? 1e7f : pv[k];
-                u = u < -1e7f ? -1e7f : u;
-                v = v < -1e7f ? -1e7f : v;
-                if (k == 0) {
-                    umin = umax = u;
-                    vmin = vmax = v;
-                    zmin = zmax = cS[0].z;
-                }
-                else {
-                    umin = fminf(umin, u);
-                    umax = fmaxf(umax, u);
-                    vmin = fminf(vmin, v);
-                    vmax = fmaxf(vmax, v);
-                    zmin = fminf(zmin, cS[k].z);
-                    zmax = fmaxf(zmax, cS[k].z);
-                }
-            }
-            const int bu0 = (int) umin, bv0 = (int) vmin, bu1 = (int) umax, bv1 = (int) vmax;
-            const PoolQuery pp = conservative_query(pool_d, f.w, f.h, f.levels - 1, bu0, bv0, bu1, bv1);
-            if (pp.known == 2)
-                continue;
-            if (zmin > pp.max + f.tau_max)
-                continue;
-            const PoolQuery sp = conservative_query(pool_s, f.w, f.h, f.levels - 1, bu0, bv0, bu1, bv1);
-            // computeVariance (volume_carver_impl.hpp:100-126)
-            {
-                const float z_diff_max = zmax - pp.min;
-                const float z_diff_min = zmin - pp.max;
-                const float tv = m.cfg.k_tau * pp.max;
-                const float tau_max = tv < f.tau_min ? f.tau_min : (f.tau_max < tv ? f.tau_max : tv);
-                const float three_sigma_min = 3.0f * sp.max;
-                if ((double) z_diff_min > 1.25 * (double) tau_max)
-                    var = 2;
-                else if ((double) z_diff_max < -1.25 * (double) three_sigma_min)
-                    var = 0;
-                else
-                    var = 1;
-            }
-            if (var != 1) {
-                OccD cd;
-                if (is_block) {
-                    const int b = slot_block(slot);
-                    const OccBlockState& st = m.block_state[b];
-                    cd = blk_max(m, b, st.finest, kOccMaxScale)[0];
-                }
-                else {
-                    cd = node_data(m, slot);
-                }
-                if (cd.observed && (double) occ_field(cd) <= 0.95 * -100.0)
-                    continue;
-            }
-            if (pp.crossing == 1)
-                should_split = true;
-            else if (pp.known == 1)
-                should_split = true;
-            else if (var == 1)
-                should_split = true;
-            projects_inside = pp.known == 0;
-        }
-        if (is_block) {
-            const int k = push(block_list, &m.counters[kOccBlockListN], m.block_capacity, slot_block(slot), err);
-            if (k < m.block_capacity) {
-                block_var[k] = var;
-                block_inside[k] = projects_inside ? 1 : 0;
-            }
-        }
-        else if (should_split) {
-            occ_allocate_children(m, slot);
-            for (int i = 0; i < 8; ++i) {
-                const int ch = m.node_child[8 * (size_t) slot + i];
-                if (ch != -1) // -1 only when a pool ran out (latched in the error word)
-                    push(out, out_n, m.node_capacity + m.block_capacity, ch, err);
-            }
-        }
-        else if (var == 0) {
-            push(node_list, &m.counters[kOccNodeListN], m.node_capacity, slot, err);
-        }
-    }
-    (void) depth;
-}
-
-__global__ void occ_leaf_aabb_kernel(OccDevice m, const int* __restrict__ node_list)
-{
-    const int n = min(m.counters[kOccNodeListN], m.node_capacity);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int node = node_list[i];
-        if (node_is_leaf(m, node)) {
-            const int4 c = m.node_coord[node];
-            occ_aabb_extend(m, c.x, c.y, c.z, c.w);
-        }
-    }
-}
-
-// ---------------------------------------------------------------- propagation sets --
-
-__device__ __forceinline__ int occ_node_depth(const OccDevice& m, int n)
-{
-    return m.log2_size - (31 - __clz(m.node_coord[n].w));
-}
-
-// Insert node n into the propagation set of its depth (std::set semantics: once per frame).
-__device__ __forceinline__ void occ_set_insert(const OccDevice& m, int* sets, int n, int frame_id)
-{
-    if (n < 0)
-        return;
-    if (atomicExch(&m.node_mark[n], frame_id) == frame_id)
-        return;
-    const int d = occ_node_depth(m, n);
-    const int k = atomicAdd(&m.counters[kOccSetN + d], 1);
-    if (k < m.node_capacity)
-        sets[(size_t) d * m.node_capacity + k] = n;
-    else
-        atomicOr(&m.counters[kOccError], kOccErrList);
-}
-
-// ---------------------------------------------------------------- block state machine --
-
-// Sums a per-lane flag over the warp.
-__device__ __forceinline__ unsigned warp_count(bool b) { return __popc(__ballot_sync(0xffffffffu, b)); }
-
-__device__ __forceinline__ void occ_update(OccD& d, float value, float max_weight)
-{
-    if (d.weight < max_weight)
-        d.weight = d.weight + 1.0f;
-    d.occ = (d.occ * (d.weight - 1.0f) + value) / d.weight;
-    d.observed = 1;
-}
-
-__device__ __forceinline__ float clampf_std(float v, float lo, float hi) { return v < lo ? lo : (hi < v ? hi : v); }
-
-// computeIntegrationScaleImpl (pinhole_camera.cpp:115-152), default ratios {1.5, 3, 6}
-__device__ int occ_integration_scale(const Pinhole& s, float z, float res, int last_scale, int min_scale)
-{
-    for (int pass = 0; pass < 2; ++pass) {
-        const float pv = (z * s.inv_fx) / res;
-        int scale = 0;
-        if (pv >= 1.5f) {
-            scale = 1;
-            if (pv >= 3.0f) {
-                scale = 2;
-                if (pv >= 6.0f)
-                    scale = 3;
-            }
-        }
-        if (pass == 0 && min_scale != -1 && scale != last_scale) {
-            z = scale > last_scale ? z - 0.25f : z + 0.25f;
-            continue;
-        }
-        return scale;
-    }
-    return 0;
-}
-
-// allocateDownTo (block_impl.hpp:540-586) by a whole warp; st is lane 0's copy
-__device__ void occ_allocate_down_to(const OccDevice& m, int b, OccBlockState& st, int new_min, int lane)
-{
-    if (new_min >= st.current_scale)
-        return;
-    for (int s = st.current_scale; s >= new_min; --s) {
-        OccD* d = blk_mean(m, b, s);
-        const int nv = (8 >> s) * (8 >> s) * (8 >> s);
-        if (s != st.current_scale)
-            for (int i = lane; i < nv; i += 32)
-                d[i] = st.init_data;
-        __syncwarp();
-        if (s != new_min) {
-            OccD* mn = m.block_min + (size_t) b * 585 + occ_scale_offset(s);
-            OccD* mx = m.block_max + (size_t) b * 585 + occ_scale_offset(s);
-            for (int i = lane; i < nv; i += 32) {
-                mn[i] = d[i];
-                mx[i] = d[i];
-            }
-        }
-        __syncwarp();
-    }
-    st.finest = new_min;
-    st.current_scale = new_min;
-    st.min_scale = new_min;
-}
-
-// the buffer set-up of updateBlock / freeBlock when the recommended scale differs
-__device__ void occ_prepare_buffer(const OccDevice& m, int b, OccBlockState& st, int rec, int last_scale, int lane)
-{
-    if (rec == st.buffer_scale)
-        return;
-    st.buffer_scale = rec; // initBuffer: resetBuffer then the new scale
-    st.buf_integr = 0ull;
-    st.buf_obs = 0ull;
-    OccD* buf = blk_buffer(m, b, st);
-    if (rec < st.current_scale) {
-        const int nv = (8 >> rec) * (8 >> rec) * (8 >> rec);
-        for (int i = lane; i < nv; i += 32)
-            buf[i] = occ_default();
-        __syncwarp();
-    }
-    if (rec < last_scale) {
-        const unsigned np = 8u >> last_scale, np2 = np * np;
-        const unsigned nb = np << 1, nb2 = nb * nb;
-        const OccD* cur = blk_mean(m, b, st.current_scale);
-        for (unsigned k = lane; k < np * np2 * 8; k += 32) {
-            const unsigned pidx = k >> 3, c = k & 7;
-            const unsigned x = pidx % np, y = (pidx / np) % np, z = pidx / np2;
-            const unsigned i = c & 1, j = (c >> 1) & 1, kk = c >> 2;
-            const OccD pd = cur[x + y * np + z * np2];
-            OccD& bd = buf[(2 * x + i) + (2 * y + j) * nb + (2 * z + kk) * nb2];
-            bd.occ = pd.occ;
-            bd.weight = pd.weight;
-            bd.observed = 0;
-        }
-        __syncwarp();
-    }
-}
-
-// switchData (block_impl.hpp:718-780); returns true when the block switched scales
-__device__ bool occ_switch_data(const OccDevice& m, int b, OccBlockState& st, int lane)
-{
-    const bool go = st.buf_integr >= 20ull
-        && (double) (st.buf_obs * (unsigned long long) ((1 << st.buffer_scale) * (1 << st.buffer_scale)
-                                                        * (1 << st.buffer_scale)))
-            >= 0.9
-                * (double) (st.curr_obs
-                            * (unsigned long long) ((1 << st.current_scale) * (1 << st.current_scale)
-                                                    * (1 << st.current_scale)));
-    if (!go)
-        return false;
-    const int bs = st.buffer_scale;
-    const int nv = (8 >> bs) * (8 >> bs) * (8 >> bs);
-    if (bs < st.current_scale) {
-        const OccD* buf = m.block_buffer + (size_t) b * 512;
-        OccD* d = blk_mean(m, b, bs);
-        for (int i = lane; i < nv; i += 32)
-            d[i] = buf[i];
-        const int nv1 = (8 >> (bs + 1)) * (8 >> (bs + 1)) * (8 >> (bs + 1));
-        OccD* mn = m.block_min + (size_t) b * 585 + occ_scale_offset(bs + 1);
-        OccD* mx = m.block_max + (size_t) b * 585 + occ_scale_offset(bs + 1);
-        for (int i = lane; i < nv1; i += 32) {
-            mn[i] = occ_default();
-            mx[i] = occ_default();
-        }
-        st.finest = bs;
-    }
-    else if (!(bs <= st.min_scale || st.min_scale == -1)) { // deleteUpTo
-        st.finest = bs;
-        st.min_scale = bs;
-    }
-    __syncwarp();
-    OccD* d = blk_mean(m, b, bs);
-    unsigned long long added = 0;
-    for (int base = 0; base < nv; base += 32) {
-        const int i = base + lane;
-        bool f = false;
-        if (i < nv) {
-            OccD e = d[i];
-            if (e.weight > 0.0f && !e.observed) {
-                e.observed = 1;
-                d[i] = e;
-                f = true;
-            }
-        }
-        added += warp_count(f);
-    }
-    st.buf_obs += added;
-    st.current_scale = bs;
-    st.min_scale = bs;
-    st.curr_integr = st.buf_integr;
-    st.curr_obs = st.buf_obs;
-    st.buffer_scale = -1;
-    st.buf_integr = 0ull;
-    st.buf_obs = 0ull;
-    __syncwarp();
-    return true;
-}
-
-__device__ __forceinline__ void occ_incr_buffer_integr(OccBlockState& st, bool do_increment)
-{
-    if (do_increment
-        || (double) (st.buf_obs * (unsigned long long) ((1 << st.buffer_scale) * (1 << st.buffer_scale)
-                                                        * (1 << st.buffer_scale)))
-            >= 0.90
-                * (double) (st.curr_obs
-                            * (unsigned long long) ((1 << st.current_scale) * (1 << st.current_scale)
-                                                    * (1 << st.current_scale))))
-        ++st.buf_integr;
-}
-
-// updateBlockData<UpdateBuffer> (multires_ofusion_updater_impl.hpp:413-545) by a warp
-__device__ void occ_update_block_data(const OccDevice& m, const OccFrame& f, const float* __restrict__ depth,
-                                      const float* __restrict__ sigma, int b, OccBlockState& st, F3 centre_C,
-                                      int scale, bool low_var, bool inside, bool to_buffer, int lane)
-{
-    const int stride = 1 << scale;
-    const int n = 8 >> scale, n2 = n * n;
-    const int cx = m.block_coord[3 * b], cy = m.block_coord[3 * b + 1], cz = m.block_coord[3 * b + 2];
-    const float off = (float) stride * 0.5f;
-    const F3 base_C = apply(f.T_SW, apply(m.T_WM, f3(((float) cx + off) * m.res, ((float) cy + off) * m.res,
-                                                   ((float) cz + off) * m.res)));
-    const float rs = m.res * (float) stride;
-    float D[9];
-    for (int i = 0; i < 9; ++i)
-        D[i] = f.T_SW.R[i] * rs;
-    const float tv = m.cfg.k_tau * centre_C.z;
-    const float tau = clampf_std(tv, f.tau_min, f.tau_max);
-    OccD* data = to_buffer ? blk_buffer(m, b, st) : blk_mean(m, b, st.current_scale);
-    const float lom = m.cfg.log_odd_min, lomax = m.cfg.log_odd_max;
-    unsigned long long newly_total = 0;
-    for (int base = 0; base < n * n2; base += 32) {
-        const int k = base + lane;
-        bool newly = false;
-        if (k < n * n2) {
-            const int x = k % n, y = (k / n) % n, z = k / n2;
-            const float fx = (float) x, fy = (float) y, fz = (float) z;
-            const F3 dl = f3((D[0] * fx + D[1] * fy) + D[2] * fz, (D[3] * fx + D[4] * fy) + D[5] * fz,
-                             (D[6] * fx + D[7] * fy) + D[8] * fz);
-            const F3 p = add(base_C, dl);
-            float u, v;
-            if (project(f.s, p, u, v)) {
-                const int px = (int) (u + 0.5f), py = (int) (v + 0.5f);
-                const float dv = depth[px + py * f.s.w];
-                if (!(dv < f.s.near_plane)) {
-                    const float three_sigma = 3.0f * sigma[px + py * f.s.w];
-                    OccD d = data[k];
-                    bool count = true;
-                    if (low_var) {
-                        newly = !d.observed;
-                        occ_update(d, lom, m.cfg.max_weight);
-                        data[k] = d;
-                    }
-                    else {
-                        const float pm = p.z;
-                        const float range = sqrtf(dot(p, p));
-                        const float range_diff = (pm - dv) * (range / pm);
-                        float sample = 0.0f;
-                        bool upd = true;
-                        if (range_diff < -three_sigma)
-                            sample = lom;
-                        else if (range_diff < tau / 2)
-                            sample = fminf(lom - lom / three_sigma * (range_diff + three_sigma), lomax);
-                        else if (range_diff < tau)
-                            sample = fminf(-lom * tau / (2 * three_sigma), lomax);
-                        else
-                            upd = false;
-                        if (upd) {
-                            newly = !d.observed;
-                            occ_update(d, sample, m.cfg.max_weight);
-                            data[k] = d;
-                        }
-                        if (dv > f.s.far_plane)
-                            count = false;
-                    }
-                    newly = newly && count;
-                }
-            }
-        }
-        newly_total += warp_count(newly);
-    }
-    if (to_buffer) {
-        st.buf_obs += newly_total;
-        occ_incr_buffer_integr(st, inside);
-    }
-    else {
-        st.curr_obs += newly_total;
-        ++st.curr_integr;
-    }
-    __syncwarp();
-}
-
-__device__ __forceinline__ int occ_recommended_scale(const OccDevice& m, const OccFrame& f, int b,
-                                                     const OccBlockState& st, F3 centre_C, bool free_min,
-                                                     int& last_scale)
-{
-    last_scale = (st.min_scale == -1) ? 0 : st.current_scale;
-    const int computed = occ_integration_scale(f.s, centre_C.z, m.res, last_scale, st.min_scale);
-    const OccD mx = blk_max(m, b, st.finest, kOccMaxScale)[0];
-    const int min_integr = (free_min && (st.min_scale == -1 || (double) mx.occ < 0.95 * (double) m.cfg.log_odd_min))
-        ? m.cfg.fs_integr_scale
-        : max(0, last_scale - 1);
-    const int max_integr = (st.min_scale == -1) ? kOccMaxScale : min(kOccMaxScale, last_scale + 1);
-    return min(max(min_integr, computed), max_integr);
-}
-
-__device__ __forceinline__ F3 occ_block_centre_C(const OccDevice& m, const OccFrame& f, int b)
-{
-    const float off = 8.0f * 0.5f;
-    return apply(f.T_SW, apply(m.T_WM, f3(((float) m.block_coord[3 * b] + off) * m.res,
-                                          ((float) m.block_coord[3 * b + 1] + off) * m.res,
-                                          ((float) m.block_coord[3 * b + 2] + off) * m.res)));
-}
-
-// Updater::updateBlock (free == false) / Updater::freeBlock (free == true), one warp per block
-__device__ void occ_process_block(const OccDevice& m, const OccFrame& f, const float* __restrict__ depth,
-                                  const float* __restrict__ sigma, int b, bool low_var, bool inside, bool free,
-                                  int lane)
-{
-    OccBlockState st = m.block_state[b];
-    const F3 centre_C = occ_block_centre_C(m, f, b);
-    int last_scale;
-    const int rec = occ_recommended_scale(m, f, b, st, centre_C, free ? true : low_var, last_scale);
-    int integration_scale = last_scale;
-    bool done = false;
-    if (st.min_scale == -1) {
-        integration_scale = rec;
-        occ_allocate_down_to(m, b, st, integration_scale, lane);
-        st.current_scale = integration_scale;
-        // initCurrCout
-        if (st.init_data.observed) {
-            st.curr_integr = (unsigned long long) st.init_data.weight;
-            const int ns = 8 >> st.current_scale;
-            st.curr_obs = (unsigned long long) (ns * ns * ns);
-        }
-        else {
-            st.curr_integr = 0ull;
-            st.curr_obs = 0ull;
-        }
-        st.init_data = occ_default();
-    }
-    else if (rec != last_scale) {
-        occ_prepare_buffer(m, b, st, rec, last_scale, lane);
-        if (free) {
-            OccD* buf = blk_buffer(m, b, st);
-            const int nv = (8 >> rec) * (8 >> rec) * (8 >> rec);
-            unsigned long long cnt = 0;
-            for (int base = 0; base < nv; base += 32) {
-                const int i = base + lane;
-                bool newly = false;
-                if (i < nv) {
-                    OccD d = buf[i];
-                    newly = !d.observed;
-                    occ_update(d, m.cfg.log_odd_min, m.cfg.max_weight);
-                    buf[i] = d;
-                }
-                cnt += warp_count(newly);
-            }
-            st.buf_obs += cnt;
-            occ_incr_buffer_integr(st, true);
-            __syncwarp();
-        }
-        else {
-            occ_update_block_data(m, f, depth, sigma, b, st, centre_C, rec, low_var, inside, true, lane);
-        }
-        done = occ_switch_data(m, b, st, lane);
-    }
-    else {
-        st.buffer_scale = -1; // resetBuffer
-        st.buf_integr = 0ull;
-        st.buf_obs = 0ull;
-    }
-    if (!done) {
-        if (free) {
-            const int nv = (8 >> integration_scale) * (8 >> integration_scale) * (8 >> integration_scale);
-            OccD* cur = blk_mean(m, b, st.current_scale);
-            unsigned long long cnt = 0;
-            for (int base = 0; base < nv; base += 32) {
-                const int i = base + lane;
-                bool newly = false;
-                if (i < nv) {
-                    OccD d = cur[i];
-                    newly = !d.observed;
-                    occ_update(d, m.cfg.log_odd_min, m.cfg.max_weight);
-                    cur[i] = d;
-                }
-                cnt += warp_count(newly);
-            }
-            st.curr_obs += cnt;
-            ++st.curr_integr;
-            __syncwarp();
-        }
-        else {
-            occ_update_block_data(m, f, depth, sigma, b, st, centre_C, integration_scale, low_var, inside, false,
-                                  lane);
-        }
-    }
-    if (lane == 0)
-        m.block_state[b] = st;
-    __syncwarp();
-}
-
-__global__ void __launch_bounds__(256) occ_update_blocks_kernel(OccDevice m, OccFrame f, const float* __restrict__ depth,
-                                                                const float* __restrict__ sigma,
-                                                                const int* __restrict__ block_list,
-                                                                const int* __restrict__ block_var,
-                                                                const int* __restrict__ block_inside)
-{
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int n_warps = (gridDim.x * blockDim.x) >> 5;
-    const int n = min(m.counters[kOccBlockListN], m.block_capacity);
-    for (int i = warp; i < n; i += n_warps)
-        occ_process_block(m, f, depth, sigma, block_list[i], block_var[i] == 0, block_inside[i] != 0, false, lane);
-}
-
-__global__ void __launch_bounds__(256) occ_free_blocks_kernel(OccDevice m, OccFrame f, const float* __restrict__ depth,
-                                                              const float* __restrict__ sigma,
-                                                              const int* __restrict__ freed)
-{
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int n_warps = (gridDim.x * blockDim.x) >> 5;
-    const int n = min(m.counters[kOccFreedN], m.block_capacity);
-    for (int i = warp; i < n; i += n_warps)
-        occ_process_block(m, f, depth, sigma, freed[i], true, true, true, lane);
-}
-
-// Updater::freeNodeRecurse, one level of the subtrees per launch
-__global__ void occ_free_nodes_kernel(OccDevice m, int frame_id, const int2* __restrict__ in, const int* __restrict__ in_n,
-                                      int2* out, int* out_n, int* freed, int* sets)
-{
-    const int n_in = min(*in_n, m.node_capacity);
-    int* err = &m.counters[kOccError];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += gridDim.x * blockDim.x) {
-        const int n = in[i].x, depth = in[i].y;
-        if (node_is_leaf(m, n)) {
-            OccD d = node_data(m, n);
-            occ_update(d, m.cfg.log_odd_min, m.cfg.max_weight);
-            m.node_min[n] = d;
-            m.node_max[n] = d;
-            occ_set_insert(m, sets, m.node_parent[n], frame_id);
-        }
-        else {
-            for (int c = 0; c < 8; ++c) {
-                const int ch = m.node_child[8 * (size_t) n + c];
-                if (ch == -1)
-                    continue;
-                if (slot_is_block(ch)) {
-                    occ_set_insert(m, sets, n, frame_id);
-                    push(freed, &m.counters[kOccFreedN], m.block_capacity, slot_block(ch), err);
-                }
-                else {
-                    const int k = atomicAdd(out_n, 1);
-                    if (k < m.node_capacity)
-                        out[k] = make_int2(ch, depth + 1);
-                    else
-                        atomicOr(err, kOccErrList);
-                }
-            }
-        }
-    }
-}
-
-__global__ void occ_seed_work_kernel(OccDevice m, const int* __restrict__ node_list, int2* work, int* work_n)
-{
-    const int n = min(m.counters[kOccNodeListN], m.node_capacity);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        work[i] = make_int2(node_list[i], occ_node_depth(m, node_list[i]));
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        *work_n = n;
-}
-
-// propagate_block_to_coarsest_scale (multires_ofusion_core_impl.hpp:120-276), one warp per block
-__device__ void occ_up_best(OccD& parent, const OccD* ch, bool want_min)
-{
-    float best = want_min ? FLT_MAX : -FLT_MAX;
-    int bi = 0, nv = 0, no = 0;
-    for (int i = 0; i < 8; ++i) {
-        if (occ_valid(ch[i])) {
-            ++nv;
-            no += ch[i].observed ? 1 : 0;
-            const float fv = occ_field(ch[i]);
-            if (want_min ? (fv < best) : (fv > best)) {
-                best = fv;
-                bi = i;
-            }
-        }
-    }
-    if (nv > 0) {
-        parent = ch[bi];
-        parent.observed = (no == 8) ? 1 : 0;
-    }
-}
-
-__device__ void occ_up_mean(OccD& parent, const OccD* ch)
-{
-    float os = 0.0f, ws = 0.0f;
-    int n = 0;
-    for (int i = 0; i < 8; ++i)
-        if (occ_valid(ch[i])) {
-            ++n;
-            os += ch[i].occ;
-            ws += ch[i].weight;
-        }
-    if (n > 0) {
-        parent.occ = os / (float) n;
-        parent.weight = ceilf(ws / (float) n);
-        parent.observed = 0;
-    }
-}
-
-__device__ void occ_propagate_block(const OccDevice& m, int b, int lane)
-{
-    const OccBlockState st = m.block_state[b];
-    if (st.current_scale == kOccMaxScale)
-        return;
-    int cs = st.current_scale;
-    for (int ps = cs + 1; ps <= kOccMaxScale; ++ps) {
-        cs = ps - 1;
-        const int np = 8 >> ps, nc = 8 >> cs;
-        OccD* pmin = blk_min(m, b, st.finest, ps);
-        OccD* pmax = blk_max(m, b, st.finest, ps);
-        OccD* pmean = blk_mean(m, b, ps);
-        const OccD* cmean = blk_mean(m, b, cs);
-        const OccD* cmin = blk_min(m, b, st.finest, cs);
-        const OccD* cmax = blk_max(m, b, st.finest, cs);
-        const bool first = ps == st.current_scale + 1;
-        for (int k = lane; k < np * np * np; k += 32) {
-            const int x = k % np, y = (k / np) % np, z = k / (np * np);
-            OccD c0[8], c1[8], c2[8];
-            for (int c = 0; c < 8; ++c) {
-                const int ci = (2 * x + (c & 1)) + (2 * y + ((c >> 1) & 1)) * nc + (2 * z + (c >> 2)) * nc * nc;
-                c0[c] = cmean[ci];
-                c1[c] = first ? cmean[ci] : cmin[ci];
-                c2[c] = first ? cmean[ci] : cmax[ci];
-            }
-            if (!(first && st.buffer_scale > st.current_scale))
-                occ_up_mean(pmean[k], c0);
-            occ_up_best(pmin[k], c1, true);
-            occ_up_best(pmax[k], c2, false);
-        }
-        __syncwarp();
-    }
-}
-
-__global__ void __launch_bounds__(256) occ_propagate_blocks_kernel(OccDevice m, const int* __restrict__ list,
-                                                                   int counter)
-{
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int n_warps = (gridDim.x * blockDim.x) >> 5;
-    const int n = min(m.counters[counter], m.block_capacity);
-    for (int i = warp; i < n; i += n_warps)
-        occ_propagate_block(m, list[i], lane);
-}
-
-__global__ void occ_seed_sets_kernel(OccDevice m, int frame_id, const int* __restrict__ block_list, int* sets)
-{
-    const int n = min(m.counters[kOccBlockListN], m.block_capacity);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        occ_set_insert(m, sets, m.block_state[block_list[i]].parent, frame_id);
-}
-
-// updater::propagate_to_parent_node (multires_ofusion_core_impl.hpp:88-117)
-__device__ OccD occ_propagate_node(const OccDevice& m, int n, int timestamp)
-{
-    m.node_ts[n] = timestamp;
-    OccD cmin[8], cmax[8];
-    for (int i = 0; i < 8; ++i) {
-        const int c = m.node_child[8 * (size_t) n + i];
-        if (c == -1) {
-            cmin[i] = occ_default();
-            cmax[i] = occ_default();
-        }
-        else if (slot_is_block(c)) {
-            const int b = slot_block(c);
-            const int fin = m.block_state[b].finest;
-            cmin[i] = blk_min(m, b, fin, kOccMaxScale)[0];
-            cmax[i] = blk_max(m, b, fin, kOccMaxScale)[0];
-        }
-        else {
-            cmin[i] = m.node_min[c];
-            cmax[i] = m.node_max[c];
-        }
-    }
-    OccD mn = m.node_min[n], mx = m.node_max[n];
-    occ_up_best(mn, cmin, true);
-    occ_up_best(mx, cmax, false);
-    m.node_min[n] = mn;
-    m.node_max[n] = mx;
-    return mx;
-}
-
-// Octree::deleteChildren: detach the subtree; its blocks stop being live
-__device__ void occ_delete_children(const OccDevice& m, int n)
-{
-    int stack[64];
-    int sp = 0;
-    stack[sp++] = n;
-    while (sp > 0) {
-        const int q = stack[--sp];
-        for (int i = 0; i < 8; ++i) {
-            const int c = m.node_child[8 * (size_t) q + i];
-            if (c == -1)
-                continue;
-            if (slot_is_block(c))
-                m.block_state[slot_block(c)].live = 0;
-            else if (sp < 64)
-                stack[sp++] = c;
-            else
-                atomicOr(&m.counters[kOccError], kOccErrList);
-            m.node_child[8 * (size_t) q + i] = -1;
-        }
-    }
-}
-
-__global__ void occ_propagate_nodes_kernel(OccDevice m, int frame_id, int timestamp, int depth, int* sets)
-{
-    const int n = min(m.counters[kOccSetN + depth], m.node_capacity);
-    const int* list = sets + (size_t) depth * m.node_capacity;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int node = list[i];
-        if (m.node_ts[node] == timestamp)
-            continue;
-        if (m.node_parent[node] < 0)
-            continue;
-        const OccD nd = occ_propagate_node(m, node, timestamp);
-        occ_set_insert(m, sets, m.node_parent[node], frame_id);
-        if (nd.observed && (double) occ_field(nd) <= 0.95 * -100.0) {
-            occ_delete_children(m, node);
-            atomicAdd(&m.counters[kOccPruned], 1);
-        }
-    }
-}
-
-__global__ void occ_propagate_root_kernel(OccDevice m, int timestamp) { occ_propagate_node(m, 0, timestamp); }
-
-__global__ void occ_reset_frame_kernel(OccDevice m)
-{
-    const int i = threadIdx.x;
-    if (i == kOccFrontierN0 || i == kOccFrontierN1 || i == kOccBlockListN || i == kOccNodeListN || i == kOccFreedN
-        || i == kOccWorkN0 || i == kOccWorkN1 || i == kOccPruned || (i >= kOccSetN && i < kOccCounters))
-        m.counters[i] = 0;
-}
 
 // ----------------------------------------------------------------- queries / raycast --
 
@@ -1709,46 +528,6 @@ se_gpu_status occ_raycast_volume(const se_gpu_occ_map* om, const se_gpu_pinhole&
 
 using namespace se_gpu;
 
-// ------------------------------------------------------------------------ host side --
-
-static se_gpu_status occ_scratch_reserve(se_gpu_occ_map* om, int w, int h)
-{
-    OccScratch& s = om->scratch;
-    OccDevice& m = om->dev;
-    if (s.w == w && s.h == h && s.sigma)
-        return SE_GPU_OK;
-    cudaFree(s.sigma);
-    cudaFree(s.pool_depth);
-    cudaFree(s.pool_sigma);
-    s.sigma = nullptr;
-    s.pool_depth = s.pool_sigma = nullptr;
-    const int image_max_dim = w < h ? w : h;
-    const int levels = (int) (std::log2((double) ((image_max_dim - 1) / 2)) + 2) - 1 + 1;
-    const size_t npx = (size_t) w * h;
-    SE_CUDA_TRY(cudaMalloc(&s.sigma, npx * sizeof(float)));
-    SE_CUDA_TRY(cudaMalloc(&s.pool_depth, (size_t) levels * npx * sizeof(float4)));
-    SE_CUDA_TRY(cudaMalloc(&s.pool_sigma, (size_t) levels * npx * sizeof(float4)));
-    if (!s.max_value) {
-        const size_t ncap = (size_t) m.node_capacity + m.block_capacity;
-        SE_CUDA_TRY(cudaMalloc(&s.max_value, 2 * sizeof(float)));
-        SE_CUDA_TRY(cudaMalloc(&s.frontier[0], ncap * sizeof(int)));
-        SE_CUDA_TRY(cudaMalloc(&s.frontier[1], ncap * sizeof(int)));
-        SE_CUDA_TRY(cudaMalloc(&s.block_list, (size_t) m.block_capacity * sizeof(int)));
-        SE_CUDA_TRY(cudaMalloc(&s.block_var, (size_t) m.block_capacity * sizeof(int)));
-        SE_CUDA_TRY(cudaMalloc(&s.block_inside, (size_t) m.block_capacity * sizeof(int)));
-        SE_CUDA_TRY(cudaMalloc(&s.node_list, (size_t) m.node_capacity * sizeof(int)));
-        SE_CUDA_TRY(cudaMalloc(&s.freed, (size_t) m.block_capacity * sizeof(int)));
-        SE_CUDA_TRY(cudaMalloc(&s.work[0], (size_t) m.node_capacity * sizeof(int2)));
-        SE_CUDA_TRY(cudaMalloc(&s.work[1], (size_t) m.node_capacity * sizeof(int2)));
-        s.set_depths = m.block_depth + 1;
-        SE_CUDA_TRY(cudaMalloc(&s.sets, (size_t) s.set_depths * m.node_capacity * sizeof(int)));
-    }
-    s.w = w;
-    s.h = h;
-    s.levels = levels;
-    return SE_GPU_OK;
-}
-
 namespace se_gpu {
 
 se_gpu_status occ_map_create(const se_gpu_map_config* cfg, const se_gpu_occupancy_config* occ, int size,
@@ -1757,7 +536,6 @@ se_gpu_status occ_map_create(const se_gpu_map_config* cfg, const se_gpu_occupanc
     se_gpu_occ_map* om = new se_gpu_occ_map();
     std::memset(&om->dev, 0, sizeof(om->dev));
     om->scratch = OccScratch();
-    om->frame_id = 0;
     OccDevice& m = om->dev;
     m.size = size;
     m.log2_size = 0;
@@ -1874,92 +652,8 @@ void occ_map_destroy(se_gpu_occ_map* om)
     cudaFree(m.block_buffer);
     cudaFree(m.aabb);
     cudaFree(m.counters);
-    OccScratch& s = om->scratch;
-    cudaFree(s.sigma);
-    cudaFree(s.pool_depth);
-    cudaFree(s.pool_sigma);
-    cudaFree(s.max_value);
-    cudaFree(s.frontier[0]);
-    cudaFree(s.frontier[1]);
-    cudaFree(s.block_list);
-    cudaFree(s.block_var);
-    cudaFree(s.block_inside);
-    cudaFree(s.node_list);
-    cudaFree(s.freed);
-    cudaFree(s.work[0]);
-    cudaFree(s.work[1]);
-    cudaFree(s.sets);
+    occ_scratch_free(om);
     delete om;
-}
-
-se_gpu_status occ_integrate(se_gpu_occ_map* om, const float* depth_dev, const se_gpu_pinhole& sensor,
-                            const float* T_WC16, int timestamp, cudaStream_t stream)
-{
-    se_gpu_status st = occ_scratch_reserve(om, sensor.width, sensor.height);
-    if (st != SE_GPU_OK)
-        return st;
-    OccDevice& m = om->dev;
-    OccScratch& s = om->scratch;
-    OccFrame f;
-    f.s = make_pinhole(sensor);
-    f.T_WS = tf_from16(T_WC16);
-    f.T_SW = inverse_iso(f.T_WS);
-    f.w = sensor.width;
-    f.h = sensor.height;
-    f.levels = s.levels;
-    f.tau_min = m.cfg.tau_min_factor * m.res;
-    f.tau_max = m.cfg.tau_max_factor * m.res;
-    f.sigma_min = m.cfg.sigma_min_factor * m.res;
-    f.sigma_max = m.cfg.sigma_max_factor * m.res;
-    f.frame_id = ++om->frame_id;
-    const int npx = f.w * f.h;
-    const int sms = device_sm_count();
-    ProfScope ps(kProfUpdate, stream);
-    occ_reset_frame_kernel<<<1, kOccCounters, 0, stream>>>(m);
-    occ_sigma_kernel<<<(npx + 255) / 256, 256, 0, stream>>>(depth_dev, npx, f.sigma_min, f.sigma_max, m.cfg.k_sigma,
-                                                           s.sigma);
-    for (int img = 0; img < 2; ++img) {
-        const float* src = img == 0 ? depth_dev : s.sigma;
-        float4* P = img == 0 ? s.pool_depth : s.pool_sigma;
-        pool_l0_kernel<<<(npx + 255) / 256, 256, 0, stream>>>(src, f.w, f.h, P);
-        if (s.levels > 1)
-            pool_l1_kernel<<<(npx + 255) / 256, 256, 0, stream>>>(P, f.w, f.h, P + (size_t) npx);
-        for (int l = 2, sz = 2; l < s.levels; ++l, sz <<= 1)
-            pool_lk_kernel<<<(npx + 255) / 256, 256, 0, stream>>>(P + (size_t) (l - 1) * npx, f.w, f.h, sz,
-                                                                  P + (size_t) l * npx);
-    }
-    pool_max_kernel<<<1, 1, 0, stream>>>(s.pool_depth + (size_t) (s.levels - 1) * npx, f.w, f.h, s.levels - 1,
-                                         f.s.far_plane, f.tau_max, s.max_value);
-    // VolumeCarver, breadth first
-    occ_carve_root_kernel<<<1, 1, 0, stream>>>(m, s.frontier[0], m.counters + kOccFrontierN0);
-    for (int d = 1; d <= m.block_depth; ++d) {
-        const int cur = (d - 1) & 1, nxt = d & 1;
-        SE_CUDA_TRY(cudaMemsetAsync(m.counters + kOccFrontierN0 + nxt, 0, sizeof(int), stream));
-        occ_carve_kernel<<<sms * 8, 128, 0, stream>>>(m, f, s.pool_depth, s.pool_sigma, s.max_value, s.frontier[cur],
-                                                      m.counters + kOccFrontierN0 + cur, s.frontier[nxt],
-                                                      m.counters + kOccFrontierN0 + nxt, s.block_list, s.block_var,
-                                                      s.block_inside, s.node_list, d);
-    }
-    occ_leaf_aabb_kernel<<<sms, 256, 0, stream>>>(m, s.node_list);
-    // Updater: free-space nodes (their subtrees breadth first), then the carver's blocks
-    occ_seed_work_kernel<<<sms, 256, 0, stream>>>(m, s.node_list, s.work[0], m.counters + kOccWorkN0);
-    for (int it = 0; it <= m.block_depth; ++it) {
-        const int cur = it & 1, nxt = (it + 1) & 1;
-        SE_CUDA_TRY(cudaMemsetAsync(m.counters + kOccWorkN0 + nxt, 0, sizeof(int), stream));
-        occ_free_nodes_kernel<<<sms * 4, 256, 0, stream>>>(m, f.frame_id, s.work[cur], m.counters + kOccWorkN0 + cur,
-                                                           s.work[nxt], m.counters + kOccWorkN0 + nxt, s.freed, s.sets);
-    }
-    occ_free_blocks_kernel<<<sms * 8, 256, 0, stream>>>(m, f, depth_dev, s.sigma, s.freed);
-    occ_update_blocks_kernel<<<sms * 8, 256, 0, stream>>>(m, f, depth_dev, s.sigma, s.block_list, s.block_var,
-                                                          s.block_inside);
-    occ_propagate_blocks_kernel<<<sms * 8, 256, 0, stream>>>(m, s.block_list, kOccBlockListN);
-    occ_propagate_blocks_kernel<<<sms * 8, 256, 0, stream>>>(m, s.freed, kOccFreedN);
-    occ_seed_sets_kernel<<<sms, 256, 0, stream>>>(m, f.frame_id, s.block_list, s.sets);
-    for (int d = m.block_depth - 1; d > 0; --d)
-        occ_propagate_nodes_kernel<<<sms * 4, 256, 0, stream>>>(m, f.frame_id, timestamp, d, s.sets);
-    occ_propagate_root_kernel<<<1, 1, 0, stream>>>(m, timestamp);
-    SE_CUDA_TRY(cudaGetLastError());
-    return SE_GPU_OK;
 }
 
 } // namespace se_gpu

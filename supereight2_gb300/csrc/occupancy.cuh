@@ -67,23 +67,153 @@ struct OccDevice {
 };
 
 // counters
+constexpr int kOccMaxDepth = 24;
 enum {
     kOccNodes = 0,
     kOccBlocks,
     kOccError,
-    kOccFrontierN0,    // frontier sizes (two buffers)
-    kOccFrontierN1,
     kOccBlockListN,
     kOccNodeListN,
     kOccFreedN,
-    kOccWorkN0,        // free-node work lists
-    kOccWorkN1,
     kOccPruned,
-    kOccSetN,          // first of kOccMaxDepth per-depth propagation-set sizes
-    kOccCounters = kOccSetN + 24
+    kOccFrontierN,     // first of kOccMaxDepth + 1 per-depth carver frontier sizes
+    kOccWorkN = kOccFrontierN + kOccMaxDepth + 1,  // per-level free-node work list sizes
+    kOccSetN = kOccWorkN + kOccMaxDepth + 1,       // per-depth propagation-set sizes
+    kOccCounters = kOccSetN + kOccMaxDepth
 };
+constexpr int kOccFirstFrameCounter = kOccBlockListN; // counters from here on restart every frame
 
 constexpr int kOccErrNodePool = 1, kOccErrBlockPool = 2, kOccErrList = 4;
+
+// ------------------------------------------------------------------------ sensors --
+
+// A spinning LiDAR (the reference's OusterLidar, whose projection model lives outside the
+// reference): columns sweep 360 degrees of azimuth clockwise from +x, u = (pi - az) w / 2pi - 0.5
+// wrapped into [-0.5, w - 0.5); rows are linear in elevation from el_max (row 0) down to el_min,
+// v = (el_max - el) (h - 1) / (el_max - el_min), projection succeeds for v in [-0.5, h - 0.5).
+struct Lidar {
+    int w, h;
+    float el_min, el_max; // radians
+    float near_plane, far_plane;
+    float u_scale, v_scale;
+    float tan_half_min_angle; // tan(min_ray_angle / 2), min_ray_angle as in ouster_lidar.cpp:59-85
+};
+
+// atan on [0, 1] by the Abramowitz-Stegun 4.4.49 polynomial (|error| <= 1e-5 rad) and atan2 by
+// octant reduction, in plain float operations so that the host and the device round alike.
+__host__ __device__ __forceinline__ float atan01_as(float x)
+{
+    const float x2 = x * x;
+    return x * (0.9998660f + x2 * (-0.3302995f + x2 * (0.1801410f + x2 * (-0.0851330f + x2 * 0.0208351f))));
+}
+
+__host__ __device__ __forceinline__ float atan2_as(float y, float x)
+{
+    const float ax = fabsf(x), ay = fabsf(y);
+    if (ax == 0.0f && ay == 0.0f)
+        return 0.0f;
+    float a = ay <= ax ? atan01_as(ay / ax) : 1.57079637f - atan01_as(ax / ay);
+    if (x < 0.0f)
+        a = 3.14159274f - a;
+    return y < 0.0f ? -a : a;
+}
+
+// Writes the pixel even when the projection fails (the carver uses it); false outside the rows.
+__host__ __device__ __forceinline__ bool lidar_project(const Lidar& L, F3 p, float& u, float& v)
+{
+    const float rxy = sqrtf(p.x * p.x + p.y * p.y);
+    if (rxy == 0.0f && p.z == 0.0f) {
+        u = v = 0.0f;
+        return false;
+    }
+    const float az = atan2_as(p.y, p.x);
+    const float el = atan2_as(p.z, rxy);
+    u = (3.14159274f - az) * L.u_scale - 0.5f;
+    if (u < -0.5f)
+        u += (float) L.w;
+    if (u >= (float) L.w - 0.5f)
+        u -= (float) L.w;
+    v = (L.el_max - el) * L.v_scale;
+    return v >= -0.5f && v < (float) L.h - 0.5f;
+}
+
+Lidar make_lidar(const se_gpu_lidar& c);
+
+// The sensor of one integration launch: a pinhole camera or a LiDAR.
+struct OccSensor {
+    int lidar;
+    Pinhole s;
+    Lidar L;
+    int w, h, levels;
+    float near_plane, far_plane;
+};
+
+// ------------------------------------------------------------------ batched launches --
+
+constexpr int kOccMaxBatch = 16;
+
+// Per-frame state of one map in device memory, written by the first launch of each frame.
+struct OccDyn {
+    Tf T_WS, T_SW;
+    const float* depth;
+    int frame_id, timestamp;
+};
+
+// One map of a launch: the octree and its scratch (all device pointers).
+struct OccJob {
+    OccDevice m;
+    float* sigma;
+    float4* pool_depth; // levels * w * h of (min, max, crossing, known)
+    float4* pool_sigma;
+    float* max_value;   // [0] max pooled depth, [1] max_depth_value
+    int* frontier[2];
+    int* block_list;    // slot block index
+    int* block_var;     // 0 Constant, 1 Gradient, 2 Undefined
+    int* block_inside;
+    int* node_list;
+    int* freed;
+    int2* work[2];      // (node, depth)
+    int* sets;          // per depth, node_capacity entries each
+    OccDyn* dyn;
+    float tau_min, tau_max, sigma_min, sigma_max;
+};
+
+// Everything a launch needs except the per-frame inputs, passed by value (__grid_constant__).
+struct OccLaunch {
+    int n;
+    int max_block_depth;
+    OccSensor sensor;
+    OccJob job[kOccMaxBatch];
+};
+static_assert(sizeof(OccLaunch) < 30000, "kernel parameter space");
+
+// The per-frame inputs of every map of a launch.
+struct OccStep {
+    float T_WS[kOccMaxBatch][16];
+    const float* depth[kOccMaxBatch];
+    int timestamp[kOccMaxBatch];
+};
+
+// Scratch of one map, sized for the last sensor it integrated.
+struct OccScratch {
+    int w = 0, h = 0, levels = 0;
+    float* sigma = nullptr;
+    float4* pool_depth = nullptr;
+    float4* pool_sigma = nullptr;
+    float* max_value = nullptr;
+    int* frontier[2] = {nullptr, nullptr};
+    int* block_list = nullptr;
+    int* block_var = nullptr;
+    int* block_inside = nullptr;
+    int* node_list = nullptr;
+    int* freed = nullptr;
+    int2* work[2] = {nullptr, nullptr};
+    int* sets = nullptr;
+    int set_depths = 0;
+    OccDyn* dyn = nullptr;
+    OccLaunch* launch_dev = nullptr; // the single-map launch description
+    OccLaunch* launch_host = nullptr; // its last uploaded contents
+};
 
 __device__ __forceinline__ bool slot_is_block(int s) { return s <= -2; }
 __device__ __forceinline__ int slot_block(int s) { return -2 - s; }
@@ -150,3 +280,8 @@ __device__ __forceinline__ int occ_voxel_idx(int ox, int oy, int oz, int s)
 }
 
 } // namespace se_gpu
+
+struct se_gpu_occ_map {
+    se_gpu::OccDevice dev;
+    se_gpu::OccScratch scratch;
+};

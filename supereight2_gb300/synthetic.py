@@ -249,3 +249,171 @@ def dataset(config: str, n_frames: int, device="cpu", seed=None):
     frames = [render_depth(scene, sensor, T, seed * 7919 + i, device=device)
               for i, T in enumerate(poses)]
     return sensor, scene, poses, frames
+
+
+# --------------------------------------------------------------------- outdoor LiDAR --
+# A seeded outdoor scene for the spinning LiDAR: the ground plane z = 0 plus 100 boxes (yawed,
+# standing on the ground) and 100 vertical cylinders over 100 x 100 m, kept out of 8 east-west
+# roads (y = -35, -25, ..., 35; 3 m either side) that the sensors drive along 1.8 m above the
+# ground. Ranges are ray traced in float64 and stored as float32 metres, with N(0, 0.01^2)
+# range noise; rays without a hit within the far plane (or nearer than the near plane) are 0.
+
+
+@dataclass
+class LidarSpec:
+    width: int = 1024
+    height: int = 64
+    elevation_min_deg: float = -22.5
+    elevation_max_deg: float = 22.5
+    near_plane: float = 0.5
+    far_plane: float = 60.0
+
+
+LIDAR_64 = LidarSpec()
+ROADS_Y = tuple(-35.0 + 10.0 * k for k in range(8))
+
+
+@dataclass
+class OutdoorScene:
+    box_c: np.ndarray    # [Nb, 3] centres (z = half height)
+    box_yaw: np.ndarray  # [Nb]
+    box_h: np.ndarray    # [Nb, 3] half extents
+    cyl_c: np.ndarray    # [Nc, 2]
+    cyl_r: np.ndarray    # [Nc]
+    cyl_top: np.ndarray  # [Nc] heights
+    seed: int = 0
+
+
+def make_outdoor_scene(seed: int, n_boxes=100, n_cylinders=100, half=50.0, road_half=3.0) -> OutdoorScene:
+    rng = np.random.default_rng(seed)
+    roads = np.asarray(ROADS_Y)
+
+    def place(radius):
+        for _ in range(10000):
+            c = rng.uniform(-half + radius, half - radius, size=2)
+            if np.min(np.abs(c[1] - roads)) > road_half + radius:
+                return c
+        raise RuntimeError("could not place object")
+
+    bh = np.stack([rng.uniform(0.5, 2.0, n_boxes), rng.uniform(0.5, 2.0, n_boxes),
+                   rng.uniform(0.5, 5.0, n_boxes)], -1)
+    bxy = np.stack([place(float(np.hypot(h[0], h[1]))) for h in bh])
+    bc = np.concatenate([bxy, bh[:, 2:3]], -1)
+    byaw = rng.uniform(-math.pi, math.pi, n_boxes)
+    cr = rng.uniform(0.3, 1.5, n_cylinders)
+    cc = np.stack([place(float(r)) for r in cr])
+    ct = rng.uniform(1.0, 10.0, n_cylinders)
+    return OutdoorScene(bc, byaw, bh, cc, cr, ct, seed)
+
+
+def lidar_directions(spec: LidarSpec) -> np.ndarray:
+    """Unit ray directions [height, width, 3] in the sensor frame (x forward, z up) through the
+    pixel centres of the equiangular model: az = pi - (u + 0.5) 2 pi / width, el linear from
+    elevation_max_deg (row 0) to elevation_min_deg."""
+    u = np.arange(spec.width, dtype=np.float64)
+    v = np.arange(spec.height, dtype=np.float64)
+    az = math.pi - (u + 0.5) * (2.0 * math.pi / spec.width)
+    el_max, el_min = math.radians(spec.elevation_max_deg), math.radians(spec.elevation_min_deg)
+    el = el_max - v * (el_max - el_min) / (spec.height - 1)
+    ce, se = np.cos(el)[:, None], np.sin(el)[:, None]
+    return np.stack([ce * np.cos(az)[None, :], ce * np.sin(az)[None, :],
+                     np.broadcast_to(se, (spec.height, spec.width))], -1)
+
+
+def road_trajectory(k: int, n_frames: int, step_m=1.0, height=1.8, phase=0.0) -> list:
+    """T_WS of a sensor driving along road k (even k eastwards from x = -45, odd k westwards
+    from x = 45), weaving 1 m across the road, heading along the motion."""
+    y0 = ROADS_Y[k % len(ROADS_Y)]
+    sgn = 1.0 if k % 2 == 0 else -1.0
+    poses = []
+    for i in range(n_frames):
+        s = i * step_m
+        x = sgn * (-45.0 + s)
+        y = y0 + math.sin(0.15 * s + phase)
+        dy = 0.15 * math.cos(0.15 * s + phase)
+        yaw = math.atan2(dy, sgn)
+        T = np.eye(4)
+        T[:3, :3] = _rot_zyx(yaw, 0.0, 0.0)
+        T[:3, 3] = (x, y, height)
+        poses.append(T)
+    return poses
+
+
+def render_range(scene: OutdoorScene, spec: LidarSpec, T_WS, frame_seed: int, keep=1.0, device="cpu",
+                 noise=True) -> np.ndarray:
+    """Ray trace one float32 range image [height, width] (metres, 0 = no return); a fraction
+    1 - keep of the returns is dropped at random."""
+    dt = torch.float64
+    dev = torch.device(device)
+    T = torch.as_tensor(np.asarray(T_WS, np.float64), dtype=dt, device=dev)
+    d = torch.as_tensor(lidar_directions(spec), dtype=dt, device=dev).reshape(-1, 3) @ T[:3, :3].T
+    o = T[:3, 3]
+    inf = torch.full((d.shape[0],), float("inf"), dtype=dt, device=dev)
+    best = inf.clone()
+    # ground
+    tg = -o[2] / torch.where(d[:, 2] < -1e-12, d[:, 2], torch.full_like(d[:, 2], -1e-12))
+    best = torch.where((d[:, 2] < -1e-12) & (tg > 0), tg, best)
+    # boxes (yawed): slabs in the box frame
+    bc = torch.as_tensor(scene.box_c, dtype=dt, device=dev)
+    bh = torch.as_tensor(scene.box_h, dtype=dt, device=dev)
+    cy_, sy_ = torch.cos(torch.as_tensor(scene.box_yaw, dtype=dt, device=dev)), torch.sin(
+        torch.as_tensor(scene.box_yaw, dtype=dt, device=dev))
+    ol = o[None, :] - bc                                                   # [Nb, 3]
+    olx = cy_ * ol[:, 0] + sy_ * ol[:, 1]
+    oly = -sy_ * ol[:, 0] + cy_ * ol[:, 1]
+    dlx = d[:, None, 0] * cy_[None] + d[:, None, 1] * sy_[None]            # [R, Nb]
+    dly = -d[:, None, 0] * sy_[None] + d[:, None, 1] * cy_[None]
+    dlz = d[:, None, 2].expand_as(dlx)
+    tn = torch.full_like(dlx, -float("inf"))
+    tf = torch.full_like(dlx, float("inf"))
+    for oc, dc, hc in ((olx, dlx, bh[:, 0]), (oly, dly, bh[:, 1]), (ol[:, 2], dlz, bh[:, 2])):
+        dc = torch.where(dc.abs() < 1e-12, torch.full_like(dc, 1e-12), dc)
+        ta = (-hc[None] - oc[None]) / dc
+        tb = (hc[None] - oc[None]) / dc
+        tn = torch.maximum(tn, torch.minimum(ta, tb))
+        tf = torch.minimum(tf, torch.maximum(ta, tb))
+    hit = (tn <= tf) & (tn > 1e-6)
+    tbox = torch.where(hit, tn, torch.full_like(tn, float("inf"))).amin(-1)
+    best = torch.minimum(best, tbox)
+    # vertical cylinders with a top cap
+    cc = torch.as_tensor(scene.cyl_c, dtype=dt, device=dev)
+    cr = torch.as_tensor(scene.cyl_r, dtype=dt, device=dev)
+    ct = torch.as_tensor(scene.cyl_top, dtype=dt, device=dev)
+    ox, oy = o[0] - cc[:, 0], o[1] - cc[:, 1]                              # [Nc]
+    a = d[:, None, 0] ** 2 + d[:, None, 1] ** 2                            # [R, 1]
+    b = d[:, None, 0] * ox[None] + d[:, None, 1] * oy[None]                # [R, Nc]
+    c = (ox * ox + oy * oy - cr * cr)[None]
+    disc = b * b - a * c
+    sq = torch.sqrt(torch.clamp(disc, min=0.0))
+    a_safe = torch.where(a < 1e-12, torch.full_like(a, 1e-12), a)
+    t0 = (-b - sq) / a_safe
+    z0 = o[2] + t0 * d[:, None, 2]
+    side = (disc >= 0) & (a >= 1e-12) & (t0 > 1e-6) & (z0 >= 0) & (z0 <= ct[None])
+    tcyl = torch.where(side, t0, torch.full_like(t0, float("inf")))
+    dz = d[:, None, 2]
+    dz_safe = torch.where(dz.abs() < 1e-12, torch.full_like(dz, -1e-12), dz)
+    tc = (ct[None] - o[2]) / dz_safe
+    px, py = ox[None] + tc * d[:, None, 0], oy[None] + tc * d[:, None, 1]
+    cap = (dz < -1e-12) & (tc > 1e-6) & (px * px + py * py <= (cr * cr)[None])
+    tcyl = torch.minimum(tcyl, torch.where(cap, tc, torch.full_like(tc, float("inf"))))
+    best = torch.minimum(best, tcyl.amin(-1))
+    r = best.reshape(spec.height, spec.width).cpu().numpy()
+    r = np.where(np.isfinite(r) & (r >= spec.near_plane) & (r <= spec.far_plane), r, 0.0)
+    rng = np.random.default_rng(frame_seed)
+    if noise:
+        r = np.where(r > 0, r + rng.standard_normal(r.shape) * 0.01, 0.0)
+    if keep < 1.0:
+        r = np.where(rng.random(r.shape) < keep, r, 0.0)
+    return r.astype(np.float32)
+
+
+def lidar_dataset(n_maps: int, n_frames: int, seed=1004, device="cpu", spec: LidarSpec = LIDAR_64):
+    """(spec, scene, poses[map][frame], ranges[map][frame], keep[map]) for the batched LiDAR
+    workload: map k drives road k with its own weave phase and keeps a fraction
+    0.40 + 0.55 k / (n_maps - 1) of its returns (40 % to 95 %)."""
+    scene = make_outdoor_scene(seed)
+    keep = [0.40 + 0.55 * k / max(n_maps - 1, 1) for k in range(n_maps)]
+    poses = [road_trajectory(k, n_frames, phase=0.7 * k) for k in range(n_maps)]
+    ranges = [[render_range(scene, spec, T, seed * 7919 + 1000 * k + i, keep=keep[k], device=device)
+               for i, T in enumerate(poses[k])] for k in range(n_maps)]
+    return spec, scene, poses, ranges, keep
