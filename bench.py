@@ -265,6 +265,10 @@ def run_ours(args, ws, rank, local):
         mr[st] = {"value": K / (v["dev_ms"] * 1e-3), "ms_per_step": v["dev_ms"] / K}
         del v["map"], v["tracker"], v["fp"]
 
+    # eight LiDAR occupancy maps in one batch
+    lidar = _lidar_bench(se, torch, dev, args.lidar_steps, args.warmup, flush)
+    lidar_data = lidar.pop("_data")
+
     times = torch.tensor([g32["dev_ms"], e2e_s, plain["dev_ms"], g16["dev_ms"]], dtype=torch.float64,
                          device=dev)
     if ws > 1:
@@ -333,11 +337,13 @@ def run_ours(args, ws, rank, local):
                                  "with the 585-entry voxel pyramid), captured graph per frame",
                      "graph_f32": mr["f32"], "graph_f16": mr["f16"]},
         "adjoint": adjoint,
+        "lidar_batch": lidar,
         "gen_s": gen_s,
         "clocks": g32["clocks"],
     }
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(frames, poses, sensor_spec, args.warmup, 2 * K, args.cpu_budget_s)
+        out["lidar_batch"]["cpu_baseline"] = lidar_cpu_baseline(lidar_data)
     return out
 
 
@@ -448,6 +454,153 @@ def _adjoint_bench(se, torch, m, sensor, T_gt, obs, flush, reps=20, gn_steps=50,
             "pose_err_final": {"m": t1, "deg": r1}}
 
 
+# ------------------------------------------------------------------ 8-map LiDAR batch --
+
+LIDAR_MAPS = 8
+LIDAR_RES = 0.4
+LIDAR_MAX_BLOCKS = 1 << 16
+
+
+def _lidar_maps(se, n):
+    T_MW = np.eye(4, dtype=np.float32)
+    T_MW[:3, 3] = (51.2, 51.2, 12.8)
+    return [se.Map(102.4, LIDAR_RES, res_type="multi", field="occupancy", max_blocks=LIDAR_MAX_BLOCKS,
+                   T_MW=T_MW) for _ in range(n)]
+
+
+def _lidar_bench(se, torch, dev, K, warmup, flush):
+    """Scans/s of 8 occupancy maps, each driving its own road with its own LiDAR stream, every
+    call integrating one scan into each map. Variants: batched launches replayed from a captured
+    CUDA graph after autotuning (the headline), batched launches without the graph, one map per
+    call (the reference's API shape), and the graph end to end from pinned host memory."""
+    from supereight2_gb300 import synthetic as syn
+    tune = 8  # the autotuner's calls, part of the warm-up
+    W = max(warmup, 3) + tune
+    n_frames = W + K
+    t0 = time.perf_counter()
+    spec, scene, poses, ranges, keep = syn.lidar_dataset(LIDAR_MAPS, n_frames, device=dev)
+    gen_s = time.perf_counter() - t0
+    sensor = se.OusterLidar.from_spec(spec)
+    imgs = [torch.from_numpy(np.stack([ranges[k][i] for k in range(LIDAR_MAPS)])).to(dev) for i in range(n_frames)]
+    Ts = [np.stack([poses[k][i] for k in range(LIDAR_MAPS)]).astype(np.float32) for i in range(n_frames)]
+    valid = [float(np.mean([(ranges[k][i] > 0).mean() for i in range(n_frames)])) for k in range(LIDAR_MAPS)]
+
+    def timed(step):
+        ev = []
+        for i in range(W):
+            step(i)
+        torch.cuda.synchronize()
+        for i in range(W, W + K):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            step(i)
+            b.record()
+            ev.append((a, b))
+        torch.cuda.synchronize()
+        return float(sum(a.elapsed_time(b) for a, b in ev))
+
+    res = {}
+    # batched + graph + autotuned
+    maps = _lidar_maps(se, LIDAR_MAPS)
+    batch = se.OccupancyBatch(maps, sensor, graph=True, autotune=True)
+    ms_graph = timed(lambda i: batch.integrate(imgs[i], Ts[i], i))
+    tiles, left = batch.tiles()
+    for m in maps:
+        m.check()
+    blocks = [int(m.occupancy_stats()[0]) for m in maps]
+    del batch, maps
+    # batched, no graph, default geometry
+    maps = _lidar_maps(se, LIDAR_MAPS)
+    batch = se.OccupancyBatch(maps, sensor, graph=False)
+    ms_batch = timed(lambda i: batch.integrate(imgs[i], Ts[i], i))
+    for m in maps:
+        m.check()
+    del batch, maps
+    # one map per call
+    maps = _lidar_maps(se, LIDAR_MAPS)
+    integ = [se.MapIntegrator(m) for m in maps]
+    ms_single = timed(lambda i: [integ[k].integrateDepth(i, imgs[i][k], sensor, Ts[i][k]) for k in range(LIDAR_MAPS)])
+    for m in maps:
+        m.check()
+    del integ, maps
+    # end to end: pinned host scans copied in every call, the maps' counters read back
+    maps = _lidar_maps(se, LIDAR_MAPS)
+    batch = se.OccupancyBatch(maps, sensor, graph=True, autotune=True)
+    host = [im.cpu().pin_memory() for im in imgs]
+    stage = torch.empty_like(imgs[0])
+    for i in range(W):
+        stage.copy_(host[i], non_blocking=True)
+        batch.integrate(stage, Ts[i], i)
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for i in range(W, W + K):
+        stage.copy_(host[i], non_blocking=True)
+        batch.integrate(stage, Ts[i], i)
+        _ = [m.occupancy_stats() for m in maps]  # synchronises; 8 x 4 counters back
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - e0
+    for m in maps:
+        m.check()
+    del batch, maps
+    scans = LIDAR_MAPS * K
+    bd = 5  # 256^3 voxels: blocks at depth 5
+    levels = 6  # pooling levels of a 64-row image
+    launches = 1 + 1 + (levels - 1) + 1 + bd + 1 + (bd + 1) + 2 + (bd - 1) + 1
+    return {
+        "workload": f"{LIDAR_MAPS} multi-res occupancy maps (256^3 voxels at {LIDAR_RES} m, 8^3 blocks), "
+                    f"LiDAR {spec.height}x{spec.width} (+-22.5 deg, {spec.near_plane}-{spec.far_plane} m), "
+                    "seeded outdoor scene (ground + 100 boxes + 100 cylinders over 100 x 100 m), each map "
+                    "driving its own road at 1 m per scan; one step = one scan into every map",
+        "metric": "scans/s", "value": scans / (ms_graph * 1e-3), "ms_per_step": ms_graph / K,
+        "steps": K, "warmup": W, "kept_return_fraction": keep, "valid_pixel_fraction": valid,
+        "blocks_listed_last_step": blocks,
+        "variants": {
+            "batched_graph_autotuned": {"value": scans / (ms_graph * 1e-3), "ms_per_step": ms_graph / K,
+                                        "tiles_ctas_per_sm": {"carve": tiles[0], "lists": tiles[1],
+                                                              "blocks": tiles[2]}},
+            "batched_no_graph": {"value": scans / (ms_batch * 1e-3), "ms_per_step": ms_batch / K},
+            "one_map_per_call": {"value": scans / (ms_single * 1e-3), "ms_per_step": ms_single / K},
+        },
+        "e2e": {"value": scans / e2e_s, "unit": "scans/s",
+                "h2d_bytes_per_step": LIDAR_MAPS * spec.width * spec.height * 4,
+                "d2h_bytes_per_step": LIDAR_MAPS * 35 * 4},
+        "gpu_launches_per_step": launches,
+        "gen_s": gen_s,
+        "l2": "flushed (256 MiB write) between steps",
+        "_data": (spec, poses, ranges, W, K),
+    }
+
+
+def lidar_cpu_baseline(data, budget_s=20.0):
+    """The oracle (all host threads) integrating the same scans: map k's scans in order, the
+    GPU's timed scans (after its warm-up) timed, maps in turn until budget_s is spent."""
+    from oracle import pyoracle as o
+    spec, poses, ranges, W, K = data
+    o.set_num_threads(os.cpu_count() or 1)
+    T_MW = np.eye(4, dtype=np.float32)
+    T_MW[:3, 3] = (51.2, 51.2, 12.8)
+    L = o.lidar(spec.width, spec.height, spec.elevation_min_deg, spec.elevation_max_deg,
+                spec.near_plane, spec.far_plane)
+    times = []
+    t_start = time.perf_counter()
+    n_maps = 0
+    for k in range(len(poses)):
+        m = o.OracleOccMap(102.4, LIDAR_RES, T_MW=T_MW)
+        for i in range(W + K):
+            t0 = time.perf_counter()
+            m.integrate_lidar(ranges[k][i], L, poses[k][i].astype(np.float32), i)
+            if i >= W:
+                times.append(time.perf_counter() - t0)
+        n_maps += 1
+        del m
+        if time.perf_counter() - t_start > budget_s:
+            break
+    return {"value": len(times) / sum(times), "unit": "scans/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"scans {W}..{W + K - 1} of {n_maps} of the {len(poses)} maps (each map's scans "
+                      f"0..{W - 1} integrated untimed first), {sum(times):.1f} s of CPU work"}
+
+
 # --------------------------------------------------------------------- CPU oracle arm --
 
 def _oracle_pipeline(frames, poses, spec, n_warm, n_steps, budget_s=None):
@@ -529,6 +682,7 @@ def main():
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
+    ap.add_argument("--lidar-steps", type=int, default=20)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

@@ -178,16 +178,24 @@ SE_GPU_API se_gpu_status se_gpu_integrate_range(se_gpu_map* map, const float* ra
 /* Batched occupancy integration; no counterpart in the reference, which integrates one map per
  * call. n (<= 16) occupancy maps with one sensor (a pinhole camera or a LiDAR: exactly one of
  * the two pointers non-NULL) integrate one frame each per call, every stage of the pipeline in
- * one launch over all maps' work (uneven block and node counts share the grid). With use_graph
- * the launches of a call are captured once into a CUDA graph (on the first call) and each call
- * replays it with that call's poses and images. The maps stay owned by the caller and must
+ * one launch over all maps' work (uneven block and node counts share the grid). The maps stay owned by the caller and must
  * outlive the batch; calls on a batch are not re-entrant and none of its maps may be used by
  * another call in flight. */
 typedef struct se_gpu_occ_batch se_gpu_occ_batch;
+/* flags: SE_GPU_OCC_BATCH_GRAPH (capture and replay, as above) and SE_GPU_OCC_BATCH_AUTOTUNE:
+ * the first 8 calls run in turn 4 candidate launch geometries (CTAs per SM of the carver, list
+ * and block stages), timed with events (these calls synchronise the stream), and the batch
+ * keeps the fastest per stage; the graph is captured after tuning. Results do not depend on the
+ * geometry. */
+#define SE_GPU_OCC_BATCH_GRAPH 1
+#define SE_GPU_OCC_BATCH_AUTOTUNE 2
 SE_GPU_API se_gpu_status se_gpu_occ_batch_create(se_gpu_map* const* maps, int n,
                                                  const se_gpu_pinhole* pinhole,
-                                                 const se_gpu_lidar* lidar, int use_graph,
+                                                 const se_gpu_lidar* lidar, int flags,
                                                  se_gpu_occ_batch** batch);
+/* The launch geometry in use (CTAs per SM: carver, lists, blocks) and the tuning calls left. */
+SE_GPU_API se_gpu_status se_gpu_occ_batch_tiles(const se_gpu_occ_batch* batch, int tiles[3],
+                                                int* tuning_calls_left);
 /* images_dev[i]: map i's depth / range image on the device; T_WS: n row-major 4x4 poses
  * (host); timestamps: n frame numbers (host). Stream-ordered. */
 SE_GPU_API se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* batch,

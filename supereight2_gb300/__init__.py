@@ -96,6 +96,7 @@ SIGNATURES = {
                                           C.c_int, C.POINTER(_VP)]),
     "se_gpu_occ_batch_integrate": (C.c_int, [_VP, _VP, _F16, _VP, _VP]),
     "se_gpu_occ_batch_destroy": (C.c_int, [_VP]),
+    "se_gpu_occ_batch_tiles": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "se_gpu_map_integrate_stats": (C.c_int, [_VP, C.POINTER(_IntegrateStats)]),
     "se_gpu_raycast": (C.c_int, [_VP, C.POINTER(_Pinhole), _F16, _VP, _VP, _VP, _VP]),
     "se_gpu_map_download_blocks": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP,
@@ -440,9 +441,11 @@ class MapIntegrator:
 class OccupancyBatch:
     """Several occupancy maps integrated together, one frame each per call, every pipeline stage
     in one launch over all maps (no counterpart in the reference). graph=True captures the
-    launches of a call into a CUDA graph on the first call and replays it afterwards."""
+    launches of a call into a CUDA graph on the first call and replays it afterwards;
+    autotune=True spends the first 8 calls timing 4 launch geometries and keeps the fastest per
+    stage (the graph is captured after that)."""
 
-    def __init__(self, maps, sensor, graph=True):
+    def __init__(self, maps, sensor, graph=True, autotune=False):
         self.maps = list(maps)
         self.sensor = sensor
         self._L = library()
@@ -451,9 +454,17 @@ class OccupancyBatch:
         pin = C.byref(s) if isinstance(sensor, PinholeCamera) else None
         lid = C.byref(s) if isinstance(sensor, OusterLidar) else None
         h = _VP()
-        _check(self._L.se_gpu_occ_batch_create(arr, len(self.maps), pin, lid, int(bool(graph)),
-                                               C.byref(h)), "se_gpu_occ_batch_create")
+        flags = (1 if graph else 0) | (2 if autotune else 0)
+        _check(self._L.se_gpu_occ_batch_create(arr, len(self.maps), pin, lid, flags, C.byref(h)),
+               "se_gpu_occ_batch_create")
         self.h = h
+
+    def tiles(self):
+        """(CTAs per SM of the carver, list and block stages), tuning calls left."""
+        t = (C.c_int * 3)()
+        left = C.c_int()
+        _check(self._L.se_gpu_occ_batch_tiles(self.h, t, C.byref(left)), "se_gpu_occ_batch_tiles")
+        return tuple(t), left.value
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -1540,40 +1540,104 @@ static OccJob occ_job(const se_gpu_occ_map* om)
     return J;
 }
 
-// Launch geometry of the stages (CTAs per SM); tuned by the batch's autotuner.
+// Launch geometry of the grid-stride stages in CTAs per SM; the batch's autotuner picks one
+// per stage kind.
+enum { kTileCarve = 0, kTileList, kTileBlocks, kTileKinds };
 struct OccTiles {
-    int carve_ctas = 8;   // 128 threads each
-    int list_ctas = 4;    // 256 threads each (node lists, free levels, propagation sets)
-    int block_ctas = 8;   // 256 threads each, one warp per block
-    int block_threads = 256;
+    int ctas[kTileKinds] = {8, 4, 8}; // carve (128 threads), lists (256), blocks (256, a warp per block)
 };
 
+// Events around the tunable launches of one frame, for the autotuner.
+struct OccStageTimer {
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> kind;
+    int used = 0;
+    se_gpu_status mark(int k, cudaStream_t stream)
+    {
+        if (used == (int) ev.size()) {
+            cudaEvent_t e;
+            SE_CUDA_TRY(cudaEventCreate(&e));
+            ev.push_back(e);
+            kind.push_back(0);
+        }
+        kind[used] = k;
+        SE_CUDA_TRY(cudaEventRecord(ev[used++], stream));
+        return SE_GPU_OK;
+    }
+    ~OccStageTimer()
+    {
+        for (cudaEvent_t e : ev)
+            cudaEventDestroy(e);
+    }
+};
+
+#define OCC_MARK(k)                                                                          \
+    do {                                                                                     \
+        if (timer) {                                                                         \
+            const se_gpu_status _s = timer->mark((k), stream);                               \
+            if (_s != SE_GPU_OK)                                                             \
+                return _s;                                                                   \
+        }                                                                                    \
+    } while (0)
+
 // Every launch of one frame of every map in L (device copy at Ld); no host synchronisation, so
-// the sequence can be captured into a graph. The begin launch is the first.
+// the sequence can be captured into a graph. The begin launch is the first. With a timer, an
+// event is recorded before each tunable launch (kind) and after it (kind -1).
 static se_gpu_status occ_enqueue(const OccLaunch& L, const OccLaunch* Ld, const OccStep& step, const OccTiles& t,
-                                 cudaStream_t stream)
+                                 cudaStream_t stream, OccStageTimer* timer = nullptr)
 {
     const int sms = device_sm_count();
     const int npx = L.sensor.w * L.sensor.h;
     const int n = L.n;
+    const int carve = sms * t.ctas[kTileCarve], list = sms * t.ctas[kTileList], blocks = sms * t.ctas[kTileBlocks];
     occ_begin_kernel<<<n, 64, 0, stream>>>(Ld, step);
     occ_pixels_kernel<<<dim3((npx + 255) / 256, n), 256, 0, stream>>>(Ld);
     for (int l = 1; l < L.sensor.levels; ++l)
         occ_pool_level_kernel<<<dim3((npx + 255) / 256, 2 * n), 256, 0, stream>>>(Ld, l);
     occ_root_kernel<<<1, 32, 0, stream>>>(Ld);
-    for (int d = 1; d <= L.max_block_depth; ++d)
-        occ_carve_kernel<<<sms * t.carve_ctas, 128, 0, stream>>>(Ld, d);
-    occ_nodes_kernel<<<sms * t.list_ctas, 256, 0, stream>>>(Ld);
-    for (int it = 0; it <= L.max_block_depth; ++it)
-        occ_free_nodes_kernel<<<sms * t.list_ctas, 256, 0, stream>>>(Ld, it);
-    occ_blocks_kernel<<<sms * t.block_ctas, t.block_threads, 0, stream>>>(Ld);
-    occ_propagate_blocks_kernel<<<sms * t.block_ctas, 256, 0, stream>>>(Ld);
-    for (int d = L.max_block_depth - 1; d > 0; --d)
-        occ_propagate_nodes_kernel<<<sms * t.list_ctas, 256, 0, stream>>>(Ld, d);
+    for (int d = 1; d <= L.max_block_depth; ++d) {
+        OCC_MARK(kTileCarve);
+        occ_carve_kernel<<<carve, 128, 0, stream>>>(Ld, d);
+    }
+    OCC_MARK(kTileList);
+    occ_nodes_kernel<<<list, 256, 0, stream>>>(Ld);
+    for (int it = 0; it <= L.max_block_depth; ++it) {
+        OCC_MARK(kTileList);
+        occ_free_nodes_kernel<<<list, 256, 0, stream>>>(Ld, it);
+    }
+    OCC_MARK(kTileBlocks);
+    occ_blocks_kernel<<<blocks, 256, 0, stream>>>(Ld);
+    OCC_MARK(kTileBlocks);
+    occ_propagate_blocks_kernel<<<blocks, 256, 0, stream>>>(Ld);
+    for (int d = L.max_block_depth - 1; d > 0; --d) {
+        OCC_MARK(kTileList);
+        occ_propagate_nodes_kernel<<<list, 256, 0, stream>>>(Ld, d);
+    }
+    OCC_MARK(-1);
     occ_propagate_root_kernel<<<1, 32, 0, stream>>>(Ld);
     SE_CUDA_TRY(cudaGetLastError());
     return SE_GPU_OK;
 }
+
+// The autotuner of a batch: during its first kTuneFrames calls each call runs one candidate
+// geometry (candidate c: carve 2 << c, lists 1 << c, blocks 2 << c CTAs per SM) with events
+// around the tunable launches; afterwards each stage kind keeps the candidate with the least
+// accumulated time. Results do not depend on the geometry: every stage is a grid-stride loop
+// over the same work.
+struct OccTuner {
+    static constexpr int kCand = 4, kRounds = 2, kTuneFrames = kCand * kRounds;
+    int frames = 0;
+    double ms[kTileKinds][kCand] = {};
+    OccStageTimer timer;
+    static OccTiles candidate(int c)
+    {
+        OccTiles t;
+        t.ctas[kTileCarve] = 2 << c;
+        t.ctas[kTileList] = 1 << c;
+        t.ctas[kTileBlocks] = 2 << c;
+        return t;
+    }
+};
 
 static void occ_fill_step(OccStep& step, int j, const float* T_WS16, const float* image, int timestamp)
 {
@@ -1632,6 +1696,7 @@ struct se_gpu_occ_batch {
     OccLaunch* launch_dev = nullptr;
     OccTiles tiles;
     int use_graph = 0;
+    OccTuner* tuner = nullptr; // while autotuning
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t begin_node = nullptr;
@@ -1692,7 +1757,9 @@ se_gpu_status se_gpu_occ_batch_create(se_gpu_map* const* maps, int n, const se_g
     const OccSensor S = occ_sensor(pinhole, lidar);
     se_gpu_occ_batch* b = new se_gpu_occ_batch();
     b->maps.assign(maps, maps + n);
-    b->use_graph = use_graph;
+    b->use_graph = use_graph & SE_GPU_OCC_BATCH_GRAPH;
+    if (use_graph & SE_GPU_OCC_BATCH_AUTOTUNE)
+        b->tuner = new OccTuner();
     b->device = maps[0]->device;
     b->launch_host = new OccLaunch();
     std::memset(b->launch_host, 0, sizeof(OccLaunch));
@@ -1736,6 +1803,33 @@ se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* b, const float* const
         occ_fill_step(step, j, T_WS + 16 * j, images_dev[j], timestamps[j]);
         b->maps[j]->last_stream = s;
     }
+    if (b->tuner) {
+        OccTuner& tu = *b->tuner;
+        const int c = tu.frames % OccTuner::kCand;
+        tu.timer.used = 0;
+        se_gpu_status st = occ_enqueue(*b->launch_host, b->launch_dev, step, OccTuner::candidate(c), s, &tu.timer);
+        if (st != SE_GPU_OK)
+            return st;
+        SE_CUDA_TRY(cudaEventSynchronize(tu.timer.ev[tu.timer.used - 1]));
+        for (int i = 0; i + 1 < tu.timer.used; ++i) {
+            float ms = 0.0f;
+            SE_CUDA_TRY(cudaEventElapsedTime(&ms, tu.timer.ev[i], tu.timer.ev[i + 1]));
+            if (tu.timer.kind[i] >= 0)
+                tu.ms[tu.timer.kind[i]][c] += ms;
+        }
+        if (++tu.frames == OccTuner::kTuneFrames) {
+            for (int k = 0; k < kTileKinds; ++k) {
+                int best = 0;
+                for (int cc = 1; cc < OccTuner::kCand; ++cc)
+                    if (tu.ms[k][cc] < tu.ms[k][best])
+                        best = cc;
+                b->tiles.ctas[k] = OccTuner::candidate(best).ctas[k];
+            }
+            delete b->tuner;
+            b->tuner = nullptr;
+        }
+        return SE_GPU_OK;
+    }
     if (!b->use_graph)
         return occ_enqueue(*b->launch_host, b->launch_dev, step, b->tiles, s);
     if (!b->exec) {
@@ -1775,10 +1869,22 @@ se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* b, const float* const
     return SE_GPU_OK;
 }
 
+se_gpu_status se_gpu_occ_batch_tiles(const se_gpu_occ_batch* b, int tiles[3], int* tuning)
+{
+    if (!b || !tiles)
+        return bad(SE_GPU_ERR_BAD_ARG, "se_gpu_occ_batch_tiles: null argument");
+    for (int k = 0; k < kTileKinds; ++k)
+        tiles[k] = b->tiles.ctas[k];
+    if (tuning)
+        *tuning = b->tuner ? OccTuner::kTuneFrames - b->tuner->frames : 0;
+    return SE_GPU_OK;
+}
+
 se_gpu_status se_gpu_occ_batch_destroy(se_gpu_occ_batch* b)
 {
     if (!b)
         return SE_GPU_OK;
+    delete b->tuner;
     if (b->exec)
         cudaGraphExecDestroy(b->exec);
     if (b->graph)

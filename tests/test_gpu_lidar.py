@@ -55,14 +55,14 @@ def test_lidar_single_map_matches_oracle(oracle, gpu):
     _compare(om, gm)
 
 
-@pytest.mark.parametrize("graph", [False, True])
-def test_lidar_batch_matches_oracle(oracle, gpu, graph):
+@pytest.mark.parametrize("graph,autotune", [(False, False), (True, False), (True, True)])
+def test_lidar_batch_matches_oracle(oracle, gpu, graph, autotune):
     import torch
     spec, poses, ranges = _lidar_data(4)
     n = len(poses)
     oms = [oracle.OracleOccMap(102.4, 0.4, T_MW=T_MW) for _ in range(n)]
     gms = [_gpu_map(gpu) for _ in range(n)]
-    batch = gpu.OccupancyBatch(gms, gpu.OusterLidar.from_spec(spec), graph=graph)
+    batch = gpu.OccupancyBatch(gms, gpu.OusterLidar.from_spec(spec), graph=graph, autotune=autotune)
     ol = _oracle_lidar(oracle, spec)
     for i in range(len(poses[0])):
         imgs = torch.from_numpy(np.stack([ranges[k][i] for k in range(n)])).cuda()
@@ -70,6 +70,8 @@ def test_lidar_batch_matches_oracle(oracle, gpu, graph):
         batch.integrate(imgs, Ts, i)
         for k in range(n):
             oms[k].integrate_lidar(ranges[k][i], ol, Ts[k], i)
+    if autotune:
+        assert batch.tiles()[1] == 8 - len(poses[0])  # still tuning: every frame ran a candidate
     counts = []
     for om, gm in zip(oms, gms):
         gm.check()
@@ -98,3 +100,21 @@ def test_pinhole_batch_matches_oracle(oracle, gpu):
     for om, gm in zip(oms, gms):
         gm.check()
         _compare(om, gm)
+
+
+def test_lidar_batch_after_tuning_matches_oracle(oracle, gpu):
+    """Ten scans: eight tuning calls, then the graph captured with the chosen geometry."""
+    import torch
+    spec, poses, ranges = _lidar_data(10, roads=(5,))
+    om = oracle.OracleOccMap(102.4, 0.4, T_MW=T_MW)
+    gm = _gpu_map(gpu)
+    batch = gpu.OccupancyBatch([gm], gpu.OusterLidar.from_spec(spec), graph=True, autotune=True)
+    ol = _oracle_lidar(oracle, spec)
+    for i, (r, T) in enumerate(zip(ranges[0], poses[0])):
+        T = T.astype(np.float32)
+        batch.integrate([torch.from_numpy(r).cuda()], T[None], i)
+        om.integrate_lidar(r, ol, T, i)
+    tiles, left = batch.tiles()
+    assert left == 0 and all(t in (1, 2, 4, 8, 16) for t in tiles)
+    gm.check()
+    _compare(om, gm)
