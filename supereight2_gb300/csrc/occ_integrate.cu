@@ -209,10 +209,44 @@ struct PoolQuery {
     int crossing, known;
 };
 
+// Number of positions the pooling loops visit between lo and hi: lo + s, lo + s + step, ...,
+// the last one clamped to hi - s (a single position hi - s when the range is narrower than 2s).
+__device__ __forceinline__ int visit_count(int lo, int hi, int s, int step)
+{
+    const int d = (hi - s) - (lo + s);
+    return d <= 0 ? 1 : (d + step - 1) / step + 1;
+}
+
 // poolBoundingBox (dense_pooling_image_impl.hpp:218-290; Ouster: 607-731, columns outside the
-// image fetched from the other side) over the pyramid of w * h levels
-__device__ PoolQuery pool_bounding_box(const float4* __restrict__ pool, int w, int h, int max_level, bool wrap,
-                                       int u_min, int u_max, int v_min, int v_max)
+// image fetched from the other side) of the depth and the sigma pyramids (w * h per level) over
+// the same box, by a whole warp: the lanes share the visited pixels, two per lane in flight, then
+// reduce. The reference's statistics only enter through "all visited pixels unknown" and "some
+// visited pixel unknown or partly known", and min / max do not depend on the order, so the
+// result equals the serial loops'. Only the sigma query's max is used by the carver.
+struct PoolPair {
+    PoolQuery d;
+    float sigma_max;
+};
+
+__device__ __forceinline__ int pool_index(int k, int nu, int u_min, int u_max, int v_min, int v_max, int s, int step,
+                                          int w, bool u_wrap)
+{
+    const int iu = k % nu, iv = k / nu;
+    const int u = min(u_min + s + iu * step, u_max - s);
+    const int v = min(v_min + s + iv * step, v_max - s);
+    int uf = u;
+    if (u_wrap) {
+        if (u < 0)
+            uf += w;
+        else if (u > w - 1)
+            uf -= w;
+    }
+    return uf + w * v;
+}
+
+__device__ PoolPair pool_bounding_box(const float4* __restrict__ pool_d, const float4* __restrict__ pool_s, int w,
+                                      int h, int max_level, bool wrap, int u_min, int u_max, int v_min, int v_max,
+                                      int lane)
 {
     const int min_side = min(u_max - u_min, v_max - v_min);
     const int half = min_side / 2;
@@ -222,53 +256,60 @@ __device__ PoolQuery pool_bounding_box(const float4* __restrict__ pool, int w, i
         lc = (int) ceil(log2((double) half));
     const int level = max(0, min(max_level, lc));
     const int s = level > 0 ? 1 << max(level - 1, 0) : 0;
-    const bool u_wrap = wrap && (u_min < 0 || u_max > w - 1);
-    PoolQuery b{FLT_MAX, FLT_MIN, 0, 0};
-    unsigned long long n = 0, n_unknown = 0, n_part = 0;
     const int step = 2 * s + 1;
-    const float4* Lv = pool + (size_t) level * w * h;
-    for (int v = v_min + s; true; v += step) {
-        if (v > v_max - s)
-            v = v_max - s;
-        for (int u = u_min + s; true; u += step) {
-            if (u > u_max - s)
-                u = u_max - s;
-            int uf = u;
-            if (u_wrap) {
-                if (u < 0)
-                    uf += w;
-                else if (u > w - 1)
-                    uf -= w;
-            }
-            const float4 p = Lv[uf + w * v];
-            if (b.max < p.y)
-                b.max = p.y;
-            if (b.min > p.x)
-                b.min = p.x;
-            if (p.w == 2.0f) {
-                ++n_unknown;
-                ++n_part;
-            }
-            else if (p.w == 1.0f) {
-                ++n_part;
-            }
-            ++n;
-            if (u == u_max - s)
-                break;
-        }
-        if (v == v_max - s)
-            break;
+    const bool u_wrap = wrap && (u_min < 0 || u_max > w - 1);
+    const int nu = visit_count(u_min, u_max, s, step), nv = visit_count(v_min, v_max, s, step);
+    const int n = nu * nv;
+    const float4* Ld = pool_d + (size_t) level * w * h;
+    const float* Ls = reinterpret_cast<const float*>(pool_s + (size_t) level * w * h) + 1; // .y = max
+    float mn = FLT_MAX, mx = FLT_MIN, smx = FLT_MIN; // Pixel::knownPixel
+    bool all_unknown = true, any_part = false;
+    for (int k = lane; k < n; k += 64) {
+        const int i0 = pool_index(k, nu, u_min, u_max, v_min, v_max, s, step, w, u_wrap);
+        const bool two = k + 32 < n;
+        const int i1 = two ? pool_index(k + 32, nu, u_min, u_max, v_min, v_max, s, step, w, u_wrap) : i0;
+        const float4 p0 = Ld[i0], p1 = Ld[i1];
+        const float s0 = Ls[4 * (size_t) i0], s1 = Ls[4 * (size_t) i1];
+        if (mx < p0.y)
+            mx = p0.y;
+        if (mn > p0.x)
+            mn = p0.x;
+        if (mx < p1.y)
+            mx = p1.y;
+        if (mn > p1.x)
+            mn = p1.x;
+        if (smx < s0)
+            smx = s0;
+        if (smx < s1)
+            smx = s1;
+        all_unknown = all_unknown && p0.w == 2.0f && p1.w == 2.0f;
+        any_part = any_part || p0.w >= 1.0f || p1.w >= 1.0f;
     }
-    if (n == n_unknown)
-        b.known = 2;
-    else if (n_part > 0)
-        b.known = 1;
-    return b;
+    for (int o = 16; o > 0; o >>= 1) {
+        const float omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
+        const float osx = __shfl_xor_sync(0xffffffffu, smx, o);
+        if (mn > omn)
+            mn = omn;
+        if (mx < omx)
+            mx = omx;
+        if (smx < osx)
+            smx = osx;
+    }
+    PoolPair r;
+    r.d = PoolQuery{mn, mx, 0, 0};
+    if (__all_sync(0xffffffffu, all_unknown))
+        r.d.known = 2;
+    else if (__any_sync(0xffffffffu, any_part))
+        r.d.known = 1;
+    r.sigma_max = smx;
+    return r;
 }
 
-// conservativeQuery (dense_pooling_image_impl.hpp:295-347; Ouster: 734-781 clips only v)
-__device__ PoolQuery conservative_query(const float4* __restrict__ pool, int w, int h, int max_level, bool wrap,
-                                        int u_min, int v_min, int u_max, int v_max)
+// conservativeQuery (dense_pooling_image_impl.hpp:295-347; Ouster: 734-781 clips only v) of the
+// depth and the sigma pyramids, by a whole warp with uniform arguments
+__device__ PoolPair conservative_query(const float4* __restrict__ pool_d, const float4* __restrict__ pool_s, int w,
+                                       int h, int max_level, bool wrap, int u_min, int v_min, int u_max, int v_max,
+                                       int lane)
 {
     bool u_in = true, u_out = false, v_in = true, v_out = false;
     const float wl = (float) (unsigned) (w - 1), hl = (float) (unsigned) (h - 1);
@@ -301,10 +342,10 @@ __device__ PoolQuery conservative_query(const float4* __restrict__ pool, int w, 
         v_max = h - 1;
     }
     if (u_out || v_out || u_min == u_max || v_min == v_max)
-        return PoolQuery{0.0f, 0.0f, 2, 2};
-    PoolQuery p = pool_bounding_box(pool, w, h, max_level, wrap, u_min, u_max, v_min, v_max);
+        return PoolPair{PoolQuery{0.0f, 0.0f, 2, 2}, 0.0f};
+    PoolPair p = pool_bounding_box(pool_d, pool_s, w, h, max_level, wrap, u_min, u_max, v_min, v_max, lane);
     if (!u_in || !v_in)
-        p.crossing = 1;
+        p.d.crossing = 1;
     return p;
 }
 
@@ -376,36 +417,37 @@ __device__ void occ_allocate_children(const OccDevice& m, int n)
         occ_aabb_extend(m, nc.x, nc.y, nc.z, nc.w);
 }
 
-// DensePoolingImage::maxValue over the coarsest level and VolumeCarver's max depth
-// (volume_carver_impl.hpp:28-38), then the root's children as the first frontier; one thread
-// per map.
+// DensePoolingImage::maxValue over the coarsest level (the lanes share the visited pixels) and
+// VolumeCarver's max depth (volume_carver_impl.hpp:28-38), then the root's children as the first
+// frontier; one warp per map.
 __global__ void occ_root_kernel(const OccLaunch* __restrict__ Lp)
 {
     const OccLaunch& L = *Lp;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= L.n)
+    const int j = blockIdx.x;
+    const int lane = threadIdx.x & 31;
+    if (j >= L.n || threadIdx.x >= 32)
         return;
     const OccJob& J = L.job[j];
     const int w = L.sensor.w, h = L.sensor.h;
     const int max_level = L.sensor.levels - 1;
     const float4* Lmax = J.pool_depth + (size_t) max_level * w * h;
     const int s = 1 << (max_level - 1);
+    // rows s, 3s, ... and the last row h - s - 1; the same for the columns
+    const int nv = visit_count(0, h - 1, s, 2 * s), nu = visit_count(0, w - 1, s, 2 * s);
     float mv = 0.0f;
-    for (int v = s; true; v += 2 * s) {
-        if (v > h - s - 1)
-            v = h - s - 1;
-        for (int u = s; true; u += 2 * s) {
-            if (u > w - s - 1)
-                u = w - s - 1;
-            const float m = Lmax[u + w * v].y;
-            if (mv < m)
-                mv = m;
-            if (u == w - s - 1)
-                break;
-        }
-        if (v == h - s - 1)
-            break;
+    for (int k = lane; k < nu * nv; k += 32) {
+        const int u = min(s + (k % nu) * 2 * s, w - s - 1), v = min(s + (k / nu) * 2 * s, h - s - 1);
+        const float m = Lmax[u + w * v].y;
+        if (mv < m)
+            mv = m;
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        const float om = __shfl_xor_sync(0xffffffffu, mv, o);
+        if (mv < om)
+            mv = om;
+    }
+    if (lane != 0)
+        return;
     J.max_value[0] = mv;
     const float t = mv + J.tau_max;
     J.max_value[1] = L.sensor.far_plane < t ? L.sensor.far_plane : t;
@@ -458,20 +500,37 @@ __device__ __forceinline__ OccD octant_max_data(const OccDevice& m, int slot)
     return node_data(m, slot);
 }
 
+// Min / max of a per-corner value over the 8 lanes of each 8-lane group (lane & 7 = corner);
+// exact in any order.
+__device__ __forceinline__ float corner_min(float v)
+{
+    for (int o = 1; o < 8; o <<= 1)
+        v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float corner_max(float v)
+{
+    for (int o = 1; o < 8; o <<= 1)
+        v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
 // The pooled-depth cases shared by both carvers; returns false when the octant is skipped.
 __device__ __forceinline__ bool carve_pooled(const OccLaunch& L, const OccJob& J, int slot, int bu0, int bv0, int bu1,
                                              int bv1, float n_min, float n_max, bool& should_split, int& var,
-                                             bool& projects_inside)
+                                             bool& projects_inside, int lane)
 {
     const OccSensor& S = L.sensor;
     const bool wrap = S.lidar != 0;
-    const PoolQuery pp = conservative_query(J.pool_depth, S.w, S.h, S.levels - 1, wrap, bu0, bv0, bu1, bv1);
+    // both pyramids in one pass; the reference queries sigma only after the two early returns
+    const PoolPair q =
+        conservative_query(J.pool_depth, J.pool_sigma, S.w, S.h, S.levels - 1, wrap, bu0, bv0, bu1, bv1, lane);
+    const PoolQuery& pp = q.d;
     if (pp.known == 2)
         return false;
     if (n_min > pp.max + J.tau_max)
         return false;
-    const PoolQuery sp = conservative_query(J.pool_sigma, S.w, S.h, S.levels - 1, wrap, bu0, bv0, bu1, bv1);
-    var = compute_variance(J, pp.min, pp.max, n_min, n_max, sp.max);
+    var = compute_variance(J, pp.min, pp.max, n_min, n_max, q.sigma_max);
     if (var != 1) {
         const OccD cd = octant_max_data(J.m, slot);
         if (cd.observed && (double) occ_field(cd) <= 0.95 * -100.0)
@@ -487,9 +546,19 @@ __device__ __forceinline__ bool carve_pooled(const OccLaunch& L, const OccJob& J
     return true;
 }
 
-// VolumeCarver<.., PinholeCamera>::operator()(octant) (volume_carver_impl.hpp:132-310)
+__device__ __forceinline__ F3 corner_point(const OccDevice& m, const Tf& T_SW, int k, int cx, int cy, int cz, int size)
+{
+    const F3 p_M = f3(((float) size * (float) (k & 1) + (float) cx) * m.res,
+                      ((float) size * (float) ((k >> 1) & 1) + (float) cy) * m.res,
+                      ((float) size * (float) (k >> 2) + (float) cz) * m.res);
+    return apply(T_SW, apply(m.T_WM, p_M));
+}
+
+// VolumeCarver<.., PinholeCamera>::operator()(octant) (volume_carver_impl.hpp:132-310) by a
+// warp: lane & 7 projects corner lane & 7, the bounding box and the pooling queries are warp-wide.
 __device__ bool carve_pinhole(const OccLaunch& L, const OccJob& J, const OccDyn& D, int slot, int cx, int cy, int cz,
-                              int size, float max_depth_value, bool& should_split, int& var, bool& projects_inside)
+                              int size, float max_depth_value, bool& should_split, int& var, bool& projects_inside,
+                              int lane)
 {
     const OccDevice& m = J.m;
     const Pinhole& ps = L.sensor.s;
@@ -502,37 +571,22 @@ __device__ bool carve_pinhole(const OccLaunch& L, const OccJob& J, const OccDyn&
     const float rad = (float) size * size_to_radius * m.res;
     if (centre_S.z - rad > max_depth_value || centre_S.z + rad < zero_depth_band)
         return false;
-    F3 cS[8];
-    int n_front = 0;
-    for (int k = 0; k < 8; ++k) {
-        const F3 p_M = f3(((float) size * (float) (k & 1) + (float) cx) * m.res,
-                          ((float) size * (float) ((k >> 1) & 1) + (float) cy) * m.res,
-                          ((float) size * (float) (k >> 2) + (float) cz) * m.res);
-        cS[k] = apply(D.T_SW, apply(m.T_WM, p_M));
-        if (!(cS[k].z < zero_depth_band))
-            ++n_front;
-    }
+    const int k = lane & 7;
+    const F3 p = corner_point(m, D.T_SW, k, cx, cy, cz, size);
+    const bool front = !(p.z < zero_depth_band);
+    const int n_front = __popc(__ballot_sync(0xffffffffu, front) & 0xffu);
     if (n_front == 0)
         return false;
-    float pu[8], pv[8];
-    bool ok[8];
-    for (int k = 0; k < 8; ++k) {
-        const F3 p = cS[k];
-        if (fabsf(p.z) < 1.0e-12f) {
-            pu[k] = pv[k] = 0.0f;
-            ok[k] = false;
-            continue;
-        }
+    float pu = 0.0f, pv = 0.0f;
+    bool ok = false;
+    if (!(fabsf(p.z) < 1.0e-12f)) {
         const float rz = 1.0f / p.z;
-        pu[k] = ps.fx * (p.x * rz) + ps.cx;
-        pv[k] = ps.fy * (p.y * rz) + ps.cy;
-        ok[k] = p.z > 0.0f && pu[k] >= -0.5f && pu[k] < (float) ps.w - 0.5f && pv[k] >= -0.5f
-            && pv[k] < (float) ps.h - 0.5f;
+        pu = ps.fx * (p.x * rz) + ps.cx;
+        pv = ps.fy * (p.y * rz) + ps.cy;
+        ok = p.z > 0.0f && pu >= -0.5f && pu < (float) ps.w - 0.5f && pv >= -0.5f && pv < (float) ps.h - 0.5f;
     }
     if (n_front < 8) {
-        bool crosses = false;
-        for (int k = 0; k < 8; ++k)
-            crosses = crosses || ok[k];
+        const bool crosses = (__ballot_sync(0xffffffffu, ok) & 0xffu) != 0u;
         if (camera_in_node(m, D.T_WS, cx, cy, cz, size) || crosses) {
             should_split = true;
             return true;
@@ -548,34 +602,21 @@ __device__ bool carve_pinhole(const OccLaunch& L, const OccJob& J, const OccDyn&
         should_split = true;
         return true;
     }
-    float umin = 0.0f, umax = 0.0f, vmin = 0.0f, vmax = 0.0f, zmin = 0.0f, zmax = 0.0f;
-    for (int k = 0; k < 8; ++k) {
-        float u = pu[k] > 1e7f ? 1e7f : pu[k];
-        float v = pv[k] > 1e7f ? 1e7f : pv[k];
-        u = u < -1e7f ? -1e7f : u;
-        v = v < -1e7f ? -1e7f : v;
-        if (k == 0) {
-            umin = umax = u;
-            vmin = vmax = v;
-            zmin = zmax = cS[0].z;
-        }
-        else {
-            umin = fminf(umin, u);
-            umax = fmaxf(umax, u);
-            vmin = fminf(vmin, v);
-            vmax = fmaxf(vmax, v);
-            zmin = fminf(zmin, cS[k].z);
-            zmax = fmaxf(zmax, cS[k].z);
-        }
-    }
+    float u = pu > 1e7f ? 1e7f : pu;
+    float v = pv > 1e7f ? 1e7f : pv;
+    u = u < -1e7f ? -1e7f : u;
+    v = v < -1e7f ? -1e7f : v;
+    const float umin = corner_min(u), umax = corner_max(u), vmin = corner_min(v), vmax = corner_max(v);
+    const float zmin = corner_min(p.z), zmax = corner_max(p.z);
     return carve_pooled(L, J, slot, (int) umin, (int) vmin, (int) umax, (int) vmax, zmin, zmax, should_split, var,
-                        projects_inside);
+                        projects_inside, lane);
 }
 
-// VolumeCarver<.., OusterLidar>::operator()(octant) (volume_carver_impl.hpp:339-537): range
-// bounds, camera-in-node first, corner columns unwrapped around the centre's column.
+// VolumeCarver<.., OusterLidar>::operator()(octant) (volume_carver_impl.hpp:339-537) by a warp:
+// range bounds, camera-in-node first, corner columns unwrapped around the centre's column.
 __device__ bool carve_lidar(const OccLaunch& L, const OccJob& J, const OccDyn& D, int slot, int cx, int cy, int cz,
-                            int size, float max_depth_value, bool& should_split, int& var, bool& projects_inside)
+                            int size, float max_depth_value, bool& should_split, int& var, bool& projects_inside,
+                            int lane)
 {
     const OccDevice& m = J.m;
     const Lidar& ld = L.sensor.L;
@@ -594,42 +635,25 @@ __device__ bool carve_lidar(const OccLaunch& L, const OccJob& J, const OccDyn& D
         should_split = true;
         return true;
     }
-    float pu[8], pv[8];
-    for (int k = 0; k < 8; ++k) {
-        const F3 p_M = f3(((float) size * (float) (k & 1) + (float) cx) * m.res,
-                          ((float) size * (float) ((k >> 1) & 1) + (float) cy) * m.res,
-                          ((float) size * (float) (k >> 2) + (float) cz) * m.res);
-        lidar_project(ld, apply(D.T_SW, apply(m.T_WM, p_M)), pu[k], pv[k]);
-    }
+    float pu, pv;
+    lidar_project(ld, corner_point(m, D.T_SW, lane & 7, cx, cy, cz, size), pu, pv);
     float cu, cv;
     lidar_project(ld, centre_S, cu, cv);
     const float W = (float) ld.w;
     float cu_comp = cu + (float) (ld.w / 2);
     if (cu_comp > W - 0.5f)
         cu_comp = cu_comp - W;
-    float umin = 0.0f, umax = 0.0f, vmin = 0.0f, vmax = 0.0f;
-    for (int k = 0; k < 8; ++k) {
-        float u = pu[k];
-        if (cu < cu_comp && u > cu && u > cu_comp)
-            u = u - W;
-        else if (cu > cu_comp && u < cu && u < cu_comp)
-            u = u + W;
-        if (k == 0) {
-            umin = umax = u;
-            vmin = vmax = pv[0];
-        }
-        else {
-            umin = fminf(umin, u);
-            umax = fmaxf(umax, u);
-            vmin = fminf(vmin, pv[k]);
-            vmax = fmaxf(vmax, pv[k]);
-        }
-    }
+    if (cu < cu_comp && pu > cu && pu > cu_comp)
+        pu = pu - W;
+    else if (cu > cu_comp && pu < cu && pu < cu_comp)
+        pu = pu + W;
+    const float umin = corner_min(pu), umax = corner_max(pu), vmin = corner_min(pv), vmax = corner_max(pv);
     return carve_pooled(L, J, slot, (int) umin, (int) vmin, (int) umax, (int) vmax, approx_min, approx_max,
-                        should_split, var, projects_inside);
+                        should_split, var, projects_inside, lane);
 }
 
-// One depth of the VolumeCarver over every map's frontier at that depth.
+// One depth of the VolumeCarver over every map's frontier at that depth, one warp per octant;
+// lane 0 lists the octant or allocates and queues its children.
 __global__ void __launch_bounds__(128) occ_carve_kernel(const OccLaunch* __restrict__ Lp, int depth)
 {
     const OccLaunch& L = *Lp;
@@ -637,7 +661,9 @@ __global__ void __launch_bounds__(128) occ_carve_kernel(const OccLaunch* __restr
     const int total = batch_prefix(L, pre, [depth](const OccJob& J) {
         return clamp_count(J.m.counters[kOccFrontierN + depth], J.m.node_capacity + J.m.block_capacity);
     });
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int n_warps = (gridDim.x * blockDim.x) >> 5;
+    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < total; idx += n_warps) {
         const int j = batch_find(pre, L.n, idx);
         const OccJob& J = L.job[j];
         const OccDevice& m = J.m;
@@ -664,29 +690,31 @@ __global__ void __launch_bounds__(128) occ_carve_kernel(const OccLaunch* __restr
         int var = 1; // Gradient
         const float max_depth_value = J.max_value[1];
         const bool keep = L.sensor.lidar
-            ? carve_lidar(L, J, D, slot, cx, cy, cz, size, max_depth_value, should_split, var, projects_inside)
-            : carve_pinhole(L, J, D, slot, cx, cy, cz, size, max_depth_value, should_split, var, projects_inside);
-        if (!keep)
-            continue;
-        if (is_block) {
-            const int k = push(J.block_list, &m.counters[kOccBlockListN], m.block_capacity, slot_block(slot), err);
-            if (k < m.block_capacity) {
-                J.block_var[k] = var;
-                J.block_inside[k] = projects_inside ? 1 : 0;
+            ? carve_lidar(L, J, D, slot, cx, cy, cz, size, max_depth_value, should_split, var, projects_inside, lane)
+            : carve_pinhole(L, J, D, slot, cx, cy, cz, size, max_depth_value, should_split, var, projects_inside,
+                            lane);
+        if (keep && lane == 0) {
+            if (is_block) {
+                const int k = push(J.block_list, &m.counters[kOccBlockListN], m.block_capacity, slot_block(slot), err);
+                if (k < m.block_capacity) {
+                    J.block_var[k] = var;
+                    J.block_inside[k] = projects_inside ? 1 : 0;
+                }
+            }
+            else if (should_split) {
+                occ_allocate_children(m, slot);
+                for (int i = 0; i < 8; ++i) {
+                    const int ch = m.node_child[8 * (size_t) slot + i];
+                    if (ch != -1) // -1 only when a pool ran out (latched in the error word)
+                        push(J.frontier[(depth + 1) & 1], &m.counters[kOccFrontierN + depth + 1],
+                             m.node_capacity + m.block_capacity, ch, err);
+                }
+            }
+            else if (var == 0) {
+                push(J.node_list, &m.counters[kOccNodeListN], m.node_capacity, slot, err);
             }
         }
-        else if (should_split) {
-            occ_allocate_children(m, slot);
-            for (int i = 0; i < 8; ++i) {
-                const int ch = m.node_child[8 * (size_t) slot + i];
-                if (ch != -1) // -1 only when a pool ran out (latched in the error word)
-                    push(J.frontier[(depth + 1) & 1], &m.counters[kOccFrontierN + depth + 1],
-                         m.node_capacity + m.block_capacity, ch, err);
-            }
-        }
-        else if (var == 0) {
-            push(J.node_list, &m.counters[kOccNodeListN], m.node_capacity, slot, err);
-        }
+        __syncwarp();
     }
 }
 
@@ -1173,7 +1201,7 @@ __device__ void occ_process_block(const OccLaunch& L, const OccJob& J, int b, bo
 
 // freeBlock on the freed blocks and updateBlock on the carver's blocks (disjoint: the carver
 // does not descend below a free-space node), one warp per block, all maps.
-__global__ void __launch_bounds__(256) occ_blocks_kernel(const OccLaunch* __restrict__ Lp)
+__global__ void __launch_bounds__(256, 3) occ_blocks_kernel(const OccLaunch* __restrict__ Lp)
 {
     const OccLaunch& L = *Lp;
     __shared__ int pre[kOccMaxBatch + 1];
@@ -1237,6 +1265,26 @@ __device__ void occ_up_mean(OccD& parent, const OccD* ch)
     }
 }
 
+// Streaming forms of the two reductions: children in index order, the same comparisons and
+// sums as occ_up_best / occ_up_mean.
+struct UpBest {
+    float best;
+    OccD pick;
+    int nv, no;
+};
+__device__ __forceinline__ void up_best_add(UpBest& a, const OccD& c, bool want_min)
+{
+    if (occ_valid(c)) {
+        ++a.nv;
+        a.no += c.observed ? 1 : 0;
+        const float fv = occ_field(c);
+        if (want_min ? (fv < a.best) : (fv > a.best)) {
+            a.best = fv;
+            a.pick = c;
+        }
+    }
+}
+
 __device__ void occ_propagate_block(const OccDevice& m, int b, int lane)
 {
     const OccBlockState st = m.block_state[b];
@@ -1253,19 +1301,52 @@ __device__ void occ_propagate_block(const OccDevice& m, int b, int lane)
         const OccD* cmin = blk_min(m, b, st.finest, cs);
         const OccD* cmax = blk_max(m, b, st.finest, cs);
         const bool first = ps == st.current_scale + 1;
+        const bool do_mean = !(first && st.buffer_scale > st.current_scale);
         for (int k = lane; k < np * np * np; k += 32) {
             const int x = k % np, y = (k / np) % np, z = k / (np * np);
-            OccD c0[8], c1[8], c2[8];
+            // ch[0] is visited first so that ties keep the lowest child index, as the array form
+            UpBest lo{FLT_MAX, OccD{0.0f, 0.0f, 0}, 0, 0}, hi{-FLT_MAX, OccD{0.0f, 0.0f, 0}, 0, 0};
+            float os = 0.0f, ws = 0.0f;
+            int nmean = 0;
+            bool lo_first = true, hi_first = true;
             for (int c = 0; c < 8; ++c) {
                 const int ci = (2 * x + (c & 1)) + (2 * y + ((c >> 1) & 1)) * nc + (2 * z + (c >> 2)) * nc * nc;
-                c0[c] = cmean[ci];
-                c1[c] = first ? cmean[ci] : cmin[ci];
-                c2[c] = first ? cmean[ci] : cmax[ci];
+                const OccD c0 = cmean[ci];
+                const OccD c1 = first ? c0 : cmin[ci];
+                const OccD c2 = first ? c0 : cmax[ci];
+                if (occ_valid(c0)) {
+                    ++nmean;
+                    os += c0.occ;
+                    ws += c0.weight;
+                }
+                // the array form starts from index 0 when no child beats the initial bound
+                if (lo_first) {
+                    lo.pick = c1;
+                    lo_first = false;
+                }
+                if (hi_first) {
+                    hi.pick = c2;
+                    hi_first = false;
+                }
+                up_best_add(lo, c1, true);
+                up_best_add(hi, c2, false);
             }
-            if (!(first && st.buffer_scale > st.current_scale))
-                occ_up_mean(pmean[k], c0);
-            occ_up_best(pmin[k], c1, true);
-            occ_up_best(pmax[k], c2, false);
+            if (do_mean && nmean > 0) {
+                OccD& p = pmean[k];
+                p.occ = os / (float) nmean;
+                p.weight = ceilf(ws / (float) nmean);
+                p.observed = 0;
+            }
+            if (lo.nv > 0) {
+                OccD r = lo.pick;
+                r.observed = (lo.no == 8) ? 1 : 0;
+                pmin[k] = r;
+            }
+            if (hi.nv > 0) {
+                OccD r = hi.pick;
+                r.observed = (hi.no == 8) ? 1 : 0;
+                pmax[k] = r;
+            }
         }
         __syncwarp();
     }
@@ -1594,7 +1675,7 @@ static se_gpu_status occ_enqueue(const OccLaunch& L, const OccLaunch* Ld, const 
     occ_pixels_kernel<<<dim3((npx + 255) / 256, n), 256, 0, stream>>>(Ld);
     for (int l = 1; l < L.sensor.levels; ++l)
         occ_pool_level_kernel<<<dim3((npx + 255) / 256, 2 * n), 256, 0, stream>>>(Ld, l);
-    occ_root_kernel<<<1, 32, 0, stream>>>(Ld);
+    occ_root_kernel<<<n, 32, 0, stream>>>(Ld);
     for (int d = 1; d <= L.max_block_depth; ++d) {
         OCC_MARK(kTileCarve);
         occ_carve_kernel<<<carve, 128, 0, stream>>>(Ld, d);
