@@ -3,8 +3,9 @@
 
 Workload (config "tsdf640"): 640x480 pinhole (fx = fy = 525, cx = 319.5, cy = 239.5), a
 single-resolution TSDF map of 1024^3 voxels at 1 cm, a seeded synthetic room trajectory with
-random-walk velocity (0.02 m, 1 deg per frame). One step is one frame: 3-level ICP {10, 5, 4}
-against the previous raycast, integration at the tracked pose, raycast at that pose.
+random-walk velocity (0.02 m, 1 deg per frame). One step is one frame: the bilateral pre-filter
+of the tracking input (5x5, 4 px, 0.03 m), 3-level ICP {10, 5, 4} against the previous raycast,
+integration of the raw depth at the tracked pose, raycast at that pose.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -144,9 +145,11 @@ def _variant(se, torch, dev, sensor, poses, depth_dev, first, steps, warmup, pat
         nrm = torch.zeros_like(pts)
         scale = torch.zeros((H, W), dtype=torch.int8, device=dev)
         state = {"T": T0}
+        filt = torch.empty((H, W), dtype=torch.float32, device=dev)
 
         def step(i, depth):
-            tracker.track(depth, state["T"], pts, nrm)
+            se.bilateral_filter(depth, out=filt, **se.BILATERAL_DEFAULTS)
+            tracker.track(filt, state["T"], pts, nrm)
             integ.integrateDepth(i, depth, sensor, state["T"])
             se.raycast_volume(m, sensor, state["T"], pts, nrm, scale)
 
@@ -155,6 +158,7 @@ def _variant(se, torch, dev, sensor, poses, depth_dev, first, steps, warmup, pat
         fp = None
     else:
         fp = se.FramePipeline(m, sensor, tracker)
+        fp.set_bilateral(**se.BILATERAL_DEFAULTS)
         fp.set_pose(T0, 0)
         fp.depth.copy_(depth_dev[0])
         fp.run(track=False)
@@ -311,6 +315,7 @@ def run_ours(args, ws, rank, local):
         "data": "synthetic (seeded room: 6x5x3 m box, 12 spheres, 8 boxes; depth noise "
                 "N(0,(0.0015 z^2)^2), 2% dropout)",
         "config": {"workload": "tsdf640: 640x480 pinhole, TSDF single-res 1024^3 @ 1 cm, "
+                               "bilateral-filtered tracking input (5x5, 4 px, 0.03 m), "
                                "ICP 3 levels {10,5,4}, integrate + raycast per frame",
                    "map_res_m": MAP_RES, "map_voxels": 1024, "storage": "f32",
                    "path": "captured CUDA graph per frame, pose on the device",
@@ -325,9 +330,9 @@ def run_ours(args, ws, rank, local):
         "roofline": roofline,
         "e2e": {"value": ws * K / e2e_max, "unit": "frames/s", "h2d_bytes_per_step": W * H * 4,
                 "d2h_bytes_per_step": 52},
-        # per tracked frame: track 25 (init, 2 half-samples, points, normals, 19 ICP
-        # iterations, check) + integrate 4 (prep, carve, frustum, update) + raycast 2
-        "gpu_launches": 31 * K,
+        # per tracked frame: bilateral 1 + track 25 (init, 2 half-samples, points, normals,
+        # 19 ICP iterations, check) + integrate 4 (prep, carve, frustum, update) + raycast 2
+        "gpu_launches": 32 * K,
         "kernel_ms_per_frame_plain": {k: v / K for k, v in kms.items()},
         "kernel_launches": kl,
         "voxels_per_s": float(np.mean(upd)) * K / (g32_ms * 1e-3),
@@ -614,6 +619,7 @@ def _oracle_pipeline(frames, poses, spec, n_warm, n_steps, budget_s=None):
                   spec.near_plane, spec.far_plane)
     cfg = o.tracker_config()
     T = poses[0].astype(np.float32)
+    bl = dict(radius=2, sigma_space=4.0, sigma_range=0.03)  # the bilateral pre-filter of the tracking input
     m.integrate_depth(frames[0], s, T, 0)
     pts, nrm, _ = m.raycast(s, T)
     times = []
@@ -623,7 +629,7 @@ def _oracle_pipeline(frames, poses, spec, n_warm, n_steps, budget_s=None):
         if i == n_warm + 1:
             t_start = time.perf_counter()
         t0 = time.perf_counter()
-        _, T, _ = o.track(s, cfg, frames[i], T, pts, nrm)
+        _, T, _ = o.track(s, cfg, o.bilateral_filter(frames[i], **bl), T, pts, nrm)
         m.integrate_depth(frames[i], s, T, i)
         pts, nrm, _ = m.raycast(s, T)
         if i > n_warm:
@@ -660,6 +666,7 @@ def run_reference(args, ws, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded room)", "impl": "reference",
         "config": {"workload": "tsdf640: 640x480 pinhole, TSDF single-res 1024^3 @ 1 cm, "
+                               "bilateral-filtered tracking input (5x5, 4 px, 0.03 m), "
                                "ICP 3 levels {10,5,4}, integrate + raycast per frame",
                    "parallelism": "OpenMP, all host threads"},
         "cpu_baseline": {"value": value, "unit": "frames/s", "cores": os.cpu_count(),

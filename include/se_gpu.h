@@ -111,6 +111,17 @@ typedef struct {
     float far_plane;
 } se_gpu_lidar;
 
+/* The bilateral pre-filter of the tracking input. No counterpart in the reference (it feeds
+ * the depth straight to the tracker); defined by this library: invalid (<= 0 or NaN) centres
+ * stay 0, the valid taps of the (2 radius + 1)^2 window inside the image are weighted by
+ * exp(-(dx^2 + dy^2) / (2 sigma_space_px^2)) * exp(-(d - c)^2 / (2 sigma_range_m^2)). The
+ * benchmark's tracked TSDF configuration uses radius 2, 4 px, 0.03 m. radius <= 7. */
+typedef struct {
+    int radius;
+    float sigma_space_px;
+    float sigma_range_m;
+} se_gpu_bilateral_config;
+
 /* se::TrackerConfig (include/se/tracker/tracker.hpp:22-33). */
 typedef struct {
     int num_levels;    /* at most 3 */
@@ -291,6 +302,12 @@ SE_GPU_API se_gpu_status se_gpu_raycast_adjoint(const se_gpu_map* map, const se_
 
 /* --------------------------------------------------------------------------- tracker -- */
 
+/* The bilateral pre-filter (see se_gpu_bilateral_config) of a device depth image into another
+ * device image (not in place). Stream-ordered. */
+SE_GPU_API se_gpu_status se_gpu_bilateral_filter(const float* in_dev, float* out_dev, int width,
+                                                 int height, const se_gpu_bilateral_config* config,
+                                                 void* stream);
+
 /* Replaces se::Tracker ctor (include/se/tracker/tracker.hpp:42-48): device buffers for the
  * depth pyramid, per-level point clouds and normals and the ICP partial sums. */
 SE_GPU_API se_gpu_status se_gpu_tracker_create(const se_gpu_pinhole* sensor,
@@ -347,6 +364,10 @@ SE_GPU_API se_gpu_status se_gpu_frame_destroy(se_gpu_frame* frame);
 SE_GPU_API se_gpu_status se_gpu_frame_buffers(se_gpu_frame* frame, float** depth_dev,
                                               float** pts_W_dev, float** nrm_W_dev,
                                               int8_t** scale_dev);
+/* Track on the bilateral-filtered input (config) or on the input itself (NULL, the default);
+ * integration always uses the unfiltered depth. The next run recaptures the graph. */
+SE_GPU_API se_gpu_status se_gpu_frame_set_bilateral(se_gpu_frame* frame,
+                                                    const se_gpu_bilateral_config* config);
 /* Set the device pose T_WS and the integration timestamp of the next run. Synchronous. */
 SE_GPU_API se_gpu_status se_gpu_frame_set_pose(se_gpu_frame* frame, const float T_WS[16],
                                                int timestamp);

@@ -457,4 +457,51 @@ static inline void round_pixel(float u, float v, int& x, int& y)
     y = (int) (v + 0.5f);
 }
 
+/* e^x for x <= 0 in float operations only: Cody & Waite (1980) argument reduction
+ * x = n ln2 + r with ln2 split into a 12-bit-short head and a tail, the degree-7 Taylor
+ * polynomial of e^r (|r| <= ln2/2, relative error < 3e-8), then 2^n exactly. The GPU build
+ * evaluates the same operations, so both round identically. */
+static inline float exp_cw(float x)
+{
+    if (x < -87.0f)
+        return 0.0f;
+    const float n = std::rint(x * 1.44269504f);
+    const float r = (x - n * 0.693145751953125f) - n * 1.42860677e-06f;
+    const float p = 1.0f
+        + r * (1.0f + r * (0.5f + r * (0.166666672f + r * (0.0416666679f + r * (0.00833333377f
+                                                     + r * (0.00138888892f + r * 0.000198412701f))))));
+    return std::ldexp(p, (int) n);
+}
+
+/* The project-defined bilateral pre-filter of the tracking input (the reference has none):
+ * invalid (<= 0 or NaN) centres stay 0; valid taps of the (2r+1)^2 window inside the image are
+ * weighted by ws[dy][dx] (spatial Gaussian, host-computed) times exp_cw(-(d - c)^2 k) with
+ * k = 1 / (2 sigma_r^2); the sums run dy outer, dx inner. */
+static inline float bilateral_pixel(const float* in, int w, int h, int x, int y, int radius, const float* ws, float k)
+{
+    const float c = in[x + y * w];
+    if (!(c > 0.0f))
+        return 0.0f;
+    float num = 0.0f, den = 0.0f;
+    const int n = 2 * radius + 1;
+    for (int dy = -radius; dy <= radius; ++dy) {
+        const int yy = y + dy;
+        if (yy < 0 || yy >= h)
+            continue;
+        for (int dx = -radius; dx <= radius; ++dx) {
+            const int xx = x + dx;
+            if (xx < 0 || xx >= w)
+                continue;
+            const float d = in[xx + yy * w];
+            if (!(d > 0.0f))
+                continue;
+            const float diff = d - c;
+            const float wgt = ws[(dy + radius) * n + (dx + radius)] * exp_cw(-(diff * diff) * k);
+            num = num + wgt * d;
+            den = den + wgt;
+        }
+    }
+    return num / den;
+}
+
 } // namespace

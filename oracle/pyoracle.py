@@ -123,6 +123,9 @@ def lib():
             "so_se3_exp": (None, [f32p, f32p]),
             "so_half_sample_robust": (None, [f32p, C.c_int, C.c_int, C.c_float, C.c_int, f32p]),
             "so_depth_to_point_cloud": (None, [f32p, C.POINTER(Pinhole), f32p]),
+            "so_bilateral_weights": (None, [C.c_int, C.c_float, f32p]),
+            "so_bilateral_filter": (None, [f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, f32p]),
+            "so_exp_cw": (C.c_float, [C.c_float]),
             "so_point_cloud_to_normal": (None, [f32p, C.c_int, C.c_int, C.c_int, f32p]),
         }
         for name, (res, args) in sig.items():
@@ -421,6 +424,19 @@ class OracleMap:
                                           np.asarray(direction, np.float32), float(t_near),
                                           float(t_far), C.byref(t))
         return bool(found), t.value
+
+
+def bilateral_filter(depth, radius=2, sigma_space=4.0, sigma_range=0.03):
+    depth = np.ascontiguousarray(depth, np.float32)
+    h, w = depth.shape
+    out = np.zeros_like(depth)
+    lib().so_bilateral_filter(depth.reshape(-1), w, h, int(radius), float(sigma_space), float(sigma_range),
+                              out.reshape(-1))
+    return out
+
+
+def exp_cw(x):
+    return np.float32(lib().so_exp_cw(float(x)))
 
 
 def tracker_config(iterations=(10, 5, 4), dist_threshold=0.1, normal_threshold=0.8,

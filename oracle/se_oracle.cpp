@@ -2031,6 +2031,30 @@ long long so_unique_at_scale(uint64_t* keys, long long n, uint64_t scale, uint64
 
 void so_se3_exp(const float twist[6], float T[16]) { tf_to16(se3_exp(twist), T); }
 
+/* spatial weights of the bilateral window, (2r+1)^2 floats: exp(-(dx^2 + dy^2) / (2 s^2)) in
+ * double, rounded to float */
+void so_bilateral_weights(int radius, float sigma_space, float* ws)
+{
+    const int n = 2 * radius + 1;
+    for (int dy = -radius; dy <= radius; ++dy)
+        for (int dx = -radius; dx <= radius; ++dx)
+            ws[(dy + radius) * n + (dx + radius)] =
+                (float) std::exp(-(double) (dx * dx + dy * dy) / (2.0 * (double) sigma_space * (double) sigma_space));
+}
+
+void so_bilateral_filter(const float* in, int w, int h, int radius, float sigma_space, float sigma_range, float* out)
+{
+    std::vector<float> ws((size_t) (2 * radius + 1) * (2 * radius + 1));
+    so_bilateral_weights(radius, sigma_space, ws.data());
+    const float k = 1.0f / (2.0f * sigma_range * sigma_range);
+#pragma omp parallel for
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+            out[x + y * w] = bilateral_pixel(in, w, h, x, y, radius, ws.data(), k);
+}
+
+float so_exp_cw(float x) { return exp_cw(x); }
+
 void so_half_sample_robust(const float* in, int w, int h, float e_d, int radius, float* out)
 {
     half_sample_robust(in, w, h, e_d, radius, out);

@@ -230,6 +230,12 @@ long long so_unique_at_scale(uint64_t* keys, long long n, uint64_t scale, uint64
 /* se(3) exponential of a twist [rho; omega] as a row-major 4x4 (math_util_impl.hpp:117-174). */
 void so_se3_exp(const float twist[6], float T[16]);
 
+/* The project-defined bilateral pre-filter of the tracking input (no reference counterpart):
+ * spatial weights and the filter itself; exp_cw is its float exponential. */
+void so_bilateral_weights(int radius, float sigma_space, float* ws);
+void so_bilateral_filter(const float* in, int w, int h, int radius, float sigma_space, float sigma_range, float* out);
+float so_exp_cw(float x);
+
 /* Preprocessing helpers exposed for tests. */
 void so_half_sample_robust(const float* in, int w, int h, float e_d, int radius, float* out);
 void so_depth_to_point_cloud(const float* depth, const so_pinhole* sensor, float* pts);

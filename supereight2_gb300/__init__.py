@@ -24,7 +24,7 @@ from . import build as _build
 
 __all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "OusterLidar",
            "OccupancyBatch", "raycast_volume",
-           "render_depth", "raycast_adjoint", "track_noalloc",
+           "render_depth", "raycast_adjoint", "track_noalloc", "bilateral_filter",
            "FramePipeline", "SeGpuError", "library", "library_path"]
 
 
@@ -62,6 +62,14 @@ class _Lidar(C.Structure):
                 ("far_plane", C.c_float)]
 
 
+class _BilateralConfig(C.Structure):
+    _fields_ = [("radius", C.c_int), ("sigma_space_px", C.c_float), ("sigma_range_m", C.c_float)]
+
+
+# The bilateral pre-filter of the tracked TSDF benchmark configuration: 5x5, 4 px, 0.03 m.
+BILATERAL_DEFAULTS = dict(radius=2, sigma_space=4.0, sigma_range=0.03)
+
+
 class _TrackerConfig(C.Structure):
     _fields_ = [("num_levels", C.c_int), ("iterations", C.c_int * 3),
                 ("dist_threshold", C.c_float), ("normal_threshold", C.c_float),
@@ -92,6 +100,8 @@ SIGNATURES = {
     "se_gpu_map_check": (C.c_int, [_VP]),
     "se_gpu_integrate_depth": (C.c_int, [_VP, _VP, C.POINTER(_Pinhole), _F16, C.c_int, _VP]),
     "se_gpu_integrate_range": (C.c_int, [_VP, _VP, C.POINTER(_Lidar), _F16, C.c_int, _VP]),
+    "se_gpu_bilateral_filter": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.POINTER(_BilateralConfig), _VP]),
+    "se_gpu_frame_set_bilateral": (C.c_int, [_VP, C.POINTER(_BilateralConfig)]),
     "se_gpu_occ_batch_create": (C.c_int, [_VP, C.c_int, C.POINTER(_Pinhole), C.POINTER(_Lidar),
                                           C.c_int, C.POINTER(_VP)]),
     "se_gpu_occ_batch_integrate": (C.c_int, [_VP, _VP, _F16, _VP, _VP]),
@@ -613,6 +623,21 @@ def track_noalloc(sensor: PinholeCamera, config: TrackerConfig, depth, T_WS,
     return bool(acc.value), np.array(red[:], np.float32)
 
 
+def bilateral_filter(depth, out=None, radius=2, sigma_space=4.0, sigma_range=0.03, stream=None):
+    """The bilateral pre-filter of the tracking input (not in the reference; defined in
+    se_gpu.h): a [H, W] float32 CUDA tensor into out (a new tensor when None)."""
+    import torch
+    H, W = depth.shape
+    pin = _dptr(depth, torch.float32, (H, W), "depth")
+    if out is None:
+        out = torch.empty_like(depth)
+    pout = _dptr(out, torch.float32, (H, W), "out")
+    cfg = _BilateralConfig(int(radius), float(sigma_space), float(sigma_range))
+    L = library()
+    _check(L.se_gpu_bilateral_filter(pin, pout, W, H, C.byref(cfg), _stream(stream)), "se_gpu_bilateral_filter")
+    return out
+
+
 class FramePipeline:
     """The reference application's per-frame loop (track, integrate, raycast) as one captured
     CUDA graph with the pose on the device. ``depth`` is the frame's input buffer (write the
@@ -641,6 +666,12 @@ class FramePipeline:
         if h:
             self._L.se_gpu_frame_destroy(h)
             self.h = None
+
+    def set_bilateral(self, radius=2, sigma_space=4.0, sigma_range=0.03, enable=True):
+        """Track on the bilateral-filtered input (integration keeps the raw depth)."""
+        cfg = _BilateralConfig(int(radius), float(sigma_space), float(sigma_range))
+        _check(self._L.se_gpu_frame_set_bilateral(self.h, C.byref(cfg) if enable else None),
+               "se_gpu_frame_set_bilateral")
 
     def set_pose(self, T_WS, timestamp=0):
         _, tp = _m16(T_WS)

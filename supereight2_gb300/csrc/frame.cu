@@ -26,6 +26,9 @@ struct se_gpu_frame {
     se_gpu_pinhole sensor;
     float* pose12;           // device T_WS (row-major 3x4)
     float* depth;            // device input depth, width * height
+    float* depth_filtered;   // the bilateral-filtered tracking input (when enabled)
+    int bilateral;
+    se_gpu_bilateral_config bilateral_config;
     float* pts;              // device raycast points (the next frame's tracking reference)
     float* nrm;
     int8_t* scale;
@@ -41,8 +44,14 @@ static se_gpu_status capture(se_gpu_frame* f, int with_track)
     cudaError_t e = cudaStreamBeginCapture(f->capture_stream, cudaStreamCaptureModeThreadLocal);
     se_gpu_status st = SE_GPU_OK;
     if (e == cudaSuccess) {
-        if (with_track)
-            st = enqueue_track(f->tracker, f->depth, f->pts, f->nrm, nullptr, f->pose12, f->capture_stream);
+        const float* track_in = f->depth;
+        if (with_track && f->bilateral) {
+            st = enqueue_bilateral(f->depth, f->depth_filtered, f->sensor.width, f->sensor.height,
+                                   f->bilateral_config, f->capture_stream);
+            track_in = f->depth_filtered;
+        }
+        if (with_track && st == SE_GPU_OK)
+            st = enqueue_track(f->tracker, track_in, f->pts, f->nrm, nullptr, f->pose12, f->capture_stream);
         if (st == SE_GPU_OK)
             st = enqueue_integrate(f->map, f->depth, f->sensor, nullptr, f->pose12, 0, f->capture_stream);
         if (st == SE_GPU_OK)
@@ -117,6 +126,7 @@ se_gpu_status se_gpu_frame_destroy(se_gpu_frame* f)
         cudaStreamDestroy(f->capture_stream);
     cudaFree(f->pose12);
     cudaFree(f->depth);
+    cudaFree(f->depth_filtered);
     cudaFree(f->pts);
     cudaFree(f->nrm);
     cudaFree(f->scale);
@@ -151,6 +161,30 @@ se_gpu_status se_gpu_frame_set_pose(se_gpu_frame* f, const float T_WS[16], int t
     SE_CUDA_TRY(cudaDeviceSynchronize());
     SE_CUDA_TRY(cudaMemcpy(f->pose12, T_WS, 12 * sizeof(float), cudaMemcpyHostToDevice));
     SE_CUDA_TRY(cudaMemcpy(f->map->timestamp_dev, &timestamp, sizeof(int), cudaMemcpyHostToDevice));
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_frame_set_bilateral(se_gpu_frame* f, const se_gpu_bilateral_config* config)
+{
+    if (!f) {
+        set_last_error("se_gpu_frame_set_bilateral: null frame");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    if (config) {
+        const se_gpu_status st = check_bilateral(config);
+        if (st != SE_GPU_OK)
+            return st;
+        if (!f->depth_filtered)
+            SE_CUDA_TRY(cudaMalloc(&f->depth_filtered, (size_t) f->sensor.width * f->sensor.height * sizeof(float)));
+        f->bilateral_config = *config;
+    }
+    f->bilateral = config ? 1 : 0;
+    // the tracked graph changes; a frame in flight keeps its own executable until it completes
+    if (f->exec[1]) {
+        SE_CUDA_TRY(cudaDeviceSynchronize());
+        cudaGraphExecDestroy(f->exec[1]);
+        f->exec[1] = nullptr;
+    }
     return SE_GPU_OK;
 }
 

@@ -31,6 +31,10 @@ se_gpu_status occ_integrate(se_gpu_occ_map* om, const float* depth_dev, const se
 se_gpu_status occ_integrate_range(se_gpu_occ_map* om, const float* range_dev, const se_gpu_lidar& sensor,
                                   const float* T_WS16, int timestamp, cudaStream_t stream);
 void occ_scratch_free(se_gpu_occ_map* om);
+// The bilateral pre-filter of the tracking input (preprocess.cu).
+se_gpu_status check_bilateral(const se_gpu_bilateral_config* c);
+se_gpu_status enqueue_bilateral(const float* in, float* out, int w, int h, const se_gpu_bilateral_config& c,
+                                cudaStream_t stream);
 // With pose12_dev_io the tracker starts from, and writes its result to, that device pose.
 se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const float* ref_pts, const float* ref_nrm,
                             const float* T_WS_host16, float* pose12_dev_io, cudaStream_t stream);
