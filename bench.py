@@ -349,6 +349,9 @@ def run_ours(args, ws, rank, local):
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(frames, poses, sensor_spec, args.warmup, 2 * K, args.cpu_budget_s)
         out["lidar_batch"]["cpu_baseline"] = lidar_cpu_baseline(lidar_data)
+        if args.precision_frames > 0:
+            out["precision_vs_f64"] = _precision_report(se, torch, torch.device("cuda", local),
+                                                        args.precision_frames, args.max_blocks)
     return out
 
 
@@ -457,6 +460,90 @@ def _adjoint_bench(se, torch, m, sensor, T_gt, obs, flush, reps=20, gn_steps=50,
             "fd_rel_err": fd_rel, "fd_h": h, "fd_pixels": int(mask.sum()),
             "gn_steps": gn_steps, "pose_err_start": {"m": t0, "deg": r0},
             "pose_err_final": {"m": t1, "deg": r1}}
+
+
+# ------------------------------------------------------- precision against an FP64 run --
+
+def _rot_deg(Ra, Rb):
+    c = (np.trace(np.asarray(Ra, np.float64) @ np.asarray(Rb, np.float64).T) - 1.0) / 2.0
+    return float(np.degrees(np.arccos(np.clip(c, -1.0, 1.0))))
+
+
+def _precision_report(se, torch, dev, n_frames, max_blocks):
+    """The multi-res TSDF pipeline (bilateral-filtered tracking input, 3-level ICP, integration,
+    raycast) on n_frames of the seeded trajectory, on the GPU with FP32 and with FP16 storage and
+    in the FP64 run of the oracle, each tracking on its own. Reports, against the FP64 run: the
+    per-frame pose, the trajectory error (ATE: RMSE of the positions against ground truth), the
+    TSDF of the blocks both hold at scale 0 after the last frame, and the raycast depth of both
+    maps at the FP64 run's last pose."""
+    from oracle import pyoracle64 as o64
+    spec, scene, poses_gt, frames = make_data(n_frames, dev)
+    sensor = se.PinholeCamera.from_spec(spec)
+    H, W = sensor.height, sensor.width
+    t0 = time.perf_counter()
+    o64.set_num_threads(os.cpu_count() or 1)
+    s64 = o64.pinhole(spec.width, spec.height, spec.fx, spec.fy, spec.cx, spec.cy, spec.near_plane, spec.far_plane)
+    cfg64 = o64.tracker_config()
+    m64 = o64.OracleMap64(MAP_DIM, MAP_RES, multires=True)
+    T = poses_gt[0].astype(np.float32).astype(np.float64)
+    traj64 = [T.copy()]
+    m64.integrate_depth(frames[0], s64, T, 0)
+    pts, nrm, _ = m64.raycast(s64, T)
+    for i in range(1, n_frames):
+        _, T, _ = o64.track(s64, cfg64, o64.bilateral_filter(frames[i], **se.BILATERAL_DEFAULTS), T, pts, nrm)
+        m64.integrate_depth(frames[i], s64, T, i)
+        pts, nrm, _ = m64.raycast(s64, T)
+        traj64.append(T.copy())
+    f64_s = time.perf_counter() - t0
+    keys64, _, t64, w64, _, _, sc64 = m64.mr_blocks()
+    T_last = traj64[-1]
+    pts64 = pts
+    gt = np.stack([P[:3, 3] for P in poses_gt])
+    ate = lambda tr: float(np.sqrt(np.mean(np.sum((np.stack([P[:3, 3] for P in tr]) - gt) ** 2, -1))))  # noqa: E731
+    out = {"workload": f"{n_frames} frames of the tsdf640 trajectory, MultiresTSDF 1024^3 at 1 cm, "
+                       "bilateral-filtered tracking input, track + integrate + raycast, each run tracking on its own",
+           "f64_oracle_s": f64_s, "ate_m": {"f64_oracle": ate(traj64)}}
+    for st in ("f32", "f16"):
+        m = se.Map(MAP_DIM, MAP_RES, max_blocks=max_blocks, storage=st, res_type="multi")
+        tr = se.Tracker(m, sensor, se.TrackerConfig())
+        fp = se.FramePipeline(m, sensor, tr)
+        fp.set_bilateral(**se.BILATERAL_DEFAULTS)
+        fp.set_pose(poses_gt[0].astype(np.float32), 0)
+        traj = []
+        for i in range(n_frames):
+            fp.depth.copy_(torch.from_numpy(frames[i]).to(dev))
+            fp.run(track=i > 0)
+            traj.append(fp.pose()[0].astype(np.float64))
+        m.check()
+        dt = [float(np.linalg.norm(a[:3, 3] - b[:3, 3])) for a, b in zip(traj, traj64)]
+        dr = [_rot_deg(a[:3, :3], b[:3, :3]) for a, b in zip(traj, traj64)]
+        keys, _, tsdf, weight, _, _, sc = m.download_multires()
+        common, ia, ib = np.intersect1d(keys, keys64, return_indices=True)
+        same0 = (sc[ia, 0] == 0) & (sc64[ib, 0] == 0)
+        ta, tb = tsdf[ia][same0][:, :512], t64[ib][same0][:, :512]
+        both = (weight[ia][same0][:, :512] > 0) & (w64[ib][same0][:, :512] > 0)
+        e = np.abs(ta[both].astype(np.float64) - tb[both])
+        rp = torch.zeros((H, W, 3), dtype=torch.float32, device=dev)
+        rn = torch.zeros_like(rp)
+        se.raycast_volume(m, sensor, T_last.astype(np.float32), rp, rn)
+        rp = rp.cpu().numpy().astype(np.float64)
+        R, t = T_last[:3, :3], T_last[:3, 3]
+        z = lambda P: ((P - t) @ R)[..., 2]  # noqa: E731
+        hit = (rp != 0).any(-1) & (pts64 != 0).any(-1)
+        ez = np.abs(z(rp)[hit] - z(pts64)[hit])
+        q = lambda a, p: float(np.quantile(a, p)) if len(a) else None  # noqa: E731
+        out[st] = {
+            "pose_err_vs_f64": {"max_m": max(dt), "mean_m": float(np.mean(dt)), "max_deg": max(dr),
+                                "mean_deg": float(np.mean(dr))},
+            "tsdf_err_vs_f64_trunc_units": {"median": q(e, 0.5), "p99": q(e, 0.99), "p999": q(e, 0.999),
+                                            "max": float(e.max()) if len(e) else None, "voxels": int(len(e)),
+                                            "blocks_same_scale0": int(same0.sum()), "blocks_common": int(len(common))},
+            "raycast_depth_err_vs_f64_m": {"median": q(ez, 0.5), "p99": q(ez, 0.99), "p999": q(ez, 0.999),
+                                           "pixels": int(hit.sum())},
+        }
+        out["ate_m"][st] = ate(traj)
+        del fp, tr, m
+    return out
 
 
 # ------------------------------------------------------------------ 8-map LiDAR batch --
@@ -690,6 +777,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     ap.add_argument("--lidar-steps", type=int, default=20)
+    ap.add_argument("--precision-frames", type=int, default=300,
+                    help="frames of the FP64 precision report (0: no report)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

@@ -11,6 +11,12 @@
 
 #include "se_oracle.h"
 
+/* The type of IEEE binary32 bit manipulations; the FP64 build of the oracle (se_oracle_f64.cpp)
+ * turns every other float into a double. */
+#ifndef SO_BITS_FLOAT
+#define SO_BITS_FLOAT float
+#endif
+
 namespace {
 
 /* ---------------------------------------------------------------- small float algebra -- */

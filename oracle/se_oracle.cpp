@@ -471,17 +471,20 @@ static inline void map_get_data_mr(const so_map& m, V3 p_W, float& tsdf, float& 
  * [1, 2]^3 scaled frame, mirrored so that every direction component is negative. Returns the
  * state after the first next(): whether a block was found, tcmin() and tmax(). */
 
+/* The traversal's bit manipulations act on IEEE binary32 values (SO_BITS_FLOAT is float in
+ * every build, also the FP64 one). */
 static inline int32_t f_as_i(float f)
 {
+    const SO_BITS_FLOAT g = (SO_BITS_FLOAT) f;
     int32_t i;
-    std::memcpy(&i, &f, 4);
+    std::memcpy(&i, &g, 4);
     return i;
 }
 static inline float i_as_f(int32_t i)
 {
-    float f;
-    std::memcpy(&f, &i, 4);
-    return f;
+    SO_BITS_FLOAT g;
+    std::memcpy(&g, &i, 4);
+    return (float) g;
 }
 
 struct RayBlockHit {
@@ -1094,8 +1097,8 @@ static void mr_propagate_down(const so_map& m, const Octant& oc, MRBlock& b, int
                             const int ci = mr_index(oc, cc, cs);
                             if (b.weight[ci] != 0.0f) {
                                 const float delta = b.tsdf[pi] - b.past_tsdf[pi];
-                                b.tsdf[ci] = std::max(b.tsdf[ci] + delta, -1.0f);
-                                b.weight[ci] = fminf(b.weight[ci] + b.past_weight[pi], m.max_weight);
+                                b.tsdf[ci] = std::max(b.tsdf[ci] + delta, (float) -1.0f);
+                                b.weight[ci] = std::fmin(b.weight[ci] + b.past_weight[pi], m.max_weight);
                                 b.past_weight[ci] = b.past_weight[pi];
                             }
                             else {
@@ -1227,7 +1230,7 @@ static long long mr_update(so_map& m, const Pinhole& s, const Tf& T_WS, const fl
                     const float sdf = (dv - mz) / mz * pn;
                     const int idx = mr_index(oc, c, curr);
                     if (!(sdf < -trunc)) {
-                        const float upd = std::min(sdf / trunc, 1.0f);
+                        const float upd = std::min(sdf / trunc, (float) 1.0f);
                         float w = b.weight[idx];
                         if (w < m.max_weight)
                             w = w + 1.0f;
@@ -1475,7 +1478,7 @@ void so_integrate_depth(so_map* map, const float* depth, const so_pinhole* senso
                     /* FieldData<TSDF>::update, data_field_impl.hpp:39-54 */
                     if (sdf < -trunc)
                         continue;
-                    const float upd = std::min(sdf / trunc, 1.0f);
+                    const float upd = std::min(sdf / trunc, (float) 1.0f);
                     const int idx = x + 8 * y + 64 * z;
                     float w = b.weight[idx];
                     if (w < m.max_weight)
