@@ -444,7 +444,7 @@ def _adjoint_bench(se, torch, m, sensor, T_gt, obs, flush, reps=20, gn_steps=50,
         Hm = (J * wgt[:, None]).T @ J
         Hm = Hm + 1e-6 * torch.trace(Hm) * torch.eye(6, dtype=torch.float64, device="cuda")
         b = J.T @ torch.clamp(r, -delta, delta)
-        Tk = _se3_exp((-torch.linalg.solve(Hm, b)).cpu().numpy()) @ Tk
+        Tk = _se3_exp(-np.linalg.solve(Hm.cpu().numpy(), b.cpu().numpy())) @ Tk  # 6x6 on the host
 
     def pose_err(Ta):
         dT = np.linalg.inv(T_gt) @ Ta
