@@ -417,6 +417,70 @@ __device__ void occ_allocate_children(const OccDevice& m, int n)
         occ_aabb_extend(m, nc.x, nc.y, nc.z, nc.w);
 }
 
+// Octree::allocateChildren by a whole warp (uniform n): lane i < 8 initialises child slot i if it
+// is empty, one atomic reserves the pool entries of all of them.
+__device__ void occ_allocate_children_warp(const OccDevice& m, int n, int lane)
+{
+    const OccD init = node_data(m, n); // read before any child slot changes
+    const int4 nc = m.node_coord[n];
+    const int csize = nc.w / 2;
+    const bool blocks_below = nc.w == 16;
+    int* child = m.node_child + 8 * (size_t) n;
+    const int i = lane & 7;
+    const bool need = lane < 8 && child[i] == -1;
+    const unsigned mask = __ballot_sync(0xffffffffu, need);
+    const int cnt = __popc(mask);
+    int base = 0;
+    if (lane == 0 && cnt > 0)
+        base = atomicAdd(&m.counters[blocks_below ? kOccBlocks : kOccNodes], cnt);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (need) {
+        const int idx = base + __popc(mask & ((1u << lane) - 1u));
+        const int cx = nc.x + csize * (i & 1), cy = nc.y + csize * ((i >> 1) & 1), cz = nc.z + csize * (i >> 2);
+        if (blocks_below) {
+            if (idx >= m.block_capacity) {
+                atomicOr(&m.counters[kOccError], kOccErrBlockPool);
+            }
+            else {
+                m.block_coord[3 * idx] = cx;
+                m.block_coord[3 * idx + 1] = cy;
+                m.block_coord[3 * idx + 2] = cz;
+                OccBlockState st;
+                st.init_data = init;
+                st.min_scale = -1;
+                st.current_scale = kOccMaxScale;
+                st.finest = kOccMaxScale;
+                st.buffer_scale = -1;
+                st.curr_integr = st.curr_obs = st.buf_integr = st.buf_obs = 0ull;
+                st.parent = n;
+                st.live = 1;
+                m.block_state[idx] = st;
+                blk_mean(m, idx, kOccMaxScale)[0] = init;
+                child[i] = -2 - idx;
+            }
+        }
+        else {
+            if (idx >= m.node_capacity) {
+                atomicOr(&m.counters[kOccError], kOccErrNodePool);
+            }
+            else {
+                m.node_coord[idx] = make_int4(cx, cy, cz, csize);
+                m.node_parent[idx] = n;
+                for (int k = 0; k < 8; ++k)
+                    m.node_child[8 * (size_t) idx + k] = -1;
+                m.node_min[idx] = init;
+                m.node_max[idx] = init;
+                m.node_mark[idx] = -1;
+                m.node_ts[idx] = -1;
+                child[i] = idx;
+            }
+        }
+    }
+    __syncwarp();
+    if (blocks_below && lane == 0)
+        occ_aabb_extend(m, nc.x, nc.y, nc.z, nc.w);
+}
+
 // DensePoolingImage::maxValue over the coarsest level (the lanes share the visited pixels) and
 // VolumeCarver's max depth (volume_carver_impl.hpp:28-38), then the root's children as the first
 // frontier; one warp per map.
@@ -693,21 +757,29 @@ __global__ void __launch_bounds__(128) occ_carve_kernel(const OccLaunch* __restr
             ? carve_lidar(L, J, D, slot, cx, cy, cz, size, max_depth_value, should_split, var, projects_inside, lane)
             : carve_pinhole(L, J, D, slot, cx, cy, cz, size, max_depth_value, should_split, var, projects_inside,
                             lane);
-        if (keep && lane == 0) {
+        if (keep && !is_block && should_split) {
+            occ_allocate_children_warp(m, slot, lane);
+            // queue the children: one atomic for all of them, lane i writes child i
+            const int ch = lane < 8 ? m.node_child[8 * (size_t) slot + lane] : -1;
+            const unsigned mask = __ballot_sync(0xffffffffu, ch != -1); // -1 only when a pool ran out
+            int base = 0;
+            if (lane == 0 && mask)
+                base = atomicAdd(&m.counters[kOccFrontierN + depth + 1], __popc(mask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (ch != -1) {
+                const int k = base + __popc(mask & ((1u << lane) - 1u));
+                if (k < m.node_capacity + m.block_capacity)
+                    J.frontier[(depth + 1) & 1][k] = ch;
+                else
+                    atomicOr(err, kOccErrList);
+            }
+        }
+        else if (keep && lane == 0) {
             if (is_block) {
                 const int k = push(J.block_list, &m.counters[kOccBlockListN], m.block_capacity, slot_block(slot), err);
                 if (k < m.block_capacity) {
                     J.block_var[k] = var;
                     J.block_inside[k] = projects_inside ? 1 : 0;
-                }
-            }
-            else if (should_split) {
-                occ_allocate_children(m, slot);
-                for (int i = 0; i < 8; ++i) {
-                    const int ch = m.node_child[8 * (size_t) slot + i];
-                    if (ch != -1) // -1 only when a pool ran out (latched in the error word)
-                        push(J.frontier[(depth + 1) & 1], &m.counters[kOccFrontierN + depth + 1],
-                             m.node_capacity + m.block_capacity, ch, err);
                 }
             }
             else if (var == 0) {
@@ -922,7 +994,8 @@ __device__ void occ_prepare_buffer(const OccDevice& m, int b, OccBlockState& st,
         const OccD* cur = blk_mean(m, b, st.current_scale);
         for (unsigned k = lane; k < np * np2 * 8; k += 32) {
             const unsigned pidx = k >> 3, c = k & 7;
-            const unsigned x = pidx % np, y = (pidx / np) % np, z = pidx / np2;
+            const unsigned ls = 3u - (unsigned) last_scale; // np = 2^ls
+            const unsigned x = pidx & (np - 1u), y = (pidx >> ls) & (np - 1u), z = pidx >> (2u * ls);
             const unsigned i = c & 1, j = (c >> 1) & 1, kk = c >> 2;
             const OccD pd = cur[x + y * np + z * np2];
             OccD& bd = buf[(2 * x + i) + (2 * y + j) * nb + (2 * z + kk) * nb2];
@@ -1030,57 +1103,83 @@ __device__ void occ_update_block_data(const OccLaunch& L, const OccJob& J, const
     const float tau = clampf_std(tv, J.tau_min, J.tau_max);
     OccD* data = to_buffer ? blk_buffer(m, b, st) : blk_mean(m, b, st.current_scale);
     const float lom = m.cfg.log_odd_min, lomax = m.cfg.log_odd_max;
-    unsigned long long newly_total = 0;
-    for (int base = 0; base < n * n2; base += 32) {
-        const int k = base + lane;
-        bool newly = false;
-        if (k < n * n2) {
-            const int x = k % n, y = (k / n) % n, z = k / n2;
-            const float fx = (float) x, fy = (float) y, fz = (float) z;
-            const F3 dl = f3((Dm[0] * fx + Dm[1] * fy) + Dm[2] * fz, (Dm[3] * fx + Dm[4] * fy) + Dm[5] * fz,
-                             (Dm[6] * fx + Dm[7] * fy) + Dm[8] * fz);
-            const F3 p = add(base_C, dl);
-            float u, v;
-            if (lidar ? lidar_project(S.L, p, u, v) : project(S.s, p, u, v)) {
-                const int px = (int) (u + 0.5f), py = (int) (v + 0.5f);
-                const float dv = depth[px + py * S.w];
-                if (!(dv < S.near_plane)) {
-                    const float three_sigma = 3.0f * sigma[px + py * S.w];
-                    OccD d = data[k];
-                    bool count = true;
-                    if (low_var) {
-                        newly = !d.observed;
-                        occ_update(d, lom, m.cfg.max_weight);
-                        data[k] = d;
-                    }
-                    else {
-                        const float range = sqrtf(dot(p, p));
-                        const float pm = lidar ? range : p.z;
-                        const float range_diff = (pm - dv) * (range / pm);
-                        float sample = 0.0f;
-                        bool upd = true;
-                        if (range_diff < -three_sigma)
-                            sample = lom;
-                        else if (range_diff < tau / 2)
-                            sample = fminf(lom - lom / three_sigma * (range_diff + three_sigma), lomax);
-                        else if (range_diff < tau)
-                            sample = fminf(-lom * tau / (2 * three_sigma), lomax);
-                        else
-                            upd = false;
-                        if (upd) {
-                            newly = !d.observed;
-                            occ_update(d, sample, m.cfg.max_weight);
-                            data[k] = d;
-                        }
-                        if (dv > S.far_plane)
-                            count = false;
-                    }
-                    newly = newly && count;
-                }
+    // four voxels per lane per round: all projections first, then every load of the round in
+    // flight together, then the updates (the same per-voxel arithmetic as one at a time)
+    constexpr int kU = 4;
+    int newly_lane = 0;
+    for (int base = 0; base < n * n2; base += 32 * kU) {
+        F3 p[kU];
+        int pix[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const int k = base + lane + 32 * u;
+            pix[u] = -1;
+            p[u] = f3(0.0f, 0.0f, 0.0f);
+            if (k < n * n2) {
+                const int x = k & (n - 1), y = (k >> (3 - scale)) & (n - 1), z = k >> (2 * (3 - scale));
+                const float fx = (float) x, fy = (float) y, fz = (float) z;
+                const F3 dl = f3((Dm[0] * fx + Dm[1] * fy) + Dm[2] * fz, (Dm[3] * fx + Dm[4] * fy) + Dm[5] * fz,
+                                 (Dm[6] * fx + Dm[7] * fy) + Dm[8] * fz);
+                p[u] = add(base_C, dl);
+                float uu, vv;
+                if (lidar ? lidar_project(S.L, p[u], uu, vv) : project(S.s, p[u], uu, vv))
+                    pix[u] = (int) (uu + 0.5f) + (int) (vv + 0.5f) * S.w;
             }
         }
-        newly_total += warp_count(newly);
+        float dv[kU], sg[kU];
+        OccD d[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            dv[u] = 0.0f;
+            sg[u] = 0.0f;
+            d[u] = occ_default();
+            if (pix[u] >= 0) {
+                dv[u] = depth[pix[u]];
+                sg[u] = sigma[pix[u]];
+                d[u] = data[base + lane + 32 * u];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            if (pix[u] < 0 || dv[u] < S.near_plane)
+                continue;
+            const int k = base + lane + 32 * u;
+            const float three_sigma = 3.0f * sg[u];
+            bool newly = false, count = true;
+            if (low_var) {
+                newly = !d[u].observed;
+                occ_update(d[u], lom, m.cfg.max_weight);
+                data[k] = d[u];
+            }
+            else {
+                const float range = sqrtf(dot(p[u], p[u]));
+                const float pm = lidar ? range : p[u].z;
+                // for the LiDAR range / pm is range / range, exactly 1
+                const float range_diff = lidar ? (pm - dv[u]) : (pm - dv[u]) * (range / pm);
+                float sample = 0.0f;
+                bool upd = true;
+                if (range_diff < -three_sigma)
+                    sample = lom;
+                else if (range_diff < tau / 2)
+                    sample = fminf(lom - lom / three_sigma * (range_diff + three_sigma), lomax);
+                else if (range_diff < tau)
+                    sample = fminf(-lom * tau / (2 * three_sigma), lomax);
+                else
+                    upd = false;
+                if (upd) {
+                    newly = !d[u].observed;
+                    occ_update(d[u], sample, m.cfg.max_weight);
+                    data[k] = d[u];
+                }
+                if (dv[u] > S.far_plane)
+                    count = false;
+            }
+            newly_lane += (newly && count) ? 1 : 0;
+        }
     }
+    unsigned long long newly_total = (unsigned long long) newly_lane;
+    for (int o = 16; o > 0; o >>= 1)
+        newly_total += __shfl_xor_sync(0xffffffffu, newly_total, o);
     if (to_buffer) {
         st.buf_obs += newly_total;
         occ_incr_buffer_integr(st, inside);
@@ -1201,7 +1300,7 @@ __device__ void occ_process_block(const OccLaunch& L, const OccJob& J, int b, bo
 
 // freeBlock on the freed blocks and updateBlock on the carver's blocks (disjoint: the carver
 // does not descend below a free-space node), one warp per block, all maps.
-__global__ void __launch_bounds__(256, 3) occ_blocks_kernel(const OccLaunch* __restrict__ Lp)
+__global__ void __launch_bounds__(256, 2) occ_blocks_kernel(const OccLaunch* __restrict__ Lp)
 {
     const OccLaunch& L = *Lp;
     __shared__ int pre[kOccMaxBatch + 1];
@@ -1293,7 +1392,7 @@ __device__ void occ_propagate_block(const OccDevice& m, int b, int lane)
     int cs = st.current_scale;
     for (int ps = cs + 1; ps <= kOccMaxScale; ++ps) {
         cs = ps - 1;
-        const int np = 8 >> ps, nc = 8 >> cs;
+        const int np = 8 >> ps;
         OccD* pmin = blk_min(m, b, st.finest, ps);
         OccD* pmax = blk_max(m, b, st.finest, ps);
         OccD* pmean = blk_mean(m, b, ps);
@@ -1303,14 +1402,16 @@ __device__ void occ_propagate_block(const OccDevice& m, int b, int lane)
         const bool first = ps == st.current_scale + 1;
         const bool do_mean = !(first && st.buffer_scale > st.current_scale);
         for (int k = lane; k < np * np * np; k += 32) {
-            const int x = k % np, y = (k / np) % np, z = k / (np * np);
+            const int lp = 3 - ps; // np = 2^lp
+            const int x = k & (np - 1), y = (k >> lp) & (np - 1), z = k >> (2 * lp);
             // ch[0] is visited first so that ties keep the lowest child index, as the array form
             UpBest lo{FLT_MAX, OccD{0.0f, 0.0f, 0}, 0, 0}, hi{-FLT_MAX, OccD{0.0f, 0.0f, 0}, 0, 0};
             float os = 0.0f, ws = 0.0f;
             int nmean = 0;
             bool lo_first = true, hi_first = true;
             for (int c = 0; c < 8; ++c) {
-                const int ci = (2 * x + (c & 1)) + (2 * y + ((c >> 1) & 1)) * nc + (2 * z + (c >> 2)) * nc * nc;
+                const int ci = (2 * x + (c & 1)) + ((2 * y + ((c >> 1) & 1)) << (lp + 1))
+                    + ((2 * z + (c >> 2)) << (2 * (lp + 1)));
                 const OccD c0 = cmean[ci];
                 const OccD c1 = first ? c0 : cmin[ci];
                 const OccD c2 = first ? c0 : cmax[ci];
