@@ -302,6 +302,18 @@ SE_GPU_API se_gpu_status se_gpu_raycast_adjoint(const se_gpu_map* map, const se_
 
 /* --------------------------------------------------------------------------- tracker -- */
 
+/* Replaces se::preprocessor::downsample_depth(input, output) (src/map/preprocessor.cpp:19-84):
+ * each output pixel is the median (upper middle for an even count) of the depths >= 1e-5 of its
+ * ratio x ratio input region (ratio = w_in / w_out = h_in / h_out, at most 8), or 0 when none is
+ * valid; map_dev (may be NULL) receives the chosen input pixel x + y * w_in as the reference's
+ * Image<size_t>. Equal depths keep their region scan order (the reference's std::sort leaves
+ * that order unspecified), which decides map_dev only. Device pointers; stream-ordered. The
+ * matching sensor is se::PinholeCamera(config, ratio): fx / ratio, fy / ratio,
+ * (cx + 0.5) / ratio - 0.5, (cy + 0.5) / ratio - 0.5 (src/sensor/pinhole_camera.cpp:29-39). */
+SE_GPU_API se_gpu_status se_gpu_downsample_depth(const float* in_dev, int w_in, int h_in,
+                                                 float* out_dev, int w_out, int h_out,
+                                                 int64_t* map_dev, void* stream);
+
 /* The bilateral pre-filter (see se_gpu_bilateral_config) of a device depth image into another
  * device image (not in place). Stream-ordered. */
 SE_GPU_API se_gpu_status se_gpu_bilateral_filter(const float* in_dev, float* out_dev, int width,

@@ -126,6 +126,7 @@ def lib():
             "so_bilateral_weights": (None, [C.c_int, C.c_float, f32p]),
             "so_bilateral_filter": (None, [f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, f32p]),
             "so_exp_cw": (C.c_float, [C.c_float]),
+            "so_downsample_depth": (None, [f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, vp]),
             "so_point_cloud_to_normal": (None, [f32p, C.c_int, C.c_int, C.c_int, f32p]),
         }
         for name, (res, args) in sig.items():
@@ -433,6 +434,16 @@ def bilateral_filter(depth, radius=2, sigma_space=4.0, sigma_range=0.03):
     lib().so_bilateral_filter(depth.reshape(-1), w, h, int(radius), float(sigma_space), float(sigma_range),
                               out.reshape(-1))
     return out
+
+
+def downsample_depth(depth, ratio):
+    """preprocessor::downsample_depth: (out [h/ratio, w/ratio] float32, map int64 of input indices)."""
+    depth = np.ascontiguousarray(depth, np.float32)
+    h, w = depth.shape
+    out = np.zeros((h // ratio, w // ratio), np.float32)
+    mp = np.zeros(out.shape, np.int64)
+    lib().so_downsample_depth(depth.reshape(-1), w, h, out.reshape(-1), w // ratio, h // ratio, mp.ctypes.data)
+    return out, mp
 
 
 def exp_cw(x):

@@ -2058,6 +2058,48 @@ void so_bilateral_filter(const float* in, int w, int h, int radius, float sigma_
 
 float so_exp_cw(float x) { return exp_cw(x); }
 
+/* preprocessor::downsample_depth (src/map/preprocessor.cpp:19-84): per output pixel the median
+ * (the upper middle element for an even count) of the region's depths >= 1e-5, or 0 with the
+ * region's first pixel when none is valid; map = the chosen input pixel x + y * w_in. The
+ * reference sorts with std::sort, which leaves the order of equal depths unspecified; here they
+ * keep their region scan order (stable sort), the order the GPU uses too. */
+void so_downsample_depth(const float* in, int w_in, int h_in, float* out, int w_out, int h_out, int64_t* map)
+{
+    const int ratio = w_in / w_out;
+    (void) h_in;
+#pragma omp parallel for
+    for (int y_out = 0; y_out < h_out; ++y_out) {
+        std::vector<std::pair<float, int64_t>> region;
+        region.reserve((size_t) ratio * ratio);
+        for (int x_out = 0; x_out < w_out; ++x_out) {
+            const int xb = x_out * ratio, yb = y_out * ratio;
+            region.clear();
+            for (int yr = 0; yr < ratio; ++yr)
+                for (int xr = 0; xr < ratio; ++xr) {
+                    const int x = xb + xr, y = yb + yr;
+                    const float d = in[x + (size_t) y * w_in];
+                    if (d >= 1e-5f)
+                        region.push_back({d, (int64_t) x + (int64_t) y * w_in});
+                }
+            const size_t o = (size_t) x_out + (size_t) y_out * w_out;
+            if (region.empty()) {
+                out[o] = 0.0f;
+                if (map)
+                    map[o] = (int64_t) xb + (int64_t) yb * w_in;
+                continue;
+            }
+            std::stable_sort(region.begin(), region.end(),
+                             [](const std::pair<float, int64_t>& a, const std::pair<float, int64_t>& b) {
+                                 return a.first < b.first;
+                             });
+            const auto& v = region[region.size() / 2];
+            out[o] = v.first;
+            if (map)
+                map[o] = v.second;
+        }
+    }
+}
+
 void so_half_sample_robust(const float* in, int w, int h, float e_d, int radius, float* out)
 {
     half_sample_robust(in, w, h, e_d, radius, out);

@@ -236,6 +236,10 @@ void so_bilateral_weights(int radius, float sigma_space, float* ws);
 void so_bilateral_filter(const float* in, int w, int h, int radius, float sigma_space, float sigma_range, float* out);
 float so_exp_cw(float x);
 
+/* preprocessor::downsample_depth: median downsampling by the integer ratio w_in / w_out
+ * (equal in both axes); map (may be NULL) receives the chosen input pixel per output pixel. */
+void so_downsample_depth(const float* in, int w_in, int h_in, float* out, int w_out, int h_out, int64_t* map);
+
 /* Preprocessing helpers exposed for tests. */
 void so_half_sample_robust(const float* in, int w, int h, float e_d, int radius, float* out);
 void so_depth_to_point_cloud(const float* depth, const so_pinhole* sensor, float* pts);

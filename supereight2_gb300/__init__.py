@@ -24,7 +24,7 @@ from . import build as _build
 
 __all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "OusterLidar",
            "OccupancyBatch", "raycast_volume",
-           "render_depth", "raycast_adjoint", "track_noalloc", "bilateral_filter",
+           "render_depth", "raycast_adjoint", "track_noalloc", "bilateral_filter", "downsample_depth",
            "FramePipeline", "SeGpuError", "library", "library_path"]
 
 
@@ -101,6 +101,7 @@ SIGNATURES = {
     "se_gpu_integrate_depth": (C.c_int, [_VP, _VP, C.POINTER(_Pinhole), _F16, C.c_int, _VP]),
     "se_gpu_integrate_range": (C.c_int, [_VP, _VP, C.POINTER(_Lidar), _F16, C.c_int, _VP]),
     "se_gpu_bilateral_filter": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.POINTER(_BilateralConfig), _VP]),
+    "se_gpu_downsample_depth": (C.c_int, [_VP, C.c_int, C.c_int, _VP, C.c_int, C.c_int, _VP, _VP]),
     "se_gpu_frame_set_bilateral": (C.c_int, [_VP, C.POINTER(_BilateralConfig)]),
     "se_gpu_occ_batch_create": (C.c_int, [_VP, C.c_int, C.POINTER(_Pinhole), C.POINTER(_Lidar),
                                           C.c_int, C.POINTER(_VP)]),
@@ -204,6 +205,14 @@ class PinholeCamera:
     @classmethod
     def from_spec(cls, s):
         return cls(s.width, s.height, s.fx, s.fy, s.cx, s.cy, s.near_plane, s.far_plane)
+
+    def downsampled(self, dsf):
+        """se::PinholeCamera(config, dsf) (src/sensor/pinhole_camera.cpp:29-39), in float32."""
+        f = np.float32
+        d = f(dsf)
+        return PinholeCamera(int(f(self.width) / d), int(f(self.height) / d), f(self.fx) / d, f(self.fy) / d,
+                             (f(self.cx) + f(0.5)) / d - f(0.5), (f(self.cy) + f(0.5)) / d - f(0.5),
+                             self.near_plane, self.far_plane)
 
     def _c(self) -> _Pinhole:
         return _Pinhole(self.width, self.height, self.fx, self.fy, self.cx, self.cy,
@@ -621,6 +630,21 @@ def track_noalloc(sensor: PinholeCamera, config: TrackerConfig, depth, T_WS,
     _check(L.se_gpu_track_noalloc(C.byref(s), C.byref(c), d, p, n, T_WS.ctypes.data_as(_F16),
                                   C.byref(acc), red, _stream(stream)), "se_gpu_track_noalloc")
     return bool(acc.value), np.array(red[:], np.float32)
+
+
+def downsample_depth(depth, out, map=None, stream=None):
+    """se::preprocessor::downsample_depth(input, output): median downsampling of a [H, W] float32
+    CUDA tensor into out ([H / r, W / r]); map (int64, out's shape, optional) receives the chosen
+    input pixel x + y * W. Returns map."""
+    import torch
+    H, W = depth.shape
+    h, w = out.shape
+    pin = _dptr(depth, torch.float32, (H, W), "depth")
+    pout = _dptr(out, torch.float32, (h, w), "out")
+    pmap = _dptr(map, torch.int64, (h, w), "map") if map is not None else None
+    _check(library().se_gpu_downsample_depth(pin, W, H, pout, w, h, pmap, _stream(stream)),
+           "se_gpu_downsample_depth")
+    return map
 
 
 def bilateral_filter(depth, out=None, radius=2, sigma_space=4.0, sigma_range=0.03, stream=None):

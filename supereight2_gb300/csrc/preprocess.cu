@@ -124,3 +124,71 @@ extern "C" se_gpu_status se_gpu_bilateral_filter(const float* in_dev, float* out
         return st;
     return enqueue_bilateral(in_dev, out_dev, width, height, *config, (cudaStream_t) stream);
 }
+
+// ------------------------------------------------------------------ depth downsampling --
+
+namespace se_gpu {
+
+constexpr int kDownsampleMaxRatio = 8;
+
+// preprocessor::downsample_depth (src/map/preprocessor.cpp:19-84), one thread per output pixel:
+// the region's depths >= 1e-5 in scan order, then the element of stable rank count / 2 (rank =
+// the smaller depths plus the equal ones earlier in the scan), i.e. the stable sort's middle
+// element; 0 and the region's first pixel when no depth is valid.
+__global__ void downsample_depth_kernel(const float* __restrict__ in, int w_in, float* __restrict__ out, int w_out,
+                                        int h_out, int ratio, long long* __restrict__ map)
+{
+    const int x_out = blockIdx.x * blockDim.x + threadIdx.x, y_out = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x_out >= w_out || y_out >= h_out)
+        return;
+    const int xb = x_out * ratio, yb = y_out * ratio;
+    float v[kDownsampleMaxRatio * kDownsampleMaxRatio];
+    int idx[kDownsampleMaxRatio * kDownsampleMaxRatio];
+    int n = 0;
+    for (int yr = 0; yr < ratio; ++yr)
+        for (int xr = 0; xr < ratio; ++xr) {
+            const float d = in[(xb + xr) + (size_t) (yb + yr) * w_in];
+            if (d >= 1e-5f) {
+                v[n] = d;
+                idx[n] = xr + yr * ratio;
+                ++n;
+            }
+        }
+    const size_t o = (size_t) x_out + (size_t) y_out * w_out;
+    if (n == 0) {
+        out[o] = 0.0f;
+        if (map)
+            map[o] = (long long) xb + (long long) yb * w_in;
+        return;
+    }
+    const int want = n / 2;
+    int pick = 0;
+    for (int i = 0; i < n; ++i) {
+        int rank = 0;
+        for (int j = 0; j < n; ++j)
+            rank += (v[j] < v[i] || (v[j] == v[i] && j < i)) ? 1 : 0;
+        if (rank == want)
+            pick = i;
+    }
+    out[o] = v[pick];
+    if (map)
+        map[o] = (long long) (xb + idx[pick] % ratio) + (long long) (yb + idx[pick] / ratio) * w_in;
+}
+
+} // namespace se_gpu
+
+extern "C" se_gpu_status se_gpu_downsample_depth(const float* in_dev, int w_in, int h_in, float* out_dev, int w_out,
+                                                 int h_out, int64_t* map_dev, void* stream)
+{
+    if (!in_dev || !out_dev || w_out <= 0 || h_out <= 0 || w_in < w_out || h_in < h_out || w_in % w_out != 0
+        || h_in % h_out != 0 || w_in / w_out != h_in / h_out || w_in / w_out > se_gpu::kDownsampleMaxRatio) {
+        se_gpu::set_last_error("se_gpu_downsample_depth: the input must be 1..%d times the output in both axes",
+                               se_gpu::kDownsampleMaxRatio);
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    const dim3 block(32, 8), grid((w_out + 31) / 32, (h_out + 7) / 8);
+    se_gpu::downsample_depth_kernel<<<grid, block, 0, (cudaStream_t) stream>>>(
+        in_dev, w_in, out_dev, w_out, h_out, w_in / w_out, reinterpret_cast<long long*>(map_dev));
+    SE_CUDA_TRY(cudaGetLastError());
+    return SE_GPU_OK;
+}
