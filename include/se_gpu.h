@@ -335,6 +335,12 @@ SE_GPU_API se_gpu_status se_gpu_tracker_destroy(se_gpu_tracker* tracker);
 SE_GPU_API se_gpu_status se_gpu_track(se_gpu_tracker* tracker, const float* depth_dev,
                            const float* ref_pts_W_dev, const float* ref_nrm_W_dev,
                            float T_WS[16], int* accepted, void* stream);
+/* ICP launch shape (no counterpart in the reference): 1 (the default when the grid fits on the
+ * device) runs all levels and iterations of a track() in one cooperative launch whose CTAs meet
+ * at a bounded grid barrier after each iteration; 0 launches one kernel per iteration. Both
+ * give bit-identical poses. A barrier that times out rejects the frame's pose (accepted = 0)
+ * and se_gpu_track returns SE_GPU_ERR_CUDA. */
+SE_GPU_API se_gpu_status se_gpu_tracker_set_persistent(se_gpu_tracker* tracker, int enable);
 /* Final 32-float reduction of the last track (icp.cpp:45-204 layout: [sum e^2, J^T e (6),
  * upper J^T J (21), inliers, distance rejects, normal rejects, other]) and the iterations run
  * per level. Synchronous. */

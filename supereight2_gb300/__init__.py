@@ -101,6 +101,7 @@ SIGNATURES = {
     "se_gpu_integrate_depth": (C.c_int, [_VP, _VP, C.POINTER(_Pinhole), _F16, C.c_int, _VP]),
     "se_gpu_integrate_range": (C.c_int, [_VP, _VP, C.POINTER(_Lidar), _F16, C.c_int, _VP]),
     "se_gpu_bilateral_filter": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.POINTER(_BilateralConfig), _VP]),
+    "se_gpu_tracker_set_persistent": (C.c_int, [_VP, C.c_int]),
     "se_gpu_downsample_depth": (C.c_int, [_VP, C.c_int, C.c_int, _VP, C.c_int, C.c_int, _VP, _VP]),
     "se_gpu_frame_set_bilateral": (C.c_int, [_VP, C.POINTER(_BilateralConfig)]),
     "se_gpu_occ_batch_create": (C.c_int, [_VP, C.c_int, C.POINTER(_Pinhole), C.POINTER(_Lidar),
@@ -564,6 +565,10 @@ class Tracker:
         _check(self._L.se_gpu_track(self.h, d, p, n, T_WS.ctypes.data_as(_F16), C.byref(acc),
                                     _stream(stream)), "se_gpu_track")
         return bool(acc.value)
+
+    def set_persistent(self, enable=True):
+        """One cooperative launch per track() (default when it fits) or one launch per ICP iteration."""
+        _check(self._L.se_gpu_tracker_set_persistent(self.h, 1 if enable else 0), "se_gpu_tracker_set_persistent")
 
     def last_reduction(self):
         red = (C.c_float * 32)()

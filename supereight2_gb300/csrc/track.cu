@@ -32,6 +32,7 @@ enum {
     kFlagDone0 = 0,  // level converged flags 0..2
     kFlagIters0 = 3, // iterations run per level 3..5
     kFlagAccepted = 6,
+    kFlagBarrierTimeout = 7, // the persistent ICP kernel's grid barrier gave up waiting
     kNumFlags = 8
 };
 
@@ -665,7 +666,9 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
 __global__ void icp_check_kernel(TrackState* st, int W, int H, float track_threshold, float* pose12_out)
 {
     const float* v = st->last_red;
-    const bool reject = ((double) sqrtf(v[0] / v[28]) > 2e-2) || (v[28] / (float) (W * H) < track_threshold);
+    // a timed-out grid barrier of the persistent ICP leaves no trustworthy pose: reject it
+    const bool reject = ((double) sqrtf(v[0] / v[28]) > 2e-2) || (v[28] / (float) (W * H) < track_threshold)
+        || st->flags[kFlagBarrierTimeout] != 0;
     if (reject) {
         for (int i = 0; i < 12; ++i) {
             st->pose_f[i] = st->ref_f[i];
@@ -676,6 +679,189 @@ __global__ void icp_check_kernel(TrackState* st, int W, int H, float track_thres
     if (pose12_out)
         for (int i = 0; i < 12; ++i)
             pose12_out[i] = st->pose_f[i];
+}
+
+// ------------------------------------------------------- persistent ICP (all iterations) --
+// The per-iteration launches above, fused into one cooperative launch per frame: every CTA
+// runs every iteration of every level; after each iteration's main pass the CTAs meet at a
+// grid barrier, and each CTA then merges the CTA partials and solves redundantly (the same
+// operations in the same order, so every CTA holds the same new pose) instead of one last CTA
+// solving and the next launch reading its result. The pixel partition, the merge order and
+// the FP64 tail are those of icp_iter_kernel, so the poses are bit-identical to it.
+
+struct IcpLevels {
+    IterParams ip[3];
+    int nctas[3];
+    int iters[3];
+    int levels;
+};
+
+constexpr unsigned kIcpSpinLimit = 1u << 22; // ~0.3 s of polling at most, then the timeout flag
+
+// Grid barrier on a monotonic counter (reset to 0 before the launch): every CTA adds one and
+// waits until the count reaches target. Bounded: on timeout (or when another CTA timed out)
+// the flag is set and the CTA goes on, so a stuck launch ends with an error instead of hanging.
+__device__ __forceinline__ void icp_grid_sync(unsigned* ctr, unsigned target, int* timeout)
+{
+    __threadfence(); // every thread's partial stores before the arrival
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicAdd(ctr, 1u);
+        unsigned spins = 0;
+        while (*((volatile unsigned*) ctr) < target) {
+            if (*((volatile int*) timeout) != 0 || ++spins > kIcpSpinLimit) {
+                atomicExch(timeout, 1);
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kTrackThreads, 3) icp_persistent_kernel(Pinhole s, IcpLevels L, TrackState* st,
+                                                                         float2* __restrict__ partials)
+{
+    constexpr int kWarps = kTrackThreads / 32;
+    __shared__ float sh_terms[kWarps][32][33];
+    __shared__ float2 sh_warp[kWarps][32];
+    __shared__ Tf T, Tri;
+    __shared__ double sh_pose[12];
+    __shared__ double sh_new[12];
+    __shared__ float sh_newf[12];
+    __shared__ double sh_val[32];
+    __shared__ int sh_conv;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < 12) {
+        const int i = threadIdx.x, r = i >> 2, c = i & 3;
+        if (c < 3) {
+            T.R[3 * r + c] = st->pose_f[i];
+            Tri.R[3 * r + c] = st->ref_inv[i];
+        }
+        else {
+            T.t[r] = st->pose_f[i];
+            Tri.t[r] = st->ref_inv[i];
+        }
+        sh_pose[i] = st->pose[i];
+    }
+    __syncthreads();
+    unsigned phase = 0;
+    for (int level = L.levels - 1; level >= 0; --level) {
+        const IterParams& ip = L.ip[level];
+        const int nct = L.nctas[level];
+        for (int iter = 0; iter < L.iters[level]; ++iter) {
+            float2* part = partials + (size_t) (phase & 1u) * kMaxTrackCtas * 32;
+            if ((int) blockIdx.x < nct) {
+                CSum acc[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+                const int npix = ip.w * ip.h;
+                const int stride = nct * kTrackThreads;
+                int i = blockIdx.x * kTrackThreads + threadIdx.x;
+                bool in_range = i < npix;
+                F3 n_cur = in_range ? ld3(ip.nrm, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
+                F3 p_cur = in_range ? ld3(ip.pts, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
+                for (int base = blockIdx.x * kTrackThreads; base < npix; base += stride) {
+                    const int i_next = i + stride;
+                    const bool next_in = i_next < npix;
+                    const F3 n_next = next_in ? ld3(ip.nrm, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
+                    const F3 p_next = next_in ? ld3(ip.pts, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
+                    float v[32];
+                    icp_pixel_terms(s, ip, T, Tri, in_range, n_cur, p_cur, v);
+#pragma unroll
+                    for (int k = 0; k < 32; ++k)
+                        sh_terms[warp][lane][k] = v[k];
+                    __syncwarp();
+#pragma unroll 4
+                    for (int j = 0; j < 32; ++j)
+                        acc[j & 3].add(sh_terms[warp][j][lane]);
+                    __syncwarp();
+                    i = i_next;
+                    in_range = next_in;
+                    n_cur = n_next;
+                    p_cur = p_next;
+                }
+                acc[0].merge(acc[1].hi, acc[1].lo);
+                acc[2].merge(acc[3].hi, acc[3].lo);
+                acc[0].merge(acc[2].hi, acc[2].lo);
+                sh_warp[warp][lane] = make_float2(acc[0].hi, acc[0].lo);
+                __syncthreads();
+                if (threadIdx.x < 32) {
+                    CSum t{0.0f, 0.0f};
+                    for (int wi = 0; wi < kWarps; ++wi)
+                        t.merge(sh_warp[wi][threadIdx.x].x, sh_warp[wi][threadIdx.x].y);
+                    part[blockIdx.x * 32 + threadIdx.x] = make_float2(t.hi, t.lo);
+                }
+            }
+            ++phase;
+            icp_grid_sync(&st->ticket, phase * gridDim.x, &st->flags[kFlagBarrierTimeout]);
+            // every CTA: merge the nct partials in icp_iter_kernel's order, solve, update
+            {
+                CSum t{0.0f, 0.0f};
+                for (int b0 = warp; b0 < nct; b0 += 16 * kWarps) {
+                    float2 pr[16];
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) {
+                        const int b = b0 + u * kWarps;
+                        pr[u] = b < nct ? __ldcg(&part[b * 32 + lane]) : make_float2(0.0f, 0.0f);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 16; ++u)
+                        t.merge(pr[u].x, pr[u].y);
+                }
+                sh_warp[warp][lane] = make_float2(t.hi, t.lo);
+            }
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                CSum t{0.0f, 0.0f};
+                for (int c = 0; c < kWarps; ++c)
+                    t.merge(sh_warp[c][threadIdx.x].x, sh_warp[c][threadIdx.x].y);
+                const double v = (double) t.hi + (double) t.lo;
+                sh_val[threadIdx.x] = v;
+                if (blockIdx.x == 0)
+                    st->last_red[threadIdx.x] = (float) v;
+            }
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                double xs[6];
+                if (!warp_solve6(sh_val, xs)) {
+#pragma unroll
+                    for (int k = 0; k < 6; ++k)
+                        xs[k] = 0.0;
+                }
+                warp_exp_compose(xs, sh_pose, sh_new, sh_newf);
+                if (threadIdx.x == 0) {
+                    double xn = 0.0;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k)
+                        xn = fma(xs[k], xs[k], xn);
+                    const double thr = (double) ip.icp_threshold;
+                    sh_conv = xn < thr * thr;
+                    if (blockIdx.x == 0)
+                        st->flags[kFlagIters0 + level] += 1;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x < 12) {
+                const int i = threadIdx.x, r = i >> 2, c = i & 3;
+                sh_pose[i] = sh_new[i];
+                if (c < 3)
+                    T.R[3 * r + c] = sh_newf[i];
+                else
+                    T.t[r] = sh_newf[i];
+            }
+            __syncthreads();
+            if (sh_conv) {
+                if (blockIdx.x == 0 && threadIdx.x == 0)
+                    st->flags[kFlagDone0 + level] = 1;
+                break;
+            }
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x < 12) {
+        st->pose[threadIdx.x] = sh_pose[threadIdx.x];
+        const int i = threadIdx.x, r = i >> 2, c = i & 3;
+        st->pose_f[i] = c < 3 ? T.R[3 * r + c] : T.t[r];
+    }
 }
 
 } // namespace se_gpu
@@ -691,9 +877,11 @@ struct se_gpu_tracker {
     float* pyr_depth[3]; // levels 1, 2 (index 0 unused: the input is level 0)
     float* pts[3];
     float* nrm[3];
-    float2* partials;
+    float2* partials;    // two sets of kMaxTrackCtas x 32 (the persistent kernel alternates)
     TrackState* state;
     int nctas[3];
+    int persistent;      // one cooperative launch per frame (when the grid fits on the GPU)
+    int persistent_ctas; // its grid: the largest level's CTA count
 };
 
 extern "C" {
@@ -738,8 +926,19 @@ se_gpu_status se_gpu_tracker_create(const se_gpu_pinhole* sensor, const se_gpu_t
         if (t->nctas[l] > kMaxTrackCtas)
             t->nctas[l] = kMaxTrackCtas;
     }
-    if ((e = cudaMalloc(&t->partials, (size_t) kMaxTrackCtas * 32 * sizeof(float2))) != cudaSuccess)
+    if ((e = cudaMalloc(&t->partials, (size_t) 2 * kMaxTrackCtas * 32 * sizeof(float2))) != cudaSuccess)
         return fail(e, "cudaMalloc(partials)");
+    {
+        // the persistent kernel needs its whole grid resident at once
+        int per_sm = 0;
+        t->persistent_ctas = 0;
+        for (int l = 0; l < t->levels; ++l)
+            t->persistent_ctas = t->nctas[l] > t->persistent_ctas ? t->nctas[l] : t->persistent_ctas;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, icp_persistent_kernel, kTrackThreads, 0))
+            != cudaSuccess)
+            return fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        t->persistent = per_sm * device_sm_count() >= t->persistent_ctas ? 1 : 0;
+    }
     if ((e = cudaMalloc(&t->state, sizeof(TrackState))) != cudaSuccess)
         return fail(e, "cudaMalloc(state)");
     if ((e = cudaMemset(t->state, 0, sizeof(TrackState))) != cudaSuccess)
@@ -803,8 +1002,11 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
         normals_kernel<<<g, b, 0, stream>>>(li, t->levels, t->s.left_hand);
     }
     }
+    IcpLevels L;
+    std::memset(&L, 0, sizeof(L));
+    L.levels = t->levels;
     for (int level = t->levels - 1; level >= 0; --level) {
-        IterParams ip;
+        IterParams& ip = L.ip[level];
         ip.ref_pts = ref_pts;
         ip.ref_nrm = ref_nrm;
         ip.pts = t->pts[level];
@@ -816,10 +1018,30 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
         ip.dist_threshold = t->config.dist_threshold;
         ip.normal_threshold = t->config.normal_threshold;
         ip.icp_threshold = t->config.icp_threshold;
-        for (int it = 0; it < t->config.iterations[level]; ++it) {
-            ProfScope ps(kProfIcpIter, stream);
-            icp_iter_kernel<<<t->nctas[level], kTrackThreads, 0, stream>>>(t->s, ip, t->state, t->partials);
-        }
+        L.nctas[level] = t->nctas[level];
+        L.iters[level] = t->config.iterations[level];
+    }
+    if (t->persistent) {
+        ProfScope ps(kProfIcpIter, stream);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(t->persistent_ctas);
+        cfg.blockDim = dim3(kTrackThreads);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        SE_CUDA_TRY(cudaLaunchKernelEx(&cfg, icp_persistent_kernel, t->s, L, t->state, t->partials));
+    }
+    else {
+        for (int level = t->levels - 1; level >= 0; --level)
+            for (int it = 0; it < t->config.iterations[level]; ++it) {
+                ProfScope ps(kProfIcpIter, stream);
+                icp_iter_kernel<<<t->nctas[level], kTrackThreads, 0, stream>>>(t->s, L.ip[level], t->state,
+                                                                               t->partials);
+            }
     }
     {
         ProfScope ps(kProfIcpCheck, stream);
@@ -857,6 +1079,29 @@ se_gpu_status se_gpu_track(se_gpu_tracker* t, const float* depth_dev, const floa
     T_WS[15] = 1.0f;
     if (accepted)
         *accepted = hs.flags[kFlagAccepted];
+    if (hs.flags[kFlagBarrierTimeout]) {
+        set_last_error("se_gpu_track: the ICP grid barrier timed out (the pose was reverted)");
+        return SE_GPU_ERR_CUDA;
+    }
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_tracker_set_persistent(se_gpu_tracker* t, int enable)
+{
+    if (!t) {
+        set_last_error("se_gpu_tracker_set_persistent: null tracker");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    if (enable) {
+        int per_sm = 0;
+        SE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, icp_persistent_kernel, kTrackThreads, 0));
+        if (per_sm * device_sm_count() < t->persistent_ctas) {
+            set_last_error("se_gpu_tracker_set_persistent: %d CTAs do not fit on the device at once",
+                           t->persistent_ctas);
+            return SE_GPU_ERR_NOT_SUPPORTED;
+        }
+    }
+    t->persistent = enable ? 1 : 0;
     return SE_GPU_OK;
 }
 
