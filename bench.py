@@ -45,7 +45,7 @@ def _peaks():
 
 
 # Bench kernel names -> the kernel names of the committed DRAM-traffic capture of this workload
-_TRAFFIC_NAMES = {"icp_iter": "icp_persistent_kernel", "update": "update_kernel<0>", "raycast": "raycast_kernel<0>",
+_TRAFFIC_NAMES = {"icp_iter": "icp_persistent_kernel", "update": "update_kernel<0>", "raycast": "raycast_kernel<0, 0>",
                   "carve": "carve_kernel", "frustum": "frustum_kernel"}
 
 

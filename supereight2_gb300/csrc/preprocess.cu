@@ -34,18 +34,21 @@ __device__ __forceinline__ float exp_cw(float x)
     const float p = 1.0f
         + r * (1.0f + r * (0.5f + r * (0.166666672f + r * (0.0416666679f + r * (0.00833333377f
                                                      + r * (0.00138888892f + r * 0.000198412701f))))));
-    return ldexpf(p, (int) n);
+    // p * 2^n: n >= -126 here, so 2^n is a normal float and the product is the correctly
+    // rounded value ldexp gives
+    return p * __int_as_float(((int) n + 127) << 23);
 }
 
 constexpr int kTileX = 32, kTileY = 8;
 
+template <int R>
 __global__ void __launch_bounds__(kTileX * kTileY) bilateral_kernel(const float* __restrict__ in,
                                                                     float* __restrict__ out,
                                                                     const __grid_constant__ BilateralParams P)
 {
-    constexpr int kMaxW = kTileX + 2 * kBilateralMaxRadius, kMaxH = kTileY + 2 * kBilateralMaxRadius;
+    constexpr int kMaxW = kTileX + 2 * R, kMaxH = kTileY + 2 * R;
     __shared__ float tile[kMaxH][kMaxW];
-    const int r = P.radius;
+    constexpr int r = R;
     const int tw = kTileX + 2 * r, th = kTileY + 2 * r;
     const int x0 = blockIdx.x * kTileX - r, y0 = blockIdx.y * kTileY - r;
     for (int i = threadIdx.y * kTileX + threadIdx.x; i < tw * th; i += kTileX * kTileY) {
@@ -63,9 +66,11 @@ __global__ void __launch_bounds__(kTileX * kTileY) bilateral_kernel(const float*
         out[x + y * P.w] = 0.0f;
         return;
     }
-    const int n = 2 * r + 1;
+    constexpr int n = 2 * r + 1;
     float num = 0.0f, den = 0.0f;
+#pragma unroll
     for (int dy = -r; dy <= r; ++dy) {
+#pragma unroll
         for (int dx = -r; dx <= r; ++dx) {
             const float d = tile[threadIdx.y + r + dy][threadIdx.x + r + dx];
             if (!(d > 0.0f))
@@ -103,7 +108,17 @@ se_gpu_status enqueue_bilateral(const float* in, float* out, int w, int h, const
         for (int dx = -c.radius; dx <= c.radius; ++dx)
             P.ws[(dy + c.radius) * n + (dx + c.radius)] = (float) std::exp(-(double) (dx * dx + dy * dy) / (2.0 * s * s));
     const dim3 grid((w + kTileX - 1) / kTileX, (h + kTileY - 1) / kTileY);
-    bilateral_kernel<<<grid, dim3(kTileX, kTileY), 0, stream>>>(in, out, P);
+    const dim3 block(kTileX, kTileY);
+    switch (c.radius) {
+    case 0: bilateral_kernel<0><<<grid, block, 0, stream>>>(in, out, P); break;
+    case 1: bilateral_kernel<1><<<grid, block, 0, stream>>>(in, out, P); break;
+    case 2: bilateral_kernel<2><<<grid, block, 0, stream>>>(in, out, P); break;
+    case 3: bilateral_kernel<3><<<grid, block, 0, stream>>>(in, out, P); break;
+    case 4: bilateral_kernel<4><<<grid, block, 0, stream>>>(in, out, P); break;
+    case 5: bilateral_kernel<5><<<grid, block, 0, stream>>>(in, out, P); break;
+    case 6: bilateral_kernel<6><<<grid, block, 0, stream>>>(in, out, P); break;
+    default: bilateral_kernel<7><<<grid, block, 0, stream>>>(in, out, P); break;
+    }
     SE_CUDA_TRY(cudaGetLastError());
     return SE_GPU_OK;
 }
