@@ -157,46 +157,70 @@ __global__ void __launch_bounds__(256) update_kernel(MapDevice m, Pinhole s, con
         const int c0 = m.block_coord[3 * blk], c1 = m.block_coord[3 * blk + 1], c2 = m.block_coord[3 * blk + 2];
         if (lane == 0)
             m.block_ts[blk] = timestamp;
-#pragma unroll 4
-        for (int k = 0; k < kBlockVoxels / 32; ++k) {
-            const int vi = lane + 32 * k;
-            const int x = vi & 7, y = (vi >> 3) & 7, z = vi >> 6;
-            bool do_update = false;
-            float upd = 0.0f;
-            const F3 p_C = apply(T_CV, f3((float) (c0 + x), (float) (c1 + y), (float) (c2 + z)));
-            // A voxel with z <= 0 never updates: z < 0 fails the far test (far / nz < 0) and
-            // z == 0 fails the projection; skipping it early changes no result.
-            const float sq = p_C.z > 0.0f ? dot(p_C, p_C) : 0.0f;
-            const float pn = sqrtf(sq);
-            // farDist(p) = far / p.normalized().z
-            const float nz = p_C.z / pn;
-            if (p_C.z > 0.0f && !(pn > s.far_plane / nz)) {
-                float u, v;
-                if (project(s, p_C, u, v)) {
-                    const int px = (int) (u + 0.5f), py = (int) (v + 0.5f);
-                    const float dv = __ldg(&depth[px + py * s.w]);
-                    if (!(dv < s.near_plane)) {
-                        const float mz = p_C.z;
-                        const float sdf = (dv - mz) / mz * pn;
-                        if (!(sdf < -trunc)) {
-                            const float r = sdf / trunc;
-                            upd = (1.0f < r) ? 1.0f : r;
-                            do_update = true;
-                        }
+        // four voxels per lane per round: their projections, then their four depth loads in
+        // flight together, then the voxel loads of those that update, then the updates (the
+        // per-voxel arithmetic is that of one voxel at a time)
+        constexpr int kU = 4;
+        for (int k0 = 0; k0 < kBlockVoxels / 32; k0 += kU) {
+            int pix[kU];
+            float mz[kU], pn[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int vi = lane + 32 * (k0 + u);
+                const int x = vi & 7, y = (vi >> 3) & 7, z = vi >> 6;
+                const F3 p_C = apply(T_CV, f3((float) (c0 + x), (float) (c1 + y), (float) (c2 + z)));
+                // A voxel with z <= 0 never updates: z < 0 fails the far test (far / nz < 0) and
+                // z == 0 fails the projection; skipping it early changes no result.
+                const float sq = p_C.z > 0.0f ? dot(p_C, p_C) : 0.0f;
+                pn[u] = sqrtf(sq);
+                mz[u] = p_C.z;
+                pix[u] = -1;
+                // farDist(p) = far / p.normalized().z
+                const float nz = p_C.z / pn[u];
+                if (p_C.z > 0.0f && !(pn[u] > s.far_plane / nz)) {
+                    float uu, vv;
+                    if (project(s, p_C, uu, vv))
+                        pix[u] = (int) (uu + 0.5f) + (int) (vv + 0.5f) * s.w;
+                }
+            }
+            float dv[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u)
+                dv[u] = pix[u] >= 0 ? __ldg(&depth[pix[u]]) : 0.0f;
+            float upd[kU];
+            bool du[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                du[u] = false;
+                upd[u] = 0.0f;
+                if (pix[u] >= 0 && !(dv[u] < s.near_plane)) {
+                    const float sdf = (dv[u] - mz[u]) / mz[u] * pn[u];
+                    if (!(sdf < -trunc)) {
+                        const float r = sdf / trunc;
+                        upd[u] = (1.0f < r) ? 1.0f : r;
+                        du[u] = true;
                     }
                 }
             }
-            if (do_update || is_new) {
-                float tsdf = 1.0f, w = 0.0f;
-                if (!is_new)
-                    load_voxel<S>(m, blk, vi, tsdf, w);
-                if (do_update) {
-                    if (w < m.max_weight)
-                        w = w + 1.0f;
-                    tsdf = (tsdf * (w - 1.0f) + upd) / w;
-                    ++n_upd;
+            float tsdf[kU], w[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                tsdf[u] = 1.0f;
+                w[u] = 0.0f;
+                if (du[u] && !is_new)
+                    load_voxel<S>(m, blk, lane + 32 * (k0 + u), tsdf[u], w[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                if (du[u] || is_new) {
+                    if (du[u]) {
+                        if (w[u] < m.max_weight)
+                            w[u] = w[u] + 1.0f;
+                        tsdf[u] = (tsdf[u] * (w[u] - 1.0f) + upd[u]) / w[u];
+                        ++n_upd;
+                    }
+                    store_voxel<S>(m, blk, lane + 32 * (k0 + u), tsdf[u], w[u]);
                 }
-                store_voxel<S>(m, blk, vi, tsdf, w);
             }
         }
     }
