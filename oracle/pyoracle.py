@@ -126,6 +126,8 @@ def lib():
             "so_bilateral_weights": (None, [C.c_int, C.c_float, f32p]),
             "so_bilateral_filter": (None, [f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, f32p]),
             "so_exp_cw": (C.c_float, [C.c_float]),
+            "so_marching_cubes": (C.c_longlong, [vp, vp, C.c_longlong]),
+            "so_mc_table": (None, [i32p, i32p]),
             "so_downsample_depth": (None, [f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, vp]),
             "so_point_cloud_to_normal": (None, [f32p, C.c_int, C.c_int, C.c_int, f32p]),
         }
@@ -393,6 +395,14 @@ class OracleMap:
                                    *[a.ctypes.data for a in arrs], scales.ctypes.data)
         return (keys, coords, *arrs, scales)
 
+    def marching_cubes(self):
+        """Faces [N, 3, 3] (float32, voxel units of the map frame)."""
+        n = int(lib().so_marching_cubes(self.h, None, 0))
+        f = np.zeros((n, 3, 3), np.float32)
+        if n:
+            lib().so_marching_cubes(self.h, f.ctypes.data, n)
+        return f
+
     def aabb(self):
         mn = np.zeros(3, np.int32)
         mx = np.zeros(3, np.int32)
@@ -434,6 +444,13 @@ def bilateral_filter(depth, radius=2, sigma_space=4.0, sigma_range=0.03):
     lib().so_bilateral_filter(depth.reshape(-1), w, h, int(radius), float(sigma_space), float(sigma_range),
                               out.reshape(-1))
     return out
+
+
+def mc_table():
+    ntri = np.zeros(256, np.int32)
+    tri = np.zeros(256 * 24, np.int32)
+    lib().so_mc_table(ntri, tri)
+    return ntri, tri.reshape(256, 24)
 
 
 def downsample_depth(depth, ratio):

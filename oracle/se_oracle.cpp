@@ -1755,6 +1755,221 @@ void so_map_blocks(const so_map* map, uint64_t* keys, int32_t* coords, float* ts
     }
 }
 
+/* ------------------------------------------------------------------ marching cubes -- */
+/* The reference triangulates with a third-party case table (edge_tables.hpp); this oracle builds
+ * its case table from a stated rule instead (the GPU library builds the same table from the
+ * same rule, independently):
+ *  - corners in the order of meshing::gather_data: c0 (0,0,0), c1 (1,0,0), c2 (1,0,1),
+ *    c3 (0,0,1), c4 (0,1,0), c5 (1,1,0), c6 (1,1,1), c7 (0,1,1); edges as edge_to_corners
+ *    (marching_cube_impl.hpp:96-127); case index bit i = corner i inside;
+ *  - on each cube face the crossed edges are joined into segments; a face with four crossed
+ *    edges (inside corners on a diagonal) gets the two segments that cut off its inside corners;
+ *  - the segments of all faces close into loops (each crossed edge lies on two faces); a loop
+ *    is walked from its lowest edge number towards the lower-numbered of that edge's two
+ *    neighbours, then reversed if its Newell normal (edge midpoints) points from outside
+ *    corners to inside ones, so that faces point away from the inside;
+ *  - each loop is fanned from its first edge; loops in the order of their lowest edge. */
+namespace {
+
+constexpr int kMcCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 0, 1}, {0, 0, 1},
+                                 {0, 1, 0}, {1, 1, 0}, {1, 1, 1}, {0, 1, 1}};
+constexpr int kMcEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {0, 3}, {4, 5}, {5, 6},
+                                {6, 7}, {4, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+constexpr int kMcFace[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 3, 7, 4}, {1, 2, 6, 5}, {0, 1, 5, 4}, {3, 2, 6, 7}};
+constexpr int kMcMaxTri = 8;
+
+struct McTable {
+    int ntri[256];
+    signed char tri[256][3 * kMcMaxTri];
+};
+
+static int mc_edge_of(int a, int b)
+{
+    for (int e = 0; e < 12; ++e)
+        if ((kMcEdge[e][0] == a && kMcEdge[e][1] == b) || (kMcEdge[e][0] == b && kMcEdge[e][1] == a))
+            return e;
+    return -1;
+}
+
+static McTable build_mc_table()
+{
+    McTable T;
+    std::memset(&T, 0, sizeof(T));
+    for (int cfg = 0; cfg < 256; ++cfg) {
+        auto in = [cfg](int c) { return ((cfg >> c) & 1) != 0; };
+        int nb[12][2];
+        int deg[12] = {0};
+        for (int f = 0; f < 6; ++f) {
+            const int* c = kMcFace[f];
+            int crossed[4], nc = 0;
+            for (int k = 0; k < 4; ++k)
+                if (in(c[k]) != in(c[(k + 1) & 3]))
+                    crossed[nc++] = k; /* edge between c[k] and c[k+1] */
+            auto link = [&](int ka, int kb) {
+                const int ea = mc_edge_of(c[ka], c[(ka + 1) & 3]), eb = mc_edge_of(c[kb], c[(kb + 1) & 3]);
+                nb[ea][deg[ea]++] = eb;
+                nb[eb][deg[eb]++] = ea;
+            };
+            if (nc == 2) {
+                link(crossed[0], crossed[1]);
+            }
+            else if (nc == 4) {
+                for (int k = 0; k < 4; ++k)
+                    if (in(c[k]))
+                        link((k + 3) & 3, k); /* the two edges at inside corner c[k] */
+            }
+        }
+        bool used[12] = {false};
+        int n = 0;
+        for (int e0 = 0; e0 < 12; ++e0) {
+            if (deg[e0] == 0 || used[e0])
+                continue;
+            int loop[12], len = 0;
+            int prev = -1, cur = e0;
+            const int first_next = nb[e0][0] < nb[e0][1] ? nb[e0][0] : nb[e0][1];
+            while (true) {
+                loop[len++] = cur;
+                used[cur] = true;
+                int next;
+                if (prev < 0)
+                    next = first_next;
+                else
+                    next = nb[cur][0] == prev ? nb[cur][1] : nb[cur][0];
+                prev = cur;
+                cur = next;
+                if (cur == e0)
+                    break;
+            }
+            /* orientation: Newell normal against the inside -> outside direction */
+            double N[3] = {0, 0, 0}, D[3] = {0, 0, 0};
+            for (int i = 0; i < len; ++i) {
+                double a[3], b[3];
+                for (int k = 0; k < 3; ++k) {
+                    a[k] = 0.5 * (kMcCorner[kMcEdge[loop[i]][0]][k] + kMcCorner[kMcEdge[loop[i]][1]][k]);
+                    b[k] = 0.5 * (kMcCorner[kMcEdge[loop[(i + 1) % len]][0]][k]
+                                  + kMcCorner[kMcEdge[loop[(i + 1) % len]][1]][k]);
+                }
+                N[0] += (a[1] - b[1]) * (a[2] + b[2]);
+                N[1] += (a[2] - b[2]) * (a[0] + b[0]);
+                N[2] += (a[0] - b[0]) * (a[1] + b[1]);
+                const int ci = in(kMcEdge[loop[i]][0]) ? kMcEdge[loop[i]][0] : kMcEdge[loop[i]][1];
+                const int co = in(kMcEdge[loop[i]][0]) ? kMcEdge[loop[i]][1] : kMcEdge[loop[i]][0];
+                for (int k = 0; k < 3; ++k)
+                    D[k] += kMcCorner[co][k] - kMcCorner[ci][k];
+            }
+            if (N[0] * D[0] + N[1] * D[1] + N[2] * D[2] < 0.0)
+                std::reverse(loop + 1, loop + len);
+            for (int i = 1; i + 1 < len; ++i) {
+                T.tri[cfg][3 * n] = (signed char) loop[0];
+                T.tri[cfg][3 * n + 1] = (signed char) loop[i];
+                T.tri[cfg][3 * n + 2] = (signed char) loop[i + 1];
+                ++n;
+            }
+        }
+        T.ntri[cfg] = n;
+    }
+    return T;
+}
+
+static const McTable& mc_table()
+{
+    static const McTable t = build_mc_table();
+    return t;
+}
+
+/* meshing::compute_intersection (marching_cube_impl.hpp:82-93): corner values by getData */
+static V3 mc_vertex(const so_map& m, int x, int y, int z, int e)
+{
+    const int* a = kMcCorner[kMcEdge[e][0]];
+    const int* b = kMcCorner[kMcEdge[e][1]];
+    const int32_t c0[3] = {x + a[0], y + a[1], z + a[2]}, c1[3] = {x + b[0], y + b[1], z + b[2]};
+    float v0, w0, v1, w1;
+    get_voxel(m, c0, v0, w0);
+    get_voxel(m, c1, v1, w1);
+    const V3 p0 = v3((float) c0[0] + 0.5f, (float) c0[1] + 0.5f, (float) c0[2] + 0.5f);
+    const V3 p1 = v3((float) c1[0] + 0.5f, (float) c1[1] + 0.5f, (float) c1[2] + 0.5f);
+    const float sfac = (0.0f - v0) / (v1 - v0);
+    return v3(p0.x + sfac * (p1.x - p0.x), p0.y + sfac * (p1.y - p0.y), p0.z + sfac * (p1.z - p0.z));
+}
+
+} // namespace
+
+/* The case table (for the tests): ntri[256], tri[256][24] edge indices. */
+void so_mc_table(int32_t* ntri, int32_t* tri)
+{
+    const McTable& t = mc_table();
+    for (int c = 0; c < 256; ++c) {
+        ntri[c] = t.ntri[c];
+        for (int k = 0; k < 3 * kMcMaxTri; ++k)
+            tri[c * 3 * kMcMaxTri + k] = k < 3 * t.ntri[c] ? t.tri[c][k] : -1;
+    }
+}
+
+/* algorithms::marching_cube single-res (marching_cube_impl.hpp:830-890, 1175-1201) with the
+ * isosurface::occupied index: per allocated block the cubes [coord, min(coord + 8, size - 1))
+ * per axis; a cube with an unobserved corner (weight 0) has no faces; a face with a vertex
+ * coordinate <= 0 or > size (checkVertex) is dropped. faces: 9 floats each (three vertices in
+ * voxel units, the map frame divided by the resolution); returns the face count (faces may be
+ * NULL to count). */
+long long so_marching_cubes(const so_map* mp, float* faces, long long capacity)
+{
+    const so_map& m = *mp;
+    const Octree& oct = m.octree;
+    const McTable& T = mc_table();
+    const int size = oct.size;
+    std::vector<std::vector<float>> per_block(oct.block_octant.size());
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long long i = 0; i < (long long) oct.block_octant.size(); ++i) {
+        const Octant& oc = oct.octants[oct.block_octant[(size_t) i]];
+        std::vector<float>& out = per_block[(size_t) i];
+        const int lx = std::min(oc.coord[0] + kBlockSize, size - 1), ly = std::min(oc.coord[1] + kBlockSize, size - 1),
+                  lz = std::min(oc.coord[2] + kBlockSize, size - 1);
+        for (int x = oc.coord[0]; x < lx; ++x)
+            for (int y = oc.coord[1]; y < ly; ++y)
+                for (int z = oc.coord[2]; z < lz; ++z) {
+                    int cfg = 0;
+                    bool valid = true;
+                    for (int k = 0; k < 8 && valid; ++k) {
+                        const int32_t c[3] = {x + kMcCorner[k][0], y + kMcCorner[k][1], z + kMcCorner[k][2]};
+                        float t, w;
+                        get_voxel(m, c, t, w);
+                        if (w == 0.0f)
+                            valid = false;
+                        else if (t < 0.0f)
+                            cfg |= 1 << k;
+                    }
+                    if (!valid || T.ntri[cfg] == 0)
+                        continue;
+                    for (int f = 0; f < T.ntri[cfg]; ++f) {
+                        V3 v[3];
+                        bool keep = true;
+                        for (int j = 0; j < 3; ++j) {
+                            v[j] = mc_vertex(m, x, y, z, T.tri[cfg][3 * f + j]);
+                            if (v[j].x <= 0.0f || v[j].y <= 0.0f || v[j].z <= 0.0f || v[j].x > (float) size
+                                || v[j].y > (float) size || v[j].z > (float) size)
+                                keep = false;
+                        }
+                        if (!keep)
+                            continue;
+                        for (int j = 0; j < 3; ++j) {
+                            out.push_back(v[j].x);
+                            out.push_back(v[j].y);
+                            out.push_back(v[j].z);
+                        }
+                    }
+                }
+    }
+    long long n = 0;
+    for (const auto& b : per_block) {
+        const long long k = (long long) b.size() / 9;
+        if (faces)
+            for (long long j = 0; j < k && n + j < capacity; ++j)
+                std::memcpy(faces + 9 * (n + j), b.data() + 9 * j, 9 * sizeof(float));
+        n += k;
+    }
+    return n;
+}
+
 int so_map_aabb(const so_map* map, int32_t mn[3], int32_t mx[3])
 {
     const Octree& oct = map->octree;

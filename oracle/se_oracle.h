@@ -240,6 +240,11 @@ float so_exp_cw(float x);
  * (equal in both axes); map (may be NULL) receives the chosen input pixel per output pixel. */
 void so_downsample_depth(const float* in, int w_in, int h_in, float* out, int w_out, int h_out, int64_t* map);
 
+/* Marching cubes of a single-res map: faces (9 floats each, voxel units), returns the count;
+ * the case table it triangulates with (ntri[256], tri[256 * 24], -1 padded). */
+long long so_marching_cubes(const so_map* map, float* faces, long long capacity);
+void so_mc_table(int32_t* ntri, int32_t* tri);
+
 /* Preprocessing helpers exposed for tests. */
 void so_half_sample_robust(const float* in, int w, int h, float e_d, int radius, float* out);
 void so_depth_to_point_cloud(const float* depth, const so_pinhole* sensor, float* pts);

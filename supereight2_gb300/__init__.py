@@ -24,7 +24,7 @@ from . import build as _build
 
 __all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "OusterLidar",
            "OccupancyBatch", "raycast_volume",
-           "render_depth", "raycast_adjoint", "track_noalloc", "bilateral_filter", "downsample_depth",
+           "render_depth", "raycast_adjoint", "track_noalloc", "bilateral_filter", "downsample_depth", "marching_cube",
            "FramePipeline", "SeGpuError", "library", "library_path"]
 
 
@@ -102,6 +102,8 @@ SIGNATURES = {
     "se_gpu_integrate_range": (C.c_int, [_VP, _VP, C.POINTER(_Lidar), _F16, C.c_int, _VP]),
     "se_gpu_bilateral_filter": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.POINTER(_BilateralConfig), _VP]),
     "se_gpu_tracker_set_persistent": (C.c_int, [_VP, C.c_int]),
+    "se_gpu_marching_cube": (C.c_int, [_VP, _VP, C.c_int64, C.POINTER(C.c_int64), _VP]),
+    "se_gpu_mc_case_table": (C.c_int, [_VP, _VP]),
     "se_gpu_downsample_depth": (C.c_int, [_VP, C.c_int, C.c_int, _VP, C.c_int, C.c_int, _VP, _VP]),
     "se_gpu_frame_set_bilateral": (C.c_int, [_VP, C.POINTER(_BilateralConfig)]),
     "se_gpu_occ_batch_create": (C.c_int, [_VP, C.c_int, C.POINTER(_Pinhole), C.POINTER(_Lidar),
@@ -635,6 +637,29 @@ def track_noalloc(sensor: PinholeCamera, config: TrackerConfig, depth, T_WS,
     _check(L.se_gpu_track_noalloc(C.byref(s), C.byref(c), d, p, n, T_WS.ctypes.data_as(_F16),
                                   C.byref(acc), red, _stream(stream)), "se_gpu_track_noalloc")
     return bool(acc.value), np.array(red[:], np.float32)
+
+
+def marching_cube(map: Map, stream=None):
+    """se::algorithms::marching_cube(octree) for a single-res TSDF map: faces [N, 3, 3] (float32
+    CUDA tensor, vertices in voxel units of the map frame; world = T_WM (res v))."""
+    import torch
+    L = library()
+    n = C.c_int64()
+    _check(L.se_gpu_marching_cube(map.h, None, 0, C.byref(n), _stream(stream)), "se_gpu_marching_cube")
+    out = torch.empty((max(n.value, 1), 3, 3), dtype=torch.float32, device="cuda")
+    cap = n.value
+    _check(L.se_gpu_marching_cube(map.h, C.c_void_p(out.data_ptr()), cap, C.byref(n), _stream(stream)),
+           "se_gpu_marching_cube")
+    return out[: n.value]
+
+
+def mc_case_table():
+    """(ntri[256], tri[256, 15]) of the library's marching-cubes case table (host only)."""
+    ntri = np.zeros(256, np.int32)
+    tri = np.zeros(256 * 15, np.int32)
+    _check(library(build_if_missing=True).se_gpu_mc_case_table(ntri.ctypes.data, tri.ctypes.data),
+           "se_gpu_mc_case_table")
+    return ntri, tri.reshape(256, 15)
 
 
 def downsample_depth(depth, out, map=None, stream=None):
