@@ -247,6 +247,35 @@ SE_GPU_API se_gpu_status se_gpu_marching_cube(se_gpu_map* map, float* faces_dev,
  * neighbour, reversed when the Newell normal points inwards, fanned from the first edge. */
 SE_GPU_API se_gpu_status se_gpu_mc_case_table(int32_t ntri[256], int32_t tri[256 * 15]);
 
+/* ------------------------------------------------------------------------------- IO -- */
+/* The reference's on-disk outputs (include/se/map/io/*), written by this library's own host code
+ * in the same standard ASCII formats. io::save_mesh (mesh_io_impl.hpp): faces (host, 9 floats
+ * each) transformed by T_OV (row-major 4x4 affine), format by extension: .ply, .vtk (polydata
+ * with a per-face scale), .obj. */
+SE_GPU_API se_gpu_status se_gpu_save_mesh(const float* faces, int64_t n, const float T_OV[16],
+                                          const char* filename);
+/* Map::mesh's transform T_OV = T_OW * T_WM * Scaling(res) (map_impl.hpp:454-459). */
+SE_GPU_API se_gpu_status se_gpu_map_mesh_transform(const se_gpu_map* map, const float T_OW[16],
+                                                   float T_OV[16]);
+/* Map::saveMesh(filename, T_OW) (map_impl.hpp:464-469) for single-res TSDF maps: marching cubes
+ * on the GPU, then se_gpu_save_mesh. Synchronous. */
+SE_GPU_API se_gpu_status se_gpu_map_save_mesh(se_gpu_map* map, const float T_OW[16],
+                                              const char* filename, void* stream);
+/* io::save_point_cloud_vtk (point_cloud_io_impl.hpp): n points (host, xyz) transformed by T_WC. */
+SE_GPU_API se_gpu_status se_gpu_save_point_cloud_vtk(const float* points, int64_t n,
+                                                     const float T_WC[16], const char* filename);
+/* get_field(getData(coord)) of a single-res TSDF map over the voxel box [lo, hi), x fastest,
+ * into out_host ((hi - lo) product floats). Synchronous. */
+SE_GPU_API se_gpu_status se_gpu_map_field_box(const se_gpu_map* map, const int32_t lo[3],
+                                              const int32_t hi[3], float* out_host);
+/* Map::saveFieldSlices(fx, fy, fz, point_W) (map_impl.hpp:273-320 with io::save_3d_slice_vtk,
+ * octree_io_impl.hpp): the x, y and z slices of the field through the voxel of point_W as VTK
+ * rectilinear grids (an empty or NULL name skips that slice). Single-res TSDF maps. */
+SE_GPU_API se_gpu_status se_gpu_map_save_field_slices(const se_gpu_map* map, const char* filename_x,
+                                                      const char* filename_y,
+                                                      const char* filename_z,
+                                                      const float point_W[3]);
+
 /* Block download for checking and checkpointing. Writes up to capacity blocks:
  * keys (Morton code << 5 | 3), coords (3 ints: the block's minimum voxel), tsdf and weight
  * (512 floats per block, x + 8y + 64z), timestamps. Host pointers, any may be NULL.

@@ -104,6 +104,12 @@ SIGNATURES = {
     "se_gpu_tracker_set_persistent": (C.c_int, [_VP, C.c_int]),
     "se_gpu_marching_cube": (C.c_int, [_VP, _VP, C.c_int64, C.POINTER(C.c_int64), _VP]),
     "se_gpu_mc_case_table": (C.c_int, [_VP, _VP]),
+    "se_gpu_save_mesh": (C.c_int, [_VP, C.c_int64, _F16, C.c_char_p]),
+    "se_gpu_map_mesh_transform": (C.c_int, [_VP, _F16, _F16]),
+    "se_gpu_map_save_mesh": (C.c_int, [_VP, _F16, C.c_char_p, _VP]),
+    "se_gpu_save_point_cloud_vtk": (C.c_int, [_VP, C.c_int64, _F16, C.c_char_p]),
+    "se_gpu_map_field_box": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "se_gpu_map_save_field_slices": (C.c_int, [_VP, C.c_char_p, C.c_char_p, C.c_char_p, _F16]),
     "se_gpu_downsample_depth": (C.c_int, [_VP, C.c_int, C.c_int, _VP, C.c_int, C.c_int, _VP, _VP]),
     "se_gpu_frame_set_bilateral": (C.c_int, [_VP, C.POINTER(_BilateralConfig)]),
     "se_gpu_occ_batch_create": (C.c_int, [_VP, C.c_int, C.POINTER(_Pinhole), C.POINTER(_Lidar),
@@ -415,6 +421,35 @@ class Map:
         """Map::getFieldInterp for a CUDA [N, 3] float32 tensor: (values [N], valid [N] bool)."""
         return self._field_query(points_W, stream, grad=False)
 
+    def mesh_transform(self, T_OW=None):
+        """T_OV = T_OW T_WM Scaling(res): voxel-unit mesh vertices to the output frame."""
+        _, tw = _m16(np.eye(4) if T_OW is None else T_OW)
+        out = np.zeros(16, np.float32)
+        _check(self._L.se_gpu_map_mesh_transform(self.h, tw, out.ctypes.data_as(_F16)), "se_gpu_map_mesh_transform")
+        return out.reshape(4, 4)
+
+    def saveMesh(self, filename, T_OW=None, stream=None):
+        """Map::saveMesh: marching cubes written as .ply / .vtk / .obj in the T_OW frame."""
+        _, tw = _m16(np.eye(4) if T_OW is None else T_OW)
+        _check(self._L.se_gpu_map_save_mesh(self.h, tw, str(filename).encode(), _stream(stream)),
+               "se_gpu_map_save_mesh")
+
+    def saveFieldSlices(self, filename_x, filename_y, filename_z, point_W):
+        """Map::saveFieldSlices: VTK rectilinear slices of the field through point_W's voxel."""
+        p = np.ascontiguousarray(np.asarray(point_W, np.float32).reshape(3))
+        enc = lambda s: str(s).encode() if s else None  # noqa: E731
+        _check(self._L.se_gpu_map_save_field_slices(self.h, enc(filename_x), enc(filename_y), enc(filename_z),
+                                                    p.ctypes.data_as(_F16)), "se_gpu_map_save_field_slices")
+
+    def field_box(self, lo, hi):
+        """get_field(getData(v)) over the voxel box [lo, hi) as an array [z, y, x]."""
+        lo = np.ascontiguousarray(lo, np.int32)
+        hi = np.ascontiguousarray(hi, np.int32)
+        out = np.zeros(tuple(int(v) for v in (hi - lo)[::-1]), np.float32)
+        _check(self._L.se_gpu_map_field_box(self.h, lo.ctypes.data, hi.ctypes.data, out.ctypes.data),
+               "se_gpu_map_field_box")
+        return out
+
     def getFieldGrad(self, points_W, stream=None):
         """Map::getFieldGrad for a CUDA [N, 3] float32 tensor: (grads [N, 3], valid [N] bool)."""
         return self._field_query(points_W, stream, grad=True)
@@ -651,6 +686,22 @@ def marching_cube(map: Map, stream=None):
     _check(L.se_gpu_marching_cube(map.h, C.c_void_p(out.data_ptr()), cap, C.byref(n), _stream(stream)),
            "se_gpu_marching_cube")
     return out[: n.value]
+
+
+def save_mesh(faces, filename, T_OV=None):
+    """io::save_mesh: faces [N, 3, 3] (numpy or tensor) transformed by T_OV (4x4, default the
+    identity), written as .ply, .vtk or .obj."""
+    f = np.ascontiguousarray(faces.cpu().numpy() if hasattr(faces, "cpu") else faces, np.float32).reshape(-1, 9)
+    _, tp = _m16(np.eye(4) if T_OV is None else T_OV)
+    _check(library().se_gpu_save_mesh(f.ctypes.data, len(f), tp, str(filename).encode()), "se_gpu_save_mesh")
+
+
+def save_point_cloud_vtk(points, filename, T_WC=None):
+    """io::save_point_cloud_vtk: points [..., 3] transformed by T_WC."""
+    p = np.ascontiguousarray(points.cpu().numpy() if hasattr(points, "cpu") else points, np.float32).reshape(-1, 3)
+    _, tp = _m16(np.eye(4) if T_WC is None else T_WC)
+    _check(library().se_gpu_save_point_cloud_vtk(p.ctypes.data, len(p), tp, str(filename).encode()),
+           "se_gpu_save_point_cloud_vtk")
 
 
 def mc_case_table():

@@ -260,7 +260,7 @@ __device__ __forceinline__ void store_voxel(const MapDevice& m, int blk, int vi,
 }
 
 // Map::contains + pointToVoxel<Safe::On> (include/se/map/impl/map_impl.hpp:58-64,538-550).
-__device__ __forceinline__ bool point_to_voxel(const MapDevice& m, F3 p_W, int& vx, int& vy, int& vz)
+__host__ __device__ __forceinline__ bool point_to_voxel(const MapDevice& m, F3 p_W, int& vx, int& vy, int& vz)
 {
     const F3 p = apply(m.T_MW, p_W);
     if (!(p.x >= 0.0f && p.x < m.dim && p.y >= 0.0f && p.y < m.dim && p.z >= 0.0f && p.z < m.dim))
@@ -270,7 +270,7 @@ __device__ __forceinline__ bool point_to_voxel(const MapDevice& m, F3 p_W, int& 
     vz = (int) (p.z / m.res);
     return true;
 }
-__device__ __forceinline__ bool point_to_voxel_f(const MapDevice& m, F3 p_W, F3& v)
+__host__ __device__ __forceinline__ bool point_to_voxel_f(const MapDevice& m, F3 p_W, F3& v)
 {
     const F3 p = apply(m.T_MW, p_W);
     if (!(p.x >= 0.0f && p.x < m.dim && p.y >= 0.0f && p.y < m.dim && p.z >= 0.0f && p.z < m.dim))
