@@ -1,0 +1,138 @@
+"""The committed golden fixtures (tests/golden/, made by tests/golden/make_golden.py):
+
+- reference_pins.json holds values extracted from the reference's own test sources; the pins the
+  oracle and GPU tests assert (tests/reference_cases.py, tests/test_oracle_occupancy.py) must be
+  those values.
+- oracle_fixtures.npz holds small inputs and the oracle's outputs on them as recorded when the
+  fixtures were made. The oracle built here must reproduce them bit for bit (its float arithmetic
+  is written out operation by operation and compiled without contraction, on any machine), and
+  the GPU path must reproduce them too: bit for bit where the parity tests require it (TSDF
+  blocks, filters, meshes, occupancy integers), within the parity tolerances elsewhere.
+"""
+import json
+import os
+import zlib
+
+import numpy as np
+import pytest
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FIX = np.load(os.path.join(HERE, "oracle_fixtures.npz"))
+PINS = json.load(open(os.path.join(HERE, "reference_pins.json")))
+
+
+def crc(a) -> int:
+    return zlib.crc32(np.ascontiguousarray(a).tobytes()) & 0xffffffff
+
+
+def _pinhole(mod):
+    from supereight2_gb300 import synthetic as syn
+    s = syn.SENSOR_320
+    return mod(s.width, s.height, s.fx, s.fy, s.cx, s.cy, s.near_plane, s.far_plane)
+
+
+def _block_crcs(keys, tsdf, weight):
+    order = np.argsort(keys)
+    return keys[order], np.array([crc(tsdf[i]) ^ (crc(weight[i]) << 1 & 0xffffffff) for i in order], np.uint64)
+
+
+def test_pins_are_the_reference_tests_values():
+    from tests import reference_cases as rc
+    assert [tuple(x) for x in PINS["map_sizes"]] == [tuple(x) for x in rc.MAP_SIZES]
+    src = open(os.path.join(os.path.dirname(HERE), "test_oracle_occupancy.py")).read()
+    for c in PINS["occupancy_free"] + PINS["occupancy_unknown"] + PINS["occupancy_interp_free"]:
+        assert "(%d, %d, %d)" % tuple(c) in src
+    assert PINS["occupancy_free_value"] == PINS["occupancy_interp_value"] == -5.015
+
+
+def test_oracle_reproduces_fixtures(oracle):
+    frames, poses = FIX["frames"], FIX["poses"]
+    s = _pinhole(oracle.pinhole)
+    m = oracle.OracleMap(10.24, 0.02)
+    for i in range(4):
+        m.integrate_depth(frames[i], s, poses[i], i)
+    keys, _, tsdf, weight, _ = m.blocks()
+    k, c = _block_crcs(keys, tsdf, weight)
+    assert np.array_equal(k, FIX["tsdf_keys"]) and np.array_equal(c, FIX["tsdf_crc"])
+    pts, nrm, _ = m.raycast(s, poses[3])
+    assert [crc(pts), crc(nrm)] == list(FIX["raycast_crc"])
+    filt = oracle.bilateral_filter(frames[4])
+    assert crc(filt) == FIX["bilateral_crc"][0]
+    acc, T4, _ = oracle.track(s, oracle.tracker_config(), filt, poses[3], pts, nrm)
+    # the oracle's ICP sums in OpenMP order, which depends on the thread count: within the pose bar
+    assert int(acc) == FIX["track_accepted"][0]
+    assert np.max(np.abs(T4.astype(np.float32) - FIX["track_pose"])) <= 1e-5
+    ds, dmap = oracle.downsample_depth(frames[4], 2)
+    assert [crc(ds), crc(dmap)] == list(FIX["downsample_crc"])
+    assert len(m.marching_cubes()) == FIX["mc_faces"][0]
+    _check_occupancy_oracle(oracle)
+
+
+def _lidar(mod):
+    from supereight2_gb300 import synthetic as syn
+    L = syn.LIDAR_64
+    return mod(L.width, L.height, L.elevation_min_deg, L.elevation_max_deg, L.near_plane, L.far_plane)
+
+
+def _t_mw():
+    T = np.eye(4, dtype=np.float32)
+    T[:3, 3] = (51.2, 51.2, 12.8)
+    return T
+
+
+def _occ_arrays(c, sc, mean):
+    key = (c[:, 0].astype(np.int64) << 40) | (c[:, 1].astype(np.int64) << 20) | c[:, 2]
+    order = np.argsort(key)
+    return (c[order], sc[order], np.array([crc(mean[i][:, 1:]) for i in order], np.uint64),
+            np.array([mean[i][:, 0].astype(np.float64).sum() for i in order]),
+            np.array([crc(mean[i]) for i in order], np.uint64))
+
+
+def _check_occupancy_oracle(oracle):
+    om = oracle.OracleOccMap(102.4, 0.4, T_MW=_t_mw())
+    st = om.integrate_lidar(FIX["lidar_scan"], _lidar(oracle.lidar), FIX["lidar_pose"], 0)
+    assert [st.n_blocks_listed, st.n_nodes_listed, st.n_blocks_freed, st.n_nodes_pruned] == list(FIX["occ_counts"])
+    c, sc, cnt, mean, _, _ = om.blocks()
+    coords, scales, ci, osum, full = _occ_arrays(c, sc, mean)
+    assert np.array_equal(coords, FIX["occ_coords"]) and np.array_equal(scales, FIX["occ_scales"])
+    assert np.array_equal(full, FIX["occ_crc"])
+
+
+@pytest.mark.gpu
+def test_gpu_reproduces_fixtures(gpu):
+    import torch
+    frames, poses = FIX["frames"], FIX["poses"]
+    from supereight2_gb300 import synthetic as syn
+    sensor = gpu.PinholeCamera.from_spec(syn.SENSOR_320)
+    m = gpu.Map(10.24, 0.02, max_blocks=1 << 16)
+    integ = gpu.MapIntegrator(m)
+    for i in range(4):
+        integ.integrateDepth(i, torch.from_numpy(frames[i]).cuda(), sensor, poses[i])
+    keys, _, tsdf, weight, _ = m.download_blocks()
+    k, c = _block_crcs(keys, tsdf, weight)
+    assert np.array_equal(k, FIX["tsdf_keys"]) and np.array_equal(c, FIX["tsdf_crc"])
+    d4 = torch.from_numpy(frames[4]).cuda()
+    filt = gpu.bilateral_filter(d4)
+    assert crc(filt.cpu().numpy()) == FIX["bilateral_crc"][0]
+    ds = torch.empty((120, 160), device="cuda")
+    dmap = torch.empty((120, 160), dtype=torch.int64, device="cuda")
+    gpu.downsample_depth(d4, ds, dmap)
+    assert [crc(ds.cpu().numpy()), crc(dmap.cpu().numpy())] == list(FIX["downsample_crc"])
+    assert len(gpu.marching_cube(m)) == FIX["mc_faces"][0]
+    pts = torch.zeros((240, 320, 3), device="cuda")
+    nrm = torch.zeros_like(pts)
+    gpu.raycast_volume(m, sensor, poses[3], pts, nrm)
+    T = poses[3].copy()
+    acc = gpu.Tracker(m, sensor).track(filt, T, pts, nrm)
+    assert int(acc) == FIX["track_accepted"][0]
+    assert np.max(np.abs(T[:3, 3] - FIX["track_pose"][:3, 3])) <= 1e-5
+    assert np.max(np.abs(T[:3, :3] - FIX["track_pose"][:3, :3])) <= 1e-5
+    om = gpu.Map(102.4, 0.4, res_type="multi", field="occupancy", max_blocks=1 << 14, T_MW=_t_mw())
+    gpu.MapIntegrator(om).integrateDepth(0, torch.from_numpy(FIX["lidar_scan"]).cuda(),
+                                         gpu.OusterLidar.from_spec(syn.LIDAR_64), FIX["lidar_pose"])
+    assert list(om.occupancy_stats()) == list(FIX["occ_counts"])
+    c, sc, cnt, mean, _, _ = om.download_occupancy()
+    coords, scales, ci, osum, _ = _occ_arrays(c, sc, mean)
+    assert np.array_equal(coords, FIX["occ_coords"]) and np.array_equal(scales, FIX["occ_scales"])
+    assert np.array_equal(ci, FIX["occ_crc_int"])
+    assert np.max(np.abs(osum - FIX["occ_sum"])) <= 1e-3
