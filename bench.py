@@ -83,23 +83,29 @@ class Clocks:
         self.proc = None
 
     def start(self):
+        """Start polling every 20 ms and return once the first sample is in, so that the timed
+        region that follows is covered (nvidia-smi takes ~0.1 s to start)."""
+        self.first = ""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.first = self.proc.stdout.readline()
         except OSError:
             self.proc = None
 
     def stop(self):
         if self.proc is None:
             return None
+        time.sleep(0.05)  # one more sample after the timed region's last step
         self.proc.terminate()
         try:
             out, _ = self.proc.communicate(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
             out, _ = self.proc.communicate()
+        out = self.first + out
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in out.splitlines():
