@@ -235,10 +235,21 @@ SE_GPU_API se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinh
  * se_gpu_mc_case_table) instead of the reference's third-party table, so a pattern's triangles
  * can differ from the reference's while the surface and its vertices do not. Faces point away
  * from the inside. Writes up to capacity faces (any order) to faces_dev and the total to
- * *count (call again with a larger buffer when *count > capacity). Synchronous. Multi-res and
- * occupancy maps: SE_GPU_ERR_NOT_SUPPORTED (the reference's dual marching cubes is not built). */
+ * *count (call again with a larger buffer when *count > capacity). Synchronous. Multi-res TSDF
+ * and occupancy maps: se_gpu_dual_marching_cube with min_desired_scale 0, without the scales. */
 SE_GPU_API se_gpu_status se_gpu_marching_cube(se_gpu_map* map, float* faces_dev, int64_t capacity,
                                               int64_t* count, void* stream);
+/* Replaces se::algorithms::marching_cube(octree, min_desired_scale) for multi-res TSDF and
+ * occupancy maps (dual_marching_cube_kernel, marching_cube_impl.hpp:895-975): each block is
+ * meshed on its dual grid at clamp(min_desired_scale, current_scale, 3), across block faces at
+ * the coarser of the two blocks' scales (gather_dual_data :683-758); inside = tsdf < 0, or
+ * occupancy * weight > 0 (faces point away from occupied space). faces_dev as for
+ * se_gpu_marching_cube (may be NULL to count); scales_dev (may be NULL) receives each face's
+ * scale (Face::scale). min_desired_scale in [0, 3]. Single-res maps: SE_GPU_ERR_NOT_SUPPORTED.
+ * Synchronous. */
+SE_GPU_API se_gpu_status se_gpu_dual_marching_cube(se_gpu_map* map, int min_desired_scale,
+                                                   float* faces_dev, int8_t* scales_dev,
+                                                   int64_t capacity, int64_t* count, void* stream);
 /* The case table: ntri[c] faces for case c (bit i = corner i inside, corners (0,0,0), (1,0,0),
  * (1,0,1), (0,0,1), (0,1,0), (1,1,0), (1,1,1), (0,1,1)), tri[15 c + 3 f + j] the edge (as
  * meshing::edge_to_corners) of vertex j of face f, -1 padded. Host only. Rule: crossed edges of a
@@ -248,19 +259,22 @@ SE_GPU_API se_gpu_status se_gpu_marching_cube(se_gpu_map* map, float* faces_dev,
 SE_GPU_API se_gpu_status se_gpu_mc_case_table(int32_t ntri[256], int32_t tri[256 * 15]);
 
 /* ------------------------------------------------------------------------------- IO -- */
-/* The reference's on-disk outputs (include/se/map/io/*), written by this library's own host code
+/* The reference's on-disk outputs (the headers of include/se/map/io), written by this library's own host code
  * in the same standard ASCII formats. io::save_mesh (mesh_io_impl.hpp): faces (host, 9 floats
- * each) transformed by T_OV (row-major 4x4 affine), format by extension: .ply, .vtk (polydata
- * with a per-face scale), .obj. */
-SE_GPU_API se_gpu_status se_gpu_save_mesh(const float* faces, int64_t n, const float T_OV[16],
-                                          const char* filename);
+ * each) transformed by T_OV (row-major 4x4 affine), format by extension: .ply (faces coloured
+ * by scale), .vtk (polydata with a per-face scale and scale colour), .obj; scales (host, one per
+ * face) may be NULL for scale 0. */
+SE_GPU_API se_gpu_status se_gpu_save_mesh(const float* faces, const int8_t* scales, int64_t n,
+                                          const float T_OV[16], const char* filename);
 /* Map::mesh's transform T_OV = T_OW * T_WM * Scaling(res) (map_impl.hpp:454-459). */
 SE_GPU_API se_gpu_status se_gpu_map_mesh_transform(const se_gpu_map* map, const float T_OW[16],
                                                    float T_OV[16]);
-/* Map::saveMesh(filename, T_OW) (map_impl.hpp:464-469) for single-res TSDF maps: marching cubes
- * on the GPU, then se_gpu_save_mesh. Synchronous. */
+/* Map::saveMesh(filename, T_OW, min_desired_scale) (map_impl.hpp:464-469): marching cubes on the
+ * GPU (dual for multi-res and occupancy maps, which take min_desired_scale), then
+ * se_gpu_save_mesh. Synchronous. */
 SE_GPU_API se_gpu_status se_gpu_map_save_mesh(se_gpu_map* map, const float T_OW[16],
-                                              const char* filename, void* stream);
+                                              int min_desired_scale, const char* filename,
+                                              void* stream);
 /* io::save_point_cloud_vtk (point_cloud_io_impl.hpp): n points (host, xyz) transformed by T_WC. */
 SE_GPU_API se_gpu_status se_gpu_save_point_cloud_vtk(const float* points, int64_t n,
                                                      const float T_WC[16], const char* filename);

@@ -128,6 +128,11 @@ def lib():
             "so_exp_cw": (C.c_float, [C.c_float]),
             "so_marching_cubes": (C.c_longlong, [vp, vp, C.c_longlong]),
             "so_mc_table": (None, [i32p, i32p]),
+            "so_dual_marching_cubes": (C.c_longlong, [vp, C.c_int, vp, vp, C.c_longlong]),
+            "so_occ_dual_marching_cubes": (C.c_longlong, [vp, C.c_int, vp, vp, C.c_longlong]),
+            "so_dual_groups": (None, [i32p, i32p, i32p, i32p]),
+            "so_map_set_mr_block": (None, [vp, i32p, f32p, f32p, C.c_int, C.c_int]),
+            "so_occ_set_block": (None, [vp, i32p, C.c_int, C.c_int, f32p]),
             "so_downsample_depth": (None, [f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, vp]),
             "so_point_cloud_to_normal": (None, [f32p, C.c_int, C.c_int, C.c_int, f32p]),
         }
@@ -250,6 +255,15 @@ class OracleOccMap:
         mn = np.zeros(3, np.int32)
         mx = np.zeros(3, np.int32)
         return (mn, mx) if lib().so_occ_aabb(self.h, mn, mx) else None
+
+    def set_block(self, coord, current_scale, min_scale, mean):
+        """Test set-up: the block at voxel coord with its scales and mean pyramid f32[585, 3]."""
+        lib().so_occ_set_block(self.h, np.asarray(coord, np.int32), int(current_scale), int(min_scale),
+                               np.ascontiguousarray(mean, np.float32).reshape(-1))
+
+    def dual_marching_cubes(self, min_desired_scale=0):
+        """(faces [N, 3, 3] float32 in voxel units, scales [N] int8) between occupied and free."""
+        return _dual_mc(lib().so_occ_dual_marching_cubes, self.h, min_desired_scale)
 
 
 def occ_depth_sigma(depth, res):
@@ -403,6 +417,15 @@ class OracleMap:
             lib().so_marching_cubes(self.h, f.ctypes.data, n)
         return f
 
+    def set_mr_block(self, coord, tsdf, weight, current_scale, min_scale):
+        """Test set-up of a multi-res block: data pyramid f32[585] x 2 and its scales."""
+        lib().so_map_set_mr_block(self.h, np.asarray(coord, np.int32), np.ascontiguousarray(tsdf, np.float32),
+                                  np.ascontiguousarray(weight, np.float32), int(current_scale), int(min_scale))
+
+    def dual_marching_cubes(self, min_desired_scale=0):
+        """Multi-res maps: (faces [N, 3, 3] float32 in voxel units, scales [N] int8)."""
+        return _dual_mc(lib().so_dual_marching_cubes, self.h, min_desired_scale)
+
     def aabb(self):
         mn = np.zeros(3, np.int32)
         mx = np.zeros(3, np.int32)
@@ -444,6 +467,27 @@ def bilateral_filter(depth, radius=2, sigma_space=4.0, sigma_range=0.03):
     lib().so_bilateral_filter(depth.reshape(-1), w, h, int(radius), float(sigma_space), float(sigma_range),
                               out.reshape(-1))
     return out
+
+
+def _dual_mc(fn, h, min_desired_scale):
+    n = int(fn(h, int(min_desired_scale), None, None, 0))
+    if n < 0:
+        raise ValueError("dual marching cubes needs a multi-res map")
+    f = np.zeros((n, 3, 3), np.float32)
+    sc = np.zeros(n, np.int8)
+    if n:
+        fn(h, int(min_desired_scale), f.ctypes.data, sc.ctypes.data, n)
+    return f, sc
+
+
+def dual_groups(rel):
+    """The partition of a block-relative primal corner's 8 dual corners: (group_of[8], above[n])."""
+    r = np.asarray(rel, np.int32)
+    g = np.zeros(8, np.int32)
+    a = np.zeros(8, np.int32)
+    n = np.zeros(1, np.int32)
+    lib().so_dual_groups(r, g, a, n)
+    return g, a[:int(n[0])]
 
 
 def mc_table():

@@ -34,6 +34,7 @@
 #endif
 
 #include "oracle_common.hpp"
+#include "oracle_dual_mc.hpp"
 
 
 /* --------------------------------------------------------------------------------- map -- */
@@ -1970,6 +1971,65 @@ long long so_marching_cubes(const so_map* mp, float* faces, long long capacity)
     return n;
 }
 
+namespace {
+
+/* A multi-res TSDF map seen by the dual marching cubes: BlockMultiRes<TSDF>::data(voxel, scale)
+ * (block_impl.hpp:164-170) reads the pyramid at any scale; get_field = tsdf (data.hpp:117-121),
+ * is_valid = weight != 0 (data_field_impl.hpp:32-35), is_inside = tsdf < 0 (data.hpp:133-137). */
+struct MrTsdfView {
+    const Octree& o;
+    int size() const { return o.size; }
+    int num_blocks() const { return (int) o.mr.size(); }
+    bool live(int) const { return true; }
+    const int32_t* coord(int b) const { return o.octants[(size_t) o.block_octant[(size_t) b]].coord; }
+    int current_scale(int b) const { return o.mr[(size_t) b].current_scale; }
+    int block_at(const int32_t c[3]) const
+    {
+        const int oc = o.block_at(c);
+        return oc < 0 ? -1 : o.octants[(size_t) oc].block;
+    }
+    bool data(int b, const int32_t c[3], int scale, float& field) const
+    {
+        const MRBlock& B = o.mr[(size_t) b];
+        const int32_t* bc = coord(b);
+        const int n = kBlockSize >> scale;
+        const int i = kMrScaleOffset[scale] + (c[0] - bc[0]) / (1 << scale) + n * ((c[1] - bc[1]) / (1 << scale))
+            + n * n * ((c[2] - bc[2]) / (1 << scale));
+        field = B.tsdf[i];
+        return B.weight[i] != 0.0f;
+    }
+    bool inside(float field) const { return field < 0.0f; }
+};
+
+} // namespace
+
+/* Dual marching cubes of a multi-res TSDF map (algorithms::marching_cube for Res::Multi,
+ * marching_cube_impl.hpp:895-975, 1175-1201): faces (9 floats each, voxel units) and the
+ * integration scale of each face; returns the face count (faces and scales may be NULL). */
+long long so_dual_marching_cubes(const so_map* map, int min_desired_scale, float* faces, int8_t* scales,
+                                 long long capacity)
+{
+    if (!map->octree.multires)
+        return -1;
+    std::vector<int32_t> ntri(256), tri(256 * 3 * kMcMaxTri);
+    so_mc_table(ntri.data(), tri.data());
+    return dual_mc::dual_marching_cubes(MrTsdfView{map->octree}, min_desired_scale, ntri.data(), tri.data(),
+                                        3 * kMcMaxTri, faces, scales, capacity);
+}
+
+/* The dual-corner partition of a primal corner at block-relative coordinate rel (each in
+ * [0, 8]): group_of[i] (0 = inside the block), above[g] (1 above, 0 below, -1 inside group). */
+void so_dual_groups(const int32_t rel[3], int32_t group_of[8], int32_t above[8], int32_t* n_groups)
+{
+    const int r[3] = {rel[0], rel[1], rel[2]};
+    const dual_mc::Groups g = dual_mc::dual_groups(r, kBlockSize);
+    for (int i = 0; i < 8; ++i) {
+        group_of[i] = g.group_of[i];
+        above[i] = i < g.n_groups ? g.above[i] : -1;
+    }
+    *n_groups = g.n_groups;
+}
+
 int so_map_aabb(const so_map* map, int32_t mn[3], int32_t mx[3])
 {
     const Octree& oct = map->octree;
@@ -1993,6 +2053,29 @@ void so_map_set_block(so_map* map, const int32_t c[3], const float* tsdf512, con
         std::memcpy(b.tsdf, tsdf512, sizeof(float) * kBlockVoxels);
     if (weight512)
         std::memcpy(b.weight, weight512, sizeof(float) * kBlockVoxels);
+}
+
+/* Test set-up of a multi-res map: allocates the block holding voxel c and sets its data
+ * pyramid (585 entries each, NULL keeps the default), its past data to the same values, and its
+ * current and minimum scales. */
+void so_map_set_mr_block(so_map* map, const int32_t c[3], const float* tsdf585, const float* weight585,
+                         int current_scale, int min_scale)
+{
+    if (!map->octree.multires)
+        return;
+    int o;
+    map->octree.allocate_key(encode_key(c[0], c[1], c[2], 0), o);
+    MRBlock& b = map->octree.mr[(size_t) map->octree.octants[(size_t) o].block];
+    if (tsdf585) {
+        std::memcpy(b.tsdf, tsdf585, sizeof(float) * kMrVoxels);
+        std::memcpy(b.past_tsdf, tsdf585, sizeof(float) * kMrVoxels);
+    }
+    if (weight585) {
+        std::memcpy(b.weight, weight585, sizeof(float) * kMrVoxels);
+        std::memcpy(b.past_weight, weight585, sizeof(float) * kMrVoxels);
+    }
+    b.current_scale = current_scale;
+    b.min_scale = min_scale;
 }
 
 int so_map_get_data(const so_map* map, const float p[3], float* tsdf, float* weight)

@@ -120,6 +120,9 @@ void so_map_mr_blocks(const so_map* map, uint64_t* keys, int32_t* coords, float*
 int so_map_aabb(const so_map* map, int32_t mn[3], int32_t mx[3]);
 /* Allocate the block containing voxel_coord (through the normal allocator) and overwrite its
  * 512 voxels. */
+/* Test set-up of a multi-res map block: data pyramid (585 entries, past data set equal), scales. */
+void so_map_set_mr_block(so_map* map, const int32_t voxel_coord[3], const float* tsdf585,
+                         const float* weight585, int current_scale, int min_scale);
 void so_map_set_block(so_map* map, const int32_t voxel_coord[3], const float* tsdf512,
                       const float* weight512);
 int so_map_get_data(const so_map* map, const float point_W[3], float* tsdf, float* weight);
@@ -168,6 +171,12 @@ void so_occ_integrate_depth(so_occ_map* map, const float* depth, const so_pinhol
                             const float T_WC[16], int timestamp, so_occ_stats* stats);
 long long so_occ_num_blocks(const so_occ_map* map);
 long long so_occ_num_nodes(const so_occ_map* map);
+/* Test set-up: the block holding voxel c with the given scales and mean pyramid (585 x 3). */
+void so_occ_set_block(so_occ_map* map, const int32_t c[3], int current_scale, int min_scale,
+                      const float* mean585);
+/* Dual marching cubes of an occupancy map: faces (9 floats each, voxel units) and face scales. */
+long long so_occ_dual_marching_cubes(const so_occ_map* map, int min_desired_scale, float* faces,
+                                     int8_t* scales, long long capacity);
 /* Live blocks in allocation order; every pointer may be NULL. coords: 3 ints; scales:
  * (current, min, buffer); counts: (curr_integr, curr_observed, buffer_integr,
  * buffer_observed); mean / min / max: 585 entries of (occupancy, weight, observed). */
@@ -244,6 +253,12 @@ void so_downsample_depth(const float* in, int w_in, int h_in, float* out, int w_
  * the case table it triangulates with (ntri[256], tri[256 * 24], -1 padded). */
 long long so_marching_cubes(const so_map* map, float* faces, long long capacity);
 void so_mc_table(int32_t* ntri, int32_t* tri);
+/* Dual marching cubes of a multi-res TSDF map: faces (9 floats each, voxel units) and the scale
+ * of each face; returns the face count (-1 for a single-res map). */
+long long so_dual_marching_cubes(const so_map* map, int min_desired_scale, float* faces, int8_t* scales,
+                                 long long capacity);
+/* The partition of the 8 dual corners of a block-relative primal corner into blocks. */
+void so_dual_groups(const int32_t rel[3], int32_t group_of[8], int32_t above[8], int32_t* n_groups);
 
 /* Preprocessing helpers exposed for tests. */
 void so_half_sample_robust(const float* in, int w, int h, float e_d, int radius, float* out);

@@ -38,6 +38,7 @@
 #endif
 
 #include "oracle_common.hpp"
+#include "oracle_dual_mc.hpp"
 
 namespace {
 
@@ -1862,6 +1863,36 @@ static int raycast_occ(const so_occ_map& m, V3 o, V3 d, float t_far, V3& hit, in
 
 /* ------------------------------------------------------------------------ C API -- */
 
+namespace {
+
+/* An occupancy map seen by the dual marching cubes: BlockMultiRes<Occupancy>::data(voxel, scale)
+ * (block_impl.hpp:326-340: the init data below the finest allocated scale), get_field =
+ * occupancy * weight (data.hpp:123-127), is_valid = weight != 0 (data_field_impl.hpp:12-15),
+ * is_inside = field > 0 (data.hpp:139-143); fetcher::block by descent from the root. */
+struct OccView {
+    const OccOctree& o;
+    int size() const { return o.size; }
+    int num_blocks() const { return (int) o.blocks.size(); }
+    bool live(int b) const { return o.block_live[(size_t) b] != 0; }
+    const int32_t* coord(int b) const { return o.blocks[(size_t) b].coord; }
+    int current_scale(int b) const { return o.blocks[(size_t) b].current_scale; }
+    int block_at(const int32_t c[3]) const
+    {
+        const int s = o.leaf(c);
+        return (s != -1 && slot_is_block(s)) ? slot_block(s) : -1;
+    }
+    bool data(int b, const int32_t c[3], int scale, float& field) const
+    {
+        const OccBlock& B = o.blocks[(size_t) b];
+        const OccData& d = scale < B.finest ? B.init_data : B.mean[kOccScaleOffset[scale] + B.voxel_idx(c, scale)];
+        field = occ_field(d);
+        return occ_valid(d);
+    }
+    bool inside(float field) const { return field > 0.0f; }
+};
+
+} // namespace
+
 extern "C" {
 
 so_occ_map* so_occ_map_create(const float dim[3], float res, const float* T_MW)
@@ -2083,6 +2114,48 @@ long long so_occ_num_blocks(const so_occ_map* m)
 }
 
 long long so_occ_num_nodes(const so_occ_map* m) { return (long long) m->octree.nodes.size(); }
+
+/* Test set-up: allocates the path to the block holding voxel c (Octree::allocateChildren at
+ * every level, as integration does) and sets the block's current and minimum scale and its mean
+ * pyramid (585 x (occupancy, weight, observed)), the finest scale taken as 0. */
+void so_occ_set_block(so_occ_map* mp, const int32_t c[3], int current_scale, int min_scale, const float* mean585)
+{
+    OccOctree& o = mp->octree;
+    int n = 0;
+    int slot = -1;
+    for (int cs = o.size >> 1; cs >= 8; cs >>= 1) {
+        const int idx = ((c[0] & cs) > 0) + 2 * ((c[1] & cs) > 0) + 4 * ((c[2] & cs) > 0);
+        if (o.nodes[(size_t) n].child[idx] == -1)
+            o.allocate_children(n);
+        slot = o.nodes[(size_t) n].child[idx];
+        if (slot_is_block(slot))
+            break;
+        n = slot;
+    }
+    if (slot == -1 || !slot_is_block(slot))
+        return;
+    OccBlock& b = o.blocks[(size_t) slot_block(slot)];
+    for (int i = 0; i < 585; ++i) {
+        b.mean[i].occ = mean585[3 * i];
+        b.mean[i].weight = mean585[3 * i + 1];
+        b.mean[i].observed = mean585[3 * i + 2] != 0.0f;
+    }
+    b.finest = 0;
+    b.current_scale = current_scale;
+    b.min_scale = min_scale;
+}
+
+/* Dual marching cubes of an occupancy map (algorithms::marching_cube for Res::Multi,
+ * marching_cube_impl.hpp:895-975, 1175-1201): faces (9 floats each, voxel units) between
+ * occupied and free space and the integration scale of each face; returns the face count. */
+long long so_occ_dual_marching_cubes(const so_occ_map* m, int min_desired_scale, float* faces, int8_t* scales,
+                                     long long capacity)
+{
+    std::vector<int32_t> ntri(256), tri(256 * 24);
+    so_mc_table(ntri.data(), tri.data());
+    return dual_mc::dual_marching_cubes(OccView{m->octree}, min_desired_scale, ntri.data(), tri.data(), 24, faces,
+                                        scales, capacity);
+}
 
 /* Live blocks in allocation order: coords (3), scales (current, min, buffer), counters
  * (curr_integr, curr_obs, buffer_integr, buffer_obs), init data, and the 585-entry mean / min /

@@ -25,6 +25,7 @@ from . import build as _build
 __all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "OusterLidar",
            "OccupancyBatch", "raycast_volume",
            "render_depth", "raycast_adjoint", "track_noalloc", "bilateral_filter", "downsample_depth", "marching_cube",
+           "dual_marching_cube", "save_mesh",
            "FramePipeline", "SeGpuError", "library", "library_path"]
 
 
@@ -103,10 +104,11 @@ SIGNATURES = {
     "se_gpu_bilateral_filter": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.POINTER(_BilateralConfig), _VP]),
     "se_gpu_tracker_set_persistent": (C.c_int, [_VP, C.c_int]),
     "se_gpu_marching_cube": (C.c_int, [_VP, _VP, C.c_int64, C.POINTER(C.c_int64), _VP]),
+    "se_gpu_dual_marching_cube": (C.c_int, [_VP, C.c_int, _VP, _VP, C.c_int64, C.POINTER(C.c_int64), _VP]),
     "se_gpu_mc_case_table": (C.c_int, [_VP, _VP]),
-    "se_gpu_save_mesh": (C.c_int, [_VP, C.c_int64, _F16, C.c_char_p]),
+    "se_gpu_save_mesh": (C.c_int, [_VP, _VP, C.c_int64, _F16, C.c_char_p]),
     "se_gpu_map_mesh_transform": (C.c_int, [_VP, _F16, _F16]),
-    "se_gpu_map_save_mesh": (C.c_int, [_VP, _F16, C.c_char_p, _VP]),
+    "se_gpu_map_save_mesh": (C.c_int, [_VP, _F16, C.c_int, C.c_char_p, _VP]),
     "se_gpu_save_point_cloud_vtk": (C.c_int, [_VP, C.c_int64, _F16, C.c_char_p]),
     "se_gpu_map_field_box": (C.c_int, [_VP, _VP, _VP, _VP]),
     "se_gpu_map_save_field_slices": (C.c_int, [_VP, C.c_char_p, C.c_char_p, C.c_char_p, _F16]),
@@ -428,11 +430,12 @@ class Map:
         _check(self._L.se_gpu_map_mesh_transform(self.h, tw, out.ctypes.data_as(_F16)), "se_gpu_map_mesh_transform")
         return out.reshape(4, 4)
 
-    def saveMesh(self, filename, T_OW=None, stream=None):
-        """Map::saveMesh: marching cubes written as .ply / .vtk / .obj in the T_OW frame."""
+    def saveMesh(self, filename, T_OW=None, min_desired_scale=0, stream=None):
+        """Map::saveMesh: marching cubes (dual for multi-res and occupancy maps, at
+        min_desired_scale or coarser) written as .ply / .vtk / .obj in the T_OW frame."""
         _, tw = _m16(np.eye(4) if T_OW is None else T_OW)
-        _check(self._L.se_gpu_map_save_mesh(self.h, tw, str(filename).encode(), _stream(stream)),
-               "se_gpu_map_save_mesh")
+        _check(self._L.se_gpu_map_save_mesh(self.h, tw, int(min_desired_scale), str(filename).encode(),
+                                            _stream(stream)), "se_gpu_map_save_mesh")
 
     def saveFieldSlices(self, filename_x, filename_y, filename_z, point_W):
         """Map::saveFieldSlices: VTK rectilinear slices of the field through point_W's voxel."""
@@ -675,8 +678,9 @@ def track_noalloc(sensor: PinholeCamera, config: TrackerConfig, depth, T_WS,
 
 
 def marching_cube(map: Map, stream=None):
-    """se::algorithms::marching_cube(octree) for a single-res TSDF map: faces [N, 3, 3] (float32
-    CUDA tensor, vertices in voxel units of the map frame; world = T_WM (res v))."""
+    """se::algorithms::marching_cube(octree): faces [N, 3, 3] (float32 CUDA tensor, vertices in
+    voxel units of the map frame; world = T_WM (res v)); multi-res and occupancy maps are meshed
+    by the dual marching cubes at their blocks' current scales."""
     import torch
     L = library()
     n = C.c_int64()
@@ -688,12 +692,35 @@ def marching_cube(map: Map, stream=None):
     return out[: n.value]
 
 
-def save_mesh(faces, filename, T_OV=None):
+def dual_marching_cube(map: Map, min_desired_scale=0, stream=None):
+    """se::algorithms::marching_cube(octree, min_desired_scale) for a multi-res TSDF or occupancy
+    map: (faces [N, 3, 3] float32, scales [N] int8), CUDA tensors."""
+    import torch
+    L = library()
+    n = C.c_int64()
+    _check(L.se_gpu_dual_marching_cube(map.h, int(min_desired_scale), None, None, 0, C.byref(n), _stream(stream)),
+           "se_gpu_dual_marching_cube")
+    out = torch.empty((max(n.value, 1), 3, 3), dtype=torch.float32, device="cuda")
+    sc = torch.empty(max(n.value, 1), dtype=torch.int8, device="cuda")
+    cap = n.value
+    _check(L.se_gpu_dual_marching_cube(map.h, int(min_desired_scale), C.c_void_p(out.data_ptr()),
+                                       C.c_void_p(sc.data_ptr()), cap, C.byref(n), _stream(stream)),
+           "se_gpu_dual_marching_cube")
+    return out[: n.value], sc[: n.value]
+
+
+def save_mesh(faces, filename, T_OV=None, scales=None):
     """io::save_mesh: faces [N, 3, 3] (numpy or tensor) transformed by T_OV (4x4, default the
-    identity), written as .ply, .vtk or .obj."""
+    identity), written as .ply, .vtk or .obj; scales [N] (default 0) colour the faces."""
     f = np.ascontiguousarray(faces.cpu().numpy() if hasattr(faces, "cpu") else faces, np.float32).reshape(-1, 9)
+    sc = None
+    if scales is not None:
+        sc = np.ascontiguousarray(scales.cpu().numpy() if hasattr(scales, "cpu") else scales, np.int8).reshape(-1)
+        if len(sc) != len(f):
+            raise SeGpuError("save_mesh: one scale per face")
     _, tp = _m16(np.eye(4) if T_OV is None else T_OV)
-    _check(library().se_gpu_save_mesh(f.ctypes.data, len(f), tp, str(filename).encode()), "se_gpu_save_mesh")
+    _check(library().se_gpu_save_mesh(f.ctypes.data, None if sc is None else sc.ctypes.data, len(f), tp,
+                                      str(filename).encode()), "se_gpu_save_mesh")
 
 
 def save_point_cloud_vtk(points, filename, T_WC=None):

@@ -40,7 +40,8 @@ struct File {
     }
 };
 
-// A face colour per integration scale (single-res meshes are all scale 0).
+// A face colour per integration scale (single-res meshes are all scale 0; io::save_mesh colours
+// faces by scale_colour(face.scale), mesh_io_impl.hpp).
 void scale_rgb(int scale, int rgb[3])
 {
     static const int palette[8][3] = {{102, 194, 165}, {252, 141, 98}, {141, 160, 203}, {231, 138, 195},
@@ -51,7 +52,7 @@ void scale_rgb(int scale, int rgb[3])
     rgb[2] = c[2];
 }
 
-se_gpu_status write_mesh(const float* faces, int64_t n, const float* T, const std::string& path)
+se_gpu_status write_mesh(const float* faces, const int8_t* scales, int64_t n, const float* T, const std::string& path)
 {
     File out(path.c_str());
     if (!out.f) {
@@ -62,8 +63,8 @@ se_gpu_status write_mesh(const float* faces, int64_t n, const float* T, const st
     std::vector<float> v((size_t) n * 9);
     for (int64_t i = 0; i < 3 * n; ++i)
         apply16(T, faces + 3 * i, v.data() + 3 * i);
+    const auto face_scale = [scales](int64_t i) { return scales ? (int) scales[i] : 0; };
     int rgb[3];
-    scale_rgb(0, rgb);
     if (ends_with(path, ".ply")) {
         std::fprintf(f, "ply\nformat ascii 1.0\ncomment supereight2_gb300 mesh\n");
         std::fprintf(f, "element vertex %lld\nproperty float x\nproperty float y\nproperty float z\n", (long long) (3 * n));
@@ -71,9 +72,11 @@ se_gpu_status write_mesh(const float* faces, int64_t n, const float* T, const st
         std::fprintf(f, "property uchar red\nproperty uchar green\nproperty uchar blue\nend_header\n");
         for (int64_t i = 0; i < 3 * n; ++i)
             std::fprintf(f, "%.9g %.9g %.9g\n", v[3 * i], v[3 * i + 1], v[3 * i + 2]);
-        for (int64_t i = 0; i < n; ++i)
+        for (int64_t i = 0; i < n; ++i) {
+            scale_rgb(face_scale(i), rgb);
             std::fprintf(f, "3 %lld %lld %lld %d %d %d\n", (long long) (3 * i), (long long) (3 * i + 1),
                          (long long) (3 * i + 2), rgb[0], rgb[1], rgb[2]);
+        }
     }
     else if (ends_with(path, ".vtk")) {
         std::fprintf(f, "# vtk DataFile Version 3.0\nsupereight2_gb300 mesh\nASCII\nDATASET POLYDATA\n\n");
@@ -85,7 +88,12 @@ se_gpu_status write_mesh(const float* faces, int64_t n, const float* T, const st
             std::fprintf(f, "3 %lld %lld %lld\n", (long long) (3 * i), (long long) (3 * i + 1), (long long) (3 * i + 2));
         std::fprintf(f, "\nCELL_DATA %lld\nSCALARS scale unsigned_char\nLOOKUP_TABLE default\n", (long long) n);
         for (int64_t i = 0; i < n; ++i)
-            std::fprintf(f, "0\n");
+            std::fprintf(f, "%d\n", face_scale(i));
+        std::fprintf(f, "COLOR_SCALARS scale_colour 3\n");
+        for (int64_t i = 0; i < n; ++i) {
+            scale_rgb(face_scale(i), rgb);
+            std::fprintf(f, "%.9g %.9g %.9g\n", rgb[0] / 255.0f, rgb[1] / 255.0f, rgb[2] / 255.0f);
+        }
     }
     else if (ends_with(path, ".obj")) {
         std::fprintf(f, "# supereight2_gb300 mesh\n");
@@ -125,13 +133,14 @@ using namespace se_gpu;
 
 extern "C" {
 
-se_gpu_status se_gpu_save_mesh(const float* faces, int64_t n, const float T_OV[16], const char* filename)
+se_gpu_status se_gpu_save_mesh(const float* faces, const int8_t* scales, int64_t n, const float T_OV[16],
+                               const char* filename)
 {
     if ((!faces && n > 0) || n < 0 || !T_OV || !filename) {
         set_last_error("se_gpu_save_mesh: invalid argument");
         return SE_GPU_ERR_BAD_ARG;
     }
-    return write_mesh(faces, n, T_OV, filename);
+    return write_mesh(faces, scales, n, T_OV, filename);
 }
 
 se_gpu_status se_gpu_map_mesh_transform(const se_gpu_map* map, const float T_OW[16], float T_OV[16])
@@ -158,23 +167,33 @@ se_gpu_status se_gpu_map_mesh_transform(const se_gpu_map* map, const float T_OW[
     return SE_GPU_OK;
 }
 
-se_gpu_status se_gpu_map_save_mesh(se_gpu_map* map, const float T_OW[16], const char* filename, void* stream)
+se_gpu_status se_gpu_map_save_mesh(se_gpu_map* map, const float T_OW[16], int min_desired_scale, const char* filename,
+                                   void* stream)
 {
     if (!map || !T_OW || !filename) {
         set_last_error("se_gpu_map_save_mesh: invalid argument");
         return SE_GPU_ERR_BAD_ARG;
     }
+    const bool dual = map->occ || map->dev.res_type == SE_GPU_RES_MULTI;
+    const auto extract = [&](float* f, int8_t* sc, int64_t cap, int64_t* cnt) {
+        return dual ? se_gpu_dual_marching_cube(map, min_desired_scale, f, sc, cap, cnt, stream)
+                    : se_gpu_marching_cube(map, f, cap, cnt, stream);
+    };
     int64_t n = 0;
-    se_gpu_status st = se_gpu_marching_cube(map, nullptr, 0, &n, stream);
+    se_gpu_status st = extract(nullptr, nullptr, 0, &n);
     if (st != SE_GPU_OK)
         return st;
-    float* d = nullptr;
     std::vector<float> h((size_t) n * 9);
+    std::vector<int8_t> hs(dual ? (size_t) n : 0);
     if (n > 0) {
-        SE_CUDA_TRY(cudaMalloc(&d, (size_t) n * 9 * sizeof(float)));
+        float* d = nullptr;
+        int8_t* ds = nullptr;
+        SE_CUDA_TRY(cudaMalloc(&d, (size_t) n * 9 * sizeof(float) + (size_t) n));
+        ds = reinterpret_cast<int8_t*>(d + (size_t) n * 9);
         int64_t n2 = 0;
-        st = se_gpu_marching_cube(map, d, n, &n2, stream);
-        if (st == SE_GPU_OK && cudaMemcpy(h.data(), d, h.size() * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+        st = extract(d, dual ? ds : nullptr, n, &n2);
+        if (st == SE_GPU_OK && (cudaMemcpy(h.data(), d, h.size() * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess
+                                || (dual && cudaMemcpy(hs.data(), ds, hs.size(), cudaMemcpyDeviceToHost) != cudaSuccess)))
             st = cuda_status(cudaGetLastError(), "cudaMemcpy(mesh)");
         cudaFree(d);
         if (st != SE_GPU_OK)
@@ -182,7 +201,7 @@ se_gpu_status se_gpu_map_save_mesh(se_gpu_map* map, const float T_OW[16], const 
     }
     float T_OV[16];
     se_gpu_map_mesh_transform(map, T_OW, T_OV);
-    return write_mesh(h.data(), n, T_OV, filename);
+    return write_mesh(h.data(), dual ? hs.data() : nullptr, n, T_OV, filename);
 }
 
 se_gpu_status se_gpu_save_point_cloud_vtk(const float* points, int64_t n, const float T_WC[16], const char* filename)

@@ -4,7 +4,9 @@ supereight2 sources; not needed to run the tests).
 reference_pins.json — values the reference's own tests assert, extracted from their sources:
   test/map/map/map_unittest.cpp (Map.initialization: dim, res, octree size) and
   test/system/multires_ofusion/multires_ofusion_systemtest.cpp (the voxels its GetField and
-  GetFieldInterpolation tests check, with the expected data).
+  GetFieldInterpolation tests check, with the expected data); and the dual-corner partition
+  that meshing::norm_dual_corner_idxs (include/se/map/algorithms/impl/marching_cube_impl.hpp)
+  tabulates for the 26 block-boundary positions of a primal corner.
 oracle_fixtures.npz — small seeded inputs (stored: five 320x240 depth frames with their poses,
   one 64x1024 LiDAR scan with its pose) and the CPU oracle's outputs on them, as per-block
   CRC32s and raw arrays, so the oracle built on another machine and the GPU path are both
@@ -60,7 +62,31 @@ def reference_pins(src):
     pins["occupancy_unknown"] = [cf[n] for n in sorted(cf) if "unknown" in n]
     pins["occupancy_free"] = [cf[n] for n in sorted(cf) if "free" in n]
     pins["occupancy_free_value"] = float(re.findall(r"EXPECT_FLOAT_EQ\((-?[\d.]+),", field)[0])
+    pins["dual_corner_partition"] = dual_corner_partition(src)
     return pins
+
+
+def dual_corner_partition(src):
+    """meshing::norm_dual_corner_idxs (marching_cube_impl.hpp): for every boundary position of a
+    primal corner (crossmask: upper x, y, z, lower x, y, z bits from high to low) the corners of
+    each neighbouring block (first: the meshed block) and the representative corners of the blocks
+    ranking below and above the meshed block."""
+    txt = open(os.path.join(src, "include/se/map/algorithms/impl/marching_cube_impl.hpp")).read()
+    body = txt[txt.index("switch (crossmask)"):]
+    body = body[: body.index("template<typename OctreeT, typename DataT>")]
+    out = {}
+    for m in re.finditer(r"case (\d+):(.*?)(?=case \d+:|\Z)", body, re.S):
+        code = m.group(2)
+
+        def ints(t):
+            return [int(v) for v in re.findall(r"\d+", t)]
+
+        lower = re.search(r"lower_priority_neighbours = \{([^}]*)\}", code).group(1)
+        higher = re.search(r"higher_priority_neighbours = \{([^}]*)\}", code).group(1)
+        nbrs = re.search(r"(?<!_)neighbours = \{(.*?)\};", code, re.S).group(1)
+        out[m.group(1)] = {"lower": ints(lower), "higher": ints(higher),
+                           "groups": [ints(g) for g in re.findall(r"\{([^{}]*)\}", nbrs)]}
+    return out
 
 
 def oracle_fixtures():

@@ -39,6 +39,26 @@ def test_mesh_formats(tmp_path):
         se.save_mesh(f, tmp_path / "m.stl", T)
 
 
+def test_mesh_face_scales(tmp_path):
+    """Multi-res meshes carry a scale per face: the VTK cell data lists it, the PLY face colour
+    follows it (io::save_mesh's scale_colour)."""
+    se = pytest.importorskip("supereight2_gb300")
+    f, T = _faces(), _T()
+    sc = np.array([0, 1, 2, 3, 1, 0, 2], np.int8)
+    se.save_mesh(f, tmp_path / "s.vtk", T, scales=sc)
+    lines = (tmp_path / "s.vtk").read_text().splitlines()
+    i = lines.index("SCALARS scale unsigned_char")
+    assert [int(v) for v in lines[i + 2: i + 9]] == sc.tolist()
+    assert "COLOR_SCALARS scale_colour 3" in lines
+    se.save_mesh(f, tmp_path / "s.ply", T, scales=sc)
+    body = (tmp_path / "s.ply").read_text().splitlines()
+    faces = body[-7:]
+    rgb = [tuple(l.split()[4:]) for l in faces]
+    assert rgb[0] == rgb[5] and rgb[1] == rgb[4] and rgb[2] == rgb[6] and len(set(rgb)) == 4
+    with pytest.raises(se.SeGpuError):
+        se.save_mesh(f, tmp_path / "s.vtk", T, scales=sc[:3])
+
+
 def test_point_cloud_vtk(tmp_path):
     se = pytest.importorskip("supereight2_gb300")
     p = np.arange(30, dtype=np.float32).reshape(10, 3)
