@@ -5,11 +5,12 @@
 //   - every thread evaluates trackKernel for a strided set of pixels (icp_impl.hpp:16-102) and
 //     accumulates the 32 reduction values of newReduce (icp.cpp:45-184) in FP32 with two-sum
 //     compensation (hi, lo pairs);
-//   - warp shuffles, then shared memory, give one compensated partial per CTA;
-//   - the last CTA to finish (atomic ticket, no waiting) adds the partials in FP64 in a fixed
-//     order, solves the 6x6 normal equations with an FP64 LDLT, applies the FP64 se(3)
-//     exponential and composes the pose in FP64 (icp.cpp:15-41,208-223,
-//     math_util_impl.hpp:117-174), and raises the level's convergence flag when |x| < threshold.
+//   - shared memory gives one compensated partial per CTA, which the CTA adds exactly (integer
+//     fixed point, order-independent) into global accumulators;
+//   - the last CTA to finish (atomic ticket, no waiting) reads the totals, solves the 6x6 normal
+//     equations by FP64 elimination, applies the FP64 se(3) exponential and composes the pose in
+//     FP64 (icp.cpp:15-41,208-223, math_util_impl.hpp:117-174), and raises the level's
+//     convergence flag when |x| < threshold.
 // Later iterations of a converged level return at entry, so the launch sequence is fixed and
 // can be captured in a CUDA graph. checkPoseKernel (icp.cpp:227-246) runs in a final kernel.
 #include <cmath>
@@ -33,7 +34,8 @@ enum {
     kFlagIters0 = 3, // iterations run per level 3..5
     kFlagAccepted = 6,
     kFlagBarrierTimeout = 7, // the persistent ICP kernel's grid barrier gave up waiting
-    kNumFlags = 8
+    kFlagOverflow = 8,       // a CTA partial outside the exact merge's range (|v| >= 2^42)
+    kNumFlags = 9
 };
 
 struct TrackState {
@@ -80,6 +82,85 @@ struct CSum {
         lo = (lo + l2) + e;
     }
 };
+
+// ------------------------------------------------------------- exact partial merge --
+// Each CTA's compensated sum (hi, lo) of a reduction term is split, by integer operations on the
+// float bits, into a fixed-point integer part in units of 2^-10 and a fraction in units of 2^-50
+// (bits below 2^-50 are dropped), and both are added with 64-bit integer atomics into one of four
+// copies of the term (by CTA index, each copy on its own 128-byte line, to spread the atomics
+// over L2). Integer sums do not depend on the order of arrival, so the merged totals, and the
+// poses computed from them, are the same run to run and between the persistent and the
+// per-iteration kernels. A partial of magnitude 2^42 or more (or not finite) raises
+// kFlagOverflow: the pose is then rejected and the call reports an error.
+constexpr int kAccCopies = 4;
+constexpr int kAccStride = 16;                                // u64 words per (copy, term)
+constexpr size_t kAccBufWords = (size_t) kAccCopies * 32 * kAccStride;
+constexpr int kAccBuffers = 3;                                // the persistent kernel rotates
+
+__device__ __forceinline__ void fixed_split(float f, long long& I, unsigned long long& F, bool& bad)
+{
+    const unsigned b = __float_as_uint(f);
+    const int e = (int) ((b >> 23) & 0xffu);
+    const unsigned long long m = (b & 0x7fffffu) | (e ? 0x800000u : 0u);
+    const int ee = e ? e : 1; // |f| = m 2^(ee - 150)
+    I = 0;
+    F = 0;
+    if (e == 0xff || ee > 168) {
+        bad = true;
+        return;
+    }
+    if (ee >= 140) {
+        I = (long long) (m << (ee - 140)); // < 2^52
+    }
+    else if (ee >= 100) {
+        const unsigned long long x = m << (ee - 100); // units of 2^-50, < 2^64
+        I = (long long) (x >> 40);
+        F = x & ((1ull << 40) - 1);
+    }
+    else if (100 - ee < 24) {
+        F = m >> (100 - ee);
+    }
+    if (b >> 31) { // -(I 2^40 + F) with F in [0, 2^40)
+        if (F) {
+            I = -I - 1;
+            F = (1ull << 40) - F;
+        }
+        else {
+            I = -I;
+        }
+    }
+}
+
+__device__ __forceinline__ void acc_add(unsigned long long* buf, int copy, int term, float hi, float lo, bool& bad)
+{
+    long long I1, I2;
+    unsigned long long F1, F2;
+    fixed_split(hi, I1, F1, bad);
+    fixed_split(lo, I2, F2, bad);
+    unsigned long long* p = buf + ((size_t) copy * 32 + term) * kAccStride;
+    atomicAdd(p, (unsigned long long) (I1 + I2));
+    atomicAdd(p + 1, F1 + F2);
+}
+
+__device__ __forceinline__ double acc_total(const unsigned long long* buf, int term)
+{
+    long long A = 0;
+    unsigned long long B = 0;
+#pragma unroll
+    for (int c = 0; c < kAccCopies; ++c) {
+        const unsigned long long* p = buf + ((size_t) c * 32 + term) * kAccStride;
+        A += (long long) __ldcg(p);
+        B += __ldcg(p + 1);
+    }
+    return fma((double) B, 0x1p-50, (double) A * 0x1p-10);
+}
+
+// Zeroes the two words of every (copy, term) of a buffer, threads tid of nthreads.
+__device__ __forceinline__ void acc_clear(unsigned long long* buf, int tid, int nthreads)
+{
+    for (int i = tid; i < kAccCopies * 32 * 2; i += nthreads)
+        buf[(size_t) (i >> 1) * kAccStride + (i & 1)] = 0ull;
+}
 
 // half_sample_robust_image (src/map/preprocessor.cpp:156-195)
 __global__ void half_sample_kernel(const float* __restrict__ in, int in_w, int in_h, float e_d, int radius,
@@ -174,8 +255,13 @@ struct TrackInit {
 
 // With pose12_in the start pose is read from the device (row-major 3x4) and its inverse is
 // formed here with the same float operations the host would use.
-__global__ void track_init_kernel(TrackState* st, TrackInit init, const float* pose12_in)
+__global__ void track_init_kernel(TrackState* st, TrackInit init, const float* pose12_in, unsigned long long* acc)
 {
+    if (acc)
+        for (int b = 0; b < kAccBuffers; ++b)
+            acc_clear(acc + (size_t) b * kAccBufWords, threadIdx.x, blockDim.x);
+    if (threadIdx.x != 0)
+        return;
     if (pose12_in) {
         const Tf T = tf_from12(pose12_in);
         const Tf Ti = inverse_iso(T);
@@ -202,11 +288,20 @@ __global__ void track_init_kernel(TrackState* st, TrackInit init, const float* p
 }
 
 // ---------------------------------------------------------------------- FP64 solve --
-// Measured on GB300: a dependent FP64 FMA takes 64 cycles and an IEEE FP64 division 650. The
-// solve below is arranged for short dependency chains: a right-looking LDL^T (each pivot
-// needs one reciprocal and one trailing update), reciprocals from an FP32 seed and one FP64
-// Newton step (relative error ~1e-14), a Rodrigues-form exponential, and the pose composition
-// spread over 12 threads.
+// Measured on GB300: the FP64 pipe of an SM sub-partition completes one warp instruction
+// (DFMA, DMUL, DADD, or a conversion to or from FP64) every ~63 cycles, with any number of
+// active lanes, and a dependent one follows after as long; warps on different sub-partitions
+// run their FP64 instructions in parallel. The solve and update are therefore arranged by the
+// number of FP64 instructions each warp issues on the critical path:
+//   - the 6x6 system [C | b] is eliminated by two warps, one entry per lane, in six
+//     division-free steps (row_i <- d_j row_i - a_ij row_j for every row i != j: LDL^T's
+//     trailing update with the back substitution folded in), two FP64 instructions per step;
+//   - the six divisions x_i = b_i / D_i at the end use one reciprocal each, seeded in FP32 on
+//     the mantissa (the pivots' products outgrow FP32's range) and refined by one FP64 Newton
+//     step (relative error ~1e-14);
+//   - the exponential's coefficients (one warp), the cross products it multiplies (another)
+//     and the convergence test (a third) run side by side, and the new pose follows from them
+//     in four FP64 instructions.
 
 __device__ __forceinline__ double drcp(double x)
 {
@@ -217,227 +312,152 @@ __device__ __forceinline__ double drcp(double x)
     return fma(r, fma(-x, r, 1.0), r);
 }
 
-// Solves C x = b for the symmetric 6x6 C given as its packed upper triangle in the order of
-// newReduce (row-major, icp.cpp:15-31). Returns false on a non-positive pivot, where the
-// reference's LLT fails and its update is zero (icp.cpp:33-41).
-__device__ __forceinline__ bool ldlt_solve6(const double* upper21, const double* b_in, double x[6])
+// d > 0 and finite, from the bits (no FP64 instruction): positive sign, nonzero, exponent not
+// all ones. A pivot failing it makes the reference's LLT fail and its update zero
+// (icp.cpp:33-41).
+__device__ __forceinline__ bool pivot_ok(double d)
 {
-    double A[6][6];
-#pragma unroll
-    for (int r = 0; r < 6; ++r)
-#pragma unroll
-        for (int c = 0; c < 6; ++c)
-            if (c >= r) {
-                A[r][c] = upper21[r * 6 - r * (r - 1) / 2 + (c - r)];
-                A[c][r] = A[r][c];
-            }
-    double inv_d[6];
-    bool ok = true;
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-        const double dj = A[j][j];
-        ok = ok && (dj > 0.0);
-        inv_d[j] = drcp(dj);
-        // column j of L, then the trailing update A_ik -= L_ij * D_j * L_kj = A_ij * L_kj
-#pragma unroll
-        for (int i = 0; i < 6; ++i)
-            if (i > j)
-                A[i][j] = A[i][j] * inv_d[j];
-#pragma unroll
-        for (int i = 0; i < 6; ++i)
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                if (i > j && k > j && k <= i)
-                    A[i][k] = fma(-A[i][j], A[k][j] * dj, A[i][k]);
-    }
-    double y[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-        y[i] = b_in[i];
-#pragma unroll
-    for (int k = 0; k < 6; ++k)
-#pragma unroll
-        for (int i = 0; i < 6; ++i)
-            if (i > k)
-                y[i] = fma(-A[i][k], y[k], y[i]);
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-        y[i] *= inv_d[i];
-#pragma unroll
-    for (int kk = 0; kk < 6; ++kk) {
-        const int k = 5 - kk;
-#pragma unroll
-        for (int i = 0; i < 6; ++i)
-            if (i < k)
-                y[i] = fma(-A[k][i], y[k], y[i]);
-    }
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-        x[i] = y[i];
-    return ok;
+    const long long b = __double_as_longlong(d);
+    return b > 0 && (b >> 52) < 0x7ff;
 }
 
-// se(3) exponential of [rho; omega] (math_util_impl.hpp:117-174) in FP64, Rodrigues form:
-// R = I + A W + B W^2 and V = I + B W + C W^2 with W = hat(omega), A = sin(t)/t,
-// B = (1 - cos t)/t^2, C = (t - sin t)/t^3 (series below |t| = 0.1), translation V rho.
-__device__ __forceinline__ void se3_exp_d(const double a[6], double R[9], double tr[3])
+// b / d for a finite d > 0 of any magnitude: d = m 2^e with m in [1, 2), 1 / m from drcp, the
+// quotient b (1 / m) rescaled by 2^-e through its exponent field.
+__device__ __forceinline__ double div_pos(double b, double d)
 {
-    const double wx = a[3], wy = a[4], wz = a[5];
-    const double x = fma(wz, wz, fma(wy, wy, wx * wx));
-    double A, B, Cc;
-    if (x < 0.01) {
-        A = 1.0 + x * (-1.0 / 6 + x * (1.0 / 120 + x * (-1.0 / 5040 + x * (1.0 / 362880))));
-        B = 0.5 + x * (-1.0 / 24 + x * (1.0 / 720 + x * (-1.0 / 40320 + x * (1.0 / 3628800))));
-        Cc = 1.0 / 6 + x * (-1.0 / 120 + x * (1.0 / 5040 + x * (-1.0 / 362880 + x * (1.0 / 39916800))));
-    }
-    else {
-        const double t = sqrt(x);
-        double sn, cs;
-        sincos(t, &sn, &cs);
-        const double it = drcp(t);
-        const double it2 = it * it;
-        A = sn * it;
-        B = (1.0 - cs) * it2;
-        Cc = (t - sn) * it2 * it;
-    }
-    const double w[3] = {wx, wy, wz};
-    const double W[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        double ti = 0.0;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const double w2 = w[i] * w[j] - (i == j ? x : 0.0); // (W^2)_ij = w_i w_j - |w|^2 d_ij
-            const double id = i == j ? 1.0 : 0.0;
-            R[3 * i + j] = fma(B, w2, fma(A, W[3 * i + j], id));
-            const double v = fma(Cc, w2, fma(B, W[3 * i + j], id));
-            ti = fma(v, a[j], ti);
-        }
-        tr[i] = ti;
-    }
+    const int hi = __double2hiint(d), lo = __double2loint(d);
+    const int e = ((hi >> 20) & 0x7ff) - 1023;
+    const double m = __hiloint2double((hi & 0x800fffff) | 0x3ff00000, lo);
+    const double q = b * drcp(m);
+    const long long qb = __double_as_longlong(q);
+    const int qe = (int) ((qb >> 52) & 0x7ff);
+    if (qe == 0 || qe == 0x7ff || qe - e <= 0 || qe - e >= 0x7ff)
+        return b / d; // zero, subnormal, or a result outside the normal range: the IEEE division
+    return __longlong_as_double(qb - (long long) e * (1LL << 52));
 }
 
-// ------------------------------------------------ warp-parallel FP64 solve and update --
-// One warp solves J^T J x = J^T e, forms exp(x) and composes the pose. Every dependent step
-// is a single FP64 instruction issued for all lanes, which on GB300 costs the same as one
-// issued for a single lane.
-//
-// Lane l < 21 holds entry (i, k), k <= i, of the symmetric matrix (l = i(i+1)/2 + k); lane
-// 21 + i holds b_i (column 6 of the augmented system). The elimination is division-free:
-// step j replaces every trailing entry by D_j A_ik - A_ij A_kj (rows scaled by the positive
-// pivot D_j instead of divided by it), so the six pivot reciprocals are formed together at
-// the end instead of one per step. Pivots <= 0 fail like the reference's LLT (icp.cpp:33-41).
-__constant__ signed char kTriRow[32] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 4, 5, 5, 5, 5, 5, 5,
-                                        0, 1, 2, 3, 4, 5, -1, -1, -1, -1, -1};
-__constant__ signed char kTriCol[32] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 4, 0, 1, 2, 3, 4, 5,
-                                        6, 6, 6, 6, 6, 6, -1, -1, -1, -1, -1};
-
-__device__ __forceinline__ int tri_lane(int i, int k) { return (i * (i + 1)) / 2 + k; }
-
-// sh_val: the 32 reduction values in shared memory (newReduce layout). Returns x in every lane.
-// The loops are deliberately rolled: the tail runs once per launch on whichever SM finishes
-// last, so its instruction stream is cold and code size costs more than loop overhead.
-__device__ __noinline__ bool warp_solve6(const double* sh_val, double x[6])
-{
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int li = kTriRow[lane], lk = kTriCol[lane];
-    double a = 0.0;
-    if (lane < 21)
-        a = sh_val[7 + lk * 6 - lk * (lk - 1) / 2 + (li - lk)]; // upper-triangle entry (k, i)
-    else if (lane < 27)
-        a = sh_val[1 + li];
-    bool ok = true;
-#pragma unroll 1
-    for (int j = 0; j < 6; ++j) {
-        const double d = __shfl_sync(full, a, tri_lane(j, j));
-        ok = ok && (d > 0.0);
-        const bool trailing = li > j && lk > j;
-        const int src_ij = trailing ? tri_lane(li, j) : 0;
-        const int src_kj = trailing ? (lk == 6 ? 21 + j : tri_lane(lk, j)) : 0;
-        const double a_ij = __shfl_sync(full, a, src_ij);
-        const double a_kj = __shfl_sync(full, a, src_kj);
-        if (trailing)
-            a = fma(d, a, -(a_ij * a_kj));
-    }
-    // reciprocal of pivot i in lane 21 + i
-    const double piv = __shfl_sync(full, a, lane < 27 && lane >= 21 ? tri_lane(li, li) : 0);
-    const double r = (lane >= 21 && lane < 27) ? drcp(piv) : 0.0;
-    // back substitution on the upper-triangular rows: x_k = b_k / D_k, then b_j -= A_kj x_k
-    double xv = 0.0; // lane 21 + k ends up holding x_k
-#pragma unroll 1
-    for (int k = 5; k >= 0; --k) {
-        const double xk = __shfl_sync(full, a * r, 21 + k);
-        if (lane == 21 + k)
-            xv = xk;
-        const bool upd = lk == 6 && li < k;
-        const double akj = __shfl_sync(full, a, upd ? tri_lane(k, li) : 0);
-        if (upd)
-            a = fma(-akj, xk, a);
-    }
-#pragma unroll
-    for (int k = 0; k < 6; ++k)
-        x[k] = __shfl_sync(full, xv, 21 + k);
-    return ok;
-}
+// x < y for x, y >= 0 (or x NaN: false), by the bits: no FP64 instruction.
+__device__ __forceinline__ bool lt_nonneg(double x, double y) { return __double_as_longlong(x) < __double_as_longlong(y); }
 
 // Series coefficients (Horner, highest first) of A = sin t / t, B = (1 - cos t) / t^2 and
-// C = (t - sin t) / t^3 in x = t^2, for lanes 0, 1, 2.
+// C = (t - sin t) / t^3 in x = t^2.
 __constant__ double kExpSeries[3][5] = {{1.0 / 362880, -1.0 / 5040, 1.0 / 120, -1.0 / 6, 1.0},
                                         {1.0 / 3628800, -1.0 / 40320, 1.0 / 720, -1.0 / 24, 0.5},
                                         {1.0 / 39916800, -1.0 / 362880, 1.0 / 5040, -1.0 / 120, 1.0 / 6}};
 
-// T <- exp(x) * T in FP64 (math_util_impl.hpp:117-174 in Rodrigues form: R = I + A W + B W^2,
-// V = I + B W + C W^2, W = hat(omega), translation V rho). pose (shared memory, row-major
-// 3x4) is read by lanes 0..11, which then write the new pose to st.
-__device__ __noinline__ void warp_exp_compose(const double x[6], const double* sh_pose, double* pose_out,
-                                              float* pose_f_out)
+__device__ __forceinline__ double pick3(int k, double a, double b, double c) { return k == 0 ? a : (k == 1 ? b : c); }
+
+// Solves C x = b (C symmetric, the packed upper triangle of the newReduce layout in sh_val[7..27],
+// b = sh_val[1..6], icp.cpp:15-41), forms exp(x) (math_util_impl.hpp:117-174 in Rodrigues form:
+// R = I + A W + B W^2, V = I + B W + C W^2, W = hat(omega), translation V rho) and composes
+// T <- exp(x) T with the pose sh_pose (row-major 3x4): R T applied column by column as
+// c + A (omega x c) + B (omega x (omega x c)), the translation plus V rho. Writes the new pose to
+// sh_new / sh_newf and |x| < threshold to *sh_conv. Called by every thread of the CTA.
+__device__ __noinline__ void icp_tail(const double* sh_val, const double* sh_pose, double* sh_new, float* sh_newf,
+                                      int* sh_conv, float icp_threshold, int wbase)
 {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const double wx = x[3], wy = x[4], wz = x[5];
-    const double xx = fma(wz, wz, fma(wy, wy, wx * wx));
-    double coef;
-    if (xx < 0.01) {
-        const int c = lane % 3;
-        coef = kExpSeries[c][0];
+    __shared__ double M[2][42];
+    __shared__ double sh_x[6];
+    __shared__ double sh_coef[3];
+    __shared__ double sh_u[16], sh_u2[16];
+    __shared__ int sh_ok;
+    // roles by warp wbase + 0 (elimination, coefficients) and wbase + 1 (elimination, cross
+    // products, convergence test): CTAs sharing an SM pass different wbase so that their FP64
+    // instructions go to different sub-partitions
+    const int warp = ((threadIdx.x >> 5) + 8 - wbase) & 7, lane = threadIdx.x & 31;
+    // elimination: entry e = 21 warp + lane (warps 0, 1, lanes < 21) is (r, c) of the 6 x 7 system
+    const bool gj = warp < 2 && lane < 21;
+    const int e = warp * 21 + lane, r = e / 7, c = e % 7;
+    if (gj) {
+        const int lo = r < c ? r : c, hi = r < c ? c : r;
+        M[0][e] = c == 6 ? sh_val[1 + r] : sh_val[7 + lo * 6 - lo * (lo - 1) / 2 + (hi - lo)];
+    }
+    if (threadIdx.x == 0)
+        sh_ok = 1;
+    __syncthreads();
 #pragma unroll 1
-        for (int u = 1; u < 5; ++u)
-            coef = fma(coef, xx, kExpSeries[c][u]);
+    for (int j = 0; j < 6; ++j) {
+        const double* Mi = M[j & 1];
+        double* Mo = M[(j + 1) & 1];
+        if (gj) {
+            const double d = Mi[7 * j + j];
+            double a = Mi[e];
+            if (r != j)
+                a = c == j ? 0.0 : fma(d, a, -(Mi[7 * r + j] * Mi[7 * j + c]));
+            Mo[e] = a;
+            if (e == 0 && !pivot_ok(d))
+                sh_ok = 0;
+        }
+        __syncthreads();
     }
-    else {
-        const double t = sqrt(xx);
-        double sn, cs;
-        sincos(t, &sn, &cs);
-        const double it = drcp(t), it2 = it * it;
-        const int c = lane % 3;
-        coef = c == 0 ? sn * it : (c == 1 ? (1.0 - cs) * it2 : (t - sn) * it2 * it);
+    if (gj && c == 6)
+        sh_x[r] = sh_ok ? div_pos(M[0][e], M[0][7 * r + r]) : 0.0;
+    __syncthreads();
+
+    const double wx = sh_x[3], wy = sh_x[4], wz = sh_x[5];
+    if (warp == 0) {
+        // lanes 0, 1, 2: the coefficients A, B, C
+        const double xx = fma(wz, wz, fma(wy, wy, wx * wx));
+        const int k = lane < 3 ? lane : 0;
+        double coef;
+        if (lt_nonneg(xx, 0.01)) {
+            // Horner in x; below 1e-5 (1e-7) the terms past x^2 (x) are under 1e-18 relative
+            const int first = lt_nonneg(xx, 1e-7) ? 3 : (lt_nonneg(xx, 1e-5) ? 2 : 0);
+            coef = kExpSeries[k][first];
+#pragma unroll 1
+            for (int u = first + 1; u < 5; ++u)
+                coef = fma(coef, xx, kExpSeries[k][u]);
+        }
+        else {
+            const double t = sqrt(xx);
+            double sn, cs;
+            sincos(t, &sn, &cs);
+            const double it = drcp(t), it2 = it * it;
+            coef = k == 0 ? sn * it : (k == 1 ? (1.0 - cs) * it2 : (t - sn) * it2 * it);
+        }
+        if (lane < 3)
+            sh_coef[lane] = coef;
     }
-    const double cA = __shfl_sync(full, coef, 0), cB = __shfl_sync(full, coef, 1), cC = __shfl_sync(full, coef, 2);
-    // lanes 0..8: R_ij; lanes 9..17: V_ij (e = lane mod 9, i = e / 3, j = e mod 3)
-    const int e = lane % 9, i = e / 3, j = e % 3;
-    const double wi = i == 0 ? wx : (i == 1 ? wy : wz);
-    const double wj = j == 0 ? wx : (j == 1 ? wy : wz);
-    const double w_hat = (i == j) ? 0.0 : ((j == (i + 1) % 3) ? -(3 - i - j == 0 ? wx : (3 - i - j == 1 ? wy : wz))
-                                                              : (3 - i - j == 0 ? wx : (3 - i - j == 1 ? wy : wz)));
-    const double w2 = fma(wi, wj, i == j ? -xx : 0.0);
-    const double c1 = lane < 9 ? cA : cB, c2 = lane < 9 ? cB : cC;
-    const double val = fma(c2, w2, fma(c1, w_hat, i == j ? 1.0 : 0.0));
-    // translation t_i = sum_j V_ij rho_j at lanes 9 + 3i
-    const double rho_j = j == 0 ? x[0] : (j == 1 ? x[1] : x[2]);
-    const double vr = (lane >= 9 && lane < 18) ? val * rho_j : 0.0;
-    const double t_i = vr + __shfl_down_sync(full, vr, 1) + __shfl_down_sync(full, vr, 2);
-    // compose: lane 4r + c (r < 3, c < 4) forms P_rc = sum_k R_rk P_kc (+ t_r for c = 3)
-    const int pr = (lane >> 2) % 3, pc = lane & 3;
-    const double r0 = __shfl_sync(full, val, 3 * pr), r1 = __shfl_sync(full, val, 3 * pr + 1);
-    const double r2 = __shfl_sync(full, val, 3 * pr + 2), tr = __shfl_sync(full, t_i, 9 + 3 * pr);
-    if (lane < 12) {
-        double v = fma(r2, sh_pose[8 + pc], fma(r1, sh_pose[4 + pc], r0 * sh_pose[pc]));
-        if (pc == 3)
-            v += tr;
-        pose_out[lane] = v;
-        pose_f_out[lane] = (float) v;
+    else if (warp == 1) {
+        // lanes 0..11: column lane / 3, row lane % 3 of the pose; lanes 12..14: rho
+        const int l = lane < 15 ? lane : 14;
+        const int col = l / 3, i = l % 3, i1 = i == 2 ? 0 : i + 1, i2 = i == 0 ? 2 : i - 1;
+        const double v1 = l < 12 ? sh_pose[4 * i1 + col] : sh_x[i1];
+        const double v2 = l < 12 ? sh_pose[4 * i2 + col] : sh_x[i2];
+        const double u = fma(pick3(i1, wx, wy, wz), v2, -(pick3(i2, wx, wy, wz) * v1)); // (omega x v)_i
+        const int base = l - i;
+        const double u1 = __shfl_sync(0xffffffffu, u, base + i1), u2 = __shfl_sync(0xffffffffu, u, base + i2);
+        const double uu = fma(pick3(i1, wx, wy, wz), u2, -(pick3(i2, wx, wy, wz) * u1));
+        if (lane < 15) {
+            sh_u[lane] = u;
+            sh_u2[lane] = uu;
+        }
+        // the convergence test in FP32, as the reference's x.norm() < icp_threshold on its FP32
+        // x (icp.cpp:218)
+        const float xf = lane < 6 ? (float) sh_x[lane] : 0.0f;
+        float q = xf * xf;
+        q += __shfl_down_sync(0xffffffffu, q, 4);
+        q += __shfl_down_sync(0xffffffffu, q, 2);
+        q += __shfl_down_sync(0xffffffffu, q, 1);
+        if (lane == 0)
+            *sh_conv = sqrtf(q) < icp_threshold;
     }
+    __syncthreads();
+    if (warp == 1) {
+        const int l = lane < 15 ? lane : 14;
+        const int col = l / 3, i = l % 3;
+        const double c1 = l < 12 ? sh_coef[0] : sh_coef[1], c2 = l < 12 ? sh_coef[1] : sh_coef[2];
+        const double v = l < 12 ? sh_pose[4 * i + col] : sh_x[i];
+        double val = fma(c2, sh_u2[l], fma(c1, sh_u[l], v));
+        const double vrho = __shfl_down_sync(0xffffffffu, val, 3); // lanes 9..11 take V rho from 12..14
+        if (lane >= 9 && lane < 12)
+            val += vrho;
+        if (lane < 12) {
+            sh_new[4 * i + col] = val;
+            sh_newf[4 * i + col] = (float) val;
+        }
+    }
+    __syncthreads();
 }
 
 struct IterParams {
@@ -451,15 +471,12 @@ struct IterParams {
     float dist_threshold, normal_threshold, icp_threshold;
 };
 
-// trackKernel for one pixel (icp_impl.hpp:16-102) given its input normal and point: the 32
-// reduction terms of newReduce (icp.cpp:45-184) in v: [e^2, e*J (6), upper J^T J (21),
+// trackKernel for one pixel (icp_impl.hpp:16-102) given its input normal and point, its 32
+// reduction terms of newReduce (icp.cpp:45-184) added into sum: [e^2, e*J (6), upper J^T J (21),
 // inlier, dist-reject, normal-reject, other reject].
-__device__ __forceinline__ void icp_pixel_terms(const Pinhole& s, const IterParams& ip, const Tf& T, const Tf& Tri,
-                                                bool in_range, F3 n_in, F3 p_S, float v[32])
+__device__ __forceinline__ void icp_pixel_add(const Pinhole& s, const IterParams& ip, const Tf& T, const Tf& Tri,
+                                              bool in_range, F3 n_in, F3 p_S, float sum[32])
 {
-#pragma unroll
-    for (int k = 0; k < 32; ++k)
-        v[k] = 0.0f;
     if (!in_range)
         return;
     int result;
@@ -508,33 +525,54 @@ __device__ __forceinline__ void icp_pixel_terms(const Pinhole& s, const IterPara
         }
     }
     if (result < 1) {
-        v[29] = result == -4 ? 1.0f : 0.0f;
-        v[30] = result == -5 ? 1.0f : 0.0f;
-        v[31] = result > -4 ? 1.0f : 0.0f;
+        sum[29] += result == -4 ? 1.0f : 0.0f;
+        sum[30] += result == -5 ? 1.0f : 0.0f;
+        sum[31] += result > -4 ? 1.0f : 0.0f;
         return;
     }
-    v[0] = e * e;
+    sum[0] += e * e;
 #pragma unroll
     for (int k = 0; k < 6; ++k)
-        v[1 + k] = e * J[k];
+        sum[1 + k] += e * J[k];
     int q = 7;
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
         for (int c = r; c < 6; ++c)
-            v[q++] = J[r] * J[c];
-    v[28] = 1.0f;
+            sum[q++] += J[r] * J[c];
+    sum[28] += 1.0f;
 }
+
+// Lane k of the warp adds term k of the 32 lanes' sums into its compensated accumulators
+// (the 32 x 32 term matrix goes through shared memory, stride 33: conflict-free), and the sums
+// restart from zero.
+__device__ __forceinline__ void icp_flush_terms(float sum[32], float (*sh_t)[33], CSum acc[4])
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+        sh_t[lane][k] = sum[k];
+        sum[k] = 0.0f;
+    }
+    __syncwarp();
+#pragma unroll 4
+    for (int j = 0; j < 32; ++j)
+        acc[j & 3].add(sh_t[j][lane]);
+    __syncwarp();
+}
+
+// Pixels a thread adds in plain FP32 before its sums go into the compensated accumulators.
+constexpr int kIcpFlushRounds = 8;
 
 // One ICP iteration: trackKernel + newReduce/reduceKernel + updatePoseKernel.
 // Main phase: each warp takes 32 pixels per tile (the next tile's input normal and point are
 // loaded before the current one is processed); the 32 x 32 term matrix goes through shared
 // memory (stride 33: conflict-free) so that lane k accumulates term k, with two-sum
 // compensation in 4 independent accumulators. Tail (last CTA to finish, found with an atomic
-// ticket, no waiting): fixed-order compensated FP32 sum of the CTA partials, then the FP64
-// solve, exponential and pose composition.
+// ticket, no waiting): the exact sum of the CTA partials, then the FP64 solve, exponential and
+// pose composition.
 __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, IterParams ip, TrackState* st,
-                                                                   float2* __restrict__ partials)
+                                                                   unsigned long long* __restrict__ acc_buf)
 {
     constexpr int kWarps = kTrackThreads / 32;
     __shared__ float sh_terms[kWarps][32][33];
@@ -564,21 +602,21 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
     bool in_range = i < npix;
     F3 n_cur = in_range ? ld3(ip.nrm, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
     F3 p_cur = in_range ? ld3(ip.pts, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
+    float sum[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k)
+        sum[k] = 0.0f;
+    int rounds = 0;
     for (int base = blockIdx.x * kTrackThreads; base < npix; base += stride) {
         const int i_next = i + stride;
         const bool next_in = i_next < npix;
         const F3 n_next = next_in ? ld3(ip.nrm, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
         const F3 p_next = next_in ? ld3(ip.pts, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
-        float v[32];
-        icp_pixel_terms(s, ip, T, Tri, in_range, n_cur, p_cur, v);
-#pragma unroll
-        for (int k = 0; k < 32; ++k)
-            sh_terms[warp][lane][k] = v[k];
-        __syncwarp();
-#pragma unroll 4
-        for (int j = 0; j < 32; ++j)
-            acc[j & 3].add(sh_terms[warp][j][lane]);
-        __syncwarp();
+        icp_pixel_add(s, ip, T, Tri, in_range, n_cur, p_cur, sum);
+        if (++rounds == kIcpFlushRounds || base + stride >= npix) { // uniform across the CTA
+            icp_flush_terms(sum, sh_terms[warp], acc);
+            rounds = 0;
+        }
         i = i_next;
         in_range = next_in;
         n_cur = n_next;
@@ -593,7 +631,10 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
         CSum t{0.0f, 0.0f};
         for (int wi = 0; wi < kWarps; ++wi)
             t.merge(sh_warp[wi][threadIdx.x].x, sh_warp[wi][threadIdx.x].y);
-        partials[blockIdx.x * 32 + threadIdx.x] = make_float2(t.hi, t.lo);
+        bool bad = false;
+        acc_add(acc_buf, (int) (blockIdx.x % kAccCopies), threadIdx.x, t.hi, t.lo, bad);
+        if (bad)
+            atomicExch(&st->flags[kFlagOverflow], 1);
     }
     __threadfence();
     __syncthreads();
@@ -607,59 +648,29 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
     // ---- last CTA
     __shared__ double sh_pose[12];
     __shared__ double sh_val[32];
+    __shared__ double sh_new[12];
+    __shared__ float sh_newf[12];
     __shared__ int sh_conv;
     if (threadIdx.x < 12)
-        sh_pose[threadIdx.x] = __ldcg(&st->pose[threadIdx.x]); // overlaps the merge below
-    {
-        // warp w merges rows w, w + 8, ...; loads are issued 16 at a time so that the L2
-        // latency is paid once per batch, not once per row
-        CSum t{0.0f, 0.0f};
-        const int nb = (int) gridDim.x;
-        for (int b0 = warp; b0 < nb; b0 += 16 * kWarps) {
-            float2 pr[16];
-#pragma unroll
-            for (int u = 0; u < 16; ++u) {
-                const int b = b0 + u * kWarps;
-                pr[u] = b < nb ? __ldcg(&partials[b * 32 + lane]) : make_float2(0.0f, 0.0f);
-            }
-#pragma unroll
-            for (int u = 0; u < 16; ++u)
-                t.merge(pr[u].x, pr[u].y);
-        }
-        sh_warp[warp][lane] = make_float2(t.hi, t.lo);
-    }
-    __syncthreads();
+        sh_pose[threadIdx.x] = __ldcg(&st->pose[threadIdx.x]);
     if (threadIdx.x < 32) {
-        CSum t{0.0f, 0.0f};
-        for (int c = 0; c < kWarps; ++c)
-            t.merge(sh_warp[c][threadIdx.x].x, sh_warp[c][threadIdx.x].y);
-        const double v = (double) t.hi + (double) t.lo;
+        const double v = acc_total(acc_buf, threadIdx.x);
         sh_val[threadIdx.x] = v;
         st->last_red[threadIdx.x] = (float) v;
     }
     __syncthreads();
-    if (threadIdx.x < 32) {
-        double xs[6];
-        if (!warp_solve6(sh_val, xs)) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                xs[k] = 0.0;
-        }
-        warp_exp_compose(xs, sh_pose, st->pose, st->pose_f);
-        if (threadIdx.x == 0) {
-            st->ticket = 0;
-            st->flags[kFlagIters0 + ip.level] += 1;
-            double xn = 0.0;
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                xn = fma(xs[k], xs[k], xn);
-            const double thr = (double) ip.icp_threshold;
-            sh_conv = xn < thr * thr;
-        }
+    icp_tail(sh_val, sh_pose, sh_new, sh_newf, &sh_conv, ip.icp_threshold, 0);
+    acc_clear(acc_buf, threadIdx.x, blockDim.x); // for the next launch (every CTA has added)
+    if (threadIdx.x < 12) {
+        st->pose[threadIdx.x] = sh_new[threadIdx.x];
+        st->pose_f[threadIdx.x] = sh_newf[threadIdx.x];
     }
-    __syncthreads();
-    if (threadIdx.x == 0 && sh_conv)
-        st->flags[kFlagDone0 + ip.level] = 1;
+    if (threadIdx.x == 0) {
+        st->ticket = 0;
+        st->flags[kFlagIters0 + ip.level] += 1;
+        if (sh_conv)
+            st->flags[kFlagDone0 + ip.level] = 1;
+    }
 }
 
 // checkPoseKernel (icp.cpp:227-246): revert to the reference pose on a poor final alignment.
@@ -668,7 +679,7 @@ __global__ void icp_check_kernel(TrackState* st, int W, int H, float track_thres
     const float* v = st->last_red;
     // a timed-out grid barrier of the persistent ICP leaves no trustworthy pose: reject it
     const bool reject = ((double) sqrtf(v[0] / v[28]) > 2e-2) || (v[28] / (float) (W * H) < track_threshold)
-        || st->flags[kFlagBarrierTimeout] != 0;
+        || st->flags[kFlagBarrierTimeout] != 0 || st->flags[kFlagOverflow] != 0;
     if (reject) {
         for (int i = 0; i < 12; ++i) {
             st->pose_f[i] = st->ref_f[i];
@@ -684,17 +695,20 @@ __global__ void icp_check_kernel(TrackState* st, int W, int H, float track_thres
 // ------------------------------------------------------- persistent ICP (all iterations) --
 // The per-iteration launches above, fused into one cooperative launch per frame: every CTA
 // runs every iteration of every level; after each iteration's main pass the CTAs meet at a
-// grid barrier, and each CTA then merges the CTA partials and solves redundantly (the same
-// operations in the same order, so every CTA holds the same new pose) instead of one last CTA
-// solving and the next launch reading its result. The pixel partition, the merge order and
-// the FP64 tail are those of icp_iter_kernel, so the poses are bit-identical to it.
+// grid barrier, and each CTA then reads the exact totals and solves redundantly (the same
+// operations on the same values, so every CTA holds the same new pose) instead of one last CTA
+// solving and the next launch reading its result. The pixel partition, the exact merge and the
+// FP64 tail are those of icp_iter_kernel, so the poses are bit-identical to it.
 
 struct IcpLevels {
     IterParams ip[3];
     int nctas[3];
     int iters[3];
     int levels;
+    unsigned* sm_slots; // per-SM arrival counters (kIcpSlotCounters, never reset)
 };
+
+constexpr int kIcpSlotCounters = 1024;
 
 constexpr unsigned kIcpSpinLimit = 1u << 22; // ~0.3 s of polling at most, then the timeout flag
 
@@ -721,7 +735,7 @@ __device__ __forceinline__ void icp_grid_sync(unsigned* ctr, unsigned target, in
 }
 
 __global__ void __launch_bounds__(kTrackThreads, 3) icp_persistent_kernel(Pinhole s, IcpLevels L, TrackState* st,
-                                                                         float2* __restrict__ partials)
+                                                                         unsigned long long* __restrict__ acc_base)
 {
     constexpr int kWarps = kTrackThreads / 32;
     __shared__ float sh_terms[kWarps][32][33];
@@ -732,7 +746,15 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_persistent_kernel(Pinhol
     __shared__ float sh_newf[12];
     __shared__ double sh_val[32];
     __shared__ int sh_conv;
+    __shared__ int sh_wbase;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        // the CTAs that share an SM count their arrivals there and alternate the warps of the
+        // FP64 tail (consecutive counts differ in parity, whatever earlier launches left)
+        unsigned smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        sh_wbase = (int) (atomicAdd(&L.sm_slots[smid % kIcpSlotCounters], 1u) & 1u) * 2;
+    }
     if (threadIdx.x < 12) {
         const int i = threadIdx.x, r = i >> 2, c = i & 3;
         if (c < 3) {
@@ -751,7 +773,7 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_persistent_kernel(Pinhol
         const IterParams& ip = L.ip[level];
         const int nct = L.nctas[level];
         for (int iter = 0; iter < L.iters[level]; ++iter) {
-            float2* part = partials + (size_t) (phase & 1u) * kMaxTrackCtas * 32;
+            unsigned long long* buf = acc_base + (size_t) (phase % kAccBuffers) * kAccBufWords;
             if ((int) blockIdx.x < nct) {
                 CSum acc[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
                 const int npix = ip.w * ip.h;
@@ -760,21 +782,21 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_persistent_kernel(Pinhol
                 bool in_range = i < npix;
                 F3 n_cur = in_range ? ld3(ip.nrm, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
                 F3 p_cur = in_range ? ld3(ip.pts, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
+                float sum[32];
+#pragma unroll
+                for (int k = 0; k < 32; ++k)
+                    sum[k] = 0.0f;
+                int rounds = 0;
                 for (int base = blockIdx.x * kTrackThreads; base < npix; base += stride) {
                     const int i_next = i + stride;
                     const bool next_in = i_next < npix;
                     const F3 n_next = next_in ? ld3(ip.nrm, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
                     const F3 p_next = next_in ? ld3(ip.pts, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
-                    float v[32];
-                    icp_pixel_terms(s, ip, T, Tri, in_range, n_cur, p_cur, v);
-#pragma unroll
-                    for (int k = 0; k < 32; ++k)
-                        sh_terms[warp][lane][k] = v[k];
-                    __syncwarp();
-#pragma unroll 4
-                    for (int j = 0; j < 32; ++j)
-                        acc[j & 3].add(sh_terms[warp][j][lane]);
-                    __syncwarp();
+                    icp_pixel_add(s, ip, T, Tri, in_range, n_cur, p_cur, sum);
+                    if (++rounds == kIcpFlushRounds || base + stride >= npix) { // uniform across the CTA
+                        icp_flush_terms(sum, sh_terms[warp], acc);
+                        rounds = 0;
+                    }
                     i = i_next;
                     in_range = next_in;
                     n_cur = n_next;
@@ -789,58 +811,29 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_persistent_kernel(Pinhol
                     CSum t{0.0f, 0.0f};
                     for (int wi = 0; wi < kWarps; ++wi)
                         t.merge(sh_warp[wi][threadIdx.x].x, sh_warp[wi][threadIdx.x].y);
-                    part[blockIdx.x * 32 + threadIdx.x] = make_float2(t.hi, t.lo);
+                    bool bad = false;
+                    acc_add(buf, (int) (blockIdx.x % kAccCopies), threadIdx.x, t.hi, t.lo, bad);
+                    if (bad)
+                        atomicExch(&st->flags[kFlagOverflow], 1);
                 }
             }
             ++phase;
             icp_grid_sync(&st->ticket, phase * gridDim.x, &st->flags[kFlagBarrierTimeout]);
-            // every CTA: merge the nct partials in icp_iter_kernel's order, solve, update
-            {
-                CSum t{0.0f, 0.0f};
-                for (int b0 = warp; b0 < nct; b0 += 16 * kWarps) {
-                    float2 pr[16];
-#pragma unroll
-                    for (int u = 0; u < 16; ++u) {
-                        const int b = b0 + u * kWarps;
-                        pr[u] = b < nct ? __ldcg(&part[b * 32 + lane]) : make_float2(0.0f, 0.0f);
-                    }
-#pragma unroll
-                    for (int u = 0; u < 16; ++u)
-                        t.merge(pr[u].x, pr[u].y);
-                }
-                sh_warp[warp][lane] = make_float2(t.hi, t.lo);
-            }
-            __syncthreads();
+            // every CTA: the merged totals, then the solve and update. The buffer used two phases
+            // ago has been read by every CTA before this barrier: CTA 0 clears it for the phase
+            // after next.
             if (threadIdx.x < 32) {
-                CSum t{0.0f, 0.0f};
-                for (int c = 0; c < kWarps; ++c)
-                    t.merge(sh_warp[c][threadIdx.x].x, sh_warp[c][threadIdx.x].y);
-                const double v = (double) t.hi + (double) t.lo;
+                const double v = acc_total(buf, threadIdx.x);
                 sh_val[threadIdx.x] = v;
                 if (blockIdx.x == 0)
                     st->last_red[threadIdx.x] = (float) v;
             }
+            if (blockIdx.x == 0)
+                acc_clear(acc_base + (size_t) ((phase + 1) % kAccBuffers) * kAccBufWords, threadIdx.x, blockDim.x);
             __syncthreads();
-            if (threadIdx.x < 32) {
-                double xs[6];
-                if (!warp_solve6(sh_val, xs)) {
-#pragma unroll
-                    for (int k = 0; k < 6; ++k)
-                        xs[k] = 0.0;
-                }
-                warp_exp_compose(xs, sh_pose, sh_new, sh_newf);
-                if (threadIdx.x == 0) {
-                    double xn = 0.0;
-#pragma unroll
-                    for (int k = 0; k < 6; ++k)
-                        xn = fma(xs[k], xs[k], xn);
-                    const double thr = (double) ip.icp_threshold;
-                    sh_conv = xn < thr * thr;
-                    if (blockIdx.x == 0)
-                        st->flags[kFlagIters0 + level] += 1;
-                }
-            }
-            __syncthreads();
+            icp_tail(sh_val, sh_pose, sh_new, sh_newf, &sh_conv, ip.icp_threshold, sh_wbase);
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+                st->flags[kFlagIters0 + level] = iter + 1; // a store: no global read on the critical path
             if (threadIdx.x < 12) {
                 const int i = threadIdx.x, r = i >> 2, c = i & 3;
                 sh_pose[i] = sh_new[i];
@@ -877,7 +870,8 @@ struct se_gpu_tracker {
     float* pyr_depth[3]; // levels 1, 2 (index 0 unused: the input is level 0)
     float* pts[3];
     float* nrm[3];
-    float2* partials;    // two sets of kMaxTrackCtas x 32 (the persistent kernel alternates)
+    unsigned long long* acc; // kAccBuffers exact-merge accumulators (the persistent kernel rotates)
+    unsigned* sm_slots;  // kIcpSlotCounters per-SM counters of the persistent kernel
     TrackState* state;
     int nctas[3];
     int persistent;      // one cooperative launch per frame (when the grid fits on the GPU)
@@ -926,8 +920,12 @@ se_gpu_status se_gpu_tracker_create(const se_gpu_pinhole* sensor, const se_gpu_t
         if (t->nctas[l] > kMaxTrackCtas)
             t->nctas[l] = kMaxTrackCtas;
     }
-    if ((e = cudaMalloc(&t->partials, (size_t) 2 * kMaxTrackCtas * 32 * sizeof(float2))) != cudaSuccess)
-        return fail(e, "cudaMalloc(partials)");
+    if ((e = cudaMalloc(&t->acc, kAccBuffers * kAccBufWords * sizeof(unsigned long long))) != cudaSuccess
+        || (e = cudaMemset(t->acc, 0, kAccBuffers * kAccBufWords * sizeof(unsigned long long))) != cudaSuccess)
+        return fail(e, "cudaMalloc(acc)");
+    if ((e = cudaMalloc(&t->sm_slots, kIcpSlotCounters * sizeof(unsigned))) != cudaSuccess
+        || (e = cudaMemset(t->sm_slots, 0, kIcpSlotCounters * sizeof(unsigned))) != cudaSuccess)
+        return fail(e, "cudaMalloc(sm_slots)");
     {
         // the persistent kernel needs its whole grid resident at once
         int per_sm = 0;
@@ -956,7 +954,8 @@ se_gpu_status se_gpu_tracker_destroy(se_gpu_tracker* t)
         cudaFree(t->pts[l]);
         cudaFree(t->nrm[l]);
     }
-    cudaFree(t->partials);
+    cudaFree(t->acc);
+    cudaFree(t->sm_slots);
     cudaFree(t->state);
     delete t;
     return SE_GPU_OK;
@@ -989,7 +988,7 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
     li.depth[0] = depth_dev;
     {
     ProfScope ps(kProfTrackPrep, stream);
-    track_init_kernel<<<1, 1, 0, stream>>>(t->state, init, pose_in);
+    track_init_kernel<<<1, 256, 0, stream>>>(t->state, init, pose_in, t->acc);
     const float e_d = 0.1f * 3;
     for (int l = 1; l < t->levels; ++l) {
         dim3 b(32, 8), g((li.w[l] + 31) / 32, (li.h[l] + 7) / 8);
@@ -1005,6 +1004,7 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
     IcpLevels L;
     std::memset(&L, 0, sizeof(L));
     L.levels = t->levels;
+    L.sm_slots = t->sm_slots;
     for (int level = t->levels - 1; level >= 0; --level) {
         IterParams& ip = L.ip[level];
         ip.ref_pts = ref_pts;
@@ -1033,14 +1033,14 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
         attr[0].val.cooperative = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        SE_CUDA_TRY(cudaLaunchKernelEx(&cfg, icp_persistent_kernel, t->s, L, t->state, t->partials));
+        SE_CUDA_TRY(cudaLaunchKernelEx(&cfg, icp_persistent_kernel, t->s, L, t->state, t->acc));
     }
     else {
         for (int level = t->levels - 1; level >= 0; --level)
             for (int it = 0; it < t->config.iterations[level]; ++it) {
                 ProfScope ps(kProfIcpIter, stream);
                 icp_iter_kernel<<<t->nctas[level], kTrackThreads, 0, stream>>>(t->s, L.ip[level], t->state,
-                                                                               t->partials);
+                                                                               t->acc);
             }
     }
     {
@@ -1081,6 +1081,10 @@ se_gpu_status se_gpu_track(se_gpu_tracker* t, const float* depth_dev, const floa
         *accepted = hs.flags[kFlagAccepted];
     if (hs.flags[kFlagBarrierTimeout]) {
         set_last_error("se_gpu_track: the ICP grid barrier timed out (the pose was reverted)");
+        return SE_GPU_ERR_CUDA;
+    }
+    if (hs.flags[kFlagOverflow]) {
+        set_last_error("se_gpu_track: an ICP partial sum exceeded the exact merge's range (the pose was reverted)");
         return SE_GPU_ERR_CUDA;
     }
     return SE_GPU_OK;
@@ -1223,21 +1227,21 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_noalloc_kernel(Pinh
     bool in_range = i < npix;
     F3 n_cur = in_range ? depth_normal(depth, s, ip.w, ip.h, i, neg_y) : f3(0.0f, 0.0f, 0.0f);
     F3 p_cur = in_range ? depth_point(depth, s, ip.w, i) : f3(0.0f, 0.0f, 0.0f);
+    float sum[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k)
+        sum[k] = 0.0f;
+    int rounds = 0;
     for (int base = blockIdx.x * kTrackThreads; base < npix; base += stride) {
         const int i_next = i + stride;
         const bool next_in = i_next < npix;
         const F3 n_next = next_in ? depth_normal(depth, s, ip.w, ip.h, i_next, neg_y) : f3(0.0f, 0.0f, 0.0f);
         const F3 p_next = next_in ? depth_point(depth, s, ip.w, i_next) : f3(0.0f, 0.0f, 0.0f);
-        float v[32];
-        icp_pixel_terms(s, ip, T, Tri, in_range, n_cur, p_cur, v);
-#pragma unroll
-        for (int k = 0; k < 32; ++k)
-            sh_terms[warp][lane][k] = v[k];
-        __syncwarp();
-#pragma unroll 4
-        for (int j = 0; j < 32; ++j)
-            acc[j & 3].add(sh_terms[warp][j][lane]);
-        __syncwarp();
+        icp_pixel_add(s, ip, T, Tri, in_range, n_cur, p_cur, sum);
+        if (++rounds == kIcpFlushRounds || base + stride >= npix) { // uniform across the CTA
+            icp_flush_terms(sum, sh_terms[warp], acc);
+            rounds = 0;
+        }
         i = i_next;
         in_range = next_in;
         n_cur = n_next;
@@ -1266,6 +1270,8 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_noalloc_kernel(Pinh
     // ---- last CTA
     __shared__ double sh_pose[12];
     __shared__ double sh_val[32];
+    __shared__ double sh_new[12];
+    __shared__ float sh_newf[12];
     __shared__ int sh_conv;
     if (threadIdx.x < 12)
         sh_pose[threadIdx.x] = __ldcg(&st->pose[threadIdx.x]); // overlaps the merge below
@@ -1297,28 +1303,17 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_noalloc_kernel(Pinh
         st->last_red[threadIdx.x] = (float) v;
     }
     __syncthreads();
-    if (threadIdx.x < 32) {
-        double xs[6];
-        if (!warp_solve6(sh_val, xs)) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                xs[k] = 0.0;
-        }
-        warp_exp_compose(xs, sh_pose, st->pose, st->pose_f);
-        if (threadIdx.x == 0) {
-            st->ticket = 0;
-            st->flags[kFlagIters0 + ip.level] += 1;
-            double xn = 0.0;
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                xn = fma(xs[k], xs[k], xn);
-            const double thr = (double) ip.icp_threshold;
-            sh_conv = xn < thr * thr;
-        }
+    icp_tail(sh_val, sh_pose, sh_new, sh_newf, &sh_conv, ip.icp_threshold, 0);
+    if (threadIdx.x < 12) {
+        st->pose[threadIdx.x] = sh_new[threadIdx.x];
+        st->pose_f[threadIdx.x] = sh_newf[threadIdx.x];
     }
-    __syncthreads();
-    if (threadIdx.x == 0 && sh_conv)
-        st->flags[kFlagDone0 + ip.level] = 1;
+    if (threadIdx.x == 0) {
+        st->ticket = 0;
+        st->flags[kFlagIters0 + ip.level] += 1;
+        if (sh_conv)
+            st->flags[kFlagDone0 + ip.level] = 1;
+    }
 }
 
 
@@ -1393,7 +1388,7 @@ extern "C" se_gpu_status se_gpu_track_noalloc(const se_gpu_pinhole* sensor, cons
         init.T_WS[4 * i + 3] = T.t[i];
         init.ref_inv[4 * i + 3] = Ti.t[i];
     }
-    track_init_kernel<<<1, 1, 0, stream>>>(&scratch->state, init, nullptr);
+    track_init_kernel<<<1, 1, 0, stream>>>(&scratch->state, init, nullptr, nullptr);
     IterParams ip;
     ip.ref_pts = ref_pts;
     ip.ref_nrm = ref_nrm;
