@@ -10,7 +10,9 @@
 //      dense block index with a one-block cache, trilinear interpolation near the surface
 //      (visitor_impl.hpp:976-1024) and the linear zero-crossing estimate;
 //   3. the surface normal from the 32-sample central-difference gradient
-//      (visitor_impl.hpp:1094-1251, map_impl.hpp:236-262).
+//      (visitor_impl.hpp:1094-1251, map_impl.hpp:236-262), its 32 loads issued together.
+// The traversal stack and the gradient's block table live in shared memory; the register cap
+// of 9 CTAs per SM (a few spilled words) is faster than the 5 CTAs that 92 registers allow.
 // Sample loops are deliberately not unrolled: one copy of the fetch path keeps the kernel
 // inside the instruction cache.
 #include <cmath>
@@ -30,10 +32,14 @@ __global__ void raycast_prep_kernel(const float* pose12, RaycastParams host_p, R
 }
 
 template <int S, bool MR>
-__global__ void __launch_bounds__(128) raycast_kernel(MapDevice m, Pinhole s, const RaycastParams* __restrict__ P,
+__global__ void __launch_bounds__(128, 9) raycast_kernel(MapDevice m, Pinhole s, const RaycastParams* __restrict__ P,
                                                       float* __restrict__ pts, float* __restrict__ nrm,
                                                       int8_t* __restrict__ scale)
 {
+    // per-thread scratch in shared memory (column threadIdx.x): the traversal stack and the
+    // gradient's block table
+    __shared__ float sh_stack[kEsvoStackDepth * 128];
+    __shared__ int sh_bt[8 * 128];
     const RaycastParams rp = *P;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
@@ -52,14 +58,14 @@ __global__ void __launch_bounds__(128) raycast_kernel(MapDevice m, Pinhole s, co
     F3 n = f3(0.0f, 0.0f, 0.0f);
     F3 p = f3(0.0f, 0.0f, 0.0f);
     int hit_scale = 0;
-    if (raycast_tsdf<S, MR>(m, rp, c, origin, dir_W, t_near, t_far, hit, hit_scale)) {
+    if (raycast_tsdf<S, MR>(m, rp, c, origin, dir_W, t_near, t_far, hit, hit_scale, sh_stack + threadIdx.x, 128)) {
         p = hit;
         F3 g;
         bool ok;
         if constexpr (MR)
             ok = mr_field_grad<S>(m, hit, g);
         else
-            ok = field_grad<S>(m, c, hit, g);
+            ok = field_grad_batched<S>(m, c, hit, g, sh_bt + threadIdx.x, 128);
         if (ok)
             n = normalized(g);
     }

@@ -14,11 +14,16 @@ namespace se_gpu {
 __device__ __forceinline__ float fmax_std(float a, float b) { return (a < b) ? b : a; } // std::max
 __device__ __forceinline__ float fmin_std(float a, float b) { return (b < a) ? b : a; } // std::min
 
-// The state of VoxelBlockRayIterator after its first next(): found, tcmin(), tmax().
+constexpr int kEsvoStackDepth = 23;
+
+// The state of VoxelBlockRayIterator after its first next(): found, tcmin(), tmax(). The
+// traversal stack (t_max per scale) is stack[scale * stride]: a caller with many threads per SM
+// passes this thread's column of a shared-memory array; with stack == nullptr it lives in the
+// thread's local memory.
 static __device__ bool first_block(const MapDevice& m, const RaycastParams& rp, F3 o_W, F3 d_W, float near_p,
-                            float far_p, float& tcmin, float& tmax)
+                                   float far_p, float& tcmin, float& tmax, float* stack = nullptr, int stride = 1)
 {
-    constexpr int kStackDepth = 23;
+    constexpr int kStackDepth = kEsvoStackDepth;
     float d[3] = {d_W.x, d_W.y, d_W.z};
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -57,10 +62,14 @@ static __device__ bool first_block(const MapDevice& m, const RaycastParams& rp, 
     }
     int scale = kStackDepth - 1;
     float scale_exp2 = 0.5f;
-    float stack_tmax[kStackDepth];
-#pragma unroll
+    float local_stack[kStackDepth];
+    float* stack_tmax = stack;
+    if (stack_tmax == nullptr) {
+        stack_tmax = local_stack;
+        stride = 1;
+    }
     for (int i = 0; i < kStackDepth; ++i)
-        stack_tmax[i] = 0.0f;
+        stack_tmax[i * stride] = 0.0f;
 
     // Bounded: every iteration descends (at most 23 times between advances) or advances the
     // ray past a cell boundary; the cap only guards against a malformed map.
@@ -99,7 +108,7 @@ static __device__ bool first_block(const MapDevice& m, const RaycastParams& rp, 
             for (int a = 0; a < 3; ++a)
                 t_centre[a] = half * t_coef[a] + tc[a];
             if (tc_max < h)
-                stack_tmax[scale] = t_max;
+                stack_tmax[scale * stride] = t_max;
             h = tc_max;
             idx = 0;
             --scale;
@@ -136,7 +145,7 @@ static __device__ bool first_block(const MapDevice& m, const RaycastParams& rp, 
             if (scale >= kStackDepth)
                 break;
             scale_exp2 = __int_as_float((scale - kStackDepth + 127) << 23);
-            t_max = stack_tmax[scale];
+            t_max = stack_tmax[scale * stride];
             int sh[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
@@ -297,6 +306,87 @@ __device__ bool field_grad(const MapDevice& m, BlockCache& c, F3 p_W, F3& g)
     return true;
 }
 
+// kGradSel as a compile-time function, for the unrolled loads below.
+__host__ __device__ constexpr int grad_sel(int i)
+{
+    constexpr unsigned char t[32] = {0x14, 0x18, 0x24, 0x28, 0x11, 0x21, 0x05, 0x15, 0x25, 0x35, 0x09,
+                                     0x19, 0x29, 0x39, 0x1d, 0x2d, 0x12, 0x22, 0x06, 0x16, 0x26, 0x36,
+                                     0x0a, 0x1a, 0x2a, 0x3a, 0x1e, 0x2e, 0x17, 0x1b, 0x27, 0x2b};
+    return t[i];
+}
+
+// field_grad with the 32 samples loaded together: the blocks of the sample neighbourhood
+// [base - 1, base + 2]^3 (at most 2 per axis) are looked up once into bt (this thread's 8
+// entries, bt[k * bs] for k = x | y << 1 | z << 2 block offsets), then the 32 voxel loads are
+// independent of one another. A failed sample fails the query as it does in field_grad, so the
+// result and its arithmetic are field_grad's.
+template <int S>
+__device__ bool field_grad_batched(const MapDevice& m, BlockCache& c, F3 p_W, F3& g, int* bt, int bs)
+{
+    F3 vf;
+    if (!point_to_voxel_f(m, p_W, vf))
+        return false;
+    const F3 s = f3(vf.x - 0.5f, vf.y - 0.5f, vf.z - 0.5f);
+    const F3 fac = f3(s.x - floorf(s.x), s.y - floorf(s.y), s.z - floorf(s.z));
+    const int base[3] = {(int) s.x, (int) s.y, (int) s.z};
+    const int top = m.size - 1;
+    int sel[3][4];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        sel[i][0] = max(base[i] - 1, 0);
+        sel[i][1] = max(base[i], 0);
+        sel[i][2] = min(base[i] + 1, top);
+        sel[i][3] = min(base[i] + 2, top);
+    }
+    if (lookup_block(m, c, base[0], base[1], base[2]) < 0)
+        return false;
+    int lo[3], two[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = sel[a][0] >> 3;
+        two[a] = (sel[a][3] >> 3) != lo[a];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+        int b = -1;
+        if ((!ox || two[0]) && (!oy || two[1]) && (!oz || two[2]))
+            b = __ldg(&m.block_index[((size_t) (lo[2] + oz) << (2 * m.log2_bps)) | ((size_t) (lo[1] + oy) << m.log2_bps)
+                                     | (size_t) (lo[0] + ox)]);
+        bt[k * bs] = b;
+    }
+    float v[32];
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+        const int code = grad_sel(i);
+        const int x = sel[0][code & 3], y = sel[1][(code >> 2) & 3], z = sel[2][(code >> 4) & 3];
+        const int b = bt[(((x >> 3) - lo[0]) | (((y >> 3) - lo[1]) << 1) | (((z >> 3) - lo[2]) << 2)) * bs];
+        float t = 1.0f, w = 0.0f;
+        if (b >= 0)
+            load_voxel<S>(m, b, (x & 7) + 8 * (y & 7) + 64 * (z & 7), t, w);
+        ok = ok && (w != 0.0f);
+        v[i] = t;
+    }
+    if (!ok)
+        return false;
+    const float rx = 1.0f - fac.x, ry = 1.0f - fac.y, rz = 1.0f - fac.z;
+    const float gx = (((v[19] - v[0]) * rx + (v[28] - v[7]) * fac.x) * ry
+                      + ((v[23] - v[1]) * rx + (v[29] - v[11]) * fac.x) * fac.y) * rz
+        + (((v[20] - v[2]) * rx + (v[30] - v[8]) * fac.x) * ry
+           + ((v[24] - v[3]) * rx + (v[31] - v[12]) * fac.x) * fac.y) * fac.z;
+    const float gy = (((v[11] - v[4]) * rx + (v[23] - v[16]) * fac.x) * ry
+                      + ((v[14] - v[7]) * rx + (v[26] - v[19]) * fac.x) * fac.y) * rz
+        + (((v[12] - v[5]) * rx + (v[24] - v[17]) * fac.x) * ry
+           + ((v[15] - v[8]) * rx + (v[27] - v[20]) * fac.x) * fac.y) * fac.z;
+    const float gz = (((v[8] - v[6]) * rx + (v[20] - v[18]) * fac.x) * ry
+                      + ((v[12] - v[10]) * rx + (v[24] - v[22]) * fac.x) * fac.y) * rz
+        + (((v[9] - v[7]) * rx + (v[21] - v[19]) * fac.x) * ry
+           + ((v[13] - v[11]) * rx + (v[25] - v[23]) * fac.x) * fac.y) * fac.z;
+    g = f3((0.5f * gx) / m.res, (0.5f * gy) / m.res, (0.5f * gz) / m.res);
+    return true;
+}
+
 // Map::getData<Safe::On> on a multi-res map: the data at the block's current scale.
 template <int S>
 __device__ __forceinline__ void mr_map_get_data(const MapDevice& m, F3 p, float& t, float& w)
@@ -338,11 +428,11 @@ __device__ __forceinline__ bool mr_field_grad(const MapDevice& m, F3 p_W, F3& g)
 // returned scale is the one of the last successful interpolation (0 for single-res maps).
 template <int S, bool MR>
 __device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockCache& c, F3 o, F3 d, float t_near,
-                             float t_far, F3& hit, int& scale_out)
+                             float t_far, F3& hit, int& scale_out, float* stack = nullptr, int stride = 1)
 {
     int scale_tt = 0;
     float t_min, t_max;
-    first_block(m, rp, o, d, t_near, t_far, t_min, t_max);
+    first_block(m, rp, o, d, t_near, t_far, t_min, t_max, stack, stride);
     if (t_min <= 0.0f)
         return false;
     const float step = m.res;
