@@ -207,11 +207,21 @@ __device__ __forceinline__ void map_get_data(const MapDevice& m, BlockCache& c, 
 
 // visitor::getInterp single-res: any unallocated block or invalid voxel gives nullopt.
 template <int S>
+__device__ bool field_interp_vf(const MapDevice& m, BlockCache& c, F3 vf, float& out);
+
+template <int S>
 __device__ bool field_interp(const MapDevice& m, BlockCache& c, F3 p_W, float& out)
 {
     F3 vf;
     if (!point_to_voxel_f(m, p_W, vf))
         return false;
+    return field_interp_vf<S>(m, c, vf, out);
+}
+
+// field_interp from the point's voxel coordinates (point_to_voxel_f, inside the map).
+template <int S>
+__device__ bool field_interp_vf(const MapDevice& m, BlockCache& c, F3 vf, float& out)
+{
     const F3 bf = f3(vf.x - 0.5f, vf.y - 0.5f, vf.z - 0.5f);
     const int b0 = (int) bf.x, b1 = (int) bf.y, b2 = (int) bf.z;
     if (b0 < 0 || b1 < 0 || b2 < 0 || b0 + 1 >= m.size || b1 + 1 >= m.size || b2 + 1 >= m.size)
@@ -453,10 +463,20 @@ __device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockC
     // every step is at least res > 0, so the march ends at t_far (NaN poses end it at once)
     for (; t < t_far; t += stepsize) {
         float f, w;
-        if constexpr (MR)
+        // single-res: the sample's voxel coordinates serve both the data lookup (their integer
+        // part, point_to_voxel) and the interpolation below
+        F3 vf;
+        bool in_map = false;
+        if constexpr (MR) {
             mr_map_get_data<S>(m, p, f, w);
-        else
-            map_get_data<S>(m, c, p, f, w);
+        }
+        else {
+            in_map = point_to_voxel_f(m, p, vf);
+            f = 1.0f;
+            w = 0.0f;
+            if (in_map)
+                fetch_voxel<S>(m, c, (int) vf.x, (int) vf.y, (int) vf.z, f, w);
+        }
         if (!(w != 0.0f)) {
             stepsize = largestep;
             p = add(p, mul(stepsize, d));
@@ -471,7 +491,7 @@ __device__ bool raycast_tsdf(const MapDevice& m, const RaycastParams& rp, BlockC
             if constexpr (MR)
                 ok = mr_field_interp<S>(m, p, fi, &scale_tt);
             else
-                ok = field_interp<S>(m, c, p, fi);
+                ok = in_map && field_interp_vf<S>(m, c, vf, fi);
             if (ok)
                 f_tt = fi;
         }
