@@ -133,9 +133,11 @@ __global__ void __launch_bounds__(256) frustum_kernel(MapDevice m, Pinhole s, co
 
 // FieldData<TSDF>::update (data_field_impl.hpp:39-54) preceded by the voxel's projection test
 // (singleres_tsdf_updater_impl.hpp:57-78). Voxel memory is read only when the update applies;
-// new blocks are written in full (the update doubles as their initialisation).
+// new blocks are written in full (the update doubles as their initialisation). Capped at 64
+// registers (4 CTAs per SM): the extra warps hide more of the depth and voxel load latency than
+// the cap costs.
 template <int S>
-__global__ void __launch_bounds__(256) update_kernel(MapDevice m, Pinhole s, const float* __restrict__ depth,
+__global__ void __launch_bounds__(256, 4) update_kernel(MapDevice m, Pinhole s, const float* __restrict__ depth,
                                                      const IntegrateParams* __restrict__ P)
 {
     const Tf T_CV = P->up.T_CV;
