@@ -59,8 +59,9 @@ def _traffic(kernel):
     with open(p) as f:
         for line in f:
             parts = line.split()
-            if parts and not line.startswith("#") and parts[0] == name:
-                return float(parts[4])
+            # name (may hold spaces), launches, read, write, total bytes per launch, us per launch
+            if len(parts) >= 6 and not line.startswith("#") and " ".join(parts[:-5]) == name:
+                return float(parts[-2])
     return None
 
 
@@ -303,6 +304,8 @@ def run_ours(args, ws, rank, local):
         launches_per_frame = kl[dom] / max(len(plain["stats"]), 1)
         algo = float(np.mean(npx)) * 48.0 / launches_per_frame
     elif dom == "raycast":
+        # outputs only here; with the CPU baseline run, the voxels the oracle's raycast reads are
+        # added below (W H 25 + N_touched S_v)
         algo = W * H * 25.0
     avg_launch_ms = kms[dom] / max(kl[dom], 1)
     achieved = (algo / (avg_launch_ms * 1e-3) / 1e9) if algo else None
@@ -316,7 +319,19 @@ def run_ours(args, ws, rank, local):
                 "avg_launch_us": avg_launch_ms * 1e3,
                 "integration": {"kernel": "update", "avg_launch_us": upd_ms * 1e3,
                                 "algorithmic_bytes_per_launch": float(np.mean(ub)),
-                                "achieved_GBps": float(np.mean(ub)) / (upd_ms * 1e-3) / 1e9 if upd_ms else None}}
+                                "achieved_GBps": float(np.mean(ub)) / (upd_ms * 1e-3) / 1e9 if upd_ms else None,
+                                "frac": float(np.mean(ub)) / (upd_ms * 1e-3) / 1e9 / hbm_peak if upd_ms else None,
+                                "traffic": _traffic("update")}}
+    icp_ms = kms.get("icp_iter", 0.0) / max(kl.get("icp_iter", 1), 1)
+    if icp_ms:
+        # 48 B per pixel of every iteration a tracked frame ran (its working set stays in L2)
+        ib = float(np.mean([sum((W >> l) * (H >> l) * it for l, it in enumerate(st["icp_iterations"]))
+                            for st in plain["stats"]])) * 48.0 / (kl["icp_iter"] / max(len(plain["stats"]), 1))
+        roofline["icp"] = {"kernel": "icp_persistent_kernel", "avg_launch_us": icp_ms * 1e3,
+                           "algorithmic_bytes_per_launch": ib, "achieved_GBps": ib / (icp_ms * 1e-3) / 1e9,
+                           "frac": ib / (icp_ms * 1e-3) / 1e9 / hbm_peak, "traffic": _traffic("icp_iter"),
+                           "iterations_per_frame": float(np.mean([sum(st["icp_iterations"])
+                                                                   for st in plain["stats"]]))}
 
     value = ws * K / (g32_ms * 1e-3)
     out = {
@@ -359,6 +374,17 @@ def run_ours(args, ws, rank, local):
     }
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(frames, poses, sensor_spec, args.warmup, 2 * K, args.cpu_budget_s)
+        touched = out["cpu_baseline"].pop("raycast_voxels_touched", None)
+        rc_ms = kms.get("raycast", 0.0) / max(kl.get("raycast", 1), 1)
+        if touched and rc_ms:
+            rb = W * H * 25.0 + touched * S_v
+            rc = {"kernel": "raycast", "avg_launch_us": rc_ms * 1e3, "algorithmic_bytes_per_launch": rb,
+                  "voxels_touched": touched, "achieved_GBps": rb / (rc_ms * 1e-3) / 1e9,
+                  "frac": rb / (rc_ms * 1e-3) / 1e9 / hbm_peak, "traffic": _traffic("raycast")}
+            out["roofline"]["raycast"] = rc
+            if dom == "raycast":
+                out["roofline"].update(achieved=rc["achieved_GBps"], frac=rc["frac"],
+                                       algorithmic_bytes_per_launch=rb)
         out["lidar_batch"]["cpu_baseline"] = lidar_cpu_baseline(lidar_data)
         if args.precision_frames > 0:
             out["precision_vs_f64"] = _precision_report(se, torch, torch.device("cuda", local),
@@ -706,7 +732,7 @@ def lidar_cpu_baseline(data, budget_s=20.0):
 
 # --------------------------------------------------------------------- CPU oracle arm --
 
-def _oracle_pipeline(frames, poses, spec, n_warm, n_steps, budget_s=None):
+def _oracle_pipeline(frames, poses, spec, n_warm, n_steps, budget_s=None, touched=None):
     """Run the oracle (OpenMP, all host threads) pipeline: integrate frame 0, run frames
     1..n_warm untimed, then time up to n_steps frames (stopping once budget_s is spent).
     Returns the per-frame seconds of the timed frames."""
@@ -734,12 +760,17 @@ def _oracle_pipeline(frames, poses, spec, n_warm, n_steps, budget_s=None):
             times.append(time.perf_counter() - t0)
             if budget_s is not None and time.perf_counter() - t_start > budget_s:
                 break
+    if touched is not None:
+        # untimed: the distinct voxels the raycast of the last timed frame reads
+        touched.append(m.raycast_touched(s, T))
     return times
 
 
 def cpu_baseline(frames, poses, spec, n_warm, n_max, budget_s):
-    times = _oracle_pipeline(frames, poses, spec, n_warm, n_max, budget_s)
+    touched = []
+    times = _oracle_pipeline(frames, poses, spec, n_warm, n_max, budget_s, touched)
     return {"value": len(times) / sum(times), "unit": "frames/s", "cores": os.cpu_count(),
+            "raycast_voxels_touched": touched[0] if touched else None,
             "kind": "port",
             "sample": f"{len(times)} frames ({n_warm + 1}..{n_warm + len(times)}: the GPU's timed "
                       f"frames) of the same trajectory, track+integrate+raycast, after replaying "

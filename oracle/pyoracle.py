@@ -131,6 +131,7 @@ def lib():
             "so_dual_marching_cubes": (C.c_longlong, [vp, C.c_int, vp, vp, C.c_longlong]),
             "so_occ_dual_marching_cubes": (C.c_longlong, [vp, C.c_int, vp, vp, C.c_longlong]),
             "so_dual_groups": (None, [i32p, i32p, i32p, i32p]),
+            "so_raycast_touched": (C.c_longlong, [vp, C.POINTER(Pinhole), f32p]),
             "so_map_set_mr_block": (None, [vp, i32p, f32p, f32p, C.c_int, C.c_int]),
             "so_occ_set_block": (None, [vp, i32p, C.c_int, C.c_int, f32p]),
             "so_downsample_depth": (None, [f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, vp]),
@@ -356,6 +357,10 @@ class OracleMap:
         lib().so_raycast_volume(self.h, C.byref(sensor), _m16(T_WS), pts.reshape(n * 3),
                                 nrm.reshape(n * 3), scale.reshape(n))
         return pts, nrm, scale
+
+    def raycast_touched(self, sensor: Pinhole, T_WS) -> int:
+        """Distinct voxels the raycast at T_WS reads (single-res maps)."""
+        return int(lib().so_raycast_touched(self.h, C.byref(sensor), _m16(T_WS)))
 
     def num_blocks(self) -> int:
         return int(lib().so_map_num_blocks(self.h))

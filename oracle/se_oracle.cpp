@@ -85,9 +85,22 @@ struct so_map {
 
 namespace {
 
+/* Measurement hook: when set (per thread), every single-res voxel read below appends the voxel's
+ * linear index, so that so_raycast_touched can count the distinct voxels a raycast reads. */
+static thread_local std::vector<uint64_t>* g_touched = nullptr;
+
+static inline void touch_voxel(const so_map& m, const int32_t c[3])
+{
+    if (g_touched) {
+        const uint64_t n = (uint64_t) m.octree.size;
+        g_touched->push_back((uint64_t) c[0] + n * ((uint64_t) c[1] + n * (uint64_t) c[2]));
+    }
+}
+
 /* visitor::getData (single-res), visitor_impl.hpp:704-717: block voxel or the default data. */
 static inline bool get_voxel(const so_map& m, const int32_t c[3], float& tsdf, float& weight)
 {
+    touch_voxel(m, c);
     const int o = m.octree.block_at(c);
     if (o < 0) {
         tsdf = 1.0f;
@@ -112,6 +125,7 @@ static inline void get_voxel_hint(const so_map& m, int hint_octant, const int32_
         const BlockData& b = m.octree.blocks[oc.block];
         const int idx =
             (c[0] - oc.coord[0]) + 8 * (c[1] - oc.coord[1]) + 64 * (c[2] - oc.coord[2]);
+        touch_voxel(m, c);
         tsdf = b.tsdf[idx];
         weight = b.weight[idx];
         return;
@@ -1539,6 +1553,29 @@ void so_raycast_volume(const so_map* map, const so_pinhole* sensor_c, const floa
             }
         }
     }
+}
+
+/* The number of distinct voxels so_raycast_volume reads on a single-res map at T_WS (the
+ * algorithmic voxel traffic of the raycast; a measurement aid, not part of the restatement). */
+long long so_raycast_touched(const so_map* map, const so_pinhole* sensor, const float T_WS[16])
+{
+    const Pinhole s = make_pinhole(sensor);
+    const int nt = omp_get_max_threads();
+    std::vector<std::vector<uint64_t>> per((size_t) nt);
+    std::vector<float> pts((size_t) s.w * s.h * 3), nrm(pts.size());
+    std::vector<int8_t> sc((size_t) s.w * s.h);
+    // the raycast's parallel loop runs on the same pool threads that set their hook here
+    omp_set_dynamic(0);
+#pragma omp parallel num_threads(nt)
+    g_touched = &per[(size_t) omp_get_thread_num()];
+    so_raycast_volume(map, sensor, T_WS, pts.data(), nrm.data(), sc.data());
+#pragma omp parallel num_threads(nt)
+    g_touched = nullptr;
+    std::vector<uint64_t> all;
+    for (auto& v : per)
+        all.insert(all.end(), v.begin(), v.end());
+    std::sort(all.begin(), all.end());
+    return (long long) (std::unique(all.begin(), all.end()) - all.begin());
 }
 
 /* Tracker::track(depth, T_WS, pts, nrm), tracker_impl.hpp:30-116 */

@@ -97,6 +97,8 @@ void so_integrate_depth(so_map* map, const float* depth, const so_pinhole* senso
                         const float T_WC[16], int timestamp, so_integrate_stats* stats);
 
 /* se::raycaster::raycast_volume. pts/nrm are width*height*3 floats, scale width*height. */
+/* Distinct voxels the single-res raycast reads at T_WS (a measurement aid). */
+long long so_raycast_touched(const so_map* map, const so_pinhole* sensor, const float T_WS[16]);
 void so_raycast_volume(const so_map* map, const so_pinhole* sensor, const float T_WS[16],
                        float* pts_W, float* nrm_W, int8_t* scale);
 
