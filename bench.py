@@ -356,9 +356,10 @@ def run_ours(args, ws, rank, local):
         "roofline": roofline,
         "e2e": {"value": ws * K / e2e_max, "unit": "frames/s", "h2d_bytes_per_step": W * H * 4,
                 "d2h_bytes_per_step": 52},
-        # per tracked frame: bilateral 1 + track 7 (init, 2 half-samples, points, normals, the
-        # persistent ICP, check) + integrate 4 (prep, carve, frustum, update) + raycast 2
-        "gpu_launches": 14 * K,
+        # per tracked frame: bilateral 1 + track 3 (state init with the depth pyramid, points
+        # with normals, the persistent ICP with its pose check) + integrate 4 (prep, carve,
+        # frustum, update) + raycast 2 (prep, raycast)
+        "gpu_launches": 10 * K,
         "kernel_ms_per_frame_plain": {k: v / K for k, v in kms.items()},
         "kernel_launches": kl,
         "voxels_per_s": float(np.mean(upd)) * K / (g32_ms * 1e-3),

@@ -47,6 +47,7 @@ struct TrackState {
     float ref_f[12];     // T_WS_ref
     float last_red[32];  // final reduction of the last iteration run
     unsigned int ticket;
+    unsigned int end_ticket; // CTAs done with the persistent kernel (the last one runs the check)
 };
 constexpr size_t kTrackReadback = sizeof(float) * 12 + sizeof(int) * kNumFlags;
 
@@ -162,20 +163,16 @@ __device__ __forceinline__ void acc_clear(unsigned long long* buf, int tid, int 
         buf[(size_t) (i >> 1) * kAccStride + (i & 1)] = 0ull;
 }
 
-// half_sample_robust_image (src/map/preprocessor.cpp:156-195)
-__global__ void half_sample_kernel(const float* __restrict__ in, int in_w, int in_h, float e_d, int radius,
-                                   float* __restrict__ out)
+// half_sample_robust_image (src/map/preprocessor.cpp:156-195) for output pixel (x, y) with
+// radius 1: the mean of the 2 x 2 input pixels within e_d of the top-left one.
+__device__ __forceinline__ float half_sample_px(const float* __restrict__ in, int in_w, int ow, int oh, float e_d,
+                                                int x, int y)
 {
-    const int ow = in_w / 2, oh = in_h / 2;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= ow || y >= oh)
-        return;
     const int px = 2 * x, py = 2 * y;
     float count = 0.0f, sum = 0.0f;
     const float centre = in[px + py * in_w];
-    for (int i = -radius + 1; i <= radius; ++i) {
-        for (int j = -radius + 1; j <= radius; ++j) {
+    for (int i = 0; i <= 1; ++i) {
+        for (int j = 0; j <= 1; ++j) {
             int qx = px + j, qy = py + i;
             qx = min(max(qx, 0), 2 * ow - 1);
             qy = min(max(qy, 0), 2 * oh - 1);
@@ -186,34 +183,50 @@ __global__ void half_sample_kernel(const float* __restrict__ in, int in_w, int i
             }
         }
     }
-    out[x + y * ow] = sum / count;
-}
-
-// depth_to_point_cloud (include/se/map/impl/preprocessor_impl.hpp:18-40), all levels
-__global__ void points_kernel(LevelImages li, int levels)
-{
-    const int l = blockIdx.z;
-    if (l >= levels)
-        return;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int w = li.w[l], h = li.h[l];
-    if (x >= w || y >= h)
-        return;
-    const float d = li.depth[l][x + y * w];
-    F3 p = f3(0.0f, 0.0f, 0.0f);
-    if (d > 0.0f)
-        p = mul(d, back_project(li.s[l], (float) x, (float) y));
-    float* o = li.pts[l] + 3 * (size_t) (x + y * w);
-    o[0] = p.x;
-    o[1] = p.y;
-    o[2] = p.z;
+    return sum / count;
 }
 
 __device__ __forceinline__ F3 ld3(const float* p, size_t i) { return f3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
 
-// point_cloud_to_normal<NegY> (src/map/preprocessor.cpp:109-152), all levels
-__global__ void normals_kernel(LevelImages li, int levels, int neg_y)
+// depth_to_point_cloud and point_cloud_to_normal<NegY> for one pixel, straight from the depth
+// image (the points of the pixel and of its four neighbours are formed on the fly with the
+// same float operations as the point image would hold).
+__device__ __forceinline__ F3 depth_point(const float* __restrict__ depth, const Pinhole& s, int w, int i)
+{
+    const float d = depth[i];
+    if (d > 0.0f)
+        return mul(d, back_project(s, (float) (i % w), (float) (i / w)));
+    return f3(0.0f, 0.0f, 0.0f);
+}
+
+// point_cloud_to_normal<NegY> for pixel i, reading the neighbours' points from the depth image
+__device__ __forceinline__ F3 depth_normal(const float* __restrict__ depth, const Pinhole& s, int w, int h, int i,
+                                           int neg_y)
+{
+    const int x = i % w, y = i / w;
+    const F3 p = depth_point(depth, s, w, i);
+    if (p.z == 0.0f)
+        return f3(0.0f, 0.0f, 0.0f);
+    const int lx = max(x - 1, 0), rx = min(x + 1, w - 1);
+    int uy, dy;
+    if (neg_y) {
+        uy = max(y - 1, 0);
+        dy = min(y + 1, h - 1);
+    }
+    else {
+        dy = max(y - 1, 0);
+        uy = min(y + 1, h - 1);
+    }
+    const F3 left = depth_point(depth, s, w, lx + w * y), right = depth_point(depth, s, w, rx + w * y);
+    const F3 up = depth_point(depth, s, w, x + w * uy), down = depth_point(depth, s, w, x + w * dy);
+    if (left.z == 0.0f || right.z == 0.0f || up.z == 0.0f || down.z == 0.0f)
+        return f3(0.0f, 0.0f, 0.0f);
+    return normalized(cross(sub(right, left), sub(up, down)));
+}
+
+// depth_to_point_cloud (include/se/map/impl/preprocessor_impl.hpp:18-40) and
+// point_cloud_to_normal<NegY> (src/map/preprocessor.cpp:109-152) for every level, one launch.
+__global__ void points_normals_kernel(LevelImages li, int levels, int neg_y)
 {
     const int l = blockIdx.z;
     if (l >= levels)
@@ -223,29 +236,17 @@ __global__ void normals_kernel(LevelImages li, int levels, int neg_y)
     const int w = li.w[l], h = li.h[l];
     if (x >= w || y >= h)
         return;
-    const float* P = li.pts[l];
-    F3 n = f3(0.0f, 0.0f, 0.0f);
-    const F3 p = ld3(P, x + (size_t) w * y);
-    if (p.z != 0.0f) {
-        const int lx = max(x - 1, 0), rx = min(x + 1, w - 1);
-        int uy, dy;
-        if (neg_y) {
-            uy = max(y - 1, 0);
-            dy = min(y + 1, h - 1);
-        }
-        else {
-            dy = max(y - 1, 0);
-            uy = min(y + 1, h - 1);
-        }
-        const F3 left = ld3(P, lx + (size_t) w * y), right = ld3(P, rx + (size_t) w * y);
-        const F3 up = ld3(P, x + (size_t) w * uy), down = ld3(P, x + (size_t) w * dy);
-        if (!(left.z == 0.0f || right.z == 0.0f || up.z == 0.0f || down.z == 0.0f))
-            n = normalized(cross(sub(right, left), sub(up, down)));
-    }
-    float* o = li.nrm[l] + 3 * (size_t) (x + y * w);
-    o[0] = n.x;
-    o[1] = n.y;
-    o[2] = n.z;
+    const int i = x + w * y;
+    const F3 p = depth_point(li.depth[l], li.s[l], w, i);
+    const F3 n = depth_normal(li.depth[l], li.s[l], w, h, i, neg_y);
+    float* op = li.pts[l] + 3 * (size_t) i;
+    float* on = li.nrm[l] + 3 * (size_t) i;
+    op[0] = p.x;
+    op[1] = p.y;
+    op[2] = p.z;
+    on[0] = n.x;
+    on[1] = n.y;
+    on[2] = n.z;
 }
 
 struct TrackInit {
@@ -254,14 +255,9 @@ struct TrackInit {
 };
 
 // With pose12_in the start pose is read from the device (row-major 3x4) and its inverse is
-// formed here with the same float operations the host would use.
-__global__ void track_init_kernel(TrackState* st, TrackInit init, const float* pose12_in, unsigned long long* acc)
+// formed here with the same float operations the host would use. One thread.
+__device__ void track_init(TrackState* st, TrackInit init, const float* pose12_in)
 {
-    if (acc)
-        for (int b = 0; b < kAccBuffers; ++b)
-            acc_clear(acc + (size_t) b * kAccBufWords, threadIdx.x, blockDim.x);
-    if (threadIdx.x != 0)
-        return;
     if (pose12_in) {
         const Tf T = tf_from12(pose12_in);
         const Tf Ti = inverse_iso(T);
@@ -285,6 +281,59 @@ __global__ void track_init_kernel(TrackState* st, TrackInit init, const float* p
     for (int i = 0; i < kNumFlags; ++i)
         st->flags[i] = 0;
     st->ticket = 0;
+    st->end_ticket = 0;
+}
+
+__global__ void track_init_kernel(TrackState* st, TrackInit init, const float* pose12_in)
+{
+    track_init(st, init, pose12_in);
+}
+
+// The first launch of a track(): block 0 initialises the state and clears the merge
+// accumulators; every thread forms the level-1 depth of its 2 x 2 pixel group and, with three
+// levels, the level-2 depth of the group from those values (half_sample_robust_image twice,
+// the second pass on the first's values). Grid: ceil(w1 / 2) x ceil(h1 / 2) threads (one block
+// when there is no pyramid).
+__global__ void pyramid_init_kernel(TrackState* st, TrackInit init, const float* pose12_in, unsigned long long* acc,
+                                    LevelImages li, int levels, float e_d, float* __restrict__ d1,
+                                    float* __restrict__ d2)
+{
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    if (blockIdx.x == 0 && blockIdx.y == 0) {
+        for (int b = 0; b < kAccBuffers; ++b)
+            acc_clear(acc + (size_t) b * kAccBufWords, tid, blockDim.x * blockDim.y);
+        if (tid == 0)
+            track_init(st, init, pose12_in);
+    }
+    if (levels < 2)
+        return;
+    const int x2 = blockIdx.x * blockDim.x + threadIdx.x, y2 = blockIdx.y * blockDim.y + threadIdx.y;
+    const int w1 = li.w[1], h1 = li.h[1];
+    float v[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+        for (int dx = 0; dx < 2; ++dx) {
+            const int x1 = 2 * x2 + dx, y1 = 2 * y2 + dy;
+            if (x1 < w1 && y1 < h1) {
+                v[dy][dx] = half_sample_px(li.depth[0], li.w[0], w1, h1, e_d, x1, y1);
+                d1[x1 + y1 * w1] = v[dy][dx];
+            }
+        }
+    if (levels < 3 || x2 >= li.w[2] || y2 >= li.h[2])
+        return;
+    // the 2 x 2 level-1 pixels of this output are in range (2 x2 + 1 <= 2 w2 - 1): no clamping
+    const float centre = v[0][0];
+    float count = 0.0f, sum = 0.0f;
+#pragma unroll
+    for (int i = 0; i <= 1; ++i)
+#pragma unroll
+        for (int j = 0; j <= 1; ++j)
+            if (fabsf(v[i][j] - centre) < e_d) {
+                count += 1.0f;
+                sum += v[i][j];
+            }
+    d2[x2 + y2 * li.w[2]] = sum / count;
 }
 
 // ---------------------------------------------------------------------- FP64 solve --
@@ -674,7 +723,7 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
 }
 
 // checkPoseKernel (icp.cpp:227-246): revert to the reference pose on a poor final alignment.
-__global__ void icp_check_kernel(TrackState* st, int W, int H, float track_threshold, float* pose12_out)
+__device__ void icp_check(TrackState* st, int W, int H, float track_threshold, float* pose12_out)
 {
     const float* v = st->last_red;
     // a timed-out grid barrier of the persistent ICP leaves no trustworthy pose: reject it
@@ -692,6 +741,11 @@ __global__ void icp_check_kernel(TrackState* st, int W, int H, float track_thres
             pose12_out[i] = st->pose_f[i];
 }
 
+__global__ void icp_check_kernel(TrackState* st, int W, int H, float track_threshold, float* pose12_out)
+{
+    icp_check(st, W, H, track_threshold, pose12_out);
+}
+
 // ------------------------------------------------------- persistent ICP (all iterations) --
 // The per-iteration launches above, fused into one cooperative launch per frame: every CTA
 // runs every iteration of every level; after each iteration's main pass the CTAs meet at a
@@ -706,6 +760,9 @@ struct IcpLevels {
     int iters[3];
     int levels;
     unsigned* sm_slots; // per-SM arrival counters (kIcpSlotCounters, never reset)
+    int W, H;           // checkPoseKernel's image size and threshold, and where the pose goes
+    float track_threshold;
+    float* pose12_out;
 };
 
 constexpr int kIcpSlotCounters = 1024;
@@ -855,6 +912,14 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_persistent_kernel(Pinhol
         const int i = threadIdx.x, r = i >> 2, c = i & 3;
         st->pose_f[i] = c < 3 ? T.R[3 * r + c] : T.t[r];
     }
+    // checkPoseKernel by the last CTA to finish: it sees the final pose and every flag
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0 && atomicAdd(&st->end_ticket, 1u) == gridDim.x - 1) {
+        __threadfence();
+        icp_check(st, L.W, L.H, L.track_threshold, L.pose12_out);
+        st->end_ticket = 0;
+    }
 }
 
 } // namespace se_gpu
@@ -988,23 +1053,27 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
     li.depth[0] = depth_dev;
     {
     ProfScope ps(kProfTrackPrep, stream);
-    track_init_kernel<<<1, 256, 0, stream>>>(t->state, init, pose_in, t->acc);
     const float e_d = 0.1f * 3;
-    for (int l = 1; l < t->levels; ++l) {
-        dim3 b(32, 8), g((li.w[l] + 31) / 32, (li.h[l] + 7) / 8);
-        half_sample_kernel<<<g, b, 0, stream>>>(li.depth[l - 1], li.w[l - 1], li.h[l - 1], e_d, 1,
-                                                t->pyr_depth[l]);
+    {
+        // one thread per 2 x 2 group of level-1 pixels (a single block without a pyramid)
+        const dim3 b(32, 8);
+        const dim3 g(t->levels > 1 ? ((li.w[1] + 1) / 2 + 31) / 32 : 1, t->levels > 1 ? ((li.h[1] + 1) / 2 + 7) / 8 : 1);
+        pyramid_init_kernel<<<g, b, 0, stream>>>(t->state, init, pose_in, t->acc, li, t->levels, e_d,
+                                                 t->pyr_depth[1], t->pyr_depth[2]);
     }
     {
-        dim3 b(32, 8), g((li.w[0] + 31) / 32, (li.h[0] + 7) / 8, t->levels);
-        points_kernel<<<g, b, 0, stream>>>(li, t->levels);
-        normals_kernel<<<g, b, 0, stream>>>(li, t->levels, t->s.left_hand);
+        const dim3 b(32, 8), g((li.w[0] + 31) / 32, (li.h[0] + 7) / 8, t->levels);
+        points_normals_kernel<<<g, b, 0, stream>>>(li, t->levels, t->s.left_hand);
     }
     }
     IcpLevels L;
     std::memset(&L, 0, sizeof(L));
     L.levels = t->levels;
     L.sm_slots = t->sm_slots;
+    L.W = t->sensor.width;
+    L.H = t->sensor.height;
+    L.track_threshold = t->config.track_threshold;
+    L.pose12_out = T_WS ? nullptr : pose12_io;
     for (int level = t->levels - 1; level >= 0; --level) {
         IterParams& ip = L.ip[level];
         ip.ref_pts = ref_pts;
@@ -1043,7 +1112,7 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
                                                                                t->acc);
             }
     }
-    {
+    if (!t->persistent) { // the persistent kernel runs the check itself
         ProfScope ps(kProfIcpCheck, stream);
         icp_check_kernel<<<1, 1, 0, stream>>>(t->state, t->sensor.width, t->sensor.height,
                                               t->config.track_threshold, T_WS ? nullptr : pose12_io);
@@ -1159,38 +1228,6 @@ struct NoAllocScratch {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
 // depth_to_point_cloud for pixel i of the full-resolution image
-__device__ __forceinline__ F3 depth_point(const float* __restrict__ depth, const Pinhole& s, int w, int i)
-{
-    const float d = depth[i];
-    if (d > 0.0f)
-        return mul(d, back_project(s, (float) (i % w), (float) (i / w)));
-    return f3(0.0f, 0.0f, 0.0f);
-}
-
-// point_cloud_to_normal<NegY> for pixel i, reading the neighbours' points from the depth image
-__device__ __forceinline__ F3 depth_normal(const float* __restrict__ depth, const Pinhole& s, int w, int h, int i,
-                                           int neg_y)
-{
-    const int x = i % w, y = i / w;
-    const F3 p = depth_point(depth, s, w, i);
-    if (p.z == 0.0f)
-        return f3(0.0f, 0.0f, 0.0f);
-    const int lx = max(x - 1, 0), rx = min(x + 1, w - 1);
-    int uy, dy;
-    if (neg_y) {
-        uy = max(y - 1, 0);
-        dy = min(y + 1, h - 1);
-    }
-    else {
-        dy = max(y - 1, 0);
-        uy = min(y + 1, h - 1);
-    }
-    const F3 left = depth_point(depth, s, w, lx + w * y), right = depth_point(depth, s, w, rx + w * y);
-    const F3 up = depth_point(depth, s, w, x + w * uy), down = depth_point(depth, s, w, x + w * dy);
-    if (left.z == 0.0f || right.z == 0.0f || up.z == 0.0f || down.z == 0.0f)
-        return f3(0.0f, 0.0f, 0.0f);
-    return normalized(cross(sub(right, left), sub(up, down)));
-}
 
 // icp_iter_kernel with its inputs formed from the depth image and its scratch in the static
 // array (same per-pixel terms, reduction order and FP64 tail).
@@ -1388,7 +1425,7 @@ extern "C" se_gpu_status se_gpu_track_noalloc(const se_gpu_pinhole* sensor, cons
         init.T_WS[4 * i + 3] = T.t[i];
         init.ref_inv[4 * i + 3] = Ti.t[i];
     }
-    track_init_kernel<<<1, 1, 0, stream>>>(&scratch->state, init, nullptr, nullptr);
+    track_init_kernel<<<1, 1, 0, stream>>>(&scratch->state, init, nullptr);
     IterParams ip;
     ip.ref_pts = ref_pts;
     ip.ref_nrm = ref_nrm;
