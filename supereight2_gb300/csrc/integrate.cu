@@ -43,8 +43,24 @@ __global__ void integrate_prep_kernel(MapDevice m, float trunc_factor, Pinhole s
     reinterpret_cast<unsigned long long*>(counters)[kCntUpdated / 2] = 0ull;
 }
 
+// (int) (x / res) for 0 <= x (a coordinate inside the map), as point_to_voxel computes it, with
+// the IEEE division only where it can matter: q = x (1/res) is within 2^-23 q of x / res (and so
+// is the rounded quotient), so when q is more than q 2^-20 away from every integer both
+// truncate to the same voxel; closer to an integer the division decides.
+__device__ __forceinline__ int voxel_of(float x, float res, float inv_res)
+{
+    const float q = x * inv_res;
+    const float f = q - truncf(q);
+    const float tol = q * 0x1p-20f;
+    if (f > tol && f < 1.0f - tol)
+        return (int) q;
+    return (int) (x / res);
+}
+
 // RaycastCarver::operator() hot loop. A CTA covers a 32 x 8 pixel tile, one warp per row
-// segment, so the 8 samples of neighbouring rays fall in few distinct blocks.
+// segment, so the 8 samples of neighbouring rays fall in few distinct blocks. Lanes whose
+// samples share a block are found by matching packed block coordinates; only the first of them
+// forms the Morton key, and only when the block is not allocated yet.
 __global__ void __launch_bounds__(256) carve_kernel(MapDevice m, Pinhole s, const float* __restrict__ depth,
                                                     const IntegrateParams* __restrict__ P)
 {
@@ -72,28 +88,32 @@ __global__ void __launch_bounds__(256) carve_kernel(MapDevice m, Pinhole s, cons
         pos = sub(point_W, mul(cp.half_band, rev));
         step = divs(mul(rev, cp.band), (float) cp.num_steps);
     }
+    const float inv_res = 1.0f / m.res;
     for (int i = 0; i < cp.num_steps; ++i) {
-        uint64_t key = kEmptyKey;
+        unsigned long long packed = ~0ull; // no block
         int vx = 0, vy = 0, vz = 0;
         if (valid) {
-            if (point_to_voxel(m, pos, vx, vy, vz)) {
+            // point_to_voxel (se_gpu_internal.cuh) with the division shortcut of voxel_of
+            const F3 p = apply(m.T_MW, pos);
+            if (p.x >= 0.0f && p.x < m.dim && p.y >= 0.0f && p.y < m.dim && p.z >= 0.0f && p.z < m.dim) {
                 // p < dim = size * res exactly, so v < size; the mask keeps the index in range
                 // regardless (the reference's octree descent ignores bits >= size too)
-                vx &= m.size - 1;
-                vy &= m.size - 1;
-                vz &= m.size - 1;
-                key = block_key(vx, vy, vz);
+                vx = voxel_of(p.x, m.res, inv_res) & (m.size - 1);
+                vy = voxel_of(p.y, m.res, inv_res) & (m.size - 1);
+                vz = voxel_of(p.z, m.res, inv_res) & (m.size - 1);
+                packed = (unsigned long long) (vx >> 3) | ((unsigned long long) (vy >> 3) << 21)
+                    | ((unsigned long long) (vz >> 3) << 42);
             }
             pos = add(pos, step);
         }
-        const unsigned peers = __match_any_sync(0xffffffffu, (unsigned long long) key);
-        if (key != kEmptyKey && lane == __ffs(peers) - 1) {
+        const unsigned peers = __match_any_sync(0xffffffffu, packed);
+        if (packed != ~0ull && lane == __ffs(peers) - 1) {
             const int bx = vx >> 3, by = vy >> 3, bz = vz >> 3;
             // plain (coherent) load: entries are being published by this kernel; a stale -1
             // only costs a probe of the hash, which is the allocation arbiter
             const int idx = m.block_index[((size_t) bz << (2 * m.log2_bps)) | ((size_t) by << m.log2_bps) | (size_t) bx];
             if (idx < 0)
-                insert_block(m, key, bx, by, bz);
+                insert_block(m, block_key(vx, vy, vz), bx, by, bz);
         }
     }
 }
