@@ -197,9 +197,17 @@ __global__ void __launch_bounds__(256, 4) update_kernel(MapDevice m, Pinhole s, 
                 pn[u] = sqrtf(sq);
                 mz[u] = p_C.z;
                 pix[u] = -1;
-                // farDist(p) = far / p.normalized().z
-                const float nz = p_C.z / pn[u];
-                if (p_C.z > 0.0f && !(pn[u] > s.far_plane / nz)) {
+                // farDist(p) = far / p.normalized().z; the test |p| > far / (z / |p|) is z > far in
+                // exact arithmetic and the two rounded divisions move it by less than 2^-22
+                // relative, so they only run within 2^-16 of the boundary
+                bool beyond;
+                if (p_C.z < s.far_plane * (1.0f - 0x1p-16f))
+                    beyond = false;
+                else if (p_C.z > s.far_plane * (1.0f + 0x1p-16f))
+                    beyond = true;
+                else
+                    beyond = pn[u] > s.far_plane / (p_C.z / pn[u]);
+                if (p_C.z > 0.0f && !beyond) {
                     float uu, vv;
                     if (project(s, p_C, uu, vv))
                         pix[u] = (int) (uu + 0.5f) + (int) (vv + 0.5f) * s.w;

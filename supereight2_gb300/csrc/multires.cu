@@ -173,8 +173,11 @@ __global__ void __launch_bounds__(256) mr_update_kernel(MapDevice m, Pinhole s, 
             // z <= 0 never passes: z < 0 fails the far test (far / nz < 0), z == 0 the projection
             const float sq = p_C.z > 0.0f ? dot(p_C, p_C) : 0.0f;
             const float pn = sqrtf(sq);
-            const float nz = p_C.z / pn;
-            if (!(p_C.z > 0.0f) || pn > s.far_plane / nz)
+            if (!(p_C.z > 0.0f))
+                continue;
+            // the far test |p| > far / (z / |p|): z > far up to 2^-22 relative (see update_kernel)
+            if (p_C.z > s.far_plane * (1.0f + 0x1p-16f)
+                || (!(p_C.z < s.far_plane * (1.0f - 0x1p-16f)) && pn > s.far_plane / (p_C.z / pn)))
                 continue;
             float u, v;
             if (!project(s, p_C, u, v))
