@@ -258,8 +258,7 @@ def run_ours(args, ws, rank, local):
     torch.cuda.synchronize()
     e0 = time.perf_counter()
     for k in range(K):
-        fp.depth.copy_(host_frames[first_e2e + k], non_blocking=True)
-        fp.run(track=True)
+        fp.run(track=True, depth=host_frames[first_e2e + k])  # host depth copied in on the stream
         T_WS, accepted = fp.pose()  # synchronises: 48 + 4 bytes device -> host
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - e0

@@ -456,6 +456,11 @@ SE_GPU_API se_gpu_status se_gpu_frame_set_pose(se_gpu_frame* frame, const float 
 /* Launch one frame on stream: [track (if track != 0)] + integrate + raycast. Asynchronous;
  * the first call per mode captures the graph (call it before any capture of your own). */
 SE_GPU_API se_gpu_status se_gpu_frame_run(se_gpu_frame* frame, int track, void* stream);
+/* se_gpu_frame_run with the frame's depth image taken from host memory (width*height floats,
+ * copied into the frame's input buffer on stream first; pinned memory keeps the copy
+ * asynchronous), as integrateDepth / track take a host Image<float>. */
+SE_GPU_API se_gpu_status se_gpu_frame_run_host(se_gpu_frame* frame, const float* depth_host, int track,
+                                               void* stream);
 /* Read the device pose (after the runs enqueued on stream) and the last run's acceptance (the
  * checkPoseKernel result; 1 when the last run did not track). Synchronous. */
 SE_GPU_API se_gpu_status se_gpu_frame_get_pose(se_gpu_frame* frame, float T_WS[16],

@@ -145,6 +145,7 @@ SIGNATURES = {
                                        C.POINTER(_VP)]),
     "se_gpu_frame_set_pose": (C.c_int, [_VP, _F16, C.c_int]),
     "se_gpu_frame_run": (C.c_int, [_VP, C.c_int, _VP]),
+    "se_gpu_frame_run_host": (C.c_int, [_VP, _VP, C.c_int, _VP]),
     "se_gpu_frame_get_pose": (C.c_int, [_VP, _F16, C.POINTER(C.c_int), _VP]),
     "se_gpu_profiling_enable": (C.c_int, [C.c_int]),
     "se_gpu_profiling_read": (C.c_int, [C.c_int, _VP, _VP, C.c_int]),
@@ -809,9 +810,26 @@ class FramePipeline:
         _, tp = _m16(T_WS)
         _check(self._L.se_gpu_frame_set_pose(self.h, tp, int(timestamp)), "se_gpu_frame_set_pose")
 
-    def run(self, track=True, stream=None):
-        _check(self._L.se_gpu_frame_run(self.h, 1 if track else 0, _stream(stream)),
-               "se_gpu_frame_run")
+    def run(self, track=True, stream=None, depth=None):
+        """One frame: [track] + integrate + raycast, asynchronous on stream. With ``depth`` (a
+        host float32 H x W array or CPU tensor, pinned for an asynchronous copy) the frame's
+        input is copied from it first; otherwise ``self.depth`` holds it."""
+        if depth is None:
+            _check(self._L.se_gpu_frame_run(self.h, 1 if track else 0, _stream(stream)), "se_gpu_frame_run")
+            return
+        if hasattr(depth, "is_cuda"):
+            if depth.is_cuda or depth.dtype != self.depth.dtype or not depth.is_contiguous():
+                raise SeGpuError("depth must be a contiguous float32 host tensor")
+            if tuple(depth.shape) != tuple(self.depth.shape):
+                raise SeGpuError("depth has the wrong shape")
+            ptr = depth.data_ptr()
+        else:
+            depth = np.ascontiguousarray(depth, np.float32)
+            if depth.shape != tuple(self.depth.shape):
+                raise SeGpuError("depth has the wrong shape")
+            ptr = depth.ctypes.data
+        _check(self._L.se_gpu_frame_run_host(self.h, C.c_void_p(ptr), 1 if track else 0, _stream(stream)),
+               "se_gpu_frame_run_host")
 
     def pose(self, stream=None):
         T = np.zeros(16, np.float32)

@@ -208,6 +208,17 @@ se_gpu_status se_gpu_frame_run(se_gpu_frame* f, int track, void* stream_p)
     return SE_GPU_OK;
 }
 
+se_gpu_status se_gpu_frame_run_host(se_gpu_frame* f, const float* depth_host, int track, void* stream_p)
+{
+    if (!f || !depth_host) {
+        set_last_error("se_gpu_frame_run_host: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    const size_t bytes = (size_t) f->sensor.width * (size_t) f->sensor.height * sizeof(float);
+    SE_CUDA_TRY(cudaMemcpyAsync(f->depth, depth_host, bytes, cudaMemcpyHostToDevice, (cudaStream_t) stream_p));
+    return se_gpu_frame_run(f, track, stream_p);
+}
+
 se_gpu_status se_gpu_frame_get_pose(se_gpu_frame* f, float T_WS[16], int* accepted, void* stream_p)
 {
     if (!f || !T_WS) {

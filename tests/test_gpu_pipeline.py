@@ -29,16 +29,20 @@ def _run_plain(gpu, sensor, poses, frames, storage):
     return m, out, pts.cpu().numpy(), nrm.cpu().numpy()
 
 
-def _run_graph(gpu, sensor, poses, frames, storage):
+def _run_graph(gpu, sensor, poses, frames, storage, from_host=False):
     import torch
     m = gpu.Map(10.24, 0.02, max_blocks=1 << 16, storage=storage)
     tr = gpu.Tracker(m, sensor)
     fp = gpu.FramePipeline(m, sensor, tr)
     fp.set_pose(poses[0].astype(np.float32), 0)
     out = []
+    host = [torch.from_numpy(d).pin_memory() for d in frames] if from_host else None
     for i, d in enumerate(frames):
-        fp.depth.copy_(torch.from_numpy(d).cuda())
-        fp.run(track=i > 0)
+        if from_host:
+            fp.run(track=i > 0, depth=host[i])   # se_gpu_frame_run_host: host depth in
+        else:
+            fp.depth.copy_(torch.from_numpy(d).cuda())
+            fp.run(track=i > 0)
         out.append(fp.pose())
     torch.cuda.synchronize()
     return m, out, fp.points_W.cpu().numpy(), fp.normals_W.cpu().numpy()
@@ -65,6 +69,18 @@ def test_graph_pipeline_bit_identical_to_blocking_calls(gpu, data, storage):
     assert np.array_equal(k1[o1_], k2[o2_])
     assert np.array_equal(t1[o1_], t2[o2_]) and np.array_equal(w1[o1_], w2[o2_])
     assert np.array_equal(ts1[o1_], ts2[o2_])
+    assert np.array_equal(p1, p2) and np.array_equal(n1, n2)
+
+
+def test_graph_pipeline_from_host_depth(gpu, data):
+    """The host-depth entry (copy into the frame's input on the stream, then the graph) gives
+    the same poses and raycast as writing the device input buffer first."""
+    spec, scene, poses, frames = data
+    sensor = gpu.PinholeCamera.from_spec(spec)
+    _, o1, p1, n1 = _run_graph(gpu, sensor, poses, frames, "f32")
+    _, o2, p2, n2 = _run_graph(gpu, sensor, poses, frames, "f32", from_host=True)
+    for (T1, a1), (T2, a2) in zip(o1, o2):
+        assert a1 == a2 and np.array_equal(T1, T2)
     assert np.array_equal(p1, p2) and np.array_equal(n1, n2)
 
 
