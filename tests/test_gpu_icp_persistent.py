@@ -37,3 +37,34 @@ def test_persistent_equals_per_iteration(gpu, icp_threshold):
     if icp_threshold == 0.0:
         assert i1 == (10, 5, 4)
     assert np.linalg.norm(T1[:3, 3] - poses[1][:3, 3]) < 0.01
+
+
+@pytest.mark.parametrize("persistent", [True, False])
+def test_merge_overflow_is_reported(gpu, persistent):
+    """A partial sum outside the exact merge's range (here: a fronto-parallel plane 3e5 m from
+    the world origin, so that |p_W x n|^2 summed over a CTA's 256 pixels exceeds 2^42) is not
+    silently wrapped: the call reports an error and the pose stays the input pose."""
+    import torch
+    W, H = 128, 96
+    sensor = gpu.PinholeCamera(width=W, height=H, fx=100.0, fy=100.0, cx=63.5, cy=47.5,
+                               near_plane=0.1, far_plane=10.0)
+    depth = np.full((H, W), 2.0, np.float32)
+    T = np.eye(4, dtype=np.float32)
+    T[0, 3] = 3.0e5
+    v, u = np.meshgrid(np.arange(H, dtype=np.float32), np.arange(W, dtype=np.float32), indexing="ij")
+    p_S = np.stack([(u - np.float32(63.5)) / np.float32(100.0) * depth,
+                    (v - np.float32(47.5)) / np.float32(100.0) * depth, depth], -1).astype(np.float32)
+    p_W = (p_S + T[:3, 3]).astype(np.float32)
+    n_ref = np.zeros_like(p_W)
+    n_ref[..., 2] = -1.0
+    m = gpu.Map(10.24, 0.02, max_blocks=1 << 10)
+    tr = gpu.Tracker(m, sensor)
+    tr.set_persistent(persistent)
+    T_in = T.copy()
+    with pytest.raises(gpu.SeGpuError, match="exact merge"):
+        tr.track(torch.from_numpy(depth).cuda(), T, torch.from_numpy(p_W).cuda(), torch.from_numpy(n_ref).cuda())
+    assert np.array_equal(T, T_in)
+    # the same plane near the origin stays within range: no error (a single plane leaves the
+    # system rank-deficient, so only the absence of the overflow report is checked)
+    T2 = np.eye(4, dtype=np.float32)
+    tr.track(torch.from_numpy(depth).cuda(), T2, torch.from_numpy(p_S.copy()).cuda(), torch.from_numpy(n_ref).cuda())
