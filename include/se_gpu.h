@@ -405,6 +405,10 @@ SE_GPU_API se_gpu_status se_gpu_track(se_gpu_tracker* tracker, const float* dept
  * give bit-identical poses. A barrier that times out rejects the frame's pose (accepted = 0)
  * and se_gpu_track returns SE_GPU_ERR_CUDA. */
 SE_GPU_API se_gpu_status se_gpu_tracker_set_persistent(se_gpu_tracker* tracker, int enable);
+/* Test aid for the failure path: with enable != 0 the persistent ICP's grid barrier waits for
+ * one CTA more than the grid holds, so its bounded wait runs out (half a second), the frame's
+ * pose is rejected and se_gpu_track returns SE_GPU_ERR_CUDA; the context stays usable. */
+SE_GPU_API se_gpu_status se_gpu_tracker_test_barrier_timeout(se_gpu_tracker* tracker, int enable);
 /* Final 32-float reduction of the last track (icp.cpp:45-204 layout: [sum e^2, J^T e (6),
  * upper J^T J (21), inliers, distance rejects, normal rejects, other]) and the iterations run
  * per level. Synchronous. */

@@ -103,6 +103,7 @@ SIGNATURES = {
     "se_gpu_integrate_range": (C.c_int, [_VP, _VP, C.POINTER(_Lidar), _F16, C.c_int, _VP]),
     "se_gpu_bilateral_filter": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.POINTER(_BilateralConfig), _VP]),
     "se_gpu_tracker_set_persistent": (C.c_int, [_VP, C.c_int]),
+    "se_gpu_tracker_test_barrier_timeout": (C.c_int, [_VP, C.c_int]),
     "se_gpu_marching_cube": (C.c_int, [_VP, _VP, C.c_int64, C.POINTER(C.c_int64), _VP]),
     "se_gpu_dual_marching_cube": (C.c_int, [_VP, C.c_int, _VP, _VP, C.c_int64, C.POINTER(C.c_int64), _VP]),
     "se_gpu_mc_case_table": (C.c_int, [_VP, _VP]),
@@ -610,6 +611,12 @@ class Tracker:
     def set_persistent(self, enable=True):
         """One cooperative launch per track() (default when it fits) or one launch per ICP iteration."""
         _check(self._L.se_gpu_tracker_set_persistent(self.h, 1 if enable else 0), "se_gpu_tracker_set_persistent")
+
+    def test_barrier_timeout(self, enable=True):
+        """Test aid: make the persistent ICP's bounded grid barrier time out (the frame's pose is
+        rejected and track() raises SeGpuError)."""
+        _check(self._L.se_gpu_tracker_test_barrier_timeout(self.h, 1 if enable else 0),
+               "se_gpu_tracker_test_barrier_timeout")
 
     def last_reduction(self):
         red = (C.c_float * 32)()

@@ -763,11 +763,20 @@ struct IcpLevels {
     int W, H;           // checkPoseKernel's image size and threshold, and where the pose goes
     float track_threshold;
     float* pose12_out;
+    int missing_ctas;   // test aid: CTAs the barrier waits for beyond the grid (0 in use)
 };
 
 constexpr int kIcpSlotCounters = 1024;
 
-constexpr unsigned kIcpSpinLimit = 1u << 22; // ~0.3 s of polling at most, then the timeout flag
+constexpr unsigned kIcpSpinLimit = 1u << 22;                // polls at most, and
+constexpr unsigned long long kIcpWaitNs = 500000000ull;     // half a second at most, then the timeout flag
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // Grid barrier on a monotonic counter (reset to 0 before the launch): every CTA adds one and
 // waits until the count reaches target. Bounded: on timeout (or when another CTA timed out)
@@ -779,8 +788,9 @@ __device__ __forceinline__ void icp_grid_sync(unsigned* ctr, unsigned target, in
     if (threadIdx.x == 0) {
         atomicAdd(ctr, 1u);
         unsigned spins = 0;
+        const unsigned long long t0 = global_ns();
         while (*((volatile unsigned*) ctr) < target) {
-            if (*((volatile int*) timeout) != 0 || ++spins > kIcpSpinLimit) {
+            if (*((volatile int*) timeout) != 0 || ++spins > kIcpSpinLimit || global_ns() - t0 > kIcpWaitNs) {
                 atomicExch(timeout, 1);
                 break;
             }
@@ -875,7 +885,7 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_persistent_kernel(Pinhol
                 }
             }
             ++phase;
-            icp_grid_sync(&st->ticket, phase * gridDim.x, &st->flags[kFlagBarrierTimeout]);
+            icp_grid_sync(&st->ticket, phase * (gridDim.x + L.missing_ctas), &st->flags[kFlagBarrierTimeout]);
             // every CTA: the merged totals, then the solve and update. The buffer used two phases
             // ago has been read by every CTA before this barrier: CTA 0 clears it for the phase
             // after next.
@@ -940,6 +950,7 @@ struct se_gpu_tracker {
     TrackState* state;
     int nctas[3];
     int persistent;      // one cooperative launch per frame (when the grid fits on the GPU)
+    int missing_ctas;    // se_gpu_tracker_test_barrier_timeout
     int persistent_ctas; // its grid: the largest level's CTA count
 };
 
@@ -1074,6 +1085,7 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
     L.H = t->sensor.height;
     L.track_threshold = t->config.track_threshold;
     L.pose12_out = T_WS ? nullptr : pose12_io;
+    L.missing_ctas = t->missing_ctas;
     for (int level = t->levels - 1; level >= 0; --level) {
         IterParams& ip = L.ip[level];
         ip.ref_pts = ref_pts;
@@ -1175,6 +1187,16 @@ se_gpu_status se_gpu_tracker_set_persistent(se_gpu_tracker* t, int enable)
         }
     }
     t->persistent = enable ? 1 : 0;
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_tracker_test_barrier_timeout(se_gpu_tracker* t, int enable)
+{
+    if (!t) {
+        set_last_error("se_gpu_tracker_test_barrier_timeout: null tracker");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    t->missing_ctas = enable ? 1 : 0;
     return SE_GPU_OK;
 }
 

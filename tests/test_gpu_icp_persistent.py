@@ -68,3 +68,35 @@ def test_merge_overflow_is_reported(gpu, persistent):
     # system rank-deficient, so only the absence of the overflow report is checked)
     T2 = np.eye(4, dtype=np.float32)
     tr.track(torch.from_numpy(depth).cuda(), T2, torch.from_numpy(p_S.copy()).cuda(), torch.from_numpy(n_ref).cuda())
+
+
+def test_barrier_timeout_is_reported(gpu):
+    """The persistent ICP's grid barrier is bounded: made to wait for a CTA that does not exist,
+    it gives up after half a second, the pose is rejected and the call reports the timeout; the
+    context stays usable and the next track succeeds."""
+    import time
+    import torch
+    from supereight2_gb300 import synthetic as syn
+    spec, scene, poses, frames = syn.dataset("tsdf320", 2)
+    sensor = gpu.PinholeCamera.from_spec(spec)
+    m = gpu.Map(10.24, 0.02, max_blocks=1 << 16)
+    integ = gpu.MapIntegrator(m)
+    T0 = poses[0].astype(np.float32)
+    integ.integrateDepth(0, torch.from_numpy(frames[0]).cuda(), sensor, T0)
+    pts = torch.zeros((sensor.height, sensor.width, 3), device="cuda")
+    nrm = torch.zeros_like(pts)
+    gpu.raycast_volume(m, sensor, T0, pts, nrm)
+    d = torch.from_numpy(frames[1]).cuda()
+    tr = gpu.Tracker(m, sensor)
+    tr.set_persistent(True)
+    tr.test_barrier_timeout(True)
+    T = T0.copy()
+    t0 = time.perf_counter()
+    with pytest.raises(gpu.SeGpuError, match="timed out"):
+        tr.track(d, T, pts, nrm)
+    assert time.perf_counter() - t0 < 30.0
+    assert np.array_equal(T, T0)
+    tr.test_barrier_timeout(False)
+    T = T0.copy()
+    assert tr.track(d, T, pts, nrm)
+    assert np.linalg.norm(T[:3, 3] - poses[1][:3, 3]) < 0.01
