@@ -27,6 +27,7 @@ namespace se_gpu {
 __global__ void integrate_prep_kernel(MapDevice m, float trunc_factor, Pinhole s, const float* pose12,
                                       IntegrateParams host_p, int* ts_counter, IntegrateParams* out)
 {
+    grid_dep_wait();
     if (pose12 == nullptr) {
         *out = host_p;
     }
@@ -64,6 +65,7 @@ __device__ __forceinline__ int voxel_of(float x, float res, float inv_res)
 __global__ void __launch_bounds__(256) carve_kernel(MapDevice m, Pinhole s, const float* __restrict__ depth,
                                                     const IntegrateParams* __restrict__ P)
 {
+    grid_dep_wait();
     const CarveParams cp = P->cp;
     const int lane = threadIdx.x & 31;
     const int x = blockIdx.x * 32 + lane;
@@ -120,6 +122,7 @@ __global__ void __launch_bounds__(256) carve_kernel(MapDevice m, Pinhole s, cons
 
 __global__ void __launch_bounds__(256) frustum_kernel(MapDevice m, Pinhole s, const IntegrateParams* __restrict__ P)
 {
+    grid_dep_wait();
     const Tf T_SW = P->fp.T_SW;
     const int n_old = m.counters[kCntNumOld];
     const int lane = threadIdx.x & 31;
@@ -160,6 +163,7 @@ template <int S>
 __global__ void __launch_bounds__(256, 4) update_kernel(MapDevice m, Pinhole s, const float* __restrict__ depth,
                                                      const IntegrateParams* __restrict__ P)
 {
+    grid_dep_wait();
     const Tf T_CV = P->up.T_CV;
     const int timestamp = P->up.timestamp;
     const int lane = threadIdx.x & 31;
@@ -272,18 +276,17 @@ se_gpu_status enqueue_integrate(se_gpu_map* map, const float* depth_dev, const s
     const int sms = device_sm_count();
     {
         ProfScope ps(kProfBeginFrame, stream);
-        integrate_prep_kernel<<<1, 1, 0, stream>>>(m, map->config.truncation_boundary_factor, s,
-                                                   T_WC_host16 ? nullptr : pose12_dev, hp, map->timestamp_dev,
-                                                   map->iparams);
+        launch_chained(integrate_prep_kernel, 1, 1, stream, m, map->config.truncation_boundary_factor, s,
+                       T_WC_host16 ? nullptr : pose12_dev, hp, map->timestamp_dev, map->iparams);
     }
     {
         ProfScope ps(kProfCarve, stream);
         dim3 cgrid((s.w + 31) / 32, (s.h + 7) / 8);
-        carve_kernel<<<cgrid, 256, 0, stream>>>(m, s, depth_dev, map->iparams);
+        launch_chained(carve_kernel, cgrid, 256, stream, m, s, depth_dev, map->iparams);
     }
     {
         ProfScope ps(kProfFrustum, stream);
-        frustum_kernel<<<sms * 4, 256, 0, stream>>>(m, s, map->iparams);
+        launch_chained(frustum_kernel, sms * 4, 256, stream, m, s, map->iparams);
     }
     if (m.res_type == SE_GPU_RES_MULTI) {
         enqueue_update_multires(m, s, depth_dev, map->iparams, stream);
@@ -291,9 +294,9 @@ se_gpu_status enqueue_integrate(se_gpu_map* map, const float* depth_dev, const s
     else {
         ProfScope ps(kProfUpdate, stream);
         if (m.storage == SE_GPU_STORAGE_F32)
-            update_kernel<SE_GPU_STORAGE_F32><<<sms * 8, 256, 0, stream>>>(m, s, depth_dev, map->iparams);
+            launch_chained(update_kernel<SE_GPU_STORAGE_F32>, sms * 8, 256, stream, m, s, depth_dev, map->iparams);
         else
-            update_kernel<SE_GPU_STORAGE_F16><<<sms * 8, 256, 0, stream>>>(m, s, depth_dev, map->iparams);
+            launch_chained(update_kernel<SE_GPU_STORAGE_F16>, sms * 8, 256, stream, m, s, depth_dev, map->iparams);
     }
     SE_CUDA_TRY(cudaGetLastError());
     return SE_GPU_OK;

@@ -25,6 +25,7 @@ namespace se_gpu {
 
 __global__ void raycast_prep_kernel(const float* pose12, RaycastParams host_p, RaycastParams* out)
 {
+    grid_dep_wait();
     RaycastParams p = host_p;
     if (pose12 != nullptr)
         p.T_WS = tf_from12(pose12);
@@ -36,6 +37,7 @@ __global__ void __launch_bounds__(128, 9) raycast_kernel(MapDevice m, Pinhole s,
                                                       float* __restrict__ pts, float* __restrict__ nrm,
                                                       int8_t* __restrict__ scale)
 {
+    grid_dep_wait();
     // per-thread scratch in shared memory (column threadIdx.x): the traversal stack and the
     // gradient's block table
     __shared__ float sh_stack[kEsvoStackDepth * 128];
@@ -132,18 +134,18 @@ se_gpu_status enqueue_raycast(const se_gpu_map* map, const se_gpu_pinhole& senso
     rp.scaling = (float) m.size * m.res;
     rp.eps = std::exp2((float) (-std::log2((double) m.size)));
     rp.min_scale = 23 - m.log2_bps;
-    raycast_prep_kernel<<<1, 1, 0, stream>>>(T_WS_host16 ? nullptr : pose12_dev, rp, map->rparams);
+    launch_chained(raycast_prep_kernel, 1, 1, stream, T_WS_host16 ? nullptr : pose12_dev, rp, map->rparams);
     dim3 grid((s.w + 15) / 16, (s.h + 7) / 8);
     ProfScope ps(kProfRaycast, stream);
     const bool mr = m.res_type == SE_GPU_RES_MULTI;
     if (m.storage == SE_GPU_STORAGE_F32 && !mr)
-        raycast_kernel<SE_GPU_STORAGE_F32, false><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+        launch_chained(raycast_kernel<SE_GPU_STORAGE_F32, false>, grid, 128, stream, m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
     else if (!mr)
-        raycast_kernel<SE_GPU_STORAGE_F16, false><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+        launch_chained(raycast_kernel<SE_GPU_STORAGE_F16, false>, grid, 128, stream, m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
     else if (m.storage == SE_GPU_STORAGE_F32)
-        raycast_kernel<SE_GPU_STORAGE_F32, true><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+        launch_chained(raycast_kernel<SE_GPU_STORAGE_F32, true>, grid, 128, stream, m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
     else
-        raycast_kernel<SE_GPU_STORAGE_F16, true><<<grid, 128, 0, stream>>>(m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+        launch_chained(raycast_kernel<SE_GPU_STORAGE_F16, true>, grid, 128, stream, m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
     SE_CUDA_TRY(cudaGetLastError());
     return SE_GPU_OK;
 }

@@ -480,4 +480,33 @@ __device__ __forceinline__ void insert_block(const MapDevice& m, uint64_t key, i
 
 int device_sm_count();
 
+// Kernels on the per-frame path are launched with programmatic stream serialisation: a kernel's
+// CTAs may be scheduled while the previous kernel on the stream drains, and each of these kernels
+// begins with grid_dep_wait(), which returns once that kernel has completed and its writes are
+// visible. Nothing runs earlier than before; only the launch latency between the kernels is
+// hidden. Each such kernel then lets the next one be scheduled at once (launch_dependents): the
+// next kernel's CTAs take free slots in this one's tail and wait there. (Without the launch
+// attribute, griddepcontrol.wait returns at once.)
+__device__ __forceinline__ void grid_dep_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline void launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t stream, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 } // namespace se_gpu

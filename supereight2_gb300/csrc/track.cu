@@ -228,6 +228,7 @@ __device__ __forceinline__ F3 depth_normal(const float* __restrict__ depth, cons
 // point_cloud_to_normal<NegY> (src/map/preprocessor.cpp:109-152) for every level, one launch.
 __global__ void points_normals_kernel(LevelImages li, int levels, int neg_y)
 {
+    grid_dep_wait();
     const int l = blockIdx.z;
     if (l >= levels)
         return;
@@ -298,6 +299,7 @@ __global__ void pyramid_init_kernel(TrackState* st, TrackInit init, const float*
                                     LevelImages li, int levels, float e_d, float* __restrict__ d1,
                                     float* __restrict__ d2)
 {
+    grid_dep_wait();
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     if (blockIdx.x == 0 && blockIdx.y == 0) {
         for (int b = 0; b < kAccBuffers; ++b)
@@ -1069,12 +1071,12 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
         // one thread per 2 x 2 group of level-1 pixels (a single block without a pyramid)
         const dim3 b(32, 8);
         const dim3 g(t->levels > 1 ? ((li.w[1] + 1) / 2 + 31) / 32 : 1, t->levels > 1 ? ((li.h[1] + 1) / 2 + 7) / 8 : 1);
-        pyramid_init_kernel<<<g, b, 0, stream>>>(t->state, init, pose_in, t->acc, li, t->levels, e_d,
-                                                 t->pyr_depth[1], t->pyr_depth[2]);
+        launch_chained(pyramid_init_kernel, g, b, stream, t->state, init, pose_in, t->acc, li, t->levels, e_d,
+                       t->pyr_depth[1], t->pyr_depth[2]);
     }
     {
         const dim3 b(32, 8), g((li.w[0] + 31) / 32, (li.h[0] + 7) / 8, t->levels);
-        points_normals_kernel<<<g, b, 0, stream>>>(li, t->levels, t->s.left_hand);
+        launch_chained(points_normals_kernel, g, b, stream, li, t->levels, t->s.left_hand);
     }
     }
     IcpLevels L;
