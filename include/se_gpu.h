@@ -469,6 +469,12 @@ SE_GPU_API se_gpu_status se_gpu_frame_run_host(se_gpu_frame* frame, const float*
  * checkPoseKernel result; 1 when the last run did not track). Synchronous. */
 SE_GPU_API se_gpu_status se_gpu_frame_get_pose(se_gpu_frame* frame, float T_WS[16],
                                                int* accepted, void* stream);
+/* The same read without waiting: the row-major 3x4 pose and the acceptance are copied into the
+ * caller's host memory (pinned, for the copies to stay asynchronous) on stream; they are valid
+ * once the stream has reached this point (an event or a synchronisation). A caller that reads
+ * each frame's pose while the next frame runs keeps two sets of buffers. */
+SE_GPU_API se_gpu_status se_gpu_frame_get_pose_async(se_gpu_frame* frame, float pose12_host[12],
+                                                     int* accepted_host, void* stream);
 
 /* ------------------------------------------------------------------------- profiling -- */
 

@@ -148,6 +148,7 @@ SIGNATURES = {
     "se_gpu_frame_run": (C.c_int, [_VP, C.c_int, _VP]),
     "se_gpu_frame_run_host": (C.c_int, [_VP, _VP, C.c_int, _VP]),
     "se_gpu_frame_get_pose": (C.c_int, [_VP, _F16, C.POINTER(C.c_int), _VP]),
+    "se_gpu_frame_get_pose_async": (C.c_int, [_VP, _VP, _VP, _VP]),
     "se_gpu_profiling_enable": (C.c_int, [C.c_int]),
     "se_gpu_profiling_read": (C.c_int, [C.c_int, _VP, _VP, C.c_int]),
     "se_gpu_profiling_name": (C.c_char_p, [C.c_int]),
@@ -844,6 +845,16 @@ class FramePipeline:
         _check(self._L.se_gpu_frame_get_pose(self.h, T.ctypes.data_as(_F16), C.byref(acc),
                                              _stream(stream)), "se_gpu_frame_get_pose")
         return T.reshape(4, 4), bool(acc.value)
+
+    def pose_async(self, pose12, accepted, stream=None):
+        """Enqueue the pose read into pinned host tensors: ``pose12`` (12 float32, the row-major
+        3x4 T_WS) and ``accepted`` (1 int32); valid once the stream has passed this point."""
+        for t, dt, n in ((pose12, "float32", 12), (accepted, "int32", 1)):
+            if t.is_cuda or str(t.dtype) != "torch." + dt or t.numel() != n or not t.is_contiguous():
+                raise SeGpuError("pose_async wants contiguous host tensors: 12 float32 and 1 int32")
+        _check(self._L.se_gpu_frame_get_pose_async(self.h, C.c_void_p(pose12.data_ptr()),
+                                                   C.c_void_p(accepted.data_ptr()), _stream(stream)),
+               "se_gpu_frame_get_pose_async")
 
 
 def _wrap_device(ptr, shape, dtype, owner):

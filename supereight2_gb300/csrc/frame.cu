@@ -239,4 +239,20 @@ se_gpu_status se_gpu_frame_get_pose(se_gpu_frame* f, float T_WS[16], int* accept
     return SE_GPU_OK;
 }
 
+se_gpu_status se_gpu_frame_get_pose_async(se_gpu_frame* f, float pose12_host[12], int* accepted_host, void* stream_p)
+{
+    if (!f || !pose12_host || !accepted_host) {
+        set_last_error("se_gpu_frame_get_pose_async: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    SE_CUDA_TRY(cudaMemcpyAsync(pose12_host, f->pose12, 12 * sizeof(float), cudaMemcpyDeviceToHost, stream));
+    if (f->tracker && f->last_tracked)
+        SE_CUDA_TRY(cudaMemcpyAsync(accepted_host, (char*) tracker_state(f->tracker) + tracker_accepted_offset(),
+                                    sizeof(int), cudaMemcpyDeviceToHost, stream));
+    else
+        *accepted_host = 1;
+    return SE_GPU_OK;
+}
+
 } // extern "C"

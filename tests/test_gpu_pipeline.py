@@ -29,7 +29,7 @@ def _run_plain(gpu, sensor, poses, frames, storage):
     return m, out, pts.cpu().numpy(), nrm.cpu().numpy()
 
 
-def _run_graph(gpu, sensor, poses, frames, storage, from_host=False):
+def _run_graph(gpu, sensor, poses, frames, storage, from_host=False, pose_async=False):
     import torch
     m = gpu.Map(10.24, 0.02, max_blocks=1 << 16, storage=storage)
     tr = gpu.Tracker(m, sensor)
@@ -37,14 +37,25 @@ def _run_graph(gpu, sensor, poses, frames, storage, from_host=False):
     fp.set_pose(poses[0].astype(np.float32), 0)
     out = []
     host = [torch.from_numpy(d).pin_memory() for d in frames] if from_host else None
+    # one set of pinned buffers per frame: every read stays pending until the end
+    bufs = [(torch.zeros(12, dtype=torch.float32).pin_memory(), torch.zeros(1, dtype=torch.int32).pin_memory())
+            for _ in frames]
     for i, d in enumerate(frames):
         if from_host:
             fp.run(track=i > 0, depth=host[i])   # se_gpu_frame_run_host: host depth in
         else:
             fp.depth.copy_(torch.from_numpy(d).cuda())
             fp.run(track=i > 0)
-        out.append(fp.pose())
+        if pose_async:
+            fp.pose_async(*bufs[i])
+        else:
+            out.append(fp.pose())
     torch.cuda.synchronize()
+    if pose_async:
+        for p12, acc in bufs:
+            T = np.eye(4, dtype=np.float32)
+            T[:3] = p12.numpy().reshape(3, 4)
+            out.append((T, bool(acc[0])))
     return m, out, fp.points_W.cpu().numpy(), fp.normals_W.cpu().numpy()
 
 
@@ -82,6 +93,18 @@ def test_graph_pipeline_from_host_depth(gpu, data):
     for (T1, a1), (T2, a2) in zip(o1, o2):
         assert a1 == a2 and np.array_equal(T1, T2)
     assert np.array_equal(p1, p2) and np.array_equal(n1, n2)
+
+
+def test_graph_pipeline_pose_async(gpu, data):
+    """se_gpu_frame_get_pose_async: every frame's pose and acceptance, read without waiting,
+    equal the synchronous reads."""
+    spec, scene, poses, frames = data
+    sensor = gpu.PinholeCamera.from_spec(spec)
+    _, o1, _, _ = _run_graph(gpu, sensor, poses, frames, "f32", from_host=True)
+    _, o2, _, _ = _run_graph(gpu, sensor, poses, frames, "f32", from_host=True, pose_async=True)
+    assert len(o1) == len(o2) == len(frames)
+    for (T1, a1), (T2, a2) in zip(o1, o2):
+        assert a1 == a2 and np.array_equal(T1, T2)
 
 
 def test_f16_storage_error_against_f32(gpu, data):
