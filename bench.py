@@ -12,7 +12,9 @@ integration of the raw depth at the tracked pose, raycast at that pose.
 Prints one JSON line (rank 0). ``value``: frames/s with the depth images resident in HBM, the
 device time of the K steps measured with CUDA events on the launching stream and L2 flushed
 (256 MiB write) between steps outside the timed pairs. ``e2e``: the same through the public API
-with each frame's depth copied from pinned host memory and the pose read back, host clock.
+with each frame's depth copied from pinned host memory and its pose read back into pinned
+memory (read on the host while the next frame runs), host clock over consecutive frames with
+no L2 flush between them.
 ``--impl reference`` times the CPU oracle (the restatement of the reference's OpenMP code) on
 all host cores. Under torchrun every rank runs an independent replica (the path does not
 shard); the value is the sum of frames over the max time across ranks.
