@@ -51,7 +51,11 @@ typedef enum { SE_GPU_FIELD_TSDF = 0, SE_GPU_FIELD_OCCUPANCY = 1 } se_gpu_field;
 typedef enum { SE_GPU_RES_SINGLE = 0, SE_GPU_RES_MULTI = 1 } se_gpu_res;
 typedef enum {
     SE_GPU_STORAGE_F32 = 0, /* float tsdf + float weight per voxel (the reference layout) */
-    SE_GPU_STORAGE_F16 = 1  /* half tsdf + uint16 weight per voxel; FP32 arithmetic */
+    SE_GPU_STORAGE_F16 = 1  /* 4 bytes per voxel, FP32 arithmetic: the tsdf as FP16 with 8 more
+                             * significand bits (bits 31..8; bits 31..16 are the binary16 value
+                             * truncated toward zero) and an 8-bit integer weight (bits 7..0,
+                             * max_weight <= 255). Within max_weight * 2^-19 truncation units
+                             * of the F32 layout (1.9e-4 at max_weight 100). */
 } se_gpu_storage;
 
 /* se::Map<Data<TSDF>, Res::Single, 8>::Config + FieldData<TSDF>::Config
@@ -65,7 +69,7 @@ typedef struct {
     int res_type;      /* se_gpu_res: single-res (Map<.., Res::Single>) or multi-res TSDF */
     int storage;       /* se_gpu_storage */
     float truncation_boundary_factor; /* reference default 8 */
-    float max_weight;  /* reference default 100; must be an integer <= 65535 */
+    float max_weight;  /* reference default 100; an integer <= 65535 (<= 255 with F16 storage) */
     int64_t max_blocks; /* block pool capacity (8^3-voxel blocks) */
 } se_gpu_map_config;
 
@@ -415,6 +419,17 @@ SE_GPU_API se_gpu_status se_gpu_tracker_test_barrier_timeout(se_gpu_tracker* tra
 SE_GPU_API se_gpu_status se_gpu_tracker_last_reduction(se_gpu_tracker* tracker, float reduction[32],
                                             int iterations_run[3]);
 
+/* The tracker's input pyramid of the last track at one level (0 = full resolution): the
+ * half-sampled depth (half_sample_robust_image, src/map/preprocessor.cpp:156-195; levels >= 1
+ * only, level 0's depth is the caller's input), the point cloud (depth_to_point_cloud,
+ * include/se/map/impl/preprocessor_impl.hpp:18-40) and the normals (point_cloud_to_normal,
+ * src/map/preprocessor.cpp:109-152), copied into caller device buffers of (W >> level) x
+ * (H >> level) floats, and 3 floats per pixel for points and normals. Any pointer may be NULL.
+ * Stream-ordered, asynchronous. */
+SE_GPU_API se_gpu_status se_gpu_tracker_level_images(se_gpu_tracker* tracker, int level,
+                                                     float* depth_dev, float* pts_dev,
+                                                     float* nrm_dev, void* stream);
+
 /* Allocation-free tracking. No counterpart in the reference. For callers that cannot
  * allocate device memory while they track (a host whose pool allocator owns the free device
  * memory, a loop with a memory budget fixed at start-up, or code that must not let
@@ -422,8 +437,12 @@ SE_GPU_API se_gpu_status se_gpu_tracker_last_reduction(se_gpu_tracker* tracker, 
  * ICP level (config->num_levels must be 1, config->iterations[0] iterations), with the
  * tracker's scratch in a static device array of about 77 KiB that the library holds on every
  * GPU that loads it. Depth images larger than 4096 x 4096 pixels are rejected. The first call
- * on a device looks up the array's device address; make that first call before any stream
- * capture. Calls share the array: calls that overlap on the GPU race. T_WS is read and
+ * on a device looks up the array's device address, and with CUDA's lazy module loading (the
+ * default since CUDA 12.2) that lookup is also when the driver loads this part of the
+ * library onto the device, which allocates the static array and the kernels' code there: make
+ * the first call at start-up, before a pool allocator takes the free memory and before any
+ * stream capture. Later calls allocate nothing. Calls share the array: calls that overlap on
+ * the GPU race. T_WS is read and
  * written on the host; accepted and reduction (32 floats, se_gpu_tracker_last_reduction's
  * layout) may be NULL. Synchronous. */
 SE_GPU_API se_gpu_status se_gpu_track_noalloc(const se_gpu_pinhole* sensor,

@@ -136,6 +136,7 @@ def lib():
             "so_occ_set_block": (None, [vp, i32p, C.c_int, C.c_int, f32p]),
             "so_downsample_depth": (None, [f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, vp]),
             "so_point_cloud_to_normal": (None, [f32p, C.c_int, C.c_int, C.c_int, f32p]),
+            "so_tracker_pyramid": (None, [C.POINTER(Pinhole), f32p, C.c_int, f32p, f32p, f32p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -532,6 +533,26 @@ def track(sensor: Pinhole, config: TrackerConfig, depth, T_WS, ref_pts, ref_nrm)
                          np.ascontiguousarray(ref_pts, np.float32).reshape(-1),
                          np.ascontiguousarray(ref_nrm, np.float32).reshape(-1), C.byref(st))
     return bool(acc), T.reshape(4, 4), st
+
+
+def tracker_pyramid(sensor: Pinhole, depth, levels=3):
+    """The tracker's input pyramid as track() forms it: [(depth, points, normals)] per level,
+    level l of size (H >> l, W >> l) (half_sample_robust_image, depth_to_point_cloud,
+    point_cloud_to_normal)."""
+    W, H = sensor.width, sensor.height
+    sizes = [(H >> l, W >> l) for l in range(levels)]
+    n = sum(h * w for h, w in sizes)
+    d = np.zeros(n, np.float32)
+    p = np.zeros(3 * n, np.float32)
+    q = np.zeros(3 * n, np.float32)
+    lib().so_tracker_pyramid(C.byref(sensor), np.ascontiguousarray(depth, np.float32).reshape(-1),
+                             int(levels), d, p, q)
+    out, off = [], 0
+    for h, w in sizes:
+        out.append((d[off:off + h * w].reshape(h, w), p[3 * off:3 * (off + h * w)].reshape(h, w, 3),
+                    q[3 * off:3 * (off + h * w)].reshape(h, w, 3)))
+        off += h * w
+    return out
 
 
 def se3_exp(twist):

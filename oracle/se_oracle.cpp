@@ -2448,4 +2448,28 @@ void so_point_cloud_to_normal(const float* pts, int w, int h, int neg_y, float* 
     points_to_normals(reinterpret_cast<const V3*>(pts), w, h, neg_y != 0, reinterpret_cast<V3*>(nrm));
 }
 
+/* The tracker's input pyramid exactly as so_track forms it (tracker_impl.hpp:30-60): level l
+ * (l < levels) is (W >> l) x (H >> l); depth_out, pts_out and nrm_out hold the levels one after
+ * another (level 0's depth is the input itself). */
+void so_tracker_pyramid(const so_pinhole* sensor_c, const float* depth, int levels, float* depth_out,
+                        float* pts_out, float* nrm_out)
+{
+    const Pinhole s = make_pinhole(sensor_c);
+    const int L = std::min(std::max(levels, 1), 3);
+    size_t off = 0;
+    std::memcpy(depth_out, depth, sizeof(float) * (size_t) s.w * s.h);
+    for (int i = 0; i < L; ++i) {
+        const int w = s.w / (1 << i), h = s.h / (1 << i);
+        if (i > 0) {
+            const int pw = s.w / (1 << (i - 1)), ph = s.h / (1 << (i - 1));
+            half_sample_robust(depth_out + off - (size_t) pw * ph, pw, ph, 0.1f * 3.0f, 1, depth_out + off);
+        }
+        const Pinhole si = downsampled(s, (float) (1 << i));
+        depth_to_points(depth_out + off, si, reinterpret_cast<V3*>(pts_out + 3 * off));
+        points_to_normals(reinterpret_cast<const V3*>(pts_out + 3 * off), si.w, si.h, s.left_hand,
+                          reinterpret_cast<V3*>(nrm_out + 3 * off));
+        off += (size_t) w * h;
+    }
+}
+
 } /* extern "C" */

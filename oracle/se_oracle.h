@@ -266,6 +266,8 @@ void so_dual_groups(const int32_t rel[3], int32_t group_of[8], int32_t above[8],
 void so_half_sample_robust(const float* in, int w, int h, float e_d, int radius, float* out);
 void so_depth_to_point_cloud(const float* depth, const so_pinhole* sensor, float* pts);
 void so_point_cloud_to_normal(const float* pts, int w, int h, int neg_y, float* nrm);
+void so_tracker_pyramid(const so_pinhole* sensor, const float* depth, int levels, float* depth_out,
+                        float* pts_out, float* nrm_out);
 
 #ifdef __cplusplus
 }

@@ -138,6 +138,7 @@ SIGNATURES = {
     "se_gpu_tracker_destroy": (C.c_int, [_VP]),
     "se_gpu_track": (C.c_int, [_VP, _VP, _VP, _VP, _F16, C.POINTER(C.c_int), _VP]),
     "se_gpu_tracker_last_reduction": (C.c_int, [_VP, _F16, C.POINTER(C.c_int)]),
+    "se_gpu_tracker_level_images": (C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP]),
     "se_gpu_track_noalloc": (C.c_int, [C.POINTER(_Pinhole), C.POINTER(_TrackerConfig), _VP, _VP,
                                        _VP, _F16, C.POINTER(C.c_int), _F16, _VP]),
     "se_gpu_frame_create": (C.c_int, [_VP, _VP, C.POINTER(_Pinhole), C.POINTER(_VP)]),
@@ -619,6 +620,20 @@ class Tracker:
         _check(self._L.se_gpu_tracker_test_barrier_timeout(self.h, 1 if enable else 0),
                "se_gpu_tracker_test_barrier_timeout")
 
+    def level_images(self, level, stream=None):
+        """The last track()'s input pyramid at one level: (depth or None at level 0, points,
+        normals), new CUDA tensors of (H >> level, W >> level) pixels."""
+        import torch
+        h, w = self.sensor.height >> level, self.sensor.width >> level
+        d = torch.zeros((h, w), dtype=torch.float32, device="cuda") if level > 0 else None
+        p = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
+        n = torch.zeros_like(p)
+        _check(self._L.se_gpu_tracker_level_images(self.h, int(level), d.data_ptr() if d is not None else None,
+                                                   p.data_ptr(), n.data_ptr(), _stream(stream)),
+               "se_gpu_tracker_level_images")
+        torch.cuda.synchronize()
+        return d, p, n
+
     def last_reduction(self):
         red = (C.c_float * 32)()
         its = (C.c_int * 3)()
@@ -666,7 +681,9 @@ def track_noalloc(sensor: PinholeCamera, config: TrackerConfig, depth, T_WS,
     """One-level ICP that allocates no device memory (no counterpart in the reference).
 
     For callers that cannot allocate while they track; the scratch is a static device array
-    inside the library, shared by all calls, so calls must not overlap on the GPU. ``config``
+    inside the library, shared by all calls, so calls must not overlap on the GPU. The first
+    call on a device also loads that part of the library onto the device (lazy module
+    loading), which allocates the array: make it at start-up. ``config``
     must have exactly one level. T_WS (float32 4x4 numpy, C-contiguous) is updated in place.
     Returns (accepted, reduction[32])."""
     import torch

@@ -16,6 +16,10 @@
 namespace se_gpu {
 int tracker_accepted_offset();
 void* tracker_state(se_gpu_tracker* t);
+
+// The acceptance of a run that did not track: copied on the stream like a tracked run's flag,
+// so that it lands in stream order after any earlier read into the same host buffer.
+static __device__ int g_accepted_untracked = 1; // never written
 } // namespace se_gpu
 
 using namespace se_gpu;
@@ -251,7 +255,8 @@ se_gpu_status se_gpu_frame_get_pose_async(se_gpu_frame* f, float pose12_host[12]
         SE_CUDA_TRY(cudaMemcpyAsync(accepted_host, (char*) tracker_state(f->tracker) + tracker_accepted_offset(),
                                     sizeof(int), cudaMemcpyDeviceToHost, stream));
     else
-        *accepted_host = 1;
+        SE_CUDA_TRY(cudaMemcpyFromSymbolAsync(accepted_host, g_accepted_untracked, sizeof(int), 0,
+                                              cudaMemcpyDeviceToHost, stream));
     return SE_GPU_OK;
 }
 

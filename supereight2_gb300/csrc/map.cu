@@ -117,6 +117,11 @@ se_gpu_status se_gpu_map_create(const se_gpu_map_config* cfg, se_gpu_map** out)
         set_last_error("se_gpu_map_create: invalid configuration");
         return SE_GPU_ERR_BAD_ARG;
     }
+    if (cfg->storage == SE_GPU_STORAGE_F16 && cfg->max_weight > 255.0f) {
+        set_last_error("se_gpu_map_create: FP16 storage keeps 8-bit weights (max_weight <= 255, got %g)",
+                       (double) cfg->max_weight);
+        return SE_GPU_ERR_BAD_ARG;
+    }
     int dev = 0;
     SE_CUDA_TRY(cudaGetDevice(&dev));
     int major = 0, minor = 0;

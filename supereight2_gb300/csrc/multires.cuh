@@ -5,7 +5,7 @@
 // each x + n*y + n^2*z. Every entry stores the data and the past data used by delta
 // down-propagation, side by side so that one 16-byte (FP32) or 8-byte (FP16) access moves both:
 //   SE_GPU_STORAGE_F32: float4 {tsdf, weight, past tsdf, past weight}
-//   SE_GPU_STORAGE_F16: uint2  {half tsdf | u16 weight << 16, half past tsdf | u16 past weight << 16}
+//   SE_GPU_STORAGE_F16: uint2  {f16x_pack(tsdf, weight), f16x_pack(past tsdf, past weight)}
 // A block's current scale is the one it integrates at; reads "at the block's data" use it.
 #pragma once
 
@@ -42,10 +42,8 @@ __device__ __forceinline__ MrVoxel mr_load(const MapDevice& m, int blk, int i)
     }
     else {
         const uint2 d = reinterpret_cast<const uint2*>(m.voxels)[(size_t) blk * kMrVoxels + i];
-        v.tsdf = __half2float(__ushort_as_half((unsigned short) (d.x & 0xffffu)));
-        v.weight = (float) (d.x >> 16);
-        v.past_tsdf = __half2float(__ushort_as_half((unsigned short) (d.y & 0xffffu)));
-        v.past_weight = (float) (d.y >> 16);
+        f16x_unpack(d.x, v.tsdf, v.weight);
+        f16x_unpack(d.y, v.past_tsdf, v.past_weight);
     }
     return v;
 }
@@ -60,17 +58,8 @@ __device__ __forceinline__ void mr_load_data(const MapDevice& m, int blk, int i,
         w = d.y;
     }
     else {
-        const uint32_t d = reinterpret_cast<const uint32_t*>(m.voxels)[2 * ((size_t) blk * kMrVoxels + i)];
-        t = __half2float(__ushort_as_half((unsigned short) (d & 0xffffu)));
-        w = (float) (d >> 16);
+        f16x_unpack(reinterpret_cast<const uint32_t*>(m.voxels)[2 * ((size_t) blk * kMrVoxels + i)], t, w);
     }
-}
-
-__device__ __forceinline__ uint32_t mr_pack16(float t, float w)
-{
-    // weights are integers; the FP16 layout saturates them at 65535
-    const float wc = w < 65535.0f ? w : 65535.0f;
-    return (uint32_t) __half_as_ushort(__float2half_rn(t)) | ((uint32_t) wc << 16);
 }
 
 template <int S>
@@ -82,7 +71,7 @@ __device__ __forceinline__ void mr_store(const MapDevice& m, int blk, int i, con
     }
     else {
         reinterpret_cast<uint2*>(m.voxels)[(size_t) blk * kMrVoxels + i] =
-            make_uint2(mr_pack16(v.tsdf, v.weight), mr_pack16(v.past_tsdf, v.past_weight));
+            make_uint2(f16x_pack(v.tsdf, v.weight), f16x_pack(v.past_tsdf, v.past_weight));
     }
 }
 

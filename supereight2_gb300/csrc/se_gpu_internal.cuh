@@ -179,7 +179,7 @@ struct MapDevice {
     int* block_coord;             // 3 ints per block
     unsigned long long* block_keys;
     int* block_ts;
-    void* voxels;                 // F32: float2 {tsdf, weight}; F16: {half tsdf, u16 weight}
+    void* voxels;                 // F32: float2 {tsdf, weight}; F16: f16x_pack words
     // Occupancy pyramid for the raycast's first-block search: level 0 has one bit per block (bps^3 bits, x fastest), level L one bit
     // per (2^L)^3 blocks. A bit is set iff an allocated block lies inside the cell, which is
     // exactly when the reference's pointer octree holds the node.
@@ -231,8 +231,43 @@ __device__ __forceinline__ int block_at(const MapDevice& m, int bx, int by, int 
     return m.block_index[((size_t) bz << (2 * m.log2_bps)) | ((size_t) by << m.log2_bps) | (size_t) bx];
 }
 
+// FP16 storage word (SE_GPU_STORAGE_F16, 4 bytes per voxel):
+//   bits 31..8  the tsdf as an FP16 number carrying 8 more significand bits: FP16's sign and
+//               5-bit exponent (bias 15) with an 18-bit significand. Bits 31..16 alone are the
+//               binary16 value truncated toward zero; the low 8 bits of the field are the
+//               running mean's rounding guard.
+//   bits 7..0   the integer weight (max_weight <= 255).
+// Rounding is to nearest (ties to even) on the 18-bit significand: |error| <= 2^-19 for
+// |tsdf| <= 1. A running mean over weights up to W then stays within W * 2^-19 of the FP32
+// layout's (each update shrinks the carried error by (w - 1) / w and adds at most 2^-19):
+// 1.9e-4 truncation units at the reference's max_weight = 100. Plain binary16 storage would
+// carry W * 2^-11 (0.049) in the worst case.
+__device__ __forceinline__ uint32_t f16x_pack(float t, float w)
+{
+    const uint32_t u = __float_as_uint(t), a = u & 0x7fffffffu;
+    uint32_t em; // exponent and significand, 23 bits
+    if (a >= 0x38800000u) { // |t| >= 2^-14: normal; round the 5 dropped bits to nearest even
+        const uint32_t r = (a + 0xfu + ((a >> 5) & 1u)) >> 5;
+        em = r - (112u << 18);
+        if (em > 0x7fffffu)
+            em = 0x7fffffu; // beyond the format's range (not reached: |tsdf| <= 1)
+    }
+    else { // subnormal: units of 2^-32 (rounds up into the smallest normal consistently)
+        em = __float2uint_rn(__uint_as_float(a) * 4294967296.0f);
+    }
+    const float wc = w < 255.0f ? w : 255.0f;
+    return (u & 0x80000000u) | (em << 8) | (uint32_t) wc;
+}
+__device__ __forceinline__ void f16x_unpack(uint32_t d, float& t, float& w)
+{
+    const uint32_t em = (d >> 8) & 0x7fffffu;
+    const float mag = em >= (1u << 18) ? __uint_as_float((em + (112u << 18)) << 5) : (float) em * 0x1p-32f;
+    t = __uint_as_float(__float_as_uint(mag) | (d & 0x80000000u));
+    w = (float) (d & 0xffu);
+}
+
 // Voxel data access; S is the se_gpu_storage layout (F32: float2 {tsdf, weight};
-// F16: uint32 {half tsdf | u16 weight << 16}).
+// F16: the uint32 word of f16x_pack).
 template <int S>
 __device__ __forceinline__ void load_voxel(const MapDevice& m, int blk, int vi, float& tsdf, float& w)
 {
@@ -242,9 +277,7 @@ __device__ __forceinline__ void load_voxel(const MapDevice& m, int blk, int vi, 
         w = d.y;
     }
     else {
-        const uint32_t d = reinterpret_cast<const uint32_t*>(m.voxels)[(size_t) blk * kBlockVoxels + vi];
-        tsdf = __half2float(__ushort_as_half((unsigned short) (d & 0xffffu)));
-        w = (float) (d >> 16);
+        f16x_unpack(reinterpret_cast<const uint32_t*>(m.voxels)[(size_t) blk * kBlockVoxels + vi], tsdf, w);
     }
 }
 template <int S>
@@ -254,8 +287,7 @@ __device__ __forceinline__ void store_voxel(const MapDevice& m, int blk, int vi,
         reinterpret_cast<float2*>(m.voxels)[(size_t) blk * kBlockVoxels + vi] = make_float2(tsdf, w);
     }
     else {
-        const uint32_t d = (uint32_t) __half_as_ushort(__float2half_rn(tsdf)) | ((uint32_t) w << 16);
-        reinterpret_cast<uint32_t*>(m.voxels)[(size_t) blk * kBlockVoxels + vi] = d;
+        reinterpret_cast<uint32_t*>(m.voxels)[(size_t) blk * kBlockVoxels + vi] = f16x_pack(tsdf, w);
     }
 }
 
@@ -493,6 +525,11 @@ __device__ __forceinline__ void grid_dep_wait()
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Rule: a cooperative kernel, or any kernel whose CTAs wait for one another (a grid barrier,
+// like the persistent ICP's), is never launched with this attribute. Early-scheduled CTAs hold
+// SM slots while they wait for their predecessor, and a grid barrier assumes that all of its
+// CTAs are resident at once. Such kernels get an ordinary (or cooperative) launch, which starts
+// only after the previous kernel has finished.
 template <typename... KArgs, typename... Args>
 inline void launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t stream, Args... args)
 {

@@ -1202,6 +1202,25 @@ se_gpu_status se_gpu_tracker_test_barrier_timeout(se_gpu_tracker* t, int enable)
     return SE_GPU_OK;
 }
 
+se_gpu_status se_gpu_tracker_level_images(se_gpu_tracker* t, int level, float* depth_dev, float* pts_dev,
+                                          float* nrm_dev, void* stream_p)
+{
+    if (!t || level < 0 || level >= t->levels) {
+        set_last_error("se_gpu_tracker_level_images: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    const size_t n = (size_t) t->li.w[level] * (size_t) t->li.h[level];
+    if (depth_dev && level > 0)
+        SE_CUDA_TRY(cudaMemcpyAsync(depth_dev, t->pyr_depth[level], n * sizeof(float), cudaMemcpyDeviceToDevice,
+                                    stream));
+    if (pts_dev)
+        SE_CUDA_TRY(cudaMemcpyAsync(pts_dev, t->pts[level], 3 * n * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+    if (nrm_dev)
+        SE_CUDA_TRY(cudaMemcpyAsync(nrm_dev, t->nrm[level], 3 * n * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+    return SE_GPU_OK;
+}
+
 se_gpu_status se_gpu_tracker_last_reduction(se_gpu_tracker* t, float reduction[32], int iterations_run[3])
 {
     if (!t) {

@@ -15,7 +15,7 @@ oracle_fixtures.npz — small seeded inputs (stored: five 320x240 depth frames w
   count), a LiDAR occupancy scan (block coordinates and CRC of the mean pyramid, counts), the
   bilateral filter and downsample_depth of one frame (CRC), and the marching-cubes face count.
 
-    python tests/golden/make_golden.py [path/to/supereight2]
+    python tests/golden/make_golden.py path/to/supereight2
 """
 import json
 import os
@@ -144,7 +144,9 @@ def oracle_fixtures():
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <supereight2 source tree>")
+    src = sys.argv[1]
     with open(os.path.join(HERE, "reference_pins.json"), "w") as f:
         json.dump(reference_pins(src), f, indent=1)
     np.savez_compressed(os.path.join(HERE, "oracle_fixtures.npz"), **oracle_fixtures())

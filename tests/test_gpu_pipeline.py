@@ -128,3 +128,36 @@ def test_f16_storage_error_against_f32(gpu, data):
     valid = w32[a] > 0
     err = np.abs(t32[a] - t16[b])[valid]
     assert err.max() <= 1e-3                          # 1e-3 truncation units
+
+
+def test_f16_storage_within_tolerance_at_full_weight(gpu):
+    """The 300-frame 640x480 trajectory (1024^3 at 1 cm) integrated at ground-truth poses into
+    an FP32 and an FP16 map: weights reach max_weight = 100 and keep updating there, where a
+    running mean rounded to binary16 would drift by up to 100 * 2^-11; the FP16 layout's 8 guard
+    bits bound the difference by 100 * 2^-19 = 1.9e-4 truncation units (bar: 1e-3)."""
+    import torch
+    from supereight2_gb300 import synthetic as syn
+    spec, _, poses, frames = syn.dataset("tsdf640", 300, device="cuda")
+    sensor = gpu.PinholeCamera.from_spec(spec)
+    maps = {}
+    for st in ("f32", "f16"):
+        m = gpu.Map(10.24, 0.01, max_blocks=1 << 19, storage=st)
+        integ = gpu.MapIntegrator(m)
+        for i, (T, d) in enumerate(zip(poses, frames)):
+            integ.integrateDepth(i, torch.from_numpy(d).cuda(), sensor, T.astype(np.float32))
+        m.check()
+        maps[st] = m.download_blocks()
+        del m, integ
+        torch.cuda.empty_cache()
+    k32, _, t32, w32, _ = maps["f32"]
+    k16, _, t16, w16, _ = maps["f16"]
+    a, b = np.argsort(k32), np.argsort(k16)
+    assert np.array_equal(k32[a], k16[b])
+    assert np.array_equal(w32[a], w16[b])             # integer weights exact
+    assert w32.max() == 100.0
+    full = w32[a] == 100.0
+    assert full.sum() > 1_000_000                     # many voxels at (and past) max_weight
+    valid = w32[a] > 0
+    err = np.abs(t32[a] - t16[b])[valid]
+    assert err.max() <= 1e-3, float(err.max())        # 1e-3 truncation units
+    assert err.max() <= 100 * 2.0 ** -19 + 2e-5       # the layout's derived bound

@@ -100,3 +100,20 @@ def test_noalloc_rejects_what_it_cannot_hold(scene, gpu):
     assert st != 0 and b"allocation-free limit" in L.se_gpu_last_error()
     del big_d, big_p, big_n
     torch.cuda.synchronize()
+
+
+def test_noalloc_repeat_call_leaves_free_device_memory_unchanged(scene, gpu):
+    """After a first call on the device (which loads this part of the library there), further
+    calls allocate nothing: the device's free memory is the same before and after them."""
+    import torch
+    cfg = gpu.TrackerConfig(iterations=(10,))
+    T_ref, pts, nrm, depth = scene["refs"][3]
+    gpu.track_noalloc(scene["gs"], cfg, depth, T_ref.copy(), pts, nrm)  # warm-up call
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    for k in (3, 4):
+        T_k, pts_k, nrm_k, depth_k = scene["refs"][k]
+        gpu.track_noalloc(scene["gs"], cfg, depth_k, T_k.copy(), pts_k, nrm_k)
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
