@@ -139,8 +139,10 @@ __device__ __forceinline__ void acc_add(unsigned long long* buf, int copy, int t
     fixed_split(hi, I1, F1, bad);
     fixed_split(lo, I2, F2, bad);
     unsigned long long* p = buf + ((size_t) copy * 32 + term) * kAccStride;
-    atomicAdd(p, (unsigned long long) (I1 + I2));
-    atomicAdd(p + 1, F1 + F2);
+    // reductions without a returned value: the issuing thread does not wait for them (the grid
+    // barrier's release orders them before the arrival)
+    asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"((unsigned long long) (I1 + I2)) : "memory");
+    asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p + 1), "l"(F1 + F2) : "memory");
 }
 
 __device__ __forceinline__ double acc_total(const unsigned long long* buf, int term)
@@ -153,7 +155,17 @@ __device__ __forceinline__ double acc_total(const unsigned long long* buf, int t
         A += (long long) __ldcg(p);
         B += __ldcg(p + 1);
     }
-    return fma((double) B, 0x1p-50, (double) A * 0x1p-10);
+    // A 2^-10 and B 2^-50 as doubles without a 64-bit integer conversion: an integer added to the
+    // bits of 1.5 2^k (|integer| < 2^51) gives 1.5 2^k + integer 2^(k-52) exactly, and subtracting
+    // 1.5 2^k leaves the scaled integer (k = 42: units of 2^-10; k = 2: units of 2^-50). The sum of
+    // the two rounds once, like fma((double) B, 2^-50, (double) A 2^-10).
+    const long long kMagic10 = 0x4298000000000000LL, kMagic50 = 0x4018000000000000LL;
+    const double hi = (A > -(1LL << 51) && A < (1LL << 51))
+        ? __longlong_as_double(kMagic10 + A) - __longlong_as_double(kMagic10)
+        : (double) A * 0x1p-10;
+    const double lo = B < (1ULL << 51) ? __longlong_as_double(kMagic50 + (long long) B) - __longlong_as_double(kMagic50)
+                                       : (double) B * 0x1p-50;
+    return hi + lo;
 }
 
 // Zeroes the two words of every (copy, term) of a buffer, threads tid of nthreads.
@@ -398,114 +410,124 @@ __constant__ double kExpSeries[3][5] = {{1.0 / 362880, -1.0 / 5040, 1.0 / 120, -
 
 __device__ __forceinline__ double pick3(int k, double a, double b, double c) { return k == 0 ? a : (k == 1 ? b : c); }
 
+// Named barrier of the first `nthreads` threads (whole warps) of the CTA.
+__device__ __forceinline__ void bar_named(int id, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // Solves C x = b (C symmetric, the packed upper triangle of the newReduce layout in sh_val[7..27],
 // b = sh_val[1..6], icp.cpp:15-41), forms exp(x) (math_util_impl.hpp:117-174 in Rodrigues form:
 // R = I + A W + B W^2, V = I + B W + C W^2, W = hat(omega), translation V rho) and composes
 // T <- exp(x) T with the pose sh_pose (row-major 3x4): R T applied column by column as
 // c + A (omega x c) + B (omega x (omega x c)), the translation plus V rho. Writes the new pose to
-// sh_new / sh_newf and |x| < threshold to *sh_conv. Called by every thread of the CTA.
+// sh_new / sh_newf and |x| < threshold to *sh_conv. Called by every thread of the CTA; warps 0
+// and 1 (two sub-partitions, so their FP64 instructions run side by side) do the work and
+// synchronise among themselves with a named barrier, the other warps wait at the CTA barrier at
+// the end.
 __device__ __noinline__ void icp_tail(const double* sh_val, const double* sh_pose, double* sh_new, float* sh_newf,
-                                      int* sh_conv, float icp_threshold, int wbase)
+                                      int* sh_conv, float icp_threshold)
 {
     __shared__ double M[2][42];
     __shared__ double sh_x[6];
     __shared__ double sh_coef[3];
     __shared__ double sh_u[16], sh_u2[16];
     __shared__ int sh_ok;
-    // roles by warp wbase + 0 (elimination, coefficients) and wbase + 1 (elimination, cross
-    // products, convergence test): CTAs sharing an SM pass different wbase so that their FP64
-    // instructions go to different sub-partitions
-    const int warp = ((threadIdx.x >> 5) + 8 - wbase) & 7, lane = threadIdx.x & 31;
-    // elimination: entry e = 21 warp + lane (warps 0, 1, lanes < 21) is (r, c) of the 6 x 7 system
-    const bool gj = warp < 2 && lane < 21;
-    const int e = warp * 21 + lane, r = e / 7, c = e % 7;
-    if (gj) {
-        const int lo = r < c ? r : c, hi = r < c ? c : r;
-        M[0][e] = c == 6 ? sh_val[1 + r] : sh_val[7 + lo * 6 - lo * (lo - 1) / 2 + (hi - lo)];
-    }
-    if (threadIdx.x == 0)
-        sh_ok = 1;
-    __syncthreads();
-#pragma unroll 1
-    for (int j = 0; j < 6; ++j) {
-        const double* Mi = M[j & 1];
-        double* Mo = M[(j + 1) & 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp < 2) {
+        // elimination: entry e = 21 warp + lane (lanes < 21) is (r, c) of the 6 x 7 system; each
+        // lane keeps its entry in a register and publishes it for the other rows each step
+        const bool gj = lane < 21;
+        const int e = warp * 21 + lane, r = e / 7, c = e % 7;
+        double a = 0.0;
         if (gj) {
-            const double d = Mi[7 * j + j];
-            double a = Mi[e];
-            if (r != j)
-                a = c == j ? 0.0 : fma(d, a, -(Mi[7 * r + j] * Mi[7 * j + c]));
-            Mo[e] = a;
-            if (e == 0 && !pivot_ok(d))
-                sh_ok = 0;
+            const int lo = r < c ? r : c, hi = r < c ? c : r;
+            a = c == 6 ? sh_val[1 + r] : sh_val[7 + lo * 6 - lo * (lo - 1) / 2 + (hi - lo)];
+            M[0][e] = a;
         }
-        __syncthreads();
-    }
-    if (gj && c == 6)
-        sh_x[r] = sh_ok ? div_pos(M[0][e], M[0][7 * r + r]) : 0.0;
-    __syncthreads();
-
-    const double wx = sh_x[3], wy = sh_x[4], wz = sh_x[5];
-    if (warp == 0) {
-        // lanes 0, 1, 2: the coefficients A, B, C
-        const double xx = fma(wz, wz, fma(wy, wy, wx * wx));
-        const int k = lane < 3 ? lane : 0;
-        double coef;
-        if (lt_nonneg(xx, 0.01)) {
-            // Horner in x; below 1e-5 (1e-7) the terms past x^2 (x) are under 1e-18 relative
-            const int first = lt_nonneg(xx, 1e-7) ? 3 : (lt_nonneg(xx, 1e-5) ? 2 : 0);
-            coef = kExpSeries[k][first];
+        if (threadIdx.x == 0)
+            sh_ok = 1;
+        bar_named(1, 64);
 #pragma unroll 1
-            for (int u = first + 1; u < 5; ++u)
-                coef = fma(coef, xx, kExpSeries[k][u]);
+        for (int j = 0; j < 6; ++j) {
+            const double* Mi = M[j & 1];
+            double* Mo = M[(j + 1) & 1];
+            if (gj) {
+                const double d = Mi[7 * j + j];
+                if (r != j)
+                    a = c == j ? 0.0 : fma(d, a, -(Mi[7 * r + j] * Mi[7 * j + c]));
+                Mo[e] = a;
+                if (e == 0 && !pivot_ok(d))
+                    sh_ok = 0;
+            }
+            bar_named(1, 64);
+        }
+        if (gj && c == 6)
+            sh_x[r] = sh_ok ? div_pos(a, M[0][7 * r + r]) : 0.0;
+        bar_named(1, 64);
+
+        const double wx = sh_x[3], wy = sh_x[4], wz = sh_x[5];
+        if (warp == 0) {
+            // lanes 0, 1, 2: the coefficients A, B, C
+            const double xx = fma(wz, wz, fma(wy, wy, wx * wx));
+            const int k = lane < 3 ? lane : 0;
+            double coef;
+            if (lt_nonneg(xx, 0.01)) {
+                // Horner in x; below 1e-5 (1e-7) the terms past x^2 (x) are under 1e-18 relative
+                const int first = lt_nonneg(xx, 1e-7) ? 3 : (lt_nonneg(xx, 1e-5) ? 2 : 0);
+                coef = kExpSeries[k][first];
+#pragma unroll 1
+                for (int u = first + 1; u < 5; ++u)
+                    coef = fma(coef, xx, kExpSeries[k][u]);
+            }
+            else {
+                const double t = sqrt(xx);
+                double sn, cs;
+                sincos(t, &sn, &cs);
+                const double it = drcp(t), it2 = it * it;
+                coef = k == 0 ? sn * it : (k == 1 ? (1.0 - cs) * it2 : (t - sn) * it2 * it);
+            }
+            if (lane < 3)
+                sh_coef[lane] = coef;
         }
         else {
-            const double t = sqrt(xx);
-            double sn, cs;
-            sincos(t, &sn, &cs);
-            const double it = drcp(t), it2 = it * it;
-            coef = k == 0 ? sn * it : (k == 1 ? (1.0 - cs) * it2 : (t - sn) * it2 * it);
+            // lanes 0..11: column lane / 3, row lane % 3 of the pose; lanes 12..14: rho
+            const int l = lane < 15 ? lane : 14;
+            const int col = l / 3, i = l % 3, i1 = i == 2 ? 0 : i + 1, i2 = i == 0 ? 2 : i - 1;
+            const double v1 = l < 12 ? sh_pose[4 * i1 + col] : sh_x[i1];
+            const double v2 = l < 12 ? sh_pose[4 * i2 + col] : sh_x[i2];
+            const double u = fma(pick3(i1, wx, wy, wz), v2, -(pick3(i2, wx, wy, wz) * v1)); // (omega x v)_i
+            const int base = l - i;
+            const double u1 = __shfl_sync(0xffffffffu, u, base + i1), u2 = __shfl_sync(0xffffffffu, u, base + i2);
+            const double uu = fma(pick3(i1, wx, wy, wz), u2, -(pick3(i2, wx, wy, wz) * u1));
+            if (lane < 15) {
+                sh_u[lane] = u;
+                sh_u2[lane] = uu;
+            }
+            // the convergence test in FP32, as the reference's x.norm() < icp_threshold on its
+            // FP32 x (icp.cpp:218)
+            const float xf = lane < 6 ? (float) sh_x[lane] : 0.0f;
+            float q = xf * xf;
+            q += __shfl_down_sync(0xffffffffu, q, 4);
+            q += __shfl_down_sync(0xffffffffu, q, 2);
+            q += __shfl_down_sync(0xffffffffu, q, 1);
+            if (lane == 0)
+                *sh_conv = sqrtf(q) < icp_threshold;
         }
-        if (lane < 3)
-            sh_coef[lane] = coef;
-    }
-    else if (warp == 1) {
-        // lanes 0..11: column lane / 3, row lane % 3 of the pose; lanes 12..14: rho
-        const int l = lane < 15 ? lane : 14;
-        const int col = l / 3, i = l % 3, i1 = i == 2 ? 0 : i + 1, i2 = i == 0 ? 2 : i - 1;
-        const double v1 = l < 12 ? sh_pose[4 * i1 + col] : sh_x[i1];
-        const double v2 = l < 12 ? sh_pose[4 * i2 + col] : sh_x[i2];
-        const double u = fma(pick3(i1, wx, wy, wz), v2, -(pick3(i2, wx, wy, wz) * v1)); // (omega x v)_i
-        const int base = l - i;
-        const double u1 = __shfl_sync(0xffffffffu, u, base + i1), u2 = __shfl_sync(0xffffffffu, u, base + i2);
-        const double uu = fma(pick3(i1, wx, wy, wz), u2, -(pick3(i2, wx, wy, wz) * u1));
-        if (lane < 15) {
-            sh_u[lane] = u;
-            sh_u2[lane] = uu;
-        }
-        // the convergence test in FP32, as the reference's x.norm() < icp_threshold on its FP32
-        // x (icp.cpp:218)
-        const float xf = lane < 6 ? (float) sh_x[lane] : 0.0f;
-        float q = xf * xf;
-        q += __shfl_down_sync(0xffffffffu, q, 4);
-        q += __shfl_down_sync(0xffffffffu, q, 2);
-        q += __shfl_down_sync(0xffffffffu, q, 1);
-        if (lane == 0)
-            *sh_conv = sqrtf(q) < icp_threshold;
-    }
-    __syncthreads();
-    if (warp == 1) {
-        const int l = lane < 15 ? lane : 14;
-        const int col = l / 3, i = l % 3;
-        const double c1 = l < 12 ? sh_coef[0] : sh_coef[1], c2 = l < 12 ? sh_coef[1] : sh_coef[2];
-        const double v = l < 12 ? sh_pose[4 * i + col] : sh_x[i];
-        double val = fma(c2, sh_u2[l], fma(c1, sh_u[l], v));
-        const double vrho = __shfl_down_sync(0xffffffffu, val, 3); // lanes 9..11 take V rho from 12..14
-        if (lane >= 9 && lane < 12)
-            val += vrho;
-        if (lane < 12) {
-            sh_new[4 * i + col] = val;
-            sh_newf[4 * i + col] = (float) val;
+        bar_named(1, 64);
+        if (warp == 1) {
+            const int l = lane < 15 ? lane : 14;
+            const int col = l / 3, i = l % 3;
+            const double c1 = l < 12 ? sh_coef[0] : sh_coef[1], c2 = l < 12 ? sh_coef[1] : sh_coef[2];
+            const double v = l < 12 ? sh_pose[4 * i + col] : sh_x[i];
+            double val = fma(c2, sh_u2[l], fma(c1, sh_u[l], v));
+            const double vrho = __shfl_down_sync(0xffffffffu, val, 3); // lanes 9..11 take V rho from 12..14
+            if (lane >= 9 && lane < 12)
+                val += vrho;
+            if (lane < 12) {
+                sh_new[4 * i + col] = val;
+                sh_newf[4 * i + col] = (float) val;
+            }
         }
     }
     __syncthreads();
@@ -520,6 +542,7 @@ struct IterParams {
     int W;             // full-resolution width (row stride of the reference images)
     int level;
     float dist_threshold, normal_threshold, icp_threshold;
+    int ncta, nthr;    // ICP pass partition: CTAs and threads per CTA that hold pixels at this level
 };
 
 // trackKernel for one pixel (icp_impl.hpp:16-102) given its input normal and point, its 32
@@ -615,23 +638,271 @@ __device__ __forceinline__ void icp_flush_terms(float sum[32], float (*sh_t)[33]
 // Pixels a thread adds in plain FP32 before its sums go into the compensated accumulators.
 constexpr int kIcpFlushRounds = 8;
 
-// One ICP iteration: trackKernel + newReduce/reduceKernel + updatePoseKernel.
-// Main phase: each warp takes 32 pixels per tile (the next tile's input normal and point are
-// loaded before the current one is processed); the 32 x 32 term matrix goes through shared
-// memory (stride 33: conflict-free) so that lane k accumulates term k, with two-sum
-// compensation in 4 independent accumulators. Tail (last CTA to finish, found with an atomic
-// ticket, no waiting): the exact sum of the CTA partials, then the FP64 solve, exponential and
-// pose composition.
-__global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, IterParams ip, TrackState* st,
-                                                                   unsigned long long* __restrict__ acc_buf)
+// ------------------------------------------------------------------ ICP main pass --
+// One CTA per SM, kIcpThreads threads. Each thread takes pixels i, i + S, i + 2S, ... of the
+// level (S = CTAs x threads) two at a time: both pixels' inputs, then both projections, then
+// both reference gathers in flight together, then both pixels' terms (the next pair's inputs
+// are loaded meanwhile). trackKernel's decisions (icp_impl.hpp:16-102) use the same float
+// operations as the oracle; the 28 reduction sums of newReduce (icp.cpp:45-184) are
+// accumulated per thread with fused multiply-adds over at most 8 pixels, then lane k of the
+// warp adds term k of the 32 lanes into two-sum compensated accumulators; the four counters
+// (inliers, distance rejects, normal rejects, other rejects) are integers.
+constexpr int kIcpThreads = 512;
+constexpr int kIcpWarps = kIcpThreads / 32;
+constexpr int kIcpPairRounds = 4; // pairs a thread adds before its sums go to the compensated accumulators
+
+struct IcpIn {
+    F3 n, p;
+    bool in;
+};
+
+__device__ __forceinline__ IcpIn icp_load(const IterParams& ip, int i, int npix)
 {
-    constexpr int kWarps = kTrackThreads / 32;
-    __shared__ float sh_terms[kWarps][32][33];
-    __shared__ float2 sh_warp[kWarps][32];
-    __shared__ int sh_last;
-    __shared__ Tf T, Tri; // the poses live in shared memory: fewer live registers per thread
-    if (st->flags[kFlagDone0 + ip.level])
+    IcpIn a;
+    a.in = i < npix;
+    if (a.in) {
+        a.n = ld3(ip.nrm, (size_t) i);
+        a.p = ld3(ip.pts, (size_t) i);
+    }
+    else {
+        a.n = f3(0.0f, 0.0f, 0.0f);
+        a.p = a.n;
+    }
+    return a;
+}
+
+// A pixel after its projection: code 0 = gather the reference pixel ri; -1 / -2 = rejected
+// (invalid input normal / projection outside); 2 = no pixel.
+struct IcpPre {
+    int code;
+    int ri;
+    F3 p_W, n_in;
+};
+
+__device__ __forceinline__ IcpPre icp_pre(const Pinhole& s, const IterParams& ip, const Tf& T, const Tf& Tri,
+                                          const IcpIn& a)
+{
+    IcpPre q;
+    q.code = 2;
+    q.ri = 0;
+    q.p_W = f3(0.0f, 0.0f, 0.0f);
+    q.n_in = a.n;
+    if (!a.in)
+        return q;
+    if (a.n.x == 0.0f && a.n.y == 0.0f && a.n.z == 0.0f) {
+        q.code = -1;
+        return q;
+    }
+    q.p_W = apply(T, a.p);
+    const F3 p_ref = apply(Tri, q.p_W);
+    float u, v;
+    if (!project(s, p_ref, u, v)) {
+        q.code = -2;
+        return q;
+    }
+    q.ri = (int) (u + 0.5f) + (int) (v + 0.5f) * ip.W;
+    q.code = 0;
+    return q;
+}
+
+struct IcpRef {
+    F3 rn, rp;
+};
+
+__device__ __forceinline__ IcpRef icp_ref(const IterParams& ip, const IcpPre& q)
+{
+    IcpRef r;
+    if (q.code == 0) {
+        r.rn = ld3(ip.ref_nrm, (size_t) q.ri);
+        r.rp = ld3(ip.ref_pts, (size_t) q.ri);
+    }
+    else {
+        r.rn = f3(0.0f, 0.0f, 0.0f);
+        r.rp = r.rn;
+    }
+    return r;
+}
+
+// The rest of trackKernel for one projected pixel, and its terms added.
+__device__ __forceinline__ void icp_finish(const IterParams& ip, const Tf& T, const IcpPre& q, const IcpRef& r,
+                                           float sum[28], int cnt[4])
+{
+    if (q.code == 2)
         return;
+    int result = q.code;
+    float e = 0.0f;
+    float J[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    if (result == 0) {
+        const F3 n_ref = f3(-r.rn.x, -r.rn.y, -r.rn.z);
+        if (n_ref.x == 0.0f && n_ref.y == 0.0f && n_ref.z == 0.0f) {
+            result = -3;
+        }
+        else {
+            const F3 diff = sub(r.rp, q.p_W);
+            const F3 n_W = rot(T, q.n_in);
+            if (norm(diff) > ip.dist_threshold) {
+                result = -4;
+            }
+            else if (dot(n_W, n_ref) < ip.normal_threshold) {
+                result = -5;
+            }
+            else {
+                result = 1;
+                e = dot(n_ref, diff);
+                const F3 c = cross(q.p_W, n_ref);
+                J[0] = n_ref.x;
+                J[1] = n_ref.y;
+                J[2] = n_ref.z;
+                J[3] = c.x;
+                J[4] = c.y;
+                J[5] = c.z;
+            }
+        }
+    }
+    if (result < 1) {
+        cnt[1] += result == -4 ? 1 : 0;
+        cnt[2] += result == -5 ? 1 : 0;
+        cnt[3] += result > -4 ? 1 : 0;
+        return;
+    }
+    cnt[0] += 1;
+    sum[0] = __fmaf_rn(e, e, sum[0]);
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        sum[1 + k] = __fmaf_rn(e, J[k], sum[1 + k]);
+    int q2 = 7;
+#pragma unroll
+    for (int rr = 0; rr < 6; ++rr)
+#pragma unroll
+        for (int cc = rr; cc < 6; ++cc) {
+            sum[q2] = __fmaf_rn(J[rr], J[cc], sum[q2]);
+            ++q2;
+        }
+}
+
+// Lane k (< 28) of the warp sums term k of the 32 lanes' sums (the 32 x 28 term matrix goes
+// through this warp's slice of shared memory, stride 29: conflict-free) in plain FP32, pairwise
+// over four partial sums of eight, and adds the result into its compensated accumulator; the
+// sums restart from zero.
+constexpr int kIcpTermStride = 29;
+constexpr size_t kIcpDynSmem = (size_t) kIcpWarps * 32 * kIcpTermStride * sizeof(float);
+
+__device__ __forceinline__ void icp_flush28(float sum[28], float* sh_t, CSum& acc)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 28; ++k) {
+        sh_t[lane * kIcpTermStride + k] = sum[k];
+        sum[k] = 0.0f;
+    }
+    __syncwarp();
+    if (lane < 28) {
+        float p[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            p[j & 3] += sh_t[j * kIcpTermStride + lane];
+        acc.add((p[0] + p[1]) + (p[2] + p[3]));
+    }
+    __syncwarp();
+}
+
+// The first pair of pixels a thread of CTA cta takes at a level (loaded ahead of the pass).
+__device__ __forceinline__ void icp_first_pair(const IterParams& ip, int cta, IcpIn& a, IcpIn& b)
+{
+    const int npix = ip.w * ip.h;
+    const int i = cta < ip.ncta && (int) threadIdx.x < ip.nthr ? cta * ip.nthr + (int) threadIdx.x : npix;
+    a = icp_load(ip, i, npix);
+    b = icp_load(ip, i + ip.ncta * ip.nthr, npix);
+}
+
+// This CTA's share of one ICP iteration: its pixels' terms summed and merged exactly into the
+// global accumulators buf (copy cta % kAccCopies). Threads tid < ip.nthr of CTAs cta < ip.ncta
+// hold pixels (at least four per thread where the level allows: the per-warp flush and the
+// merge are fixed costs); (a, b) is the thread's first pair (icp_first_pair). Every thread of
+// the CTA calls it; ends with a CTA barrier. Warp 0 merges the warps' compensated partials of
+// term k (lane k) in warp order.
+__device__ __forceinline__ void icp_cta_pass(const Pinhole& s, const IterParams& ip, const Tf T, const Tf Tri,
+                                             int cta, unsigned long long* buf, int* overflow_flag, IcpIn a, IcpIn b)
+{
+    extern __shared__ float icp_dyn_smem[]; // kIcpDynSmem bytes: the warps' term matrices
+    __shared__ float2 sh_warp[kIcpWarps][32];
+    __shared__ int sh_cnt[4];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool active = cta < ip.ncta && (int) threadIdx.x < ip.nthr; // uniform per warp
+    if (threadIdx.x < 4)
+        sh_cnt[threadIdx.x] = 0;
+    CSum acc{0.0f, 0.0f};
+    int cnt[4] = {0, 0, 0, 0};
+    if (active) {
+        float sum[28];
+#pragma unroll
+        for (int k = 0; k < 28; ++k)
+            sum[k] = 0.0f;
+        const int npix = ip.w * ip.h;
+        const int stride = ip.ncta * ip.nthr;
+        int i = cta * ip.nthr + threadIdx.x;
+        int rounds = 0;
+        for (int base = cta * ip.nthr; base < npix; base += 2 * stride) { // uniform across the active warps
+            const int inext = i + 2 * stride;
+            const IcpIn a2 = icp_load(ip, inext, npix), b2 = icp_load(ip, inext + stride, npix);
+            const IcpPre qa = icp_pre(s, ip, T, Tri, a), qb = icp_pre(s, ip, T, Tri, b);
+            const IcpRef ra = icp_ref(ip, qa), rb = icp_ref(ip, qb);
+            icp_finish(ip, T, qa, ra, sum, cnt);
+            icp_finish(ip, T, qb, rb, sum, cnt);
+            if (++rounds == kIcpPairRounds || base + 2 * stride >= npix) {
+                icp_flush28(sum, icp_dyn_smem + warp * 32 * kIcpTermStride, acc);
+                rounds = 0;
+            }
+            a = a2;
+            b = b2;
+            i = inext;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            cnt[k] = __reduce_add_sync(0xffffffffu, cnt[k]);
+        sh_warp[warp][lane] = make_float2(acc.hi, acc.lo);
+    }
+    __syncthreads();
+    if (active && lane < 4 && cnt[lane] != 0)
+        atomicAdd(&sh_cnt[lane], cnt[lane]);
+    __syncthreads();
+    if (warp == 0 && cta < ip.ncta) {
+        float hi, lo;
+        if (lane < 28) {
+            CSum t{0.0f, 0.0f};
+            const int nw = ip.nthr >> 5;
+            for (int wi = 0; wi < nw; ++wi)
+                t.merge(sh_warp[wi][lane].x, sh_warp[wi][lane].y);
+            hi = t.hi;
+            lo = t.lo;
+        }
+        else {
+            hi = (float) sh_cnt[lane - 28]; // exact: at most 2^24 pixels per CTA
+            lo = 0.0f;
+        }
+        bool bad = false;
+        acc_add(buf, cta % kAccCopies, lane, hi, lo, bad);
+        if (bad)
+            atomicExch(overflow_flag, 1);
+    }
+    __syncthreads();
+}
+
+// The merged totals of buf in sh_val (warp 0), and the final reduction in st->last_red when
+// record is set.
+__device__ __forceinline__ void icp_read_totals(const unsigned long long* buf, double* sh_val, TrackState* st,
+                                                bool record)
+{
+    if (threadIdx.x < 32) {
+        const double v = acc_total(buf, threadIdx.x);
+        sh_val[threadIdx.x] = v;
+        if (record)
+            st->last_red[threadIdx.x] = (float) v;
+    }
+}
+
+__device__ __forceinline__ void icp_pose_to_shared(const TrackState* st, Tf& T, Tf& Tri, double* sh_pose)
+{
     if (threadIdx.x < 12) {
         const int i = threadIdx.x, r = i >> 2, c = i & 3;
         if (c < 3) {
@@ -642,51 +913,27 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
             T.t[r] = st->pose_f[i];
             Tri.t[r] = st->ref_inv[i];
         }
+        if (sh_pose)
+            sh_pose[i] = st->pose[i];
     }
-    __syncthreads();
+}
 
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    CSum acc[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
-    const int npix = ip.w * ip.h;
-    const int stride = gridDim.x * kTrackThreads;
-    int i = blockIdx.x * kTrackThreads + threadIdx.x;
-    bool in_range = i < npix;
-    F3 n_cur = in_range ? ld3(ip.nrm, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
-    F3 p_cur = in_range ? ld3(ip.pts, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
-    float sum[32];
-#pragma unroll
-    for (int k = 0; k < 32; ++k)
-        sum[k] = 0.0f;
-    int rounds = 0;
-    for (int base = blockIdx.x * kTrackThreads; base < npix; base += stride) {
-        const int i_next = i + stride;
-        const bool next_in = i_next < npix;
-        const F3 n_next = next_in ? ld3(ip.nrm, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
-        const F3 p_next = next_in ? ld3(ip.pts, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
-        icp_pixel_add(s, ip, T, Tri, in_range, n_cur, p_cur, sum);
-        if (++rounds == kIcpFlushRounds || base + stride >= npix) { // uniform across the CTA
-            icp_flush_terms(sum, sh_terms[warp], acc);
-            rounds = 0;
-        }
-        i = i_next;
-        in_range = next_in;
-        n_cur = n_next;
-        p_cur = p_next;
-    }
-    acc[0].merge(acc[1].hi, acc[1].lo);
-    acc[2].merge(acc[3].hi, acc[3].lo);
-    acc[0].merge(acc[2].hi, acc[2].lo);
-    sh_warp[warp][lane] = make_float2(acc[0].hi, acc[0].lo);
+// One ICP iteration (the fallback when the persistent grid cannot be resident at once):
+// every CTA adds its partial; the last CTA to finish (atomic ticket, no waiting) solves and
+// updates the pose. Same partition, merge and tail as the persistent kernel: bit-identical poses.
+__global__ void __launch_bounds__(kIcpThreads, 1) icp_iter_kernel(Pinhole s, IterParams ip, TrackState* st,
+                                                                 unsigned long long* __restrict__ acc_buf)
+{
+    __shared__ Tf T, Tri;
+    __shared__ int sh_last;
+    if (st->flags[kFlagDone0 + ip.level])
+        return;
+    icp_pose_to_shared(st, T, Tri, nullptr);
     __syncthreads();
-    if (threadIdx.x < 32) {
-        CSum t{0.0f, 0.0f};
-        for (int wi = 0; wi < kWarps; ++wi)
-            t.merge(sh_warp[wi][threadIdx.x].x, sh_warp[wi][threadIdx.x].y);
-        bool bad = false;
-        acc_add(acc_buf, (int) (blockIdx.x % kAccCopies), threadIdx.x, t.hi, t.lo, bad);
-        if (bad)
-            atomicExch(&st->flags[kFlagOverflow], 1);
-    }
+    const Tf Tl = T, Tril = Tri;
+    IcpIn a, b;
+    icp_first_pair(ip, blockIdx.x, a, b);
+    icp_cta_pass(s, ip, Tl, Tril, blockIdx.x, acc_buf, &st->flags[kFlagOverflow], a, b);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0)
@@ -704,13 +951,9 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_kernel(Pinhole s, I
     __shared__ int sh_conv;
     if (threadIdx.x < 12)
         sh_pose[threadIdx.x] = __ldcg(&st->pose[threadIdx.x]);
-    if (threadIdx.x < 32) {
-        const double v = acc_total(acc_buf, threadIdx.x);
-        sh_val[threadIdx.x] = v;
-        st->last_red[threadIdx.x] = (float) v;
-    }
+    icp_read_totals(acc_buf, sh_val, st, true);
     __syncthreads();
-    icp_tail(sh_val, sh_pose, sh_new, sh_newf, &sh_conv, ip.icp_threshold, 0);
+    icp_tail(sh_val, sh_pose, sh_new, sh_newf, &sh_conv, ip.icp_threshold);
     acc_clear(acc_buf, threadIdx.x, blockDim.x); // for the next launch (every CTA has added)
     if (threadIdx.x < 12) {
         st->pose[threadIdx.x] = sh_new[threadIdx.x];
@@ -749,9 +992,9 @@ __global__ void icp_check_kernel(TrackState* st, int W, int H, float track_thres
 }
 
 // ------------------------------------------------------- persistent ICP (all iterations) --
-// The per-iteration launches above, fused into one cooperative launch per frame: every CTA
-// runs every iteration of every level; after each iteration's main pass the CTAs meet at a
-// grid barrier, and each CTA then reads the exact totals and solves redundantly (the same
+// The per-iteration launches above, fused into one cooperative launch per frame, one CTA per
+// SM: every CTA runs every iteration of every level; after each iteration's pass the CTAs meet
+// at a grid barrier, and each CTA then reads the exact totals and solves redundantly (the same
 // operations on the same values, so every CTA holds the same new pose) instead of one last CTA
 // solving and the next launch reading its result. The pixel partition, the exact merge and the
 // FP64 tail are those of icp_iter_kernel, so the poses are bit-identical to it.
@@ -761,16 +1004,13 @@ struct IcpLevels {
     int nctas[3];
     int iters[3];
     int levels;
-    unsigned* sm_slots; // per-SM arrival counters (kIcpSlotCounters, never reset)
     int W, H;           // checkPoseKernel's image size and threshold, and where the pose goes
     float track_threshold;
     float* pose12_out;
     int missing_ctas;   // test aid: CTAs the barrier waits for beyond the grid (0 in use)
 };
 
-constexpr int kIcpSlotCounters = 1024;
-
-constexpr unsigned kIcpSpinLimit = 1u << 22;                // polls at most, and
+constexpr unsigned kIcpSpinLimit = 1u << 24;                // polls at most, and
 constexpr unsigned long long kIcpWaitNs = 500000000ull;     // half a second at most, then the timeout flag
 
 __device__ __forceinline__ unsigned long long global_ns()
@@ -780,127 +1020,74 @@ __device__ __forceinline__ unsigned long long global_ns()
     return t;
 }
 
-// Grid barrier on a monotonic counter (reset to 0 before the launch): every CTA adds one and
-// waits until the count reaches target. Bounded: on timeout (or when another CTA timed out)
-// the flag is set and the CTA goes on, so a stuck launch ends with an error instead of hanging.
+// Grid barrier on a monotonic counter (reset to 0 before the launch): after a CTA barrier (the
+// CTA's atomics precede it), one thread adds its arrival with release semantics and polls with
+// acquire loads until the count reaches target; the CTA barrier after it orders every thread's
+// later reads of the merged totals. Bounded: on timeout (or when another CTA timed out) the flag
+// is set and the CTA goes on, so a stuck launch ends with an error instead of hanging.
 __device__ __forceinline__ void icp_grid_sync(unsigned* ctr, unsigned target, int* timeout)
 {
-    __threadfence(); // every thread's partial stores before the arrival
     __syncthreads();
     if (threadIdx.x == 0) {
-        atomicAdd(ctr, 1u);
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctr) : "memory");
         unsigned spins = 0;
         const unsigned long long t0 = global_ns();
-        while (*((volatile unsigned*) ctr) < target) {
-            if (*((volatile int*) timeout) != 0 || ++spins > kIcpSpinLimit || global_ns() - t0 > kIcpWaitNs) {
+        while (true) {
+            unsigned v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+            if (v >= target)
+                break;
+            if ((++spins & 63u) == 0u
+                && (*((volatile int*) timeout) != 0 || spins > kIcpSpinLimit || global_ns() - t0 > kIcpWaitNs)) {
                 atomicExch(timeout, 1);
                 break;
             }
-            __nanosleep(32);
         }
-        __threadfence();
     }
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kTrackThreads, 3) icp_persistent_kernel(Pinhole s, IcpLevels L, TrackState* st,
-                                                                         unsigned long long* __restrict__ acc_base)
+__global__ void __launch_bounds__(kIcpThreads, 1) icp_persistent_kernel(Pinhole s, IcpLevels L, TrackState* st,
+                                                                       unsigned long long* __restrict__ acc_base)
 {
-    constexpr int kWarps = kTrackThreads / 32;
-    __shared__ float sh_terms[kWarps][32][33];
-    __shared__ float2 sh_warp[kWarps][32];
     __shared__ Tf T, Tri;
     __shared__ double sh_pose[12];
     __shared__ double sh_new[12];
     __shared__ float sh_newf[12];
     __shared__ double sh_val[32];
     __shared__ int sh_conv;
-    __shared__ int sh_wbase;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) {
-        // the CTAs that share an SM count their arrivals there and alternate the warps of the
-        // FP64 tail (consecutive counts differ in parity, whatever earlier launches left)
-        unsigned smid;
-        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-        sh_wbase = (int) (atomicAdd(&L.sm_slots[smid % kIcpSlotCounters], 1u) & 1u) * 2;
-    }
-    if (threadIdx.x < 12) {
-        const int i = threadIdx.x, r = i >> 2, c = i & 3;
-        if (c < 3) {
-            T.R[3 * r + c] = st->pose_f[i];
-            Tri.R[3 * r + c] = st->ref_inv[i];
-        }
-        else {
-            T.t[r] = st->pose_f[i];
-            Tri.t[r] = st->ref_inv[i];
-        }
-        sh_pose[i] = st->pose[i];
-    }
+    icp_pose_to_shared(st, T, Tri, sh_pose);
+    // the first pair of the next pass is loaded before the barrier and the tail of the current
+    // iteration (its inputs do not depend on the pose), assuming the level goes on; a level that
+    // converges early reloads it
+    int pf_level = L.levels - 1;
+    IcpIn pa, pb;
+    icp_first_pair(L.ip[pf_level], blockIdx.x, pa, pb);
     __syncthreads();
     unsigned phase = 0;
     for (int level = L.levels - 1; level >= 0; --level) {
         const IterParams& ip = L.ip[level];
-        const int nct = L.nctas[level];
         for (int iter = 0; iter < L.iters[level]; ++iter) {
             unsigned long long* buf = acc_base + (size_t) (phase % kAccBuffers) * kAccBufWords;
-            if ((int) blockIdx.x < nct) {
-                CSum acc[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
-                const int npix = ip.w * ip.h;
-                const int stride = nct * kTrackThreads;
-                int i = blockIdx.x * kTrackThreads + threadIdx.x;
-                bool in_range = i < npix;
-                F3 n_cur = in_range ? ld3(ip.nrm, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
-                F3 p_cur = in_range ? ld3(ip.pts, (size_t) i) : f3(0.0f, 0.0f, 0.0f);
-                float sum[32];
-#pragma unroll
-                for (int k = 0; k < 32; ++k)
-                    sum[k] = 0.0f;
-                int rounds = 0;
-                for (int base = blockIdx.x * kTrackThreads; base < npix; base += stride) {
-                    const int i_next = i + stride;
-                    const bool next_in = i_next < npix;
-                    const F3 n_next = next_in ? ld3(ip.nrm, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
-                    const F3 p_next = next_in ? ld3(ip.pts, (size_t) i_next) : f3(0.0f, 0.0f, 0.0f);
-                    icp_pixel_add(s, ip, T, Tri, in_range, n_cur, p_cur, sum);
-                    if (++rounds == kIcpFlushRounds || base + stride >= npix) { // uniform across the CTA
-                        icp_flush_terms(sum, sh_terms[warp], acc);
-                        rounds = 0;
-                    }
-                    i = i_next;
-                    in_range = next_in;
-                    n_cur = n_next;
-                    p_cur = p_next;
-                }
-                acc[0].merge(acc[1].hi, acc[1].lo);
-                acc[2].merge(acc[3].hi, acc[3].lo);
-                acc[0].merge(acc[2].hi, acc[2].lo);
-                sh_warp[warp][lane] = make_float2(acc[0].hi, acc[0].lo);
-                __syncthreads();
-                if (threadIdx.x < 32) {
-                    CSum t{0.0f, 0.0f};
-                    for (int wi = 0; wi < kWarps; ++wi)
-                        t.merge(sh_warp[wi][threadIdx.x].x, sh_warp[wi][threadIdx.x].y);
-                    bool bad = false;
-                    acc_add(buf, (int) (blockIdx.x % kAccCopies), threadIdx.x, t.hi, t.lo, bad);
-                    if (bad)
-                        atomicExch(&st->flags[kFlagOverflow], 1);
-                }
+            if (pf_level != level)
+                icp_first_pair(ip, blockIdx.x, pa, pb);
+            {
+                const Tf Tl = T, Tril = Tri; // the poses in registers for the pass
+                icp_cta_pass(s, ip, Tl, Tril, blockIdx.x, buf, &st->flags[kFlagOverflow], pa, pb);
             }
+            pf_level = iter + 1 < L.iters[level] ? level : level - 1;
+            if (pf_level >= 0)
+                icp_first_pair(L.ip[pf_level], blockIdx.x, pa, pb);
             ++phase;
             icp_grid_sync(&st->ticket, phase * (gridDim.x + L.missing_ctas), &st->flags[kFlagBarrierTimeout]);
             // every CTA: the merged totals, then the solve and update. The buffer used two phases
             // ago has been read by every CTA before this barrier: CTA 0 clears it for the phase
             // after next.
-            if (threadIdx.x < 32) {
-                const double v = acc_total(buf, threadIdx.x);
-                sh_val[threadIdx.x] = v;
-                if (blockIdx.x == 0)
-                    st->last_red[threadIdx.x] = (float) v;
-            }
+            icp_read_totals(buf, sh_val, st, blockIdx.x == 0);
             if (blockIdx.x == 0)
                 acc_clear(acc_base + (size_t) ((phase + 1) % kAccBuffers) * kAccBufWords, threadIdx.x, blockDim.x);
             __syncthreads();
-            icp_tail(sh_val, sh_pose, sh_new, sh_newf, &sh_conv, ip.icp_threshold, sh_wbase);
+            icp_tail(sh_val, sh_pose, sh_new, sh_newf, &sh_conv, ip.icp_threshold);
             if (blockIdx.x == 0 && threadIdx.x == 0)
                 st->flags[kFlagIters0 + level] = iter + 1; // a store: no global read on the critical path
             if (threadIdx.x < 12) {
@@ -936,6 +1123,7 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_persistent_kernel(Pinhol
 
 } // namespace se_gpu
 
+
 using namespace se_gpu;
 
 struct se_gpu_tracker {
@@ -948,13 +1136,40 @@ struct se_gpu_tracker {
     float* pts[3];
     float* nrm[3];
     unsigned long long* acc; // kAccBuffers exact-merge accumulators (the persistent kernel rotates)
-    unsigned* sm_slots;  // kIcpSlotCounters per-SM counters of the persistent kernel
     TrackState* state;
-    int nctas[3];
+    int nctas[3];        // CTAs that hold pixels at each level (at most one per SM)
+    int nthrs[3];        // threads per CTA that hold pixels at each level
     int persistent;      // one cooperative launch per frame (when the grid fits on the GPU)
     int missing_ctas;    // se_gpu_tracker_test_barrier_timeout
-    int persistent_ctas; // its grid: the largest level's CTA count
+    int persistent_ctas; // its grid: one CTA per SM
 };
+
+namespace se_gpu {
+// The ICP kernels' dynamic shared memory (above the 48 KiB default), set once per process.
+static cudaError_t icp_kernel_attributes()
+{
+    static std::once_flag once;
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [] {
+        err = cudaFuncSetAttribute(icp_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int) kIcpDynSmem);
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(icp_iter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int) kIcpDynSmem);
+    });
+    return err;
+}
+
+// Whether the persistent ICP's grid (one CTA per SM) can be resident at once.
+static cudaError_t icp_persistent_fits(int ctas, bool& fits)
+{
+    int per_sm = 0;
+    const cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, icp_persistent_kernel, kIcpThreads, kIcpDynSmem);
+    fits = e == cudaSuccess && per_sm * device_sm_count() >= ctas;
+    return e;
+}
+} // namespace se_gpu
 
 extern "C" {
 
@@ -992,28 +1207,30 @@ se_gpu_status se_gpu_tracker_create(const se_gpu_pinhole* sensor, const se_gpu_t
         t->li.pts[l] = t->pts[l];
         t->li.nrm[l] = t->nrm[l];
         t->li.depth[l] = t->pyr_depth[l];
-        const int tiles = (w * h + kTrackThreads - 1) / kTrackThreads; // one tile = 256 pixels
-        const int ctas = tiles < 300 ? tiles : 300;
-        t->nctas[l] = ctas < 2 * device_sm_count() ? (ctas > 0 ? ctas : 1) : 2 * device_sm_count();
-        if (t->nctas[l] > kMaxTrackCtas)
-            t->nctas[l] = kMaxTrackCtas;
+        // at least four pixels per thread where the level allows (the per-warp flush and the
+        // merge of the warps' partials are fixed costs), at most one CTA per SM
+        const long long want = ((long long) w * h + 3) / 4;
+        const int sms = device_sm_count() < kMaxTrackCtas ? device_sm_count() : kMaxTrackCtas;
+        const long long warps = (want + 31) / 32;
+        t->nctas[l] = (int) (warps < sms ? (warps > 0 ? warps : 1) : sms);
+        const long long per = (want + t->nctas[l] - 1) / t->nctas[l];
+        const long long thr = (per + 31) / 32 * 32;
+        t->nthrs[l] = (int) (thr < 32 ? 32 : (thr > kIcpThreads ? kIcpThreads : thr));
     }
     if ((e = cudaMalloc(&t->acc, kAccBuffers * kAccBufWords * sizeof(unsigned long long))) != cudaSuccess
         || (e = cudaMemset(t->acc, 0, kAccBuffers * kAccBufWords * sizeof(unsigned long long))) != cudaSuccess)
         return fail(e, "cudaMalloc(acc)");
-    if ((e = cudaMalloc(&t->sm_slots, kIcpSlotCounters * sizeof(unsigned))) != cudaSuccess
-        || (e = cudaMemset(t->sm_slots, 0, kIcpSlotCounters * sizeof(unsigned))) != cudaSuccess)
-        return fail(e, "cudaMalloc(sm_slots)");
+    if ((e = icp_kernel_attributes()) != cudaSuccess)
+        return fail(e, "cudaFuncSetAttribute(ICP shared memory)");
     {
         // the persistent kernel needs its whole grid resident at once
-        int per_sm = 0;
         t->persistent_ctas = 0;
         for (int l = 0; l < t->levels; ++l)
             t->persistent_ctas = t->nctas[l] > t->persistent_ctas ? t->nctas[l] : t->persistent_ctas;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, icp_persistent_kernel, kTrackThreads, 0))
-            != cudaSuccess)
+        bool fits = false;
+        if ((e = icp_persistent_fits(t->persistent_ctas, fits)) != cudaSuccess)
             return fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-        t->persistent = per_sm * device_sm_count() >= t->persistent_ctas ? 1 : 0;
+        t->persistent = fits ? 1 : 0;
     }
     if ((e = cudaMalloc(&t->state, sizeof(TrackState))) != cudaSuccess)
         return fail(e, "cudaMalloc(state)");
@@ -1033,7 +1250,6 @@ se_gpu_status se_gpu_tracker_destroy(se_gpu_tracker* t)
         cudaFree(t->nrm[l]);
     }
     cudaFree(t->acc);
-    cudaFree(t->sm_slots);
     cudaFree(t->state);
     delete t;
     return SE_GPU_OK;
@@ -1082,7 +1298,6 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
     IcpLevels L;
     std::memset(&L, 0, sizeof(L));
     L.levels = t->levels;
-    L.sm_slots = t->sm_slots;
     L.W = t->sensor.width;
     L.H = t->sensor.height;
     L.track_threshold = t->config.track_threshold;
@@ -1102,14 +1317,16 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
         ip.normal_threshold = t->config.normal_threshold;
         ip.icp_threshold = t->config.icp_threshold;
         L.nctas[level] = t->nctas[level];
+        ip.ncta = t->nctas[level];
+        ip.nthr = t->nthrs[level];
         L.iters[level] = t->config.iterations[level];
     }
     if (t->persistent) {
         ProfScope ps(kProfIcpIter, stream);
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(t->persistent_ctas);
-        cfg.blockDim = dim3(kTrackThreads);
-        cfg.dynamicSmemBytes = 0;
+        cfg.blockDim = dim3(kIcpThreads);
+        cfg.dynamicSmemBytes = kIcpDynSmem;
         cfg.stream = stream;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeCooperative;
@@ -1122,8 +1339,8 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
         for (int level = t->levels - 1; level >= 0; --level)
             for (int it = 0; it < t->config.iterations[level]; ++it) {
                 ProfScope ps(kProfIcpIter, stream);
-                icp_iter_kernel<<<t->nctas[level], kTrackThreads, 0, stream>>>(t->s, L.ip[level], t->state,
-                                                                               t->acc);
+                icp_iter_kernel<<<t->nctas[level], kIcpThreads, kIcpDynSmem, stream>>>(t->s, L.ip[level], t->state,
+                                                                                       t->acc);
             }
     }
     if (!t->persistent) { // the persistent kernel runs the check itself
@@ -1180,9 +1397,9 @@ se_gpu_status se_gpu_tracker_set_persistent(se_gpu_tracker* t, int enable)
         return SE_GPU_ERR_BAD_ARG;
     }
     if (enable) {
-        int per_sm = 0;
-        SE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, icp_persistent_kernel, kTrackThreads, 0));
-        if (per_sm * device_sm_count() < t->persistent_ctas) {
+        bool fits = false;
+        SE_CUDA_TRY(icp_persistent_fits(t->persistent_ctas, fits));
+        if (!fits) {
             set_last_error("se_gpu_tracker_set_persistent: %d CTAs do not fit on the device at once",
                            t->persistent_ctas);
             return SE_GPU_ERR_NOT_SUPPORTED;
@@ -1383,7 +1600,7 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_noalloc_kernel(Pinh
         st->last_red[threadIdx.x] = (float) v;
     }
     __syncthreads();
-    icp_tail(sh_val, sh_pose, sh_new, sh_newf, &sh_conv, ip.icp_threshold, 0);
+    icp_tail(sh_val, sh_pose, sh_new, sh_newf, &sh_conv, ip.icp_threshold);
     if (threadIdx.x < 12) {
         st->pose[threadIdx.x] = sh_new[threadIdx.x];
         st->pose_f[threadIdx.x] = sh_newf[threadIdx.x];
@@ -1481,6 +1698,8 @@ extern "C" se_gpu_status se_gpu_track_noalloc(const se_gpu_pinhole* sensor, cons
     ip.dist_threshold = config->dist_threshold;
     ip.normal_threshold = config->normal_threshold;
     ip.icp_threshold = config->icp_threshold;
+    ip.ncta = 0; // the allocation-free kernel partitions by its own grid
+    ip.nthr = 0;
     const long long tiles = (npix + kTrackThreads - 1) / kTrackThreads;
     int ctas = (int) (tiles < kNoAllocMaxCtas ? tiles : kNoAllocMaxCtas);
     if (ctas > 2 * device_sm_count())
