@@ -173,6 +173,11 @@ se_gpu_status se_gpu_map_create(const se_gpu_map_config* cfg, se_gpu_map** out)
         m.T_MW.t[2] = cfg->dim[2] / 2.0f;
     }
     m.T_WM = inverse_iso(m.T_MW);
+    m.inv_res = 1.0f / cfg->res;
+    m.T_MW_translation = 1;
+    for (int i = 0; i < 9; ++i)
+        if (m.T_MW.R[i] != ((i % 4 == 0) ? 1.0f : 0.0f))
+            m.T_MW_translation = 0;
     m.trunc = cfg->res * cfg->truncation_boundary_factor;
     m.max_weight = cfg->max_weight;
     m.storage = cfg->storage;
@@ -278,6 +283,7 @@ se_gpu_status se_gpu_map_create_occupancy(const se_gpu_map_config* cfg, const se
     map->occ = nullptr;
     map->dev.size = size;
     map->dev.res = cfg->res;
+    map->dev.inv_res = 1.0f / cfg->res;
     map->dev.dim = (float) size * cfg->res;
     map->dev.res_type = -1; // not a TSDF map
     const se_gpu_status st = occ_map_create(cfg, occ, size, &map->occ);

@@ -312,7 +312,7 @@ __device__ bool field_grad(const MapDevice& m, BlockCache& c, F3 p_W, F3& g)
                       + ((v[12] - v[10]) * rx + (v[24] - v[22]) * fac.x) * fac.y) * rz
         + (((v[9] - v[7]) * rx + (v[21] - v[19]) * fac.x) * ry
            + ((v[13] - v[11]) * rx + (v[25] - v[23]) * fac.x) * fac.y) * fac.z;
-    g = f3((0.5f * gx) / m.res, (0.5f * gy) / m.res, (0.5f * gz) / m.res);
+    g = f3(div_res(m, 0.5f * gx), div_res(m, 0.5f * gy), div_res(m, 0.5f * gz));
     return true;
 }
 
@@ -393,7 +393,7 @@ __device__ bool field_grad_batched(const MapDevice& m, BlockCache& c, F3 p_W, F3
                       + ((v[12] - v[10]) * rx + (v[24] - v[22]) * fac.x) * fac.y) * rz
         + (((v[9] - v[7]) * rx + (v[21] - v[19]) * fac.x) * ry
            + ((v[13] - v[11]) * rx + (v[25] - v[23]) * fac.x) * fac.y) * fac.z;
-    g = f3((0.5f * gx) / m.res, (0.5f * gy) / m.res, (0.5f * gz) / m.res);
+    g = f3(div_res(m, 0.5f * gx), div_res(m, 0.5f * gy), div_res(m, 0.5f * gz));
     return true;
 }
 
@@ -430,7 +430,7 @@ __device__ __forceinline__ bool mr_field_grad(const MapDevice& m, F3 p_W, F3& g)
     F3 gv;
     if (!mr_grad<S>(m, vf, gv))
         return false;
-    g = f3(gv.x / m.res, gv.y / m.res, gv.z / m.res);
+    g = f3(div_res(m, gv.x), div_res(m, gv.y), div_res(m, gv.z));
     return true;
 }
 

@@ -164,9 +164,11 @@ struct MapDevice {
     int bps;             // blocks per side = size / 8
     int log2_bps;
     float res;
+    float inv_res;       // RN(1 / res), for div_res
     float dim;           // size * res
     Tf T_MW;
     Tf T_WM;
+    int T_MW_translation; // T_MW's rotation is exactly the identity (the reference's default)
     float trunc;         // res * truncation_boundary_factor
     float max_weight;
     int storage;         // se_gpu_storage
@@ -291,23 +293,46 @@ __device__ __forceinline__ void store_voxel(const MapDevice& m, int blk, int vi,
     }
 }
 
+// x / res, correctly rounded, without a division: q = RN(x r) with r = RN(1 / res), the
+// residual x - q res is exact as one fused multiply-add, and RN(q + (x - q res) r) is RN(x / res)
+// (Markstein's theorem on the correction step of Newton-Raphson division: r within half an ulp
+// of 1 / res and q within one ulp of the quotient give the correctly rounded quotient, barring
+// underflow and overflow). Tiny and non-finite x take the IEEE division. The identity is checked
+// exhaustively for every float x in [2^-72, 2^14) and ten resolutions (tests/test_exact_division.py).
+__host__ __device__ __forceinline__ float div_res(const MapDevice& m, float x)
+{
+    if (!(fabsf(x) >= 0x1p-100f && fabsf(x) < 0x1p100f))
+        return x / m.res;
+    const float q = x * m.inv_res;
+    return fmaf(fmaf(-q, m.res, x), m.inv_res, q);
+}
+
+// T_MW p: with an identity rotation the three products by 1 and the six by 0 change nothing
+// but the sign of a zero, so p + t gives the same voxel coordinates.
+__host__ __device__ __forceinline__ F3 to_map(const MapDevice& m, F3 p_W)
+{
+    if (m.T_MW_translation)
+        return f3(p_W.x + m.T_MW.t[0], p_W.y + m.T_MW.t[1], p_W.z + m.T_MW.t[2]);
+    return apply(m.T_MW, p_W);
+}
+
 // Map::contains + pointToVoxel<Safe::On> (include/se/map/impl/map_impl.hpp:58-64,538-550).
 __host__ __device__ __forceinline__ bool point_to_voxel(const MapDevice& m, F3 p_W, int& vx, int& vy, int& vz)
 {
-    const F3 p = apply(m.T_MW, p_W);
+    const F3 p = to_map(m, p_W);
     if (!(p.x >= 0.0f && p.x < m.dim && p.y >= 0.0f && p.y < m.dim && p.z >= 0.0f && p.z < m.dim))
         return false;
-    vx = (int) (p.x / m.res);
-    vy = (int) (p.y / m.res);
-    vz = (int) (p.z / m.res);
+    vx = (int) div_res(m, p.x);
+    vy = (int) div_res(m, p.y);
+    vz = (int) div_res(m, p.z);
     return true;
 }
 __host__ __device__ __forceinline__ bool point_to_voxel_f(const MapDevice& m, F3 p_W, F3& v)
 {
-    const F3 p = apply(m.T_MW, p_W);
+    const F3 p = to_map(m, p_W);
     if (!(p.x >= 0.0f && p.x < m.dim && p.y >= 0.0f && p.y < m.dim && p.z >= 0.0f && p.z < m.dim))
         return false;
-    v = f3(p.x / m.res, p.y / m.res, p.z / m.res);
+    v = f3(div_res(m, p.x), div_res(m, p.y), div_res(m, p.z));
     return true;
 }
 
