@@ -198,10 +198,11 @@ SE_GPU_API se_gpu_status se_gpu_integrate_range(se_gpu_map* map, const float* ra
  * another call in flight. */
 typedef struct se_gpu_occ_batch se_gpu_occ_batch;
 /* flags: SE_GPU_OCC_BATCH_GRAPH (capture and replay, as above) and SE_GPU_OCC_BATCH_AUTOTUNE:
- * the first 8 calls run in turn 4 candidate launch geometries (CTAs per SM of the carver, list
- * and block stages), timed with events (these calls synchronise the stream), and the batch
- * keeps the fastest per stage; the graph is captured after tuning. Results do not depend on the
- * geometry. */
+ * the first 4 calls run the default geometry (the maps grow from empty), the next 12 run in turn
+ * 4 candidate launch geometries (CTAs per SM of the carver, list and block stages) three times,
+ * timed with events (these calls synchronise the stream), and the batch keeps per stage the
+ * candidate with the least time in its best round; the graph is captured after tuning. Results
+ * do not depend on the geometry. */
 #define SE_GPU_OCC_BATCH_GRAPH 1
 #define SE_GPU_OCC_BATCH_AUTOTUNE 2
 SE_GPU_API se_gpu_status se_gpu_occ_batch_create(se_gpu_map* const* maps, int n,

@@ -506,8 +506,9 @@ class OccupancyBatch:
     """Several occupancy maps integrated together, one frame each per call, every pipeline stage
     in one launch over all maps (no counterpart in the reference). graph=True captures the
     launches of a call into a CUDA graph on the first call and replays it afterwards;
-    autotune=True spends the first 8 calls timing 4 launch geometries and keeps the fastest per
-    stage (the graph is captured after that)."""
+    autotune=True runs the default geometry for the first 4 calls, then spends 12 calls timing
+    4 launch geometries three times each and keeps per stage the one with the least time in its
+    best round (the graph is captured after that)."""
 
     def __init__(self, maps, sensor, graph=True, autotune=False):
         self.maps = list(maps)

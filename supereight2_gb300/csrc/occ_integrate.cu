@@ -81,7 +81,7 @@ __device__ __forceinline__ int push(int* list, int* count, int cap, int v, int* 
 
 // -------------------------------------------------------------------------- begin --
 
-__global__ void occ_begin_kernel(const OccLaunch* __restrict__ Lp, const __grid_constant__ OccStep step)
+__device__ __forceinline__ void occ_begin(const OccLaunch* __restrict__ Lp, const OccStep& step)
 {
     const OccLaunch& L = *Lp;
     const int j = blockIdx.x;
@@ -99,6 +99,18 @@ __global__ void occ_begin_kernel(const OccLaunch* __restrict__ Lp, const __grid_
         d.timestamp = step.timestamp[j];
         *J.dyn = d;
     }
+}
+
+// The frame's poses, images and timestamps by value (single-map calls) or from a device buffer
+// that the call fills on the stream before the launches (batches: their captured graph then
+// replays unchanged).
+__global__ void occ_begin_kernel(const OccLaunch* __restrict__ Lp, const __grid_constant__ OccStep step)
+{
+    occ_begin(Lp, step);
+}
+__global__ void occ_begin_dev_kernel(const OccLaunch* __restrict__ Lp, const OccStep* __restrict__ step)
+{
+    occ_begin(Lp, *step);
 }
 
 // ------------------------------------------------------------------ per-pixel inputs --
@@ -1765,14 +1777,17 @@ struct OccStageTimer {
 // Every launch of one frame of every map in L (device copy at Ld); no host synchronisation, so
 // the sequence can be captured into a graph. The begin launch is the first. With a timer, an
 // event is recorded before each tunable launch (kind) and after it (kind -1).
-static se_gpu_status occ_enqueue(const OccLaunch& L, const OccLaunch* Ld, const OccStep& step, const OccTiles& t,
-                                 cudaStream_t stream, OccStageTimer* timer = nullptr)
+static se_gpu_status occ_enqueue(const OccLaunch& L, const OccLaunch* Ld, const OccStep& step, const OccStep* step_dev,
+                                 const OccTiles& t, cudaStream_t stream, OccStageTimer* timer = nullptr)
 {
     const int sms = device_sm_count();
     const int npx = L.sensor.w * L.sensor.h;
     const int n = L.n;
     const int carve = sms * t.ctas[kTileCarve], list = sms * t.ctas[kTileList], blocks = sms * t.ctas[kTileBlocks];
-    occ_begin_kernel<<<n, 64, 0, stream>>>(Ld, step);
+    if (step_dev)
+        occ_begin_dev_kernel<<<n, 64, 0, stream>>>(Ld, step_dev);
+    else
+        occ_begin_kernel<<<n, 64, 0, stream>>>(Ld, step);
     occ_pixels_kernel<<<dim3((npx + 255) / 256, n), 256, 0, stream>>>(Ld);
     for (int l = 1; l < L.sensor.levels; ++l)
         occ_pool_level_kernel<<<dim3((npx + 255) / 256, 2 * n), 256, 0, stream>>>(Ld, l);
@@ -1801,16 +1816,24 @@ static se_gpu_status occ_enqueue(const OccLaunch& L, const OccLaunch* Ld, const 
     return SE_GPU_OK;
 }
 
-// The autotuner of a batch: during its first kTuneFrames calls each call runs one candidate
-// geometry (candidate c: carve 2 << c, lists 1 << c, blocks 2 << c CTAs per SM) with events
-// around the tunable launches; afterwards each stage kind keeps the candidate with the least
-// accumulated time. Results do not depend on the geometry: every stage is a grid-stride loop
+// The autotuner of a batch: its first kSkip calls run the default geometry untimed (the maps
+// grow from empty, so the first frames' work is not representative), then each of the next
+// kCand * kRounds calls runs one candidate geometry (candidate c: carve 2 << c, lists 1 << c,
+// blocks 2 << c CTAs per SM) with events around the tunable launches; afterwards each stage kind
+// keeps the candidate with the least time in its best round (the minimum discards calls slowed
+// by anything else). Results do not depend on the geometry: every stage is a grid-stride loop
 // over the same work.
 struct OccTuner {
-    static constexpr int kCand = 4, kRounds = 2, kTuneFrames = kCand * kRounds;
+    static constexpr int kSkip = 4, kCand = 4, kRounds = 3, kTuneFrames = kSkip + kCand * kRounds;
     int frames = 0;
-    double ms[kTileKinds][kCand] = {};
+    double ms[kTileKinds][kCand];
     OccStageTimer timer;
+    OccTuner()
+    {
+        for (int k = 0; k < kTileKinds; ++k)
+            for (int c = 0; c < kCand; ++c)
+                ms[k][c] = 1e30;
+    }
     static OccTiles candidate(int c)
     {
         OccTiles t;
@@ -1851,7 +1874,7 @@ static se_gpu_status occ_integrate_one(se_gpu_occ_map* om, const float* image_de
     std::memset(&step, 0, sizeof(step));
     occ_fill_step(step, 0, T16, image_dev, timestamp);
     ProfScope ps(kProfUpdate, stream);
-    return occ_enqueue(L, om->scratch.launch_dev, step, OccTiles(), stream);
+    return occ_enqueue(L, om->scratch.launch_dev, step, nullptr, OccTiles(), stream);
 }
 
 se_gpu_status occ_integrate(se_gpu_occ_map* om, const float* depth_dev, const se_gpu_pinhole& sensor,
@@ -1881,8 +1904,13 @@ struct se_gpu_occ_batch {
     OccTuner* tuner = nullptr; // while autotuning
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaGraphNode_t begin_node = nullptr;
-    cudaKernelNodeParams begin_params;
+    // the per-call parameters: a device copy that the launches read, filled on the stream from a
+    // ring of pinned host copies (a slot is reused once its previous copy has completed)
+    static constexpr int kStepRing = 4;
+    OccStep* step_dev = nullptr;
+    OccStep* step_pinned = nullptr;
+    cudaEvent_t step_ev[kStepRing] = {};
+    int ring = 0;
     int device = 0;
 };
 
@@ -1961,6 +1989,12 @@ se_gpu_status se_gpu_occ_batch_create(se_gpu_map* const* maps, int n, const se_g
     cudaError_t e = cudaMalloc(&b->launch_dev, sizeof(OccLaunch));
     if (e == cudaSuccess)
         e = cudaMemcpy(b->launch_dev, &L, sizeof(OccLaunch), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&b->step_dev, sizeof(OccStep));
+    if (e == cudaSuccess)
+        e = cudaHostAlloc(&b->step_pinned, se_gpu_occ_batch::kStepRing * sizeof(OccStep), cudaHostAllocDefault);
+    for (int r = 0; r < se_gpu_occ_batch::kStepRing && e == cudaSuccess; ++r)
+        e = cudaEventCreateWithFlags(&b->step_ev[r], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         se_gpu_occ_batch_destroy(b);
         return cuda_status(e, "se_gpu_occ_batch_create");
@@ -1985,20 +2019,37 @@ se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* b, const float* const
         occ_fill_step(step, j, T_WS + 16 * j, images_dev[j], timestamps[j]);
         b->maps[j]->last_stream = s;
     }
+    // this call's parameters into the device copy, on the stream ahead of the launches
+    {
+        const int r = b->ring;
+        b->ring = (r + 1) % se_gpu_occ_batch::kStepRing;
+        SE_CUDA_TRY(cudaEventSynchronize(b->step_ev[r]));
+        b->step_pinned[r] = step;
+        SE_CUDA_TRY(cudaMemcpyAsync(b->step_dev, &b->step_pinned[r], sizeof(OccStep), cudaMemcpyHostToDevice, s));
+        SE_CUDA_TRY(cudaEventRecord(b->step_ev[r], s));
+    }
+    if (b->tuner && b->tuner->frames < OccTuner::kSkip) {
+        ++b->tuner->frames;
+        return occ_enqueue(*b->launch_host, b->launch_dev, step, b->step_dev, b->tiles, s);
+    }
     if (b->tuner) {
         OccTuner& tu = *b->tuner;
-        const int c = tu.frames % OccTuner::kCand;
+        const int c = (tu.frames - OccTuner::kSkip) % OccTuner::kCand;
         tu.timer.used = 0;
-        se_gpu_status st = occ_enqueue(*b->launch_host, b->launch_dev, step, OccTuner::candidate(c), s, &tu.timer);
+        se_gpu_status st =
+            occ_enqueue(*b->launch_host, b->launch_dev, step, b->step_dev, OccTuner::candidate(c), s, &tu.timer);
         if (st != SE_GPU_OK)
             return st;
         SE_CUDA_TRY(cudaEventSynchronize(tu.timer.ev[tu.timer.used - 1]));
+        double round_ms[kTileKinds] = {};
         for (int i = 0; i + 1 < tu.timer.used; ++i) {
             float ms = 0.0f;
             SE_CUDA_TRY(cudaEventElapsedTime(&ms, tu.timer.ev[i], tu.timer.ev[i + 1]));
             if (tu.timer.kind[i] >= 0)
-                tu.ms[tu.timer.kind[i]][c] += ms;
+                round_ms[tu.timer.kind[i]] += ms;
         }
+        for (int k = 0; k < kTileKinds; ++k)
+            tu.ms[k][c] = round_ms[k] < tu.ms[k][c] ? round_ms[k] : tu.ms[k][c];
         if (++tu.frames == OccTuner::kTuneFrames) {
             for (int k = 0; k < kTileKinds; ++k) {
                 int best = 0;
@@ -2013,14 +2064,15 @@ se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* b, const float* const
         return SE_GPU_OK;
     }
     if (!b->use_graph)
-        return occ_enqueue(*b->launch_host, b->launch_dev, step, b->tiles, s);
+        return occ_enqueue(*b->launch_host, b->launch_dev, step, b->step_dev, b->tiles, s);
     if (!b->exec) {
+        // captured once: the launches read this and every later call's parameters from step_dev
         cudaStream_t cs;
         SE_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
         se_gpu_status st = SE_GPU_OK;
         if (e == cudaSuccess)
-            st = occ_enqueue(*b->launch_host, b->launch_dev, step, b->tiles, cs);
+            st = occ_enqueue(*b->launch_host, b->launch_dev, step, b->step_dev, b->tiles, cs);
         cudaGraph_t graph = nullptr;
         const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
         cudaStreamDestroy(cs);
@@ -2030,23 +2082,9 @@ se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* b, const float* const
             return st != SE_GPU_OK ? st : cuda_status(e != cudaSuccess ? e : e2, "occupancy batch capture");
         }
         b->graph = graph;
-        size_t nroots = 0;
-        SE_CUDA_TRY(cudaGraphGetRootNodes(graph, nullptr, &nroots));
-        if (nroots != 1)
-            return bad(SE_GPU_ERR_CUDA, "occupancy batch graph: expected one root node");
-        SE_CUDA_TRY(cudaGraphGetRootNodes(graph, &b->begin_node, &nroots));
-        SE_CUDA_TRY(cudaGraphKernelNodeGetParams(b->begin_node, &b->begin_params));
         SE_CUDA_TRY(cudaGraphInstantiate(&b->exec, graph, 0));
-        SE_CUDA_TRY(cudaGraphLaunch(b->exec, s));
-        return SE_GPU_OK;
+        SE_CUDA_TRY(cudaGraphUpload(b->exec, s)); // the graph's resources set up before its first launch
     }
-    // the begin node takes this call's poses, images and timestamps by value
-    const OccLaunch* ld = b->launch_dev;
-    void* args[2] = {(void*) &ld, (void*) &step};
-    cudaKernelNodeParams p = b->begin_params;
-    p.kernelParams = args;
-    p.extra = nullptr;
-    SE_CUDA_TRY(cudaGraphExecKernelNodeSetParams(b->exec, b->begin_node, &p));
     SE_CUDA_TRY(cudaGraphLaunch(b->exec, s));
     return SE_GPU_OK;
 }
@@ -2072,6 +2110,11 @@ se_gpu_status se_gpu_occ_batch_destroy(se_gpu_occ_batch* b)
     if (b->graph)
         cudaGraphDestroy(b->graph);
     cudaFree(b->launch_dev);
+    cudaFree(b->step_dev);
+    cudaFreeHost(b->step_pinned);
+    for (int r = 0; r < se_gpu_occ_batch::kStepRing; ++r)
+        if (b->step_ev[r])
+            cudaEventDestroy(b->step_ev[r]);
     delete b->launch_host;
     delete b;
     return SE_GPU_OK;
