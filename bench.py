@@ -136,12 +136,16 @@ def make_data(n_frames, device):
 
 # ----------------------------------------------------------------------------- GPU arm --
 
+TUNE_FRAMES = 12  # the frame pipeline's autotuner runs (part of the untimed frames)
+
+
 def _variant(se, torch, dev, sensor, poses, depth_dev, first, steps, warmup, path, storage, max_blocks,
              flush, profile=False, clocks=None, res_type="single"):
-    """Run frame 0 untimed, `warmup` untimed frames, then time `steps` frames (CUDA events per
+    """Run frame 0 and frames 1..first-1 untimed, then time `steps` frames (CUDA events per
     step on the launching stream, L2 flushed between steps outside the timed pairs).
     path "plain": the blocking reference-style calls (track with host pose readback, integrate,
-    raycast); path "graph": the captured whole-frame pipeline with the pose on the device."""
+    raycast); path "graph": the captured whole-frame pipeline with the pose on the device, whose
+    first TUNE_FRAMES untimed frames are its autotuner's runs."""
     import ctypes as C
     W, H = sensor.width, sensor.height
     m = se.Map(MAP_DIM, MAP_RES, max_blocks=max_blocks, storage=storage, res_type=res_type)
@@ -171,15 +175,17 @@ def _variant(se, torch, dev, sensor, poses, depth_dev, first, steps, warmup, pat
         fp.set_pose(T0, 0)
         fp.depth.copy_(depth_dev[0])
         fp.run(track=False)
+        fp.autotune(TUNE_FRAMES)
 
         def step(i, depth):
             fp.depth.copy_(depth, non_blocking=True)
             fp.run(track=True)
 
-    for i in range(1, 1 + warmup):
+    for i in range(1, first):
         step(i, depth_dev[i])
     torch.cuda.synchronize()
     m.check()
+    tiles = fp.tiles()[0] if fp is not None else None
 
     L = se.library()
     n_prof = L.se_gpu_profiling_count()
@@ -217,7 +223,7 @@ def _variant(se, torch, dev, sensor, poses, depth_dev, first, steps, warmup, pat
     dev_ms = float(sum(a.elapsed_time(b) for a, b in ev))
     return {"dev_ms": dev_ms, "wall_s": wall, "stats": stats, "kernel_ms": kernel_ms,
             "kernel_launches": kernel_launches, "clocks": clk, "map": m, "fp": fp,
-            "tracker": tracker, "num_blocks": m.num_blocks()}
+            "tracker": tracker, "num_blocks": m.num_blocks(), "tiles": tiles}
 
 
 def run_ours(args, ws, rank, local):
@@ -226,7 +232,7 @@ def run_ours(args, ws, rank, local):
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    n_frames = 1 + args.warmup + 2 * args.steps + 1  # the last frame is held out (adjoint)
+    n_frames = 1 + TUNE_FRAMES + args.warmup + 2 * args.steps + 1  # the last frame is held out (adjoint)
     t0 = time.perf_counter()
     sensor_spec, scene, poses, frames = make_data(n_frames, dev)
     gen_s = time.perf_counter() - t0
@@ -234,7 +240,7 @@ def run_ours(args, ws, rank, local):
     W, H = sensor.width, sensor.height
     depth_dev = [torch.from_numpy(f).to(dev) for f in frames]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    first = 1 + args.warmup
+    first = 1 + TUNE_FRAMES + args.warmup
     K = args.steps
 
     # plain FP32 (blocking calls) with per-kernel events: the roofline and kernel breakdown
@@ -358,13 +364,15 @@ def run_ours(args, ws, rank, local):
                                "ICP 3 levels {10,5,4}, integrate + raycast per frame",
                    "map_res_m": MAP_RES, "map_voxels": 1024, "storage": "f32",
                    "path": "captured CUDA graph per frame, pose on the device",
-                   "parallelism": f"replicas x{ws}", "l2": "flushed (256 MiB write) between steps"},
+                   "parallelism": f"replicas x{ws}", "l2": "flushed (256 MiB write) between steps",
+                   "untimed_frames": f"frame 0, {TUNE_FRAMES} autotuner runs of the graph variants, "
+                                     f"{args.warmup} warm-up frames"},
         "variants": {
             "plain_f32": {"value": ws * K / (plain_ms * 1e-3), "ms_per_step": plain_ms / K,
                           "api": "blocking se:: calls: track (host pose), integrateDepth, raycast_volume"},
-            "graph_f32": {"value": value, "ms_per_step": g32_ms / K},
-            "graph_f16": {"value": ws * K / (g16_ms * 1e-3), "ms_per_step": g16_ms / K,
-                          "storage": "half tsdf + uint16 weight, FP32 arithmetic"},
+            "graph_f32": {"value": value, "ms_per_step": g32_ms / K, "tiles": g32["tiles"]},
+            "graph_f16": {"value": ws * K / (g16_ms * 1e-3), "ms_per_step": g16_ms / K, "tiles": g16["tiles"],
+                          "storage": "FP16 tsdf with 8 guard bits + 8-bit weight (4 B per voxel), FP32 arithmetic"},
             "graph_vs_plain": plain_ms / g32_ms, "graph_f16_vs_plain": plain_ms / g16_ms},
         "roofline": roofline,
         "e2e": {"value": ws * K / e2e_max, "unit": "frames/s", "h2d_bytes_per_step": W * H * 4,
@@ -390,7 +398,7 @@ def run_ours(args, ws, rank, local):
         "clocks": g32["clocks"],
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(frames, poses, sensor_spec, args.warmup, 2 * K, args.cpu_budget_s)
+        out["cpu_baseline"] = cpu_baseline(frames, poses, sensor_spec, first - 1, 2 * K, args.cpu_budget_s)
         touched = out["cpu_baseline"].pop("raycast_voxels_touched", None)
         rc_ms = kms.get("raycast", 0.0) / max(kl.get("raycast", 1), 1)
         if touched and rc_ms:

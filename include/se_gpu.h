@@ -480,6 +480,18 @@ SE_GPU_API se_gpu_status se_gpu_frame_set_pose(se_gpu_frame* frame, const float 
 /* Launch one frame on stream: [track (if track != 0)] + integrate + raycast. Asynchronous;
  * the first call per mode captures the graph (call it before any capture of your own). */
 SE_GPU_API se_gpu_status se_gpu_frame_run(se_gpu_frame* frame, int track, void* stream);
+/* The frame path's autotuner (no counterpart in the reference): the next `runs` runs of the
+ * frame (runs >= 6; 0 stops tuning) are launched directly on the stream instead of from the
+ * graph, each with one candidate launch geometry of the voxel update (4, 8 or 16 CTAs per SM; 4
+ * or 2 voxels per lane per round) and of the raycast (8 x 4 or 16 x 2 pixels per warp), timed
+ * with events (these runs synchronise the stream); afterwards the map keeps per kernel the
+ * candidate with the least time seen and the graphs are captured again with it. Results do not
+ * depend on the geometry. Run it on a grown map. */
+SE_GPU_API se_gpu_status se_gpu_frame_autotune(se_gpu_frame* frame, int runs);
+/* The geometry in use: tiles[0] update CTAs per SM, tiles[1] voxels per lane per round,
+ * tiles[2] raycast warp tile (0: 8 x 4, 1: 16 x 2); tuning_left (may be NULL) the tuning runs
+ * still to come. */
+SE_GPU_API se_gpu_status se_gpu_frame_tiles(const se_gpu_frame* frame, int tiles[3], int* tuning_left);
 /* se_gpu_frame_run with the frame's depth image taken from host memory (width*height floats,
  * copied into the frame's input buffer on stream first; pinned memory keeps the copy
  * asynchronous), as integrateDepth / track take a host Image<float>. */

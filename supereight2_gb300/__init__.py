@@ -138,6 +138,8 @@ SIGNATURES = {
     "se_gpu_tracker_destroy": (C.c_int, [_VP]),
     "se_gpu_track": (C.c_int, [_VP, _VP, _VP, _VP, _F16, C.POINTER(C.c_int), _VP]),
     "se_gpu_tracker_last_reduction": (C.c_int, [_VP, _F16, C.POINTER(C.c_int)]),
+    "se_gpu_frame_autotune": (C.c_int, [_VP, C.c_int]),
+    "se_gpu_frame_tiles": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "se_gpu_tracker_level_images": (C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP]),
     "se_gpu_track_noalloc": (C.c_int, [C.POINTER(_Pinhole), C.POINTER(_TrackerConfig), _VP, _VP,
                                        _VP, _F16, C.POINTER(C.c_int), _F16, _VP]),
@@ -863,6 +865,20 @@ class FramePipeline:
         _check(self._L.se_gpu_frame_get_pose(self.h, T.ctypes.data_as(_F16), C.byref(acc),
                                              _stream(stream)), "se_gpu_frame_get_pose")
         return T.reshape(4, 4), bool(acc.value)
+
+    def autotune(self, runs=12):
+        """Time the next ``runs`` runs with candidate launch geometries of the voxel update and
+        the raycast (each run synchronises) and keep the fastest; results are unchanged."""
+        _check(self._L.se_gpu_frame_autotune(self.h, int(runs)), "se_gpu_frame_autotune")
+
+    def tiles(self):
+        """({"update_ctas_per_sm", "update_voxels_per_lane_round", "raycast_warp_tile"},
+        tuning runs left)."""
+        t = (C.c_int * 3)()
+        left = C.c_int()
+        _check(self._L.se_gpu_frame_tiles(self.h, t, C.byref(left)), "se_gpu_frame_tiles")
+        return ({"update_ctas_per_sm": t[0], "update_voxels_per_lane_round": t[1],
+                 "raycast_warp_tile": "8x4" if t[2] == 0 else "16x2"}, left.value)
 
     def pose_async(self, pose12, accepted, stream=None):
         """Enqueue the pose read into pinned host tensors: ``pose12`` (12 float32, the row-major

@@ -17,6 +17,19 @@ namespace se_gpu {
 int tracker_accepted_offset();
 void* tracker_state(se_gpu_tracker* t);
 
+// The autotuner's candidates: update grid 4, 8 or 16 CTAs per SM with 4 or 2 voxels per lane
+// per round (update candidate u), raycast warp tile 8 x 4 or 16 x 2 (raycast candidate r).
+constexpr int kUpdateCandidates = 6, kRaycastCandidates = 2;
+static FrameTiles tune_candidate(int u, int r)
+{
+    static const int ctas[3] = {4, 8, 16};
+    FrameTiles t;
+    t.update_ctas_per_sm = ctas[u % 3];
+    t.update_round = u < 3 ? 4 : 2;
+    t.raycast_tile = r;
+    return t;
+}
+
 // The acceptance of a run that did not track: copied on the stream like a tracked run's flag,
 // so that it lands in stream order after any earlier read into the same host buffer.
 static __device__ int g_accepted_untracked = 1; // never written
@@ -39,7 +52,31 @@ struct se_gpu_frame {
     cudaStream_t capture_stream;
     cudaGraphExec_t exec[2]; // [0] integrate + raycast, [1] track + integrate + raycast
     int last_tracked;        // whether the last run tracked (acceptance is 1 otherwise)
+    // autotuner: the runs left to time, the events, and per candidate the least time seen
+    int tune_left, tune_done;
+    FrameTuneEvents* tune_ev;
+    float update_ms[kUpdateCandidates];
+    float raycast_ms[kRaycastCandidates];
 };
+
+// One frame's launches on stream (captured into the graph, or run directly while tuning).
+static se_gpu_status enqueue_frame(se_gpu_frame* f, int with_track, cudaStream_t stream)
+{
+    se_gpu_status st = SE_GPU_OK;
+    const float* track_in = f->depth;
+    if (with_track && f->bilateral) {
+        st = enqueue_bilateral(f->depth, f->depth_filtered, f->sensor.width, f->sensor.height, f->bilateral_config,
+                               stream);
+        track_in = f->depth_filtered;
+    }
+    if (with_track && st == SE_GPU_OK)
+        st = enqueue_track(f->tracker, track_in, f->pts, f->nrm, nullptr, f->pose12, stream);
+    if (st == SE_GPU_OK)
+        st = enqueue_integrate(f->map, f->depth, f->sensor, nullptr, f->pose12, 0, stream);
+    if (st == SE_GPU_OK)
+        st = enqueue_raycast(f->map, f->sensor, nullptr, f->pose12, f->pts, f->nrm, f->scale, stream);
+    return st;
+}
 
 static se_gpu_status capture(se_gpu_frame* f, int with_track)
 {
@@ -48,18 +85,7 @@ static se_gpu_status capture(se_gpu_frame* f, int with_track)
     cudaError_t e = cudaStreamBeginCapture(f->capture_stream, cudaStreamCaptureModeThreadLocal);
     se_gpu_status st = SE_GPU_OK;
     if (e == cudaSuccess) {
-        const float* track_in = f->depth;
-        if (with_track && f->bilateral) {
-            st = enqueue_bilateral(f->depth, f->depth_filtered, f->sensor.width, f->sensor.height,
-                                   f->bilateral_config, f->capture_stream);
-            track_in = f->depth_filtered;
-        }
-        if (with_track && st == SE_GPU_OK)
-            st = enqueue_track(f->tracker, track_in, f->pts, f->nrm, nullptr, f->pose12, f->capture_stream);
-        if (st == SE_GPU_OK)
-            st = enqueue_integrate(f->map, f->depth, f->sensor, nullptr, f->pose12, 0, f->capture_stream);
-        if (st == SE_GPU_OK)
-            st = enqueue_raycast(f->map, f->sensor, nullptr, f->pose12, f->pts, f->nrm, f->scale, f->capture_stream);
+        st = enqueue_frame(f, with_track, f->capture_stream);
         const cudaError_t e2 = cudaStreamEndCapture(f->capture_stream, &graph);
         if (e2 != cudaSuccess && st == SE_GPU_OK)
             st = cuda_status(e2, "cudaStreamEndCapture");
@@ -128,6 +154,12 @@ se_gpu_status se_gpu_frame_destroy(se_gpu_frame* f)
             cudaGraphExecDestroy(f->exec[i]);
     if (f->capture_stream)
         cudaStreamDestroy(f->capture_stream);
+    if (f->tune_ev) {
+        for (int i = 0; i < 4; ++i)
+            if (f->tune_ev->ev[i])
+                cudaEventDestroy(f->tune_ev->ev[i]);
+        delete f->tune_ev;
+    }
     cudaFree(f->pose12);
     cudaFree(f->depth);
     cudaFree(f->depth_filtered);
@@ -199,16 +231,85 @@ se_gpu_status se_gpu_frame_run(se_gpu_frame* f, int track, void* stream_p)
         return SE_GPU_ERR_BAD_ARG;
     }
     const int mode = track ? 1 : 0;
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    if (f->tune_left > 0) {
+        // a tuning run: the launches directly on the stream with the next candidate geometry,
+        // the update and raycast timed with events (the run synchronises the stream)
+        const int k = f->tune_done++;
+        const int u = k % kUpdateCandidates, r = k % kRaycastCandidates;
+        f->map->tiles = tune_candidate(u, r);
+        f->map->tune = f->tune_ev;
+        f->map->last_stream = stream;
+        f->last_tracked = mode;
+        const se_gpu_status st = enqueue_frame(f, mode, stream);
+        f->map->tune = nullptr;
+        if (st != SE_GPU_OK)
+            return st;
+        SE_CUDA_TRY(cudaEventSynchronize(f->tune_ev->ev[3]));
+        float up = 0.0f, rc = 0.0f;
+        SE_CUDA_TRY(cudaEventElapsedTime(&up, f->tune_ev->ev[0], f->tune_ev->ev[1]));
+        SE_CUDA_TRY(cudaEventElapsedTime(&rc, f->tune_ev->ev[2], f->tune_ev->ev[3]));
+        f->update_ms[u] = up < f->update_ms[u] ? up : f->update_ms[u];
+        f->raycast_ms[r] = rc < f->raycast_ms[r] ? rc : f->raycast_ms[r];
+        if (--f->tune_left == 0) {
+            int bu = 0, br = 0;
+            for (int c = 1; c < kUpdateCandidates; ++c)
+                bu = f->update_ms[c] < f->update_ms[bu] ? c : bu;
+            for (int c = 1; c < kRaycastCandidates; ++c)
+                br = f->raycast_ms[c] < f->raycast_ms[br] ? c : br;
+            f->map->tiles = tune_candidate(bu, br);
+            // the graphs are captured again with the chosen geometry
+            for (int i = 0; i < 2; ++i)
+                if (f->exec[i]) {
+                    SE_CUDA_TRY(cudaGraphExecDestroy(f->exec[i]));
+                    f->exec[i] = nullptr;
+                }
+        }
+        return SE_GPU_OK;
+    }
     if (!f->exec[mode]) {
         const se_gpu_status st = capture(f, mode);
         if (st != SE_GPU_OK)
             return st;
     }
-    cudaStream_t stream = (cudaStream_t) stream_p;
     f->map->last_stream = stream;
     f->last_tracked = mode;
     ProfScope ps(kProfFrameGraph, stream);
     SE_CUDA_TRY(cudaGraphLaunch(f->exec[mode], stream));
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_frame_autotune(se_gpu_frame* f, int runs)
+{
+    if (!f || runs < 0 || runs > 1000 || (runs > 0 && runs < kUpdateCandidates)) {
+        set_last_error("se_gpu_frame_autotune: invalid argument (0 or %d..1000 runs)", kUpdateCandidates);
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    if (runs > 0 && !f->tune_ev) {
+        f->tune_ev = new FrameTuneEvents();
+        for (int i = 0; i < 4; ++i)
+            SE_CUDA_TRY(cudaEventCreate(&f->tune_ev->ev[i]));
+    }
+    for (int c = 0; c < kUpdateCandidates; ++c)
+        f->update_ms[c] = 1e30f;
+    for (int c = 0; c < kRaycastCandidates; ++c)
+        f->raycast_ms[c] = 1e30f;
+    f->tune_left = runs;
+    f->tune_done = 0;
+    return SE_GPU_OK;
+}
+
+se_gpu_status se_gpu_frame_tiles(const se_gpu_frame* f, int tiles[3], int* tuning_left)
+{
+    if (!f || !tiles) {
+        set_last_error("se_gpu_frame_tiles: invalid argument");
+        return SE_GPU_ERR_BAD_ARG;
+    }
+    tiles[0] = f->map->tiles.update_ctas_per_sm;
+    tiles[1] = f->map->tiles.update_round;
+    tiles[2] = f->map->tiles.raycast_tile;
+    if (tuning_left)
+        *tuning_left = f->tune_left;
     return SE_GPU_OK;
 }
 

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) frustum_kernel(MapDevice m, Pinhole s, co
 // new blocks are written in full (the update doubles as their initialisation). Capped at 64
 // registers (4 CTAs per SM): the extra warps hide more of the depth and voxel load latency than
 // the cap costs.
-template <int S>
+template <int S, int KU>
 __global__ void __launch_bounds__(256, 4) update_kernel(MapDevice m, Pinhole s, const float* __restrict__ depth,
                                                      const IntegrateParams* __restrict__ P)
 {
@@ -183,10 +183,10 @@ __global__ void __launch_bounds__(256, 4) update_kernel(MapDevice m, Pinhole s, 
         const int c0 = m.block_coord[3 * blk], c1 = m.block_coord[3 * blk + 1], c2 = m.block_coord[3 * blk + 2];
         if (lane == 0)
             m.block_ts[blk] = timestamp;
-        // four voxels per lane per round: their projections, then their four depth loads in
-        // flight together, then the voxel loads of those that update, then the updates (the
-        // per-voxel arithmetic is that of one voxel at a time)
-        constexpr int kU = 4;
+        // KU voxels per lane per round: their projections, then their depth loads in flight
+        // together, then the voxel loads of those that update, then the updates (the per-voxel
+        // arithmetic is that of one voxel at a time)
+        constexpr int kU = KU;
         for (int k0 = 0; k0 < kBlockVoxels / 32; k0 += kU) {
             int pix[kU];
             float mz[kU], pn[kU];
@@ -289,14 +289,28 @@ se_gpu_status enqueue_integrate(se_gpu_map* map, const float* depth_dev, const s
         launch_chained(frustum_kernel, sms * 4, 256, stream, m, s, map->iparams);
     }
     if (m.res_type == SE_GPU_RES_MULTI) {
+        if (map->tune)
+            SE_CUDA_TRY(cudaEventRecord(map->tune->ev[0], stream));
         enqueue_update_multires(m, s, depth_dev, map->iparams, stream);
+        if (map->tune)
+            SE_CUDA_TRY(cudaEventRecord(map->tune->ev[1], stream));
     }
     else {
         ProfScope ps(kProfUpdate, stream);
-        if (m.storage == SE_GPU_STORAGE_F32)
-            launch_chained(update_kernel<SE_GPU_STORAGE_F32>, sms * 8, 256, stream, m, s, depth_dev, map->iparams);
+        const int grid = sms * map->tiles.update_ctas_per_sm;
+        const bool r2 = map->tiles.update_round == 2;
+        if (map->tune)
+            SE_CUDA_TRY(cudaEventRecord(map->tune->ev[0], stream));
+        if (m.storage == SE_GPU_STORAGE_F32 && r2)
+            launch_chained(update_kernel<SE_GPU_STORAGE_F32, 2>, grid, 256, stream, m, s, depth_dev, map->iparams);
+        else if (m.storage == SE_GPU_STORAGE_F32)
+            launch_chained(update_kernel<SE_GPU_STORAGE_F32, 4>, grid, 256, stream, m, s, depth_dev, map->iparams);
+        else if (r2)
+            launch_chained(update_kernel<SE_GPU_STORAGE_F16, 2>, grid, 256, stream, m, s, depth_dev, map->iparams);
         else
-            launch_chained(update_kernel<SE_GPU_STORAGE_F16>, sms * 8, 256, stream, m, s, depth_dev, map->iparams);
+            launch_chained(update_kernel<SE_GPU_STORAGE_F16, 4>, grid, 256, stream, m, s, depth_dev, map->iparams);
+        if (map->tune)
+            SE_CUDA_TRY(cudaEventRecord(map->tune->ev[1], stream));
     }
     SE_CUDA_TRY(cudaGetLastError());
     return SE_GPU_OK;

@@ -32,7 +32,8 @@ __global__ void raycast_prep_kernel(const float* pose12, RaycastParams host_p, R
     *out = p;
 }
 
-template <int S, bool MR>
+// TILE 0: each warp takes 8 x 4 pixels (a CTA 16 x 8); TILE 1: 16 x 2 (a CTA 32 x 4).
+template <int S, bool MR, int TILE>
 __global__ void __launch_bounds__(128, 9) raycast_kernel(MapDevice m, Pinhole s, const RaycastParams* __restrict__ P,
                                                       float* __restrict__ pts, float* __restrict__ nrm,
                                                       int8_t* __restrict__ scale)
@@ -44,8 +45,9 @@ __global__ void __launch_bounds__(128, 9) raycast_kernel(MapDevice m, Pinhole s,
     __shared__ int sh_bt[8 * 128];
     const RaycastParams rp = *P;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
-    const int y = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+    constexpr int kWx = TILE == 0 ? 8 : 16, kWy = 32 / kWx; // warp tile
+    const int x = blockIdx.x * (2 * kWx) + (warp & 1) * kWx + (lane % kWx);
+    const int y = blockIdx.y * (2 * kWy) + (warp >> 1) * kWy + (lane / kWx);
     if (x >= s.w || y >= s.h)
         return;
     const size_t idx = (size_t) x + (size_t) y * s.w;
@@ -135,17 +137,32 @@ se_gpu_status enqueue_raycast(const se_gpu_map* map, const se_gpu_pinhole& senso
     rp.eps = std::exp2((float) (-std::log2((double) m.size)));
     rp.min_scale = 23 - m.log2_bps;
     launch_chained(raycast_prep_kernel, 1, 1, stream, T_WS_host16 ? nullptr : pose12_dev, rp, map->rparams);
-    dim3 grid((s.w + 15) / 16, (s.h + 7) / 8);
+    const int tile = map->tiles.raycast_tile;
+    const dim3 grid = tile == 0 ? dim3((s.w + 15) / 16, (s.h + 7) / 8) : dim3((s.w + 31) / 32, (s.h + 3) / 4);
     ProfScope ps(kProfRaycast, stream);
     const bool mr = m.res_type == SE_GPU_RES_MULTI;
+    if (map->tune)
+        SE_CUDA_TRY(cudaEventRecord(map->tune->ev[2], stream));
+#define SE_RAYCAST_LAUNCH(S_, MR_)                                                                                  \
+    do {                                                                                                            \
+        if (tile == 0)                                                                                              \
+            launch_chained(raycast_kernel<S_, MR_, 0>, grid, 128, stream, m, s, map->rparams, pts_dev, nrm_dev,     \
+                           scale_dev);                                                                              \
+        else                                                                                                        \
+            launch_chained(raycast_kernel<S_, MR_, 1>, grid, 128, stream, m, s, map->rparams, pts_dev, nrm_dev,     \
+                           scale_dev);                                                                              \
+    } while (0)
     if (m.storage == SE_GPU_STORAGE_F32 && !mr)
-        launch_chained(raycast_kernel<SE_GPU_STORAGE_F32, false>, grid, 128, stream, m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+        SE_RAYCAST_LAUNCH(SE_GPU_STORAGE_F32, false);
     else if (!mr)
-        launch_chained(raycast_kernel<SE_GPU_STORAGE_F16, false>, grid, 128, stream, m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+        SE_RAYCAST_LAUNCH(SE_GPU_STORAGE_F16, false);
     else if (m.storage == SE_GPU_STORAGE_F32)
-        launch_chained(raycast_kernel<SE_GPU_STORAGE_F32, true>, grid, 128, stream, m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+        SE_RAYCAST_LAUNCH(SE_GPU_STORAGE_F32, true);
     else
-        launch_chained(raycast_kernel<SE_GPU_STORAGE_F16, true>, grid, 128, stream, m, s, map->rparams, pts_dev, nrm_dev, scale_dev);
+        SE_RAYCAST_LAUNCH(SE_GPU_STORAGE_F16, true);
+#undef SE_RAYCAST_LAUNCH
+    if (map->tune)
+        SE_CUDA_TRY(cudaEventRecord(map->tune->ev[3], stream));
     SE_CUDA_TRY(cudaGetLastError());
     return SE_GPU_OK;
 }

@@ -469,6 +469,20 @@ __host__ __device__ inline Tf tf_from12(const float* m)
 
 struct se_gpu_occ_map;
 
+namespace se_gpu {
+// Launch geometry of the frame path's two largest kernels, chosen by the frame pipeline's
+// autotuner (se_gpu_frame_autotune); results do not depend on it.
+struct FrameTiles {
+    int update_ctas_per_sm = 8; // update_kernel grid: SMs x this (a grid-stride loop over the listed blocks)
+    int update_round = 4;       // voxels a lane projects together per round (2 or 4)
+    int raycast_tile = 0;       // raycast warp tile: 0 = 8 x 4 pixels, 1 = 16 x 2
+};
+// Events around the update and raycast launches while the autotuner times a frame.
+struct FrameTuneEvents {
+    cudaEvent_t ev[4];          // update start / end, raycast start / end
+};
+} // namespace se_gpu
+
 struct se_gpu_map {
     se_gpu::MapDevice dev;
     se_gpu_occ_map* occ;              // occupancy maps only (dev holds the geometry)
@@ -478,6 +492,8 @@ struct se_gpu_map {
     se_gpu::IntegrateParams* iparams; // device copy of the current integrate's parameters
     se_gpu::RaycastParams* rparams;   // device copy of the current raycast's parameters
     int* timestamp_dev;               // device frame counter used by captured pipelines
+    se_gpu::FrameTiles tiles;         // launch geometry of the update and raycast kernels
+    se_gpu::FrameTuneEvents* tune;    // non-null while the frame autotuner times a run
 };
 
 namespace se_gpu {

@@ -29,12 +29,14 @@ def _run_plain(gpu, sensor, poses, frames, storage):
     return m, out, pts.cpu().numpy(), nrm.cpu().numpy()
 
 
-def _run_graph(gpu, sensor, poses, frames, storage, from_host=False, pose_async=False):
+def _run_graph(gpu, sensor, poses, frames, storage, from_host=False, pose_async=False, autotune=0):
     import torch
     m = gpu.Map(10.24, 0.02, max_blocks=1 << 16, storage=storage)
     tr = gpu.Tracker(m, sensor)
     fp = gpu.FramePipeline(m, sensor, tr)
     fp.set_pose(poses[0].astype(np.float32), 0)
+    if autotune:
+        fp.autotune(autotune)
     out = []
     host = [torch.from_numpy(d).pin_memory() for d in frames] if from_host else None
     # one set of pinned buffers per frame: every read stays pending until the end
@@ -56,6 +58,9 @@ def _run_graph(gpu, sensor, poses, frames, storage, from_host=False, pose_async=
             T = np.eye(4, dtype=np.float32)
             T[:3] = p12.numpy().reshape(3, 4)
             out.append((T, bool(acc[0])))
+    if autotune:
+        tiles, left = fp.tiles()
+        assert left == max(0, autotune - len(frames))
     return m, out, fp.points_W.cpu().numpy(), fp.normals_W.cpu().numpy()
 
 
@@ -161,3 +166,26 @@ def test_f16_storage_within_tolerance_at_full_weight(gpu):
     err = np.abs(t32[a] - t16[b])[valid]
     assert err.max() <= 1e-3, float(err.max())        # 1e-3 truncation units
     assert err.max() <= 100 * 2.0 ** -19 + 2e-5       # the layout's derived bound
+
+
+def test_autotuned_pipeline_bit_identical(gpu, data):
+    """The autotuner's runs (every candidate launch geometry of the voxel update and of the
+    raycast, launched directly on the stream) and the graph captured afterwards with the chosen
+    geometry give the untuned graph's maps, poses and raycasts bit for bit."""
+    spec, scene, poses, frames = data
+    sensor = gpu.PinholeCamera.from_spec(spec)
+    m1, o1, p1, n1 = _run_graph(gpu, sensor, poses, frames, "f32")
+    # six tuning runs (one per update candidate) then graph replays with the chosen geometry
+    frames2 = list(frames) + list(frames[::-1])
+    poses2 = list(poses) + list(poses[::-1])
+    m1b, o1b, p1b, n1b = _run_graph(gpu, sensor, poses2, frames2, "f32")
+    m2, o2, p2, n2 = _run_graph(gpu, sensor, poses2, frames2, "f32", autotune=6)
+    for (T1, a1), (T2, a2) in zip(o1b, o2):
+        assert a1 == a2
+        assert np.array_equal(T1[:3], T2[:3])
+    k1, c1, t1, w1, _ = m1b.download_blocks()
+    k2, c2, t2, w2, _ = m2.download_blocks()
+    a, b = np.argsort(k1), np.argsort(k2)
+    assert np.array_equal(k1[a], k2[b])
+    assert np.array_equal(t1[a], t2[b]) and np.array_equal(w1[a], w2[b])
+    assert np.array_equal(p1b, p2) and np.array_equal(n1b, n2)
