@@ -235,11 +235,10 @@ SE_GPU_API se_gpu_status se_gpu_raycast(const se_gpu_map* map, const se_gpu_pinh
  * (include/se/map/algorithms/impl/marching_cube_impl.hpp:830-890, 1175-1201): the faces of the
  * surface between observed inside (tsdf < 0) and observed outside voxels, 9 floats each (three
  * vertices in voxel units of the map frame, the reference's Face::vertexes; world = T_WM *
- * (res * v)). Vertices follow meshing::compute_intersection exactly; the triangulation of each
- * crossing pattern comes from a case table this library builds from a stated rule (see
- * se_gpu_mc_case_table) instead of the reference's third-party table, so a pattern's triangles
- * can differ from the reference's while the surface and its vertices do not. Faces point away
- * from the inside. Writes up to capacity faces (any order) to faces_dev and the total to
+ * (res * v)). Vertices follow meshing::compute_intersection exactly and each crossing pattern
+ * is triangulated by the reference's case table (edge_tables.hpp, triTable; see
+ * se_gpu_mc_case_table), so the faces are the reference's face for face. Faces point away from
+ * the inside. Writes up to capacity faces (any order) to faces_dev and the total to
  * *count (call again with a larger buffer when *count > capacity). Synchronous. Multi-res TSDF
  * and occupancy maps: se_gpu_dual_marching_cube with min_desired_scale 0, without the scales. */
 SE_GPU_API se_gpu_status se_gpu_marching_cube(se_gpu_map* map, float* faces_dev, int64_t capacity,
@@ -257,10 +256,8 @@ SE_GPU_API se_gpu_status se_gpu_dual_marching_cube(se_gpu_map* map, int min_desi
                                                    int64_t capacity, int64_t* count, void* stream);
 /* The case table: ntri[c] faces for case c (bit i = corner i inside, corners (0,0,0), (1,0,0),
  * (1,0,1), (0,0,1), (0,1,0), (1,1,0), (1,1,1), (0,1,1)), tri[15 c + 3 f + j] the edge (as
- * meshing::edge_to_corners) of vertex j of face f, -1 padded. Host only. Rule: crossed edges of a
- * cube face are joined into segments, a face with four crossed edges cutting off its inside
- * corners; the segments close into loops, walked from the lowest edge towards its lower
- * neighbour, reversed when the Newell normal points inwards, fanned from the first edge. */
+ * meshing::edge_to_corners) of vertex j of face f, -1 padded: the reference's triTable
+ * (include/se/map/algorithms/edge_tables.hpp) row for row. Host only. */
 SE_GPU_API se_gpu_status se_gpu_mc_case_table(int32_t ntri[256], int32_t tri[256 * 15]);
 
 /* ------------------------------------------------------------------------------- IO -- */

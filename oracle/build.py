@@ -17,7 +17,8 @@ LIB_PATH = os.path.join(BUILD_DIR, "libse_oracle.so")
 LIB64_PATH = os.path.join(BUILD_DIR, "libse_oracle_f64.so")
 SOURCES = [os.path.join(HERE, f) for f in ("se_oracle.cpp", "se_oracle_occ.cpp")]
 SOURCES64 = [os.path.join(HERE, "se_oracle_f64.cpp")]
-HEADERS = [os.path.join(HERE, f) for f in ("se_oracle.h", "oracle_common.hpp", "se_oracle.cpp")]
+HEADERS = [os.path.join(HERE, f) for f in ("se_oracle.h", "oracle_common.hpp", "se_oracle.cpp")] + [
+    os.path.join(os.path.dirname(HERE), "supereight2_gb300", "csrc", "mc_case_table.inc")]
 FLAGS = ["-std=c++17", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-Wall",
          "-Wno-unknown-pragmas", "-Wno-unused-function", "-Wno-subobject-linkage"]
 

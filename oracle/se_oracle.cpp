@@ -1794,26 +1794,20 @@ void so_map_blocks(const so_map* map, uint64_t* keys, int32_t* coords, float* ts
 }
 
 /* ------------------------------------------------------------------ marching cubes -- */
-/* The reference triangulates with a third-party case table (edge_tables.hpp); this oracle builds
- * its case table from a stated rule instead (the GPU library builds the same table from the
- * same rule, independently):
- *  - corners in the order of meshing::gather_data: c0 (0,0,0), c1 (1,0,0), c2 (1,0,1),
- *    c3 (0,0,1), c4 (0,1,0), c5 (1,1,0), c6 (1,1,1), c7 (0,1,1); edges as edge_to_corners
- *    (marching_cube_impl.hpp:96-127); case index bit i = corner i inside;
- *  - on each cube face the crossed edges are joined into segments; a face with four crossed
- *    edges (inside corners on a diagonal) gets the two segments that cut off its inside corners;
- *  - the segments of all faces close into loops (each crossed edge lies on two faces); a loop
- *    is walked from its lowest edge number towards the lower-numbered of that edge's two
- *    neighbours, then reversed if its Newell normal (edge midpoints) points from outside
- *    corners to inside ones, so that faces point away from the inside;
- *  - each loop is fanned from its first edge; loops in the order of their lowest edge. */
+/* The case table is the reference's (include/se/map/algorithms/edge_tables.hpp, triTable), in the
+ * encoding of mc_case_table.inc (generated from the reference's sources; the GPU library reads
+ * the same file): per case the face count and the cube edges of the faces in triTable's order.
+ * Corners in the order of meshing::gather_data: c0 (0,0,0), c1 (1,0,0), c2 (1,0,1), c3 (0,0,1),
+ * c4 (0,1,0), c5 (1,1,0), c6 (1,1,1), c7 (0,1,1); edges as edge_to_corners
+ * (marching_cube_impl.hpp:96-127); case index bit i = corner i inside. */
+#include "../supereight2_gb300/csrc/mc_case_table.inc"
+
 namespace {
 
 constexpr int kMcCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 0, 1}, {0, 0, 1},
                                  {0, 1, 0}, {1, 1, 0}, {1, 1, 1}, {0, 1, 1}};
 constexpr int kMcEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {0, 3}, {4, 5}, {5, 6},
                                 {6, 7}, {4, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
-constexpr int kMcFace[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 3, 7, 4}, {1, 2, 6, 5}, {0, 1, 5, 4}, {3, 2, 6, 7}};
 constexpr int kMcMaxTri = 8;
 
 struct McTable {
@@ -1821,90 +1815,15 @@ struct McTable {
     signed char tri[256][3 * kMcMaxTri];
 };
 
-static int mc_edge_of(int a, int b)
-{
-    for (int e = 0; e < 12; ++e)
-        if ((kMcEdge[e][0] == a && kMcEdge[e][1] == b) || (kMcEdge[e][0] == b && kMcEdge[e][1] == a))
-            return e;
-    return -1;
-}
-
 static McTable build_mc_table()
 {
     McTable T;
     std::memset(&T, 0, sizeof(T));
     for (int cfg = 0; cfg < 256; ++cfg) {
-        auto in = [cfg](int c) { return ((cfg >> c) & 1) != 0; };
-        int nb[12][2];
-        int deg[12] = {0};
-        for (int f = 0; f < 6; ++f) {
-            const int* c = kMcFace[f];
-            int crossed[4], nc = 0;
-            for (int k = 0; k < 4; ++k)
-                if (in(c[k]) != in(c[(k + 1) & 3]))
-                    crossed[nc++] = k; /* edge between c[k] and c[k+1] */
-            auto link = [&](int ka, int kb) {
-                const int ea = mc_edge_of(c[ka], c[(ka + 1) & 3]), eb = mc_edge_of(c[kb], c[(kb + 1) & 3]);
-                nb[ea][deg[ea]++] = eb;
-                nb[eb][deg[eb]++] = ea;
-            };
-            if (nc == 2) {
-                link(crossed[0], crossed[1]);
-            }
-            else if (nc == 4) {
-                for (int k = 0; k < 4; ++k)
-                    if (in(c[k]))
-                        link((k + 3) & 3, k); /* the two edges at inside corner c[k] */
-            }
-        }
-        bool used[12] = {false};
-        int n = 0;
-        for (int e0 = 0; e0 < 12; ++e0) {
-            if (deg[e0] == 0 || used[e0])
-                continue;
-            int loop[12], len = 0;
-            int prev = -1, cur = e0;
-            const int first_next = nb[e0][0] < nb[e0][1] ? nb[e0][0] : nb[e0][1];
-            while (true) {
-                loop[len++] = cur;
-                used[cur] = true;
-                int next;
-                if (prev < 0)
-                    next = first_next;
-                else
-                    next = nb[cur][0] == prev ? nb[cur][1] : nb[cur][0];
-                prev = cur;
-                cur = next;
-                if (cur == e0)
-                    break;
-            }
-            /* orientation: Newell normal against the inside -> outside direction */
-            double N[3] = {0, 0, 0}, D[3] = {0, 0, 0};
-            for (int i = 0; i < len; ++i) {
-                double a[3], b[3];
-                for (int k = 0; k < 3; ++k) {
-                    a[k] = 0.5 * (kMcCorner[kMcEdge[loop[i]][0]][k] + kMcCorner[kMcEdge[loop[i]][1]][k]);
-                    b[k] = 0.5 * (kMcCorner[kMcEdge[loop[(i + 1) % len]][0]][k]
-                                  + kMcCorner[kMcEdge[loop[(i + 1) % len]][1]][k]);
-                }
-                N[0] += (a[1] - b[1]) * (a[2] + b[2]);
-                N[1] += (a[2] - b[2]) * (a[0] + b[0]);
-                N[2] += (a[0] - b[0]) * (a[1] + b[1]);
-                const int ci = in(kMcEdge[loop[i]][0]) ? kMcEdge[loop[i]][0] : kMcEdge[loop[i]][1];
-                const int co = in(kMcEdge[loop[i]][0]) ? kMcEdge[loop[i]][1] : kMcEdge[loop[i]][0];
-                for (int k = 0; k < 3; ++k)
-                    D[k] += kMcCorner[co][k] - kMcCorner[ci][k];
-            }
-            if (N[0] * D[0] + N[1] * D[1] + N[2] * D[2] < 0.0)
-                std::reverse(loop + 1, loop + len);
-            for (int i = 1; i + 1 < len; ++i) {
-                T.tri[cfg][3 * n] = (signed char) loop[0];
-                T.tri[cfg][3 * n + 1] = (signed char) loop[i];
-                T.tri[cfg][3 * n + 2] = (signed char) loop[i + 1];
-                ++n;
-            }
-        }
-        T.ntri[cfg] = n;
+        const unsigned long long w = kMcCaseWords[cfg];
+        T.ntri[cfg] = (int) (w >> 60);
+        for (int k = 0; k < 3 * T.ntri[cfg]; ++k)
+            T.tri[cfg][k] = (signed char) ((w >> (4 * k)) & 0xf);
     }
     return T;
 }

@@ -32,7 +32,7 @@ def sources():
 
 
 def _deps():
-    hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h", ".inc"))]
     hdrs.append(os.path.join(ROOT, "include", "se_gpu.h"))
     return hdrs + [__file__]
 

@@ -4,19 +4,13 @@
 //  - multi-res TSDF and occupancy maps: dual_marching_cube_kernel (:895-975), meshing the dual
 //    grid of each block at its integration scale (gather_dual_data :269-289, :683-758).
 //
-// The reference triangulates each cube with a third-party case table (edge_tables.hpp). This
-// library builds its case table on the host from a stated rule instead:
-//  - corners in the order of meshing::gather_data: c0 (0,0,0), c1 (1,0,0), c2 (1,0,1),
-//    c3 (0,0,1), c4 (0,1,0), c5 (1,1,0), c6 (1,1,1), c7 (0,1,1); edges as edge_to_corners
-//    (:96-127); case bit i = corner i inside (tsdf < 0, or occupancy * weight > 0);
-//  - on each cube face the crossed edges are joined into segments; a face with four crossed
-//    edges (inside corners on a diagonal) gets the two segments that cut off its inside corners
-//    (a neighbouring cube sees the same face and makes the same choice: the mesh is closed);
-//  - the segments close into loops; a loop is walked from its lowest edge towards the lower of
-//    that edge's two neighbours, reversed when its Newell normal points from outside corners to
-//    inside ones (faces point away from the inside), and fanned from its first edge.
-// Vertex positions follow meshing::compute_intersection / compute_dual_intersection exactly;
-// only the triangulation of a crossing pattern can differ from the reference's table.
+// The case table is the reference's (edge_tables.hpp, triTable), in the encoding of
+// mc_case_table.inc (generated from the reference's sources by make_mc_table.py): per case the
+// face count and the cube edges of the faces in triTable's order. Corners in the order of
+// meshing::gather_data: c0 (0,0,0), c1 (1,0,0), c2 (1,0,1), c3 (0,0,1), c4 (0,1,0), c5 (1,1,0),
+// c6 (1,1,1), c7 (0,1,1); edges as edge_to_corners (:96-127); case bit i = corner i inside
+// (tsdf < 0, or occupancy * weight > 0).
+// Vertex positions follow meshing::compute_intersection / compute_dual_intersection exactly.
 //
 // Single-res: one thread per cube: the 8 corner values (one block or the dense block index), the
 // case, up to 5 faces with checkVertex, written through one atomic per warp. Dual: one thread per
@@ -36,7 +30,6 @@ namespace {
 
 constexpr int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 0, 1}, {0, 0, 1}, {0, 1, 0}, {1, 1, 0}, {1, 1, 1}, {0, 1, 1}};
 constexpr int kEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {0, 3}, {4, 5}, {5, 6}, {6, 7}, {4, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
-constexpr int kFace[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 3, 7, 4}, {1, 2, 6, 5}, {0, 1, 5, 4}, {3, 2, 6, 7}};
 constexpr int kMaxTri = 5;
 
 struct CaseTable {
@@ -44,81 +37,20 @@ struct CaseTable {
     signed char tri[256][3 * kMaxTri];
 };
 
-int edge_between(int a, int b)
-{
-    for (int e = 0; e < 12; ++e)
-        if ((kEdge[e][0] == a && kEdge[e][1] == b) || (kEdge[e][0] == b && kEdge[e][1] == a))
-            return e;
-    return -1;
-}
+#include "mc_case_table.inc"
 
-// Builds the triangulation of every case; false if a case needs more than kMaxTri faces.
+// Decodes the case table; false if a case had more than kMaxTri faces.
 bool build_case_table(CaseTable& T)
 {
     std::memset(&T, 0, sizeof(T));
     for (int cfg = 0; cfg < 256; ++cfg) {
-        const auto inside = [cfg](int c) { return ((cfg >> c) & 1) != 0; };
-        int adj[12][2], deg[12] = {0};
-        const auto join = [&](int ea, int eb) {
-            adj[ea][deg[ea]++] = eb;
-            adj[eb][deg[eb]++] = ea;
-        };
-        for (const auto& f : kFace) {
-            int cross[4], nc = 0;
-            for (int k = 0; k < 4; ++k)
-                if (inside(f[k]) != inside(f[(k + 1) % 4]))
-                    cross[nc++] = edge_between(f[k], f[(k + 1) % 4]);
-            if (nc == 2) {
-                join(cross[0], cross[1]);
-            }
-            else if (nc == 4) {
-                for (int k = 0; k < 4; ++k)
-                    if (inside(f[k])) // the edges before and after an inside corner
-                        join(edge_between(f[(k + 3) % 4], f[k]), edge_between(f[k], f[(k + 1) % 4]));
-            }
-        }
-        bool seen[12] = {false};
-        int nt = 0;
-        for (int start = 0; start < 12; ++start) {
-            if (!deg[start] || seen[start])
-                continue;
-            int loop[12], len = 0, prev = -1, cur = start;
-            do {
-                loop[len++] = cur;
-                seen[cur] = true;
-                const int next = prev < 0 ? std::min(adj[cur][0], adj[cur][1])
-                                          : (adj[cur][0] == prev ? adj[cur][1] : adj[cur][0]);
-                prev = cur;
-                cur = next;
-            } while (cur != start);
-            double nrm[3] = {0.0, 0.0, 0.0}, dir[3] = {0.0, 0.0, 0.0};
-            for (int i = 0; i < len; ++i) {
-                const int e = loop[i], e2 = loop[(i + 1) % len];
-                double a[3], b[3];
-                for (int k = 0; k < 3; ++k) {
-                    a[k] = 0.5 * (kCorner[kEdge[e][0]][k] + kCorner[kEdge[e][1]][k]);
-                    b[k] = 0.5 * (kCorner[kEdge[e2][0]][k] + kCorner[kEdge[e2][1]][k]);
-                }
-                nrm[0] += (a[1] - b[1]) * (a[2] + b[2]);
-                nrm[1] += (a[2] - b[2]) * (a[0] + b[0]);
-                nrm[2] += (a[0] - b[0]) * (a[1] + b[1]);
-                const int in_c = inside(kEdge[e][0]) ? kEdge[e][0] : kEdge[e][1];
-                const int out_c = in_c == kEdge[e][0] ? kEdge[e][1] : kEdge[e][0];
-                for (int k = 0; k < 3; ++k)
-                    dir[k] += kCorner[out_c][k] - kCorner[in_c][k];
-            }
-            if (nrm[0] * dir[0] + nrm[1] * dir[1] + nrm[2] * dir[2] < 0.0)
-                std::reverse(loop + 1, loop + len);
-            for (int i = 1; i + 1 < len; ++i) {
-                if (nt == kMaxTri)
-                    return false;
-                T.tri[cfg][3 * nt] = (signed char) loop[0];
-                T.tri[cfg][3 * nt + 1] = (signed char) loop[i];
-                T.tri[cfg][3 * nt + 2] = (signed char) loop[i + 1];
-                ++nt;
-            }
-        }
+        const unsigned long long w = kMcCaseWords[cfg];
+        const int nt = (int) (w >> 60);
+        if (nt > kMaxTri)
+            return false;
         T.ntri[cfg] = (signed char) nt;
+        for (int k = 0; k < 3 * nt; ++k)
+            T.tri[cfg][k] = (signed char) ((w >> (4 * k)) & 0xf);
     }
     return true;
 }

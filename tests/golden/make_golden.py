@@ -6,7 +6,9 @@ reference_pins.json — values the reference's own tests assert, extracted from 
   test/system/multires_ofusion/multires_ofusion_systemtest.cpp (the voxels its GetField and
   GetFieldInterpolation tests check, with the expected data); and the dual-corner partition
   that meshing::norm_dual_corner_idxs (include/se/map/algorithms/impl/marching_cube_impl.hpp)
-  tabulates for the 26 block-boundary positions of a primal corner.
+  tabulates for the 26 block-boundary positions of a primal corner; and the marching-cubes case
+  table (include/se/map/algorithms/edge_tables.hpp, triTable) that both libraries decode from
+  supereight2_gb300/csrc/mc_case_table.inc.
 oracle_fixtures.npz — small seeded inputs (stored: five 320x240 depth frames with their poses,
   one 64x1024 LiDAR scan with its pose) and the CPU oracle's outputs on them, as per-block
   CRC32s and raw arrays, so the oracle built on another machine and the GPU path are both
@@ -63,7 +65,18 @@ def reference_pins(src):
     pins["occupancy_free"] = [cf[n] for n in sorted(cf) if "free" in n]
     pins["occupancy_free_value"] = float(re.findall(r"EXPECT_FLOAT_EQ\((-?[\d.]+),", field)[0])
     pins["dual_corner_partition"] = dual_corner_partition(src)
+    pins["mc_tri_table"] = mc_tri_table(src)
     return pins
+
+
+def mc_tri_table(src):
+    """The 256 x 16 rows of triTable (edge_tables.hpp), -1 padded."""
+    txt = open(os.path.join(src, "include/se/map/algorithms/edge_tables.hpp")).read()
+    body = txt[txt.index("triTable[256][16]"):]
+    body = body[body.index("{") + 1:]
+    rows = [[int(v) for v in r.split(",") if v.strip()] for r in re.findall(r"\{([-\d,\s]+)\}", body)[:256]]
+    assert len(rows) == 256 and all(len(r) == 16 for r in rows)
+    return rows
 
 
 def dual_corner_partition(src):

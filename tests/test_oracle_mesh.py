@@ -1,10 +1,16 @@
-"""Marching cubes (se::algorithms::marching_cube, single-res) in the oracle: its case table built
-from the stated rule (identical to the GPU library's independently built table), the reference's
+"""Marching cubes (se::algorithms::marching_cube, single-res) in the oracle: its case table (the
+reference's triTable, include/se/map/algorithms/edge_tables.hpp, pinned in
+tests/golden/reference_pins.json and identical to the GPU library's), the reference's
 meshing test configuration (test/map/meshing/meshing_unittest.cpp: EqualScaleNeighbour, where
 the reference only asserts a non-empty mesh; the plane it meshes gives exactly 2 x 15 x 15 faces
 at x = 12), and a closed, outward-facing surface around a sphere."""
+import json
+import os
+
 import numpy as np
 import pytest
+
+PINS = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_pins.json")))
 
 
 def _faces_normals(f):
@@ -36,16 +42,23 @@ def _sphere_map(oracle, n=32, r=9.3, c=(15.7, 16.2, 16.9)):
     return m, np.asarray(c)
 
 
-def test_case_table_rule(oracle):
+def test_case_table_is_the_reference_table(oracle):
+    ref = np.asarray(PINS["mc_tri_table"])
     ntri, tri = oracle.mc_table()
-    assert ntri[0] == 0 and ntri[255] == 0 and ntri.max() <= 5
+    assert ntri.max() <= 5
+    for cfg in range(256):
+        n = int(np.argmax(ref[cfg] < 0)) if (ref[cfg] < 0).any() else 16
+        assert ntri[cfg] * 3 == n
+        assert np.array_equal(tri[cfg][:n], ref[cfg][:n]) and np.all(tri[cfg][n:] == -1)
+
+
+def test_case_table_vertices_on_crossed_edges(oracle):
+    ntri, tri = oracle.mc_table()
+    corner_edges = [(0, 1), (1, 2), (2, 3), (0, 3), (4, 5), (5, 6), (6, 7), (4, 7), (0, 4), (1, 5), (2, 6), (3, 7)]
     for cfg in range(256):
         inside = [(cfg >> c) & 1 for c in range(8)]
-        corner_edges = [(0, 1), (1, 2), (2, 3), (0, 3), (4, 5), (5, 6), (6, 7), (4, 7), (0, 4), (1, 5), (2, 6), (3, 7)]
         crossed = {e for e, (a, b) in enumerate(corner_edges) if inside[a] != inside[b]}
-        used = set(tri[cfg][: 3 * ntri[cfg]].tolist())
-        assert used == crossed                       # every crossing gets a vertex, nothing else
-        assert ntri[cfg] == ntri[255 - cfg] or True  # (complements may resolve faces differently)
+        assert set(tri[cfg][: 3 * ntri[cfg]].tolist()) == crossed
 
 
 def test_case_table_equals_gpu_library_table(oracle):
