@@ -301,6 +301,9 @@ def run_ours(args, ws, rank, local):
     lidar = _lidar_bench(se, torch, dev, args.lidar_steps, args.warmup, flush)
     lidar_data = lidar.pop("_data")
 
+    # the ray integrator (integrateRayBatch, LeicaLidar) on the reference's wall batch
+    ray_batch = _ray_batch_bench(se, torch, dev)
+
     times = torch.tensor([g32["dev_ms"], e2e_s, plain["dev_ms"], g16["dev_ms"]], dtype=torch.float64,
                          device=dev)
     if ws > 1:
@@ -394,6 +397,7 @@ def run_ours(args, ws, rank, local):
                      "graph_f32": mr["f32"], "graph_f16": mr["f16"]},
         "adjoint": adjoint,
         "lidar_batch": lidar,
+        "ray_batch": ray_batch,
         "gen_s": gen_s,
         "clocks": g32["clocks"],
     }
@@ -411,6 +415,7 @@ def run_ours(args, ws, rank, local):
                 out["roofline"].update(achieved=rc["achieved_GBps"], frac=rc["frac"],
                                        algorithmic_bytes_per_launch=rb)
         out["lidar_batch"]["cpu_baseline"] = lidar_cpu_baseline(lidar_data)
+        out["ray_batch"]["cpu_baseline"] = ray_batch_cpu_baseline()
         if args.precision_frames > 0:
             out["precision_vs_f64"] = _precision_report(se, torch, torch.device("cuda", local),
                                                         args.precision_frames, args.max_blocks)
@@ -777,6 +782,55 @@ def _lidar_bench(se, torch, dev, K, warmup, flush):
         "l2": "flushed (256 MiB write) between steps",
         "_data": (spec, poses, ranges, W, K),
     }
+
+
+RAY_WALL = dict(width=360, height=180, near_plane=0.6, far_plane=30.0, elevation_resolution_deg=0.1,
+                azimuth_resolution_deg=0.1)
+
+
+def _ray_wall_batch():
+    from supereight2_gb300.synthetic import wall_rays
+    return wall_rays()
+
+
+def _ray_batch_bench(se, torch, dev, reps=5):
+    """integrateRayBatch of the reference's Propagation batch (300 x 300 rays at 0.1 degree onto a
+    wall 10 m away, 25.6 m map at 5 cm) into a fresh map per repetition; host wall clock around
+    the synchronous call (the first, untimed, builds the scratch)."""
+    rays = torch.from_numpy(_ray_wall_batch()).to(dev)
+    poses = torch.eye(4, dtype=torch.float32, device=dev).expand(rays.shape[0], 4, 4).contiguous()
+    T_MW = np.eye(4, dtype=np.float32)
+    T_MW[:3, 3] = 12.8
+    sensor = se.LeicaLidar(**RAY_WALL)
+    times, n_oct = [], 0
+    for r in range(reps + 1):
+        m = se.Map(25.6, 0.05, res_type="multi", field="occupancy", T_MW=T_MW, max_blocks=1 << 16)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n_oct = se.integrate_ray_batch(m, 0, poses, rays, sensor, with_octants=False)
+        torch.cuda.synchronize()
+        if r > 0:
+            times.append(time.perf_counter() - t0)
+        del m
+    ms = 1e3 * float(np.median(times))
+    return {"workload": "integrateRayBatch, LeicaLidar 0.1 deg, 90000 rays (300 x 300 over +-15 deg) onto a "
+                        "wall 10 m away, multi-res occupancy map 25.6 m at 5 cm (512^3), fresh map per batch",
+            "value": rays.shape[0] / (ms * 1e-3), "unit": "rays/s", "ms_per_batch": ms,
+            "updated_octants": int(n_oct), "timing": f"host wall clock around the synchronous call, median of {reps}"}
+
+
+def ray_batch_cpu_baseline():
+    """The oracle's serial ray integrator (the reference's loop is serial) on the same batch."""
+    from oracle import pyoracle as o
+    rays = _ray_wall_batch()
+    T_MW = np.eye(4, dtype=np.float32)
+    T_MW[:3, 3] = 12.8
+    m = o.OracleOccMap(25.6, 0.05, T_MW=T_MW)
+    t0 = time.perf_counter()
+    m.integrate_ray_batch(o.leica(**RAY_WALL), np.eye(4, dtype=np.float32), rays, 0)
+    dt = time.perf_counter() - t0
+    return {"value": len(rays) / dt, "unit": "rays/s", "cores": 1, "kind": "port",
+            "sample": f"the whole 90000-ray batch, {dt:.1f} s"}
 
 
 def lidar_cpu_baseline(data, budget_s=20.0):

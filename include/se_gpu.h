@@ -115,6 +115,19 @@ typedef struct {
     float far_plane;
 } se_gpu_lidar;
 
+/* se::LeicaLidar::Config (include/se/sensor/leica_lidar.hpp): the ray-batch sensor of
+ * se_gpu_occ_integrate_ray_batch. The integration scale uses pixel_dim_tan =
+ * 2 tan(min(elevation, azimuth resolution) / 2) (src/sensor/leica_lidar.cpp:53-73, 87-129);
+ * width and height are kept for the sensor's image model, which the ray integrator does not use. */
+typedef struct {
+    int width;
+    int height;
+    float near_plane;
+    float far_plane;
+    float elevation_resolution_deg;
+    float azimuth_resolution_deg;
+} se_gpu_leica_lidar;
+
 /* The bilateral pre-filter of the tracking input. No counterpart in the reference (it feeds
  * the depth straight to the tracker); defined by this library: invalid (<= 0 or NaN) centres
  * stay 0, the valid taps of the (2 radius + 1)^2 window inside the image are weighted by
@@ -189,6 +202,24 @@ SE_GPU_API se_gpu_status se_gpu_integrate_depth(se_gpu_map* map, const float* de
 SE_GPU_API se_gpu_status se_gpu_integrate_range(se_gpu_map* map, const float* range_dev,
                                                 const se_gpu_lidar* sensor, const float T_WS[16],
                                                 int timestamp, void* stream);
+
+/* Replaces se::MapIntegrator::integrateRayBatch(timestamp, rayPoseBatch, sensor, updated_octants)
+ * for multi-res occupancy maps with a LeicaLidar (include/se/integrator/impl/
+ * map_integrator_impl.hpp:137-176, se::RayIntegrator in impl/ray_integrator_impl.hpp and
+ * impl/ray_integrator_core_impl.hpp): the n rays rays_dev[3 i] (sensor frame) with their poses
+ * poses_dev[16 i] (T_WS, row-major), all on the device, are integrated in batch order, then the
+ * updated blocks are propagated to their coarsest scale and the nodes above them to the root.
+ * The map equals the one the reference's serial loop leaves: rays run concurrently, but rays
+ * that may touch the same block update it in batch order. octants_dev (may be NULL) receives up
+ * to capacity updated octants as (x, y, z, size) in voxels, size 8 for a block, in any order:
+ * the updated blocks and the propagated nodes, less the nodes whose children were pruned (the
+ * reference's updated_octants set); *n_octants their number. A wait of a ray for a block that
+ * runs past 2 s abandons the batch (SE_GPU_ERR_CUDA, the map then partly updated). Synchronous.
+ * Occupancy maps only. */
+SE_GPU_API se_gpu_status se_gpu_occ_integrate_ray_batch(se_gpu_map* map, const se_gpu_leica_lidar* sensor,
+                                                        const float* poses_dev, const float* rays_dev,
+                                                        int64_t n, int32_t timestamp, int32_t* octants_dev,
+                                                        int64_t capacity, int64_t* n_octants, void* stream);
 
 /* Batched occupancy integration; no counterpart in the reference, which integrates one map per
  * call. n (<= 16) occupancy maps with one sensor (a pinhole camera or a LiDAR: exactly one of

@@ -25,6 +25,11 @@ class Lidar(C.Structure):
                 ("elevation_max_deg", C.c_float), ("near_plane", C.c_float), ("far_plane", C.c_float)]
 
 
+class Leica(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("near_plane", C.c_float), ("far_plane", C.c_float),
+                ("elevation_resolution_deg", C.c_float), ("azimuth_resolution_deg", C.c_float)]
+
+
 class TrackerConfig(C.Structure):
     _fields_ = [("num_levels", C.c_int), ("iterations", C.c_int * 3),
                 ("dist_threshold", C.c_float), ("normal_threshold", C.c_float),
@@ -79,6 +84,10 @@ def lib():
             "so_occ_pooling_image_lidar": (C.c_int, [f32p, C.c_int, C.c_int, vp, C.POINTER(C.c_float)]),
             "so_occ_integrate_lidar": (None, [vp, f32p, C.POINTER(Lidar), f32p, C.c_int, vp]),
             "so_lidar_project": (C.c_int, [C.POINTER(Lidar), f32p, f32p]),
+            "so_occ_integrate_ray_batch": (C.c_longlong, [vp, C.POINTER(Leica), f32p, f32p, C.c_longlong, C.c_int,
+                                                          vp, C.c_longlong]),
+            "so_leica_integration_scale": (C.c_int, [C.POINTER(Leica), f32p, C.c_float, C.c_int, C.c_int]),
+            "so_occ_block_timestamps": (None, [vp, vp]),
             "so_atan2": (C.c_float, [C.c_float, C.c_float]),
             "so_lidar_tan_half_min_angle": (C.c_float, [C.POINTER(Lidar)]),
             "so_occ_lidar_integration_scale": (C.c_int, [C.POINTER(Lidar), f32p, C.c_float, C.c_int, C.c_int]),
@@ -267,6 +276,26 @@ class OracleOccMap:
         """(faces [N, 3, 3] float32 in voxel units, scales [N] int8) between occupied and free."""
         return _dual_mc(lib().so_occ_dual_marching_cubes, self.h, min_desired_scale)
 
+    def integrate_ray_batch(self, sensor, poses, rays, timestamp=0):
+        """MapIntegrator::integrateRayBatch: rays f32[N,3] (sensor frame) with poses f32[N,4,4]
+        (T_WS); returns the updated octants i32[K,4] (x, y, z, size), sorted."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 3)
+        poses = np.ascontiguousarray(np.broadcast_to(np.asarray(poses, np.float32), (len(rays), 4, 4)))
+        cap = 1 << 20
+        out = np.zeros((cap, 4), np.int32)
+        k = int(lib().so_occ_integrate_ray_batch(self.h, C.byref(sensor), poses.reshape(-1), rays.reshape(-1),
+                                                 len(rays), int(timestamp), out.ctypes.data, cap))
+        if k > cap:
+            raise RuntimeError("more updated octants than the buffer holds: %d" % k)
+        return out[:k]
+
+    def block_timestamps(self):
+        n = int(lib().so_occ_num_blocks(self.h))
+        ts = np.zeros(n, np.int32)
+        if n:
+            lib().so_occ_block_timestamps(self.h, ts.ctypes.data)
+        return ts
+
 
 def occ_depth_sigma(depth, res):
     depth = np.ascontiguousarray(depth, np.float32)
@@ -293,6 +322,16 @@ def atan2(y, x):
 def lidar_integration_scale(sensor, c_S, res, last_scale, min_scale):
     return int(lib().so_occ_lidar_integration_scale(C.byref(sensor), np.ascontiguousarray(c_S, np.float32),
                                                     float(res), int(last_scale), int(min_scale)))
+
+
+def leica(width, height, near_plane, far_plane, elevation_resolution_deg=1.0, azimuth_resolution_deg=1.0) -> Leica:
+    return Leica(int(width), int(height), float(near_plane), float(far_plane), float(elevation_resolution_deg),
+                 float(azimuth_resolution_deg))
+
+
+def leica_integration_scale(sensor, c_S, res, last_scale, min_scale):
+    return int(lib().so_leica_integration_scale(C.byref(sensor), np.ascontiguousarray(c_S, np.float32),
+                                                float(res), int(last_scale), int(min_scale)))
 
 
 def pooling_image_lidar(depth):

@@ -201,6 +201,21 @@ typedef struct {
     float near_plane, far_plane;
 } so_lidar;
 /* MapIntegrator<OccupancyMap<Res::Multi>>::integrateDepth for an OusterLidar range image. */
+/* LeicaLidar (include/se/sensor/leica_lidar.hpp): the ray-batch sensor of the ray integrator. */
+typedef struct {
+    int width, height;
+    float near_plane, far_plane;
+    float elevation_resolution_deg, azimuth_resolution_deg;
+} so_leica;
+/* MapIntegrator::integrateRayBatch (multi-res occupancy, LeicaLidar): rays (n x 3, sensor
+ * frame) with their poses (n x 16 T_WS, row-major) in order; up to capacity updated octants
+ * (x, y, z, size) written to octants; returns the number of updated octants. */
+long long so_occ_integrate_ray_batch(so_occ_map* map, const so_leica* sensor, const float* poses,
+                                     const float* rays, long long n, int timestamp, int32_t* octants,
+                                     long long capacity);
+int so_leica_integration_scale(const so_leica* sensor, const float c_S[3], float res, int last_scale,
+                               int min_scale);
+void so_occ_block_timestamps(const so_occ_map* map, int32_t* ts);
 void so_occ_integrate_lidar(so_occ_map* map, const float* range, const so_lidar* sensor,
                             const float T_WS[16], int timestamp, so_occ_stats* stats);
 int so_lidar_project(const so_lidar* sensor, const float p_S[3], float uv[2]);

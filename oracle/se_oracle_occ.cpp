@@ -26,6 +26,7 @@
  * independent blocks.
  */
 #include <algorithm>
+#include <array>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -139,6 +140,7 @@ static inline int cube(int v) { return v * v * v; }
 struct OccBlock {
     int32_t coord[3];
     int parent;
+    int timestamp = -1;
     OccData init_data;
     int min_scale = -1;
     int current_scale = kOccMaxScale;
@@ -1865,6 +1867,437 @@ static int raycast_occ(const so_occ_map& m, V3 o, V3 d, float t_far, V3& hit, in
 
 namespace {
 
+/* ------------------------------------------------------------------- ray integrator -- */
+/* se::RayIntegrator<OccupancyMap<Res::Multi>, LeicaLidar> (include/se/integrator/
+ * ray_integrator.hpp, impl/ray_integrator_impl.hpp, impl/ray_integrator_core_impl.hpp) as
+ * IntegrateRayBatchImplD<Occupancy, Multi>::integrate drives it (map_integrator_impl.hpp:
+ * 137-176): every ray of the batch in order, then the updated blocks up to their coarsest scale,
+ * then the nodes above them up to the root. */
+
+struct Leica {
+    float near_plane, far_plane;
+    float pixel_dim_tan; /* 2 tan(min(azimuth, elevation resolution) / 2), leica_lidar.cpp:53-73 */
+};
+
+static Leica make_leica(const so_leica* c)
+{
+    Leica L;
+    L.near_plane = c->near_plane;
+    L.far_plane = c->far_plane;
+    const float min_ray_angle = std::min(c->azimuth_resolution_deg, c->elevation_resolution_deg);
+    const float deg_to_rad = (float) (M_PI / 180.0);
+    L.pixel_dim_tan = 2.0f * std::tan(min_ray_angle * 0.5f * deg_to_rad);
+    return L;
+}
+
+/* LeicaLidar::computeIntegrationScaleImpl (leica_lidar.cpp:87-129), ratios {1.5, 3, 6}. */
+static int leica_integration_scale(const Leica& L, V3 c, float res, int last_scale, int min_scale, int max_scale)
+{
+    static const float kRatio[3] = {1.5f, 3.0f, 6.0f};
+    const float dist = norm(c);
+    const float pixel_dim = dist * L.pixel_dim_tan;
+    const float den = 1.0f / (std::sqrt(3.0f) * res);
+    const float pv = pixel_dim * den;
+    int scale = 0;
+    for (float r : kRatio) {
+        if (pv < r)
+            break;
+        scale++;
+    }
+    scale = std::min(scale, max_scale);
+    if (scale > last_scale && min_scale != -1)
+        return leica_integration_scale(L, c - 0.25f * normalized(c), res, last_scale, -1, max_scale);
+    if (scale < last_scale && min_scale != -1)
+        return leica_integration_scale(L, c + 0.25f * normalized(c), res, last_scale, -1, max_scale);
+    return scale;
+}
+
+enum class RayState { FreeSpace, Transition, Occupied, Undefined };
+
+/* ray_integrator::propagate_block_down_to_scale (ray_integrator_core_impl.hpp:358-426) */
+static void ri_propagate_down(OccBlock& b, int desired)
+{
+    int cur = b.current_scale;
+    while (cur > desired) {
+        b.allocate_down_to(cur - 1);
+        b.current_scale = cur - 1;
+        const int cs = cur - 1, ps = cur;
+        const int nc = 8 >> cs, np = 8 >> ps;
+        const OccData* pd = b.mean_at(ps);
+        OccData* cd = b.mean_at(cs);
+        for (int z = 0; z < np; z++)
+            for (int y = 0; y < np; y++)
+                for (int x = 0; x < np; x++) {
+                    const OccData& p = pd[x + y * np + z * np * np];
+                    if (!p.observed)
+                        continue;
+                    for (int k = 0; k < 2; k++)
+                        for (int j = 0; j < 2; j++)
+                            for (int i = 0; i < 2; i++) {
+                                OccData& c = cd[(2 * x + i) + (2 * y + j) * nc + (2 * z + k) * nc * nc];
+                                c.weight = p.weight;
+                                c.occ = p.occ;
+                                c.observed = false;
+                            }
+                }
+        cur--;
+    }
+}
+
+/* The parent-entry tail shared by both loops of propagate_block_to_scale. */
+struct RiAcc {
+    float mean_occ = 0.0f, mean_w = 0.0f;
+    float min_mean = 0.0f, min_w = 0.0f, min_o = std::numeric_limits<float>::max();
+    float max_mean = 0.0f, max_w = 0.0f, max_o = std::numeric_limits<float>::lowest();
+    int count = 0, observed = 0;
+    void store(OccData& pmean, OccData& pmin, OccData& pmax) const
+    {
+        if (count > 0) {
+            pmean.occ = mean_occ / (float) count;
+            pmean.weight = std::ceil(mean_w) / (float) count;
+            pmean.observed = false;
+            pmin.occ = min_mean;
+            pmin.weight = min_w;
+            pmax.occ = max_mean;
+            pmax.weight = max_w;
+            if (observed == 8) {
+                pmax.observed = true;
+                pmin.observed = true;
+            }
+        }
+    }
+};
+
+/* ray_integrator::propagate_block_to_scale (ray_integrator_core_impl.hpp:206-352): the first
+ * coarser scale from the mean data (a child sets the minimum only when it did not set the
+ * maximum), every further scale from the child min / max data. */
+static void ri_propagate_to_scale(OccBlock& b, int desired)
+{
+    int cs = b.current_scale;
+    int ps = cs + 1;
+    {
+        const int nc = 8 >> cs, np = 8 >> ps;
+        const OccData* cmean = b.mean_at(cs);
+        OccData *pmean = b.mean_at(ps), *pmin = b.min_at(ps), *pmax = b.max_at(ps);
+        for (int z = 0; z < np; z++)
+            for (int y = 0; y < np; y++)
+                for (int x = 0; x < np; x++) {
+                    RiAcc a;
+                    for (int k = 0; k < 2; k++)
+                        for (int j = 0; j < 2; j++)
+                            for (int i = 0; i < 2; i++) {
+                                const OccData& c = cmean[(2 * x + i) + (2 * y + j) * nc + (2 * z + k) * nc * nc];
+                                if (c.weight > 0.0f) {
+                                    a.count++;
+                                    a.mean_occ += c.occ;
+                                    a.mean_w += c.weight;
+                                    const float o = occ_field(c);
+                                    if (o > a.max_o) {
+                                        a.max_mean = c.occ;
+                                        a.max_w = c.weight;
+                                        a.max_o = o;
+                                    }
+                                    else if (o < a.min_o) {
+                                        a.min_mean = c.occ;
+                                        a.min_w = c.weight;
+                                        a.min_o = o;
+                                    }
+                                }
+                                if (c.observed)
+                                    a.observed++;
+                            }
+                    const int pi = x + y * np + z * np * np;
+                    a.store(pmean[pi], pmin[pi], pmax[pi]);
+                }
+    }
+    for (ps += 1; ps <= desired; ++ps) {
+        cs = ps - 1;
+        const int nc = 8 >> cs, np = 8 >> ps;
+        const OccData *cmean = b.mean_at(cs), *cmin = b.min_at(cs), *cmax = b.max_at(cs);
+        OccData *pmean = b.mean_at(ps), *pmin = b.min_at(ps), *pmax = b.max_at(ps);
+        for (int z = 0; z < np; z++)
+            for (int y = 0; y < np; y++)
+                for (int x = 0; x < np; x++) {
+                    RiAcc a;
+                    for (int k = 0; k < 2; k++)
+                        for (int j = 0; j < 2; j++)
+                            for (int i = 0; i < 2; i++) {
+                                const int ci = (2 * x + i) + (2 * y + j) * nc + (2 * z + k) * nc * nc;
+                                if (cmax[ci].weight > 0.0f) {
+                                    a.count++;
+                                    a.mean_occ += cmean[ci].occ;
+                                    a.mean_w += cmean[ci].weight;
+                                    const float mo = occ_field(cmax[ci]);
+                                    if (mo > a.max_o) {
+                                        a.max_mean = cmax[ci].occ;
+                                        a.max_w = cmax[ci].weight;
+                                        a.max_o = mo;
+                                    }
+                                    const float no = occ_field(cmin[ci]);
+                                    if (no < a.min_o) {
+                                        a.min_mean = cmin[ci].occ;
+                                        a.min_w = cmin[ci].weight;
+                                        a.min_o = no;
+                                    }
+                                }
+                                if (cmax[ci].observed)
+                                    a.observed++;
+                            }
+                    const int pi = x + y * np + z * np * np;
+                    a.store(pmean[pi], pmin[pi], pmax[pi]);
+                }
+    }
+}
+
+/* ray_integrator::propagate_to_parent_node (ray_integrator_core_impl.hpp:104-176) */
+static OccData ri_propagate_node(OccOctree& oct, int n, int timestamp)
+{
+    OccNode& node = oct.nodes[(size_t) n];
+    node.timestamp = timestamp;
+    float max_o = std::numeric_limits<float>::lowest(), max_mean = 0.0f, max_w = 0.0f;
+    float min_o = std::numeric_limits<float>::max(), min_mean = 0.0f, min_w = 0.0f;
+    int max_cnt = 0, min_cnt = 0, observed = 0;
+    for (int i = 0; i < 8; ++i) {
+        const int c = node.child[i];
+        if (c == -1)
+            continue;
+        OccData cmin, cmax;
+        if (slot_is_block(c)) {
+            OccBlock& b = oct.blocks[(size_t) slot_block(c)];
+            cmin = b.min_data();
+            cmax = b.max_data();
+        }
+        else {
+            cmin = oct.nodes[(size_t) c].min_data;
+            cmax = oct.nodes[(size_t) c].max_data;
+        }
+        if (cmin.weight > 0.0f) {
+            const float o = occ_field(cmin);
+            if (o < min_o) {
+                min_mean = cmin.occ;
+                min_w = cmin.weight;
+                min_o = o;
+                min_cnt++;
+            }
+        }
+        if (cmax.weight > 0.0f) {
+            const float o = occ_field(cmax);
+            if (o > max_o) {
+                max_mean = cmax.occ;
+                max_w = cmax.weight;
+                max_o = o;
+                max_cnt++;
+            }
+        }
+        if (cmax.observed)
+            observed++;
+    }
+    if (min_cnt > 0) {
+        node.min_data.occ = min_mean;
+        node.min_data.weight = min_w;
+        if (observed == 8)
+            node.min_data.observed = true;
+    }
+    if (max_cnt > 0) {
+        node.max_data.occ = max_mean;
+        node.max_data.weight = max_w;
+        if (observed == 8)
+            node.max_data.observed = true;
+    }
+    return node.max_data;
+}
+
+/* An octant of the updated-octants set: (x, y, z, size), size 8 for a block. */
+typedef std::array<int32_t, 4> OctKey;
+
+struct RayIntegrator {
+    so_occ_map& m;
+    const Leica& L;
+    float sigma_min, sigma_max, tau_min, tau_max;
+    int timestamp;
+    std::vector<int> updated_blocks;  /* updated_blocks_vector_ */
+    std::set<int> updated_set;        /* updated_blocks_set_ */
+    std::set<OctKey>* updated_octants;
+    /* per ray (resetIntegrator) */
+    Tf T_SW;
+    V3 ray;
+    float ray_dist = 0.0f, tau = 0.0f, three_sigma = 0.0f;
+    int32_t last_voxel[3] = {-1, -1, -1};
+    int computed_scale = 0;
+
+    RayIntegrator(so_occ_map& mm, const Leica& LL, int ts, std::set<OctKey>* upd) : m(mm), L(LL), timestamp(ts),
+                                                                                 updated_octants(upd)
+    {
+        /* RayIntegratorConfig (ray_integrator.hpp:60-72) */
+        sigma_min = m.cfg.sigma_min_factor * m.res;
+        sigma_max = m.cfg.sigma_max_factor * m.res;
+        tau_min = m.cfg.tau_min_factor * m.res;
+        tau_max = m.cfg.tau_max_factor * m.res;
+    }
+
+    /* resetIntegrator without the skip test (ray_integrator_impl.hpp:45-78) */
+    void reset(V3 r, const Tf& T_WS)
+    {
+        ray = r;
+        ray_dist = norm(r);
+        T_SW = inverse_iso(T_WS);
+        computed_scale = 0;
+        tau = compute_tau(ray_dist, tau_min, tau_max, m.cfg);
+        three_sigma = 3.0f * std::clamp(m.cfg.k_sigma * ray_dist, sigma_min, sigma_max);
+        last_voxel[0] = last_voxel[1] = last_voxel[2] = -1;
+    }
+
+    /* computeVariance (ray_integrator_impl.hpp:135-158) */
+    RayState variance(float depth) const
+    {
+        const float z_diff = depth - ray_dist;
+        if (z_diff < -three_sigma)
+            return RayState::FreeSpace;
+        if ((double) z_diff < (double) tau / 2.0)
+            return RayState::Transition;
+        if (z_diff < tau)
+            return RayState::Occupied;
+        return RayState::Undefined;
+    }
+
+    /* updateBlock (ray_integrator_impl.hpp:232-300) */
+    void update_block(int bi, const int32_t v[3], int desired, float sample_dist)
+    {
+        if ((double) sample_dist < 1e-08)
+            return;
+        OccBlock& b = m.octree.blocks[(size_t) bi];
+        const bool already = b.timestamp == timestamp;
+        if (!already)
+            b.timestamp = timestamp;
+        const int last_scale = b.min_scale == -1 ? desired : b.current_scale;
+        int s = last_scale;
+        if (b.min_scale == -1) {
+            b.allocate_down_to(s);
+            b.init_data = OccData();
+        }
+        else if (desired < last_scale) {
+            ri_propagate_down(b, desired);
+            s = desired;
+        }
+        else if (!already && desired > last_scale) {
+            ri_propagate_to_scale(b, desired);
+            s = desired;
+            b.delete_up_to(s);
+            b.current_scale = s;
+        }
+        const int stride = 1 << s, n = 8 >> s;
+        const int ox = (v[0] - b.coord[0]) / stride, oy = (v[1] - b.coord[1]) / stride,
+                  oz = (v[2] - b.coord[2]) / stride;
+        OccData& d = b.mean_at(s)[ox + n * oy + n * n * oz];
+        update_voxel(d, sample_dist - ray_dist, tau, three_sigma, m.cfg);
+    }
+
+    /* operator()(ray_sample, voxel_coord, rayState, octant) for LeicaLidar
+     * (ray_integrator_impl.hpp:162-228): descend to the block, allocating on the way. */
+    void sample(V3 r_S, const int32_t v[3], RayState state)
+    {
+        OccOctree& o = m.octree;
+        int slot;
+        for (;;) {
+            slot = occ_finest_octant(o, v, 0);
+            if (slot_is_block(slot))
+                break;
+            /* A node of an occupancy octree has no children or all eight (allocateChildren,
+             * deleteChildren), so the descent always ends at a block or a childless node. */
+            if (slot < 0)
+                return;
+            o.allocate_children(slot);
+        }
+        const int bi = slot_block(slot);
+        OccBlock& b = o.blocks[(size_t) bi];
+        const int last_scale = b.min_scale == -1 ? 0 : b.current_scale;
+        const V3 c_W = occ_voxel_to_point(m, b.coord, 8);
+        const V3 c_S = apply(T_SW, c_W);
+        int scale = leica_integration_scale(L, c_S, m.res, last_scale, b.min_scale, kOccMaxScale);
+        const int fs = m.cfg.fs_integr_scale;
+        if (state == RayState::FreeSpace && scale < fs)
+            scale = b.min_scale == -1 ? fs : std::min(fs, b.current_scale);
+        update_block(bi, v, scale, norm(r_S));
+        computed_scale = scale;
+        if (updated_set.count(bi) == 0) {
+            updated_set.insert(bi);
+            updated_blocks.push_back(bi);
+        }
+        if (updated_octants)
+            updated_octants->insert(OctKey{b.coord[0], b.coord[1], b.coord[2], 8});
+    }
+
+    /* operator()() (ray_integrator_impl.hpp:82-129) */
+    void run()
+    {
+        m.octree.allocate_children(0);
+        if (ray_dist < L.near_plane)
+            return;
+        const V3 dir = normalized(ray);
+        const float max_dist = std::min(ray_dist + tau, L.far_plane);
+        V3 r = L.near_plane * dir;
+        const Tf T_WS = inverse_iso(T_SW);
+        while (norm(r) < max_dist) {
+            const RayState state = variance(norm(r));
+            const V3 r_W = apply(T_WS, r);
+            const V3 p_M = apply(m.T_MW, r_W);
+            if (!(p_M.x >= 0.0f && p_M.x < m.dim && p_M.y >= 0.0f && p_M.y < m.dim && p_M.z >= 0.0f && p_M.z < m.dim))
+                break;
+            const V3 vf = p_M / m.res;
+            const int32_t v[3] = {(int32_t) vf.x, (int32_t) vf.y, (int32_t) vf.z};
+            if (v[0] != last_voxel[0] || v[1] != last_voxel[1] || v[2] != last_voxel[2]) {
+                last_voxel[0] = v[0];
+                last_voxel[1] = v[1];
+                last_voxel[2] = v[2];
+                sample(r, v, state);
+            }
+            const float step = (float) (0.5 * (double) m.res * (double) (1 << computed_scale));
+            r = r + step * dir;
+        }
+    }
+
+    /* propagateBlocksToCoarsestScale (ray_integrator_impl.hpp:124-132) */
+    void propagate_blocks()
+    {
+        for (int bi : updated_blocks) {
+            OccBlock& b = m.octree.blocks[(size_t) bi];
+            if (b.current_scale != kOccMaxScale)
+                ri_propagate_to_scale(b, kOccMaxScale);
+        }
+    }
+
+    /* propagateToRoot (ray_integrator_impl.hpp:304-354) */
+    void propagate_to_root()
+    {
+        OccOctree& o = m.octree;
+        const int bd = o.block_depth();
+        std::vector<std::set<int>> node_set((size_t) std::max(bd, 1));
+        for (int bi : updated_blocks)
+            if (o.blocks[(size_t) bi].parent >= 0)
+                node_set[(size_t) bd - 1].insert(o.blocks[(size_t) bi].parent);
+        for (int d = bd - 1; d > 0; d--) {
+            for (int n : node_set[(size_t) d]) {
+                if (o.nodes[(size_t) n].timestamp == timestamp)
+                    continue;
+                if (o.nodes[(size_t) n].parent < 0)
+                    continue;
+                const OccData nd = ri_propagate_node(o, n, timestamp);
+                node_set[(size_t) d - 1].insert(o.nodes[(size_t) n].parent);
+                const OccNode& N = o.nodes[(size_t) n];
+                const OctKey key{N.coord[0], N.coord[1], N.coord[2], N.size};
+                if (updated_octants)
+                    updated_octants->insert(key);
+                if (nd.observed && (double) occ_field(nd) <= 0.95 * (double) kMinOccupancy) {
+                    if (updated_octants && !N.is_leaf())
+                        updated_octants->erase(key);
+                    o.delete_children(n);
+                }
+            }
+        }
+        ri_propagate_node(o, 0, timestamp);
+    }
+};
+
 /* An occupancy map seen by the dual marching cubes: BlockMultiRes<Occupancy>::data(voxel, scale)
  * (block_impl.hpp:326-340: the init data below the finest allocated scale), get_field =
  * occupancy * weight (data.hpp:123-127), is_valid = weight != 0 (data_field_impl.hpp:12-15),
@@ -2103,6 +2536,47 @@ int so_occ_pooling_image_lidar(const float* depth, int w, int h, float* out, flo
     if (max_value)
         *max_value = P.max_value;
     return P.max_level;
+}
+
+/* MapIntegrator::integrateRayBatch for a multi-res occupancy map and a LeicaLidar
+ * (map_integrator_impl.hpp:137-176): rays[3 i] (sensor frame) with poses[16 i] (T_WS, row-major),
+ * in order; writes up to capacity updated octants (x, y, z, size) and returns their number. */
+long long so_occ_integrate_ray_batch(so_occ_map* mp, const so_leica* sensor, const float* poses, const float* rays,
+                                     long long n, int timestamp, int32_t* octants, long long capacity)
+{
+    const Leica L = make_leica(sensor);
+    std::set<OctKey> updated;
+    RayIntegrator ri(*mp, L, timestamp, &updated);
+    for (long long i = 0; i < n; ++i) {
+        ri.reset(v3(rays[3 * i], rays[3 * i + 1], rays[3 * i + 2]), tf_from16(poses + 16 * i));
+        ri.run();
+    }
+    ri.propagate_blocks();
+    ri.propagate_to_root();
+    long long k = 0;
+    for (const OctKey& key : updated) {
+        if (octants && k < capacity)
+            for (int a = 0; a < 4; ++a)
+                octants[4 * k + a] = key[(size_t) a];
+        ++k;
+    }
+    return k;
+}
+
+/* LeicaLidar::computeIntegrationScale for a block centre in the sensor frame. */
+int so_leica_integration_scale(const so_leica* sensor, const float c_S[3], float res, int last_scale, int min_scale)
+{
+    const Leica L = make_leica(sensor);
+    return leica_integration_scale(L, v3(c_S[0], c_S[1], c_S[2]), res, last_scale, min_scale, kOccMaxScale);
+}
+
+/* Block timestamps of the live blocks in allocation order (Octant::timestamp). */
+void so_occ_block_timestamps(const so_occ_map* mp, int32_t* ts)
+{
+    long long k = 0;
+    for (size_t i = 0; i < mp->octree.blocks.size(); ++i)
+        if (mp->octree.block_live[i])
+            ts[k++] = mp->octree.blocks[i].timestamp;
 }
 
 long long so_occ_num_blocks(const so_occ_map* m)

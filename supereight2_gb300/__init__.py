@@ -22,7 +22,8 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "OusterLidar",
+__all__ = ["Map", "MapIntegrator", "Tracker", "TrackerConfig", "PinholeCamera", "OusterLidar", "LeicaLidar",
+           "integrate_ray_batch",
            "OccupancyBatch", "raycast_volume",
            "render_depth", "raycast_adjoint", "track_noalloc", "bilateral_filter", "downsample_depth", "marching_cube",
            "dual_marching_cube", "save_mesh",
@@ -63,6 +64,12 @@ class _Lidar(C.Structure):
                 ("far_plane", C.c_float)]
 
 
+class _LeicaLidar(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("near_plane", C.c_float),
+                ("far_plane", C.c_float), ("elevation_resolution_deg", C.c_float),
+                ("azimuth_resolution_deg", C.c_float)]
+
+
 class _BilateralConfig(C.Structure):
     _fields_ = [("radius", C.c_int), ("sigma_space_px", C.c_float), ("sigma_range_m", C.c_float)]
 
@@ -101,6 +108,8 @@ SIGNATURES = {
     "se_gpu_map_check": (C.c_int, [_VP]),
     "se_gpu_integrate_depth": (C.c_int, [_VP, _VP, C.POINTER(_Pinhole), _F16, C.c_int, _VP]),
     "se_gpu_integrate_range": (C.c_int, [_VP, _VP, C.POINTER(_Lidar), _F16, C.c_int, _VP]),
+    "se_gpu_occ_integrate_ray_batch": (C.c_int, [_VP, C.POINTER(_LeicaLidar), _VP, _VP, C.c_int64, C.c_int32,
+                                                 _VP, C.c_int64, C.POINTER(C.c_int64), _VP]),
     "se_gpu_bilateral_filter": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.POINTER(_BilateralConfig), _VP]),
     "se_gpu_tracker_set_persistent": (C.c_int, [_VP, C.c_int]),
     "se_gpu_tracker_test_barrier_timeout": (C.c_int, [_VP, C.c_int]),
@@ -255,6 +264,21 @@ class OusterLidar:
     def _c(self) -> _Lidar:
         return _Lidar(self.width, self.height, self.elevation_min_deg, self.elevation_max_deg,
                       self.near_plane, self.far_plane)
+
+
+class LeicaLidar:
+    """se::LeicaLidar::Config: the ray-batch sensor (angular resolutions in degrees)."""
+
+    def __init__(self, width=360, height=180, near_plane=0.2, far_plane=30.0, elevation_resolution_deg=1.0,
+                 azimuth_resolution_deg=1.0):
+        self.width, self.height = int(width), int(height)
+        self.near_plane, self.far_plane = float(near_plane), float(far_plane)
+        self.elevation_resolution_deg = float(elevation_resolution_deg)
+        self.azimuth_resolution_deg = float(azimuth_resolution_deg)
+
+    def _c(self) -> _LeicaLidar:
+        return _LeicaLidar(self.width, self.height, self.near_plane, self.far_plane,
+                           self.elevation_resolution_deg, self.azimuth_resolution_deg)
 
 
 class TrackerConfig:
@@ -502,6 +526,33 @@ class MapIntegrator:
             return
         _check(L.se_gpu_integrate_depth(self.map.h, ptr, C.byref(s), tp, int(timestamp),
                                         _stream(stream)), "se_gpu_integrate_depth")
+
+
+def integrate_ray_batch(map: Map, timestamp, poses, rays, sensor: LeicaLidar, stream=None,
+                        with_octants=True):
+    """se::MapIntegrator::integrateRayBatch(timestamp, rayPoseBatch, sensor, updated_octants) for
+    an occupancy map: rays (N, 3) float32 CUDA tensor in the sensor frame, poses (N, 4, 4) float32
+    CUDA tensor (T_WS per ray). Returns the updated octants as an (K, 4) int32 CUDA tensor of
+    (x, y, z, size) in voxels (any order), or their number when with_octants is False."""
+    import torch
+    n = int(rays.shape[0]) if rays.dim() == 2 else -1
+    rp = _dptr(rays, torch.float32, (n, 3), "rays")
+    pp = _dptr(poses, torch.float32, (n, 4, 4), "poses")
+    cnt = C.c_int64()
+    s = sensor._c()
+    L = map._L
+    if not with_octants:
+        _check(L.se_gpu_occ_integrate_ray_batch(map.h, C.byref(s), pp, rp, n, int(timestamp), None, 0,
+                                                C.byref(cnt), _stream(stream)), "se_gpu_occ_integrate_ray_batch")
+        return cnt.value
+    cap = max(4096, 64 * n)
+    out = torch.empty((cap, 4), dtype=torch.int32, device=rays.device)
+    _check(L.se_gpu_occ_integrate_ray_batch(map.h, C.byref(s), pp, rp, n, int(timestamp),
+                                            C.c_void_p(out.data_ptr()), cap, C.byref(cnt), _stream(stream)),
+           "se_gpu_occ_integrate_ray_batch")
+    if cnt.value > cap:
+        raise SeGpuError("more updated octants (%d) than the output holds" % cnt.value)
+    return out[: cnt.value]
 
 
 class OccupancyBatch:

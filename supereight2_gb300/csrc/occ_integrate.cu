@@ -406,6 +406,7 @@ __device__ void occ_allocate_children(const OccDevice& m, int n)
             st.live = 1;
             m.block_state[b] = st;
             blk_mean(m, b, kOccMaxScale)[0] = init;
+            m.block_ts[b] = -1;
             child[i] = -2 - b;
         }
         else {
@@ -468,6 +469,7 @@ __device__ void occ_allocate_children_warp(const OccDevice& m, int n, int lane)
                 st.live = 1;
                 m.block_state[idx] = st;
                 blk_mean(m, idx, kOccMaxScale)[0] = init;
+                m.block_ts[idx] = -1;
                 child[i] = -2 - idx;
             }
         }

@@ -605,6 +605,7 @@ se_gpu_status occ_map_create(const se_gpu_map_config* cfg, const se_gpu_occupanc
     if ((e = cudaMalloc(&m.block_min, bc * 585 * sizeof(OccD))) != cudaSuccess) return fail(e, "cudaMalloc(blocks)");
     if ((e = cudaMalloc(&m.block_max, bc * 585 * sizeof(OccD))) != cudaSuccess) return fail(e, "cudaMalloc(blocks)");
     if ((e = cudaMalloc(&m.block_buffer, bc * 512 * sizeof(OccD))) != cudaSuccess) return fail(e, "cudaMalloc(blocks)");
+    if ((e = cudaMalloc(&m.block_ts, bc * sizeof(int))) != cudaSuccess) return fail(e, "cudaMalloc(blocks)");
     if ((e = cudaMalloc(&m.aabb, 8 * sizeof(int))) != cudaSuccess) return fail(e, "cudaMalloc(aabb)");
     if ((e = cudaMalloc(&m.counters, kOccCounters * sizeof(int))) != cudaSuccess) return fail(e, "cudaMalloc(counters)");
     {
@@ -650,9 +651,11 @@ void occ_map_destroy(se_gpu_occ_map* om)
     cudaFree(m.block_min);
     cudaFree(m.block_max);
     cudaFree(m.block_buffer);
+    cudaFree(m.block_ts);
     cudaFree(m.aabb);
     cudaFree(m.counters);
     occ_scratch_free(om);
+    ri_scratch_free(om->ri);
     delete om;
 }
 

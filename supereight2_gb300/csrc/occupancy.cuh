@@ -61,6 +61,7 @@ struct OccDevice {
     OccD* block_min;       // 585 per block
     OccD* block_max;       // 585 per block
     OccD* block_buffer;    // 512 per block
+    int* block_ts;         // Octant::timestamp of blocks (kept by the ray integrator)
     // map-wide
     int* aabb;             // min xyz, max xyz; aabb[6] = empty flag
     int* counters;         // see kOcc* below
@@ -281,7 +282,13 @@ __device__ __forceinline__ int occ_voxel_idx(int ox, int oy, int oz, int s)
 
 } // namespace se_gpu
 
+namespace se_gpu {
+struct RiScratch;
+void ri_scratch_free(RiScratch* s);
+} // namespace se_gpu
+
 struct se_gpu_occ_map {
     se_gpu::OccDevice dev;
     se_gpu::OccScratch scratch;
+    se_gpu::RiScratch* ri = nullptr; // ray-batch integration scratch, made on first use
 };

@@ -417,3 +417,21 @@ def lidar_dataset(n_maps: int, n_frames: int, seed=1004, device="cpu", spec: Lid
     ranges = [[render_range(scene, spec, T, seed * 7919 + 1000 * k + i, keep=keep[k], device=device)
                for i, T in enumerate(poses[k])] for k in range(n_maps)]
     return spec, scene, poses, ranges, keep
+
+
+def wall_rays(d=10.0, lo=-15.0, res=0.1, n=300) -> np.ndarray:
+    """Ray batch of a LeicaLidar facing a wall d metres away along x: n x n rays over [lo, lo + n
+    res) degrees of elevation and azimuth (the batch of the reference's RayIntegrator.Propagation
+    test, test/integrator/ray_integrator_unittest.cpp, angles accumulated in float as there)."""
+    deg = np.float32(np.pi / 180.0)
+    rays = []
+    el = np.float32(lo)
+    for _ in range(n):
+        z = np.float32(d * np.tan(np.float32(el * deg)))
+        az = np.float32(lo)
+        for _ in range(n):
+            y = np.float32(d * np.tan(np.float32(az * deg)))
+            rays.append((d, y, z))
+            az = np.float32(az + np.float32(res))
+        el = np.float32(el + np.float32(res))
+    return np.array(rays, np.float32)
