@@ -378,14 +378,15 @@ __device__ __forceinline__ bool ri_aborted(const RiArgs& A)
     return *((volatile int*) &A.ctl->abort) != 0;
 }
 
-// Waits (lane 0, bounded) until *p == want; every lane then reads it with acquire semantics.
+// Waits (lane 0, bounded) until the ticket *p reaches want; every lane then reads it with
+// acquire semantics. A ray far back in a block's queue polls rarely, the next in line often.
 __device__ bool ri_wait_eq(const RiArgs& A, const int* p, int want, int lane)
 {
     int ok = 1;
     if (lane == 0) {
         const unsigned long long t0 = globaltimer();
-        unsigned ns = 32;
-        while (ld_acquire(p) != want) {
+        int v = ld_acquire(p);
+        while (v != want) {
             if (ri_aborted(A)) {
                 ok = 0;
                 break;
@@ -395,8 +396,9 @@ __device__ bool ri_wait_eq(const RiArgs& A, const int* p, int want, int lane)
                 ok = 0;
                 break;
             }
-            __nanosleep(ns);
-            ns = ns < 1024 ? 2 * ns : ns;
+            const int gap = want - v;
+            __nanosleep(gap <= 1 ? 20u : (unsigned) min(gap, 512) * 128u);
+            v = ld_acquire(p);
         }
     }
     ok = __shfl_sync(kFull, ok, 0);
@@ -556,6 +558,7 @@ struct RiBlock {
     int ts;
     OccD init;
     int cx, cy, cz;
+    int marked; // in this batch's updated-block list
 };
 
 __device__ void ri_load_block(const RiArgs& A, int b, RiBlock& B)
@@ -570,6 +573,7 @@ __device__ void ri_load_block(const RiArgs& A, int b, RiBlock& B)
     B.cx = __ldcg(&A.m.block_coord[3 * b]);
     B.cy = __ldcg(&A.m.block_coord[3 * b + 1]);
     B.cz = __ldcg(&A.m.block_coord[3 * b + 2]);
+    B.marked = __ldcg(&A.block_mark[b]) == A.stamp;
 }
 
 __device__ void ri_store_scales(const RiArgs& A, const RiBlock& B, int lane)
@@ -845,8 +849,101 @@ __device__ bool ri_pass(const RiArgs& A, long long e, int lane)
     return true;
 }
 
+// updated_blocks_set_ / updated_blocks_vector_: the block joins this batch's list once.
+__device__ __forceinline__ void ri_mark(const RiArgs& A, RiBlock& B, int lane)
+{
+    if (B.marked)
+        return;
+    B.marked = 1;
+    if (lane == 0) {
+        A.block_mark[B.b] = A.stamp;
+        const int k = atomicAdd(&A.ctl->n_updated, 1);
+        if (k < A.updated_cap)
+            A.updated[k] = B.b;
+        else
+            ri_abort(A, kRiErrList);
+    }
+    __syncwarp();
+}
+
+// The samples that follow in a held, already integrated block, one per lane: lane k takes the
+// sample k steps ahead (its position accumulated step by step, as the serial loop does). The run
+// ends before the first sample that leaves the block, the map or the update distance, or whose
+// scale would change the block (a finer integration scale); a sample whose scale changes the step
+// ends it after itself. The updates are applied in sample order per voxel (the lowest lane of
+// each voxel's group applies its group's updates in turn), so the result is the serial one.
+// Returns the samples processed; r, the last voxel and the computed scale advance past them.
+__device__ int ri_run(const RiArgs& A, const RiRay& R, const RiBlock& B, F3& r, int& lx, int& ly, int& lz,
+                      int& computed, float* s_rd, int lane)
+{
+    const OccDevice& m = A.m;
+    const float st = (float) (0.5 * (double) m.res * (double) (1 << computed));
+    const float sx = st * R.dir.x, sy = st * R.dir.y, sz = st * R.dir.z;
+    F3 q = r;
+    for (int k = 0; k < lane; ++k)
+        q = f3(q.x + sx, q.y + sy, q.z + sz);
+    const float rn = norm(q);
+    const F3 p_M = apply(m.T_MW, apply(R.T_WS, q));
+    const bool inside = p_M.x >= 0.0f && p_M.x < m.dim && p_M.y >= 0.0f && p_M.y < m.dim && p_M.z >= 0.0f
+        && p_M.z < m.dim;
+    const int vx = inside ? (int) (p_M.x / m.res) : -1, vy = inside ? (int) (p_M.y / m.res) : -1,
+              vz = inside ? (int) (p_M.z / m.res) : -1;
+    const bool in_block = inside && (vx & ~7) == B.cx && (vy & ~7) == B.cy && (vz & ~7) == B.cz;
+    // the block's scale decision (the same block centre and state for every lane)
+    const F3 c_M = f3(((float) B.cx + 4.0f) * m.res, ((float) B.cy + 4.0f) * m.res, ((float) B.cz + 4.0f) * m.res);
+    const int s0 = leica_scale(A, apply(R.T_SW, apply(m.T_WM, c_M)), B.current_scale, B.min_scale);
+    const int fs = m.cfg.fs_integr_scale;
+    const bool free_space = rn - R.ray_dist < -R.three_sigma;
+    const int desired = (free_space && s0 < fs) ? (fs < B.current_scale ? fs : B.current_scale) : s0;
+    // the previous sample's voxel, for the serial loop's repeat test
+    int px = __shfl_up_sync(kFull, vx, 1), py = __shfl_up_sync(kFull, vy, 1), pz = __shfl_up_sync(kFull, vz, 1);
+    if (lane == 0) {
+        px = lx;
+        py = ly;
+        pz = lz;
+    }
+    const bool dup = vx == px && vy == py && vz == pz;
+    const bool stop = !(rn < R.max_dist) || !in_block || !((double) rn >= 1e-08)
+        || (!dup && desired < B.current_scale);
+    const unsigned stops = __ballot_sync(kFull, stop);
+    int len = stops ? __ffs(stops) - 1 : 32;
+    const unsigned changes = __ballot_sync(kFull, !dup && desired != computed) & ((len >= 32) ? kFull : ((1u << len) - 1u));
+    if (changes)
+        len = __ffs(changes); // include the sample whose scale changes the step
+    if (len == 0)
+        return 0;
+    const bool upd = lane < len && !dup;
+    const int s = B.current_scale, n = 8 >> s;
+    const int idx = upd ? ((vx - B.cx) >> s) + n * ((vy - B.cy) >> s) + n * n * ((vz - B.cz) >> s) : -1;
+    s_rd[lane] = rn - R.ray_dist;
+    __syncwarp();
+    const unsigned upd_mask = __ballot_sync(kFull, upd);
+    const unsigned group = __match_any_sync(kFull, idx) & upd_mask;
+    if (upd && (group & ((1u << lane) - 1u)) == 0u) {
+        OccD* p = blk_mean(m, B.b, s) + idx;
+        OccD d = ldcg_occ(p);
+        for (unsigned g = group; g; g &= g - 1u)
+            ri_update_voxel(d, s_rd[__ffs(g) - 1], R.tau, R.three_sigma, m.cfg);
+        *p = d;
+    }
+    __syncwarp();
+    // the state after the run's last sample
+    const int last = len - 1;
+    const unsigned upd_in = upd_mask & ((len >= 32) ? kFull : ((1u << len) - 1u));
+    if (upd_in)
+        computed = __shfl_sync(kFull, desired, 31 - __clz(upd_in));
+    lx = __shfl_sync(kFull, vx, last);
+    ly = __shfl_sync(kFull, vy, last);
+    lz = __shfl_sync(kFull, vz, last);
+    const float qx = __shfl_sync(kFull, q.x, last), qy = __shfl_sync(kFull, q.y, last),
+                qz = __shfl_sync(kFull, q.z, last);
+    const float st2 = (float) (0.5 * (double) m.res * (double) (1 << computed));
+    r = f3(qx + st2 * R.dir.x, qy + st2 * R.dir.y, qz + st2 * R.dir.z);
+    return len;
+}
+
 // RayIntegrator::operator()() (ray_integrator_impl.hpp:82-129) for one ray, by one warp.
-__device__ void ri_ray(const RiArgs& A, int ray, int lane)
+__device__ void ri_ray(const RiArgs& A, int ray, int lane, float* s_rd)
 {
     const OccDevice& m = A.m;
     const RiRay& R = A.R[ray];
@@ -882,9 +979,6 @@ __device__ void ri_ray(const RiArgs& A, int ray, int lane)
                 break;
             const int vx = (int) (p_M.x / m.res), vy = (int) (p_M.y / m.res), vz = (int) (p_M.z / m.res);
             if (vx != lx || vy != ly || vz != lz) {
-                lx = vx;
-                ly = vy;
-                lz = vz;
                 const int bx = vx & ~7, by = vy & ~7, bz = vz & ~7;
                 if (cur_e < 0 || A.entries[cur_e].bx != bx || A.entries[cur_e].by != by || A.entries[cur_e].bz != bz) {
                     long long e = -1;
@@ -899,6 +993,10 @@ __device__ void ri_ray(const RiArgs& A, int ray, int lane)
                         ri_abort(A, kRiErrEntry);
                         return;
                     }
+                    // the descent (and any allocation) does not depend on the batch order
+                    const int b = ri_block(A, vx, vy, vz, lane);
+                    if (b < 0)
+                        return;
                     if (!A.entries[e].held) {
                         if (!ri_wait_eq(A, &A.done[A.entries[e].slot], A.entries[e].rank, lane))
                             return;
@@ -908,11 +1006,22 @@ __device__ void ri_ray(const RiArgs& A, int ray, int lane)
                         __syncwarp();
                     }
                     cur_e = e;
-                    const int b = ri_block(A, vx, vy, vz, lane);
-                    if (b < 0)
-                        return;
                     ri_load_block(A, b, B);
                 }
+                // a block an earlier sample of this batch integrated: this sample and the ones
+                // after it in the block as one run
+                if (B.min_scale != -1 && B.ts == A.timestamp) {
+                    int k = ri_run(A, R, B, r, lx, ly, lz, computed, s_rd, lane);
+                    if (k > 0) {
+                        ri_mark(A, B, lane);
+                        while (k == 32)
+                            k = ri_run(A, R, B, r, lx, ly, lz, computed, s_rd, lane);
+                        continue;
+                    }
+                }
+                lx = vx;
+                ly = vy;
+                lz = vz;
                 // operator()(ray_sample, voxel, state, octant) at block level (:174-214)
                 const int last_scale = B.min_scale == -1 ? 0 : B.current_scale;
                 const F3 c_M = f3(((float) B.cx + 4.0f) * m.res, ((float) B.cy + 4.0f) * m.res, ((float) B.cz + 4.0f) * m.res);
@@ -923,18 +1032,14 @@ __device__ void ri_ray(const RiArgs& A, int ray, int lane)
                     scale = B.min_scale == -1 ? fs : (fs < B.current_scale ? fs : B.current_scale);
                 ri_update_block(A, R, B, vx, vy, vz, scale, rn, lane);
                 computed = scale;
-                if (lane == 0 && __ldcg(&A.block_mark[B.b]) != A.stamp) {
-                    A.block_mark[B.b] = A.stamp;
-                    const int k = atomicAdd(&A.ctl->n_updated, 1);
-                    if (k < A.updated_cap)
-                        A.updated[k] = B.b;
-                    else
-                        ri_abort(A, kRiErrList);
-                }
-                __syncwarp();
+                ri_mark(A, B, lane);
             }
             const float step = (float) (0.5 * (double) m.res * (double) (1 << computed));
             r = f3(r.x + step * R.dir.x, r.y + step * R.dir.y, r.z + step * R.dir.z);
+            // the rest of the samples in this block, one per lane
+            if (B.b >= 0 && B.min_scale != -1 && B.ts == A.timestamp)
+                while (ri_run(A, R, B, r, lx, ly, lz, computed, s_rd, lane) == 32) {
+                }
         }
     }
     for (; rel < e1; ++rel)
@@ -944,6 +1049,7 @@ __device__ void ri_ray(const RiArgs& A, int ray, int lane)
 
 __global__ void __launch_bounds__(256) ri_rays_kernel(RiArgs A)
 {
+    __shared__ float s_rd[8][32];
     const int lane = threadIdx.x & 31;
     for (;;) {
         int ray = 0;
@@ -952,7 +1058,7 @@ __global__ void __launch_bounds__(256) ri_rays_kernel(RiArgs A)
         ray = __shfl_sync(kFull, ray, 0);
         if (ray >= A.n)
             return;
-        ri_ray(A, ray, lane);
+        ri_ray(A, ray, lane, s_rd[threadIdx.x >> 5]);
     }
 }
 
