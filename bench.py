@@ -48,7 +48,7 @@ def _peaks():
 
 # Bench kernel names -> the kernel names of the committed DRAM-traffic capture of this workload
 _TRAFFIC_NAMES = {"icp_iter": "icp_persistent_kernel", "update": "update_kernel<0>", "raycast": "raycast_kernel<0, 0>",
-                  "carve": "carve_kernel", "frustum": "frustum_kernel"}
+                  "carve": "carve_kernel", "frustum": "frustum_kernel", "mr_update": "mr_update_kernel<0>"}
 
 
 def _traffic(kernel):
@@ -297,6 +297,11 @@ def run_ours(args, ws, rank, local):
         mr[st] = {"value": K / (v["dev_ms"] * 1e-3), "ms_per_step": v["dev_ms"] / K}
         del v["map"], v["tracker"], v["fp"]
 
+    # the multi-res update's own time per frame (blocking calls, per-kernel events) and the
+    # integration scales of the blocks it updates, for its roofline
+    mr_roof = _mr_update_roofline(se, torch, dev, sensor, poses, depth_dev, first, K, args.warmup,
+                                  args.max_blocks, flush, W, H)
+
     # eight LiDAR occupancy maps in one batch
     lidar = _lidar_bench(se, torch, dev, args.lidar_steps, args.warmup, flush)
     lidar_data = lidar.pop("_data")
@@ -344,6 +349,11 @@ def run_ours(args, ws, rank, local):
                                 "achieved_GBps": float(np.mean(ub)) / (upd_ms * 1e-3) / 1e9 if upd_ms else None,
                                 "frac": float(np.mean(ub)) / (upd_ms * 1e-3) / 1e9 / hbm_peak if upd_ms else None,
                                 "traffic": _traffic("update")}}
+    if mr_roof:
+        mr_roof["achieved_GBps"] = mr_roof["algorithmic_bytes_per_launch"] / (mr_roof["avg_launch_us"] * 1e-6) / 1e9
+        mr_roof["frac"] = mr_roof["achieved_GBps"] / hbm_peak
+        mr_roof["traffic"] = _traffic("mr_update")
+        roofline["multires_update"] = mr_roof
     icp_ms = kms.get("icp_iter", 0.0) / max(kl.get("icp_iter", 1), 1)
     if icp_ms:
         # 48 B per pixel of every iteration a tracked frame ran (its working set stays in L2)
@@ -419,6 +429,40 @@ def run_ours(args, ws, rank, local):
         if args.precision_frames > 0:
             out["precision_vs_f64"] = _precision_report(se, torch, torch.device("cuda", local),
                                                         args.precision_frames, args.max_blocks)
+    return out
+
+
+def _mr_update_roofline(se, torch, dev, sensor, poses, depth_dev, first, K, warmup, max_blocks, flush, W, H):
+    """Algorithmic bytes of the multi-res TSDF update (both launches: scale selection with down-
+    propagation, then the update with up-propagation) against its time in the blocking FP32 path.
+    Per listed block at integration scale s: its (8 >> s)^3 entries read and written (16 B each,
+    data and past data), and every coarser entry written by the up-propagation and read back;
+    a new block also writes its 585 default entries; plus the depth image. The scale mix is the
+    one of the blocks the last timed frame updated; the block counts are the timed frames' mean."""
+    v = _variant(se, torch, dev, sensor, poses, depth_dev, first, K, warmup, "plain", "f32", max_blocks, flush,
+                 profile=True, res_type="multi")
+    kms, kl = v["kernel_ms"], v["kernel_launches"]
+    if not kms.get("update"):
+        return None
+    m = v["map"]
+    keys, _, _, _, ts = m.download_blocks(voxels=False)
+    mk, _, _, _, _, _, sc = m.download_multires()
+    scale_of = dict(zip(mk.tolist(), sc[:, 0].tolist()))
+    last = int(ts.max())
+    cur = [scale_of[k] for k, t in zip(keys.tolist(), ts.tolist()) if t == last]
+    entries = {0: 512, 1: 64, 2: 8, 3: 1}
+    coarser = {0: 73, 1: 9, 2: 1, 3: 0}
+    E = 16
+    per_block = float(np.mean([2 * E * (entries[s] + coarser[s]) for s in cur])) if cur else 0.0
+    n_list = float(np.mean([st["n_listed_blocks"] for st in v["stats"]]))
+    n_new = float(np.mean([st["n_new_blocks"] for st in v["stats"]]))
+    algo = n_list * per_block + n_new * 585 * E + W * H * 4
+    hist = {int(s): int(c) for s, c in zip(*np.unique(np.asarray(cur), return_counts=True))} if cur else {}
+    out = {"kernel": "mr_scale_down_kernel + mr_update_kernel (FP32)",
+           "avg_launch_us": kms["update"] / kl["update"] * 1e3, "algorithmic_bytes_per_launch": algo,
+           "listed_blocks": n_list, "new_blocks": n_new, "scale_histogram_last_frame": hist,
+           "bytes_per_listed_block": per_block}
+    del v["map"], v["tracker"], v["fp"]
     return out
 
 

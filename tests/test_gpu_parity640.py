@@ -12,8 +12,9 @@ checked on its own:
     icp.cpp:45-246), acceptance equal, inlier counts within 1e-4, iterations per level within one
     (where the convergence test |x| < 1e-5 falls the other way, against the oracle run for the
     GPU's iteration counts); on a frame where the ICP sits at its convergence floor (the two stop
-    a level one iteration apart, or the oracle's own results from start poses one float step away
-    spread by more than half the bar) within two threshold-sized updates;
+    a level one iteration apart, or the oracle's own results from start poses one float step away,
+    or with its sums in other orders, spread by more than half the bar) within two threshold-sized
+    updates and twice that spread;
   - the integration counters are equal each frame; after the last frame the allocated block-key
     set and integer weights are bit-exact and the TSDF values within 1e-5 * truncation;
   - the raycast depth is within 1e-4 m on >= 99.9 % of the pixels both hit.
@@ -73,7 +74,8 @@ def run640(oracle, gpu):
             rec["filter"].append(np.array_equal(fg_h, fo))
             acc_o, T_new, st_o = oracle.track(os_, cfg_o, fo, T_o, op, on)
             # the oracle's own sensitivity: its results from start poses one float step away in
-            # each translation component
+            # each translation component, and with its ICP sums in other orders (other thread
+            # counts: the GPU's reductions sum in yet another order)
             spread_t = spread_r = 0.0
             for a in range(3):
                 for direction in (np.inf, -np.inf):
@@ -82,6 +84,13 @@ def run640(oracle, gpu):
                     _, T_q, _ = oracle.track(os_, cfg_o, fo, T_p, op, on)
                     dt_q, dr_q = _pose_diff(T_q, T_new)
                     spread_t, spread_r = max(spread_t, dt_q), max(spread_r, dr_q)
+            n_threads = oracle.num_threads()
+            for nt in (1, 2, 3, 4, 6, 12, 16):
+                oracle.set_num_threads(nt)
+                _, T_q, _ = oracle.track(os_, cfg_o, fo, T_o, op, on)
+                dt_q, dr_q = _pose_diff(T_q, T_new)
+                spread_t, spread_r = max(spread_t, dt_q), max(spread_r, dr_q)
+            oracle.set_num_threads(n_threads)
             # the GPU tracks from the same start pose against the oracle's reference images
             pts.copy_(torch.from_numpy(op))
             nrm.copy_(torch.from_numpy(on))
@@ -147,7 +156,8 @@ def test_tracked_pose_per_frame(run640):
     up to (1 + |t|) 1e-5 m (omega rotates about the world origin, |t| ~ 1.5 m here). A frame is at
     this floor when the GPU and the oracle stop a level one iteration apart (the test |x| < 1e-5
     falling either side between FP64 and FP32 solves), or when the oracle's own results from
-    start poses one float step away spread by more than half the bar; there the GPU (exact
+    start poses one float step away (or with its sums in other orders) spread by more than half
+    the bar; there the GPU (exact
     reductions, FP64 solve and pose update) must lie within two such updates (and twice that
     spread) of the oracle; every other frame is held to the bar itself."""
     assert len(run640["track"]) == N_FRAMES - 1
