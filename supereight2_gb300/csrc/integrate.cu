@@ -279,15 +279,23 @@ se_gpu_status enqueue_integrate(se_gpu_map* map, const float* depth_dev, const s
         launch_chained(integrate_prep_kernel, 1, 1, stream, m, map->config.truncation_boundary_factor, s,
                        T_WC_host16 ? nullptr : pose12_dev, hp, map->timestamp_dev, map->iparams);
     }
+    // the frustum test of the old blocks on the side stream, the carver on the caller's: the
+    // carver only adds blocks past the old-block snapshot, and the frustum test only reads those
+    // before it
+    SE_CUDA_TRY(cudaEventRecord(map->fork_ev, stream));
+    SE_CUDA_TRY(cudaStreamWaitEvent(map->side, map->fork_ev, 0));
+    {
+        ProfScope ps(kProfFrustum, map->side);
+        frustum_kernel<<<sms * 4, 256, 0, map->side>>>(m, s, map->iparams);
+        SE_CUDA_TRY(cudaGetLastError());
+    }
     {
         ProfScope ps(kProfCarve, stream);
         dim3 cgrid((s.w + 31) / 32, (s.h + 7) / 8);
         launch_chained(carve_kernel, cgrid, 256, stream, m, s, depth_dev, map->iparams);
     }
-    {
-        ProfScope ps(kProfFrustum, stream);
-        launch_chained(frustum_kernel, sms * 4, 256, stream, m, s, map->iparams);
-    }
+    SE_CUDA_TRY(cudaEventRecord(map->join_ev, map->side));
+    SE_CUDA_TRY(cudaStreamWaitEvent(stream, map->join_ev, 0));
     if (m.res_type == SE_GPU_RES_MULTI) {
         if (map->tune)
             SE_CUDA_TRY(cudaEventRecord(map->tune->ev[0], stream));

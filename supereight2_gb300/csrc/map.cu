@@ -232,6 +232,9 @@ se_gpu_status se_gpu_map_create(const se_gpu_map_config* cfg, se_gpu_map** out)
         if ((e = cudaMalloc(&m.occ[L], words * 4)) != cudaSuccess) return fail(e, "cudaMalloc(occupancy)");
         if ((e = cudaMemset(m.occ[L], 0, words * 4)) != cudaSuccess) return fail(e, "cudaMemset(occupancy)");
     }
+    if ((e = cudaStreamCreateWithFlags(&map->side, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "cudaStreamCreate");
+    if ((e = cudaEventCreateWithFlags(&map->fork_ev, cudaEventDisableTiming)) != cudaSuccess) return fail(e, "cudaEventCreate");
+    if ((e = cudaEventCreateWithFlags(&map->join_ev, cudaEventDisableTiming)) != cudaSuccess) return fail(e, "cudaEventCreate");
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e, "cudaDeviceSynchronize");
     *out = map;
     return SE_GPU_OK;
@@ -321,6 +324,12 @@ se_gpu_status se_gpu_map_destroy(se_gpu_map* map)
     cudaFree(map->timestamp_dev);
     for (int L = 0; L < 11; ++L)
         cudaFree(m.occ[L]);
+    if (map->side)
+        cudaStreamDestroy(map->side);
+    if (map->fork_ev)
+        cudaEventDestroy(map->fork_ev);
+    if (map->join_ev)
+        cudaEventDestroy(map->join_ev);
     delete map;
     return SE_GPU_OK;
 }

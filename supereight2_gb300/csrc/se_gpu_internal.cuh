@@ -494,6 +494,10 @@ struct se_gpu_map {
     int* timestamp_dev;               // device frame counter used by captured pipelines
     se_gpu::FrameTiles tiles;         // launch geometry of the update and raycast kernels
     se_gpu::FrameTuneEvents* tune;    // non-null while the frame autotuner times a run
+    // the frustum test runs beside the carver (neither reads what the other writes): a second
+    // stream forked from and joined back into the caller's stream around them
+    cudaStream_t side;
+    cudaEvent_t fork_ev, join_ev;
 };
 
 namespace se_gpu {
