@@ -766,6 +766,14 @@ def _lidar_bench(se, torch, dev, K, warmup, flush):
         m.check()
     blocks = [int(m.occupancy_stats()[0]) for m in maps]
     del batch, maps
+    # batched, one persistent cooperative launch per step, in a captured graph, autotuned
+    maps = _lidar_maps(se, LIDAR_MAPS)
+    batch = se.OccupancyBatch(maps, sensor, graph=True, autotune=True, persistent=True)
+    ms_persist = timed(lambda i: batch.integrate(imgs[i], Ts[i], i))
+    ptiles, _ = batch.tiles()
+    for m in maps:
+        m.check()
+    del batch, maps
     # batched, no graph, default geometry
     maps = _lidar_maps(se, LIDAR_MAPS)
     batch = se.OccupancyBatch(maps, sensor, graph=False)
@@ -815,6 +823,8 @@ def _lidar_bench(se, torch, dev, K, warmup, flush):
             "batched_graph_autotuned": {"value": scans / (ms_graph * 1e-3), "ms_per_step": ms_graph / K,
                                         "tiles_ctas_per_sm": {"carve": tiles[0], "lists": tiles[1],
                                                               "blocks": tiles[2]}},
+            "batched_persistent_graph_autotuned": {"value": scans / (ms_persist * 1e-3), "ms_per_step": ms_persist / K,
+                                                   "launches_per_step": 1, "ctas_per_sm": ptiles[0]},
             "batched_no_graph": {"value": scans / (ms_batch * 1e-3), "ms_per_step": ms_batch / K},
             "one_map_per_call": {"value": scans / (ms_single * 1e-3), "ms_per_step": ms_single / K},
         },

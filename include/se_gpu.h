@@ -236,6 +236,11 @@ typedef struct se_gpu_occ_batch se_gpu_occ_batch;
  * do not depend on the geometry. */
 #define SE_GPU_OCC_BATCH_GRAPH 1
 #define SE_GPU_OCC_BATCH_AUTOTUNE 2
+/* SE_GPU_OCC_BATCH_PERSISTENT: each call runs as one cooperative launch, every stage a
+ * grid-stride loop over the whole batch separated by grid barriers (a barrier that waits past
+ * 1 s abandons the frame and se_gpu_map_check reports it); with AUTOTUNE the tuned geometry is
+ * its CTAs per SM (1 or 2; tiles[0]). Results equal the multi-launch path's. */
+#define SE_GPU_OCC_BATCH_PERSISTENT 4
 SE_GPU_API se_gpu_status se_gpu_occ_batch_create(se_gpu_map* const* maps, int n,
                                                  const se_gpu_pinhole* pinhole,
                                                  const se_gpu_lidar* lidar, int flags,

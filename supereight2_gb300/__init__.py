@@ -561,9 +561,11 @@ class OccupancyBatch:
     launches of a call into a CUDA graph on the first call and replays it afterwards;
     autotune=True runs the default geometry for the first 4 calls, then spends 12 calls timing
     4 launch geometries three times each and keeps per stage the one with the least time in its
-    best round (the graph is captured after that)."""
+    best round (the graph is captured after that). persistent=True runs each call as one
+    cooperative launch (every stage a grid-stride loop, grid barriers between them); its tuned
+    geometry is the CTAs per SM of that launch."""
 
-    def __init__(self, maps, sensor, graph=True, autotune=False):
+    def __init__(self, maps, sensor, graph=True, autotune=False, persistent=False):
         self.maps = list(maps)
         self.sensor = sensor
         self._L = library()
@@ -572,7 +574,7 @@ class OccupancyBatch:
         pin = C.byref(s) if isinstance(sensor, PinholeCamera) else None
         lid = C.byref(s) if isinstance(sensor, OusterLidar) else None
         h = _VP()
-        flags = (1 if graph else 0) | (2 if autotune else 0)
+        flags = (1 if graph else 0) | (2 if autotune else 0) | (4 if persistent else 0)
         _check(self._L.se_gpu_occ_batch_create(arr, len(self.maps), pin, lid, flags, C.byref(h)),
                "se_gpu_occ_batch_create")
         self.h = h

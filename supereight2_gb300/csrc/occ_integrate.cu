@@ -81,10 +81,8 @@ __device__ __forceinline__ int push(int* list, int* count, int cap, int v, int* 
 
 // -------------------------------------------------------------------------- begin --
 
-__device__ __forceinline__ void occ_begin(const OccLaunch* __restrict__ Lp, const OccStep& step)
+__device__ __forceinline__ void occ_begin(const OccLaunch& L, const OccStep& step, int j)
 {
-    const OccLaunch& L = *Lp;
-    const int j = blockIdx.x;
     if (j >= L.n)
         return;
     const OccJob& J = L.job[j];
@@ -106,25 +104,19 @@ __device__ __forceinline__ void occ_begin(const OccLaunch* __restrict__ Lp, cons
 // replays unchanged).
 __global__ void occ_begin_kernel(const OccLaunch* __restrict__ Lp, const __grid_constant__ OccStep step)
 {
-    occ_begin(Lp, step);
+    occ_begin(*Lp, step, blockIdx.x);
 }
 __global__ void occ_begin_dev_kernel(const OccLaunch* __restrict__ Lp, const OccStep* __restrict__ step)
 {
-    occ_begin(Lp, *step);
+    occ_begin(*Lp, *step, blockIdx.x);
 }
 
 // ------------------------------------------------------------------ per-pixel inputs --
 
 // uncert::depth_sigma with the linear model, and level 0 of both pooling images
 // (Pixel::knownPixel / unknownPixel: min = FLT_MAX, max = FLT_MIN, the smallest normal float)
-__global__ void occ_pixels_kernel(const OccLaunch* __restrict__ Lp)
+__device__ __forceinline__ void occ_pixel(const OccLaunch& L, int j, int i)
 {
-    const OccLaunch& L = *Lp;
-    const int npx = L.sensor.w * L.sensor.h;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y;
-    if (i >= npx || j >= L.n)
-        return;
     const OccJob& J = L.job[j];
     const float d = J.dyn->depth[i];
     float sg;
@@ -140,20 +132,26 @@ __global__ void occ_pixels_kernel(const OccLaunch* __restrict__ Lp)
     J.pool_sigma[i] = sg <= 0.0f ? make_float4(FLT_MAX, FLT_MIN, 0.0f, 2.0f) : make_float4(sg, sg, 0.0f, 0.0f);
 }
 
+__global__ void occ_pixels_kernel(const OccLaunch* __restrict__ Lp)
+{
+    const OccLaunch& L = *Lp;
+    const int npx = L.sensor.w * L.sensor.h;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= npx || j >= L.n)
+        return;
+    occ_pixel(L, j, i);
+}
+
 // Level 1 (3x3 windows, dense_pooling_image_impl.hpp:92-165 / 423-478) or level l >= 2 (the four
 // overlapping windows of level l - 1, :167-213 / 480-565) of both images of every map; the LiDAR
 // image wraps around in u.
-__global__ void occ_pool_level_kernel(const OccLaunch* __restrict__ Lp, int level)
+__device__ __forceinline__ void occ_pool_pixel(const OccLaunch& L, int level, int j, int which, int i)
 {
-    const OccLaunch& L = *Lp;
     const int w = L.sensor.w, h = L.sensor.h, npx = w * h;
     const bool wrap = L.sensor.lidar != 0;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y >> 1;
-    if (i >= npx || j >= L.n)
-        return;
     const OccJob& J = L.job[j];
-    float4* base = (blockIdx.y & 1) ? J.pool_sigma : J.pool_depth;
+    float4* base = which ? J.pool_sigma : J.pool_depth;
     const float4* P = base + (size_t) (level - 1) * npx;
     const int x = i % w, y = i / w;
     float4 p = make_float4(FLT_MAX, FLT_MIN, 1.0f, 0.0f); // crossingKnownPixel
@@ -214,6 +212,17 @@ __global__ void occ_pool_level_kernel(const OccLaunch* __restrict__ Lp, int leve
             p.z = 0.0f;
     }
     base[(size_t) level * npx + i] = p;
+}
+
+__global__ void occ_pool_level_kernel(const OccLaunch* __restrict__ Lp, int level)
+{
+    const OccLaunch& L = *Lp;
+    const int npx = L.sensor.w * L.sensor.h;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y >> 1;
+    if (i >= npx || j >= L.n)
+        return;
+    occ_pool_pixel(L, level, j, blockIdx.y & 1, i);
 }
 
 struct PoolQuery {
@@ -498,13 +507,8 @@ __device__ void occ_allocate_children_warp(const OccDevice& m, int n, int lane)
 // DensePoolingImage::maxValue over the coarsest level (the lanes share the visited pixels) and
 // VolumeCarver's max depth (volume_carver_impl.hpp:28-38), then the root's children as the first
 // frontier; one warp per map.
-__global__ void occ_root_kernel(const OccLaunch* __restrict__ Lp)
+__device__ void occ_root(const OccLaunch& L, int j, int lane)
 {
-    const OccLaunch& L = *Lp;
-    const int j = blockIdx.x;
-    const int lane = threadIdx.x & 31;
-    if (j >= L.n || threadIdx.x >= 32)
-        return;
     const OccJob& J = L.job[j];
     const int w = L.sensor.w, h = L.sensor.h;
     const int max_level = L.sensor.levels - 1;
@@ -536,6 +540,14 @@ __global__ void occ_root_kernel(const OccLaunch* __restrict__ Lp)
         if (m.node_child[i] != -1)
             J.frontier[1][n++] = m.node_child[i]; // depth 1 reads frontier[1]
     m.counters[kOccFrontierN + 1] = n;
+}
+
+__global__ void occ_root_kernel(const OccLaunch* __restrict__ Lp)
+{
+    const OccLaunch& L = *Lp;
+    if (blockIdx.x >= L.n || threadIdx.x >= 32)
+        return;
+    occ_root(L, blockIdx.x, threadIdx.x & 31);
 }
 
 // cameraInNode with pointToVoxel<Safe::On> (volume_carver_impl.hpp:83-98)
@@ -732,16 +744,15 @@ __device__ bool carve_lidar(const OccLaunch& L, const OccJob& J, const OccDyn& D
 
 // One depth of the VolumeCarver over every map's frontier at that depth, one warp per octant;
 // lane 0 lists the octant or allocates and queues its children.
-__global__ void __launch_bounds__(128) occ_carve_kernel(const OccLaunch* __restrict__ Lp, int depth)
+__device__ void occ_carve_stage(const OccLaunch& L, int depth, int bid, int nbid)
 {
-    const OccLaunch& L = *Lp;
     __shared__ int pre[kOccMaxBatch + 1];
     const int total = batch_prefix(L, pre, [depth](const OccJob& J) {
         return clamp_count(J.m.counters[kOccFrontierN + depth], J.m.node_capacity + J.m.block_capacity);
     });
     const int lane = threadIdx.x & 31;
-    const int n_warps = (gridDim.x * blockDim.x) >> 5;
-    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < total; idx += n_warps) {
+    const int n_warps = (nbid * blockDim.x) >> 5;
+    for (int idx = (bid * blockDim.x + threadIdx.x) >> 5; idx < total; idx += n_warps) {
         const int j = batch_find(pre, L.n, idx);
         const OccJob& J = L.job[j];
         const OccDevice& m = J.m;
@@ -804,6 +815,11 @@ __global__ void __launch_bounds__(128) occ_carve_kernel(const OccLaunch* __restr
     }
 }
 
+__global__ void __launch_bounds__(128) occ_carve_kernel(const OccLaunch* __restrict__ Lp, int depth)
+{
+    occ_carve_stage(*Lp, depth, blockIdx.x, gridDim.x);
+}
+
 // ---------------------------------------------------------------- propagation sets --
 
 __device__ __forceinline__ int occ_node_depth(const OccDevice& m, int n)
@@ -828,15 +844,14 @@ __device__ __forceinline__ void occ_set_insert(const OccDevice& m, int* sets, in
 
 // The carver's free-space nodes: the AABB grows by the leaves among them (Updater, multires_
 // ofusion_updater_impl.hpp:70-78) and they seed level 0 of freeNodeRecurse.
-__global__ void occ_nodes_kernel(const OccLaunch* __restrict__ Lp)
+__device__ void occ_nodes_stage(const OccLaunch& L, int bid, int nbid)
 {
-    const OccLaunch& L = *Lp;
     __shared__ int pre[kOccMaxBatch + 1];
     const int total = batch_prefix(
         L, pre, [](const OccJob& J) { return clamp_count(J.m.counters[kOccNodeListN], J.m.node_capacity); });
-    if (blockIdx.x == 0 && threadIdx.x < L.n)
+    if (bid == 0 && threadIdx.x < L.n)
         L.job[threadIdx.x].m.counters[kOccWorkN] = pre[threadIdx.x + 1] - pre[threadIdx.x];
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    for (int idx = bid * blockDim.x + threadIdx.x; idx < total; idx += nbid * blockDim.x) {
         const int j = batch_find(pre, L.n, idx);
         const OccJob& J = L.job[j];
         const OccDevice& m = J.m;
@@ -850,6 +865,11 @@ __global__ void occ_nodes_kernel(const OccLaunch* __restrict__ Lp)
     }
 }
 
+__global__ void occ_nodes_kernel(const OccLaunch* __restrict__ Lp)
+{
+    occ_nodes_stage(*Lp, blockIdx.x, gridDim.x);
+}
+
 __device__ __forceinline__ void occ_update(OccD& d, float value, float max_weight)
 {
     if (d.weight < max_weight)
@@ -860,13 +880,12 @@ __device__ __forceinline__ void occ_update(OccD& d, float value, float max_weigh
 
 // Updater::freeNodeRecurse, one level of the subtrees per launch: leaves are freed in place,
 // blocks go to the freed list, inner nodes queue their children.
-__global__ void occ_free_nodes_kernel(const OccLaunch* __restrict__ Lp, int level)
+__device__ void occ_free_nodes_stage(const OccLaunch& L, int level, int bid, int nbid)
 {
-    const OccLaunch& L = *Lp;
     __shared__ int pre[kOccMaxBatch + 1];
     const int total = batch_prefix(
         L, pre, [level](const OccJob& J) { return clamp_count(J.m.counters[kOccWorkN + level], J.m.node_capacity); });
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    for (int idx = bid * blockDim.x + threadIdx.x; idx < total; idx += nbid * blockDim.x) {
         const int j = batch_find(pre, L.n, idx);
         const OccJob& J = L.job[j];
         const OccDevice& m = J.m;
@@ -900,6 +919,11 @@ __global__ void occ_free_nodes_kernel(const OccLaunch* __restrict__ Lp, int leve
             }
         }
     }
+}
+
+__global__ void occ_free_nodes_kernel(const OccLaunch* __restrict__ Lp, int level)
+{
+    occ_free_nodes_stage(*Lp, level, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------- block state machine --
@@ -1314,17 +1338,16 @@ __device__ void occ_process_block(const OccLaunch& L, const OccJob& J, int b, bo
 
 // freeBlock on the freed blocks and updateBlock on the carver's blocks (disjoint: the carver
 // does not descend below a free-space node), one warp per block, all maps.
-__global__ void __launch_bounds__(256, 2) occ_blocks_kernel(const OccLaunch* __restrict__ Lp)
+__device__ void occ_blocks_stage(const OccLaunch& L, int bid, int nbid)
 {
-    const OccLaunch& L = *Lp;
     __shared__ int pre[kOccMaxBatch + 1];
     const int total = batch_prefix(L, pre, [](const OccJob& J) {
         return clamp_count(J.m.counters[kOccFreedN], J.m.block_capacity)
             + clamp_count(J.m.counters[kOccBlockListN], J.m.block_capacity);
     });
     const int lane = threadIdx.x & 31;
-    const int n_warps = (gridDim.x * blockDim.x) >> 5;
-    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < total; idx += n_warps) {
+    const int n_warps = (nbid * blockDim.x) >> 5;
+    for (int idx = (bid * blockDim.x + threadIdx.x) >> 5; idx < total; idx += n_warps) {
         const int j = batch_find(pre, L.n, idx);
         const OccJob& J = L.job[j];
         const int n_freed = clamp_count(J.m.counters[kOccFreedN], J.m.block_capacity);
@@ -1335,6 +1358,11 @@ __global__ void __launch_bounds__(256, 2) occ_blocks_kernel(const OccLaunch* __r
             occ_process_block(L, J, J.block_list[i - n_freed], J.block_var[i - n_freed] == 0,
                               J.block_inside[i - n_freed] != 0, false, lane);
     }
+}
+
+__global__ void __launch_bounds__(256, 2) occ_blocks_kernel(const OccLaunch* __restrict__ Lp)
+{
+    occ_blocks_stage(*Lp, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------- propagation --
@@ -1469,17 +1497,16 @@ __device__ void occ_propagate_block(const OccDevice& m, int b, int lane)
 
 // Block propagation on the freed and the carver's blocks (one warp per block); the carver's
 // blocks also put their parents in the first propagation set (propagateToRoot's seeds).
-__global__ void __launch_bounds__(256) occ_propagate_blocks_kernel(const OccLaunch* __restrict__ Lp)
+__device__ void occ_propagate_blocks_stage(const OccLaunch& L, int bid, int nbid)
 {
-    const OccLaunch& L = *Lp;
     __shared__ int pre[kOccMaxBatch + 1];
     const int total = batch_prefix(L, pre, [](const OccJob& J) {
         return clamp_count(J.m.counters[kOccFreedN], J.m.block_capacity)
             + clamp_count(J.m.counters[kOccBlockListN], J.m.block_capacity);
     });
     const int lane = threadIdx.x & 31;
-    const int n_warps = (gridDim.x * blockDim.x) >> 5;
-    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < total; idx += n_warps) {
+    const int n_warps = (nbid * blockDim.x) >> 5;
+    for (int idx = (bid * blockDim.x + threadIdx.x) >> 5; idx < total; idx += n_warps) {
         const int j = batch_find(pre, L.n, idx);
         const OccJob& J = L.job[j];
         const OccDevice& m = J.m;
@@ -1490,6 +1517,11 @@ __global__ void __launch_bounds__(256) occ_propagate_blocks_kernel(const OccLaun
         if (i >= n_freed && lane == 0)
             occ_set_insert(m, J.sets, m.block_state[b].parent, J.dyn->frame_id);
     }
+}
+
+__global__ void __launch_bounds__(256) occ_propagate_blocks_kernel(const OccLaunch* __restrict__ Lp)
+{
+    occ_propagate_blocks_stage(*Lp, blockIdx.x, gridDim.x);
 }
 
 // updater::propagate_to_parent_node (multires_ofusion_core_impl.hpp:88-117)
@@ -1546,13 +1578,12 @@ __device__ void occ_delete_children(const OccDevice& m, int n)
 }
 
 // One depth of propagateToRoot over every map's propagation set at that depth.
-__global__ void occ_propagate_nodes_kernel(const OccLaunch* __restrict__ Lp, int depth)
+__device__ void occ_propagate_nodes_stage(const OccLaunch& L, int depth, int bid, int nbid)
 {
-    const OccLaunch& L = *Lp;
     __shared__ int pre[kOccMaxBatch + 1];
     const int total = batch_prefix(
         L, pre, [depth](const OccJob& J) { return clamp_count(J.m.counters[kOccSetN + depth], J.m.node_capacity); });
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    for (int idx = bid * blockDim.x + threadIdx.x; idx < total; idx += nbid * blockDim.x) {
         const int j = batch_find(pre, L.n, idx);
         const OccJob& J = L.job[j];
         const OccDevice& m = J.m;
@@ -1571,6 +1602,11 @@ __global__ void occ_propagate_nodes_kernel(const OccLaunch* __restrict__ Lp, int
     }
 }
 
+__global__ void occ_propagate_nodes_kernel(const OccLaunch* __restrict__ Lp, int depth)
+{
+    occ_propagate_nodes_stage(*Lp, depth, blockIdx.x, gridDim.x);
+}
+
 __global__ void occ_propagate_root_kernel(const OccLaunch* __restrict__ Lp)
 {
     const OccLaunch& L = *Lp;
@@ -1579,6 +1615,115 @@ __global__ void occ_propagate_root_kernel(const OccLaunch* __restrict__ Lp)
         return;
     const OccJob& J = L.job[j];
     occ_propagate_node(J.m, 0, J.dyn->timestamp);
+}
+
+// ------------------------------------------------------------- one persistent launch --
+
+// A whole frame of every map of a batch in one cooperative launch: the stages above in order,
+// each a grid-stride loop over the persistent grid, separated by grid barriers.
+
+constexpr unsigned long long kOccBarrierNs = 1000000000ull; // 1 s per barrier wait
+
+struct OccBarrier {
+    unsigned count;
+    int timeout;
+};
+
+__device__ __forceinline__ unsigned long long occ_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Every CTA adds itself with release semantics, then one thread per CTA polls with acquire
+// semantics, so the CTA's loads after the barrier see every CTA's writes before it. A wait past
+// kOccBarrierNs raises the timeout flag, and every CTA then leaves at its next check; false once
+// the flag is up.
+__device__ bool occ_grid_sync(OccBarrier* bar, unsigned& phase)
+{
+    ++phase;
+    const unsigned target = phase * gridDim.x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&bar->count) : "memory");
+        const unsigned long long t0 = occ_ns();
+        unsigned spins = 0;
+        for (;;) {
+            unsigned v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(&bar->count) : "memory");
+            if (v >= target)
+                break;
+            if ((++spins & 63u) == 0u && (*((volatile int*) &bar->timeout) != 0 || occ_ns() - t0 > kOccBarrierNs)) {
+                atomicExch(&bar->timeout, 1);
+                break;
+            }
+        }
+    }
+    __syncthreads();
+    return *((volatile int*) &bar->timeout) == 0;
+}
+
+__global__ void __launch_bounds__(256, 2) occ_persistent_kernel(const OccLaunch* __restrict__ Lp,
+                                                                const OccStep* __restrict__ step, OccBarrier* bar)
+{
+    const OccLaunch& L = *Lp;
+    const int bid = blockIdx.x, nbid = gridDim.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const long long tid = (long long) bid * blockDim.x + threadIdx.x, nthreads = (long long) nbid * blockDim.x;
+    const long long npx = (long long) L.sensor.w * L.sensor.h;
+    unsigned phase = 0;
+    for (int j = bid; j < L.n; j += nbid)
+        occ_begin(L, *step, j);
+    bool ok = occ_grid_sync(bar, phase);
+    if (ok) {
+        for (long long k = tid; k < L.n * npx; k += nthreads)
+            occ_pixel(L, (int) (k / npx), (int) (k % npx));
+        ok = occ_grid_sync(bar, phase);
+    }
+    for (int l = 1; ok && l < L.sensor.levels; ++l) {
+        for (long long k = tid; k < 2 * L.n * npx; k += nthreads) {
+            const int jj = (int) (k / npx);
+            occ_pool_pixel(L, l, jj >> 1, jj & 1, (int) (k % npx));
+        }
+        ok = occ_grid_sync(bar, phase);
+    }
+    if (ok) {
+        for (int j = bid * nwarps + warp; j < L.n; j += nbid * nwarps)
+            occ_root(L, j, lane);
+        ok = occ_grid_sync(bar, phase);
+    }
+    for (int d = 1; ok && d <= L.max_block_depth; ++d) {
+        occ_carve_stage(L, d, bid, nbid);
+        ok = occ_grid_sync(bar, phase);
+    }
+    if (ok) {
+        occ_nodes_stage(L, bid, nbid);
+        ok = occ_grid_sync(bar, phase);
+    }
+    for (int it = 0; ok && it <= L.max_block_depth; ++it) {
+        occ_free_nodes_stage(L, it, bid, nbid);
+        ok = occ_grid_sync(bar, phase);
+    }
+    if (ok) {
+        occ_blocks_stage(L, bid, nbid);
+        ok = occ_grid_sync(bar, phase);
+    }
+    if (ok) {
+        occ_propagate_blocks_stage(L, bid, nbid);
+        ok = occ_grid_sync(bar, phase);
+    }
+    for (int d = L.max_block_depth - 1; ok && d > 0; --d) {
+        occ_propagate_nodes_stage(L, d, bid, nbid);
+        ok = occ_grid_sync(bar, phase);
+    }
+    if (bid == 0 && threadIdx.x < L.n) {
+        const OccJob& J = L.job[threadIdx.x];
+        if (ok)
+            occ_propagate_node(J.m, 0, J.dyn->timestamp);
+        else
+            atomicOr(&J.m.counters[kOccError], kOccErrTimeout);
+    }
 }
 
 // ------------------------------------------------------------------------ host side --
@@ -1818,6 +1963,36 @@ static se_gpu_status occ_enqueue(const OccLaunch& L, const OccLaunch* Ld, const 
     return SE_GPU_OK;
 }
 
+// The same frame as one cooperative launch of occ_persistent_kernel, ctas_per_sm CTAs per SM
+// (capped at what fits on an SM), its barrier counter cleared on the stream first.
+static se_gpu_status occ_enqueue_persistent(const OccLaunch* Ld, const OccStep* step_dev, OccBarrier* bar,
+                                            int ctas_per_sm, cudaStream_t stream, OccStageTimer* timer = nullptr)
+{
+    static int fits = 0;
+    if (fits == 0) {
+        SE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fits, occ_persistent_kernel, 256, 0));
+        if (fits < 1) {
+            set_last_error("the persistent occupancy kernel does not fit on an SM");
+            return SE_GPU_ERR_CUDA;
+        }
+    }
+    const int grid = device_sm_count() * (ctas_per_sm < fits ? ctas_per_sm : fits);
+    SE_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(OccBarrier), stream));
+    OCC_MARK(kTileCarve);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SE_CUDA_TRY(cudaLaunchKernelEx(&cfg, occ_persistent_kernel, Ld, step_dev, bar));
+    OCC_MARK(-1);
+    return SE_GPU_OK;
+}
+
 // The autotuner of a batch: its first kSkip calls run the default geometry untimed (the maps
 // grow from empty, so the first frames' work is not representative), then each of the next
 // kCand * kRounds calls runs one candidate geometry (candidate c: carve 2 << c, lists 1 << c,
@@ -1903,6 +2078,8 @@ struct se_gpu_occ_batch {
     OccLaunch* launch_dev = nullptr;
     OccTiles tiles;
     int use_graph = 0;
+    int persistent = 0;          // SE_GPU_OCC_BATCH_PERSISTENT: one cooperative launch per call
+    OccBarrier* bar = nullptr;   // its grid barrier
     OccTuner* tuner = nullptr; // while autotuning
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1915,6 +2092,24 @@ struct se_gpu_occ_batch {
     int ring = 0;
     int device = 0;
 };
+
+// The tuner's candidate c for this batch: in persistent mode 1 or 2 CTAs per SM of the one launch.
+static OccTiles batch_candidate(const se_gpu_occ_batch* b, int c)
+{
+    if (!b->persistent)
+        return OccTuner::candidate(c);
+    OccTiles t;
+    t.ctas[kTileCarve] = 1 + (c & 1);
+    return t;
+}
+
+static se_gpu_status batch_enqueue(se_gpu_occ_batch* b, const OccStep& step, const OccTiles& t, cudaStream_t s,
+                                   OccStageTimer* timer = nullptr)
+{
+    if (b->persistent)
+        return occ_enqueue_persistent(b->launch_dev, b->step_dev, b->bar, t.ctas[kTileCarve], s, timer);
+    return occ_enqueue(*b->launch_host, b->launch_dev, step, b->step_dev, t, s, timer);
+}
 
 static se_gpu_status bad(se_gpu_status st, const char* msg)
 {
@@ -1970,6 +2165,9 @@ se_gpu_status se_gpu_occ_batch_create(se_gpu_map* const* maps, int n, const se_g
     se_gpu_occ_batch* b = new se_gpu_occ_batch();
     b->maps.assign(maps, maps + n);
     b->use_graph = use_graph & SE_GPU_OCC_BATCH_GRAPH;
+    b->persistent = (use_graph & SE_GPU_OCC_BATCH_PERSISTENT) != 0;
+    if (b->persistent)
+        b->tiles.ctas[kTileCarve] = 2;
     if (use_graph & SE_GPU_OCC_BATCH_AUTOTUNE)
         b->tuner = new OccTuner();
     b->device = maps[0]->device;
@@ -1993,6 +2191,8 @@ se_gpu_status se_gpu_occ_batch_create(se_gpu_map* const* maps, int n, const se_g
         e = cudaMemcpy(b->launch_dev, &L, sizeof(OccLaunch), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMalloc(&b->step_dev, sizeof(OccStep));
+    if (e == cudaSuccess && b->persistent)
+        e = cudaMalloc(&b->bar, sizeof(OccBarrier));
     if (e == cudaSuccess)
         e = cudaHostAlloc(&b->step_pinned, se_gpu_occ_batch::kStepRing * sizeof(OccStep), cudaHostAllocDefault);
     for (int r = 0; r < se_gpu_occ_batch::kStepRing && e == cudaSuccess; ++r)
@@ -2032,14 +2232,13 @@ se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* b, const float* const
     }
     if (b->tuner && b->tuner->frames < OccTuner::kSkip) {
         ++b->tuner->frames;
-        return occ_enqueue(*b->launch_host, b->launch_dev, step, b->step_dev, b->tiles, s);
+        return batch_enqueue(b, step, b->tiles, s);
     }
     if (b->tuner) {
         OccTuner& tu = *b->tuner;
         const int c = (tu.frames - OccTuner::kSkip) % OccTuner::kCand;
         tu.timer.used = 0;
-        se_gpu_status st =
-            occ_enqueue(*b->launch_host, b->launch_dev, step, b->step_dev, OccTuner::candidate(c), s, &tu.timer);
+        se_gpu_status st = batch_enqueue(b, step, batch_candidate(b, c), s, &tu.timer);
         if (st != SE_GPU_OK)
             return st;
         SE_CUDA_TRY(cudaEventSynchronize(tu.timer.ev[tu.timer.used - 1]));
@@ -2058,7 +2257,7 @@ se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* b, const float* const
                 for (int cc = 1; cc < OccTuner::kCand; ++cc)
                     if (tu.ms[k][cc] < tu.ms[k][best])
                         best = cc;
-                b->tiles.ctas[k] = OccTuner::candidate(best).ctas[k];
+                b->tiles.ctas[k] = batch_candidate(b, best).ctas[k];
             }
             delete b->tuner;
             b->tuner = nullptr;
@@ -2066,7 +2265,7 @@ se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* b, const float* const
         return SE_GPU_OK;
     }
     if (!b->use_graph)
-        return occ_enqueue(*b->launch_host, b->launch_dev, step, b->step_dev, b->tiles, s);
+        return batch_enqueue(b, step, b->tiles, s);
     if (!b->exec) {
         // captured once: the launches read this and every later call's parameters from step_dev
         cudaStream_t cs;
@@ -2074,7 +2273,7 @@ se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* b, const float* const
         cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
         se_gpu_status st = SE_GPU_OK;
         if (e == cudaSuccess)
-            st = occ_enqueue(*b->launch_host, b->launch_dev, step, b->step_dev, b->tiles, cs);
+            st = batch_enqueue(b, step, b->tiles, cs);
         cudaGraph_t graph = nullptr;
         const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
         cudaStreamDestroy(cs);
@@ -2113,6 +2312,7 @@ se_gpu_status se_gpu_occ_batch_destroy(se_gpu_occ_batch* b)
         cudaGraphDestroy(b->graph);
     cudaFree(b->launch_dev);
     cudaFree(b->step_dev);
+    cudaFree(b->bar);
     cudaFreeHost(b->step_pinned);
     for (int r = 0; r < se_gpu_occ_batch::kStepRing; ++r)
         if (b->step_ev[r])

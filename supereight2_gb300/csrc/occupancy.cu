@@ -678,6 +678,10 @@ se_gpu_status occ_check(se_gpu_occ_map* om)
         set_last_error("occupancy node pool of %d nodes is full", om->dev.node_capacity);
         return SE_GPU_ERR_POOL_FULL;
     }
+    if (err & kOccErrTimeout) {
+        set_last_error("a grid barrier of the persistent batch launch waited past its limit; the frame is incomplete");
+        return SE_GPU_ERR_CUDA;
+    }
     set_last_error("an occupancy work list overflowed");
     return SE_GPU_ERR_POOL_FULL;
 }

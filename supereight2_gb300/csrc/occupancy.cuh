@@ -84,7 +84,7 @@ enum {
 };
 constexpr int kOccFirstFrameCounter = kOccBlockListN; // counters from here on restart every frame
 
-constexpr int kOccErrNodePool = 1, kOccErrBlockPool = 2, kOccErrList = 4;
+constexpr int kOccErrNodePool = 1, kOccErrBlockPool = 2, kOccErrList = 4, kOccErrTimeout = 8;
 
 // ------------------------------------------------------------------------ sensors --
 

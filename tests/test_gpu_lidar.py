@@ -55,14 +55,17 @@ def test_lidar_single_map_matches_oracle(oracle, gpu):
     _compare(om, gm)
 
 
-@pytest.mark.parametrize("graph,autotune", [(False, False), (True, False), (True, True)])
-def test_lidar_batch_matches_oracle(oracle, gpu, graph, autotune):
+@pytest.mark.parametrize("graph,autotune,persistent", [(False, False, False), (True, False, False),
+                                                        (True, True, False), (False, False, True),
+                                                        (True, True, True)])
+def test_lidar_batch_matches_oracle(oracle, gpu, graph, autotune, persistent):
     import torch
     spec, poses, ranges = _lidar_data(4)
     n = len(poses)
     oms = [oracle.OracleOccMap(102.4, 0.4, T_MW=T_MW) for _ in range(n)]
     gms = [_gpu_map(gpu) for _ in range(n)]
-    batch = gpu.OccupancyBatch(gms, gpu.OusterLidar.from_spec(spec), graph=graph, autotune=autotune)
+    batch = gpu.OccupancyBatch(gms, gpu.OusterLidar.from_spec(spec), graph=graph, autotune=autotune,
+                               persistent=persistent)
     ol = _oracle_lidar(oracle, spec)
     for i in range(len(poses[0])):
         imgs = torch.from_numpy(np.stack([ranges[k][i] for k in range(n)])).cuda()
@@ -80,7 +83,8 @@ def test_lidar_batch_matches_oracle(oracle, gpu, graph, autotune):
     assert len(set(counts)) == n          # uneven work across the batch
 
 
-def test_pinhole_batch_matches_oracle(oracle, gpu):
+@pytest.mark.parametrize("persistent", [False, True])
+def test_pinhole_batch_matches_oracle(oracle, gpu, persistent):
     import torch
     sensor, _, poses, frames = syn.dataset("mr160", 6)
     spec = dict(width=sensor.width, height=sensor.height, fx=sensor.fx, fy=sensor.fy, cx=sensor.cx,
@@ -88,7 +92,7 @@ def test_pinhole_batch_matches_oracle(oracle, gpu):
     s = oracle.pinhole(**spec)
     oms = [oracle.OracleOccMap(10.24, 0.02) for _ in range(2)]
     gms = [gpu.Map(10.24, 0.02, res_type="multi", field="occupancy", max_blocks=1 << 18) for _ in range(2)]
-    batch = gpu.OccupancyBatch(gms, gpu.PinholeCamera(**spec), graph=True)
+    batch = gpu.OccupancyBatch(gms, gpu.PinholeCamera(**spec), graph=True, persistent=persistent)
     for i in range(len(frames)):
         # the second map sees the frames in reverse order
         idx = [i, len(frames) - 1 - i]
@@ -102,14 +106,16 @@ def test_pinhole_batch_matches_oracle(oracle, gpu):
         _compare(om, gm)
 
 
-def test_lidar_batch_after_tuning_matches_oracle(oracle, gpu):
+@pytest.mark.parametrize("persistent", [False, True])
+def test_lidar_batch_after_tuning_matches_oracle(oracle, gpu, persistent):
     """Eighteen scans: sixteen tuning calls (four untimed), then the graph captured with the
     chosen geometry."""
     import torch
     spec, poses, ranges = _lidar_data(18, roads=(5,))
     om = oracle.OracleOccMap(102.4, 0.4, T_MW=T_MW)
     gm = _gpu_map(gpu)
-    batch = gpu.OccupancyBatch([gm], gpu.OusterLidar.from_spec(spec), graph=True, autotune=True)
+    batch = gpu.OccupancyBatch([gm], gpu.OusterLidar.from_spec(spec), graph=True, autotune=True,
+                               persistent=persistent)
     ol = _oracle_lidar(oracle, spec)
     for i, (r, T) in enumerate(zip(ranges[0], poses[0])):
         T = T.astype(np.float32)
@@ -117,5 +123,7 @@ def test_lidar_batch_after_tuning_matches_oracle(oracle, gpu):
         om.integrate_lidar(r, ol, T, i)
     tiles, left = batch.tiles()
     assert left == 0 and all(t in (1, 2, 4, 8, 16) for t in tiles)
+    if persistent:
+        assert tiles[0] in (1, 2)
     gm.check()
     _compare(om, gm)
