@@ -47,14 +47,14 @@ def _peaks():
 
 
 # Bench kernel names -> the kernel names of the committed DRAM-traffic capture of this workload
-_TRAFFIC_NAMES = {"icp_iter": "icp_persistent_kernel", "update": "update_kernel<0>", "raycast": "raycast_kernel<0, 0>",
-                  "carve": "carve_kernel", "frustum": "frustum_kernel", "mr_update": "mr_update_kernel<0>"}
+_TRAFFIC_NAMES = {"icp_iter": "icp_persistent_kernel", "update": "update_kernel<0, 4>",
+                  "raycast": "raycast_kernel<0, 0, 0>", "mr_update": "mr_update_kernel<0>"}
 
 
 def _traffic(kernel):
-    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu capture of this
-    workload (profiles/dram_traffic_tsdf640_bench.txt), or None."""
-    p = os.path.join(ROOT, "profiles", "dram_traffic_tsdf640_bench.txt")
+    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu captures of this
+    workload, one kernel each (profiles/dram_traffic_per_kernel_tsdf640.txt), or None."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic_per_kernel_tsdf640.txt")
     name = _TRAFFIC_NAMES.get(kernel)
     if not name or not os.path.exists(p):
         return None
@@ -341,7 +341,7 @@ def run_ours(args, ws, rank, local):
     upd_ms = kms.get("update", 0.0) / max(kl.get("update", 1), 1)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": (achieved / hbm_peak) if achieved else None, "traffic": _traffic(dom),
-                "traffic_source": "profiles/dram_traffic_tsdf640_bench.txt (ncu, --cache-control none)",
+                "traffic_source": "profiles/dram_traffic_per_kernel_tsdf640.txt (ncu, one kernel per capture, --cache-control none)",
                 "peak_kind": peak_kind, "algorithmic_bytes_per_launch": algo,
                 "avg_launch_us": avg_launch_ms * 1e3,
                 "integration": {"kernel": "update", "avg_launch_us": upd_ms * 1e3,
