@@ -378,8 +378,8 @@ __device__ __forceinline__ bool ri_aborted(const RiArgs& A)
     return *((volatile int*) &A.ctl->abort) != 0;
 }
 
-// Waits (lane 0, bounded) until the ticket *p reaches want; every lane then reads it with
-// acquire semantics. A ray far back in a block's queue polls rarely, the next in line often.
+// Waits (lane 0, bounded) until the ticket *p reaches want, polling with acquire semantics. A
+// ray far back in a block's queue polls rarely, the next in line often.
 __device__ bool ri_wait_eq(const RiArgs& A, const int* p, int want, int lane)
 {
     int ok = 1;
@@ -402,15 +402,15 @@ __device__ bool ri_wait_eq(const RiArgs& A, const int* p, int want, int lane)
         }
     }
     ok = __shfl_sync(kFull, ok, 0);
-    if (ok)
-        (void) ld_acquire(p);
+    // the warp barrier orders lane 0's acquire before every lane's later loads
+    __syncwarp();
     return ok != 0;
 }
 
-// Publishes the warp's writes, then sets *p = v.
+// Sets *p = v after the warp's writes: the warp barrier orders every lane's writes before lane
+// 0's store, whose release semantics carry them to the next acquirer.
 __device__ __forceinline__ void ri_release(int* p, int v, int lane)
 {
-    __threadfence();
     __syncwarp();
     if (lane == 0)
         st_release(p, v);
