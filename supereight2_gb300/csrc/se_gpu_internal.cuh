@@ -244,28 +244,26 @@ __device__ __forceinline__ int block_at(const MapDevice& m, int bx, int by, int 
 // layout's (each update shrinks the carried error by (w - 1) / w and adds at most 2^-19):
 // 1.9e-4 truncation units at the reference's max_weight = 100. Plain binary16 storage would
 // carry W * 2^-11 (0.049) in the worst case.
+// Both directions work on the float's bits scaled by 2^-112, which puts FP16's exponent range
+// (bias 15) at the bottom of FP32's (bias 127): a tsdf of at least 2^-14 keeps its significand
+// and loses 112 from its exponent, a smaller one becomes an FP32 subnormal in units of 2^-149
+// (the scaling rounds it to nearest even there), and dropping the 5 low bits of those bits with
+// rounding to nearest even gives the 23-bit field in either case. Unpacking shifts the field
+// back into an FP32 pattern and scales by 2^112, exact for normal and subnormal fields alike.
+// The weight moves through the low bits of 2^23 + w. No branches, no conversion instructions.
 __device__ __forceinline__ uint32_t f16x_pack(float t, float w)
 {
-    const uint32_t u = __float_as_uint(t), a = u & 0x7fffffffu;
-    uint32_t em; // exponent and significand, 23 bits
-    if (a >= 0x38800000u) { // |t| >= 2^-14: normal; round the 5 dropped bits to nearest even
-        const uint32_t r = (a + 0xfu + ((a >> 5) & 1u)) >> 5;
-        em = r - (112u << 18);
-        if (em > 0x7fffffu)
-            em = 0x7fffffu; // beyond the format's range (not reached: |tsdf| <= 1)
-    }
-    else { // subnormal: units of 2^-32 (rounds up into the smallest normal consistently)
-        em = __float2uint_rn(__uint_as_float(a) * 4294967296.0f);
-    }
+    const uint32_t b = __float_as_uint(fabsf(t) * 0x1p-112f);
+    uint32_t em = (b + 0xfu + ((b >> 5) & 1u)) >> 5; // exponent and significand, 23 bits
+    em = em < 0x7fffffu ? em : 0x7fffffu;            // beyond the format's range (not reached: |tsdf| <= 1)
     const float wc = w < 255.0f ? w : 255.0f;
-    return (u & 0x80000000u) | (em << 8) | (uint32_t) wc;
+    return (__float_as_uint(t) & 0x80000000u) | (em << 8) | (__float_as_uint(wc + 8388608.0f) & 0xffu);
 }
 __device__ __forceinline__ void f16x_unpack(uint32_t d, float& t, float& w)
 {
-    const uint32_t em = (d >> 8) & 0x7fffffu;
-    const float mag = em >= (1u << 18) ? __uint_as_float((em + (112u << 18)) << 5) : (float) em * 0x1p-32f;
+    const float mag = __uint_as_float((d >> 3) & 0x0fffffe0u) * 0x1p112f;
     t = __uint_as_float(__float_as_uint(mag) | (d & 0x80000000u));
-    w = (float) (d & 0xffu);
+    w = __uint_as_float(0x4b000000u | (d & 0xffu)) - 8388608.0f;
 }
 
 // Voxel data access; S is the se_gpu_storage layout (F32: float2 {tsdf, weight};
