@@ -525,9 +525,12 @@ SE_GPU_API se_gpu_status se_gpu_frame_autotune(se_gpu_frame* frame, int runs);
  * tiles[2] raycast warp tile (0: 8 x 4, 1: 16 x 2); tuning_left (may be NULL) the tuning runs
  * still to come. */
 SE_GPU_API se_gpu_status se_gpu_frame_tiles(const se_gpu_frame* frame, int tiles[3], int* tuning_left);
-/* se_gpu_frame_run with the frame's depth image taken from host memory (width*height floats,
- * copied into the frame's input buffer on stream first; pinned memory keeps the copy
- * asynchronous), as integrateDepth / track take a host Image<float>. */
+/* se_gpu_frame_run with the frame's depth image taken from host memory (width*height floats),
+ * as integrateDepth / track take a host Image<float>. The host copy runs on the frame's own copy
+ * stream into one of two device staging buffers, so the next call's copy overlaps this frame's
+ * work; the frame's stream then waits for it and copies the staging buffer into the input
+ * buffer. Pinned memory keeps the copy asynchronous; the host buffer must stay unchanged until
+ * the frame's stream has passed this call. */
 SE_GPU_API se_gpu_status se_gpu_frame_run_host(se_gpu_frame* frame, const float* depth_host, int track,
                                                void* stream);
 /* Read the device pose (after the runs enqueued on stream) and the last run's acceptance (the

@@ -57,6 +57,12 @@ struct se_gpu_frame {
     FrameTuneEvents* tune_ev;
     float update_ms[kUpdateCandidates];
     float raycast_ms[kRaycastCandidates];
+    // host inputs: two device staging slots filled on a copy stream, so that the next frame's
+    // copy runs while this frame computes; the frame's stream copies a slot into `depth`
+    float* staging[2];
+    cudaStream_t copy_stream;
+    cudaEvent_t copied[2], consumed[2];
+    int slot;
 };
 
 // One frame's launches on stream (captured into the graph, or run directly while tuning).
@@ -140,6 +146,15 @@ se_gpu_status se_gpu_frame_create(se_gpu_map* map, se_gpu_tracker* tracker, cons
     if ((e = cudaMemset(f->nrm, 0, npx * 3 * sizeof(float))) != cudaSuccess) return fail(e, "cudaMemset");
     if ((e = cudaStreamCreateWithFlags(&f->capture_stream, cudaStreamNonBlocking)) != cudaSuccess)
         return fail(e, "cudaStreamCreate");
+    if ((e = cudaStreamCreateWithFlags(&f->copy_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return fail(e, "cudaStreamCreate");
+    for (int i = 0; i < 2; ++i) {
+        if ((e = cudaMalloc(&f->staging[i], npx * sizeof(float))) != cudaSuccess) return fail(e, "cudaMalloc(staging)");
+        if ((e = cudaEventCreateWithFlags(&f->copied[i], cudaEventDisableTiming)) != cudaSuccess)
+            return fail(e, "cudaEventCreate");
+        if ((e = cudaEventCreateWithFlags(&f->consumed[i], cudaEventDisableTiming)) != cudaSuccess)
+            return fail(e, "cudaEventCreate");
+    }
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e, "cudaDeviceSynchronize");
     *out = f;
     return SE_GPU_OK;
@@ -154,6 +169,15 @@ se_gpu_status se_gpu_frame_destroy(se_gpu_frame* f)
             cudaGraphExecDestroy(f->exec[i]);
     if (f->capture_stream)
         cudaStreamDestroy(f->capture_stream);
+    if (f->copy_stream)
+        cudaStreamDestroy(f->copy_stream);
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(f->staging[i]);
+        if (f->copied[i])
+            cudaEventDestroy(f->copied[i]);
+        if (f->consumed[i])
+            cudaEventDestroy(f->consumed[i]);
+    }
     if (f->tune_ev) {
         for (int i = 0; i < 4; ++i)
             if (f->tune_ev->ev[i])
@@ -320,7 +344,17 @@ se_gpu_status se_gpu_frame_run_host(se_gpu_frame* f, const float* depth_host, in
         return SE_GPU_ERR_BAD_ARG;
     }
     const size_t bytes = (size_t) f->sensor.width * (size_t) f->sensor.height * sizeof(float);
-    SE_CUDA_TRY(cudaMemcpyAsync(f->depth, depth_host, bytes, cudaMemcpyHostToDevice, (cudaStream_t) stream_p));
+    cudaStream_t stream = (cudaStream_t) stream_p;
+    // the host copy on the copy stream into a staging slot (free once the frame stream's copy out
+    // of it from two calls ago has run), then the device copy on the frame's stream
+    const int k = f->slot;
+    f->slot ^= 1;
+    SE_CUDA_TRY(cudaStreamWaitEvent(f->copy_stream, f->consumed[k], 0));
+    SE_CUDA_TRY(cudaMemcpyAsync(f->staging[k], depth_host, bytes, cudaMemcpyHostToDevice, f->copy_stream));
+    SE_CUDA_TRY(cudaEventRecord(f->copied[k], f->copy_stream));
+    SE_CUDA_TRY(cudaStreamWaitEvent(stream, f->copied[k], 0));
+    SE_CUDA_TRY(cudaMemcpyAsync(f->depth, f->staging[k], bytes, cudaMemcpyDeviceToDevice, stream));
+    SE_CUDA_TRY(cudaEventRecord(f->consumed[k], stream));
     return se_gpu_frame_run(f, track, stream_p);
 }
 
