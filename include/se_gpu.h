@@ -254,6 +254,12 @@ SE_GPU_API se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* batch,
                                                     const float* const* images_dev,
                                                     const float* T_WS, const int* timestamps,
                                                     void* stream);
+/* The four per-frame counters of every map of the batch (as se_gpu_map_occupancy_stats: blocks
+ * listed, free-space nodes listed, blocks freed, nodes pruned), 4 int32 per map into stats_host
+ * (pinned for an asynchronous copy), enqueued on stream: valid once the stream passes this call,
+ * so that a caller reads step k's counters while step k + 1 runs. */
+SE_GPU_API se_gpu_status se_gpu_occ_batch_stats_async(const se_gpu_occ_batch* batch, int32_t* stats_host,
+                                                      void* stream);
 SE_GPU_API se_gpu_status se_gpu_occ_batch_destroy(se_gpu_occ_batch* batch);
 
 /* Counters of the last integrate_depth; synchronises the stream. */

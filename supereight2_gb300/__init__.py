@@ -108,6 +108,7 @@ SIGNATURES = {
     "se_gpu_map_check": (C.c_int, [_VP]),
     "se_gpu_integrate_depth": (C.c_int, [_VP, _VP, C.POINTER(_Pinhole), _F16, C.c_int, _VP]),
     "se_gpu_integrate_range": (C.c_int, [_VP, _VP, C.POINTER(_Lidar), _F16, C.c_int, _VP]),
+    "se_gpu_occ_batch_stats_async": (C.c_int, [_VP, _VP, _VP]),
     "se_gpu_occ_integrate_ray_batch": (C.c_int, [_VP, C.POINTER(_LeicaLidar), _VP, _VP, C.c_int64, C.c_int32,
                                                  _VP, C.c_int64, C.POINTER(C.c_int64), _VP]),
     "se_gpu_bilateral_filter": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.POINTER(_BilateralConfig), _VP]),
@@ -578,6 +579,15 @@ class OccupancyBatch:
         _check(self._L.se_gpu_occ_batch_create(arr, len(self.maps), pin, lid, flags, C.byref(h)),
                "se_gpu_occ_batch_create")
         self.h = h
+
+    def stats_async(self, out, stream=None):
+        """Enqueue the copy of every map's four per-frame counters into out, a pinned int32 host
+        tensor of shape (n, 4); valid once the stream passes this call."""
+        import torch
+        if out.is_cuda or out.dtype != torch.int32 or tuple(out.shape) != (len(self.maps), 4) or not out.is_contiguous():
+            raise SeGpuError("out must be a contiguous (n, 4) int32 host tensor")
+        _check(self._L.se_gpu_occ_batch_stats_async(self.h, C.c_void_p(out.data_ptr()), _stream(stream)),
+               "se_gpu_occ_batch_stats_async")
 
     def tiles(self):
         """(CTAs per SM of the carver, list and block stages), tuning calls left."""

@@ -2290,6 +2290,19 @@ se_gpu_status se_gpu_occ_batch_integrate(se_gpu_occ_batch* b, const float* const
     return SE_GPU_OK;
 }
 
+se_gpu_status se_gpu_occ_batch_stats_async(const se_gpu_occ_batch* b, int32_t* stats_host, void* stream)
+{
+    if (!b || !stats_host)
+        return bad(SE_GPU_ERR_BAD_ARG, "se_gpu_occ_batch_stats_async: null argument");
+    static_assert(kOccNodeListN == kOccBlockListN + 1 && kOccFreedN == kOccBlockListN + 2
+                      && kOccPruned == kOccBlockListN + 3,
+                  "the four per-frame counters are contiguous");
+    for (size_t j = 0; j < b->maps.size(); ++j)
+        SE_CUDA_TRY(cudaMemcpyAsync(stats_host + 4 * j, b->maps[j]->occ->dev.counters + kOccBlockListN,
+                                    4 * sizeof(int32_t), cudaMemcpyDeviceToHost, (cudaStream_t) stream));
+    return SE_GPU_OK;
+}
+
 se_gpu_status se_gpu_occ_batch_tiles(const se_gpu_occ_batch* b, int tiles[3], int* tuning)
 {
     if (!b || !tiles)

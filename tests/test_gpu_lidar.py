@@ -127,3 +127,19 @@ def test_lidar_batch_after_tuning_matches_oracle(oracle, gpu, persistent):
         assert tiles[0] in (1, 2)
     gm.check()
     _compare(om, gm)
+
+
+def test_batch_stats_async_equals_map_stats(gpu):
+    import torch
+    spec, poses, ranges = _lidar_data(2, roads=(0, 3))
+    gms = [_gpu_map(gpu) for _ in range(2)]
+    batch = gpu.OccupancyBatch(gms, gpu.OusterLidar.from_spec(spec), graph=True)
+    out = torch.zeros((2, 4), dtype=torch.int32).pin_memory()
+    for i in range(2):
+        imgs = torch.from_numpy(np.stack([ranges[k][i] for k in range(2)])).cuda()
+        batch.integrate(imgs, np.stack([poses[k][i] for k in range(2)]).astype(np.float32), i)
+        batch.stats_async(out)
+        torch.cuda.synchronize()
+        for k, gm in enumerate(gms):
+            assert tuple(int(v) for v in out[k]) == tuple(gm.occupancy_stats())
+    assert int(out[:, 0].min()) > 0
