@@ -2,17 +2,17 @@
 // Map::getFieldInterp / Map::getFieldGrad queries.
 //
 // One thread per pixel (an 8 x 4 pixel tile per warp for coherent block lookups):
-//   1. first allocated block on the ray: the sparse-voxel-octree traversal of
-//      VoxelBlockRayIterator (voxel_block_ray_iterator_impl.hpp:19-249, Laine & Karras 2010)
-//      with the same float expressions; node existence is a bit test in the occupancy pyramid
-//      instead of a child-pointer chase, and the traversal stack keeps only t_max;
+//   1. first allocated block on the ray (VoxelBlockRayIterator,
+//      voxel_block_ray_iterator_impl.hpp:19-249): a level DDA over the occupancy pyramid from
+//      cells of 4^3 blocks down to blocks, with the reference traversal's plane parameters and
+//      child choices (first_block in raycast_core.cuh);
 //   2. the TSDF march of raycast<TSDF> (raycaster_impl.hpp:456-533): voxel fetches through the
 //      dense block index with a one-block cache, trilinear interpolation near the surface
 //      (visitor_impl.hpp:976-1024) and the linear zero-crossing estimate;
 //   3. the surface normal from the 32-sample central-difference gradient
 //      (visitor_impl.hpp:1094-1251, map_impl.hpp:236-262), its 32 loads issued together.
-// The traversal stack and the gradient's block table live in shared memory; the register cap
-// of 9 CTAs per SM (a few spilled words) is faster than the 5 CTAs that 92 registers allow.
+// The gradient's block table lives in shared memory; the register cap of 9 CTAs per SM (a few
+// spilled words) is faster than the 5 CTAs that 92 registers allow.
 // Sample loops are deliberately not unrolled: one copy of the fetch path keeps the kernel
 // inside the instruction cache.
 #include <cmath>
@@ -39,9 +39,7 @@ __global__ void __launch_bounds__(128, 9) raycast_kernel(MapDevice m, Pinhole s,
                                                       int8_t* __restrict__ scale)
 {
     grid_dep_wait();
-    // per-thread scratch in shared memory (column threadIdx.x): the traversal stack and the
-    // gradient's block table
-    __shared__ float sh_stack[kEsvoStackDepth * 128];
+    // per-thread scratch in shared memory (column threadIdx.x): the gradient's block table
     __shared__ int sh_bt[8 * 128];
     const RaycastParams rp = *P;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -62,7 +60,7 @@ __global__ void __launch_bounds__(128, 9) raycast_kernel(MapDevice m, Pinhole s,
     F3 n = f3(0.0f, 0.0f, 0.0f);
     F3 p = f3(0.0f, 0.0f, 0.0f);
     int hit_scale = 0;
-    if (raycast_tsdf<S, MR>(m, rp, c, origin, dir_W, t_near, t_far, hit, hit_scale, sh_stack + threadIdx.x, 128)) {
+    if (raycast_tsdf<S, MR>(m, rp, c, origin, dir_W, t_near, t_far, hit, hit_scale)) {
         p = hit;
         F3 g;
         bool ok;
