@@ -200,23 +200,23 @@ __device__ __forceinline__ float half_sample_px(const float* __restrict__ in, in
 
 __device__ __forceinline__ F3 ld3(const float* p, size_t i) { return f3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
 
-// depth_to_point_cloud and point_cloud_to_normal<NegY> for one pixel, straight from the depth
-// image (the points of the pixel and of its four neighbours are formed on the fly with the
-// same float operations as the point image would hold).
-__device__ __forceinline__ F3 depth_point(const float* __restrict__ depth, const Pinhole& s, int w, int i)
+// depth_to_point_cloud and point_cloud_to_normal<NegY> for one pixel (x, y), straight from the
+// depth image (the points of the pixel and of its four neighbours are formed on the fly with
+// the same float operations as the point image would hold).
+__device__ __forceinline__ F3 depth_point(const float* __restrict__ depth, const Pinhole& s, int w, int x, int y)
 {
-    const float d = depth[i];
+    const float d = depth[x + w * y];
     if (d > 0.0f)
-        return mul(d, back_project(s, (float) (i % w), (float) (i / w)));
+        return mul(d, back_project(s, (float) x, (float) y));
     return f3(0.0f, 0.0f, 0.0f);
 }
 
-// point_cloud_to_normal<NegY> for pixel i, reading the neighbours' points from the depth image
-__device__ __forceinline__ F3 depth_normal(const float* __restrict__ depth, const Pinhole& s, int w, int h, int i,
-                                           int neg_y)
+// point_cloud_to_normal<NegY> for pixel (x, y), reading the neighbours' points from the depth
+// image
+__device__ __forceinline__ F3 depth_normal(const float* __restrict__ depth, const Pinhole& s, int w, int h, int x,
+                                           int y, int neg_y)
 {
-    const int x = i % w, y = i / w;
-    const F3 p = depth_point(depth, s, w, i);
+    const F3 p = depth_point(depth, s, w, x, y);
     if (p.z == 0.0f)
         return f3(0.0f, 0.0f, 0.0f);
     const int lx = max(x - 1, 0), rx = min(x + 1, w - 1);
@@ -229,8 +229,8 @@ __device__ __forceinline__ F3 depth_normal(const float* __restrict__ depth, cons
         dy = max(y - 1, 0);
         uy = min(y + 1, h - 1);
     }
-    const F3 left = depth_point(depth, s, w, lx + w * y), right = depth_point(depth, s, w, rx + w * y);
-    const F3 up = depth_point(depth, s, w, x + w * uy), down = depth_point(depth, s, w, x + w * dy);
+    const F3 left = depth_point(depth, s, w, lx, y), right = depth_point(depth, s, w, rx, y);
+    const F3 up = depth_point(depth, s, w, x, uy), down = depth_point(depth, s, w, x, dy);
     if (left.z == 0.0f || right.z == 0.0f || up.z == 0.0f || down.z == 0.0f)
         return f3(0.0f, 0.0f, 0.0f);
     return normalized(cross(sub(right, left), sub(up, down)));
@@ -250,8 +250,8 @@ __global__ void points_normals_kernel(LevelImages li, int levels, int neg_y)
     if (x >= w || y >= h)
         return;
     const int i = x + w * y;
-    const F3 p = depth_point(li.depth[l], li.s[l], w, i);
-    const F3 n = depth_normal(li.depth[l], li.s[l], w, h, i, neg_y);
+    const F3 p = depth_point(li.depth[l], li.s[l], w, x, y);
+    const F3 n = depth_normal(li.depth[l], li.s[l], w, h, x, y, neg_y);
     float* op = li.pts[l] + 3 * (size_t) i;
     float* on = li.nrm[l] + 3 * (size_t) i;
     op[0] = p.x;
@@ -303,10 +303,12 @@ __global__ void track_init_kernel(TrackState* st, TrackInit init, const float* p
 }
 
 // The first launch of a track(): block 0 initialises the state and clears the merge
-// accumulators; every thread forms the level-1 depth of its 2 x 2 pixel group and, with three
-// levels, the level-2 depth of the group from those values (half_sample_robust_image twice,
-// the second pass on the first's values). Grid: ceil(w1 / 2) x ceil(h1 / 2) threads (one block
-// when there is no pyramid).
+// accumulators; every thread forms the depth of one level-1 pixel and, with three levels, the
+// first thread of each 2 x 2 group forms the level-2 depth from the group's values
+// (half_sample_robust_image twice, the second pass on the first's values). A warp covers 16 x 2
+// level-1 pixels (lane & 15, lane >> 4), so a group's values meet by shuffles; a CTA of 32 x 8
+// threads covers 16 x 16. Grid: ceil(w1 / 16) x ceil(h1 / 16) (one block when there is no
+// pyramid).
 __global__ void pyramid_init_kernel(TrackState* st, TrackInit init, const float* pose12_in, unsigned long long* acc,
                                     LevelImages li, int levels, float e_d, float* __restrict__ d1,
                                     float* __restrict__ d2)
@@ -321,31 +323,37 @@ __global__ void pyramid_init_kernel(TrackState* st, TrackInit init, const float*
     }
     if (levels < 2)
         return;
-    const int x2 = blockIdx.x * blockDim.x + threadIdx.x, y2 = blockIdx.y * blockDim.y + threadIdx.y;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int x1 = blockIdx.x * 16 + (lane & 15), y1 = blockIdx.y * 16 + 2 * warp + (lane >> 4);
     const int w1 = li.w[1], h1 = li.h[1];
-    float v[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
-#pragma unroll
-    for (int dy = 0; dy < 2; ++dy)
-#pragma unroll
-        for (int dx = 0; dx < 2; ++dx) {
-            const int x1 = 2 * x2 + dx, y1 = 2 * y2 + dy;
-            if (x1 < w1 && y1 < h1) {
-                v[dy][dx] = half_sample_px(li.depth[0], li.w[0], w1, h1, e_d, x1, y1);
-                d1[x1 + y1 * w1] = v[dy][dx];
-            }
-        }
-    if (levels < 3 || x2 >= li.w[2] || y2 >= li.h[2])
+    float v = 0.0f;
+    if (x1 < w1 && y1 < h1) {
+        v = half_sample_px(li.depth[0], li.w[0], w1, h1, e_d, x1, y1);
+        d1[x1 + y1 * w1] = v;
+    }
+    if (levels < 3)
+        return;
+    // the group of (x1, y1) with x1, y1 even: (x1 + 1, y1), (x1, y1 + 1), (x1 + 1, y1 + 1)
+    float q[2][2];
+    q[0][0] = v;
+    q[0][1] = __shfl_down_sync(0xffffffffu, v, 1);
+    q[1][0] = __shfl_down_sync(0xffffffffu, v, 16);
+    q[1][1] = __shfl_down_sync(0xffffffffu, v, 17);
+    if ((lane & 1) != 0 || lane >= 16)
+        return;
+    const int x2 = x1 >> 1, y2 = y1 >> 1;
+    if (x2 >= li.w[2] || y2 >= li.h[2])
         return;
     // the 2 x 2 level-1 pixels of this output are in range (2 x2 + 1 <= 2 w2 - 1): no clamping
-    const float centre = v[0][0];
+    const float centre = q[0][0];
     float count = 0.0f, sum = 0.0f;
 #pragma unroll
     for (int i = 0; i <= 1; ++i)
 #pragma unroll
         for (int j = 0; j <= 1; ++j)
-            if (fabsf(v[i][j] - centre) < e_d) {
+            if (fabsf(q[i][j] - centre) < e_d) {
                 count += 1.0f;
-                sum += v[i][j];
+                sum += q[i][j];
             }
     d2[x2 + y2 * li.w[2]] = sum / count;
 }
@@ -1284,9 +1292,9 @@ se_gpu_status enqueue_track(se_gpu_tracker* t, const float* depth_dev, const flo
     ProfScope ps(kProfTrackPrep, stream);
     const float e_d = 0.1f * 3;
     {
-        // one thread per 2 x 2 group of level-1 pixels (a single block without a pyramid)
+        // one thread per level-1 pixel, 16 x 16 per block (a single block without a pyramid)
         const dim3 b(32, 8);
-        const dim3 g(t->levels > 1 ? ((li.w[1] + 1) / 2 + 31) / 32 : 1, t->levels > 1 ? ((li.h[1] + 1) / 2 + 7) / 8 : 1);
+        const dim3 g(t->levels > 1 ? (li.w[1] + 15) / 16 : 1, t->levels > 1 ? (li.h[1] + 15) / 16 : 1);
         launch_chained(pyramid_init_kernel, g, b, stream, t->state, init, pose_in, t->acc, li, t->levels, e_d,
                        t->pyr_depth[1], t->pyr_depth[2]);
     }
@@ -1522,8 +1530,11 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_noalloc_kernel(Pinh
     const int stride = gridDim.x * kTrackThreads;
     int i = blockIdx.x * kTrackThreads + threadIdx.x;
     bool in_range = i < npix;
-    F3 n_cur = in_range ? depth_normal(depth, s, ip.w, ip.h, i, neg_y) : f3(0.0f, 0.0f, 0.0f);
-    F3 p_cur = in_range ? depth_point(depth, s, ip.w, i) : f3(0.0f, 0.0f, 0.0f);
+    // (x, y) of pixel i, advanced with i by the grid stride
+    const int sdy = stride / ip.w, sdx = stride - sdy * ip.w;
+    int x = i % ip.w, y = i / ip.w;
+    F3 n_cur = in_range ? depth_normal(depth, s, ip.w, ip.h, x, y, neg_y) : f3(0.0f, 0.0f, 0.0f);
+    F3 p_cur = in_range ? depth_point(depth, s, ip.w, x, y) : f3(0.0f, 0.0f, 0.0f);
     float sum[32];
 #pragma unroll
     for (int k = 0; k < 32; ++k)
@@ -1532,14 +1543,21 @@ __global__ void __launch_bounds__(kTrackThreads, 3) icp_iter_noalloc_kernel(Pinh
     for (int base = blockIdx.x * kTrackThreads; base < npix; base += stride) {
         const int i_next = i + stride;
         const bool next_in = i_next < npix;
-        const F3 n_next = next_in ? depth_normal(depth, s, ip.w, ip.h, i_next, neg_y) : f3(0.0f, 0.0f, 0.0f);
-        const F3 p_next = next_in ? depth_point(depth, s, ip.w, i_next) : f3(0.0f, 0.0f, 0.0f);
+        int x_next = x + sdx, y_next = y + sdy;
+        if (x_next >= ip.w) {
+            x_next -= ip.w;
+            ++y_next;
+        }
+        const F3 n_next = next_in ? depth_normal(depth, s, ip.w, ip.h, x_next, y_next, neg_y) : f3(0.0f, 0.0f, 0.0f);
+        const F3 p_next = next_in ? depth_point(depth, s, ip.w, x_next, y_next) : f3(0.0f, 0.0f, 0.0f);
         icp_pixel_add(s, ip, T, Tri, in_range, n_cur, p_cur, sum);
         if (++rounds == kIcpFlushRounds || base + stride >= npix) { // uniform across the CTA
             icp_flush_terms(sum, sh_terms[warp], acc);
             rounds = 0;
         }
         i = i_next;
+        x = x_next;
+        y = y_next;
         in_range = next_in;
         n_cur = n_next;
         p_cur = p_next;
