@@ -559,8 +559,7 @@ def _adjoint_bench(se, torch, m, sensor, T_gt, obs, flush, reps=20, gn_steps=50,
 
     def pose_err(Ta):
         dT = np.linalg.inv(T_gt) @ Ta
-        return (float(np.linalg.norm(dT[:3, 3])),
-                float(np.degrees(np.arccos(np.clip((np.trace(dT[:3, :3]) - 1) / 2, -1, 1)))))
+        return float(np.linalg.norm(dT[:3, 3])), _rot_deg(dT[:3, :3], np.eye(3))
 
     t0, r0 = pose_err(T)
     t1, r1 = pose_err(Tk)
@@ -576,8 +575,11 @@ def _adjoint_bench(se, torch, m, sensor, T_gt, obs, flush, reps=20, gn_steps=50,
 # ------------------------------------------------------- precision against an FP64 run --
 
 def _rot_deg(Ra, Rb):
-    c = (np.trace(np.asarray(Ra, np.float64) @ np.asarray(Rb, np.float64).T) - 1.0) / 2.0
-    return float(np.degrees(np.arccos(np.clip(c, -1.0, 1.0))))
+    """Angle of Ra Rb^T in degrees: atan2 of the skew part's norm and (trace - 1) / 2, which keeps
+    small angles that arccos of (trace - 1) / 2 loses to the rounding of float32 rotations."""
+    R = np.asarray(Ra, np.float64) @ np.asarray(Rb, np.float64).T
+    s = 0.5 * float(np.linalg.norm([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]]))
+    return float(np.degrees(np.arctan2(s, (float(np.trace(R)) - 1.0) / 2.0)))
 
 
 def _precision_report(se, torch, dev, n_frames, max_blocks):

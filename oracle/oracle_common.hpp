@@ -465,24 +465,30 @@ static inline void round_pixel(float u, float v, int& x, int& y)
 
 /* e^x for x <= 0 in float operations only: Cody & Waite (1980) argument reduction
  * x = n ln2 + r with ln2 split into a 12-bit-short head and a tail, the degree-7 Taylor
- * polynomial of e^r (|r| <= ln2/2, relative error < 3e-8), then 2^n exactly. The GPU build
- * evaluates the same operations, so both round identically. */
+ * polynomial of e^r (|r| <= ln2/2, relative error < 3e-8) by Horner's rule in fused
+ * multiply-adds, then 2^n exactly. The GPU build evaluates the same operations (IEEE fused
+ * multiply-add is exactly specified), so both round identically. */
 static inline float exp_cw(float x)
 {
     if (x < -87.0f)
         return 0.0f;
     const float n = std::rint(x * 1.44269504f);
-    const float r = (x - n * 0.693145751953125f) - n * 1.42860677e-06f;
-    const float p = 1.0f
-        + r * (1.0f + r * (0.5f + r * (0.166666672f + r * (0.0416666679f + r * (0.00833333377f
-                                                     + r * (0.00138888892f + r * 0.000198412701f))))));
+    const float r = std::fmaf(-n, 1.42860677e-06f, std::fmaf(-n, 0.693145751953125f, x));
+    float p = 0.000198412701f;
+    p = std::fmaf(p, r, 0.00138888892f);
+    p = std::fmaf(p, r, 0.00833333377f);
+    p = std::fmaf(p, r, 0.0416666679f);
+    p = std::fmaf(p, r, 0.166666672f);
+    p = std::fmaf(p, r, 0.5f);
+    p = std::fmaf(p, r, 1.0f);
+    p = std::fmaf(p, r, 1.0f);
     return std::ldexp(p, (int) n);
 }
 
 /* The project-defined bilateral pre-filter of the tracking input (the reference has none):
  * invalid (<= 0 or NaN) centres stay 0; valid taps of the (2r+1)^2 window inside the image are
  * weighted by ws[dy][dx] (spatial Gaussian, host-computed) times exp_cw(-(d - c)^2 k) with
- * k = 1 / (2 sigma_r^2); the sums run dy outer, dx inner. */
+ * k = 1 / (2 sigma_r^2); the sums run dy outer, dx inner, the numerator by fused multiply-adds. */
 static inline float bilateral_pixel(const float* in, int w, int h, int x, int y, int radius, const float* ws, float k)
 {
     const float c = in[x + y * w];
@@ -503,7 +509,7 @@ static inline float bilateral_pixel(const float* in, int w, int h, int x, int y,
                 continue;
             const float diff = d - c;
             const float wgt = ws[(dy + radius) * n + (dx + radius)] * exp_cw(-(diff * diff) * k);
-            num = num + wgt * d;
+            num = std::fmaf(wgt, d, num);
             den = den + wgt;
         }
     }

@@ -4,9 +4,10 @@
 // bilateral-filtered tracking input, defined here as: invalid (<= 0 or NaN) centres stay 0;
 // the valid taps of the (2r+1)^2 window inside the image are weighted by a spatial Gaussian
 // (sigma_space pixels, weights computed in double on the host and rounded to float) times
-// exp(-(d - c)^2 / (2 sigma_range^2)); the weighted mean is summed dy outer, dx inner. The
-// exponential is evaluated in float operations only (Cody & Waite reduction and a degree-7
-// Taylor polynomial), the same operations as the CPU oracle, so both give identical images.
+// exp(-(d - c)^2 / (2 sigma_range^2)); the weighted mean is summed dy outer, dx inner, the
+// numerator by fused multiply-adds. The exponential is evaluated in float operations only (Cody &
+// Waite reduction and a degree-7 Taylor polynomial by Horner's rule in fused multiply-adds), the
+// same operations as the CPU oracle, so both give identical images.
 #include <cmath>
 
 #include "pipeline.cuh"
@@ -24,16 +25,21 @@ struct BilateralParams {
 
 // e^x for x <= 0: x = n ln2 + r with ln2 split into a head exact in 12 bits and a tail
 // (Cody & Waite, 1980), e^r by its degree-7 Taylor polynomial (|r| <= ln2/2, relative error
-// below 3e-8), then 2^n exactly.
+// below 3e-8) by Horner's rule in fused multiply-adds, then 2^n exactly.
 __device__ __forceinline__ float exp_cw(float x)
 {
     if (x < -87.0f)
         return 0.0f;
     const float n = rintf(x * 1.44269504f);
-    const float r = (x - n * 0.693145751953125f) - n * 1.42860677e-06f;
-    const float p = 1.0f
-        + r * (1.0f + r * (0.5f + r * (0.166666672f + r * (0.0416666679f + r * (0.00833333377f
-                                                     + r * (0.00138888892f + r * 0.000198412701f))))));
+    const float r = fmaf(-n, 1.42860677e-06f, fmaf(-n, 0.693145751953125f, x));
+    float p = 0.000198412701f;
+    p = fmaf(p, r, 0.00138888892f);
+    p = fmaf(p, r, 0.00833333377f);
+    p = fmaf(p, r, 0.0416666679f);
+    p = fmaf(p, r, 0.166666672f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
     // p * 2^n: n >= -126 here, so 2^n is a normal float and the product is the correctly
     // rounded value ldexp gives
     return p * __int_as_float(((int) n + 127) << 23);
@@ -77,7 +83,7 @@ __global__ void __launch_bounds__(kTileX * kTileY) bilateral_kernel(const float*
                 continue;
             const float diff = d - c;
             const float wgt = P.ws[(dy + r) * n + (dx + r)] * exp_cw(-(diff * diff) * P.k);
-            num = num + wgt * d;
+            num = fmaf(wgt, d, num);
             den = den + wgt;
         }
     }

@@ -17,8 +17,12 @@ POSE_TOL_RAD = 1e-5
 
 
 def _rot_angle(R):
-    c = (np.trace(R) - 1.0) / 2.0
-    return float(np.arccos(np.clip(c, -1.0, 1.0)))
+    """Rotation angle of R: atan2 of the skew part's norm and (trace - 1) / 2. Near the identity
+    arccos((trace - 1) / 2) is dominated by the rounding of float32 rotation matrices (a trace
+    off by 1e-7 reads as 4.5e-4 rad); the skew part carries the small angle itself."""
+    s = 0.5 * float(np.linalg.norm([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]]))
+    c = (float(np.trace(R)) - 1.0) / 2.0
+    return float(np.arctan2(s, c))
 
 
 @pytest.fixture(scope="module")
