@@ -1215,9 +1215,13 @@ se_gpu_status se_gpu_tracker_create(const se_gpu_pinhole* sensor, const se_gpu_t
         t->li.pts[l] = t->pts[l];
         t->li.nrm[l] = t->nrm[l];
         t->li.depth[l] = t->pyr_depth[l];
-        // at least four pixels per thread where the level allows (the per-warp flush and the
-        // merge of the warps' partials are fixed costs), at most one CTA per SM
-        const long long want = ((long long) w * h + 3) / 4;
+        // one pixel per thread where the level allows, at most one CTA of kIcpThreads per SM:
+        // every pixel's chain (projection, reference gather, terms) is latency-bound, so the
+        // coarse levels run fastest with all their pixels in flight at once (measured at
+        // 640x480 on GB300, ICP per frame: 4 pixels per thread at every level 118 us, 2 at
+        // levels 1-2 106 us, 1 at levels 1-2 104 us); the full-resolution level fills the
+        // grid with about four pixels per thread
+        const long long want = (long long) w * h;
         const int sms = device_sm_count() < kMaxTrackCtas ? device_sm_count() : kMaxTrackCtas;
         const long long warps = (want + 31) / 32;
         t->nctas[l] = (int) (warps < sms ? (warps > 0 ? warps : 1) : sms);
