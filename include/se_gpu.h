@@ -444,12 +444,12 @@ SE_GPU_API se_gpu_status se_gpu_track(se_gpu_tracker* tracker, const float* dept
                            const float* ref_pts_W_dev, const float* ref_nrm_W_dev,
                            float T_WS[16], int* accepted, void* stream);
 /* ICP launch shape (no counterpart in the reference): 1 (the default when the grid fits on the
- * device) runs all levels and iterations of a track() in one cooperative launch whose CTAs meet
- * at a bounded grid barrier after each iteration; 0 launches one kernel per iteration. Both
- * give bit-identical poses. A barrier that times out rejects the frame's pose (accepted = 0)
- * and se_gpu_track returns SE_GPU_ERR_CUDA. */
+ * device) runs all levels and iterations of a track() in one cooperative launch whose CTAs wait,
+ * bounded, for each iteration's merged totals to be complete; 0 launches one kernel per
+ * iteration. Both give bit-identical poses. A wait that times out rejects the frame's pose
+ * (accepted = 0) and se_gpu_track returns SE_GPU_ERR_CUDA. */
 SE_GPU_API se_gpu_status se_gpu_tracker_set_persistent(se_gpu_tracker* tracker, int enable);
-/* Test aid for the failure path: with enable != 0 the persistent ICP's grid barrier waits for
+/* Test aid for the failure path: with enable != 0 the persistent ICP waits for the partial of
  * one CTA more than the grid holds, so its bounded wait runs out (half a second), the frame's
  * pose is rejected and se_gpu_track returns SE_GPU_ERR_CUDA; the context stays usable. */
 SE_GPU_API se_gpu_status se_gpu_tracker_test_barrier_timeout(se_gpu_tracker* tracker, int enable);

@@ -681,8 +681,8 @@ class Tracker:
         _check(self._L.se_gpu_tracker_set_persistent(self.h, 1 if enable else 0), "se_gpu_tracker_set_persistent")
 
     def test_barrier_timeout(self, enable=True):
-        """Test aid: make the persistent ICP's bounded grid barrier time out (the frame's pose is
-        rejected and track() raises SeGpuError)."""
+        """Test aid: make the persistent ICP's bounded wait for the merged totals time out (the
+        frame's pose is rejected and track() raises SeGpuError)."""
         _check(self._L.se_gpu_tracker_test_barrier_timeout(self.h, 1 if enable else 0),
                "se_gpu_tracker_test_barrier_timeout")
 

@@ -33,8 +33,8 @@ enum {
     kFlagDone0 = 0,  // level converged flags 0..2
     kFlagIters0 = 3, // iterations run per level 3..5
     kFlagAccepted = 6,
-    kFlagBarrierTimeout = 7, // the persistent ICP kernel's grid barrier gave up waiting
-    kFlagOverflow = 8,       // a CTA partial outside the exact merge's range (|v| >= 2^42)
+    kFlagBarrierTimeout = 7, // the persistent ICP kernel's wait for an iteration's merged totals gave up
+    kFlagOverflow = 8,       // a CTA partial outside the exact merge's range (|v| >= 2^38)
     kNumFlags = 9
 };
 
@@ -91,8 +91,12 @@ struct CSum {
 // copies of the term (by CTA index, each copy on its own 128-byte line, to spread the atomics
 // over L2). Integer sums do not depend on the order of arrival, so the merged totals, and the
 // poses computed from them, are the same run to run and between the persistent and the
-// per-iteration kernels. A partial of magnitude 2^42 or more (or not finite) raises
-// kFlagOverflow: the pose is then rejected and the call reports an error.
+// per-iteration kernels. A partial of magnitude 2^38 or more (or not finite) raises
+// kFlagOverflow: the pose is then rejected and the call reports an error. The persistent kernel
+// adds 2^56 to both words with every partial: the top byte of a word counts the partials it has
+// received (at most 128 CTAs per copy, so the values stay below 2^55 in magnitude), and a CTA
+// knows the totals of an iteration are complete when every word's count is, without a
+// separate barrier (icp_await_totals).
 constexpr int kAccCopies = 4;
 constexpr int kAccStride = 16;                                // u64 words per (copy, term)
 constexpr size_t kAccBufWords = (size_t) kAccCopies * 32 * kAccStride;
@@ -106,7 +110,7 @@ __device__ __forceinline__ void fixed_split(float f, long long& I, unsigned long
     const int ee = e ? e : 1; // |f| = m 2^(ee - 150)
     I = 0;
     F = 0;
-    if (e == 0xff || ee > 168) {
+    if (e == 0xff || ee > 164) { // |f| >= 2^38: |I| could reach 2^48
         bad = true;
         return;
     }
@@ -132,7 +136,8 @@ __device__ __forceinline__ void fixed_split(float f, long long& I, unsigned long
     }
 }
 
-__device__ __forceinline__ void acc_add(unsigned long long* buf, int copy, int term, float hi, float lo, bool& bad)
+__device__ __forceinline__ void acc_add(unsigned long long* buf, int copy, int term, float hi, float lo, bool& bad,
+                                        unsigned long long count = 0)
 {
     long long I1, I2;
     unsigned long long F1, F2;
@@ -141,8 +146,25 @@ __device__ __forceinline__ void acc_add(unsigned long long* buf, int copy, int t
     unsigned long long* p = buf + ((size_t) copy * 32 + term) * kAccStride;
     // reductions without a returned value: the issuing thread does not wait for them (the grid
     // barrier's release orders them before the arrival)
-    asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"((unsigned long long) (I1 + I2)) : "memory");
-    asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p + 1), "l"(F1 + F2) : "memory");
+    asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"((unsigned long long) (I1 + I2) + count)
+                 : "memory");
+    asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p + 1), "l"(F1 + F2 + count) : "memory");
+}
+
+// The total A 2^-10 + B 2^-50 of a term's merged integer sums.
+__device__ __forceinline__ double acc_total_of(long long A, unsigned long long B)
+{
+    // A 2^-10 and B 2^-50 as doubles without a 64-bit integer conversion: an integer added to the
+    // bits of 1.5 2^k (|integer| < 2^51) gives 1.5 2^k + integer 2^(k-52) exactly, and subtracting
+    // 1.5 2^k leaves the scaled integer (k = 42: units of 2^-10; k = 2: units of 2^-50). The sum of
+    // the two rounds once, like fma((double) B, 2^-50, (double) A 2^-10).
+    const long long kMagic10 = 0x4298000000000000LL, kMagic50 = 0x4018000000000000LL;
+    const double hi = (A > -(1LL << 51) && A < (1LL << 51))
+        ? __longlong_as_double(kMagic10 + A) - __longlong_as_double(kMagic10)
+        : (double) A * 0x1p-10;
+    const double lo = B < (1ULL << 51) ? __longlong_as_double(kMagic50 + (long long) B) - __longlong_as_double(kMagic50)
+                                       : (double) B * 0x1p-50;
+    return hi + lo;
 }
 
 __device__ __forceinline__ double acc_total(const unsigned long long* buf, int term)
@@ -155,17 +177,7 @@ __device__ __forceinline__ double acc_total(const unsigned long long* buf, int t
         A += (long long) __ldcg(p);
         B += __ldcg(p + 1);
     }
-    // A 2^-10 and B 2^-50 as doubles without a 64-bit integer conversion: an integer added to the
-    // bits of 1.5 2^k (|integer| < 2^51) gives 1.5 2^k + integer 2^(k-52) exactly, and subtracting
-    // 1.5 2^k leaves the scaled integer (k = 42: units of 2^-10; k = 2: units of 2^-50). The sum of
-    // the two rounds once, like fma((double) B, 2^-50, (double) A 2^-10).
-    const long long kMagic10 = 0x4298000000000000LL, kMagic50 = 0x4018000000000000LL;
-    const double hi = (A > -(1LL << 51) && A < (1LL << 51))
-        ? __longlong_as_double(kMagic10 + A) - __longlong_as_double(kMagic10)
-        : (double) A * 0x1p-10;
-    const double lo = B < (1ULL << 51) ? __longlong_as_double(kMagic50 + (long long) B) - __longlong_as_double(kMagic50)
-                                       : (double) B * 0x1p-50;
-    return hi + lo;
+    return acc_total_of(A, B);
 }
 
 // Zeroes the two words of every (copy, term) of a buffer, threads tid of nthreads.
@@ -825,12 +837,16 @@ __device__ __forceinline__ void icp_first_pair(const IterParams& ip, int cta, Ic
 
 // This CTA's share of one ICP iteration: its pixels' terms summed and merged exactly into the
 // global accumulators buf (copy cta % kAccCopies). Threads tid < ip.nthr of CTAs cta < ip.ncta
-// hold pixels (at least four per thread where the level allows: the per-warp flush and the
-// merge are fixed costs); (a, b) is the thread's first pair (icp_first_pair). Every thread of
-// the CTA calls it; ends with a CTA barrier. Warp 0 merges the warps' compensated partials of
-// term k (lane k) in warp order.
+// hold pixels (one per thread at the coarse levels, about four at full resolution); (a, b) is
+// the thread's first pair (icp_first_pair). Every thread of the CTA calls it; ends with a CTA
+// barrier. Warp 0 merges the warps' compensated partials of term k (lane k) in warp order. With
+// counted set (the persistent kernel) every CTA adds, those without pixels zeros, and each
+// addition carries the count kAccCount.
+constexpr unsigned long long kAccCount = 1ull << 56;
+
 __device__ __forceinline__ void icp_cta_pass(const Pinhole& s, const IterParams& ip, const Tf T, const Tf Tri,
-                                             int cta, unsigned long long* buf, int* overflow_flag, IcpIn a, IcpIn b)
+                                             int cta, unsigned long long* buf, int* overflow_flag, IcpIn a, IcpIn b,
+                                             bool counted)
 {
     extern __shared__ float icp_dyn_smem[]; // kIcpDynSmem bytes: the warps' term matrices
     __shared__ float2 sh_warp[kIcpWarps][32];
@@ -874,9 +890,12 @@ __device__ __forceinline__ void icp_cta_pass(const Pinhole& s, const IterParams&
     if (active && lane < 4 && cnt[lane] != 0)
         atomicAdd(&sh_cnt[lane], cnt[lane]);
     __syncthreads();
-    if (warp == 0 && cta < ip.ncta) {
-        float hi, lo;
-        if (lane < 28) {
+    if (warp == 0 && (counted || cta < ip.ncta)) {
+        float hi = 0.0f, lo = 0.0f;
+        if (cta >= ip.ncta) {
+            // no pixels at this level: zeros, so that the counts stay those of the whole grid
+        }
+        else if (lane < 28) {
             CSum t{0.0f, 0.0f};
             const int nw = ip.nthr >> 5;
             for (int wi = 0; wi < nw; ++wi)
@@ -889,7 +908,7 @@ __device__ __forceinline__ void icp_cta_pass(const Pinhole& s, const IterParams&
             lo = 0.0f;
         }
         bool bad = false;
-        acc_add(buf, cta % kAccCopies, lane, hi, lo, bad);
+        acc_add(buf, cta % kAccCopies, lane, hi, lo, bad, counted ? kAccCount : 0ull);
         if (bad)
             atomicExch(overflow_flag, 1);
     }
@@ -941,7 +960,7 @@ __global__ void __launch_bounds__(kIcpThreads, 1) icp_iter_kernel(Pinhole s, Ite
     const Tf Tl = T, Tril = Tri;
     IcpIn a, b;
     icp_first_pair(ip, blockIdx.x, a, b);
-    icp_cta_pass(s, ip, Tl, Tril, blockIdx.x, acc_buf, &st->flags[kFlagOverflow], a, b);
+    icp_cta_pass(s, ip, Tl, Tril, blockIdx.x, acc_buf, &st->flags[kFlagOverflow], a, b, false);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0)
@@ -979,7 +998,7 @@ __global__ void __launch_bounds__(kIcpThreads, 1) icp_iter_kernel(Pinhole s, Ite
 __device__ void icp_check(TrackState* st, int W, int H, float track_threshold, float* pose12_out)
 {
     const float* v = st->last_red;
-    // a timed-out grid barrier of the persistent ICP leaves no trustworthy pose: reject it
+    // a timed-out wait for the totals of the persistent ICP leaves no trustworthy pose: reject it
     const bool reject = ((double) sqrtf(v[0] / v[28]) > 2e-2) || (v[28] / (float) (W * H) < track_threshold)
         || st->flags[kFlagBarrierTimeout] != 0 || st->flags[kFlagOverflow] != 0;
     if (reject) {
@@ -1001,11 +1020,12 @@ __global__ void icp_check_kernel(TrackState* st, int W, int H, float track_thres
 
 // ------------------------------------------------------- persistent ICP (all iterations) --
 // The per-iteration launches above, fused into one cooperative launch per frame, one CTA per
-// SM: every CTA runs every iteration of every level; after each iteration's pass the CTAs meet
-// at a grid barrier, and each CTA then reads the exact totals and solves redundantly (the same
-// operations on the same values, so every CTA holds the same new pose) instead of one last CTA
-// solving and the next launch reading its result. The pixel partition, the exact merge and the
-// FP64 tail are those of icp_iter_kernel, so the poses are bit-identical to it.
+// SM: every CTA runs every iteration of every level; after each iteration's pass every CTA waits
+// until the merged totals are complete (the count bytes of the accumulator words, no separate
+// barrier), reads them and solves redundantly (the same operations on the same values, so every
+// CTA holds the same new pose) instead of one last CTA solving and the next launch reading its
+// result. The pixel partition, the exact merge's integer totals and the FP64 tail are those of
+// icp_iter_kernel, so the poses are bit-identical to it.
 
 struct IcpLevels {
     IterParams ip[3];
@@ -1028,31 +1048,71 @@ __device__ __forceinline__ unsigned long long global_ns()
     return t;
 }
 
-// Grid barrier on a monotonic counter (reset to 0 before the launch): after a CTA barrier (the
-// CTA's atomics precede it), one thread adds its arrival with release semantics and polls with
-// acquire loads until the count reaches target; the CTA barrier after it orders every thread's
-// later reads of the merged totals. Bounded: on timeout (or when another CTA timed out) the flag
-// is set and the CTA goes on, so a stuck launch ends with an error instead of hanging.
-__device__ __forceinline__ void icp_grid_sync(unsigned* ctr, unsigned target, int* timeout)
+// The merged totals of one iteration of the persistent kernel, awaited by warp 0 of every CTA in
+// place of a grid barrier: lane k reads the two words of term k in the four copies (relaxed
+// loads at GPU scope, all in flight together) until every word's count byte has advanced, since
+// this buffer's previous use (prev, this CTA's copy of the words then, in shared memory), by the
+// number of CTAs that add into that copy (the grid's CTAs of that residue; copy 0 waits for
+// `missing` more, a test aid); the totals are the advances less their counts. The buffers are
+// never cleared within a launch: a CTA adds to a buffer again only three iterations later, after
+// every CTA's additions of the two iterations between, which every CTA makes only after it has
+// read this one. Bounded: on timeout (or when another CTA timed out) the flag is set and the CTA
+// goes on with what has arrived, so a stuck launch ends with an error instead of hanging.
+__device__ __forceinline__ void icp_await_totals(const unsigned long long* buf, unsigned long long (*prev)[32],
+                                                 int ngrid, int missing, double* sh_val, TrackState* st,
+                                                 bool record, int* timeout)
 {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctr) : "memory");
-        unsigned spins = 0;
-        const unsigned long long t0 = global_ns();
-        while (true) {
-            unsigned v;
-            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
-            if (v >= target)
-                break;
-            if ((++spins & 63u) == 0u
-                && (*((volatile int*) timeout) != 0 || spins > kIcpSpinLimit || global_ns() - t0 > kIcpWaitNs)) {
-                atomicExch(timeout, 1);
+    if (threadIdx.x >= 32)
+        return;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x;
+    unsigned long long w[kAccCopies][2];
+    long long A = 0;
+    unsigned long long B = 0;
+    unsigned spins = 0;
+    const unsigned long long t0 = global_ns();
+    while (true) {
+#pragma unroll
+        for (int c = 0; c < kAccCopies; ++c) {
+            const unsigned long long* p = buf + ((size_t) c * 32 + lane) * kAccStride;
+            asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(w[c][0]) : "l"(p) : "memory");
+            asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(w[c][1]) : "l"(p + 1) : "memory");
+        }
+        bool ok = true;
+        A = 0;
+        B = 0;
+#pragma unroll
+        for (int c = 0; c < kAccCopies; ++c) {
+            const unsigned long long n =
+                (unsigned long long) ((ngrid - c + kAccCopies - 1) / kAccCopies + (c == 0 ? missing : 0)) & 0xffull;
+            const unsigned long long dI = w[c][0] - prev[2 * c][lane], dF = w[c][1] - prev[2 * c + 1][lane];
+            const unsigned long long cI = (dI + (kAccCount >> 1)) >> 56, cF = (dF + (kAccCount >> 1)) >> 56;
+            ok = ok && cI == n && cF == n;
+            A += (long long) (dI - (cI << 56));
+            B += dF - (cF << 56);
+        }
+        if (__all_sync(full, ok))
+            break;
+        // uniform across the warp: spins is, and the decision is the warp's
+        if ((++spins & 15u) == 0u) {
+            const bool give_up = *((volatile int*) timeout) != 0 || spins > kIcpSpinLimit
+                || global_ns() - t0 > kIcpWaitNs;
+            if (__any_sync(full, give_up)) {
+                if (lane == 0)
+                    atomicExch(timeout, 1);
                 break;
             }
         }
     }
-    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < kAccCopies; ++c) {
+        prev[2 * c][lane] = w[c][0];
+        prev[2 * c + 1][lane] = w[c][1];
+    }
+    const double v = acc_total_of(A, B);
+    sh_val[lane] = v;
+    if (record)
+        st->last_red[lane] = (float) v;
 }
 
 __global__ void __launch_bounds__(kIcpThreads, 1) icp_persistent_kernel(Pinhole s, IcpLevels L, TrackState* st,
@@ -1064,10 +1124,15 @@ __global__ void __launch_bounds__(kIcpThreads, 1) icp_persistent_kernel(Pinhole 
     __shared__ float sh_newf[12];
     __shared__ double sh_val[32];
     __shared__ int sh_conv;
+    // the accumulator words as this CTA last read them, per buffer (zero: the tracker's state
+    // init clears the buffers before the launch)
+    __shared__ unsigned long long sh_prev[kAccBuffers][2 * kAccCopies][32];
+    for (int i = threadIdx.x; i < kAccBuffers * 2 * kAccCopies * 32; i += blockDim.x)
+        (&sh_prev[0][0][0])[i] = 0ull;
     icp_pose_to_shared(st, T, Tri, sh_pose);
-    // the first pair of the next pass is loaded before the barrier and the tail of the current
-    // iteration (its inputs do not depend on the pose), assuming the level goes on; a level that
-    // converges early reloads it
+    // the first pair of the next pass is loaded before the wait for the totals and the tail of the
+    // current iteration (its inputs do not depend on the pose), assuming the level goes on; a
+    // level that converges early reloads it
     int pf_level = L.levels - 1;
     IcpIn pa, pb;
     icp_first_pair(L.ip[pf_level], blockIdx.x, pa, pb);
@@ -1081,19 +1146,15 @@ __global__ void __launch_bounds__(kIcpThreads, 1) icp_persistent_kernel(Pinhole 
                 icp_first_pair(ip, blockIdx.x, pa, pb);
             {
                 const Tf Tl = T, Tril = Tri; // the poses in registers for the pass
-                icp_cta_pass(s, ip, Tl, Tril, blockIdx.x, buf, &st->flags[kFlagOverflow], pa, pb);
+                icp_cta_pass(s, ip, Tl, Tril, blockIdx.x, buf, &st->flags[kFlagOverflow], pa, pb, true);
             }
             pf_level = iter + 1 < L.iters[level] ? level : level - 1;
             if (pf_level >= 0)
                 icp_first_pair(L.ip[pf_level], blockIdx.x, pa, pb);
+            // every CTA: the merged totals, once complete, then the solve and update
+            icp_await_totals(buf, sh_prev[phase % kAccBuffers], gridDim.x, L.missing_ctas, sh_val, st,
+                             blockIdx.x == 0, &st->flags[kFlagBarrierTimeout]);
             ++phase;
-            icp_grid_sync(&st->ticket, phase * (gridDim.x + L.missing_ctas), &st->flags[kFlagBarrierTimeout]);
-            // every CTA: the merged totals, then the solve and update. The buffer used two phases
-            // ago has been read by every CTA before this barrier: CTA 0 clears it for the phase
-            // after next.
-            icp_read_totals(buf, sh_val, st, blockIdx.x == 0);
-            if (blockIdx.x == 0)
-                acc_clear(acc_base + (size_t) ((phase + 1) % kAccBuffers) * kAccBufWords, threadIdx.x, blockDim.x);
             __syncthreads();
             icp_tail(sh_val, sh_pose, sh_new, sh_newf, &sh_conv, ip.icp_threshold);
             if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -1174,7 +1235,8 @@ static cudaError_t icp_persistent_fits(int ctas, bool& fits)
     int per_sm = 0;
     const cudaError_t e =
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, icp_persistent_kernel, kIcpThreads, kIcpDynSmem);
-    fits = e == cudaSuccess && per_sm * device_sm_count() >= ctas;
+    // the count byte of the exact merge's words holds at most 128 CTAs per copy
+    fits = e == cudaSuccess && per_sm * device_sm_count() >= ctas && ctas <= kAccCopies * 128;
     return e;
 }
 } // namespace se_gpu
@@ -1392,7 +1454,7 @@ se_gpu_status se_gpu_track(se_gpu_tracker* t, const float* depth_dev, const floa
     if (accepted)
         *accepted = hs.flags[kFlagAccepted];
     if (hs.flags[kFlagBarrierTimeout]) {
-        set_last_error("se_gpu_track: the ICP grid barrier timed out (the pose was reverted)");
+        set_last_error("se_gpu_track: the ICP's wait for the merged totals timed out (the pose was reverted)");
         return SE_GPU_ERR_CUDA;
     }
     if (hs.flags[kFlagOverflow]) {

@@ -1,7 +1,7 @@
 """The persistent ICP (all levels and iterations of a track() in one cooperative launch, CTAs
-meeting at a bounded grid barrier) against the one-launch-per-iteration ICP: poses, final
-reductions and iteration counts bit-identical, on a converging and on a non-converging
-(threshold 0) configuration."""
+waiting, bounded, for each iteration's merged totals) against the one-launch-per-iteration ICP:
+poses, final reductions and iteration counts bit-identical, on a converging and on a
+non-converging (threshold 0) configuration."""
 import numpy as np
 import pytest
 
@@ -42,7 +42,7 @@ def test_persistent_equals_per_iteration(gpu, icp_threshold):
 @pytest.mark.parametrize("persistent", [True, False])
 def test_merge_overflow_is_reported(gpu, persistent):
     """A partial sum outside the exact merge's range (here: a fronto-parallel plane 3e5 m from
-    the world origin, so that |p_W x n|^2 summed over a CTA's 256 pixels exceeds 2^42) is not
+    the world origin, so that |p_W x n|^2 summed over a CTA's 256 pixels exceeds 2^38) is not
     silently wrapped: the call reports an error and the pose stays the input pose."""
     import torch
     W, H = 128, 96
@@ -71,9 +71,9 @@ def test_merge_overflow_is_reported(gpu, persistent):
 
 
 def test_barrier_timeout_is_reported(gpu):
-    """The persistent ICP's grid barrier is bounded: made to wait for a CTA that does not exist,
-    it gives up after half a second, the pose is rejected and the call reports the timeout; the
-    context stays usable and the next track succeeds."""
+    """The persistent ICP's wait for the merged totals is bounded: made to wait for a CTA that
+    does not exist, it gives up after half a second, the pose is rejected and the call reports the
+    timeout; the context stays usable and the next track succeeds."""
     import time
     import torch
     from supereight2_gb300 import synthetic as syn
