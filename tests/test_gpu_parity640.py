@@ -10,8 +10,9 @@ checked on its own:
     normals at all three levels) are bit-identical;
   - the tracked pose is within 1e-5 m / 1e-5 rad of the oracle's track (tracker_impl.hpp:30-116,
     icp.cpp:45-246), acceptance equal, inlier counts within 1e-4, iterations per level within one
-    (where the convergence test |x| < 1e-5 falls the other way, against the oracle run for the
-    GPU's iteration counts); on a frame where the ICP sits at its convergence floor (the two stop
+    of the range the oracle's own variants (other start poses and summation orders) run (where
+    the convergence test |x| < 1e-5 falls the other way, against the oracle run for the GPU's
+    iteration counts); on a frame where the ICP sits at its convergence floor (the two stop
     a level one iteration apart, or the oracle's own results from start poses one float step away,
     or with its sums in other orders, spread by more than half the bar) within two threshold-sized
     updates and twice that spread;
@@ -81,19 +82,22 @@ def run640(oracle, gpu):
             # each translation component, and with its ICP sums in other orders (other thread
             # counts: the GPU's reductions sum in yet another order)
             spread_t = spread_r = 0.0
+            its_var = [list(st_o.converged_iterations)]
             for a in range(3):
                 for direction in (np.inf, -np.inf):
                     T_p = T_o.copy()
                     T_p[a, 3] = np.nextafter(T_p[a, 3], np.float32(direction))
-                    _, T_q, _ = oracle.track(os_, cfg_o, fo, T_p, op, on)
+                    _, T_q, st_q = oracle.track(os_, cfg_o, fo, T_p, op, on)
                     dt_q, dr_q = _pose_diff(T_q, T_new)
                     spread_t, spread_r = max(spread_t, dt_q), max(spread_r, dr_q)
+                    its_var.append(list(st_q.converged_iterations))
             n_threads = oracle.num_threads()
             for nt in (1, 2, 3, 4, 6, 12, 16):
                 oracle.set_num_threads(nt)
-                _, T_q, _ = oracle.track(os_, cfg_o, fo, T_o, op, on)
+                _, T_q, st_q = oracle.track(os_, cfg_o, fo, T_o, op, on)
                 dt_q, dr_q = _pose_diff(T_q, T_new)
                 spread_t, spread_r = max(spread_t, dt_q), max(spread_r, dr_q)
+                its_var.append(list(st_q.converged_iterations))
             oracle.set_num_threads(n_threads)
             # the GPU tracks from the same start pose against the oracle's reference images
             pts.copy_(torch.from_numpy(op))
@@ -111,7 +115,9 @@ def run640(oracle, gpu):
                 red_cmp = st_f.reduction
             rec["track"].append(dict(frame=k, acc=(acc_g, acc_o), T=(T_g, T_cmp.astype(np.float32)),
                                      T_oracle=T_new.astype(np.float32), spread=(spread_t, spread_r),
-                                     its=(list(its_g), its_o),
+                                     its=(list(its_g), its_o), its_oracle_range=(
+                                         [min(v[l] for v in its_var) for l in range(3)],
+                                         [max(v[l] for v in its_var) for l in range(3)]),
                                      inliers=(float(red_g[28]), float(red_cmp[28]))))
             pyr_o = oracle.tracker_pyramid(os_, fo, 3)
             levels = []
@@ -186,9 +192,13 @@ def test_tracked_pose_per_frame(run640):
         assert dt <= tol_t, (t["frame"], dt, spread_t)
         assert dr <= tol_r, (t["frame"], dr, spread_r)
         # the convergence test |x| < 1e-5 can fall either side of the threshold between the
-        # FP64 solve and the oracle's FP32 one: then the level runs one iteration more or less and
-        # T_o above is the oracle run for the GPU's iteration counts
-        assert all(abs(a - b) <= 1 for a, b in zip(*t["its"])), (t["frame"], t["its"])
+        # FP64 solve and the oracle's FP32 one: then the level runs a different number of
+        # iterations and T_o above is the oracle run for the GPU's iteration counts. At the floor
+        # the oracle's own count moves with its summation order (frame 1 of this trajectory
+        # stops level 0 after 3 to 7 iterations with 1 to 16 threads): the GPU's count lies
+        # within one of the range of the oracle's own variants
+        lo, hi = t["its_oracle_range"]
+        assert all(lo[l] - 1 <= t["its"][0][l] <= hi[l] + 1 for l in range(3)), (t["frame"], t["its"], lo, hi)
     # the floor is decided by the oracle's own sensitivity (its thread count changes its sums) and
     # by iteration-count flips, never by the GPU's pose error; several frames stay on the bar itself
     assert len(run640["track"]) - floor_frames >= 3, floor_frames
