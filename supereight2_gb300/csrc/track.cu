@@ -1,18 +1,21 @@
 // track.cu — se::Tracker::track: projective point-to-plane ICP over a 3-level depth pyramid.
 //
 // Per frame: half_sample_robust_image x2, depth_to_point_cloud and point_cloud_to_normal for the
-// three levels, then one fused launch per ICP iteration (coarse to fine, {4, 5, 10} by default):
+// three levels, then the ICP iterations (coarse to fine, {4, 5, 10} by default):
 //   - every thread evaluates trackKernel for a strided set of pixels (icp_impl.hpp:16-102) and
 //     accumulates the 32 reduction values of newReduce (icp.cpp:45-184) in FP32 with two-sum
 //     compensation (hi, lo pairs);
 //   - shared memory gives one compensated partial per CTA, which the CTA adds exactly (integer
 //     fixed point, order-independent) into global accumulators;
-//   - the last CTA to finish (atomic ticket, no waiting) reads the totals, solves the 6x6 normal
-//     equations by FP64 elimination, applies the FP64 se(3) exponential and composes the pose in
-//     FP64 (icp.cpp:15-41,208-223, math_util_impl.hpp:117-174), and raises the level's
-//     convergence flag when |x| < threshold.
-// Later iterations of a converged level return at entry, so the launch sequence is fixed and
-// can be captured in a CUDA graph. checkPoseKernel (icp.cpp:227-246) runs in a final kernel.
+//   - the totals give the 6x6 normal equations, solved by FP64 elimination; the FP64 se(3)
+//     exponential is applied and the pose composed in FP64 (icp.cpp:15-41,208-223,
+//     math_util_impl.hpp:117-174), and the level stops when |x| < threshold.
+// By default one cooperative launch per frame runs every iteration (icp_persistent_kernel: each
+// CTA waits for the complete totals and solves redundantly) and checkPoseKernel
+// (icp.cpp:227-246) at its end. Where that grid cannot be resident at once, one launch per
+// iteration (icp_iter_kernel: the last CTA to finish, by an atomic ticket, solves; later
+// iterations of a converged level return at entry, so the launch sequence is fixed and can be
+// captured in a CUDA graph) and a final check kernel give the same poses bit for bit.
 #include <cmath>
 #include <cstddef>
 #include <cstring>
