@@ -73,3 +73,26 @@ def test_se3_exp_small_and_general(oracle):
     V = np.eye(3) + (1 - math.cos(th)) / th ** 2 * K + (th - math.sin(th)) / th ** 3 * K @ K
     assert np.allclose(T[:3, :3], R, atol=2e-6)
     assert np.allclose(T[:3, 3], V @ tw[:3], atol=2e-6)
+
+
+def test_multires_interpolation_known_answers(oracle):
+    # octree_visitor_unittest.cpp:114-200 (TEST(VisitorTSDFMultiRes, Interpolation)): a 32^3 octree
+    # whose eight blocks of the 16^3 corner hold, at their current scale 1, the value of their
+    # index; interpolation at scale 1 across block borders gives the reference's answers, and
+    # outside the allocated blocks nothing. Voxel coordinates are the map's (1 m voxels, the
+    # world origin at the map centre).
+    m = oracle.OracleMap(32.0, 1.0, multires=True)
+    for i, c in enumerate(rc.INTERP_BLOCKS):
+        tsdf = np.ones(585, np.float32)
+        weight = np.zeros(585, np.float32)
+        tsdf[512:576] = float(i)
+        weight[512:576] = 1.0
+        m.set_mr_block(c, tsdf, weight, 1, -1)
+    cases = [((2, 2, 2), 0.0), ((8, 2, 2), 0.5), ((2, 8, 2), 1.0), ((8, 8, 2), 1.5), ((2, 2, 8), 2.0),
+             ((8, 2, 8), 2.5), ((2, 8, 8), 3.0), ((8, 8, 8), 3.5), ((16, 16, 16), None)]
+    for v, want in cases:
+        got = m.field_interp(np.array(v, np.float32) - np.float32(16.0))
+        if want is None:
+            assert got is None, v
+        else:
+            assert got == want, (v, got, want)
