@@ -52,8 +52,19 @@ void scale_rgb(int scale, int rgb[3])
     rgb[2] = c[2];
 }
 
+// io::has_supported_mesh_extension (src/map/io/mesh_io.cpp:13-21): .ply, .vtk, .obj
+bool supported_mesh_extension(const std::string& path)
+{
+    return ends_with(path, ".ply") || ends_with(path, ".vtk") || ends_with(path, ".obj");
+}
+
 se_gpu_status write_mesh(const float* faces, const int8_t* scales, int64_t n, const float* T, const std::string& path)
 {
+    // an unsupported name is refused before any file is created
+    if (!supported_mesh_extension(path)) {
+        set_last_error("unknown mesh file extension (.ply, .vtk or .obj): %s", path.c_str());
+        return SE_GPU_ERR_BAD_ARG;
+    }
     File out(path.c_str());
     if (!out.f) {
         set_last_error("cannot write %s", path.c_str());

@@ -39,6 +39,21 @@ def test_mesh_formats(tmp_path):
         se.save_mesh(f, tmp_path / "m.stl", T)
 
 
+def test_supported_mesh_extensions(tmp_path):
+    """mesh_io_unittest.cpp (MeshIO.hasSupportedMeshExtension): .ply, .vtk and .obj names are
+    written, a bare ".ply" included; other names (an image extension, the empty name) are refused
+    before any file is created."""
+    se = pytest.importorskip("supereight2_gb300")
+    f, T = _faces(), _T()
+    for name in ("foo.ply", "bar.vtk", "bar.obj", ".ply"):
+        se.save_mesh(f, tmp_path / name, T)
+        assert (tmp_path / name).stat().st_size > 0
+    for name in ("foo.png", ""):
+        with pytest.raises(se.SeGpuError):
+            se.save_mesh(f, str(tmp_path / name) if name else name, T)
+    assert not (tmp_path / "foo.png").exists()
+
+
 def test_mesh_face_scales(tmp_path):
     """Multi-res meshes carry a scale per face: the VTK cell data lists it, the PLY face colour
     follows it (io::save_mesh's scale_colour)."""
