@@ -49,7 +49,8 @@ class TrackStats(C.Structure):
 def lib():
     global _lib
     if _lib is None:
-        path = _build.build()
+        # SE_ORACLE_LIB: another build of the same sources (the sanitizer test's)
+        path = os.environ.get("SE_ORACLE_LIB") or _build.build()
         L = C.CDLL(path)
         f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
         u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
