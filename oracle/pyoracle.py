@@ -71,6 +71,7 @@ def lib():
             "so_occ_map_create_cfg": (vp, [f32p, C.c_float, vp, vp]),
             "so_occ_get_data": (None, [vp, f32p, f32p]),
             "so_occ_get_field_interp": (C.c_int, [vp, f32p, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
+            "so_occ_get_field_grad": (C.c_int, [vp, f32p, f32p]),
             "so_occ_map_size": (C.c_int, [vp]),
             "so_occ_integrate_depth": (None, [vp, f32p, C.POINTER(Pinhole), f32p, C.c_int,
                                               C.POINTER(OccStats)]),
@@ -218,6 +219,12 @@ class OracleOccMap:
         v, sc = C.c_float(), C.c_int()
         ok = lib().so_occ_get_field_interp(self.h, np.ascontiguousarray(p, np.float32), C.byref(v), C.byref(sc))
         return (v.value, sc.value) if ok else None
+
+    def get_field_grad(self, p):
+        """Map::getFieldGrad(point): f32[3] or None."""
+        g = np.zeros(3, np.float32)
+        ok = lib().so_occ_get_field_grad(self.h, np.ascontiguousarray(p, np.float32), g)
+        return g if ok else None
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -167,6 +167,7 @@ void so_occ_map_destroy(so_occ_map* map);
  * observed); the interpolation returns 0 for nullopt. */
 void so_occ_get_data(const so_occ_map* map, const float point_W[3], float out[3]);
 int so_occ_get_field_interp(const so_occ_map* map, const float point_W[3], float* value, int* scale);
+int so_occ_get_field_grad(const so_occ_map* map, const float point_W[3], float grad[3]);
 int so_occ_map_size(const so_occ_map* map);
 /* MapIntegrator<OccupancyMap<Res::Multi>>::integrateDepth for a pinhole camera. */
 void so_occ_integrate_depth(so_occ_map* map, const float* depth, const so_pinhole* sensor,

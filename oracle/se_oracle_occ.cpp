@@ -2395,6 +2395,20 @@ int so_occ_get_field_interp(const so_occ_map* mp, const float p[3], float* value
     return 1;
 }
 
+/* Map::getFieldGrad(point) (Safe::Off, map_impl.hpp:238-265): the multi-res gradient at the point's
+ * voxel coordinates, divided by the resolution. Returns 0 for nullopt. */
+int so_occ_get_field_grad(const so_occ_map* mp, const float p[3], float g[3])
+{
+    const V3 pm = apply(mp->T_MW, v3(p[0], p[1], p[2]));
+    V3 gv;
+    if (!occ_grad(*mp, pm / mp->res, gv))
+        return 0;
+    g[0] = gv.x / mp->res;
+    g[1] = gv.y / mp->res;
+    g[2] = gv.z / mp->res;
+    return 1;
+}
+
 /* MapIntegrator<OccupancyMap<Res::Multi>>::integrateDepth after the sensor-specific frame set-up:
  * sigma image, pooling images, VolumeCarver, Updater (map_integrator_impl.hpp:96-125). */
 static void occ_integrate_frame(so_occ_map& m, Frame& f, const float* depth, const float T_WC[16], float far_plane,

@@ -99,3 +99,50 @@ def test_raycast_finds_the_wall(oracle):
     n_ok = (nrm != 0).any(-1) & hit
     assert n_ok.mean() > 0.5
     assert np.median(nrm[n_ok][:, 2]) < -0.9   # normals face the camera (-z)
+
+
+def test_map_gradient_reference_cases(oracle):
+    """map_unittest.cpp:11-113 (TEST(Map, Gradient)): a 32 m occupancy map at 3 cm, a 640x480
+    pinhole downsampled by 2 (fx 262.5, near 0.4 m, far 20 m) at the identity pose integrates a
+    uniform 15 m depth image with the test's field parameters. In free space (z = 4, 6, 8 m) the
+    interpolated occupancy is log_odd_min and the gradient zero; in the linear part of the inverse
+    sensor model (z = 14.85 ... 15 m) the gradient matches central differences of the
+    interpolation (step res / 10) within 1e-2; behind the surface (z = 15.35 m) the occupancy is
+    positive and the gradient zero."""
+    def float_eq(a, b):
+        # googletest's EXPECT_FLOAT_EQ: within 4 units in the last place
+        ia, ib = (int(np.array(x, np.float32).view(np.int32)) for x in (a, b))
+        ia, ib = (x if x >= 0 else -(x & 0x7fffffff) for x in (ia, ib))
+        return abs(ia - ib) <= 4
+
+    cfg = dict(tau_min_factor=20.0, tau_max_factor=20.0, k_tau=1.0, sigma_min_factor=1.0,
+               sigma_max_factor=3.0, k_sigma=0.05)
+    res = 0.03
+    m = oracle.OracleOccMap(32.0, res, **cfg)
+    s = oracle.pinhole(320, 240, 262.5, 262.5, (319.5 + 0.5) / 2 - 0.5, (239.5 + 0.5) / 2 - 0.5, 0.4, 20.0)
+    m.integrate_depth(np.full((240, 320), 15.0, np.float32), s, np.eye(4, dtype=np.float32), 0)
+    for z in (4.0, 6.0, 8.0):
+        p = np.array([0.0, 0.0, z], np.float32)
+        v = m.get_field_interp(p)
+        assert v is not None and float_eq(v[0], -5.015), v
+        g = m.get_field_grad(p)
+        assert g is not None and float_eq(np.linalg.norm(g), 0.0), g
+    delta = np.float32(res / 10)
+    for z in (14.85, 14.90, 14.95, 15.00):
+        p = np.array([0.0, 0.0, z], np.float32)
+        num = np.zeros(3, np.float32)
+        for i in range(3):
+            d = np.zeros(3, np.float32)
+            d[i] = delta
+            vm, vp = m.get_field_interp(p - d), m.get_field_interp(p + d)
+            assert vm is not None and vp is not None
+            if abs(vp[0] - vm[0]) > 1e-6:
+                num[i] = (vp[0] - vm[0]) / (2 * delta)
+        g = m.get_field_grad(p)
+        assert g is not None
+        assert np.all(np.abs(num - g) <= 1e-2), (z, num, g)
+    p = np.array([0.0, 0.0, 15.35], np.float32)
+    v = m.get_field_interp(p)
+    assert v is not None and v[0] > 0.0
+    g = m.get_field_grad(p)
+    assert g is not None and float_eq(np.linalg.norm(g), 0.0), g
