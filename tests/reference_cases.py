@@ -79,3 +79,22 @@ def check_wall_aabb(vmin, vmax, truncation_boundary_factor=8.0):
     assert np.isclose(hi[2], hi[1], rtol=0, atol=4e-6)
     assert dim_to_blocks(float(lo[1]), block_dim) == -half_wall_blocks
     assert dim_to_blocks(float(hi[1]), block_dim) == half_wall_blocks
+
+
+def check_wall_aabb_occupancy(vmin, vmax):
+    """The assertions of TEST(Map, aabbOccupancy), map_aabb_unittest.cpp:62-86: from the sensor
+    (x = 0) to three blocks behind the wall, and one block more than the wall's half width on
+    either side in y and z."""
+    res = WALL_MAP_RES
+    lo, hi = world_aabb(vmin, vmax, res, [WALL_MAP_DIM / 2] * 3)
+    f = np.float32
+    block_dim = f(res) * f(8)
+    hfov = f(2.0) * f(math.atan(f(100) / (f(2.0) * f(100.0))))
+    half_wall_dim = f(WALL_DEPTH) * f(math.tan(hfov / f(2)))
+    half_wall_blocks = dim_to_blocks(half_wall_dim, block_dim)
+    assert abs(float(lo[0])) <= 1e-6, lo
+    assert np.isclose(hi[0], f(WALL_DEPTH) + f(3) * block_dim, rtol=0, atol=4e-6), hi
+    assert np.isclose(lo[2], lo[1], rtol=0, atol=4e-6)
+    assert np.isclose(hi[2], hi[1], rtol=0, atol=4e-6)
+    assert dim_to_blocks(float(lo[1]), block_dim) == -half_wall_blocks - 1
+    assert dim_to_blocks(float(hi[1]), block_dim) == half_wall_blocks + 1

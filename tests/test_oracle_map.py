@@ -37,6 +37,18 @@ def test_wall_aabb(oracle):
     rc.check_wall_aabb(mn, mx)
 
 
+def test_wall_aabb_occupancy(oracle):
+    # map_aabb_unittest.cpp:62-86 (TEST(Map, aabbOccupancy))
+    spec, T_WC = rc.wall_sensor()
+    m = oracle.OracleOccMap(rc.WALL_MAP_DIM, rc.WALL_MAP_RES)
+    assert m.aabb() is None
+    s = oracle.pinhole(**spec)
+    depth = np.full((spec["height"], spec["width"]), rc.WALL_DEPTH, np.float32)
+    m.integrate_depth(depth, s, T_WC, 0)
+    mn, mx = m.aabb()
+    rc.check_wall_aabb_occupancy(mn, mx)
+
+
 def test_empty_and_invalid_depth_allocates_nothing(oracle):
     m = oracle.OracleMap(10.24, 0.02)
     s = oracle.pinhole(64, 48, 50.0, 50.0, 31.5, 23.5, 0.4, 6.0)
