@@ -11,6 +11,8 @@ the oracle, against the reference's own tests (test/integrator/ray_integrator_un
   scales: propagate_block_to_scale sets a parent's minimum from the mean data only for children
   that did not raise the maximum (ray_integrator_core_impl.hpp:262-272), so a parent with one
   valid child keeps a zero minimum; the oracle keeps that behaviour.
+- And the map's box after the wall batch on either side of the scanner
+  (test/map/map/map_aabb_unittest.cpp, aabb_ray_batch).
 """
 import numpy as np
 import pytest
@@ -118,3 +120,32 @@ def test_propagation_blocks(wall_map):
                                          min_side=False)
                     checked += 1
     assert checked > 10000
+
+
+def test_aabb_of_ray_batches(oracle):
+    """map_aabb_unittest.cpp:88-214 (TEST(Map, aabb_ray_batch)): the wall batch at x = +10 m, then
+    the same wall at x = -10 m, into a fresh 25.6 m map at 5 cm. The map's box reaches from the
+    block of the near plane to the block past the wall plus tau (3 res), and one block more
+    than the wall's half width on either side in y and z."""
+    from tests.reference_cases import dim_to_blocks, world_aabb
+    m, T_MW = _map(oracle)
+    L = oracle.leica(1, 1, 0.6, 30.0, 0.1, 0.1)
+    f = np.float32
+    d, res = 10.0, f(RES)
+    block_dim = f(res * f(8))
+    half_wall_blocks = dim_to_blocks(float(f(d) * np.tan(f(15.0) * f(np.pi / 180.0))), block_dim)
+    n_blocks_x = int(np.ceil(f(f(d) + f(3) * res) / block_dim))
+    rays = wall_rays(d)
+    for side in (1, -1):
+        r = rays.copy()
+        r[:, 0] *= side
+        m.integrate_ray_batch(L, np.eye(4, dtype=np.float32), r, 0)
+        lo, hi = world_aabb(*m.aabb(), res, T_MW[:3, 3])
+        if side == 1:
+            assert abs(float(lo[0]) - float(block_dim * np.floor(f(0.6) / (f(2) * block_dim)))) <= 1e-2, lo
+        else:
+            assert np.isclose(lo[0], np.floor(-f(f(d) + f(3) * res) / block_dim) * block_dim, rtol=0, atol=4e-6), lo
+        assert np.isclose(hi[0], n_blocks_x * block_dim, rtol=0, atol=4e-6), hi
+        assert np.isclose(lo[2], lo[1], rtol=0, atol=4e-6) and np.isclose(hi[2], hi[1], rtol=0, atol=4e-6)
+        assert dim_to_blocks(float(lo[1]), block_dim) == -half_wall_blocks - 1
+        assert dim_to_blocks(float(hi[1]), block_dim) == half_wall_blocks + 1
