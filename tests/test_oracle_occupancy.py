@@ -146,3 +146,23 @@ def test_map_gradient_reference_cases(oracle):
     assert v is not None and v[0] > 0.0
     g = m.get_field_grad(p)
     assert g is not None and float_eq(np.linalg.norm(g), 0.0), g
+
+
+def test_block_allocation_keeps_the_octree_path(oracle):
+    """octree_allocator_unittest.cpp:40-233 (SingleResAllocation.BlockKey) for 8^3 blocks, on the
+    occupancy map's pointer octree: allocating the block of a voxel gives the block at the
+    voxel's coordinates rounded down to 8, and its ancestors are the nodes at the voxel's
+    coordinates rounded down to 2^s at every scale s up to the root (a 256^3 octree)."""
+    m = oracle.OracleOccMap(25.6, 0.1)
+    assert m.size == 256
+    voxels = [(253, 74, 135), (114, 244, 65), (38, 104, 85)]
+    mean = np.zeros((585, 3), np.float32)
+    for v in voxels:
+        m.set_block(tuple(((np.array(v) >> 3) << 3).tolist()), 0, 0, mean)
+    coords = {tuple(c) for c in m.blocks()[0].tolist()}
+    nodes = {tuple(c) for c in m.nodes()[0].tolist()}
+    for v in voxels:
+        v = np.array(v)
+        assert tuple(((v >> 3) << 3).tolist()) in coords
+        for s in range(4, 9):
+            assert tuple(((v >> s) << s).tolist()) + (1 << s,) in nodes, (v, s)
